@@ -1,0 +1,292 @@
+"""Seeded synthetic AMOEBA systems and the host-side description the library
+consumes.
+
+Water model: AMOEBA-WATER-2003 (Tinker test/file/commit_6fe8e913/water03.prm,
+multipoles :139-150, polarize :159-160, scale factors :31-54), identical to
+types 36/37 of amoeba09.prm.  Ions: amoeba09.prm Na+ (type 7, multipole :1221,
+polarize :3051) and Cl- (type 15, :1261, :3059).  Geometry: rigid water,
+O-H 0.9572 A, H-O-H 104.52 degrees.
+"""
+import math
+from dataclasses import dataclass, field
+from typing import Optional
+
+import numpy as np
+
+from . import topology as topo
+
+# type ids follow water03.prm for water and amoeba09.prm for the ions
+WATER_O, WATER_H, NA_ION, CL_ION = 1, 2, 7, 15
+
+# multipole records (kz, kx, ky, values in parameter-file units)
+AMOEBA_RECORDS = {
+    WATER_O: [(-2, -2, 0, [-0.51966, 0.0, 0.0, 0.14279, 0.37928, 0.0, -0.41809, 0.0, 0.0, 0.03881])],
+    WATER_H: [(1, 2, 0, [0.25983, -0.03859, 0.0, -0.05818, -0.03673, 0.0, -0.10739, -0.00203, 0.0, 0.14412])],
+    NA_ION: [(0, 0, 0, [1.0] + [0.0] * 9)],
+    CL_ION: [(0, 0, 0, [-1.0] + [0.0] * 9)],
+}
+# polarizability (A^3), Thole, polarization-group partner types
+AMOEBA_POLAR = {
+    WATER_O: (0.837, 0.39, (WATER_H,)),
+    WATER_H: (0.496, 0.39, (WATER_O,)),
+    NA_ION: (0.12, 0.39, ()),
+    CL_ION: (4.0, 0.39, ()),
+}
+
+OH_BOND = 0.9572
+HOH_ANGLE = 104.52
+
+
+@dataclass
+class System:
+    """Everything the polarization path needs about one system."""
+
+    xyz: np.ndarray  # [n][3] float64, molecules kept whole (not wrapped)
+    types: np.ndarray  # [n] int
+    frames: np.ndarray  # [n][4] int32: zaxis, xaxis, yaxis (1-based signed), kind
+    pole: np.ndarray  # [n][10] local-frame multipoles, MPL order
+    polarity: np.ndarray  # [n]
+    thole: np.ndarray  # [n]
+    pdamp: np.ndarray  # [n]
+    excl_ik: np.ndarray  # [m][2] int32, i < k
+    excl_scale: np.ndarray  # [m][4]: m, d, p, u
+    box: Optional[np.ndarray] = None  # orthorhombic edge lengths, None = no PBC
+    mol_start: Optional[np.ndarray] = None  # first atom of each molecule
+    mol_size: Optional[np.ndarray] = None
+    name: str = ""
+    settings: dict = field(default_factory=dict)
+
+    @property
+    def n(self):
+        return int(self.xyz.shape[0])
+
+
+def build_system(xyz, types, bonds, records, polar, scales=None, box=None, name="", mol_start=None, mol_size=None):
+    """Assemble frames, multipoles, polarizabilities and scaled pairs."""
+    n = len(types)
+    types = list(int(t) for t in types)
+    adj, _ = topo.bond_distance_lists(n, bonds, 1)
+    frames, pole = topo.assign_frames(types, adj, records)
+    alpha = np.array([polar[t][0] for t in types], dtype=np.float64)
+    thole = np.array([polar[t][1] for t in types], dtype=np.float64)
+    pdamp = alpha ** (1.0 / 6.0)
+    grp = topo.polar_groups(types, bonds, {t: set(v[2]) for t, v in polar.items()})
+    sc = dict(topo.DEFAULT_SCALES)
+    if scales:
+        sc.update(scales)
+    ik, scl = topo.scale_table(n, bonds, grp, sc)
+    return System(
+        xyz=np.asarray(xyz, dtype=np.float64).reshape(n, 3),
+        types=np.array(types, dtype=np.int32),
+        frames=frames,
+        pole=pole,
+        polarity=alpha,
+        thole=thole,
+        pdamp=pdamp,
+        excl_ik=ik,
+        excl_scale=scl,
+        box=None if box is None else np.asarray(box, dtype=np.float64),
+        name=name,
+        mol_start=mol_start,
+        mol_size=mol_size,
+    )
+
+
+def _random_rotations(rng, m):
+    """Uniform rotations on SO(3) from uniform unit quaternions (Shoemake)."""
+    u1, u2, u3 = rng.random(m), rng.random(m), rng.random(m)
+    q = np.stack(
+        [
+            np.sqrt(1 - u1) * np.sin(2 * np.pi * u2),
+            np.sqrt(1 - u1) * np.cos(2 * np.pi * u2),
+            np.sqrt(u1) * np.sin(2 * np.pi * u3),
+            np.sqrt(u1) * np.cos(2 * np.pi * u3),
+        ],
+        axis=1,
+    )
+    return quat_to_mat(q)
+
+
+def quat_to_mat(q):
+    x, y, z, w = q[:, 0], q[:, 1], q[:, 2], q[:, 3]
+    r = np.empty((q.shape[0], 3, 3))
+    r[:, 0, 0] = 1 - 2 * (y * y + z * z)
+    r[:, 0, 1] = 2 * (x * y - z * w)
+    r[:, 0, 2] = 2 * (x * z + y * w)
+    r[:, 1, 0] = 2 * (x * y + z * w)
+    r[:, 1, 1] = 1 - 2 * (x * x + z * z)
+    r[:, 1, 2] = 2 * (y * z - x * w)
+    r[:, 2, 0] = 2 * (x * z - y * w)
+    r[:, 2, 1] = 2 * (y * z + x * w)
+    r[:, 2, 2] = 1 - 2 * (x * x + y * y)
+    return r
+
+
+def water_geometry():
+    """Body-frame O, H1, H2 positions (O at the origin, molecule in xz)."""
+    half = math.radians(HOH_ANGLE) / 2
+    return np.array(
+        [
+            [0.0, 0.0, 0.0],
+            [OH_BOND * math.sin(half), 0.0, OH_BOND * math.cos(half)],
+            [-OH_BOND * math.sin(half), 0.0, OH_BOND * math.cos(half)],
+        ]
+    )
+
+
+@dataclass
+class Lattice:
+    """Seeded lattice of rigid molecules: centres, orientations, species."""
+
+    centers: np.ndarray  # [m][3]
+    rot: np.ndarray  # [m][3][3]
+    species: np.ndarray  # [m]: 0 water, 1 Na+, 2 Cl-
+    box: float
+
+
+def make_lattice(nside, box, seed, jitter=0.1, n_sites=None, n_ion_pairs=0):
+    rng = np.random.default_rng(seed)
+    spacing = box / nside
+    g = (np.arange(nside) + 0.5) * spacing - box / 2
+    cx, cy, cz = np.meshgrid(g, g, g, indexing="ij")
+    centers = np.stack([cx.ravel(), cy.ravel(), cz.ravel()], axis=1)
+    if n_sites is not None and n_sites < len(centers):
+        pick = np.sort(rng.permutation(len(centers))[:n_sites])
+        centers = centers[pick]
+    m = len(centers)
+    centers = centers + rng.uniform(-jitter, jitter, size=(m, 3))
+    rot = _random_rotations(rng, m)
+    species = np.zeros(m, dtype=np.int32)
+    if n_ion_pairs:
+        ions = rng.permutation(m)[: 2 * n_ion_pairs]
+        species[ions[:n_ion_pairs]] = 1
+        species[ions[n_ion_pairs:]] = 2
+    return Lattice(centers=centers, rot=rot, species=species, box=box)
+
+
+def lattice_system(lat: Lattice, name=""):
+    """Expand a lattice into atoms (O, H, H per water; one atom per ion)."""
+    geom = water_geometry()
+    xyz, types, bonds, mstart, msize = [], [], [], [], []
+    for j in range(len(lat.centers)):
+        base = len(types)
+        mstart.append(base)
+        if lat.species[j] == 0:
+            pos = lat.centers[j] + geom @ lat.rot[j].T
+            xyz.extend(pos.tolist())
+            types.extend([WATER_O, WATER_H, WATER_H])
+            bonds.extend([(base, base + 1), (base, base + 2)])
+            msize.append(3)
+        else:
+            xyz.append(lat.centers[j].tolist())
+            types.append(NA_ION if lat.species[j] == 1 else CL_ION)
+            msize.append(1)
+    return build_system(
+        xyz,
+        types,
+        bonds,
+        AMOEBA_RECORDS,
+        AMOEBA_POLAR,
+        box=[lat.box] * 3,
+        name=name,
+        mol_start=np.array(mstart, dtype=np.int64),
+        mol_size=np.array(msize, dtype=np.int64),
+    )
+
+
+# The benchmark configurations: (molecules per side, box A, seed, PME grid,
+# sites kept, ion pairs)
+CONFIGS = {
+    "water648": dict(nside=6, box=18.643, seed=0, nfft=24),
+    "water12288": dict(nside=16, box=49.31, seed=1, nfft=64),
+    "nacl23142": dict(nside=20, box=61.7, seed=2, nfft=72, n_sites=7742, n_ion_pairs=21),
+    "water98304": dict(nside=32, box=98.62, seed=4, nfft=128),
+}
+
+# Polarization settings shared by every configuration.  Tinker keeps these
+# keyword defaults in Fortran (kpolar, kewald, kneigh), absent from the
+# reference checkout, so they are set here explicitly.
+DEFAULT_SETTINGS = dict(
+    aewald=0.5446,  # 1/A, Ewald coefficient for a 7 A cutoff at 1e-8
+    ewald_cutoff=7.0,
+    bsorder=5,
+    poleps=1.0e-6,  # Debye, RMS residual
+    politer=100,
+    pcgprec=1,
+    pcgguess=1,
+    pcgpeek=1.0,
+    udiag=2.0,  # uaccel
+    usolve_cutoff=4.5,
+    pbuffer=2.0,  # preconditioner list buffer
+    list_buffer=2.0,
+)
+
+
+def make_config(name, **over):
+    cfg = dict(CONFIGS[name])
+    cfg.update(over)
+    lat = make_lattice(
+        cfg["nside"],
+        cfg["box"],
+        cfg["seed"],
+        n_sites=cfg.get("n_sites"),
+        n_ion_pairs=cfg.get("n_ion_pairs", 0),
+    )
+    s = lattice_system(lat, name=name)
+    s.settings = dict(DEFAULT_SETTINGS)
+    s.settings["nfft"] = (cfg["nfft"],) * 3
+    s.settings["use_ewald"] = 1
+    s.lattice = lat
+    return s
+
+
+class Trajectory:
+    """Smooth seeded motion of rigid molecules about their lattice sites.
+
+    Each molecule rattles (translation amplitude ~0.15 A, periods 80-200 fs)
+    and librates (rotation amplitude ~20 degrees about a seeded axis, periods
+    40-120 fs).  Frames 1 fs apart are correlated the way MD frames are, which
+    is what the dipole predictors and the learned guess rely on.
+    """
+
+    def __init__(self, system, seed=11, dt_fs=1.0):
+        lat = system.lattice
+        rng = np.random.default_rng(seed)
+        m = len(lat.centers)
+        self.sys = system
+        self.lat = lat
+        self.dt = dt_fs
+        d = rng.normal(size=(m, 3))
+        self.tdir = d / np.linalg.norm(d, axis=1, keepdims=True) * 0.15
+        self.tw = 2 * np.pi / rng.uniform(80, 200, size=m)
+        self.tph = rng.uniform(0, 2 * np.pi, size=m)
+        a = rng.normal(size=(m, 3))
+        self.raxis = a / np.linalg.norm(a, axis=1, keepdims=True)
+        self.ramp = np.radians(20.0)
+        self.rw = 2 * np.pi / rng.uniform(40, 120, size=m)
+        self.rph = rng.uniform(0, 2 * np.pi, size=m)
+        self.geom = water_geometry()
+
+    def frame(self, step):
+        t = step * self.dt
+        lat = self.lat
+        c = lat.centers + self.tdir * np.sin(self.tw * t + self.tph)[:, None]
+        ang = self.ramp * np.sin(self.rw * t + self.rph)
+        k = self.raxis
+        kx = np.zeros((len(k), 3, 3))
+        kx[:, 0, 1], kx[:, 0, 2] = -k[:, 2], k[:, 1]
+        kx[:, 1, 0], kx[:, 1, 2] = k[:, 2], -k[:, 0]
+        kx[:, 2, 0], kx[:, 2, 1] = -k[:, 1], k[:, 0]
+        s, cth = np.sin(ang)[:, None, None], np.cos(ang)[:, None, None]
+        rlib = np.eye(3)[None] + s * kx + (1 - cth) * (kx @ kx)
+        rot = rlib @ lat.rot
+        xyz = np.empty((self.sys.n, 3))
+        water = lat.species == 0
+        starts = self.sys.mol_start
+        wpos = c[water][:, None, :] + np.einsum("mij,aj->mai", rot[water], self.geom)
+        ws = starts[water]
+        for a in range(3):
+            xyz[ws + a] = wpos[:, a, :]
+        ions = ~water
+        xyz[starts[ions]] = c[ions]
+        return xyz
