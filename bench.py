@@ -1,0 +1,393 @@
+"""Benchmark of the AMOEBA induce() hot path on one GB300 (replicas for N>1).
+
+A step is one induce() call -- permanent field (PME + real space), PCG to a
+1e-6 Debye RMS residual with the sparse preconditioner and the ASPC predictor
+-- on one frame of a seeded 1 fs trajectory of the 12,288-atom AMOEBA water
+box (49.31 A, PME 64^3, order 5, a = 0.5446, 7 A cutoff).  Frames are
+synthetic: molecules librate and rattle about seeded lattice sites (the
+reference's 2 ps NVT relaxation needs the MD rows that are not built yet).
+
+value: induce() calls per second over all ranks, inputs resident in HBM.
+e2e:   the same through t9gb_induce_host: host coordinates in, host dipoles
+       out, both copies inside the timed region.
+The working set (~10 MB) is smaller than L2, so L2 is flushed (a 512 MB
+write) between timed steps, outside the per-step CUDA-event brackets.
+
+--impl reference times the CPU implementation of the same step: the FP64 C
+restatement of the reference's host path (oracle/), all host threads.
+"""
+import argparse
+import importlib
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "AMOEBA water ns/day & induce ms/step, learned vs plain PCG at 1e-6 D, 1 GB300"
+WORKLOAD = "water12288"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default=WORKLOAD)
+    ap.add_argument("--predictor", default="aspc", choices=["aspc", "none"])
+    ap.add_argument("--history", type=int, default=20, help="trajectory frames run before warm-up (predictor ring)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = (
+        "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+        "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+        "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+    )
+
+    def __init__(self, gpu_index):
+        self.gpu = str(gpu_index)
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", self.gpu, f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True,
+            )
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except FileNotFoundError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+                power.append(float(parts[3]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {
+            "sm_mhz": float(np.median(sm)) if sm else None,
+            "sm_max_mhz": max(smax) if smax else None,
+            "reasons": sorted(reasons),
+            "samples": len(sm),
+            "power_w_max": max(power) if power else None,
+        }
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+# Algorithmic (compulsory) bytes per launch of each kernel: every input read
+# once, every output written once.  "entries" = neighbour-list entries.
+def algorithmic_bytes(kernel, n, entries, nfft):
+    ng = nfft ** 3
+    if kernel == "ufield_real":
+        # pos 16 + dipoles 24 + damping 8 + recip field 24 in, field 24 out, list 4/entry
+        return n * (16 + 24 + 8 + 24 + 24) + 4 * entries
+    if kernel == "dfield_real":
+        # pos 16 + multipoles 40 + damping 8 + recip field 24 in, field 24 out
+        return n * (16 + 40 + 8 + 24 + 24) + 4 * entries
+    if kernel == "precond_sparse":
+        return n * (16 + 24 + 8 + 4 + 24) + 4 * entries
+    if kernel == "spread_uind":
+        # pos + dipoles in, fixed-point grid (16 B per point) written once
+        return n * (16 + 24) + 16 * ng
+    if kernel == "spread_mpole":
+        return n * (16 + 40) + 16 * ng
+    if kernel == "fft_conv":
+        # fixed grid read + clear 32 B/pt, float grid write 8, conv r/w 16 + table 4, two FFTs r/w 32
+        return ng * (32 + 8 + 16 + 4 + 32)
+    if kernel in ("gather_uind", "gather_mpole"):
+        return 8 * ng + n * (16 + 24 + 24)
+    if kernel == "pcg_vector":
+        return n * 6 * 4 * 8
+    if kernel == "nblist":
+        return n * 16 + 4 * entries
+    return n * 16
+
+
+def run_reference(args, world, rank):
+    """CPU implementation of the step (oracle port, all host threads)."""
+    if rank != 0:
+        return
+    tg = importlib.import_module("tinker-gpu_gb300")
+    from oracle import oracle as O
+
+    O.build()
+    cores = os.cpu_count() or 1
+    O.set_threads(cores)
+    s = tg.systems.make_config(args.config)
+    tr = tg.systems.Trajectory(s)
+    times = []
+    iters = []
+    total = args.warmup + args.steps
+    for step in range(total):
+        x = tr.frame(args.history + step)
+        t0 = time.perf_counter()
+        o = O.OracleSystem(s, xyz=x)
+        u = o.induce()
+        dt = time.perf_counter() - t0
+        if step >= args.warmup:
+            times.append(dt)
+            iters.append(u[4])
+    sec = float(np.sum(times))
+    value = len(times) / sec
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": "induce() calls/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1000 * sec / len(times),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded AMOEBA water trajectory)",
+        "config": {"workload": args.config, "atoms": s.n, "pme_grid": list(s.settings["nfft"]),
+                   "poleps_debye": s.settings["poleps"], "guess": "direct (alpha E)"},
+        "pcg_iterations_per_step": float(np.mean(iters)),
+        "cpu_baseline": {"value": value, "unit": "induce() calls/s", "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} timed induce() calls on {args.config} after {args.warmup} warm-up"},
+        "e2e": {"value": value, "unit": "induce() calls/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_sample(args, s, tr):
+    """One bounded sample of the CPU implementation (oracle port)."""
+    from oracle import oracle as O
+
+    O.build()
+    cores = os.cpu_count() or 1
+    O.set_threads(cores)
+    t0 = time.perf_counter()
+    nsteps = 0
+    while nsteps < 3 and time.perf_counter() - t0 < 20:
+        o = O.OracleSystem(s, xyz=tr.frame(args.history + nsteps))
+        o.induce()
+        nsteps += 1
+    dt = time.perf_counter() - t0
+    return {"value": nsteps / dt, "unit": "induce() calls/s", "cores": cores, "kind": "port",
+            "sample": f"{nsteps} induce() calls on {args.config} (FP64, direct guess, all host threads)"}
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.init_process_group("gloo")
+        run_reference(args, world, rank)
+        return
+
+    import torch
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    tg = importlib.import_module("tinker-gpu_gb300")
+    b = importlib.import_module("tinker-gpu_gb300.build")
+    b.build()
+    abi = importlib.import_module("tinker-gpu_gb300.abi")
+
+    s = tg.systems.make_config(args.config)
+    tr = tg.systems.Trajectory(s, seed=11 + rank)
+    pred = 1 if args.predictor == "aspc" else 0
+    stream = torch.cuda.Stream()
+    eng = abi.Engine(s, predictor=pred, stream=stream)
+    eng.prepare(tr.frame(0))
+    nsteps = args.history + args.warmup + args.steps
+    frames = np.stack([tr.frame(t) for t in range(nsteps)]).astype(np.float32)
+    # device-resident inputs for the kernel-only measurement
+    dev_frames = torch.from_numpy(frames).to("cuda")
+    ud = torch.zeros((s.n, 3), device="cuda")
+    up = torch.zeros((s.n, 3), device="cuda")
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def step_device(t):
+        eng.set_xyz_device(dev_frames[t])
+        eng.mpole_init()
+        eng.induce(out=(ud, up))
+
+    # trajectory history fills the predictor ring (outside every timed region)
+    with torch.cuda.stream(stream):
+        for t in range(args.history):
+            step_device(t)
+        for t in range(args.history, args.history + args.warmup):
+            step_device(t)
+    torch.cuda.synchronize()
+
+    # ---- timed region: device-resident inputs ----
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    iters = []
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    wall0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.fill_(float(k))
+            ev[k][0].record(stream)
+            step_device(args.history + args.warmup + k)
+            ev[k][1].record(stream)
+            iters.append(eng.stats()[0])
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    if world > 1:
+        dist.barrier()
+    ck = clocks.stop()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    dev_sec = sum(step_ms) / 1000.0
+    if world > 1:
+        t = torch.tensor([dev_sec], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_sec = float(t.item())
+    value = world * args.steps / dev_sec
+
+    # ---- e2e: host coordinates in, host dipoles out ----
+    hu = np.zeros((s.n, 3))
+    hp = np.zeros((s.n, 3))
+    e2e_t = []
+    for k in range(args.steps):
+        x = frames[args.history + args.warmup + k].astype(np.float64)
+        flush.fill_(float(k))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        eng.induce_host(x, hu, hp)
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_sec = float(np.sum(e2e_t))
+    if world > 1:
+        t = torch.tensor([e2e_sec], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_sec = float(t.item())
+    e2e_value = world * args.steps / e2e_sec
+
+    # ---- per-kernel timing pass (CUDA events on the library stream) ----
+    eng.profile(True)
+    eng.profile_read(reset=True)
+    prof_iters = []
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            step_device(args.history + args.warmup + k)
+            prof_iters.append(eng.stats()[0])
+    prof = eng.profile_read(reset=True)
+    eng.profile(False)
+    kernels = {k: {"ms_total": v[0], "launches": v[1], "ms_per_launch": (v[0] / v[1] if v[1] else None)}
+               for k, v in prof.items() if v[1]}
+    dom = max(kernels, key=lambda k: kernels[k]["ms_total"])
+    nfft = s.settings["nfft"][0]
+    ls = eng.list_stats()
+    alg = algorithmic_bytes(dom, s.n, ls["entries"], nfft)
+    peak, peak_kind = measured_peaks()
+    per_launch_s = kernels[dom]["ms_per_launch"] / 1000.0
+    achieved = alg / per_launch_s / 1e9
+    mean_it = float(np.mean(iters))
+    # own kernels per step: positions 1, rotpole 2, list 5, reset 1, dfield 5, guess 1, ufield 5, r0 1,
+    # M r0 1, dots 1, history 1, output 1; per PCG iteration: ufield 5 + precond 1 + vector 4
+    launches_per_step = 25 + 10 * mean_it
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline_sample(args, s, tr)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC,
+            "value": value,
+            "unit": "induce() calls/s",
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": 1000 * dev_sec / args.steps,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32 pair/spline math, fixed-point i64 accumulation, f64 PCG scalars",
+            "data": "synthetic (seeded AMOEBA water lattice, 1 fs librating trajectory)",
+            "config": {
+                "workload": args.config, "atoms": s.n, "pme_grid": list(s.settings["nfft"]), "cutoff_A": 7.0,
+                "poleps_debye": s.settings["poleps"], "predictor": args.predictor, "history_frames": args.history,
+                "l2": "flushed (512 MB write) between timed steps", "parallelism": f"replicas x{world}",
+            },
+            "induce_ms_per_step": 1000 * dev_sec / args.steps,
+            "pcg_iterations_per_step": mean_it,
+            "ns_per_day": None,
+            "ns_per_day_note": "needs the MD rows (HAL vdW, valence, integrator); not built",
+            "wall_s_timed": wall,
+            "e2e": {"value": e2e_value, "unit": "induce() calls/s", "ms_per_step": 1000 * e2e_sec / args.steps,
+                    "h2d_bytes_per_step": 3 * s.n * 4, "d2h_bytes_per_step": 6 * s.n * 4},
+            "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
+                         "algorithmic_bytes_per_launch": alg},
+            "kernels": kernels,
+            "lists": ls,
+            "gpu_launches": int(round(launches_per_step * args.steps)),
+            "clocks": ck,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    eng.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,151 @@
+/*
+ * t9gb.h -- C ABI of the GB300-native AMOEBA mutual-polarization library.
+ *
+ * Drop-in boundary for Tinker9's induce() hot path.  Every entry point is
+ * plain C: opaque context, plain pointers and sizes, int status codes, no
+ * exceptions.  Each function names the reference routine it replaces
+ * (paths are within the TinkerTools/tinker-gpu tree).
+ *
+ * Conventions
+ *  - Atom arrays are in the caller's atom order; [n][3] arrays are row-major.
+ *  - "_device" arrays are device pointers of the context's CUDA device; all
+ *    work is issued on the context's stream (t9gb_set_stream).
+ *  - Multipoles use Tinker9's MPL order: q, dx, dy, dz, qxx, qyy, qzz, qxy,
+ *    qxz, qyz, in e, e*A, e*A^2 with the 1/3 quadrupole factor
+ *    (include/ff/amoeba/mpole.h:4-21).
+ *  - Local frames: zaxis, xaxis (0-based), yaxis (1-based, signed),
+ *    kind 0 None, 1 Z-Only, 2 Z-then-X, 3 Bisector, 4 Z-Bisect, 5 3-Fold
+ *    (include/ff/amoeba/mpole.h:22-36, src/elec.cpp:99-124).
+ *  - Scaled pairs: rows (i, k), i < k, with scales (m, d, p, u), the union
+ *    of the reference's mexclude/dpexclude/uexclude/dpuexclude tables
+ *    (src/amoeba/epolar.cpp:88-484).
+ */
+#ifndef T9GB_H
+#define T9GB_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes (replace FatalError/TINKER_THROW, include/tool/error.h:15-44) */
+#define T9GB_OK 0
+#define T9GB_NOT_CONVERGED 1 /* PCG hit its iteration cap (src/cu/amoeba/pcg.cu:180-184) */
+#define T9GB_NAN_DETECTED 2  /* non-finite residual */
+#define T9GB_BAD_ARG 3
+#define T9GB_CUDA_ERR 4
+#define T9GB_NO_DEVICE 5
+#define T9GB_NOT_READY 6 /* topology / positions / list missing */
+
+typedef struct t9gb_context t9gb_context;
+
+/* Run-time settings.  In the reference they are Fortran module globals
+ * (polpot, polpcg, ewald, pme, neigh, units); here the caller passes them. */
+typedef struct {
+   int n;               /* atoms */
+   double box[3];       /* orthorhombic edge lengths in A; all zero: no PBC */
+   int use_ewald;       /* 1: PME + Ewald real space; 0: damped Coulomb */
+   double aewald;       /* Ewald coefficient, 1/A (pme.h PME::aewald) */
+   int nfft[3];         /* PME grid (pme.h nfft1..3) */
+   int bsorder;         /* B-spline order, must be 5 */
+   double cutoff;       /* real-space cutoff, A (switchOff EWALD / MPOLE) */
+   double list_buffer;  /* spatial-list buffer, A (neigh::lbuffer) */
+   double usolve_cutoff;/* sparse-preconditioner cutoff, A (switchOff USOLVE) */
+   double pbuffer;      /* preconditioner list buffer, A (neigh::pbuffer) */
+   double poleps;       /* RMS residual threshold, Debye (polpot::poleps) */
+   int politer;         /* iteration cap (polpot::politer) */
+   double pcgpeek;      /* polpcg::pcgpeek */
+   double udiag;        /* polpot::uaccel */
+   int pcgprec;         /* 1: sparse preconditioner, 0: diagonal (polpcg::pcgprec) */
+   int pcgguess;        /* 1: direct guess alpha*E, 0: zero (polpcg::pcgguess) */
+   int predictor;       /* 0: none, 1: ASPC (uprior::polpred) */
+   double electric;     /* kcal*A/(mol*e^2) (units::electric) */
+   double debye;        /* Debye per e*A (units::debye) */
+} t9gb_config;
+
+/* Create a context on the current CUDA device.  Replaces the RcMan set-up
+ * chain for this path (src/rcman.cpp:49-80: epolarData, pmeData, fftData,
+ * nblistData). */
+int t9gb_create(const t9gb_config* cfg, t9gb_context** out);
+void t9gb_destroy(t9gb_context* ctx);
+const char* t9gb_status_string(int status);
+const char* t9gb_last_error(const t9gb_context* ctx);
+
+/* Use the caller's cudaStream_t (passed as void*); NULL selects the
+ * context's own stream.  Replaces g::s0 (src/cudalib.cpp:34-54). */
+int t9gb_set_stream(t9gb_context* ctx, void* stream);
+
+/* Topology, host pointers, copied once.  Replaces epolarData/mpoleData INIT
+ * (src/amoeba/epolar.cpp:486-508, src/elec.cpp:91-140).
+ * frames[n][4], pole[n][10] local-frame multipoles, polarity/thole/pdamp[n],
+ * excl_ik[nexcl][2], excl_scale[nexcl][4] (m, d, p, u). */
+int t9gb_set_topology(t9gb_context* ctx, const int* frames, const double* pole, const double* polarity,
+   const double* thole, const double* pdamp, int nexcl, const int* excl_ik, const double* excl_scale);
+
+/* Coordinates [n][3].  Replace copyPosToXyz (src/atom.cpp:161-166). */
+int t9gb_set_xyz_host(t9gb_context* ctx, const double* xyz);
+int t9gb_set_xyz_device(t9gb_context* ctx, const float* xyz_device);
+
+/* Build the spatial (Morton) order of the atoms from the current coordinates
+ * and the scaled-partner table; the exact neighbour list is then rebuilt on
+ * the device whenever coordinates change.  Replaces spatialBuild /
+ * spatialUpdate (src/spatial.cpp:201-205, src/cu/spatial.cu:149-960). */
+int t9gb_nblist_build(t9gb_context* ctx);
+
+/* Local -> global multipoles with the chirality check.  Replaces mpoleInit's
+ * chkpole + rotpole (src/amoeba/mpole.cpp:28-57, src/cu/amoeba/rotpole.cu:6-43). */
+int t9gb_mpole_init(t9gb_context* ctx);
+
+/* Permanent-multipole field on d and p.  Replaces
+ * void dfield(real (*field)[3], real (*fieldp)[3]) (src/amoeba/field.cpp:56-63).
+ * field/fieldp: [n][3] float, device. */
+int t9gb_dfield(t9gb_context* ctx, float* field_device, float* fieldp_device);
+
+/* Mutual field -T u for d and p.  Replaces
+ * void ufield(const real (*uind)[3], const real (*uinp)[3], real (*field)[3],
+ * real (*fieldp)[3]) (src/amoeba/field.cpp:110-117). */
+int t9gb_ufield(t9gb_context* ctx, const float* uind_device, const float* uinp_device, float* field_device,
+   float* fieldp_device);
+
+/* z = M r with the sparse preconditioner.  Replaces sparsePrecondApply
+ * (src/amoeba/induce.cpp:22-26, src/cu/amoeba/precond.cu:28-43). */
+int t9gb_sparse_precond_apply(t9gb_context* ctx, const float* rsd_device, const float* rsdp_device,
+   float* zrsd_device, float* zrsdp_device);
+
+/* Mutual induced dipoles by PCG.  Replaces
+ * void induce(real (*uind)[3], real (*uinp)[3]) (src/amoeba/induce.cpp:108-113,
+ * src/cu/amoeba/pcg.cu:14-185).  Calls dfield itself; saves the predictor
+ * history like ulspredSave.  Returns T9GB_NOT_CONVERGED like the reference's
+ * FatalError at the iteration cap. */
+int t9gb_induce(t9gb_context* ctx, float* uind_device, float* uinp_device);
+
+/* End-to-end form for callers with host memory: copies xyz [n][3] in, runs
+ * mpole_init + induce and copies the dipoles [n][3] out (either output may be
+ * NULL). */
+int t9gb_induce_host(t9gb_context* ctx, const double* xyz, double* uind, double* uinp);
+
+/* Statistics of the last induce: iterations, final RMS residual (Debye),
+ * status. */
+int t9gb_induce_stats(const t9gb_context* ctx, int* iterations, double* eps_debye, int* status);
+
+/* Direct dipoles alpha*E of the last induce/dfield, [n][3] device. */
+int t9gb_get_udir(t9gb_context* ctx, float* udir_device, float* udirp_device);
+
+/* Neighbour-list sizes: row capacity, entries of the current list (both
+ * directions) and scaled pairs (the reference's Spatial::nakpl/niak,
+ * include/ff/spatial.h:15-140). */
+int t9gb_nblist_stats(t9gb_context* ctx, int* capacity, long long* entries, int* nscaled);
+
+/* Tracing: per-kernel CUDA-event timing of every launch of the listed
+ * categories (the reference has only cudaProfilerStart/Stop,
+ * src/cudalib.cpp:20,53).  Enabling allocates the event pool; reading
+ * returns the accumulated milliseconds and launch count of one category and
+ * reset != 0 clears them. */
+#define T9GB_PROF_NCAT 10
+int t9gb_profile_enable(t9gb_context* ctx, int enable);
+int t9gb_profile_read(t9gb_context* ctx, int category, double* total_ms, long long* launches, int reset);
+const char* t9gb_profile_name(int category);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,91 @@
+"""CUDA induce() (PCG) against the FP64 oracle and the reference's known
+answers.  Both solves stop at an RMS residual below poleps (1e-6 Debye);
+the dipoles must agree to DIPOLE_RMS_DEBYE RMS."""
+import numpy as np
+import pytest
+
+import lf_fixture as L
+from gpu_util import cpu, engine_for, rms_err
+
+pytestmark = pytest.mark.gpu
+DIPOLE_RMS_DEBYE = 2.0e-5
+DIPOLE_MAX_DEBYE = 2.0e-4
+GOLDEN_MARGIN = 1.0e-4
+
+
+@pytest.mark.parametrize("ewald", [0, 1], ids=["nonewald", "pme"])
+def test_localframe_induce(gpu_lib, oracle, tg, ewald):
+    s, fx = L.system(ewald)
+    e = engine_for(s)
+    ud, up, rc = e.induce()
+    assert rc == 0
+    it, eps, st = e.stats()
+    assert eps < s.settings["poleps"] and 3 <= it < 100
+    D = tg.units.DEBYE
+    ex = L.expected(fx, ewald)["induce"]
+    assert np.abs(cpu(ud) * D - ex["ref_ud_debye"]).max() < GOLDEN_MARGIN
+    assert np.abs(cpu(up) * D - ex["ref_up_debye"]).max() < GOLDEN_MARGIN
+    ou, op, *_ = oracle.OracleSystem(s).induce()
+    assert rms_err(cpu(ud) * D, ou * D) < DIPOLE_RMS_DEBYE
+
+
+@pytest.mark.parametrize("name", ["water648", "nacl23142"])
+def test_water_induce(gpu_lib, oracle, tg, name):
+    s = tg.systems.make_config(name)
+    e = engine_for(s)
+    ud, up, rc = e.induce()
+    assert rc == 0
+    it, eps, st = e.stats()
+    ou, op, _, _, oit, oeps = oracle.OracleSystem(s).induce()
+    D = tg.units.DEBYE
+    print(name, "gpu iters", it, "eps", eps, "oracle iters", oit, "eps", oeps)
+    assert eps < 1e-6 and abs(it - oit) <= 2
+    assert rms_err(cpu(ud) * D, ou * D) < DIPOLE_RMS_DEBYE
+    assert rms_err(cpu(up) * D, op * D) < DIPOLE_RMS_DEBYE
+    assert np.abs(cpu(ud) - ou).max() * D < DIPOLE_MAX_DEBYE
+
+
+def test_induce_host_entry_matches_device_entry(gpu_lib, tg):
+    s = tg.systems.make_config("water648")
+    e = engine_for(s)
+    ud, up, _ = e.induce()
+    hd, hp, rc = e.induce_host(s.xyz)
+    assert rc == 0
+    assert np.array_equal(cpu(ud).astype(np.float32), hd.astype(np.float32))
+
+
+def test_induce_bit_reproducible(gpu_lib, tg):
+    s = tg.systems.make_config("water648")
+    e = engine_for(s)
+    a = cpu(e.induce()[0])
+    b = cpu(e.induce()[0])
+    assert np.array_equal(a, b)
+
+
+def test_not_converged_status(gpu_lib, tg):
+    """politer = 1 forces the reference's non-convergence error path."""
+    abi = __import__("importlib").import_module("tinker-gpu_gb300.abi")
+    s = tg.systems.make_config("water648")
+    e = abi.Engine(s, politer=1)
+    e.prepare()
+    _, _, rc = e.induce()
+    assert rc == abi.T9GB_NOT_CONVERGED
+
+
+def test_aspc_predictor_trajectory(gpu_lib, oracle, tg):
+    """ASPC guess after 16 saved steps: fewer iterations, same answer."""
+    s = tg.systems.make_config("water648")
+    tr = tg.systems.Trajectory(s)
+    plain = engine_for(s)
+    pred = engine_for(s, predictor=1)
+    its_plain, its_pred = [], []
+    for step in range(20):
+        x = tr.frame(step)
+        ud0, _, _ = plain.induce_host(x)
+        its_plain.append(plain.stats()[0])
+        ud1, _, rc = pred.induce_host(x)
+        assert rc == 0
+        its_pred.append(pred.stats()[0])
+    D = tg.units.DEBYE
+    assert rms_err(ud1 * D, ud0 * D) < DIPOLE_RMS_DEBYE
+    assert np.mean(its_pred[17:]) < np.mean(its_plain[17:])

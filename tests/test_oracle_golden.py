@@ -1,0 +1,75 @@
+"""The FP64 oracle against the reference's own known answers (Tinker9
+test/localframe.cpp, Local-Frame-3 non-Ewald and Local-Frame-4 PME), margin
+1e-4 as in the reference test (localframe.cpp:211, :382)."""
+import numpy as np
+import pytest
+
+import lf_fixture as L
+
+MARGIN = 1.0e-4
+
+
+@pytest.mark.parametrize("ewald", [0, 1], ids=["nonewald", "pme"])
+def test_dfield_golden(oracle, ewald):
+    s, fx = L.system(ewald)
+    ex = L.expected(fx, ewald)["dfield"]
+    f, fp = oracle.OracleSystem(s).dfield()
+    assert np.abs(f - ex["ref_dir_field_d"]).max() < MARGIN
+    assert np.abs(fp - ex["ref_dir_field_p"]).max() < MARGIN
+
+
+@pytest.mark.parametrize("ewald", [0, 1], ids=["nonewald", "pme"])
+def test_ufield_golden(oracle, ewald):
+    s, fx = L.system(ewald)
+    ex = L.expected(fx, ewald)["ufield"]
+    ud, up = L.synthetic_dipoles(s.n)
+    f, fp = oracle.OracleSystem(s).ufield(ud, up)
+    assert np.abs(f - ex["ref_ufield_d"]).max() < MARGIN
+    assert np.abs(fp - ex["ref_ufield_p"]).max() < MARGIN
+
+
+@pytest.mark.parametrize("ewald", [0, 1], ids=["nonewald", "pme"])
+def test_induce_golden(oracle, tg, ewald):
+    s, fx = L.system(ewald)
+    ex = L.expected(fx, ewald)["induce"]
+    u, p, _, _, it, eps = oracle.OracleSystem(s).induce()
+    d = tg.units.DEBYE
+    assert eps < s.settings["poleps"]
+    assert 3 <= it < 100
+    assert np.abs(u * d - ex["ref_ud_debye"]).max() < MARGIN
+    assert np.abs(p * d - ex["ref_up_debye"]).max() < MARGIN
+
+
+def test_fft_matches_numpy(oracle):
+    """The oracle's mixed-radix FFT against numpy on a 24 x 18 x 10 grid."""
+    import ctypes as C
+
+    lib = oracle.lib()
+    rng = np.random.default_rng(0)
+    g = (rng.normal(size=(10, 18, 24)) + 1j * rng.normal(size=(10, 18, 24))).astype(np.complex128)
+    ref = np.fft.fftn(g)
+    h = np.ascontiguousarray(g.copy())
+    lib.or_fft3d.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int]
+    lib.or_fft3d(h.ctypes.data, 24, 18, 10, -1)
+    assert np.abs(h - ref).max() < 1e-9 * np.abs(ref).max()
+
+
+def test_bspline_partition_of_unity(oracle):
+    for w in (0.0, 0.13, 0.5, 0.99):
+        th = oracle.bsplgen(w, 5, 4)
+        assert abs(th[:, 0].sum() - 1) < 1e-14
+        assert abs(th[:, 1].sum()) < 1e-14  # derivative of a constant
+        assert abs(th[:, 2].sum()) < 1e-13
+
+
+def test_bsmod_positive(oracle):
+    for n in (24, 64, 72, 128):
+        m = oracle.bsmod(n)
+        assert (m > 0).all() and abs(m[0] - 1) < 1e-12
+
+
+def test_aspc_weights_sum_to_one(oracle):
+    """ASPC extrapolation reproduces a constant history."""
+    hist = np.ones((16, 6))
+    for nualt in (16, 17, 31):
+        assert np.allclose(oracle.aspc_sum(hist, nualt), 1.0, atol=1e-12)

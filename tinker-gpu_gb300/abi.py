@@ -1,0 +1,282 @@
+"""ctypes binding of the C ABI in include/t9gb.h and a thin Python host API.
+
+The CUDA library (csrc/_build/libt9gb.so) is the only compute path: if it is
+missing or cannot load, every entry point here raises; there is no CPU
+fallback.  Device buffers are torch CUDA tensors (torch is used for device
+memory and streams only).
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+from .units import DEBYE, ELECTRIC
+
+LIB_PATH = _build.LIB
+
+T9GB_OK, T9GB_NOT_CONVERGED, T9GB_NAN_DETECTED, T9GB_BAD_ARG, T9GB_CUDA_ERR, T9GB_NO_DEVICE, T9GB_NOT_READY = range(7)
+
+# every symbol include/t9gb.h declares
+EXPORTS = [
+    "t9gb_create", "t9gb_destroy", "t9gb_status_string", "t9gb_last_error", "t9gb_set_stream",
+    "t9gb_set_topology", "t9gb_set_xyz_host", "t9gb_set_xyz_device", "t9gb_nblist_build", "t9gb_mpole_init",
+    "t9gb_dfield", "t9gb_ufield", "t9gb_sparse_precond_apply", "t9gb_induce", "t9gb_induce_host",
+    "t9gb_induce_stats", "t9gb_get_udir", "t9gb_nblist_stats", "t9gb_profile_enable", "t9gb_profile_read", "t9gb_profile_name",
+]
+
+
+class T9Config(C.Structure):
+    _fields_ = [
+        ("n", C.c_int),
+        ("box", C.c_double * 3),
+        ("use_ewald", C.c_int),
+        ("aewald", C.c_double),
+        ("nfft", C.c_int * 3),
+        ("bsorder", C.c_int),
+        ("cutoff", C.c_double),
+        ("list_buffer", C.c_double),
+        ("usolve_cutoff", C.c_double),
+        ("pbuffer", C.c_double),
+        ("poleps", C.c_double),
+        ("politer", C.c_int),
+        ("pcgpeek", C.c_double),
+        ("udiag", C.c_double),
+        ("pcgprec", C.c_int),
+        ("pcgguess", C.c_int),
+        ("predictor", C.c_int),
+        ("electric", C.c_double),
+        ("debye", C.c_double),
+    ]
+
+
+class T9Error(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(msg)
+        self.code = code
+
+
+_lib = None
+
+
+def load(path=None):
+    """Load libt9gb.so; raises if it was not built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise T9Error(-1, f"CUDA library not built: {path} (run __graft_entry__.build())")
+    lib = C.CDLL(path)
+    vp, ip, dp, fp = C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double), C.c_void_p
+    lib.t9gb_create.argtypes = [C.POINTER(T9Config), C.POINTER(vp)]
+    lib.t9gb_destroy.argtypes = [vp]
+    lib.t9gb_destroy.restype = None
+    lib.t9gb_status_string.argtypes = [C.c_int]
+    lib.t9gb_status_string.restype = C.c_char_p
+    lib.t9gb_last_error.argtypes = [vp]
+    lib.t9gb_last_error.restype = C.c_char_p
+    lib.t9gb_set_stream.argtypes = [vp, vp]
+    lib.t9gb_set_topology.argtypes = [vp, ip, dp, dp, dp, dp, C.c_int, ip, dp]
+    lib.t9gb_set_xyz_host.argtypes = [vp, dp]
+    lib.t9gb_set_xyz_device.argtypes = [vp, fp]
+    lib.t9gb_nblist_build.argtypes = [vp]
+    lib.t9gb_mpole_init.argtypes = [vp]
+    lib.t9gb_dfield.argtypes = [vp, fp, fp]
+    lib.t9gb_ufield.argtypes = [vp, fp, fp, fp, fp]
+    lib.t9gb_sparse_precond_apply.argtypes = [vp, fp, fp, fp, fp]
+    lib.t9gb_induce.argtypes = [vp, fp, fp]
+    lib.t9gb_induce_host.argtypes = [vp, dp, dp, dp]
+    lib.t9gb_induce_stats.argtypes = [vp, ip, dp, ip]
+    lib.t9gb_get_udir.argtypes = [vp, fp, fp]
+    lib.t9gb_nblist_stats.argtypes = [vp, ip, C.POINTER(C.c_longlong), ip]
+    lib.t9gb_profile_enable.argtypes = [vp, C.c_int]
+    lib.t9gb_profile_read.argtypes = [vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_longlong), C.c_int]
+    lib.t9gb_profile_name.argtypes = [C.c_int]
+    lib.t9gb_profile_name.restype = C.c_char_p
+    _lib = lib
+    return lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def make_config(system, predictor=0, **over):
+    st = dict(system.settings)
+    st.update(over)
+    cfg = T9Config()
+    cfg.n = system.n
+    if system.box is not None:
+        for d in range(3):
+            cfg.box[d] = float(system.box[d])
+    cfg.use_ewald = int(st.get("use_ewald", 1))
+    cfg.aewald = float(st.get("aewald", 0.0))
+    nf = st.get("nfft", (0, 0, 0))
+    for d in range(3):
+        cfg.nfft[d] = int(nf[d])
+    cfg.bsorder = int(st.get("bsorder", 5))
+    cfg.cutoff = float(st.get("ewald_cutoff", 1.0e9))
+    cfg.list_buffer = float(st.get("list_buffer", 2.0))
+    cfg.usolve_cutoff = float(st.get("usolve_cutoff", 4.5))
+    cfg.pbuffer = float(st.get("pbuffer", 2.0))
+    cfg.poleps = float(st.get("poleps", 1e-6))
+    cfg.politer = int(st.get("politer", 100))
+    cfg.pcgpeek = float(st.get("pcgpeek", 1.0))
+    cfg.udiag = float(st.get("udiag", 2.0))
+    cfg.pcgprec = int(st.get("pcgprec", 1))
+    cfg.pcgguess = int(st.get("pcgguess", 1))
+    cfg.predictor = int(predictor)
+    cfg.electric = ELECTRIC
+    cfg.debye = DEBYE
+    return cfg
+
+
+class Engine:
+    """One library context for one system (mirrors the reference's global
+    state for the polarization path)."""
+
+    def __init__(self, system, predictor=0, stream=None, **over):
+        import torch
+
+        self.torch = torch
+        self.lib = load()
+        self.sys = system
+        self.n = system.n
+        self.cfg = make_config(system, predictor=predictor, **over)
+        h = C.c_void_p()
+        self._check(self.lib.t9gb_create(C.byref(self.cfg), C.byref(h)), None)
+        self.h = h
+        s = stream if stream is not None else torch.cuda.current_stream()
+        self._check(self.lib.t9gb_set_stream(self.h, C.c_void_p(s.cuda_stream)))
+        frames = np.ascontiguousarray(system.frames, dtype=np.int32)
+        pole = np.ascontiguousarray(system.pole, dtype=np.float64)
+        pol = np.ascontiguousarray(system.polarity, dtype=np.float64)
+        thl = np.ascontiguousarray(system.thole, dtype=np.float64)
+        pdm = np.ascontiguousarray(system.pdamp, dtype=np.float64)
+        eik = np.ascontiguousarray(system.excl_ik, dtype=np.int32).reshape(-1)
+        esc = np.ascontiguousarray(system.excl_scale, dtype=np.float64).reshape(-1)
+        self._check(
+            self.lib.t9gb_set_topology(
+                self.h, _ip(frames), _dp(pole), _dp(pol), _dp(thl), _dp(pdm), len(eik) // 2, _ip(eik), _dp(esc)
+            )
+        )
+
+    def _check(self, rc, h=-1, allow=()):
+        if rc == T9GB_OK or rc in allow:
+            return rc
+        msg = self.lib.t9gb_status_string(rc).decode()
+        hh = self.h if h == -1 else h
+        if hh:
+            msg += ": " + self.lib.t9gb_last_error(hh).decode()
+        raise T9Error(rc, msg)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.t9gb_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- state ----
+    def set_xyz(self, xyz):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        self._check(self.lib.t9gb_set_xyz_host(self.h, _dp(xyz)))
+
+    def set_xyz_device(self, xyz_t):
+        self._check(self.lib.t9gb_set_xyz_device(self.h, C.c_void_p(xyz_t.data_ptr())))
+
+    def nblist_build(self):
+        self._check(self.lib.t9gb_nblist_build(self.h))
+
+    def mpole_init(self):
+        self._check(self.lib.t9gb_mpole_init(self.h))
+
+    def prepare(self, xyz=None):
+        self.set_xyz(self.sys.xyz if xyz is None else xyz)
+        self.nblist_build()
+        self.mpole_init()
+
+    # ---- fields ----
+    def _empty3(self):
+        return self.torch.zeros((self.n, 3), dtype=self.torch.float32, device="cuda")
+
+    def dfield(self):
+        f, fp = self._empty3(), self._empty3()
+        self._check(self.lib.t9gb_dfield(self.h, C.c_void_p(f.data_ptr()), C.c_void_p(fp.data_ptr())))
+        return f, fp
+
+    def ufield(self, uind, uinp):
+        t = self.torch
+        ud = t.as_tensor(np.asarray(uind, dtype=np.float32), device="cuda").contiguous()
+        up = t.as_tensor(np.asarray(uinp, dtype=np.float32), device="cuda").contiguous()
+        f, fp = self._empty3(), self._empty3()
+        self._check(
+            self.lib.t9gb_ufield(
+                self.h, C.c_void_p(ud.data_ptr()), C.c_void_p(up.data_ptr()), C.c_void_p(f.data_ptr()),
+                C.c_void_p(fp.data_ptr()),
+            )
+        )
+        return f, fp
+
+    def sparse_precond(self, rsd, rsdp):
+        t = self.torch
+        r = t.as_tensor(np.asarray(rsd, dtype=np.float32), device="cuda").contiguous()
+        rp = t.as_tensor(np.asarray(rsdp, dtype=np.float32), device="cuda").contiguous()
+        z, zp = self._empty3(), self._empty3()
+        self._check(
+            self.lib.t9gb_sparse_precond_apply(
+                self.h, C.c_void_p(r.data_ptr()), C.c_void_p(rp.data_ptr()), C.c_void_p(z.data_ptr()),
+                C.c_void_p(zp.data_ptr()),
+            )
+        )
+        return z, zp
+
+    def induce(self, out=None):
+        ud, up = (self._empty3(), self._empty3()) if out is None else out
+        rc = self.lib.t9gb_induce(self.h, C.c_void_p(ud.data_ptr()), C.c_void_p(up.data_ptr()))
+        self._check(rc, allow=(T9GB_NOT_CONVERGED, T9GB_NAN_DETECTED))
+        return ud, up, rc
+
+    def induce_host(self, xyz, uind=None, uinp=None):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        ud = np.zeros((self.n, 3)) if uind is None else uind
+        up = np.zeros((self.n, 3)) if uinp is None else uinp
+        rc = self.lib.t9gb_induce_host(self.h, _dp(xyz), _dp(ud), _dp(up))
+        self._check(rc, allow=(T9GB_NOT_CONVERGED, T9GB_NAN_DETECTED))
+        return ud, up, rc
+
+    def stats(self):
+        it, eps, st = C.c_int(), C.c_double(), C.c_int()
+        self.lib.t9gb_induce_stats(self.h, C.byref(it), C.byref(eps), C.byref(st))
+        return it.value, eps.value, st.value
+
+    def list_stats(self):
+        a, b, c = C.c_int(), C.c_longlong(), C.c_int()
+        self._check(self.lib.t9gb_nblist_stats(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return {"capacity": a.value, "entries": b.value, "scaled_pairs": c.value}
+
+    def profile(self, enable=True):
+        self._check(self.lib.t9gb_profile_enable(self.h, 1 if enable else 0))
+
+    def profile_read(self, reset=True):
+        """{category: (total_ms, launches)} accumulated since the last reset."""
+        out = {}
+        for c in range(10):
+            ms, cnt = C.c_double(), C.c_longlong()
+            self._check(self.lib.t9gb_profile_read(self.h, c, C.byref(ms), C.byref(cnt), 1 if reset else 0))
+            out[self.lib.t9gb_profile_name(c).decode()] = (ms.value, cnt.value)
+        return out
+
+    def udir(self):
+        f, fp = self._empty3(), self._empty3()
+        self._check(self.lib.t9gb_get_udir(self.h, C.c_void_p(f.data_ptr()), C.c_void_p(fp.data_ptr())))
+        return f, fp

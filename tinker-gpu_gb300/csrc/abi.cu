@@ -1,0 +1,451 @@
+// C ABI (include/t9gb.h): context lifetime, topology and coordinate upload,
+// and the public entry points.  Nothing here allocates inside the hot path:
+// every buffer is sized once in t9gb_create from the atom count.
+#include <cmath>
+#include <cstring>
+#include <new>
+
+#include "common.cuh"
+
+struct t9gb_context {
+   t9gb::Context c;
+};
+
+namespace t9gb {
+int induce_sorted(Context* ctx);
+int public_dfield(Context* ctx, float* field, float* fieldp);
+int public_ufield(Context* ctx, const float* uind, const float* uinp, float* field, float* fieldp);
+int public_precond(Context* ctx, const float* rsd, const float* rsdp, float* zrsd, float* zrsdp);
+}  // namespace t9gb
+
+using namespace t9gb;
+
+static int alloc_all(Context* ctx)
+{
+   const int n = ctx->n, npad = ctx->npad;
+   T9_CUDA(cudaMalloc(&ctx->frames, sizeof(int4) * n));
+   T9_CUDA(cudaMalloc(&ctx->pole, sizeof(float) * 10 * n));
+   T9_CUDA(cudaMalloc(&ctx->xyz, sizeof(float) * 3 * n));
+   T9_CUDA(cudaMalloc(&ctx->spos, sizeof(float4) * npad));
+   T9_CUDA(cudaMalloc(&ctx->spolar, sizeof(float) * npad));
+   T9_CUDA(cudaMalloc(&ctx->spolinv, sizeof(float) * npad));
+   T9_CUDA(cudaMalloc(&ctx->sdamp, sizeof(float2) * npad));
+   T9_CUDA(cudaMalloc(&ctx->srpole, sizeof(float) * 10 * npad));
+   T9_CUDA(cudaMalloc(&ctx->nnbr, sizeof(int) * npad));
+   T9_CUDA(cudaMemset(ctx->nnbr, 0, sizeof(int) * npad));
+   T9_CUDA(cudaMalloc(&ctx->nbr_over, sizeof(int)));
+   T9_CUDA(cudaMemset(ctx->nbr_over, 0, sizeof(int)));
+   T9_CUDA(cudaMallocHost(&ctx->h_over, sizeof(int)));
+   *ctx->h_over = 0;
+   T9_CUDA(cudaMalloc(&ctx->cell_atoms, sizeof(int) * npad));
+   T9_CUDA(cudaMalloc(&ctx->atom_cell, sizeof(int) * npad));
+   float** v6[] = {&ctx->rcp6, &ctx->fld6, &ctx->udir, &ctx->efield, &ctx->uind, &ctx->rsd, &ctx->zrsd,
+      &ctx->conj, &ctx->vec, &ctx->tmp6};
+   for (float** p : v6) {
+      T9_CUDA(cudaMalloc(p, sizeof(float) * 6 * npad));
+      T9_CUDA(cudaMemset(*p, 0, sizeof(float) * 6 * npad));
+   }
+   T9_CUDA(cudaMalloc(&ctx->red, sizeof(double) * RED_SLOTS * RED_MAX));
+   T9_CUDA(cudaMalloc(&ctx->scal, sizeof(double) * 64));
+   T9_CUDA(cudaMemset(ctx->scal, 0, sizeof(double) * 64));
+   T9_CUDA(cudaMalloc(&ctx->status, sizeof(int) * 16));
+   T9_CUDA(cudaMemset(ctx->status, 0, sizeof(int) * 16));
+   T9_CUDA(cudaMallocHost(&ctx->h_status, sizeof(int) * 16));
+   T9_CUDA(cudaMallocHost(&ctx->h_scal, sizeof(double) * 64));
+   if (ctx->cfg.predictor == 1) {
+      T9_CUDA(cudaMalloc(&ctx->aspc_hist, sizeof(float) * 16 * 6 * (size_t)npad));
+      T9_CUDA(cudaMemset(ctx->aspc_hist, 0, sizeof(float) * 16 * 6 * (size_t)npad));
+   }
+   ctx->h_stage_bytes = sizeof(float) * 6 * (size_t)npad;
+   T9_CUDA(cudaMallocHost(&ctx->h_stage, ctx->h_stage_bytes));
+   return T9GB_OK;
+}
+
+static void free_all(Context* ctx)
+{
+   void* dev[] = {ctx->frames, ctx->pole, ctx->xyz, ctx->perm, ctx->iperm, ctx->spos, ctx->spolar, ctx->spolinv,
+      ctx->sdamp, ctx->srpole, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->nbr, ctx->nnbr, ctx->nbr_over,
+      ctx->cell_count, ctx->cell_start, ctx->cell_atoms, ctx->atom_cell, ctx->rcp6, ctx->fld6, ctx->udir,
+      ctx->efield, ctx->uind, ctx->rsd, ctx->zrsd, ctx->conj, ctx->vec, ctx->tmp6, ctx->red, ctx->scal, ctx->status,
+      ctx->aspc_hist};
+   for (void* p : dev)
+      if (p)
+         cudaFree(p);
+   if (ctx->h_status)
+      cudaFreeHost(ctx->h_status);
+   if (ctx->h_scal)
+      cudaFreeHost(ctx->h_scal);
+   if (ctx->h_stage)
+      cudaFreeHost(ctx->h_stage);
+   if (ctx->h_over)
+      cudaFreeHost(ctx->h_over);
+   pme_free(ctx);
+   if (ctx->own_stream && ctx->stream)
+      cudaStreamDestroy(ctx->stream);
+}
+
+extern "C" {
+
+const char* t9gb_status_string(int status)
+{
+   switch (status) {
+   case T9GB_OK:
+      return "ok";
+   case T9GB_NOT_CONVERGED:
+      return "induced dipoles are not converged";
+   case T9GB_NAN_DETECTED:
+      return "non-finite residual in the induced-dipole solve";
+   case T9GB_BAD_ARG:
+      return "bad argument";
+   case T9GB_CUDA_ERR:
+      return "CUDA error";
+   case T9GB_NO_DEVICE:
+      return "no CUDA device";
+   case T9GB_NOT_READY:
+      return "topology, coordinates or neighbour list missing";
+   default:
+      return "unknown status";
+   }
+}
+
+const char* t9gb_last_error(const t9gb_context* h) { return h ? h->c.last_error.c_str() : "null context"; }
+
+int t9gb_create(const t9gb_config* cfg, t9gb_context** out)
+{
+   if (!cfg || !out || cfg->n <= 0)
+      return T9GB_BAD_ARG;
+   *out = nullptr;
+   int ndev = 0;
+   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+      return T9GB_NO_DEVICE;
+   if (cfg->bsorder != 5 && cfg->use_ewald)
+      return T9GB_BAD_ARG;
+   const bool pbc = cfg->box[0] > 0 && cfg->box[1] > 0 && cfg->box[2] > 0;
+   if (cfg->use_ewald && (!pbc || cfg->nfft[0] < 8 || cfg->nfft[1] < 8 || cfg->nfft[2] < 8 || cfg->aewald <= 0))
+      return T9GB_BAD_ARG;
+   if (cfg->politer < 1 || cfg->poleps <= 0)
+      return T9GB_BAD_ARG;
+   t9gb_context* h = new (std::nothrow) t9gb_context;
+   if (!h)
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   ctx->cfg = *cfg;
+   ctx->n = cfg->n;
+   ctx->npad = ((cfg->n + WARP - 1) / WARP) * WARP;
+   cudaGetDevice(&ctx->dev);
+   int rc = T9GB_OK;
+   if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess)
+      rc = T9GB_CUDA_ERR;
+   ctx->own_stream = true;
+   if (rc == T9GB_OK)
+      rc = alloc_all(ctx);
+   if (rc == T9GB_OK)
+      rc = pme_setup(ctx);
+   if (rc != T9GB_OK) {
+      free_all(ctx);
+      delete h;
+      return rc;
+   }
+   *out = h;
+   return T9GB_OK;
+}
+
+void t9gb_destroy(t9gb_context* h)
+{
+   if (!h)
+      return;
+   cudaStreamSynchronize(h->c.stream);
+   free_all(&h->c);
+   delete h;
+}
+
+int t9gb_set_stream(t9gb_context* h, void* stream)
+{
+   if (!h)
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   if (stream) {
+      if (ctx->own_stream && ctx->stream)
+         cudaStreamDestroy(ctx->stream);
+      ctx->stream = (cudaStream_t)stream;
+      ctx->own_stream = false;
+   } else if (!ctx->own_stream) {
+      T9_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+      ctx->own_stream = true;
+   }
+   return T9GB_OK;
+}
+
+int t9gb_set_topology(t9gb_context* h, const int* frames, const double* pole, const double* polarity,
+   const double* thole, const double* pdamp, int nexcl, const int* excl_ik, const double* excl_scale)
+{
+   if (!h || !frames || !pole || !polarity || !thole || !pdamp || nexcl < 0 || (nexcl > 0 && (!excl_ik || !excl_scale)))
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   const int n = ctx->n;
+   for (int i = 0; i < n; ++i) {
+      const int* f = frames + 4 * i;
+      if (f[3] < 0 || f[3] > 5)
+         return T9GB_BAD_ARG;
+      if (f[3] != 0 && (f[0] < 0 || f[0] >= n))
+         return T9GB_BAD_ARG;
+      if ((f[3] >= 2) && (f[1] < 0 || f[1] >= n))
+         return T9GB_BAD_ARG;
+      if ((f[3] == 4 || f[3] == 5 || (f[3] == 2 && f[2] != 0)) && (std::abs(f[2]) < 1 || std::abs(f[2]) > n))
+         return T9GB_BAD_ARG;
+   }
+   for (int j = 0; j < nexcl; ++j) {
+      int a = excl_ik[2 * j], b = excl_ik[2 * j + 1];
+      if (a < 0 || b < 0 || a >= n || b >= n || a == b)
+         return T9GB_BAD_ARG;
+   }
+   ctx->h_polarity.assign(polarity, polarity + n);
+   ctx->h_thole.assign(thole, thole + n);
+   ctx->h_pdamp.assign(pdamp, pdamp + n);
+   ctx->h_excl_ik.assign(excl_ik, excl_ik + 2 * nexcl);
+   ctx->h_excl_scale.assign(excl_scale, excl_scale + 4 * nexcl);
+   std::vector<float> pf(10 * (size_t)n);
+   for (size_t i = 0; i < pf.size(); ++i)
+      pf[i] = (float)pole[i];
+   T9_CUDA(cudaMemcpy(ctx->frames, frames, sizeof(int4) * n, cudaMemcpyHostToDevice));
+   T9_CUDA(cudaMemcpy(ctx->pole, pf.data(), sizeof(float) * 10 * n, cudaMemcpyHostToDevice));
+   ctx->have_topology = true;
+   ctx->have_order = false;
+   return T9GB_OK;
+}
+
+int t9gb_set_xyz_host(t9gb_context* h, const double* xyz)
+{
+   if (!h || !xyz)
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   const int n = ctx->n;
+   ctx->h_xyz.assign(xyz, xyz + 3 * n);
+   float* st = ctx->h_stage;
+   for (int i = 0; i < 3 * n; ++i) {
+      if (!std::isfinite(xyz[i]))
+         return T9GB_BAD_ARG;
+      st[i] = (float)xyz[i];
+   }
+   T9_CUDA(cudaMemcpyAsync(ctx->xyz, st, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
+   ctx->have_xyz = true;
+   if (ctx->have_order)
+      T9_CHECK(scatter_positions(ctx));
+   // the staging buffer is reused by the next call: finish the copy
+   T9_CUDA(cudaStreamSynchronize(ctx->stream));
+   return T9GB_OK;
+}
+
+int t9gb_set_xyz_device(t9gb_context* h, const float* xyz_device)
+{
+   if (!h || !xyz_device)
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   T9_CUDA(cudaMemcpyAsync(ctx->xyz, xyz_device, sizeof(float) * 3 * ctx->n, cudaMemcpyDeviceToDevice, ctx->stream));
+   if (!ctx->have_xyz || ctx->h_xyz.empty()) {
+      // the host list builder needs a host copy of the first coordinates
+      std::vector<float> tmp(3 * (size_t)ctx->n);
+      T9_CUDA(cudaMemcpyAsync(tmp.data(), xyz_device, sizeof(float) * 3 * ctx->n, cudaMemcpyDeviceToHost, ctx->stream));
+      T9_CUDA(cudaStreamSynchronize(ctx->stream));
+      ctx->h_xyz.assign(tmp.begin(), tmp.end());
+   }
+   ctx->have_xyz = true;
+   if (ctx->have_order)
+      T9_CHECK(scatter_positions(ctx));
+   return T9GB_OK;
+}
+
+int t9gb_nblist_build(t9gb_context* h)
+{
+   if (!h)
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   if (!ctx->have_topology || !ctx->have_xyz)
+      return T9GB_NOT_READY;
+   if (ctx->h_xyz.empty() || (int)ctx->h_xyz.size() != 3 * ctx->n) {
+      std::vector<float> tmp(3 * (size_t)ctx->n);
+      T9_CUDA(cudaMemcpyAsync(tmp.data(), ctx->xyz, sizeof(float) * 3 * ctx->n, cudaMemcpyDeviceToHost, ctx->stream));
+      T9_CUDA(cudaStreamSynchronize(ctx->stream));
+      ctx->h_xyz.assign(tmp.begin(), tmp.end());
+   }
+   T9_CUDA(cudaStreamSynchronize(ctx->stream));
+   T9_CHECK(order_build(ctx));
+   T9_CHECK(scatter_positions(ctx));
+   return T9GB_OK;
+}
+
+int t9gb_mpole_init(t9gb_context* h)
+{
+   if (!h)
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   if (!ctx->have_order)
+      return T9GB_NOT_READY;
+   return rotpole_sorted(ctx);
+}
+
+int t9gb_dfield(t9gb_context* h, float* field, float* fieldp)
+{
+   if (!h || !field || !fieldp)
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   if (!ctx->have_order)
+      return T9GB_NOT_READY;
+   return public_dfield(ctx, field, fieldp);
+}
+
+int t9gb_ufield(t9gb_context* h, const float* uind, const float* uinp, float* field, float* fieldp)
+{
+   if (!h || !uind || !uinp || !field || !fieldp)
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   if (!ctx->have_order)
+      return T9GB_NOT_READY;
+   return public_ufield(ctx, uind, uinp, field, fieldp);
+}
+
+int t9gb_sparse_precond_apply(t9gb_context* h, const float* rsd, const float* rsdp, float* zrsd, float* zrsdp)
+{
+   if (!h || !rsd || !rsdp || !zrsd || !zrsdp)
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   if (!ctx->have_order || !ctx->cfg.pcgprec)
+      return T9GB_NOT_READY;
+   return public_precond(ctx, rsd, rsdp, zrsd, zrsdp);
+}
+
+int t9gb_induce(t9gb_context* h, float* uind, float* uinp)
+{
+   if (!h)
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   if (!ctx->have_order)
+      return T9GB_NOT_READY;
+   int st = induce_sorted(ctx);
+   if (st != T9GB_OK && st != T9GB_NOT_CONVERGED && st != T9GB_NAN_DETECTED)
+      return st;
+   if (uind || uinp) {
+      int rc = scatter_from_sorted3(ctx, ctx->uind, uind, uinp);
+      if (rc != T9GB_OK)
+         return rc;
+   }
+   return st;
+}
+
+int t9gb_induce_host(t9gb_context* h, const double* xyz, double* uind, double* uinp)
+{
+   if (!h || !xyz)
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   T9_CHECK(t9gb_set_xyz_host(h, xyz));
+   if (!ctx->have_order)
+      T9_CHECK(t9gb_nblist_build(h));
+   T9_CHECK(t9gb_mpole_init(h));
+   int st = induce_sorted(ctx);
+   if (st != T9GB_OK && st != T9GB_NOT_CONVERGED && st != T9GB_NAN_DETECTED)
+      return st;
+   const int n = ctx->n;
+   // dipoles to caller order in the scratch vector, then one D2H copy
+   T9_CHECK(scatter_from_sorted3(ctx, ctx->uind, ctx->tmp6, ctx->tmp6 + 3 * n));
+   T9_CUDA(cudaMemcpyAsync(ctx->h_stage, ctx->tmp6, sizeof(float) * 6 * n, cudaMemcpyDeviceToHost, ctx->stream));
+   T9_CUDA(cudaStreamSynchronize(ctx->stream));
+   for (int i = 0; i < 3 * n; ++i) {
+      if (uind)
+         uind[i] = ctx->h_stage[i];
+      if (uinp)
+         uinp[i] = ctx->h_stage[3 * n + i];
+   }
+   return st;
+}
+
+int t9gb_induce_stats(const t9gb_context* h, int* iterations, double* eps, int* status)
+{
+   if (!h)
+      return T9GB_BAD_ARG;
+   if (iterations)
+      *iterations = h->c.last_iter;
+   if (eps)
+      *eps = h->c.last_eps;
+   if (status)
+      *status = h->c.last_status;
+   return T9GB_OK;
+}
+
+int t9gb_get_udir(t9gb_context* h, float* udir, float* udirp)
+{
+   if (!h || (!udir && !udirp))
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   if (!ctx->have_order)
+      return T9GB_NOT_READY;
+   return scatter_from_sorted3(ctx, ctx->udir, udir, udirp);
+}
+
+int t9gb_nblist_stats(t9gb_context* h, int* capacity, long long* entries, int* nscaled)
+{
+   if (!h)
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   if (capacity)
+      *capacity = ctx->nbr_cap;
+   if (nscaled)
+      *nscaled = ctx->nsp / 2;
+   if (entries) {
+      *entries = 0;
+      if (ctx->have_order && !ctx->list_stale) {
+         std::vector<int> cnt(ctx->npad);
+         T9_CUDA(cudaMemcpyAsync(cnt.data(), ctx->nnbr, sizeof(int) * ctx->npad, cudaMemcpyDeviceToHost, ctx->stream));
+         T9_CUDA(cudaStreamSynchronize(ctx->stream));
+         for (int c : cnt)
+            *entries += c;
+      }
+   }
+   return T9GB_OK;
+}
+
+int t9gb_profile_enable(t9gb_context* h, int enable)
+{
+   if (!h)
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   Profiler& p = ctx->prof;
+   if (enable && p.ev.empty()) {
+      const int npair = 8192;
+      p.ev.resize(2 * npair);
+      p.cat.resize(npair);
+      for (auto& e : p.ev)
+         T9_CUDA(cudaEventCreate(&e));
+   }
+   p.on = enable != 0;
+   p.used = 0;
+   return T9GB_OK;
+}
+
+int t9gb_profile_read(t9gb_context* h, int category, double* total_ms, long long* launches, int reset)
+{
+   if (!h || category < 0 || category >= P_NCAT)
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   T9_CUDA(cudaStreamSynchronize(ctx->stream));
+   prof_collect(ctx);
+   if (total_ms)
+      *total_ms = ctx->prof.ms[category];
+   if (launches)
+      *launches = ctx->prof.cnt[category];
+   if (reset) {
+      ctx->prof.ms[category] = 0;
+      ctx->prof.cnt[category] = 0;
+   }
+   return T9GB_OK;
+}
+
+const char* t9gb_profile_name(int category)
+{
+   static const char* names[P_NCAT] = {"dfield_real", "ufield_real", "precond_sparse", "spread_mpole",
+      "spread_uind", "fft_conv", "gather_mpole", "gather_uind", "pcg_vector", "nblist"};
+   if (category < 0 || category >= P_NCAT)
+      return "";
+   return names[category];
+}
+
+}  // extern "C"

@@ -1,0 +1,238 @@
+// Shared definitions of the GB300 polarization library: the context that owns
+// every device buffer, fixed-point helpers, the Hastings erfc, and the
+// per-kernel event profiler.
+#pragma once
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/t9gb.h"
+
+namespace t9gb {
+
+constexpr int WARP = 32;
+constexpr int BSORDER = 5;
+constexpr int GROUP = 8;  // lanes per atom in the real-space kernels
+
+// The PME grid accumulates in signed 64-bit fixed point with 40 fractional
+// bits: order-independent (bit-reproducible) sums, range +-8.4e6,
+// resolution 9.1e-13.
+constexpr double FX_SCALE = 1099511627776.0;  // 2^40
+constexpr double FX_INV = 1.0 / 1099511627776.0;
+
+__device__ __forceinline__ long long to_fx(float v) { return __float2ll_rn(v * 1099511627776.0f); }
+__device__ __forceinline__ float from_fx(long long v) { return (float)((double)v * FX_INV); }
+
+// Complementary error function, Hastings' rational approximation (C. Hastings,
+// Approximations for Digital Computers, Princeton 1955, p. 167; Abramowitz &
+// Stegun 7.1.26), sharing exp(-x^2) with the caller; the reference's float
+// build uses the same approximation (include/math/libfunc.h:12-28).
+__device__ __forceinline__ float erfc_hastings(float x, float expmx2)
+{
+   float t = __frcp_rn(1.0f + 0.3275911f * x);
+   return (0.254829592f + (-0.284496736f + (1.421413741f + (-1.453152027f + 1.061405429f * t) * t) * t) * t) * t
+      * expmx2;
+}
+
+__device__ __forceinline__ float image1(float d, float l, float linv) { return d - l * rintf(d * linv); }
+
+struct PmeGrid {
+   int n1 = 0, n2 = 0, n3 = 0;
+   cufftHandle plan = 0;
+   float2* qgrid = nullptr;   // complex grid [n3][n2][n1]
+   long long* qfx = nullptr;  // fixed-point accumulation grid [n3][n2][n1][2]
+   float* infl = nullptr;     // influence function [n3][n2][n1]
+};
+
+// Per-kernel event timing (tracing): categories of timed launches.
+enum ProfCat {
+   P_DFIELD_REAL = 0,
+   P_UFIELD_REAL,
+   P_PRECOND,
+   P_SPREAD_MPOLE,
+   P_SPREAD_UIND,
+   P_FFT_CONV,
+   P_GATHER_MPOLE,
+   P_GATHER_UIND,
+   P_VECTOR,
+   P_NBLIST,
+   P_NCAT
+};
+
+struct Profiler {
+   bool on = false;
+   std::vector<cudaEvent_t> ev;  // pairs
+   std::vector<int> cat;
+   int used = 0;
+   double ms[P_NCAT] = {0};
+   long long cnt[P_NCAT] = {0};
+};
+
+struct Context {
+   t9gb_config cfg;
+   Profiler prof;
+   int n = 0;
+   int npad = 0;  // n rounded up to 32
+   int dev = 0;
+   cudaStream_t stream = nullptr;
+   bool own_stream = false;
+   std::string last_error;
+
+   // topology, caller atom order
+   int4* frames = nullptr;  // zaxis, xaxis, yaxis (1-based signed), kind
+   float* pole = nullptr;   // [n][10] local frame
+   std::vector<double> h_polarity, h_thole, h_pdamp;
+   std::vector<int> h_excl_ik;
+   std::vector<double> h_excl_scale;
+
+   // coordinates, caller order
+   float* xyz = nullptr;       // [n][3]
+   std::vector<double> h_xyz;  // copy for the host-side ordering
+   bool have_xyz = false;
+   bool have_topology = false;
+   bool have_order = false;
+
+   // sorted layout: the internal order of every hot-path array
+   int* perm = nullptr;   // slot -> atom (-1 for padding)
+   int* iperm = nullptr;  // atom -> slot
+   std::vector<int> h_perm, h_iperm;
+   float4* spos = nullptr;   // [npad]
+   float* spolar = nullptr;  // [npad] polarizability (0 on padding)
+   float* spolinv = nullptr; // [npad] 1/max(alpha, 1e-16)
+   float2* sdamp = nullptr;  // [npad] pdamp, thole
+   float* srpole = nullptr;  // [npad][10] global-frame multipoles
+
+   // scaled partners of every slot, both directions (CSR over slots)
+   int* sp_start = nullptr;  // [npad + 1]
+   int* sp_j = nullptr;      // partner slot
+   float4* sp_sc = nullptr;  // m, d, p, u
+   int nsp = 0;
+
+   // per-step neighbour list (exact cutoff, scaled partners excluded)
+   float list_cut = 0;
+   int nbr_cap = 0;
+   int* nbr = nullptr;       // [npad][nbr_cap]
+   int* nnbr = nullptr;      // [npad]
+   int* nbr_over = nullptr;  // device max count seen (overflow check)
+   int* h_over = nullptr;    // pinned mirror
+   bool list_stale = true;
+   bool use_cells = false;
+   int nc[3] = {0, 0, 0};
+   int ncell = 0;
+   int* cell_count = nullptr;
+   int* cell_start = nullptr;  // [ncell + 1]
+   int* cell_atoms = nullptr;  // [npad]
+   int* atom_cell = nullptr;   // [npad]
+
+   // PME
+   PmeGrid pme;
+
+   // fields and PCG work, all sorted [npad][6]: d xyz, p xyz
+   float* rcp6 = nullptr;   // reciprocal + self field
+   float* fld6 = nullptr;   // total field of the last dfield/ufield
+   float* udir = nullptr;
+   float* efield = nullptr;
+   float* uind = nullptr;
+   float* rsd = nullptr;
+   float* zrsd = nullptr;
+   float* conj = nullptr;
+   float* vec = nullptr;
+   float* tmp6 = nullptr;
+   double* red = nullptr;   // reduction partials [RED_SLOTS][RED_MAX]
+   double* scal = nullptr;  // device scalars
+   int* status = nullptr;   // device status words
+   int* h_status = nullptr; // pinned mirrors
+   double* h_scal = nullptr;
+
+   // ASPC predictor ring, sorted [16][npad][6]
+   float* aspc_hist = nullptr;
+   int nualt = 0;
+
+   // last induce statistics
+   int last_iter = 0;
+   double last_eps = 0;
+   int last_status = 0;
+
+   // pinned staging for host entry points
+   float* h_stage = nullptr;
+   size_t h_stage_bytes = 0;
+};
+
+// reductions: up to RED_MAX block partials per slot
+constexpr int RED_MAX = 1024;
+constexpr int RED_SLOTS = 8;
+
+#define T9_CUDA(call)                                                                                                  \
+   do {                                                                                                                \
+      cudaError_t err_ = (call);                                                                                       \
+      if (err_ != cudaSuccess) {                                                                                       \
+         ctx->last_error = std::string(#call) + ": " + cudaGetErrorString(err_);                                       \
+         return T9GB_CUDA_ERR;                                                                                         \
+      }                                                                                                                \
+   } while (0)
+
+#define T9_CHECK(expr)                                                                                                 \
+   do {                                                                                                                \
+      int rc_ = (expr);                                                                                                \
+      if (rc_ != T9GB_OK)                                                                                              \
+         return rc_;                                                                                                   \
+   } while (0)
+
+inline int grid_for(long long n, int block) { return (int)((n + block - 1) / block); }
+
+// timed launch bracket; a no-op unless profiling is on
+inline void prof_begin(Context* ctx, int cat)
+{
+   Profiler& p = ctx->prof;
+   if (!p.on || p.used + 1 >= (int)p.cat.size())
+      return;
+   cudaEventRecord(p.ev[2 * p.used], ctx->stream);
+   p.cat[p.used] = cat;
+}
+inline void prof_end(Context* ctx)
+{
+   Profiler& p = ctx->prof;
+   if (!p.on || p.used + 1 >= (int)p.cat.size())
+      return;
+   cudaEventRecord(p.ev[2 * p.used + 1], ctx->stream);
+   p.used++;
+}
+// accumulate recorded pairs (call after the stream is synchronised)
+inline void prof_collect(Context* ctx)
+{
+   Profiler& p = ctx->prof;
+   for (int i = 0; i < p.used; ++i) {
+      float ms = 0;
+      if (cudaEventElapsedTime(&ms, p.ev[2 * i], p.ev[2 * i + 1]) == cudaSuccess) {
+         p.ms[p.cat[i]] += ms;
+         p.cnt[p.cat[i]] += 1;
+      }
+   }
+   p.used = 0;
+}
+
+// ---- entry points implemented across the translation units ----
+int order_build(Context* ctx);  // host: spatial order, scaled partners
+int list_update(Context* ctx);  // device: exact neighbour list
+int scatter_positions(Context* ctx);
+int rotpole_sorted(Context* ctx);
+int pme_setup(Context* ctx);
+void pme_free(Context* ctx);
+
+// real space (pair.cu): out6 = base6 (may be null) + real-space field
+int launch_dfield_real(Context* ctx, const float* base6, float* out6);
+int launch_ufield_real(Context* ctx, const float* u6, const float* base6, float* out6);
+int launch_precond_sparse(Context* ctx, const float* r6, float* z6);
+
+// reciprocal space (pme.cu): out6 = recip + self field (plain store)
+int launch_dfield_recip(Context* ctx, float* out6);
+int launch_ufield_recip(Context* ctx, const float* u6, float* out6);
+
+// permutation helpers (nblist.cu)
+int gather_to_sorted3(Context* ctx, const float* a, const float* b, float* s6);
+int scatter_from_sorted3(Context* ctx, const float* s6, float* a, float* b);
+
+}  // namespace t9gb

@@ -1,0 +1,660 @@
+// Sorted layout, scaled-partner table, per-step neighbour list, permutation
+// and multipole-rotation kernels.
+//
+// The reference keeps atom arrays in input order and reaches them through
+// SortedAtom::unsorted inside every pair kernel, with a 32x32 block-pair list
+// rebuilt when atoms leave the list buffer (include/ff/spatial.h:15-140,
+// src/cu/spatial.cu:149-960, src/spatial.cpp:201-205).  Here:
+//  - the hot path lives in one spatial (Morton) order fixed when the order is
+//    built; only the public entry points permute;
+//  - every step (new coordinates) the device rebuilds an exact per-atom list
+//    of neighbours within the cutoff from a cell grid (cells >= cutoff / 2,
+//    5x5x5 stencil scanned as 25 contiguous x-runs), so the pair kernels
+//    evaluate no pair beyond the cutoff and need no list buffer;
+//  - scaled pairs (exclusions) are kept out of the list and evaluated from a
+//    small per-atom partner table with their m/d/p/u scales, which is the
+//    reference's exclusion-loop semantics (src/cu/amoeba/dfield_cu1.cc:30-106);
+//  - list order is fixed (stencil order, then ascending slot within a cell),
+//    so every real-space sum has a deterministic order.
+#include <algorithm>
+#include <cmath>
+#include <map>
+
+#include "common.cuh"
+
+namespace t9gb {
+
+static inline uint64_t spread_bits(uint64_t v)
+{
+   v &= 0x1fffff;
+   v = (v | v << 32) & 0x1f00000000ffffULL;
+   v = (v | v << 16) & 0x1f0000ff0000ffULL;
+   v = (v | v << 8) & 0x100f00f00f00f00fULL;
+   v = (v | v << 4) & 0x10c30c30c30c30c3ULL;
+   v = (v | v << 2) & 0x1249249249249249ULL;
+   return v;
+}
+
+static bool is_pbc(const t9gb_config& c) { return c.box[0] > 0 && c.box[1] > 0 && c.box[2] > 0; }
+
+static double list_cutoff(const t9gb_config& c)
+{
+   double r = c.cutoff;
+   if (c.pcgprec)
+      r = std::max(r, c.usolve_cutoff + c.pbuffer);
+   return r;
+}
+
+// Host: Morton order of the current coordinates, per-slot parameters, the
+// scaled-partner table and the neighbour-list storage.
+int order_build(Context* ctx)
+{
+   const int n = ctx->n, npad = ctx->npad;
+   const t9gb_config& cfg = ctx->cfg;
+   const bool pbc = is_pbc(cfg);
+   const double* p = ctx->h_xyz.data();
+
+   double lo[3], len[3];
+   for (int d = 0; d < 3; ++d) {
+      if (pbc) {
+         lo[d] = 0;
+         len[d] = cfg.box[d];
+      } else {
+         double mn = 1e300, mx = -1e300;
+         for (int i = 0; i < n; ++i) {
+            mn = std::min(mn, p[3 * i + d]);
+            mx = std::max(mx, p[3 * i + d]);
+         }
+         lo[d] = mn;
+         len[d] = std::max(mx - mn, 1.0);
+      }
+   }
+   const double lmax = std::max(len[0], std::max(len[1], len[2]));
+   int bits = 1;
+   while ((1 << bits) * 1.5 < lmax && bits < 20)
+      ++bits;
+   const int g = 1 << bits;
+   std::vector<std::pair<uint64_t, int>> key(n);
+   for (int i = 0; i < n; ++i) {
+      uint64_t c[3];
+      for (int d = 0; d < 3; ++d) {
+         double f = (p[3 * i + d] - lo[d]) / len[d];
+         if (pbc)
+            f -= std::floor(f);
+         long v = (long)(f * g);
+         v = std::min<long>(std::max<long>(v, 0), g - 1);
+         c[d] = (uint64_t)v;
+      }
+      key[i] = {spread_bits(c[0]) | spread_bits(c[1]) << 1 | spread_bits(c[2]) << 2, i};
+   }
+   std::sort(key.begin(), key.end());
+   ctx->h_perm.assign(npad, -1);
+   ctx->h_iperm.assign(n, -1);
+   for (int s = 0; s < n; ++s) {
+      ctx->h_perm[s] = key[s].second;
+      ctx->h_iperm[key[s].second] = s;
+   }
+
+   // scaled partners per slot, both directions, ascending partner slot
+   const int nex = (int)ctx->h_excl_scale.size() / 4;
+   std::vector<std::vector<std::pair<int, float4>>> part(npad);
+   for (int j = 0; j < nex; ++j) {
+      int si = ctx->h_iperm[ctx->h_excl_ik[2 * j]];
+      int sk = ctx->h_iperm[ctx->h_excl_ik[2 * j + 1]];
+      const double* v = &ctx->h_excl_scale[4 * j];
+      float4 sc = make_float4((float)v[0], (float)v[1], (float)v[2], (float)v[3]);
+      part[si].push_back({sk, sc});
+      part[sk].push_back({si, sc});
+   }
+   std::vector<int> sp_start(npad + 1, 0), sp_j;
+   std::vector<float4> sp_sc;
+   for (int s = 0; s < npad; ++s) {
+      auto& v = part[s];
+      std::sort(v.begin(), v.end(), [](const std::pair<int, float4>& a, const std::pair<int, float4>& b) {
+         return a.first < b.first;
+      });
+      sp_start[s + 1] = sp_start[s] + (int)v.size();
+      for (auto& e : v) {
+         sp_j.push_back(e.first);
+         sp_sc.push_back(e.second);
+      }
+   }
+   ctx->nsp = (int)sp_j.size();
+
+   // per-slot polarization parameters
+   std::vector<float> pol(npad, 0.f), pinv(npad, 0.f);
+   std::vector<float2> dmp(npad, make_float2(0.f, 0.f));
+   for (int s = 0; s < n; ++s) {
+      int a = ctx->h_perm[s];
+      pol[s] = (float)ctx->h_polarity[a];
+      pinv[s] = (float)(1.0 / std::max(ctx->h_polarity[a], 1.0e-16));
+      dmp[s] = make_float2((float)ctx->h_pdamp[a], (float)ctx->h_thole[a]);
+   }
+
+   // cell grid and list capacity
+   const double R = list_cutoff(cfg);
+   ctx->list_cut = (float)R;
+   ctx->use_cells = false;
+   if (pbc && R < 1.0e6) {
+      bool ok = true;
+      for (int d = 0; d < 3; ++d) {
+         ctx->nc[d] = (int)std::floor(cfg.box[d] / (0.5 * R * 1.0001));
+         if (ctx->nc[d] < 5)
+            ok = false;
+      }
+      ctx->use_cells = ok;
+   }
+   if (!ctx->use_cells && n > 16384) {
+      ctx->last_error = "box too small for the cell grid (needs >= 2.5 cutoffs per edge) and too many atoms for "
+                        "the all-pairs list";
+      return T9GB_BAD_ARG;
+   }
+   int cap;
+   if (ctx->use_cells) {
+      ctx->ncell = ctx->nc[0] * ctx->nc[1] * ctx->nc[2];
+      double vol = cfg.box[0] * cfg.box[1] * cfg.box[2];
+      double expect = n / vol * 4.18879020478639 * R * R * R;
+      cap = (int)(expect * 1.5) + 32;
+   } else {
+      ctx->ncell = 0;
+      cap = npad;
+   }
+   cap = ((cap + 31) / 32) * 32;
+   cap = std::max(cap, ctx->nbr_cap);
+
+   cudaFree(ctx->perm);
+   cudaFree(ctx->iperm);
+   cudaFree(ctx->sp_start);
+   cudaFree(ctx->sp_j);
+   cudaFree(ctx->sp_sc);
+   cudaFree(ctx->cell_count);
+   cudaFree(ctx->cell_start);
+   ctx->perm = ctx->iperm = ctx->sp_start = ctx->sp_j = ctx->cell_count = ctx->cell_start = nullptr;
+   ctx->sp_sc = nullptr;
+   T9_CUDA(cudaMalloc(&ctx->perm, sizeof(int) * npad));
+   T9_CUDA(cudaMalloc(&ctx->iperm, sizeof(int) * n));
+   T9_CUDA(cudaMalloc(&ctx->sp_start, sizeof(int) * (npad + 1)));
+   T9_CUDA(cudaMalloc(&ctx->sp_j, sizeof(int) * std::max(1, ctx->nsp)));
+   T9_CUDA(cudaMalloc(&ctx->sp_sc, sizeof(float4) * std::max(1, ctx->nsp)));
+   T9_CUDA(cudaMemcpy(ctx->perm, ctx->h_perm.data(), sizeof(int) * npad, cudaMemcpyHostToDevice));
+   T9_CUDA(cudaMemcpy(ctx->iperm, ctx->h_iperm.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+   T9_CUDA(cudaMemcpy(ctx->sp_start, sp_start.data(), sizeof(int) * (npad + 1), cudaMemcpyHostToDevice));
+   if (ctx->nsp) {
+      T9_CUDA(cudaMemcpy(ctx->sp_j, sp_j.data(), sizeof(int) * ctx->nsp, cudaMemcpyHostToDevice));
+      T9_CUDA(cudaMemcpy(ctx->sp_sc, sp_sc.data(), sizeof(float4) * ctx->nsp, cudaMemcpyHostToDevice));
+   }
+   T9_CUDA(cudaMemcpy(ctx->spolar, pol.data(), sizeof(float) * npad, cudaMemcpyHostToDevice));
+   T9_CUDA(cudaMemcpy(ctx->spolinv, pinv.data(), sizeof(float) * npad, cudaMemcpyHostToDevice));
+   T9_CUDA(cudaMemcpy(ctx->sdamp, dmp.data(), sizeof(float2) * npad, cudaMemcpyHostToDevice));
+   if (ctx->use_cells) {
+      T9_CUDA(cudaMalloc(&ctx->cell_count, sizeof(int) * ctx->ncell));
+      T9_CUDA(cudaMalloc(&ctx->cell_start, sizeof(int) * (ctx->ncell + 1)));
+   }
+   if (cap != ctx->nbr_cap) {
+      cudaFree(ctx->nbr);
+      ctx->nbr = nullptr;
+      T9_CUDA(cudaMalloc(&ctx->nbr, sizeof(int) * (size_t)npad * cap));
+      ctx->nbr_cap = cap;
+   }
+   ctx->have_order = true;
+   ctx->list_stale = true;
+   // a new order invalidates the predictor history
+   ctx->nualt = 0;
+   return T9GB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// device list build
+
+struct CellParams {
+   int n, npad;
+   int ncx, ncy, ncz;
+   float lx, ly, lz, ilx, ily, ilz;
+   float r2;
+   int cap;
+};
+
+__device__ __forceinline__ int cell_coord(float x, float il, int nc)
+{
+   float f = x * il;
+   f -= floorf(f);
+   int c = (int)(f * nc);
+   return c < 0 ? 0 : (c >= nc ? nc - 1 : c);
+}
+
+__global__ void k_cell_assign(CellParams C, const float4* __restrict__ spos, int* __restrict__ atom_cell,
+   int* __restrict__ cell_count)
+{
+   int s = blockIdx.x * blockDim.x + threadIdx.x;
+   if (s >= C.n)
+      return;
+   float4 p = spos[s];
+   int cx = cell_coord(p.x, C.ilx, C.ncx), cy = cell_coord(p.y, C.ily, C.ncy), cz = cell_coord(p.z, C.ilz, C.ncz);
+   int c = (cz * C.ncy + cy) * C.ncx + cx;
+   atom_cell[s] = c;
+   atomicAdd(cell_count + c, 1);
+}
+
+// exclusive scan of the cell counts (one block); clears the counts for reuse
+// as fill cursors
+__global__ void k_cell_scan(int ncell, int* __restrict__ count, int* __restrict__ start)
+{
+   __shared__ int part[1024];
+   const int t = threadIdx.x, nt = blockDim.x;
+   const int chunk = (ncell + nt - 1) / nt;
+   const int a = t * chunk, b = min(ncell, a + chunk);
+   int sum = 0;
+   for (int c = a; c < b; ++c)
+      sum += count[c];
+   part[t] = sum;
+   __syncthreads();
+   for (int o = 1; o < nt; o <<= 1) {
+      int v = t >= o ? part[t - o] : 0;
+      __syncthreads();
+      part[t] += v;
+      __syncthreads();
+   }
+   int run = part[t] - sum;
+   for (int c = a; c < b; ++c) {
+      start[c] = run;
+      run += count[c];
+      count[c] = 0;
+   }
+   if (t == nt - 1)
+      start[ncell] = part[t];
+}
+
+__global__ void k_cell_fill(int n, const int* __restrict__ atom_cell, const int* __restrict__ start,
+   int* __restrict__ cursor, int* __restrict__ cell_atoms)
+{
+   int s = blockIdx.x * blockDim.x + threadIdx.x;
+   if (s >= n)
+      return;
+   int c = atom_cell[s];
+   cell_atoms[start[c] + atomicAdd(cursor + c, 1)] = s;
+}
+
+// ascending slots inside each cell (fixes the list order)
+__global__ void k_cell_sort(int ncell, const int* __restrict__ start, int* __restrict__ cell_atoms)
+{
+   int c = blockIdx.x * blockDim.x + threadIdx.x;
+   if (c >= ncell)
+      return;
+   int a = start[c], b = start[c + 1];
+   for (int i = a + 1; i < b; ++i) {
+      int v = cell_atoms[i];
+      int j = i - 1;
+      while (j >= a && cell_atoms[j] > v) {
+         cell_atoms[j + 1] = cell_atoms[j];
+         --j;
+      }
+      cell_atoms[j + 1] = v;
+   }
+}
+
+__device__ __forceinline__ bool is_partner(const int* __restrict__ sp_j, int a, int b, int j)
+{
+   for (int q = a; q < b; ++q)
+      if (sp_j[q] == j)
+         return true;
+   return false;
+}
+
+// one warp per atom; 25 x-runs of five cells, compacted with ballots
+__global__ void __launch_bounds__(256) k_nbr_cells(CellParams C, const float4* __restrict__ spos,
+   const int* __restrict__ atom_cell, const int* __restrict__ start, const int* __restrict__ cell_atoms,
+   const int* __restrict__ sp_start, const int* __restrict__ sp_j, int* __restrict__ nbr, int* __restrict__ nnbr,
+   int* __restrict__ over)
+{
+   const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+   const int lane = threadIdx.x & 31;
+   if (i >= C.npad)
+      return;
+   if (i >= C.n) {
+      if (lane == 0)
+         nnbr[i] = 0;
+      return;
+   }
+   const float4 pi = spos[i];
+   const int ci = atom_cell[i];
+   const int cix = ci % C.ncx, ciy = (ci / C.ncx) % C.ncy, ciz = ci / (C.ncx * C.ncy);
+   const int pa = sp_start[i], pb = sp_start[i + 1];
+   const unsigned lt = (1u << lane) - 1u;
+   int cnt = 0;
+   int* out = nbr + (size_t)i * C.cap;
+   for (int dz = -2; dz <= 2; ++dz) {
+      int cz = ciz + dz;
+      cz += (cz < 0 ? C.ncz : 0) - (cz >= C.ncz ? C.ncz : 0);
+      for (int dy = -2; dy <= 2; ++dy) {
+         int cy = ciy + dy;
+         cy += (cy < 0 ? C.ncy : 0) - (cy >= C.ncy ? C.ncy : 0);
+         const int row = (cz * C.ncy + cy) * C.ncx;
+         int x0 = cix - 2, x1 = cix + 2;
+         // up to two runs of consecutive cells along x
+         int ra[2], rb[2], nrun = 0;
+         if (x0 < 0) {
+            ra[nrun] = x0 + C.ncx;
+            rb[nrun++] = C.ncx - 1;
+            x0 = 0;
+         }
+         if (x1 >= C.ncx) {
+            ra[nrun] = x0;
+            rb[nrun++] = C.ncx - 1;
+            ra[nrun] = 0;
+            rb[nrun++] = x1 - C.ncx;
+         } else {
+            ra[nrun] = x0;
+            rb[nrun++] = x1;
+         }
+         for (int r = 0; r < nrun; ++r) {
+            const int a = start[row + ra[r]], b = start[row + rb[r] + 1];
+            for (int t = a; t < b; t += 32) {
+               const int idx = t + lane;
+               bool acc = false;
+               int j = -1;
+               if (idx < b) {
+                  j = cell_atoms[idx];
+                  float4 pj = spos[j];
+                  float dx = image1(pj.x - pi.x, C.lx, C.ilx);
+                  float dy2 = image1(pj.y - pi.y, C.ly, C.ily);
+                  float dz2 = image1(pj.z - pi.z, C.lz, C.ilz);
+                  acc = j != i && dx * dx + dy2 * dy2 + dz2 * dz2 <= C.r2 && !is_partner(sp_j, pa, pb, j);
+               }
+               const unsigned m = __ballot_sync(0xffffffffu, acc);
+               const int pos = cnt + __popc(m & lt);
+               if (acc && pos < C.cap)
+                  out[pos] = j;
+               cnt += __popc(m);
+            }
+         }
+      }
+   }
+   if (lane == 0) {
+      nnbr[i] = min(cnt, C.cap);
+      if (cnt > C.cap)
+         atomicMax(over, cnt);
+   }
+}
+
+// small or non-periodic systems: every slot is a candidate
+__global__ void __launch_bounds__(256) k_nbr_all(CellParams C, const float4* __restrict__ spos,
+   const int* __restrict__ sp_start, const int* __restrict__ sp_j, int* __restrict__ nbr, int* __restrict__ nnbr,
+   int* __restrict__ over)
+{
+   const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+   const int lane = threadIdx.x & 31;
+   if (i >= C.npad)
+      return;
+   if (i >= C.n) {
+      if (lane == 0)
+         nnbr[i] = 0;
+      return;
+   }
+   const float4 pi = spos[i];
+   const int pa = sp_start[i], pb = sp_start[i + 1];
+   const unsigned lt = (1u << lane) - 1u;
+   int cnt = 0;
+   int* out = nbr + (size_t)i * C.cap;
+   for (int t = 0; t < C.n; t += 32) {
+      const int j = t + lane;
+      bool acc = false;
+      if (j < C.n && j != i) {
+         float4 pj = spos[j];
+         float dx = image1(pj.x - pi.x, C.lx, C.ilx);
+         float dy = image1(pj.y - pi.y, C.ly, C.ily);
+         float dz = image1(pj.z - pi.z, C.lz, C.ilz);
+         acc = dx * dx + dy * dy + dz * dz <= C.r2 && !is_partner(sp_j, pa, pb, j);
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, acc);
+      const int pos = cnt + __popc(m & lt);
+      if (acc && pos < C.cap)
+         out[pos] = j;
+      cnt += __popc(m);
+   }
+   if (lane == 0) {
+      nnbr[i] = min(cnt, C.cap);
+      if (cnt > C.cap)
+         atomicMax(over, cnt);
+   }
+}
+
+int list_update(Context* ctx)
+{
+   const t9gb_config& cfg = ctx->cfg;
+   const bool pbc = is_pbc(cfg);
+   CellParams C;
+   C.n = ctx->n;
+   C.npad = ctx->npad;
+   C.ncx = ctx->nc[0];
+   C.ncy = ctx->nc[1];
+   C.ncz = ctx->nc[2];
+   C.lx = pbc ? (float)cfg.box[0] : 0.f;
+   C.ly = pbc ? (float)cfg.box[1] : 0.f;
+   C.lz = pbc ? (float)cfg.box[2] : 0.f;
+   C.ilx = pbc ? (float)(1.0 / cfg.box[0]) : 0.f;
+   C.ily = pbc ? (float)(1.0 / cfg.box[1]) : 0.f;
+   C.ilz = pbc ? (float)(1.0 / cfg.box[2]) : 0.f;
+   double r2 = (double)ctx->list_cut * ctx->list_cut;
+   C.r2 = r2 > 3.0e38 ? 3.0e38f : (float)r2;
+   C.cap = ctx->nbr_cap;
+   prof_begin(ctx, P_NBLIST);
+   if (ctx->use_cells) {
+      T9_CUDA(cudaMemsetAsync(ctx->cell_count, 0, sizeof(int) * ctx->ncell, ctx->stream));
+      k_cell_assign<<<grid_for(ctx->n, 256), 256, 0, ctx->stream>>>(C, ctx->spos, ctx->atom_cell, ctx->cell_count);
+      k_cell_scan<<<1, 1024, 0, ctx->stream>>>(ctx->ncell, ctx->cell_count, ctx->cell_start);
+      k_cell_fill<<<grid_for(ctx->n, 256), 256, 0, ctx->stream>>>(ctx->n, ctx->atom_cell, ctx->cell_start,
+         ctx->cell_count, ctx->cell_atoms);
+      k_cell_sort<<<grid_for(ctx->ncell, 128), 128, 0, ctx->stream>>>(ctx->ncell, ctx->cell_start, ctx->cell_atoms);
+      k_nbr_cells<<<grid_for((long long)ctx->npad * 32, 256), 256, 0, ctx->stream>>>(C, ctx->spos, ctx->atom_cell,
+         ctx->cell_start, ctx->cell_atoms, ctx->sp_start, ctx->sp_j, ctx->nbr, ctx->nnbr, ctx->nbr_over);
+   } else {
+      k_nbr_all<<<grid_for((long long)ctx->npad * 32, 256), 256, 0, ctx->stream>>>(C, ctx->spos, ctx->sp_start,
+         ctx->sp_j, ctx->nbr, ctx->nnbr, ctx->nbr_over);
+   }
+   prof_end(ctx);
+   T9_CUDA(cudaGetLastError());
+   ctx->list_stale = false;
+   return T9GB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// positions and permutations
+
+__global__ void k_scatter_pos(int npad, const int* __restrict__ perm, const float* __restrict__ xyz,
+   float4* __restrict__ spos)
+{
+   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < npad; s += gridDim.x * blockDim.x) {
+      int a = perm[s];
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (a >= 0)
+         v = make_float4(xyz[3 * a], xyz[3 * a + 1], xyz[3 * a + 2], 0.f);
+      spos[s] = v;
+   }
+}
+
+int scatter_positions(Context* ctx)
+{
+   k_scatter_pos<<<grid_for(ctx->npad, 256), 256, 0, ctx->stream>>>(ctx->npad, ctx->perm, ctx->xyz, ctx->spos);
+   T9_CUDA(cudaGetLastError());
+   ctx->list_stale = true;
+   return T9GB_OK;
+}
+
+__global__ void k_gather6(int npad, const int* __restrict__ perm, const float* __restrict__ a,
+   const float* __restrict__ b, float* __restrict__ s6)
+{
+   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < npad; s += gridDim.x * blockDim.x) {
+      int at = perm[s];
+      float v[6] = {0, 0, 0, 0, 0, 0};
+      if (at >= 0) {
+         for (int d = 0; d < 3; ++d) {
+            v[d] = a[3 * at + d];
+            v[3 + d] = b ? b[3 * at + d] : 0.f;
+         }
+      }
+      for (int d = 0; d < 6; ++d)
+         s6[6 * s + d] = v[d];
+   }
+}
+
+int gather_to_sorted3(Context* ctx, const float* a, const float* b, float* s6)
+{
+   k_gather6<<<grid_for(ctx->npad, 256), 256, 0, ctx->stream>>>(ctx->npad, ctx->perm, a, b, s6);
+   T9_CUDA(cudaGetLastError());
+   return T9GB_OK;
+}
+
+__global__ void k_scatter6(int npad, const int* __restrict__ perm, const float* __restrict__ s6, float* __restrict__ a,
+   float* __restrict__ b)
+{
+   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < npad; s += gridDim.x * blockDim.x) {
+      int at = perm[s];
+      if (at < 0)
+         continue;
+      for (int d = 0; d < 3; ++d) {
+         if (a)
+            a[3 * at + d] = s6[6 * s + d];
+         if (b)
+            b[3 * at + d] = s6[6 * s + 3 + d];
+      }
+   }
+}
+
+int scatter_from_sorted3(Context* ctx, const float* s6, float* a, float* b)
+{
+   k_scatter6<<<grid_for(ctx->npad, 256), 256, 0, ctx->stream>>>(ctx->npad, ctx->perm, s6, a, b);
+   T9_CUDA(cudaGetLastError());
+   return T9GB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// multipole rotation (include/seq/rotpole.h:7-224), sorted output
+
+__device__ __forceinline__ void norm3(float* a)
+{
+   float r = rsqrtf(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+   a[0] *= r;
+   a[1] *= r;
+   a[2] *= r;
+}
+
+// chirality check (rotpole.h:7-50): flips y-odd components once, in place
+__global__ void k_chkpole(int n, int4* __restrict__ frames, float* __restrict__ pole, const float* __restrict__ xyz)
+{
+   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+      int4 f = frames[i];
+      if (f.w != 2 || f.z == 0)
+         continue;
+      int id = abs(f.z) - 1;
+      const float* pa = xyz + 3 * i;
+      const float* pb = xyz + 3 * f.x;
+      const float* pc = xyz + 3 * f.y;
+      const float* pd = xyz + 3 * id;
+      float xad = pa[0] - pd[0], yad = pa[1] - pd[1], zad = pa[2] - pd[2];
+      float xbd = pb[0] - pd[0], ybd = pb[1] - pd[1], zbd = pb[2] - pd[2];
+      float xcd = pc[0] - pd[0], ycd = pc[1] - pd[1], zcd = pc[2] - pd[2];
+      float c1 = ybd * zcd - zbd * ycd, c2 = ycd * zad - zcd * yad, c3 = yad * zbd - zad * ybd;
+      float vol = xad * c1 + xbd * c2 + xcd * c3;
+      if ((f.z < 0 && vol > 0) || (f.z > 0 && vol < 0)) {
+         frames[i].z = -f.z;
+         pole[10 * i + 2] = -pole[10 * i + 2];
+         pole[10 * i + 7] = -pole[10 * i + 7];
+         pole[10 * i + 9] = -pole[10 * i + 9];
+      }
+   }
+}
+
+__global__ void k_rotpole(int npad, const int* __restrict__ perm, const int4* __restrict__ frames,
+   const float* __restrict__ pole, const float* __restrict__ xyz, float* __restrict__ rpole)
+{
+   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < npad; s += gridDim.x * blockDim.x) {
+      int i = perm[s];
+      float* rp = rpole + 10 * s;
+      if (i < 0) {
+         for (int c = 0; c < 10; ++c)
+            rp[c] = 0.f;
+         continue;
+      }
+      int4 f = frames[i];
+      float a[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+      if (f.w != 0) {
+         float xi = xyz[3 * i], yi = xyz[3 * i + 1], zi = xyz[3 * i + 2];
+         float* xx = a[0];
+         float* yy = a[1];
+         float* zz = a[2];
+         zz[0] = xyz[3 * f.x] - xi;
+         zz[1] = xyz[3 * f.x + 1] - yi;
+         zz[2] = xyz[3 * f.x + 2] - zi;
+         norm3(zz);
+         if (f.w == 1) {
+            bool okay = !(fabsf(zz[0]) > 0.866f);
+            xx[0] = okay ? 1.f : 0.f;
+            xx[1] = okay ? 0.f : 1.f;
+            xx[2] = 0.f;
+         } else {
+            xx[0] = xyz[3 * f.y] - xi;
+            xx[1] = xyz[3 * f.y + 1] - yi;
+            xx[2] = xyz[3 * f.y + 2] - zi;
+            norm3(xx);
+         }
+         if (f.w == 4 || f.w == 5) {
+            int iy = abs(f.z) - 1;
+            yy[0] = xyz[3 * iy] - xi;
+            yy[1] = xyz[3 * iy + 1] - yi;
+            yy[2] = xyz[3 * iy + 2] - zi;
+            norm3(yy);
+         }
+         if (f.w == 3) {
+            for (int d = 0; d < 3; ++d)
+               zz[d] += xx[d];
+            norm3(zz);
+         } else if (f.w == 4) {
+            for (int d = 0; d < 3; ++d)
+               xx[d] += yy[d];
+            norm3(xx);
+         } else if (f.w == 5) {
+            for (int d = 0; d < 3; ++d)
+               zz[d] += xx[d] + yy[d];
+            norm3(zz);
+         }
+         float dot = xx[0] * zz[0] + xx[1] * zz[1] + xx[2] * zz[2];
+         for (int d = 0; d < 3; ++d)
+            xx[d] -= dot * zz[d];
+         norm3(xx);
+         a[1][0] = a[0][2] * a[2][1] - a[0][1] * a[2][2];
+         a[1][1] = a[0][0] * a[2][2] - a[0][2] * a[2][0];
+         a[1][2] = a[0][1] * a[2][0] - a[0][0] * a[2][1];
+      }
+      const float* p = pole + 10 * i;
+      rp[0] = p[0];
+      for (int c = 0; c < 3; ++c)
+         rp[1 + c] = p[1] * a[0][c] + p[2] * a[1][c] + p[3] * a[2][c];
+      float mp[3][3] = {{p[4], p[7], p[8]}, {p[7], p[5], p[9]}, {p[8], p[9], p[6]}};
+      float q[3][3];
+      for (int c = 0; c < 3; ++c)
+         for (int j = 0; j <= c; ++j) {
+            float acc = 0.f;
+            for (int k = 0; k < 3; ++k)
+               for (int m = 0; m < 3; ++m)
+                  acc += a[k][c] * a[m][j] * mp[m][k];
+            q[j][c] = acc;
+         }
+      rp[4] = q[0][0];
+      rp[5] = q[1][1];
+      rp[6] = q[2][2];
+      rp[7] = q[0][1];
+      rp[8] = q[0][2];
+      rp[9] = q[1][2];
+   }
+}
+
+int rotpole_sorted(Context* ctx)
+{
+   k_chkpole<<<grid_for(ctx->n, 256), 256, 0, ctx->stream>>>(ctx->n, ctx->frames, ctx->pole, ctx->xyz);
+   k_rotpole<<<grid_for(ctx->npad, 128), 128, 0, ctx->stream>>>(ctx->npad, ctx->perm, ctx->frames, ctx->pole,
+      ctx->xyz, ctx->srpole);
+   T9_CUDA(cudaGetLastError());
+   return T9GB_OK;
+}
+
+}  // namespace t9gb

@@ -1,0 +1,431 @@
+// Real-space pair kernels over the per-step neighbour list.
+//
+// GROUP (8) consecutive lanes own one atom i: lane g walks the list entries
+// g, g+8, g+16, ... of atom i (consecutive addresses per step), then the
+// scaled partners of i the same way; the eight partial fields are combined
+// with a fixed xor-shuffle tree and written with plain stores.  Every pair is
+// evaluated from both sides (full list), so no atomics are needed and each
+// field component is a sum in a fixed order: results are bit-reproducible.
+// 12,288 atoms give 98,304 threads, enough to fill 152 SMs.
+//
+// Pair arithmetic restates the reference's pair_dfield_v2 / pair_ufield_v2
+// (include/seq/pair_field.h:127-256, :333-420) for the atom-i side, Thole
+// damping damp_thole2/3 (include/seq/damp.h:8-44), the Ewald b_n recursion
+// damp_ewald (include/seq/damp.h:136-151), and the preconditioner pair of
+// sparsePrecond_cu1 (src/cu/amoeba/sparsePrecond_cu1.cc:60-120).  The k side
+// of the reference's pair functions equals the i-side formula evaluated from
+// atom k with the separation reversed, which is what the full list does.
+#include "common.cuh"
+
+namespace t9gb {
+
+struct PairParams {
+   int n;
+   float lx, ly, lz;     // box lengths (0 without PBC)
+   float ilx, ily, ilz;  // inverse lengths (0 without PBC)
+   float cut2;
+   int ewald;
+   float aewald;
+   float ec1, ec2, ec3;  // (2a^2)^j / (sqrt(pi) a), j = 1..3
+   int cap;              // list row stride
+};
+
+__device__ __forceinline__ void thole_damp(float r, float pdi, float pti, float pdk, float ptk, float& s3, float& s5,
+   float& s7)
+{
+   float pgamma = fminf(pti, ptk);
+   float damp = pdi * pdk;
+   float ratio = r * __frcp_rn(damp);
+   damp = (damp == 0.f) ? -1.0e16f : -pgamma * ratio * ratio * ratio;
+   float ex = __expf(damp);
+   s3 = 1.f - ex;
+   s5 = 1.f - ex * (1.f - damp);
+   s7 = 1.f - ex * (1.f - damp + 0.6f * damp * damp);
+}
+
+__device__ __forceinline__ void ewald_bn(const PairParams& P, float r, float invr, float rr2, float& b1, float& b2,
+   float& b3)
+{
+   float ralpha = P.aewald * r;
+   float exp2a = __expf(-ralpha * ralpha);
+   float b0 = erfc_hastings(ralpha, exp2a) * invr;
+   b1 = (b0 + P.ec1 * exp2a) * rr2;
+   b2 = (3.f * b1 + P.ec2 * exp2a) * rr2;
+   b3 = (5.f * b2 + P.ec3 * exp2a) * rr2;
+}
+
+__device__ __forceinline__ float3 sep(const PairParams& P, float4 pi, float4 pk)
+{
+   return make_float3(image1(pk.x - pi.x, P.lx, P.ilx), image1(pk.y - pi.y, P.ly, P.ily),
+      image1(pk.z - pi.z, P.lz, P.ilz));
+}
+
+template <int N>
+__device__ __forceinline__ void group_reduce(float* v)
+{
+#pragma unroll
+   for (int c = 0; c < N; ++c) {
+#pragma unroll
+      for (int o = GROUP / 2; o > 0; o >>= 1)
+         v[c] += __shfl_xor_sync(0xffffffffu, v[c], o);
+   }
+}
+
+__device__ __forceinline__ void load6(const float* __restrict__ a, int s, float* v)
+{
+   const float2* p = reinterpret_cast<const float2*>(a + 6 * s);
+   float2 x = p[0], y = p[1], z = p[2];
+   v[0] = x.x;
+   v[1] = x.y;
+   v[2] = y.x;
+   v[3] = y.y;
+   v[4] = z.x;
+   v[5] = z.y;
+}
+
+__device__ __forceinline__ float pick6(const float* f, int g)
+{
+   float v = f[0];
+#pragma unroll
+   for (int c = 1; c < 6; ++c)
+      if (g == c)
+         v = f[c];
+   return v;
+}
+
+// lanes g < 6 of the group store component g: out = base + f
+__device__ __forceinline__ void store6(float* __restrict__ out, const float* __restrict__ base, int s, int g,
+   const float* f)
+{
+   if (g < 6) {
+      float v = pick6(f, g);
+      if (base)
+         v += base[6 * s + g];
+      out[6 * s + g] = v;
+   }
+}
+
+// ---------------------------------------------------------------------------
+// mutual field -T u, i side (pair_ufield_v2)
+
+__device__ __forceinline__ void ufield_i(const PairParams& P, float r2, float3 d, float uscale, float pdi, float pti,
+   float pdk, float ptk, const float* uk, float* f)
+{
+   float invr = rsqrtf(r2);
+   float r = r2 * invr;
+   float rr2 = invr * invr;
+   float rr3 = invr * rr2;
+   float rr5 = 3.f * rr3 * rr2;
+   float s3, s5, s7;
+   thole_damp(r, pdi, pti, pdk, ptk, s3, s5, s7);
+   float b1, b2;
+   if (P.ewald) {
+      float e1, e2, e3;
+      ewald_bn(P, r, invr, rr2, e1, e2, e3);
+      b1 = e1 - (1.f - uscale * s3) * rr3;
+      b2 = e2 - (1.f - uscale * s5) * rr5;
+   } else {
+      b1 = uscale * s3 * rr3;
+      b2 = uscale * s5 * rr5;
+   }
+   float c = b2 * (d.x * uk[0] + d.y * uk[1] + d.z * uk[2]);
+   f[0] += c * d.x - b1 * uk[0];
+   f[1] += c * d.y - b1 * uk[1];
+   f[2] += c * d.z - b1 * uk[2];
+   c = b2 * (d.x * uk[3] + d.y * uk[4] + d.z * uk[5]);
+   f[3] += c * d.x - b1 * uk[3];
+   f[4] += c * d.y - b1 * uk[4];
+   f[5] += c * d.z - b1 * uk[5];
+}
+
+__global__ void __launch_bounds__(256) k_ufield_real(PairParams P, int npad, const int* __restrict__ nbr,
+   const int* __restrict__ nnbr, const int* __restrict__ sp_start, const int* __restrict__ sp_j,
+   const float4* __restrict__ sp_sc, const float4* __restrict__ spos, const float* __restrict__ u6,
+   const float2* __restrict__ sdamp, const float* __restrict__ base6, float* __restrict__ out6)
+{
+   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+   const int i = tid / GROUP, g = tid % GROUP;
+   if (i >= npad)
+      return;
+   float f[6] = {0, 0, 0, 0, 0, 0};
+   if (i < P.n) {
+      const float4 pi = spos[i];
+      const float2 di = sdamp[i];
+      const int* row = nbr + (size_t)i * P.cap;
+      const int cnt = nnbr[i];
+      for (int k = g; k < cnt; k += GROUP) {
+         const int j = row[k];
+         const float4 pk = spos[j];
+         const float3 d = sep(P, pi, pk);
+         const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
+         if (r2 <= P.cut2) {
+            float uk[6];
+            load6(u6, j, uk);
+            const float2 dk = sdamp[j];
+            ufield_i(P, r2, d, 1.f, di.x, di.y, dk.x, dk.y, uk, f);
+         }
+      }
+      const int pa = sp_start[i], pb = sp_start[i + 1];
+      for (int q = pa + g; q < pb; q += GROUP) {
+         const int j = sp_j[q];
+         const float4 pk = spos[j];
+         const float3 d = sep(P, pi, pk);
+         const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
+         if (r2 <= P.cut2) {
+            float uk[6];
+            load6(u6, j, uk);
+            const float2 dk = sdamp[j];
+            ufield_i(P, r2, d, sp_sc[q].w, di.x, di.y, dk.x, dk.y, uk, f);
+         }
+      }
+   }
+   group_reduce<6>(f);
+   store6(out6, i < P.n ? base6 : nullptr, i, g, f);
+}
+
+// ---------------------------------------------------------------------------
+// permanent field, i side (pair_dfield_v2)
+
+__device__ __forceinline__ void dfield_i(const PairParams& P, float r2, float3 d, float dscale, float pscale,
+   float pdi, float pti, float pdk, float ptk, const float* mk, float* f)
+{
+   float invr = rsqrtf(r2);
+   float r = r2 * invr;
+   float rr2 = invr * invr;
+   float rr3 = invr * rr2;
+   float rr5 = 3.f * rr3 * rr2;
+   float rr7 = 5.f * rr5 * rr2;
+   float s3, s5, s7;
+   thole_damp(r, pdi, pti, pdk, ptk, s3, s5, s7);
+   float e1 = 0.f, e2 = 0.f, e3 = 0.f;
+   if (P.ewald)
+      ewald_bn(P, r, invr, rr2, e1, e2, e3);
+   // mk: c, dx, dy, dz, qxx, qyy, qzz, qxy, qxz, qyz
+   const float dkr = mk[1] * d.x + mk[2] * d.y + mk[3] * d.z;
+   const float qkx = mk[4] * d.x + mk[7] * d.y + mk[8] * d.z;
+   const float qky = mk[7] * d.x + mk[5] * d.y + mk[9] * d.z;
+   const float qkz = mk[8] * d.x + mk[9] * d.y + mk[6] * d.z;
+   const float qkr = qkx * d.x + qky * d.y + qkz * d.z;
+   float b1, b2, b3;
+   if (P.ewald) {
+      b1 = e1 - (1.f - dscale * s3) * rr3;
+      b2 = e2 - (1.f - dscale * s5) * rr5;
+      b3 = e3 - (1.f - dscale * s7) * rr7;
+   } else {
+      b1 = dscale * s3 * rr3;
+      b2 = dscale * s5 * rr5;
+      b3 = dscale * s7 * rr7;
+   }
+   float c1 = -(b1 * mk[0] - b2 * dkr + b3 * qkr);
+   float fx = c1 * d.x - b1 * mk[1] + 2.f * b2 * qkx;
+   float fy = c1 * d.y - b1 * mk[2] + 2.f * b2 * qky;
+   float fz = c1 * d.z - b1 * mk[3] + 2.f * b2 * qkz;
+   f[0] += fx;
+   f[1] += fy;
+   f[2] += fz;
+   if (pscale != dscale) {
+      if (P.ewald) {
+         b1 = e1 - (1.f - pscale * s3) * rr3;
+         b2 = e2 - (1.f - pscale * s5) * rr5;
+         b3 = e3 - (1.f - pscale * s7) * rr7;
+      } else {
+         b1 = pscale * s3 * rr3;
+         b2 = pscale * s5 * rr5;
+         b3 = pscale * s7 * rr7;
+      }
+      c1 = -(b1 * mk[0] - b2 * dkr + b3 * qkr);
+      fx = c1 * d.x - b1 * mk[1] + 2.f * b2 * qkx;
+      fy = c1 * d.y - b1 * mk[2] + 2.f * b2 * qky;
+      fz = c1 * d.z - b1 * mk[3] + 2.f * b2 * qkz;
+   }
+   f[3] += fx;
+   f[4] += fy;
+   f[5] += fz;
+}
+
+__device__ __forceinline__ void load10(const float* __restrict__ rp, int s, float* m)
+{
+   const float2* p = reinterpret_cast<const float2*>(rp + 10 * s);
+#pragma unroll
+   for (int c = 0; c < 5; ++c) {
+      float2 v = p[c];
+      m[2 * c] = v.x;
+      m[2 * c + 1] = v.y;
+   }
+}
+
+__global__ void __launch_bounds__(256) k_dfield_real(PairParams P, int npad, const int* __restrict__ nbr,
+   const int* __restrict__ nnbr, const int* __restrict__ sp_start, const int* __restrict__ sp_j,
+   const float4* __restrict__ sp_sc, const float4* __restrict__ spos, const float* __restrict__ rp,
+   const float2* __restrict__ sdamp, const float* __restrict__ base6, float* __restrict__ out6)
+{
+   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+   const int i = tid / GROUP, g = tid % GROUP;
+   if (i >= npad)
+      return;
+   float f[6] = {0, 0, 0, 0, 0, 0};
+   if (i < P.n) {
+      const float4 pi = spos[i];
+      const float2 di = sdamp[i];
+      const int* row = nbr + (size_t)i * P.cap;
+      const int cnt = nnbr[i];
+      for (int k = g; k < cnt; k += GROUP) {
+         const int j = row[k];
+         const float4 pk = spos[j];
+         const float3 d = sep(P, pi, pk);
+         const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
+         if (r2 <= P.cut2) {
+            float mk[10];
+            load10(rp, j, mk);
+            const float2 dk = sdamp[j];
+            dfield_i(P, r2, d, 1.f, 1.f, di.x, di.y, dk.x, dk.y, mk, f);
+         }
+      }
+      const int pa = sp_start[i], pb = sp_start[i + 1];
+      for (int q = pa + g; q < pb; q += GROUP) {
+         const int j = sp_j[q];
+         const float4 pk = spos[j];
+         const float3 d = sep(P, pi, pk);
+         const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
+         if (r2 <= P.cut2) {
+            float mk[10];
+            load10(rp, j, mk);
+            const float2 dk = sdamp[j];
+            const float4 sc = sp_sc[q];
+            dfield_i(P, r2, d, sc.y, sc.z, di.x, di.y, dk.x, dk.y, mk, f);
+         }
+      }
+   }
+   group_reduce<6>(f);
+   store6(out6, i < P.n ? base6 : nullptr, i, g, f);
+}
+
+// ---------------------------------------------------------------------------
+// sparse preconditioner: z_i = udiag alpha_i r_i + sum_k alpha_i alpha_k T_ik r_k
+
+__global__ void __launch_bounds__(256) k_precond_sparse(PairParams P, int npad, float udiag,
+   const int* __restrict__ nbr, const int* __restrict__ nnbr, const int* __restrict__ sp_start,
+   const int* __restrict__ sp_j, const float4* __restrict__ sp_sc, const float4* __restrict__ spos,
+   const float* __restrict__ r6, const float2* __restrict__ sdamp, const float* __restrict__ spolar,
+   float* __restrict__ z6)
+{
+   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+   const int i = tid / GROUP, g = tid % GROUP;
+   if (i >= npad)
+      return;
+   float f[6] = {0, 0, 0, 0, 0, 0};
+   const float poli = spolar[i];
+   if (i < P.n) {
+      const float4 pi = spos[i];
+      const float2 di = sdamp[i];
+      const int* row = nbr + (size_t)i * P.cap;
+      const int cnt = nnbr[i];
+      const int pa = sp_start[i], pb = sp_start[i + 1];
+      const int tot = cnt + (pb - pa);
+      for (int k = g; k < tot; k += GROUP) {
+         int j;
+         float us = 1.f;
+         if (k < cnt) {
+            j = row[k];
+         } else {
+            j = sp_j[pa + k - cnt];
+            us = sp_sc[pa + k - cnt].w;
+         }
+         const float4 pk = spos[j];
+         const float3 d = sep(P, pi, pk);
+         const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
+         if (r2 <= P.cut2) {
+            float rk[6];
+            load6(r6, j, rk);
+            const float2 dk = sdamp[j];
+            float invr = rsqrtf(r2);
+            float r = r2 * invr;
+            float s3, s5, s7;
+            thole_damp(r, di.x, di.y, dk.x, dk.y, s3, s5, s7);
+            const float polik = poli * spolar[j];
+            const float rr3 = us * s3 * polik * invr * invr * invr;
+            const float rr5 = 3.f * us * s5 * polik * invr * invr * invr * invr * invr;
+            float c = rr5 * (d.x * rk[0] + d.y * rk[1] + d.z * rk[2]);
+            f[0] += c * d.x - rr3 * rk[0];
+            f[1] += c * d.y - rr3 * rk[1];
+            f[2] += c * d.z - rr3 * rk[2];
+            c = rr5 * (d.x * rk[3] + d.y * rk[4] + d.z * rk[5]);
+            f[3] += c * d.x - rr3 * rk[3];
+            f[4] += c * d.y - rr3 * rk[4];
+            f[5] += c * d.z - rr3 * rk[5];
+         }
+      }
+   }
+   group_reduce<6>(f);
+   if (g < 6)
+      z6[6 * i + g] = udiag * poli * r6[6 * i + g] + pick6(f, g);
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+
+static PairParams make_params(const Context* ctx, double cutoff)
+{
+   PairParams P;
+   const t9gb_config& c = ctx->cfg;
+   const bool pbc = c.box[0] > 0 && c.box[1] > 0 && c.box[2] > 0;
+   P.n = ctx->n;
+   P.lx = pbc ? (float)c.box[0] : 0.f;
+   P.ly = pbc ? (float)c.box[1] : 0.f;
+   P.lz = pbc ? (float)c.box[2] : 0.f;
+   P.ilx = pbc ? (float)(1.0 / c.box[0]) : 0.f;
+   P.ily = pbc ? (float)(1.0 / c.box[1]) : 0.f;
+   P.ilz = pbc ? (float)(1.0 / c.box[2]) : 0.f;
+   double cut2 = cutoff * cutoff;
+   P.cut2 = cut2 > 3.0e38 ? 3.0e38f : (float)cut2;
+   P.ewald = c.use_ewald;
+   P.aewald = (float)c.aewald;
+   const double a = c.aewald;
+   const double alsq2 = 2 * a * a;
+   const double base = a > 0 ? 1.0 / (1.77245385090551602730 * a) : 0.0;
+   P.ec1 = (float)(base * alsq2);
+   P.ec2 = (float)(base * alsq2 * alsq2);
+   P.ec3 = (float)(base * alsq2 * alsq2 * alsq2);
+   P.cap = ctx->nbr_cap;
+   return P;
+}
+
+static constexpr int PAIR_THREADS = 256;
+
+int launch_ufield_real(Context* ctx, const float* u6, const float* base6, float* out6)
+{
+   PairParams P = make_params(ctx, ctx->cfg.cutoff);
+   prof_begin(ctx, P_UFIELD_REAL);
+   k_ufield_real<<<grid_for((long long)ctx->npad * GROUP, PAIR_THREADS), PAIR_THREADS, 0, ctx->stream>>>(P,
+      ctx->npad, ctx->nbr, ctx->nnbr, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos, u6, ctx->sdamp, base6, out6);
+   prof_end(ctx);
+   T9_CUDA(cudaGetLastError());
+   return T9GB_OK;
+}
+
+int launch_dfield_real(Context* ctx, const float* base6, float* out6)
+{
+   PairParams P = make_params(ctx, ctx->cfg.cutoff);
+   prof_begin(ctx, P_DFIELD_REAL);
+   k_dfield_real<<<grid_for((long long)ctx->npad * GROUP, PAIR_THREADS), PAIR_THREADS, 0, ctx->stream>>>(P,
+      ctx->npad, ctx->nbr, ctx->nnbr, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos, ctx->srpole, ctx->sdamp, base6,
+      out6);
+   prof_end(ctx);
+   T9_CUDA(cudaGetLastError());
+   return T9GB_OK;
+}
+
+int launch_precond_sparse(Context* ctx, const float* r6, float* z6)
+{
+   PairParams P = make_params(ctx, ctx->cfg.usolve_cutoff + ctx->cfg.pbuffer);
+   P.ewald = 0;
+   prof_begin(ctx, P_PRECOND);
+   k_precond_sparse<<<grid_for((long long)ctx->npad * GROUP, PAIR_THREADS), PAIR_THREADS, 0, ctx->stream>>>(P,
+      ctx->npad, (float)ctx->cfg.udiag, ctx->nbr, ctx->nnbr, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos, r6,
+      ctx->sdamp, ctx->spolar, z6);
+   prof_end(ctx);
+   T9_CUDA(cudaGetLastError());
+   return T9GB_OK;
+}
+
+}  // namespace t9gb

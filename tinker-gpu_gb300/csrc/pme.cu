@@ -1,0 +1,503 @@
+// PME reciprocal-space field for AMOEBA: B-spline spreading of fractional
+// multipoles or induced dipoles, convolution with the Ewald influence
+// function, and the gather of potential derivatives fused with the
+// reciprocal-self field terms.
+//
+// Reference pieces replaced (src/cu/pme.cu): gridPut_cu1<MPOLE> :14-183,
+// gridPut_cu2<UIND> :185-255, fphiGet_cu<MPOLE/UIND2> :383-870, pmeConv_cu1
+// :908-1031, cmpToFmp/cuindToFuind/fphiToCphi :1052-1300, and the recip-self
+// kernels dfieldEwaldRecipSelfP2_cu1 / ufieldEwaldRecipSelfP1_cu1
+// (src/cu/amoeba/field.cu:12-33, :71-118).
+//
+// Differences by design (same results up to rounding):
+//  - the fractional transforms are folded into spread and gather (orthogonal
+//    boxes: the transforms are diagonal);
+//  - dfield and ufield only consume first derivatives of the potential, so the
+//    gather evaluates 3 (MPOLE) or 6 (UIND) sums instead of 20 / 20;
+//  - the influence function exp(-pi^2 h^2/a^2)/(pi V h^2 |b|^2) is tabulated
+//    once per box (the reference recomputes it in every pmeConv call);
+//  - the grid accumulates in 64-bit fixed point (order-independent), then one
+//    pass converts it to the complex float grid and clears the fixed grid.
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+
+namespace t9gb {
+
+// ---------------------------------------------------------------------------
+// B-spline moduli |b(m)|^2 (Essmann et al., J. Chem. Phys. 103, 8577 (1995))
+// with Tinker's optimal-zeta correction of Euler-spline zeros.
+
+static void cardinal_bspline_knots(int order, double* c)
+{
+   const double x = 0;
+   c[0] = 1 - x;
+   c[1] = x;
+   for (int k = 3; k <= order; ++k) {
+      double denom = 1.0 / (k - 1);
+      c[k - 1] = x * c[k - 2] * denom;
+      for (int i = 1; i <= k - 2; ++i)
+         c[k - i - 1] = ((x + i) * c[k - i - 2] + (k - i - x) * c[k - i - 1]) * denom;
+      c[0] = (1 - x) * c[0] * denom;
+   }
+}
+
+static void bspline_moduli(int nfft, int order, std::vector<double>& mod)
+{
+   const double pi = 3.14159265358979323846;
+   std::vector<double> arr(nfft + order + 2, 0.0);
+   double c[16];
+   cardinal_bspline_knots(order, c);
+   for (int i = 0; i < order; ++i)
+      arr[i + 1] = c[i];
+   mod.assign(nfft, 0.0);
+   for (int i = 0; i < nfft; ++i) {
+      double s1 = 0, s2 = 0;
+      for (int j = 0; j < nfft; ++j) {
+         double arg = 2 * pi * (double)i * (double)j / nfft;
+         s1 += arr[j] * std::cos(arg);
+         s2 += arr[j] * std::sin(arg);
+      }
+      mod[i] = s1 * s1 + s2 * s2;
+   }
+   const double eps = 1.0e-7;
+   if (mod[0] < eps)
+      mod[0] = 0.5 * mod[1];
+   for (int i = 1; i < nfft - 1; ++i)
+      if (mod[i] < eps)
+         mod[i] = 0.5 * (mod[i - 1] + mod[i + 1]);
+   if (mod[nfft - 1] < eps)
+      mod[nfft - 1] = 0.5 * mod[nfft - 2];
+   for (int i = 0; i < nfft; ++i) {
+      int k = (i + 1 > nfft / 2) ? i - nfft : i;
+      double zeta = 1;
+      if (k != 0) {
+         double s1 = 1, s2 = 1, f = pi * k / nfft;
+         for (int j = 1; j <= 50; ++j) {
+            double a1 = f / (f + pi * j), a2 = f / (f - pi * j);
+            s1 += std::pow(a1, order) + std::pow(a2, order);
+            s2 += std::pow(a1, 2 * order) + std::pow(a2, 2 * order);
+         }
+         zeta = s2 / s1;
+      }
+      mod[i] *= zeta * zeta;
+   }
+}
+
+// ---------------------------------------------------------------------------
+// per-site B-spline weights (include/seq/bsplgen.h:27-116), order 5
+
+template <int LEVEL>
+__device__ __forceinline__ void bspline5(float w, float th[5][LEVEL])
+{
+   float b[6][6];  // b[order][i], 1-based
+   b[2][2] = w;
+   b[2][1] = 1.f - w;
+   b[3][3] = 0.5f * w * b[2][2];
+   b[3][2] = 0.5f * ((1.f + w) * b[2][1] + (2.f - w) * b[2][2]);
+   b[3][1] = 0.5f * (1.f - w) * b[2][1];
+#pragma unroll
+   for (int i = 4; i <= 5; ++i) {
+      const int k = i - 1;
+      const float denom = 1.f / k;
+      b[i][i] = denom * w * b[k][k];
+#pragma unroll
+      for (int j = 1; j <= i - 2; ++j)
+         b[i][i - j] = denom * ((w + j) * b[k][i - j - 1] + (i - j - w) * b[k][i - j]);
+      b[i][1] = denom * (1.f - w) * b[k][1];
+   }
+   // derivative rows by repeated differencing of the lower-order rows
+#pragma unroll
+   for (int lv = 2; lv <= LEVEL; ++lv) {
+      const int k = 5 - lv + 1;
+#pragma unroll
+      for (int pass = 0; pass < lv - 1; ++pass) {
+         const int top = 5 - (lv - 2) + pass;
+         b[k][top] = b[k][top - 1];
+#pragma unroll
+         for (int i = top - 1; i >= 2; --i)
+            b[k][i] = b[k][i - 1] - b[k][i];
+         b[k][1] = -b[k][1];
+      }
+   }
+#pragma unroll
+   for (int i = 1; i <= 5; ++i)
+#pragma unroll
+      for (int j = 1; j <= LEVEL; ++j)
+         th[i - 1][j - 1] = b[5 - j + 1][i];
+}
+
+struct GridParams {
+   int n1, n2, n3;
+   float r1, r2, r3;  // 1/box
+   float a1, a2, a3;  // nfft / box
+   float selfterm;    // 4 a^3 / (3 sqrt(pi))
+};
+
+__device__ __forceinline__ void site(const GridParams& G, float4 p, int& i1, int& i2, int& i3, float& w1, float& w2,
+   float& w3)
+{
+   float w = p.x * G.r1;
+   w = w + 0.5f - floorf(w + 0.5f);
+   float fr = G.n1 * w;
+   i1 = (int)floorf(fr);
+   w1 = fr - i1;
+   w = p.y * G.r2;
+   w = w + 0.5f - floorf(w + 0.5f);
+   fr = G.n2 * w;
+   i2 = (int)floorf(fr);
+   w2 = fr - i2;
+   w = p.z * G.r3;
+   w = w + 0.5f - floorf(w + 0.5f);
+   fr = G.n3 * w;
+   i3 = (int)floorf(fr);
+   w3 = fr - i3;
+   i1 -= BSORDER - 1;
+   i2 -= BSORDER - 1;
+   i3 -= BSORDER - 1;
+   i1 += (i1 < 0 ? G.n1 : 0);
+   i2 += (i2 < 0 ? G.n2 : 0);
+   i3 += (i3 < 0 ? G.n3 : 0);
+}
+
+__device__ __forceinline__ void grid_add(unsigned long long* q, size_t idx, float v)
+{
+   if (v != 0.f)
+      atomicAdd(q + idx, (unsigned long long)to_fx(v));
+}
+
+// spread fractional multipoles (real part)
+__global__ void k_spread_mpole(int n, GridParams G, const float4* __restrict__ spos, const float* __restrict__ rp,
+   unsigned long long* __restrict__ q)
+{
+   int s = blockIdx.x * blockDim.x + threadIdx.x;
+   if (s >= n)
+      return;
+   int i1, i2, i3;
+   float w1, w2, w3;
+   site(G, spos[s], i1, i2, i3, w1, w2, w3);
+   float t1[5][3], t2[5][3], t3[5][3];
+   bspline5<3>(w1, t1);
+   bspline5<3>(w2, t2);
+   bspline5<3>(w3, t3);
+   const float* m = rp + 10 * s;
+   // Cartesian -> fractional (orthogonal box; quadrupole off-diagonals doubled)
+   const float f0 = m[0];
+   const float fx = G.a1 * m[1], fy = G.a2 * m[2], fz = G.a3 * m[3];
+   const float fxx = G.a1 * G.a1 * m[4], fyy = G.a2 * G.a2 * m[5], fzz = G.a3 * G.a3 * m[6];
+   const float fxy = 2.f * G.a1 * G.a2 * m[7], fxz = 2.f * G.a1 * G.a3 * m[8], fyz = 2.f * G.a2 * G.a3 * m[9];
+   const int nxy = G.n1 * G.n2;
+#pragma unroll
+   for (int kz = 0; kz < 5; ++kz) {
+      int zb = i3 + kz;
+      zb -= (zb >= G.n3 ? G.n3 : 0);
+      const float v0 = t3[kz][0], v1 = t3[kz][1], v2 = t3[kz][2];
+#pragma unroll
+      for (int jy = 0; jy < 5; ++jy) {
+         int yb = i2 + jy;
+         yb -= (yb >= G.n2 ? G.n2 : 0);
+         const float u0 = t2[jy][0], u1 = t2[jy][1], u2 = t2[jy][2];
+         const float term0 = f0 * u0 * v0 + fy * u1 * v0 + fz * u0 * v1 + fyy * u2 * v0 + fzz * u0 * v2
+            + fyz * u1 * v1;
+         const float term1 = fx * u0 * v0 + fxy * u1 * v0 + fxz * u0 * v1;
+         const float term2 = fxx * u0 * v0;
+         const size_t row = (size_t)zb * nxy + (size_t)yb * G.n1;
+#pragma unroll
+         for (int ix = 0; ix < 5; ++ix) {
+            int xb = i1 + ix;
+            xb -= (xb >= G.n1 ? G.n1 : 0);
+            grid_add(q, 2 * (row + xb), term0 * t1[ix][0] + term1 * t1[ix][1] + term2 * t1[ix][2]);
+         }
+      }
+   }
+}
+
+// spread fractional induced dipoles: d -> real part, p -> imaginary part
+__global__ void k_spread_uind(int n, GridParams G, const float4* __restrict__ spos, const float* __restrict__ u6,
+   unsigned long long* __restrict__ q)
+{
+   int s = blockIdx.x * blockDim.x + threadIdx.x;
+   if (s >= n)
+      return;
+   int i1, i2, i3;
+   float w1, w2, w3;
+   site(G, spos[s], i1, i2, i3, w1, w2, w3);
+   float t1[5][2], t2[5][2], t3[5][2];
+   bspline5<2>(w1, t1);
+   bspline5<2>(w2, t2);
+   bspline5<2>(w3, t3);
+   const float* u = u6 + 6 * s;
+   const float dx = G.a1 * u[0], dy = G.a2 * u[1], dz = G.a3 * u[2];
+   const float px = G.a1 * u[3], py = G.a2 * u[4], pz = G.a3 * u[5];
+   const int nxy = G.n1 * G.n2;
+#pragma unroll
+   for (int kz = 0; kz < 5; ++kz) {
+      int zb = i3 + kz;
+      zb -= (zb >= G.n3 ? G.n3 : 0);
+      const float v0 = t3[kz][0], v1 = t3[kz][1];
+#pragma unroll
+      for (int jy = 0; jy < 5; ++jy) {
+         int yb = i2 + jy;
+         yb -= (yb >= G.n2 ? G.n2 : 0);
+         const float u0 = t2[jy][0], u1 = t2[jy][1];
+         const float d01 = dy * u1 * v0 + dz * u0 * v1, d11 = dx * u0 * v0;
+         const float p01 = py * u1 * v0 + pz * u0 * v1, p11 = px * u0 * v0;
+         const size_t row = (size_t)zb * nxy + (size_t)yb * G.n1;
+#pragma unroll
+         for (int ix = 0; ix < 5; ++ix) {
+            int xb = i1 + ix;
+            xb -= (xb >= G.n1 ? G.n1 : 0);
+            grid_add(q, 2 * (row + xb), d01 * t1[ix][0] + d11 * t1[ix][1]);
+            grid_add(q, 2 * (row + xb) + 1, p01 * t1[ix][0] + p11 * t1[ix][1]);
+         }
+      }
+   }
+}
+
+// fixed -> complex float, clearing the fixed grid for the next spread
+__global__ void k_fx_to_grid(size_t ng, long long* __restrict__ q, float2* __restrict__ g)
+{
+   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < ng; i += (size_t)gridDim.x * blockDim.x) {
+      longlong2 v = reinterpret_cast<longlong2*>(q)[i];
+      g[i] = make_float2(from_fx(v.x), from_fx(v.y));
+      reinterpret_cast<longlong2*>(q)[i] = make_longlong2(0, 0);
+   }
+}
+
+// reciprocal convolution with the tabulated influence function
+__global__ void k_conv(size_t ng, const float* __restrict__ infl, float2* __restrict__ g)
+{
+   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < ng; i += (size_t)gridDim.x * blockDim.x) {
+      float2 v = g[i];
+      float f = infl[i];
+      g[i] = make_float2(v.x * f, v.y * f);
+   }
+}
+
+// gather first derivatives and store the recip + self field (plain store).
+// MODE 0 (multipoles): real part -> d and p field, self term with the
+// permanent dipole.  MODE 1 (dipoles): real -> d, imaginary -> p, self term
+// with the induced dipoles u6.
+template <int MODE>
+__global__ void k_gather_field(int n, GridParams G, const float4* __restrict__ spos, const float2* __restrict__ g,
+   const float* __restrict__ rp, const float* __restrict__ u6, float* __restrict__ out6)
+{
+   int s = blockIdx.x * blockDim.x + threadIdx.x;
+   if (s >= n)
+      return;
+   int i1, i2, i3;
+   float w1, w2, w3;
+   site(G, spos[s], i1, i2, i3, w1, w2, w3);
+   float t1[5][2], t2[5][2], t3[5][2];
+   bspline5<2>(w1, t1);
+   bspline5<2>(w2, t2);
+   bspline5<2>(w3, t3);
+   float r100 = 0.f, r010 = 0.f, r001 = 0.f, i100 = 0.f, i010 = 0.f, i001 = 0.f;
+   const int nxy = G.n1 * G.n2;
+#pragma unroll
+   for (int kz = 0; kz < 5; ++kz) {
+      int zb = i3 + kz;
+      zb -= (zb >= G.n3 ? G.n3 : 0);
+      const float v0 = t3[kz][0], v1 = t3[kz][1];
+      float ru00 = 0.f, ru10 = 0.f, ru01 = 0.f, iu00 = 0.f, iu10 = 0.f, iu01 = 0.f;
+#pragma unroll
+      for (int jy = 0; jy < 5; ++jy) {
+         int yb = i2 + jy;
+         yb -= (yb >= G.n2 ? G.n2 : 0);
+         const float u0 = t2[jy][0], u1 = t2[jy][1];
+         const size_t row = (size_t)zb * nxy + (size_t)yb * G.n1;
+         float rt0 = 0.f, rt1 = 0.f, it0 = 0.f, it1 = 0.f;
+#pragma unroll
+         for (int ix = 0; ix < 5; ++ix) {
+            int xb = i1 + ix;
+            xb -= (xb >= G.n1 ? G.n1 : 0);
+            float2 q = g[row + xb];
+            rt0 += q.x * t1[ix][0];
+            rt1 += q.x * t1[ix][1];
+            if (MODE == 1) {
+               it0 += q.y * t1[ix][0];
+               it1 += q.y * t1[ix][1];
+            }
+         }
+         ru00 += rt0 * u0;
+         ru10 += rt1 * u0;
+         ru01 += rt0 * u1;
+         if (MODE == 1) {
+            iu00 += it0 * u0;
+            iu10 += it1 * u0;
+            iu01 += it0 * u1;
+         }
+      }
+      r100 += ru10 * v0;
+      r010 += ru01 * v0;
+      r001 += ru00 * v1;
+      if (MODE == 1) {
+         i100 += iu10 * v0;
+         i010 += iu01 * v0;
+         i001 += iu00 * v1;
+      }
+   }
+   float* a = out6 + 6 * s;
+   if (MODE == 0) {
+      const float* m = rp + 10 * s;
+      const float fx = -G.a1 * r100 + G.selfterm * m[1];
+      const float fy = -G.a2 * r010 + G.selfterm * m[2];
+      const float fz = -G.a3 * r001 + G.selfterm * m[3];
+      a[0] = fx;
+      a[1] = fy;
+      a[2] = fz;
+      a[3] = fx;
+      a[4] = fy;
+      a[5] = fz;
+   } else {
+      const float* u = u6 + 6 * s;
+      a[0] = G.selfterm * u[0] - G.a1 * r100;
+      a[1] = G.selfterm * u[1] - G.a2 * r010;
+      a[2] = G.selfterm * u[2] - G.a3 * r001;
+      a[3] = G.selfterm * u[3] - G.a1 * i100;
+      a[4] = G.selfterm * u[4] - G.a2 * i010;
+      a[5] = G.selfterm * u[5] - G.a3 * i001;
+   }
+}
+
+// ---------------------------------------------------------------------------
+
+int pme_setup(Context* ctx)
+{
+   const t9gb_config& c = ctx->cfg;
+   PmeGrid& P = ctx->pme;
+   if (!c.use_ewald)
+      return T9GB_OK;
+   P.n1 = c.nfft[0];
+   P.n2 = c.nfft[1];
+   P.n3 = c.nfft[2];
+   const size_t ng = (size_t)P.n1 * P.n2 * P.n3;
+   T9_CUDA(cudaMalloc(&P.qgrid, sizeof(float2) * ng));
+   T9_CUDA(cudaMalloc(&P.qfx, sizeof(long long) * 2 * ng));
+   T9_CUDA(cudaMemset(P.qfx, 0, sizeof(long long) * 2 * ng));
+   // influence function in double precision, stored as float
+   std::vector<double> m1, m2, m3;
+   bspline_moduli(P.n1, c.bsorder, m1);
+   bspline_moduli(P.n2, c.bsorder, m2);
+   bspline_moduli(P.n3, c.bsorder, m3);
+   const double pi = 3.14159265358979323846;
+   const double pterm = (pi / c.aewald) * (pi / c.aewald);
+   const double vol = c.box[0] * c.box[1] * c.box[2];
+   std::vector<float> infl(ng);
+   for (int k3 = 0; k3 < P.n3; ++k3)
+      for (int k2 = 0; k2 < P.n2; ++k2)
+         for (int k1 = 0; k1 < P.n1; ++k1) {
+            size_t i = ((size_t)k3 * P.n2 + k2) * P.n1 + k1;
+            int r1 = (k1 < (P.n1 + 1) / 2) ? k1 : k1 - P.n1;
+            int r2 = (k2 < (P.n2 + 1) / 2) ? k2 : k2 - P.n2;
+            int r3 = (k3 < (P.n3 + 1) / 2) ? k3 : k3 - P.n3;
+            double h1 = r1 / c.box[0], h2 = r2 / c.box[1], h3 = r3 / c.box[2];
+            double hsq = h1 * h1 + h2 * h2 + h3 * h3;
+            double term = -pterm * hsq;
+            double e = 0;
+            if (i != 0 && term > -50)
+               e = std::exp(term) / (hsq * pi * vol * m1[k1] * m2[k2] * m3[k3]);
+            infl[i] = (float)e;
+         }
+   float* d_infl = nullptr;
+   T9_CUDA(cudaMalloc(&d_infl, sizeof(float) * ng));
+   T9_CUDA(cudaMemcpy(d_infl, infl.data(), sizeof(float) * ng, cudaMemcpyHostToDevice));
+   P.infl = d_infl;
+   if (cufftPlan3d(&P.plan, P.n3, P.n2, P.n1, CUFFT_C2C) != CUFFT_SUCCESS) {
+      ctx->last_error = "cufftPlan3d failed";
+      return T9GB_CUDA_ERR;
+   }
+   return T9GB_OK;
+}
+
+void pme_free(Context* ctx)
+{
+   PmeGrid& P = ctx->pme;
+   if (P.plan)
+      cufftDestroy(P.plan);
+   cudaFree(P.qgrid);
+   cudaFree(P.qfx);
+   cudaFree(P.infl);
+   P = PmeGrid();
+}
+
+static GridParams grid_params(const Context* ctx)
+{
+   const t9gb_config& c = ctx->cfg;
+   GridParams G;
+   G.n1 = c.nfft[0];
+   G.n2 = c.nfft[1];
+   G.n3 = c.nfft[2];
+   G.r1 = (float)(1.0 / c.box[0]);
+   G.r2 = (float)(1.0 / c.box[1]);
+   G.r3 = (float)(1.0 / c.box[2]);
+   G.a1 = (float)(c.nfft[0] / c.box[0]);
+   G.a2 = (float)(c.nfft[1] / c.box[1]);
+   G.a3 = (float)(c.nfft[2] / c.box[2]);
+   G.selfterm = (float)(4.0 * c.aewald * c.aewald * c.aewald / (3.0 * 1.77245385090551602730));
+   return G;
+}
+
+static int fft_conv(Context* ctx)
+{
+   PmeGrid& P = ctx->pme;
+   const size_t ng = (size_t)P.n1 * P.n2 * P.n3;
+   const int cb = (int)std::min<size_t>((ng + 255) / 256, 152 * 16);
+   prof_begin(ctx, P_FFT_CONV);
+   k_fx_to_grid<<<cb, 256, 0, ctx->stream>>>(ng, P.qfx, P.qgrid);
+   T9_CUDA(cudaGetLastError());
+   cufftSetStream(P.plan, ctx->stream);
+   if (cufftExecC2C(P.plan, (cufftComplex*)P.qgrid, (cufftComplex*)P.qgrid, CUFFT_FORWARD) != CUFFT_SUCCESS) {
+      ctx->last_error = "cufftExecC2C forward failed";
+      return T9GB_CUDA_ERR;
+   }
+   k_conv<<<cb, 256, 0, ctx->stream>>>(ng, P.infl, P.qgrid);
+   T9_CUDA(cudaGetLastError());
+   if (cufftExecC2C(P.plan, (cufftComplex*)P.qgrid, (cufftComplex*)P.qgrid, CUFFT_INVERSE) != CUFFT_SUCCESS) {
+      ctx->last_error = "cufftExecC2C inverse failed";
+      return T9GB_CUDA_ERR;
+   }
+   prof_end(ctx);
+   return T9GB_OK;
+}
+
+int launch_dfield_recip(Context* ctx, float* out6)
+{
+   if (!ctx->cfg.use_ewald)
+      return T9GB_OK;
+   GridParams G = grid_params(ctx);
+   prof_begin(ctx, P_SPREAD_MPOLE);
+   k_spread_mpole<<<grid_for(ctx->n, 128), 128, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->srpole,
+      reinterpret_cast<unsigned long long*>(ctx->pme.qfx));
+   prof_end(ctx);
+   T9_CUDA(cudaGetLastError());
+   T9_CHECK(fft_conv(ctx));
+   prof_begin(ctx, P_GATHER_MPOLE);
+   k_gather_field<0><<<grid_for(ctx->n, 128), 128, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->pme.qgrid,
+      ctx->srpole, nullptr, out6);
+   prof_end(ctx);
+   T9_CUDA(cudaGetLastError());
+   return T9GB_OK;
+}
+
+int launch_ufield_recip(Context* ctx, const float* u6, float* out6)
+{
+   if (!ctx->cfg.use_ewald)
+      return T9GB_OK;
+   GridParams G = grid_params(ctx);
+   prof_begin(ctx, P_SPREAD_UIND);
+   k_spread_uind<<<grid_for(ctx->n, 128), 128, 0, ctx->stream>>>(ctx->n, G, ctx->spos, u6,
+      reinterpret_cast<unsigned long long*>(ctx->pme.qfx));
+   prof_end(ctx);
+   T9_CUDA(cudaGetLastError());
+   T9_CHECK(fft_conv(ctx));
+   prof_begin(ctx, P_GATHER_UIND);
+   k_gather_field<1><<<grid_for(ctx->n, 128), 128, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->pme.qgrid, nullptr,
+      u6, out6);
+   prof_end(ctx);
+   T9_CUDA(cudaGetLastError());
+   return T9GB_OK;
+}
+
+}  // namespace t9gb
