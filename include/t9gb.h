@@ -130,6 +130,13 @@ int t9gb_induce_stats(const t9gb_context* ctx, int* iterations, double* eps_deby
 /* Direct dipoles alpha*E of the last induce/dfield, [n][3] device. */
 int t9gb_get_udir(t9gb_context* ctx, float* udir_device, float* udirp_device);
 
+/* Run induce() as one CUDA graph (default, enable = 1: neighbour list,
+ * permanent field, guess and the PCG loop as a conditional WHILE node with
+ * the convergence test on the device) or as individually launched kernels
+ * with one host synchronisation per iteration (enable = 0, the reference's
+ * pattern, pcg.cu:144-145).  Both give bit-identical dipoles. */
+int t9gb_use_graph(t9gb_context* ctx, int enable);
+
 /* Neighbour-list sizes: row capacity, entries of the current list (both
  * directions) and scaled pairs (the reference's Spatial::nakpl/niak,
  * include/ff/spatial.h:15-140). */

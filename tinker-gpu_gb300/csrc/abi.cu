@@ -80,6 +80,12 @@ static void free_all(Context* ctx)
    if (ctx->h_over)
       cudaFreeHost(ctx->h_over);
    pme_free(ctx);
+   if (ctx->graph_exec)
+      cudaGraphExecDestroy(ctx->graph_exec);
+   if (ctx->cap_stream)
+      cudaStreamDestroy(ctx->cap_stream);
+   for (auto& e : ctx->prof.ev)
+      cudaEventDestroy(e);
    if (ctx->own_stream && ctx->stream)
       cudaStreamDestroy(ctx->stream);
 }
@@ -379,6 +385,14 @@ int t9gb_get_udir(t9gb_context* h, float* udir, float* udirp)
    if (!ctx->have_order)
       return T9GB_NOT_READY;
    return scatter_from_sorted3(ctx, ctx->udir, udir, udirp);
+}
+
+int t9gb_use_graph(t9gb_context* h, int enable)
+{
+   if (!h)
+      return T9GB_BAD_ARG;
+   h->c.use_graph = enable != 0;
+   return T9GB_OK;
 }
 
 int t9gb_nblist_stats(t9gb_context* h, int* capacity, long long* entries, int* nscaled)

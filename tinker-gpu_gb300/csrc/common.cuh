@@ -15,7 +15,7 @@ namespace t9gb {
 
 constexpr int WARP = 32;
 constexpr int BSORDER = 5;
-constexpr int GROUP = 8;  // lanes per atom in the real-space kernels
+constexpr int GROUP = 16;  // lanes per atom in the real-space kernels
 
 // The PME grid accumulates in signed 64-bit fixed point with 40 fractional
 // bits: order-independent (bit-reproducible) sums, range +-8.4e6,
@@ -147,9 +147,13 @@ struct Context {
    int* h_status = nullptr; // pinned mirrors
    double* h_scal = nullptr;
 
-   // ASPC predictor ring, sorted [16][npad][6]
+   // ASPC predictor ring, sorted [16][npad][6]; the ring count is device state
    float* aspc_hist = nullptr;
-   int nualt = 0;
+
+   // whole-induce CUDA graph
+   bool use_graph = true;
+   cudaGraphExec_t graph_exec = nullptr;
+   cudaStream_t cap_stream = nullptr;
 
    // last induce statistics
    int last_iter = 0;
@@ -219,6 +223,7 @@ int order_build(Context* ctx);  // host: spatial order, scaled partners
 int list_update(Context* ctx);  // device: exact neighbour list
 int scatter_positions(Context* ctx);
 int rotpole_sorted(Context* ctx);
+int reset_predictor(Context* ctx);
 int pme_setup(Context* ctx);
 void pme_free(Context* ctx);
 

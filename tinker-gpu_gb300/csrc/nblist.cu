@@ -198,9 +198,12 @@ int order_build(Context* ctx)
    }
    ctx->have_order = true;
    ctx->list_stale = true;
+   if (ctx->graph_exec) {
+      cudaGraphExecDestroy(ctx->graph_exec);
+      ctx->graph_exec = nullptr;
+   }
    // a new order invalidates the predictor history
-   ctx->nualt = 0;
-   return T9GB_OK;
+   return reset_predictor(ctx);
 }
 
 // ---------------------------------------------------------------------------
@@ -274,21 +277,32 @@ __global__ void k_cell_fill(int n, const int* __restrict__ atom_cell, const int*
    cell_atoms[start[c] + atomicAdd(cursor + c, 1)] = s;
 }
 
-// ascending slots inside each cell (fixes the list order)
+// ascending slots inside each cell (fixes the list order): one warp per cell,
+// each lane's rank is the count of smaller slots in the cell
 __global__ void k_cell_sort(int ncell, const int* __restrict__ start, int* __restrict__ cell_atoms)
 {
-   int c = blockIdx.x * blockDim.x + threadIdx.x;
+   const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+   const int lane = threadIdx.x & 31;
    if (c >= ncell)
       return;
-   int a = start[c], b = start[c + 1];
-   for (int i = a + 1; i < b; ++i) {
-      int v = cell_atoms[i];
-      int j = i - 1;
-      while (j >= a && cell_atoms[j] > v) {
-         cell_atoms[j + 1] = cell_atoms[j];
-         --j;
+   const int a = start[c], b = start[c + 1], cnt = b - a;
+   if (cnt <= 32) {
+      const int v = lane < cnt ? cell_atoms[a + lane] : 0x7fffffff;
+      int rank = 0;
+      for (int k = 0; k < 32; ++k)
+         rank += __shfl_sync(0xffffffffu, v, k) < v ? 1 : 0;
+      if (lane < cnt)
+         cell_atoms[a + rank] = v;
+   } else if (lane == 0) {
+      for (int i = a + 1; i < b; ++i) {
+         int v = cell_atoms[i];
+         int j = i - 1;
+         while (j >= a && cell_atoms[j] > v) {
+            cell_atoms[j + 1] = cell_atoms[j];
+            --j;
+         }
+         cell_atoms[j + 1] = v;
       }
-      cell_atoms[j + 1] = v;
    }
 }
 
@@ -300,12 +314,20 @@ __device__ __forceinline__ bool is_partner(const int* __restrict__ sp_j, int a, 
    return false;
 }
 
-// one warp per atom; 25 x-runs of five cells, compacted with ballots
+// One warp per atom.  The 5x5x5 stencil is 25 x-rows of five consecutive
+// cells, i.e. at most 50 contiguous runs of cell_atoms (a row splits in two
+// where it wraps).  Lanes first record every run's start and length, then
+// walk the concatenated candidate stream 32 at a time (a binary search maps a
+// stream position to its run) and compact accepted neighbours with ballots,
+// which keeps the list order fixed.
 __global__ void __launch_bounds__(256) k_nbr_cells(CellParams C, const float4* __restrict__ spos,
    const int* __restrict__ atom_cell, const int* __restrict__ start, const int* __restrict__ cell_atoms,
    const int* __restrict__ sp_start, const int* __restrict__ sp_j, int* __restrict__ nbr, int* __restrict__ nnbr,
    int* __restrict__ over)
 {
+   __shared__ int s_off[8][52];
+   __shared__ int s_beg[8][52];
+   const int w = threadIdx.x >> 5;
    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
    const int lane = threadIdx.x & 31;
    if (i >= C.npad)
@@ -318,56 +340,95 @@ __global__ void __launch_bounds__(256) k_nbr_cells(CellParams C, const float4* _
    const float4 pi = spos[i];
    const int ci = atom_cell[i];
    const int cix = ci % C.ncx, ciy = (ci / C.ncx) % C.ncy, ciz = ci / (C.ncx * C.ncy);
-   const int pa = sp_start[i], pb = sp_start[i + 1];
-   const unsigned lt = (1u << lane) - 1u;
-   int cnt = 0;
-   int* out = nbr + (size_t)i * C.cap;
-   for (int dz = -2; dz <= 2; ++dz) {
-      int cz = ciz + dz;
-      cz += (cz < 0 ? C.ncz : 0) - (cz >= C.ncz ? C.ncz : 0);
-      for (int dy = -2; dy <= 2; ++dy) {
-         int cy = ciy + dy;
+   int len[2], beg[2];
+#pragma unroll
+   for (int h = 0; h < 2; ++h) {
+      const int r = lane + 32 * h;
+      len[h] = 0;
+      beg[h] = 0;
+      if (r < 50) {
+         const int q = r >> 1, part = r & 1;
+         int cz = ciz + q / 5 - 2, cy = ciy + q % 5 - 2;
+         cz += (cz < 0 ? C.ncz : 0) - (cz >= C.ncz ? C.ncz : 0);
          cy += (cy < 0 ? C.ncy : 0) - (cy >= C.ncy ? C.ncy : 0);
          const int row = (cz * C.ncy + cy) * C.ncx;
-         int x0 = cix - 2, x1 = cix + 2;
-         // up to two runs of consecutive cells along x
-         int ra[2], rb[2], nrun = 0;
+         const int x0 = cix - 2, x1 = cix + 2;
+         int ca = 0, cb = -1;
          if (x0 < 0) {
-            ra[nrun] = x0 + C.ncx;
-            rb[nrun++] = C.ncx - 1;
-            x0 = 0;
-         }
-         if (x1 >= C.ncx) {
-            ra[nrun] = x0;
-            rb[nrun++] = C.ncx - 1;
-            ra[nrun] = 0;
-            rb[nrun++] = x1 - C.ncx;
-         } else {
-            ra[nrun] = x0;
-            rb[nrun++] = x1;
-         }
-         for (int r = 0; r < nrun; ++r) {
-            const int a = start[row + ra[r]], b = start[row + rb[r] + 1];
-            for (int t = a; t < b; t += 32) {
-               const int idx = t + lane;
-               bool acc = false;
-               int j = -1;
-               if (idx < b) {
-                  j = cell_atoms[idx];
-                  float4 pj = spos[j];
-                  float dx = image1(pj.x - pi.x, C.lx, C.ilx);
-                  float dy2 = image1(pj.y - pi.y, C.ly, C.ily);
-                  float dz2 = image1(pj.z - pi.z, C.lz, C.ilz);
-                  acc = j != i && dx * dx + dy2 * dy2 + dz2 * dz2 <= C.r2 && !is_partner(sp_j, pa, pb, j);
-               }
-               const unsigned m = __ballot_sync(0xffffffffu, acc);
-               const int pos = cnt + __popc(m & lt);
-               if (acc && pos < C.cap)
-                  out[pos] = j;
-               cnt += __popc(m);
+            if (part == 0) {
+               ca = x0 + C.ncx;
+               cb = C.ncx - 1;
+            } else {
+               ca = 0;
+               cb = x1;
             }
+         } else if (x1 >= C.ncx) {
+            if (part == 0) {
+               ca = x0;
+               cb = C.ncx - 1;
+            } else {
+               ca = 0;
+               cb = x1 - C.ncx;
+            }
+         } else if (part == 0) {
+            ca = x0;
+            cb = x1;
+         }
+         if (cb >= ca) {
+            beg[h] = start[row + ca];
+            len[h] = start[row + cb + 1] - beg[h];
          }
       }
+   }
+   // exclusive offsets of the 64 run slots
+   int inc0 = len[0], inc1 = len[1];
+#pragma unroll
+   for (int o = 1; o < 32; o <<= 1) {
+      int v0 = __shfl_up_sync(0xffffffffu, inc0, o);
+      int v1 = __shfl_up_sync(0xffffffffu, inc1, o);
+      if (lane >= o) {
+         inc0 += v0;
+         inc1 += v1;
+      }
+   }
+   const int tot0 = __shfl_sync(0xffffffffu, inc0, 31);
+   const int total = tot0 + __shfl_sync(0xffffffffu, inc1, 31);
+   s_off[w][lane] = inc0 - len[0];
+   s_beg[w][lane] = beg[0];
+   if (lane < 20) {
+      s_off[w][32 + lane] = tot0 + inc1 - len[1];
+      s_beg[w][32 + lane] = beg[1];
+   }
+   __syncwarp();
+   const int pa = sp_start[i], pb = sp_start[i + 1];
+   const unsigned lt = (1u << lane) - 1u;
+   int* out = nbr + (size_t)i * C.cap;
+   int cnt = 0;
+   for (int t0 = 0; t0 < total; t0 += 32) {
+      const int t = t0 + lane;
+      bool acc = false;
+      int j = -1;
+      if (t < total) {
+         int lo = 0, hi = 49;
+         while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (s_off[w][mid] <= t)
+               lo = mid;
+            else
+               hi = mid - 1;
+         }
+         j = cell_atoms[s_beg[w][lo] + (t - s_off[w][lo])];
+         const float4 pj = spos[j];
+         const float dx = image1(pj.x - pi.x, C.lx, C.ilx);
+         const float dy = image1(pj.y - pi.y, C.ly, C.ily);
+         const float dz = image1(pj.z - pi.z, C.lz, C.ilz);
+         acc = j != i && dx * dx + dy * dy + dz * dz <= C.r2 && !is_partner(sp_j, pa, pb, j);
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, acc);
+      const int pos = cnt + __popc(m & lt);
+      if (acc && pos < C.cap)
+         out[pos] = j;
+      cnt += __popc(m);
    }
    if (lane == 0) {
       nnbr[i] = min(cnt, C.cap);
@@ -444,7 +505,8 @@ int list_update(Context* ctx)
       k_cell_scan<<<1, 1024, 0, ctx->stream>>>(ctx->ncell, ctx->cell_count, ctx->cell_start);
       k_cell_fill<<<grid_for(ctx->n, 256), 256, 0, ctx->stream>>>(ctx->n, ctx->atom_cell, ctx->cell_start,
          ctx->cell_count, ctx->cell_atoms);
-      k_cell_sort<<<grid_for(ctx->ncell, 128), 128, 0, ctx->stream>>>(ctx->ncell, ctx->cell_start, ctx->cell_atoms);
+      k_cell_sort<<<grid_for((long long)ctx->ncell * 32, 256), 256, 0, ctx->stream>>>(ctx->ncell, ctx->cell_start,
+         ctx->cell_atoms);
       k_nbr_cells<<<grid_for((long long)ctx->npad * 32, 256), 256, 0, ctx->stream>>>(C, ctx->spos, ctx->atom_cell,
          ctx->cell_start, ctx->cell_atoms, ctx->sp_start, ctx->sp_j, ctx->nbr, ctx->nnbr, ctx->nbr_over);
    } else {

@@ -1,12 +1,13 @@
 // Real-space pair kernels over the per-step neighbour list.
 //
-// GROUP (8) consecutive lanes own one atom i: lane g walks the list entries
-// g, g+8, g+16, ... of atom i (consecutive addresses per step), then the
-// scaled partners of i the same way; the eight partial fields are combined
-// with a fixed xor-shuffle tree and written with plain stores.  Every pair is
+// GROUP (16) consecutive lanes own one atom i: lane g walks the list entries
+// g, g+16, g+32, ... of atom i (consecutive addresses per step, two entries
+// in flight per trip), then the scaled partners of i the same way; the
+// partial fields are combined with a fixed xor-shuffle tree and written with
+// plain stores.  Every pair is
 // evaluated from both sides (full list), so no atomics are needed and each
 // field component is a sum in a fixed order: results are bit-reproducible.
-// 12,288 atoms give 98,304 threads, enough to fill 152 SMs.
+// 12,288 atoms give 196,608 threads, ~40 warps on each of the 152 SMs.
 //
 // Pair arithmetic restates the reference's pair_dfield_v2 / pair_ufield_v2
 // (include/seq/pair_field.h:127-256, :333-420) for the atom-i side, Thole
@@ -60,13 +61,13 @@ __device__ __forceinline__ float3 sep(const PairParams& P, float4 pi, float4 pk)
       image1(pk.z - pi.z, P.lz, P.ilz));
 }
 
-template <int N>
+template <int G, int N>
 __device__ __forceinline__ void group_reduce(float* v)
 {
 #pragma unroll
    for (int c = 0; c < N; ++c) {
 #pragma unroll
-      for (int o = GROUP / 2; o > 0; o >>= 1)
+      for (int o = G / 2; o > 0; o >>= 1)
          v[c] += __shfl_xor_sync(0xffffffffu, v[c], o);
    }
 }
@@ -138,13 +139,14 @@ __device__ __forceinline__ void ufield_i(const PairParams& P, float r2, float3 d
    f[5] += c * d.z - b1 * uk[5];
 }
 
+template <int G>
 __global__ void __launch_bounds__(256) k_ufield_real(PairParams P, int npad, const int* __restrict__ nbr,
    const int* __restrict__ nnbr, const int* __restrict__ sp_start, const int* __restrict__ sp_j,
    const float4* __restrict__ sp_sc, const float4* __restrict__ spos, const float* __restrict__ u6,
    const float2* __restrict__ sdamp, const float* __restrict__ base6, float* __restrict__ out6)
 {
    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-   const int i = tid / GROUP, g = tid % GROUP;
+   const int i = tid / G, g = tid % G;
    if (i >= npad)
       return;
    float f[6] = {0, 0, 0, 0, 0, 0};
@@ -153,7 +155,24 @@ __global__ void __launch_bounds__(256) k_ufield_real(PairParams P, int npad, con
       const float2 di = sdamp[i];
       const int* row = nbr + (size_t)i * P.cap;
       const int cnt = nnbr[i];
-      for (int k = g; k < cnt; k += GROUP) {
+      int k = g;
+      // two neighbours per trip: both sets of loads are in flight together
+      for (; k + G < cnt; k += 2 * G) {
+         const int j0 = row[k], j1 = row[k + G];
+         const float4 p0 = spos[j0], p1 = spos[j1];
+         float u0[6], u1[6];
+         load6(u6, j0, u0);
+         load6(u6, j1, u1);
+         const float2 d0 = sdamp[j0], d1 = sdamp[j1];
+         const float3 s0 = sep(P, pi, p0), s1 = sep(P, pi, p1);
+         const float r0 = s0.x * s0.x + s0.y * s0.y + s0.z * s0.z;
+         const float r1 = s1.x * s1.x + s1.y * s1.y + s1.z * s1.z;
+         if (r0 <= P.cut2)
+            ufield_i(P, r0, s0, 1.f, di.x, di.y, d0.x, d0.y, u0, f);
+         if (r1 <= P.cut2)
+            ufield_i(P, r1, s1, 1.f, di.x, di.y, d1.x, d1.y, u1, f);
+      }
+      if (k < cnt) {
          const int j = row[k];
          const float4 pk = spos[j];
          const float3 d = sep(P, pi, pk);
@@ -166,7 +185,7 @@ __global__ void __launch_bounds__(256) k_ufield_real(PairParams P, int npad, con
          }
       }
       const int pa = sp_start[i], pb = sp_start[i + 1];
-      for (int q = pa + g; q < pb; q += GROUP) {
+      for (int q = pa + g; q < pb; q += G) {
          const int j = sp_j[q];
          const float4 pk = spos[j];
          const float3 d = sep(P, pi, pk);
@@ -179,7 +198,7 @@ __global__ void __launch_bounds__(256) k_ufield_real(PairParams P, int npad, con
          }
       }
    }
-   group_reduce<6>(f);
+   group_reduce<G, 6>(f);
    store6(out6, i < P.n ? base6 : nullptr, i, g, f);
 }
 
@@ -254,13 +273,14 @@ __device__ __forceinline__ void load10(const float* __restrict__ rp, int s, floa
    }
 }
 
+template <int G>
 __global__ void __launch_bounds__(256) k_dfield_real(PairParams P, int npad, const int* __restrict__ nbr,
    const int* __restrict__ nnbr, const int* __restrict__ sp_start, const int* __restrict__ sp_j,
    const float4* __restrict__ sp_sc, const float4* __restrict__ spos, const float* __restrict__ rp,
    const float2* __restrict__ sdamp, const float* __restrict__ base6, float* __restrict__ out6)
 {
    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-   const int i = tid / GROUP, g = tid % GROUP;
+   const int i = tid / G, g = tid % G;
    if (i >= npad)
       return;
    float f[6] = {0, 0, 0, 0, 0, 0};
@@ -269,7 +289,7 @@ __global__ void __launch_bounds__(256) k_dfield_real(PairParams P, int npad, con
       const float2 di = sdamp[i];
       const int* row = nbr + (size_t)i * P.cap;
       const int cnt = nnbr[i];
-      for (int k = g; k < cnt; k += GROUP) {
+      for (int k = g; k < cnt; k += G) {
          const int j = row[k];
          const float4 pk = spos[j];
          const float3 d = sep(P, pi, pk);
@@ -282,7 +302,7 @@ __global__ void __launch_bounds__(256) k_dfield_real(PairParams P, int npad, con
          }
       }
       const int pa = sp_start[i], pb = sp_start[i + 1];
-      for (int q = pa + g; q < pb; q += GROUP) {
+      for (int q = pa + g; q < pb; q += G) {
          const int j = sp_j[q];
          const float4 pk = spos[j];
          const float3 d = sep(P, pi, pk);
@@ -296,13 +316,35 @@ __global__ void __launch_bounds__(256) k_dfield_real(PairParams P, int npad, con
          }
       }
    }
-   group_reduce<6>(f);
+   group_reduce<G, 6>(f);
    store6(out6, i < P.n ? base6 : nullptr, i, g, f);
 }
 
 // ---------------------------------------------------------------------------
 // sparse preconditioner: z_i = udiag alpha_i r_i + sum_k alpha_i alpha_k T_ik r_k
 
+__device__ __forceinline__ void precond_i(float r2, float3 d, float us, float poli, float polk, float2 di, float2 dk,
+   const float* rk, float* f)
+{
+   float invr = rsqrtf(r2);
+   float r = r2 * invr;
+   float s3, s5, s7;
+   thole_damp(r, di.x, di.y, dk.x, dk.y, s3, s5, s7);
+   const float polik = poli * polk;
+   const float ir3 = invr * invr * invr;
+   const float rr3 = us * s3 * polik * ir3;
+   const float rr5 = 3.f * us * s5 * polik * ir3 * invr * invr;
+   float c = rr5 * (d.x * rk[0] + d.y * rk[1] + d.z * rk[2]);
+   f[0] += c * d.x - rr3 * rk[0];
+   f[1] += c * d.y - rr3 * rk[1];
+   f[2] += c * d.z - rr3 * rk[2];
+   c = rr5 * (d.x * rk[3] + d.y * rk[4] + d.z * rk[5]);
+   f[3] += c * d.x - rr3 * rk[3];
+   f[4] += c * d.y - rr3 * rk[4];
+   f[5] += c * d.z - rr3 * rk[5];
+}
+
+template <int G>
 __global__ void __launch_bounds__(256) k_precond_sparse(PairParams P, int npad, float udiag,
    const int* __restrict__ nbr, const int* __restrict__ nnbr, const int* __restrict__ sp_start,
    const int* __restrict__ sp_j, const float4* __restrict__ sp_sc, const float4* __restrict__ spos,
@@ -310,7 +352,7 @@ __global__ void __launch_bounds__(256) k_precond_sparse(PairParams P, int npad, 
    float* __restrict__ z6)
 {
    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-   const int i = tid / GROUP, g = tid % GROUP;
+   const int i = tid / G, g = tid % G;
    if (i >= npad)
       return;
    float f[6] = {0, 0, 0, 0, 0, 0};
@@ -320,43 +362,46 @@ __global__ void __launch_bounds__(256) k_precond_sparse(PairParams P, int npad, 
       const float2 di = sdamp[i];
       const int* row = nbr + (size_t)i * P.cap;
       const int cnt = nnbr[i];
-      const int pa = sp_start[i], pb = sp_start[i + 1];
-      const int tot = cnt + (pb - pa);
-      for (int k = g; k < tot; k += GROUP) {
-         int j;
-         float us = 1.f;
-         if (k < cnt) {
-            j = row[k];
-         } else {
-            j = sp_j[pa + k - cnt];
-            us = sp_sc[pa + k - cnt].w;
-         }
-         const float4 pk = spos[j];
-         const float3 d = sep(P, pi, pk);
+      int k = g;
+      for (; k + G < cnt; k += 2 * G) {
+         const int j0 = row[k], j1 = row[k + G];
+         const float4 p0 = spos[j0], p1 = spos[j1];
+         float r0v[6], r1v[6];
+         load6(r6, j0, r0v);
+         load6(r6, j1, r1v);
+         const float2 d0 = sdamp[j0], d1 = sdamp[j1];
+         const float a0 = spolar[j0], a1 = spolar[j1];
+         const float3 s0 = sep(P, pi, p0), s1 = sep(P, pi, p1);
+         const float q0 = s0.x * s0.x + s0.y * s0.y + s0.z * s0.z;
+         const float q1 = s1.x * s1.x + s1.y * s1.y + s1.z * s1.z;
+         if (q0 <= P.cut2)
+            precond_i(q0, s0, 1.f, poli, a0, di, d0, r0v, f);
+         if (q1 <= P.cut2)
+            precond_i(q1, s1, 1.f, poli, a1, di, d1, r1v, f);
+      }
+      if (k < cnt) {
+         const int j = row[k];
+         const float3 d = sep(P, pi, spos[j]);
          const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
          if (r2 <= P.cut2) {
             float rk[6];
             load6(r6, j, rk);
-            const float2 dk = sdamp[j];
-            float invr = rsqrtf(r2);
-            float r = r2 * invr;
-            float s3, s5, s7;
-            thole_damp(r, di.x, di.y, dk.x, dk.y, s3, s5, s7);
-            const float polik = poli * spolar[j];
-            const float rr3 = us * s3 * polik * invr * invr * invr;
-            const float rr5 = 3.f * us * s5 * polik * invr * invr * invr * invr * invr;
-            float c = rr5 * (d.x * rk[0] + d.y * rk[1] + d.z * rk[2]);
-            f[0] += c * d.x - rr3 * rk[0];
-            f[1] += c * d.y - rr3 * rk[1];
-            f[2] += c * d.z - rr3 * rk[2];
-            c = rr5 * (d.x * rk[3] + d.y * rk[4] + d.z * rk[5]);
-            f[3] += c * d.x - rr3 * rk[3];
-            f[4] += c * d.y - rr3 * rk[4];
-            f[5] += c * d.z - rr3 * rk[5];
+            precond_i(r2, d, 1.f, poli, spolar[j], di, sdamp[j], rk, f);
+         }
+      }
+      const int pa = sp_start[i], pb = sp_start[i + 1];
+      for (int q = pa + g; q < pb; q += G) {
+         const int j = sp_j[q];
+         const float3 d = sep(P, pi, spos[j]);
+         const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
+         if (r2 <= P.cut2) {
+            float rk[6];
+            load6(r6, j, rk);
+            precond_i(r2, d, sp_sc[q].w, poli, spolar[j], di, sdamp[j], rk, f);
          }
       }
    }
-   group_reduce<6>(f);
+   group_reduce<G, 6>(f);
    if (g < 6)
       z6[6 * i + g] = udiag * poli * r6[6 * i + g] + pick6(f, g);
 }
@@ -396,7 +441,7 @@ int launch_ufield_real(Context* ctx, const float* u6, const float* base6, float*
 {
    PairParams P = make_params(ctx, ctx->cfg.cutoff);
    prof_begin(ctx, P_UFIELD_REAL);
-   k_ufield_real<<<grid_for((long long)ctx->npad * GROUP, PAIR_THREADS), PAIR_THREADS, 0, ctx->stream>>>(P,
+   k_ufield_real<GROUP><<<grid_for((long long)ctx->npad * GROUP, PAIR_THREADS), PAIR_THREADS, 0, ctx->stream>>>(P,
       ctx->npad, ctx->nbr, ctx->nnbr, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos, u6, ctx->sdamp, base6, out6);
    prof_end(ctx);
    T9_CUDA(cudaGetLastError());
@@ -407,7 +452,7 @@ int launch_dfield_real(Context* ctx, const float* base6, float* out6)
 {
    PairParams P = make_params(ctx, ctx->cfg.cutoff);
    prof_begin(ctx, P_DFIELD_REAL);
-   k_dfield_real<<<grid_for((long long)ctx->npad * GROUP, PAIR_THREADS), PAIR_THREADS, 0, ctx->stream>>>(P,
+   k_dfield_real<GROUP><<<grid_for((long long)ctx->npad * GROUP, PAIR_THREADS), PAIR_THREADS, 0, ctx->stream>>>(P,
       ctx->npad, ctx->nbr, ctx->nnbr, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos, ctx->srpole, ctx->sdamp, base6,
       out6);
    prof_end(ctx);
@@ -420,7 +465,7 @@ int launch_precond_sparse(Context* ctx, const float* r6, float* z6)
    PairParams P = make_params(ctx, ctx->cfg.usolve_cutoff + ctx->cfg.pbuffer);
    P.ewald = 0;
    prof_begin(ctx, P_PRECOND);
-   k_precond_sparse<<<grid_for((long long)ctx->npad * GROUP, PAIR_THREADS), PAIR_THREADS, 0, ctx->stream>>>(P,
+   k_precond_sparse<GROUP><<<grid_for((long long)ctx->npad * GROUP, PAIR_THREADS), PAIR_THREADS, 0, ctx->stream>>>(P,
       ctx->npad, (float)ctx->cfg.udiag, ctx->nbr, ctx->nnbr, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos, r6,
       ctx->sdamp, ctx->spolar, z6);
    prof_end(ctx);

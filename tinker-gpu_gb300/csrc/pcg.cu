@@ -9,24 +9,33 @@
 //         eps = debye sqrt(max(r.r)/n); stop when eps < poleps (at least 3
 //         iterations, at most politer); then u += pcgpeek alpha r.
 // The reference runs ~20 launches per iteration including eight cuBLAS Sdot
-// calls and a host synchronisation (pcg.cu:144-145).  Here an iteration is
-// the ufield chain, the preconditioner and four element-parallel vector
-// kernels.  Every dot product is an FP64 block partial that each consumer
-// block re-reduces in a fixed order (bit-reproducible); the convergence test
-// runs on the device.
+// calls and a host synchronisation (pcg.cu:144-145).  Here:
+//  - dot products are FP64 block partials; the last block of the producing
+//    kernel (threadfence + ticket) sums them in a fixed order and derives
+//    the CG scalars, so results are bit-reproducible and no extra launch or
+//    host round trip is needed;
+//  - the convergence test, the iteration count and the predictor ring index
+//    live on the device; the whole induce() -- neighbour list, permanent
+//    field, guess, r0, the PCG loop as a conditional WHILE node, and the
+//    predictor save -- is one CUDA graph, launched once per call.
 #include <cmath>
 
 #include "common.cuh"
 
 namespace t9gb {
 
-// device PCG state (ctx->scal as doubles, ctx->status as ints)
-enum { S_SUM_D = 0, S_SUM_P = 1, S_EPS = 2, S_COEF = 8, S_NSCAL = 24 };
-enum { ST_ITER = 0, ST_DONE = 1, ST_STATUS = 2, ST_NSTAT = 4 };
-// reduction slots
-enum { R_PAP_D = 0, R_PAP_P = 1, R_RZ_D = 2, R_RZ_P = 3, R_RR_D = 4, R_RR_P = 5 };
+// device doubles (ctx->scal) and ints (ctx->status)
+enum { S_SUM_D = 0, S_SUM_P, S_A_D, S_A_P, S_B_D, S_B_P, S_EPS, S_NSCAL = 16 };
+enum { ST_ITER = 0, ST_DONE, ST_STATUS, ST_NUALT, ST_TICKET0, ST_TICKET1, ST_NSTAT = 8 };
+enum { R_PAP_D = 0, R_PAP_P, R_RZ_D, R_RZ_P, R_RR_D, R_RR_P };
 
 constexpr int VB = 256;  // vector-kernel block size
+
+// ASPC extrapolation weights (Kolafa, J. Comput. Chem. 25, 335 (2004)); the
+// reference tabulates them in src/cu/upredict.cu:40-55.
+__constant__ double c_aspc[16] = {62. / 17., -310. / 51., 2170. / 323., -2329. / 400., 1701. / 409., -806. / 323.,
+   1024. / 809., -479. / 883., 257. / 1316., -434. / 7429., 191. / 13375., -62. / 22287., 3. / 7217.,
+   -3. / 67015., 2. / 646323., -1. / 9694845.};
 
 __device__ double block_sum(double v, double* sh)
 {
@@ -48,31 +57,47 @@ __device__ double block_sum(double v, double* sh)
    return r;  // valid in thread 0
 }
 
-// deterministic sum of nb partials, broadcast to the block
-__device__ double finalize(const double* part, int nb, double* sh)
+// fixed-order sum of nb partials (valid in thread 0)
+__device__ double sum_partials(const double* part, int nb, double* sh)
 {
    double v = 0;
    for (int i = threadIdx.x; i < nb; i += blockDim.x)
       v += part[i];
-   v = block_sum(v, sh);
-   if (threadIdx.x == 0)
-      sh[32] = v;
-   __syncthreads();
-   double r = sh[32];
-   __syncthreads();
-   return r;
+   return block_sum(v, sh);
 }
 
-__device__ __forceinline__ void store_partial(double* red, int slot, double v, double* sh)
+// store this block's partial sum of v
+__device__ void store_partial(double* red, int slot, double v, double* sh)
 {
    v = block_sum(v, sh);
    if (threadIdx.x == 0)
       red[slot * RED_MAX + blockIdx.x] = v;
 }
 
+// true in the block that finishes last (threadfence + ticket); it resets the
+// ticket for the next launch
+
+__device__ bool last_block(int* ticket)
+{
+   __shared__ bool last;
+   __threadfence();
+   __syncthreads();
+   if (threadIdx.x == 0) {
+      unsigned prev = atomicAdd(reinterpret_cast<unsigned*>(ticket), 1u);
+      last = prev == gridDim.x - 1;
+   }
+   __syncthreads();
+   if (last) {
+      __threadfence();
+      if (threadIdx.x == 0)
+         *ticket = 0;
+   }
+   return last;
+}
+
 struct VecArgs {
    int ne;  // 6 * npad elements
-   int nb;  // blocks of every vector kernel (fixed: partial counts match)
+   int nb;  // blocks of every vector kernel
    const float* polar;
    const float* polinv;
    int sparse;
@@ -80,11 +105,18 @@ struct VecArgs {
 
 // ---- start of induce ----
 
-// E = field, udir = alpha E, initial guess (guess 0 zero, 1 direct, 2 ASPC)
+// E = field, udir = alpha E, guess: ASPC when 16 frames are saved, else the
+// direct guess alpha E (pcgguess) or zero
 __global__ void k_init_guess(VecArgs A, const float* __restrict__ fld, float* __restrict__ efield,
-   float* __restrict__ udir, float* __restrict__ uind, int guess, const float* __restrict__ hist,
-   const double* __restrict__ coef)
+   float* __restrict__ udir, float* __restrict__ uind, int pcgguess, int predictor, const float* __restrict__ hist,
+   const int* __restrict__ state)
 {
+   const int nualt = state[ST_NUALT];
+   const bool predict = predictor && nualt >= 16;
+   double coef[16];
+   if (predict)
+      for (int k = 0; k < 16; ++k)
+         coef[k] = c_aspc[((nualt - 1 - k) % 16 + 16) % 16];
    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.ne; e += gridDim.x * blockDim.x) {
       const float pol = A.polar[e / 6];
       const float f = fld[e];
@@ -92,41 +124,38 @@ __global__ void k_init_guess(VecArgs A, const float* __restrict__ fld, float* __
       const float ud = pol * f;
       udir[e] = ud;
       float u = 0.f;
-      if (guess == 1) {
-         u = ud;
-      } else if (guess == 2) {
+      if (predict) {
          double v = 0;
          for (int k = 0; k < 16; ++k)
             v += coef[k] * (double)hist[(size_t)k * A.ne + e];
          u = (float)v;
+      } else if (pcgguess) {
+         u = ud;
       }
       uind[e] = u;
    }
 }
 
-// r0 from the guess (fld holds ufield(u0) when guess != 0)
+// r0 = (udir - u0)/alpha + ufield(u0)  [= ufield(udir) for the direct guess,
+// E for the zero guess]
 __global__ void k_init_rsd(VecArgs A, const float* __restrict__ fld, const float* __restrict__ efield,
-   const float* __restrict__ udir, const float* __restrict__ uind, float* __restrict__ rsd, int guess)
+   const float* __restrict__ udir, const float* __restrict__ uind, float* __restrict__ rsd, int zero_guess)
 {
    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.ne; e += gridDim.x * blockDim.x) {
       const int s = e / 6;
-      float r;
-      if (guess == 2)
-         r = (udir[e] - uind[e]) * A.polinv[s] + fld[e];
-      else if (guess == 1)
-         r = fld[e];
-      else
-         r = efield[e];
+      float r = zero_guess ? efield[e] : (udir[e] - uind[e]) * A.polinv[s] + fld[e];
       if (A.polar[s] == 0.f)
          r = 0.f;
       rsd[e] = r;
    }
 }
 
-// z = M r (diagonal here, or read from the sparse kernel); p = z on init;
-// partials r.z and r.r
+// z = M r (diagonal here, else read from the sparse kernel), p = z on init,
+// partials r.z and r.r.  The last block: init -> s = r.z; loop -> b = s1/s,
+// s = s1, eps, iteration count, convergence, graph condition.
 __global__ void k_precond_dot(VecArgs A, const float* __restrict__ rsd, float* __restrict__ zrsd,
-   float* __restrict__ conj, double* __restrict__ red, int init)
+   float* __restrict__ conj, double* __restrict__ red, double* __restrict__ scal, int* __restrict__ state, int init,
+   int n, double debye, double poleps, int politer, int miniter, cudaGraphConditionalHandle handle, int use_handle)
 {
    __shared__ double sh[40];
    double rz_d = 0, rz_p = 0, rr_d = 0, rr_p = 0;
@@ -153,17 +182,52 @@ __global__ void k_precond_dot(VecArgs A, const float* __restrict__ rsd, float* _
    store_partial(red, R_RZ_P, rz_p, sh);
    store_partial(red, R_RR_D, rr_d, sh);
    store_partial(red, R_RR_P, rr_p, sh);
+   if (!last_block(state + ST_TICKET0))
+      return;
+   const double s1_d = sum_partials(red + R_RZ_D * RED_MAX, gridDim.x, sh);
+   const double s1_p = sum_partials(red + R_RZ_P * RED_MAX, gridDim.x, sh);
+   const double q_d = sum_partials(red + R_RR_D * RED_MAX, gridDim.x, sh);
+   const double q_p = sum_partials(red + R_RR_P * RED_MAX, gridDim.x, sh);
+   if (threadIdx.x != 0)
+      return;
+   if (init) {
+      scal[S_SUM_D] = s1_d;
+      scal[S_SUM_P] = s1_p;
+      state[ST_ITER] = 0;
+      state[ST_DONE] = 0;
+      state[ST_STATUS] = T9GB_OK;
+      return;
+   }
+   const double s_d = scal[S_SUM_D], s_p = scal[S_SUM_P];
+   scal[S_B_D] = s_d == 0 ? 0.0 : s1_d / s_d;
+   scal[S_B_P] = s_p == 0 ? 0.0 : s1_p / s_p;
+   scal[S_SUM_D] = s1_d;
+   scal[S_SUM_P] = s1_p;
+   const double eps = debye * sqrt(fmax(q_d, q_p) / n);
+   const int iter = state[ST_ITER] + 1;
+   state[ST_ITER] = iter;
+   bool done = eps < poleps;
+   if (iter < miniter)
+      done = false;
+   if (iter >= politer)
+      done = true;
+   const bool nan = !(eps == eps);
+   if (nan)
+      done = true;
+   scal[S_EPS] = eps;
+   state[ST_DONE] = done ? 1 : 0;
+   state[ST_STATUS] = nan ? T9GB_NAN_DETECTED : (done && !(eps < poleps) ? T9GB_NOT_CONVERGED : T9GB_OK);
+   if (use_handle)
+      cudaGraphSetConditional(handle, done ? 0u : 1u);
 }
 
 // ---- loop body ----
 
-// Ap = p/alpha - ufield(p); partials p.Ap; counts the iteration
+// Ap = p/alpha - ufield(p); partials p.Ap; last block: a = s / p.Ap
 __global__ void k_pcg_p1(VecArgs A, const float* __restrict__ fld, const float* __restrict__ conj,
-   float* __restrict__ vec, double* __restrict__ red, int* __restrict__ state)
+   float* __restrict__ vec, double* __restrict__ red, double* __restrict__ scal, int* __restrict__ state)
 {
    __shared__ double sh[40];
-   if (blockIdx.x == 0 && threadIdx.x == 0)
-      state[ST_ITER] += 1;
    double dd = 0, dp = 0;
    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.ne; e += gridDim.x * blockDim.x) {
       const float p = conj[e];
@@ -176,23 +240,21 @@ __global__ void k_pcg_p1(VecArgs A, const float* __restrict__ fld, const float* 
    }
    store_partial(red, R_PAP_D, dd, sh);
    store_partial(red, R_PAP_P, dp, sh);
+   if (!last_block(state + ST_TICKET1))
+      return;
+   const double pap_d = sum_partials(red + R_PAP_D * RED_MAX, gridDim.x, sh);
+   const double pap_p = sum_partials(red + R_PAP_P * RED_MAX, gridDim.x, sh);
+   if (threadIdx.x == 0) {
+      scal[S_A_D] = pap_d == 0 ? 0.0 : scal[S_SUM_D] / pap_d;
+      scal[S_A_P] = pap_p == 0 ? 0.0 : scal[S_SUM_P] / pap_p;
+   }
 }
 
-// a = s / p.Ap; u += a p; r -= a Ap; records s for the b step
-__global__ void k_pcg_p2(VecArgs A, const double* __restrict__ red, double* __restrict__ scal,
-   float* __restrict__ uind, const float* __restrict__ conj, float* __restrict__ rsd, const float* __restrict__ vec)
+// u += a p; r -= a Ap
+__global__ void k_pcg_p2(VecArgs A, const double* __restrict__ scal, float* __restrict__ uind,
+   const float* __restrict__ conj, float* __restrict__ rsd, const float* __restrict__ vec)
 {
-   __shared__ double sh[40];
-   const double pap_d = finalize(red + R_PAP_D * RED_MAX, A.nb, sh);
-   const double pap_p = finalize(red + R_PAP_P * RED_MAX, A.nb, sh);
-   const double sum_d = finalize(red + R_RZ_D * RED_MAX, A.nb, sh);
-   const double sum_p = finalize(red + R_RZ_P * RED_MAX, A.nb, sh);
-   if (blockIdx.x == 0 && threadIdx.x == 0) {
-      scal[S_SUM_D] = sum_d;
-      scal[S_SUM_P] = sum_p;
-   }
-   const float a = pap_d == 0 ? 0.f : (float)(sum_d / pap_d);
-   const float ap = pap_p == 0 ? 0.f : (float)(sum_p / pap_p);
+   const float a = (float)scal[S_A_D], ap = (float)scal[S_A_P];
    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.ne; e += gridDim.x * blockDim.x) {
       const float g = e % 6 < 3 ? a : ap;
       uind[e] += g * conj[e];
@@ -203,58 +265,36 @@ __global__ void k_pcg_p2(VecArgs A, const double* __restrict__ red, double* __re
    }
 }
 
-// b = s1/s; p = z + b p; convergence test; peek on the last iteration
-__global__ void k_pcg_p4(VecArgs A, const double* __restrict__ red, double* __restrict__ scal,
-   int* __restrict__ state, float* __restrict__ conj, const float* __restrict__ zrsd, float* __restrict__ uind,
-   const float* __restrict__ rsd, int n, double debye, double poleps, int politer, int miniter, float pcgpeek)
+// p = z + b p; peek on the last iteration
+__global__ void k_pcg_p4(VecArgs A, const double* __restrict__ scal, const int* __restrict__ state,
+   float* __restrict__ conj, const float* __restrict__ zrsd, float* __restrict__ uind, const float* __restrict__ rsd,
+   float pcgpeek)
 {
-   __shared__ double sh[40];
-   const double s1_d = finalize(red + R_RZ_D * RED_MAX, A.nb, sh);
-   const double s1_p = finalize(red + R_RZ_P * RED_MAX, A.nb, sh);
-   const double rr_d = finalize(red + R_RR_D * RED_MAX, A.nb, sh);
-   const double rr_p = finalize(red + R_RR_P * RED_MAX, A.nb, sh);
-   const double s_d = scal[S_SUM_D], s_p = scal[S_SUM_P];
-   const float b = s_d == 0 ? 0.f : (float)(s1_d / s_d);
-   const float bp = s_p == 0 ? 0.f : (float)(s1_p / s_p);
-   const double eps = debye * sqrt(fmax(rr_d, rr_p) / n);
-   const int iter = state[ST_ITER];
-   bool done = eps < poleps;
-   if (iter < miniter)
-      done = false;
-   if (iter >= politer)
-      done = true;
-   if (!(eps == eps))  // NaN: stop and report
-      done = true;
+   const float b = (float)scal[S_B_D], bp = (float)scal[S_B_P];
+   const bool done = state[ST_DONE] != 0;
    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.ne; e += gridDim.x * blockDim.x) {
       const float g = e % 6 < 3 ? b : bp;
       conj[e] = zrsd[e] + g * conj[e];
       if (done)
          uind[e] += pcgpeek * A.polar[e / 6] * rsd[e];
    }
-   if (blockIdx.x == 0 && threadIdx.x == 0) {
-      scal[S_EPS] = eps;
-      state[ST_DONE] = done ? 1 : 0;
-      int st = T9GB_OK;
-      if (!(eps == eps))
-         st = T9GB_NAN_DETECTED;
-      else if (done && !(eps < poleps))
-         st = T9GB_NOT_CONVERGED;
-      state[ST_STATUS] = st;
-   }
 }
 
-__global__ void k_reset_state(int* state, double* scal)
+// predictor ring save (ulspredSave, src/amoeba/induce.cpp:29-63)
+__global__ void k_save_hist(int ne, const float* __restrict__ uind, float* __restrict__ hist, int* __restrict__ state)
 {
-   state[ST_ITER] = 0;
-   state[ST_DONE] = 0;
-   state[ST_STATUS] = 0;
-   scal[S_EPS] = 0;
-}
-
-__global__ void k_copy(int ne, const float* __restrict__ src, float* __restrict__ dst)
-{
+   const int slot = state[ST_NUALT] % 16;
+   float* dst = hist + (size_t)slot * ne;
    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ne; i += gridDim.x * blockDim.x)
-      dst[i] = src[i];
+      dst[i] = uind[i];
+}
+
+__global__ void k_bump_nualt(int* state)
+{
+   int v = state[ST_NUALT] + 1;
+   if (v > 32)
+      v -= 16;
+   state[ST_NUALT] = v;
 }
 
 // ---------------------------------------------------------------------------
@@ -270,19 +310,22 @@ static VecArgs vec_args(const Context* ctx)
    return A;
 }
 
-// neighbour list for the current coordinates; overflow is checked after the
-// caller's final synchronisation (check_list_overflow)
-static int ensure_list(Context* ctx)
+static int list_now(Context* ctx)
 {
-   if (!ctx->list_stale)
-      return T9GB_OK;
    T9_CHECK(list_update(ctx));
    T9_CUDA(cudaMemcpyAsync(ctx->h_over, ctx->nbr_over, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
    return T9GB_OK;
 }
 
-// after a synchronisation: grow the list if any atom had more neighbours
-// than the row capacity; returns 1 when the caller must redo its work
+static int ensure_list(Context* ctx)
+{
+   if (!ctx->list_stale)
+      return T9GB_OK;
+   return list_now(ctx);
+}
+
+// after a synchronisation: grow the list if an atom had more neighbours than
+// the row capacity; *redo = 1 when the caller must repeat its work
 static int check_list_overflow(Context* ctx, int* redo)
 {
    *redo = 0;
@@ -296,6 +339,10 @@ static int check_list_overflow(Context* ctx, int* redo)
    *ctx->h_over = 0;
    T9_CUDA(cudaMemset(ctx->nbr_over, 0, sizeof(int)));
    ctx->list_stale = true;
+   if (ctx->graph_exec) {
+      cudaGraphExecDestroy(ctx->graph_exec);
+      ctx->graph_exec = nullptr;
+   }
    *redo = 1;
    return T9GB_OK;
 }
@@ -314,101 +361,184 @@ static int dfield6(Context* ctx, float* out6)
    return T9GB_OK;
 }
 
-// ASPC extrapolation weights (Kolafa, J. Comput. Chem. 25, 335 (2004)); the
-// reference tabulates them in src/cu/upredict.cu:40-55.
-static const double ASPC[16] = {62. / 17., -310. / 51., 2170. / 323., -2329. / 400., 1701. / 409., -806. / 323.,
-   1024. / 809., -479. / 883., 257. / 1316., -434. / 7429., 191. / 13375., -62. / 22287., 3. / 7217.,
-   -3. / 67015., 2. / 646323., -1. / 9694845.};
-
-static int pcg_body(Context* ctx, const VecArgs& A)
+static int pcg_body(Context* ctx, const VecArgs& A, cudaGraphConditionalHandle handle, int use_handle)
 {
    const t9gb_config& c = ctx->cfg;
    T9_CHECK(ufield6(ctx, ctx->conj, ctx->fld6));
    prof_begin(ctx, P_VECTOR);
-   k_pcg_p1<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->fld6, ctx->conj, ctx->vec, ctx->red, ctx->status);
-   k_pcg_p2<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->red, ctx->scal, ctx->uind, ctx->conj, ctx->rsd, ctx->vec);
+   k_pcg_p1<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->fld6, ctx->conj, ctx->vec, ctx->red, ctx->scal, ctx->status);
+   k_pcg_p2<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->scal, ctx->uind, ctx->conj, ctx->rsd, ctx->vec);
    prof_end(ctx);
    if (A.sparse)
       T9_CHECK(launch_precond_sparse(ctx, ctx->rsd, ctx->zrsd));
-   const int miniter = std::min(3, ctx->n);
    prof_begin(ctx, P_VECTOR);
-   k_precond_dot<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->rsd, ctx->zrsd, ctx->conj, ctx->red, 0);
-   k_pcg_p4<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->red, ctx->scal, ctx->status, ctx->conj, ctx->zrsd, ctx->uind,
-      ctx->rsd, ctx->n, c.debye, c.poleps, c.politer, miniter, (float)c.pcgpeek);
+   k_precond_dot<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->rsd, ctx->zrsd, ctx->conj, ctx->red, ctx->scal, ctx->status,
+      0, ctx->n, c.debye, c.poleps, c.politer, std::min(3, ctx->n), handle, use_handle);
+   k_pcg_p4<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->scal, ctx->status, ctx->conj, ctx->zrsd, ctx->uind, ctx->rsd,
+      (float)c.pcgpeek);
    prof_end(ctx);
    T9_CUDA(cudaGetLastError());
    return T9GB_OK;
 }
 
-// dfield, guess, r0 and M r0: everything before the loop
-static int pcg_start(Context* ctx, const VecArgs& A)
+// neighbour list, permanent field, guess, r0, M r0 and s = r.z
+static int pcg_start(Context* ctx, const VecArgs& A, bool graph)
 {
    const t9gb_config& c = ctx->cfg;
-   int guess = c.pcgguess ? 1 : 0;
-   if (c.predictor == 1 && ctx->nualt >= 16) {
-      guess = 2;
-      double coef[16];
-      for (int s = 0; s < 16; ++s)
-         coef[s] = ASPC[((ctx->nualt - 1 - s) % 16 + 16) % 16];
-      for (int s = 0; s < 16; ++s)
-         ctx->h_scal[S_COEF + s] = coef[s];
-      T9_CUDA(cudaMemcpyAsync(ctx->scal + S_COEF, ctx->h_scal + S_COEF, sizeof(double) * 16, cudaMemcpyHostToDevice,
-         ctx->stream));
-   }
-   k_reset_state<<<1, 1, 0, ctx->stream>>>(ctx->status, ctx->scal);
-   T9_CHECK(ensure_list(ctx));
+   T9_CHECK(graph ? list_now(ctx) : ensure_list(ctx));
    T9_CHECK(dfield6(ctx, ctx->fld6));
-   k_init_guess<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->fld6, ctx->efield, ctx->udir, ctx->uind, guess,
-      ctx->aspc_hist, ctx->scal + S_COEF);
-   if (guess != 0)
+   k_init_guess<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->fld6, ctx->efield, ctx->udir, ctx->uind, c.pcgguess,
+      c.predictor == 1 ? 1 : 0, ctx->aspc_hist, ctx->status);
+   const bool zero_guess = !c.pcgguess && c.predictor != 1;
+   if (!zero_guess)
       T9_CHECK(ufield6(ctx, ctx->uind, ctx->fld6));
-   k_init_rsd<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->fld6, ctx->efield, ctx->udir, ctx->uind, ctx->rsd, guess);
+   k_init_rsd<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->fld6, ctx->efield, ctx->udir, ctx->uind, ctx->rsd,
+      zero_guess ? 1 : 0);
    if (A.sparse)
       T9_CHECK(launch_precond_sparse(ctx, ctx->rsd, ctx->zrsd));
-   k_precond_dot<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->rsd, ctx->zrsd, ctx->conj, ctx->red, 1);
+   k_precond_dot<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->rsd, ctx->zrsd, ctx->conj, ctx->red, ctx->scal, ctx->status,
+      1, ctx->n, c.debye, c.poleps, c.politer, 3, 0, 0);
    T9_CUDA(cudaGetLastError());
    return T9GB_OK;
 }
 
-static int induce_once(Context* ctx)
+static int pcg_finish(Context* ctx, const VecArgs& A)
+{
+   if (ctx->cfg.predictor == 1) {
+      k_save_hist<<<A.nb, VB, 0, ctx->stream>>>(A.ne, ctx->uind, ctx->aspc_hist, ctx->status);
+      k_bump_nualt<<<1, 1, 0, ctx->stream>>>(ctx->status);
+   }
+   T9_CUDA(cudaMemcpyAsync(ctx->h_status, ctx->status, sizeof(int) * ST_NSTAT, cudaMemcpyDeviceToHost, ctx->stream));
+   T9_CUDA(cudaMemcpyAsync(ctx->h_scal, ctx->scal, sizeof(double) * S_NSCAL, cudaMemcpyDeviceToHost, ctx->stream));
+   T9_CUDA(cudaGetLastError());
+   return T9GB_OK;
+}
+
+// host-driven loop (used while profiling: every launch is bracketed)
+static int induce_stepwise(Context* ctx)
 {
    const VecArgs A = vec_args(ctx);
-   T9_CHECK(pcg_start(ctx, A));
+   T9_CHECK(pcg_start(ctx, A, false));
    const int politer = std::max(1, ctx->cfg.politer);
    for (int it = 0; it < politer; ++it) {
-      T9_CHECK(pcg_body(ctx, A));
+      T9_CHECK(pcg_body(ctx, A, 0, 0));
       T9_CUDA(cudaMemcpyAsync(ctx->h_status, ctx->status, sizeof(int) * ST_NSTAT, cudaMemcpyDeviceToHost,
          ctx->stream));
       T9_CUDA(cudaStreamSynchronize(ctx->stream));
       if (ctx->h_status[ST_DONE])
          break;
    }
-   T9_CUDA(cudaMemcpyAsync(ctx->h_scal, ctx->scal, sizeof(double) * S_COEF, cudaMemcpyDeviceToHost, ctx->stream));
+   T9_CHECK(pcg_finish(ctx, A));
    T9_CUDA(cudaStreamSynchronize(ctx->stream));
+   return T9GB_OK;
+}
+
+// capture the whole induce() into one graph with a conditional WHILE loop
+static int induce_capture(Context* ctx)
+{
+   const VecArgs A = vec_args(ctx);
+   cudaStream_t s0 = ctx->stream;
+   if (!ctx->cap_stream)
+      T9_CUDA(cudaStreamCreateWithFlags(&ctx->cap_stream, cudaStreamNonBlocking));
+   cudaGraph_t graph = nullptr;
+   T9_CUDA(cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal));
+   int rc = pcg_start(ctx, A, true);
+   cudaStreamCaptureStatus cs;
+   cudaGraph_t cap = nullptr;
+   const cudaGraphNode_t* deps = nullptr;
+   size_t ndeps = 0;
+   cudaGraphConditionalHandle handle = 0;
+   cudaGraphNode_t cnode = nullptr;
+   cudaGraphNodeParams cp = {};
+   if (rc == T9GB_OK && cudaStreamGetCaptureInfo(s0, &cs, nullptr, &cap, &deps, nullptr, &ndeps) != cudaSuccess)
+      rc = T9GB_CUDA_ERR;
+   if (rc == T9GB_OK && cudaGraphConditionalHandleCreate(&handle, cap, 1, cudaGraphCondAssignDefault) != cudaSuccess)
+      rc = T9GB_CUDA_ERR;
+   if (rc == T9GB_OK) {
+      cp.type = cudaGraphNodeTypeConditional;
+      cp.conditional.handle = handle;
+      cp.conditional.type = cudaGraphCondTypeWhile;
+      cp.conditional.size = 1;
+      if (cudaGraphAddNode(&cnode, cap, deps, nullptr, ndeps, &cp) != cudaSuccess)
+         rc = T9GB_CUDA_ERR;
+   }
+   if (rc == T9GB_OK && cudaStreamUpdateCaptureDependencies(s0, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies)
+         != cudaSuccess)
+      rc = T9GB_CUDA_ERR;
+   if (rc == T9GB_OK) {
+      cudaGraph_t body = cp.conditional.phGraph_out[0];
+      if (cudaStreamBeginCaptureToGraph(ctx->cap_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)
+         != cudaSuccess)
+         rc = T9GB_CUDA_ERR;
+      if (rc == T9GB_OK) {
+         ctx->stream = ctx->cap_stream;
+         rc = pcg_body(ctx, A, handle, 1);
+         ctx->stream = s0;
+         cudaGraph_t tmp = nullptr;
+         if (cudaStreamEndCapture(ctx->cap_stream, &tmp) != cudaSuccess && rc == T9GB_OK)
+            rc = T9GB_CUDA_ERR;
+      }
+   }
+   if (rc == T9GB_OK)
+      rc = pcg_finish(ctx, A);
+   cudaError_t e = cudaStreamEndCapture(s0, &graph);
+   if (rc == T9GB_OK && e != cudaSuccess) {
+      ctx->last_error = std::string("graph capture: ") + cudaGetErrorString(e);
+      rc = T9GB_CUDA_ERR;
+   }
+   if (rc == T9GB_OK) {
+      e = cudaGraphInstantiate(&ctx->graph_exec, graph, 0);
+      if (e != cudaSuccess) {
+         ctx->last_error = std::string("graph instantiate: ") + cudaGetErrorString(e);
+         rc = T9GB_CUDA_ERR;
+         ctx->graph_exec = nullptr;
+      }
+   }
+   if (graph)
+      cudaGraphDestroy(graph);
+   cudaGetLastError();
+   // the FFT plan was bound to the capture stream during the body
+   cufftSetStream(ctx->pme.plan, ctx->stream);
+   return rc;
+}
+
+static int induce_graph(Context* ctx)
+{
+   if (!ctx->graph_exec)
+      T9_CHECK(induce_capture(ctx));
+   T9_CUDA(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+   T9_CUDA(cudaStreamSynchronize(ctx->stream));
+   ctx->list_stale = false;
    return T9GB_OK;
 }
 
 int induce_sorted(Context* ctx)
 {
-   int redo = 0;
-   T9_CHECK(induce_once(ctx));
-   T9_CHECK(check_list_overflow(ctx, &redo));
-   if (redo)
-      T9_CHECK(induce_once(ctx));
-   // predictor history (ulspredSave, src/amoeba/induce.cpp:29-63)
-   if (ctx->cfg.predictor == 1) {
-      float* dst = ctx->aspc_hist + (size_t)(ctx->nualt % 16) * 6 * ctx->npad;
-      k_copy<<<grid_for(6 * ctx->npad, 256), 256, 0, ctx->stream>>>(6 * ctx->npad, ctx->uind, dst);
-      T9_CUDA(cudaGetLastError());
-      ctx->nualt += 1;
-      if (ctx->nualt > 32)
-         ctx->nualt -= 16;
+   const bool graph = ctx->use_graph && !ctx->prof.on;
+   for (int attempt = 0; attempt < 2; ++attempt) {
+      T9_CHECK(graph ? induce_graph(ctx) : induce_stepwise(ctx));
+      int redo = 0;
+      T9_CHECK(check_list_overflow(ctx, &redo));
+      if (!redo)
+         break;
+      // the overflowed solve saved a history frame: drop it
+      if (ctx->cfg.predictor == 1) {
+         T9_CUDA(cudaMemcpy(ctx->h_status, ctx->status, sizeof(int) * ST_NSTAT, cudaMemcpyDeviceToHost));
+         int v = ctx->h_status[ST_NUALT] - 1;
+         T9_CUDA(cudaMemcpy(ctx->status + ST_NUALT, &v, sizeof(int), cudaMemcpyHostToDevice));
+      }
    }
    prof_collect(ctx);
    ctx->last_iter = ctx->h_status[ST_ITER];
    ctx->last_eps = ctx->h_scal[S_EPS];
    ctx->last_status = ctx->h_status[ST_STATUS];
    return ctx->last_status;
+}
+
+int reset_predictor(Context* ctx)
+{
+   T9_CUDA(cudaMemsetAsync(ctx->status + ST_NUALT, 0, sizeof(int), ctx->stream));
+   return T9GB_OK;
 }
 
 // ---------------------------------------------------------------------------
