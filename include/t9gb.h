@@ -35,6 +35,7 @@ extern "C" {
 #define T9GB_CUDA_ERR 4
 #define T9GB_NO_DEVICE 5
 #define T9GB_NOT_READY 6 /* topology / positions / list missing */
+#define T9GB_TOO_LARGE 7 /* more atoms than a fixed-capacity entry point holds */
 
 typedef struct t9gb_context t9gb_context;
 
@@ -141,6 +142,27 @@ int t9gb_use_graph(t9gb_context* ctx, int enable);
  * directions) and scaled pairs (the reference's Spatial::nakpl/niak,
  * include/ff/spatial.h:15-140). */
 int t9gb_nblist_stats(t9gb_context* ctx, int* capacity, long long* entries, int* nscaled);
+
+/* Mutual field without any allocation.  No counterpart in the reference: it
+ * is for callers that may not call cudaMalloc when they need the field --
+ * hosts that own every device allocation, code running inside a CUDA-graph
+ * stream capture, real-time loops that forbid allocator calls after
+ * start-up.  Inputs and outputs are the caller's device arrays (xyz, uind,
+ * uinp, field, fieldp [n][3]; pdamp, thole [n]); the working memory is a
+ * static device array inside the library sized for
+ * T9GB_NOALLOC_MAX_ATOMS atoms (384 KiB, held by every GPU that loads the
+ * library until the process exits).  It computes the damped (non-Ewald)
+ * field -T u of pairs within `cutoff` (minimum image when box != NULL has
+ * three positive edges), all mutual scales 1, like t9gb_ufield on a context
+ * with use_ewald = 0.  n > T9GB_NOALLOC_MAX_ATOMS returns T9GB_TOO_LARGE.
+ * The first call on each device looks up the array's address
+ * (cudaGetSymbolAddress) and should therefore happen before any stream
+ * capture.  Every call reuses the same array: calls that can overlap on the
+ * GPU (different streams, no ordering between them) race. */
+#define T9GB_NOALLOC_MAX_ATOMS 8192
+int t9gb_ufield_noalloc(int n, const double* box, double cutoff, const float* xyz_device, const float* pdamp_device,
+   const float* thole_device, const float* uind_device, const float* uinp_device, float* field_device,
+   float* fieldp_device, void* stream);
 
 /* Tracing: per-kernel CUDA-event timing of every launch of the listed
  * categories (the reference has only cudaProfilerStart/Stop,

@@ -16,6 +16,8 @@ from .units import DEBYE, ELECTRIC
 LIB_PATH = _build.LIB
 
 T9GB_OK, T9GB_NOT_CONVERGED, T9GB_NAN_DETECTED, T9GB_BAD_ARG, T9GB_CUDA_ERR, T9GB_NO_DEVICE, T9GB_NOT_READY = range(7)
+T9GB_TOO_LARGE = 7
+T9GB_NOALLOC_MAX_ATOMS = 8192
 
 # every symbol include/t9gb.h declares
 EXPORTS = [
@@ -23,6 +25,7 @@ EXPORTS = [
     "t9gb_set_topology", "t9gb_set_xyz_host", "t9gb_set_xyz_device", "t9gb_nblist_build", "t9gb_mpole_init",
     "t9gb_dfield", "t9gb_ufield", "t9gb_sparse_precond_apply", "t9gb_induce", "t9gb_induce_host",
     "t9gb_induce_stats", "t9gb_get_udir", "t9gb_use_graph", "t9gb_nblist_stats", "t9gb_profile_enable", "t9gb_profile_read", "t9gb_profile_name",
+    "t9gb_ufield_noalloc",
 ]
 
 
@@ -95,6 +98,7 @@ def load(path=None):
     lib.t9gb_profile_read.argtypes = [vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_longlong), C.c_int]
     lib.t9gb_profile_name.argtypes = [C.c_int]
     lib.t9gb_profile_name.restype = C.c_char_p
+    lib.t9gb_ufield_noalloc.argtypes = [C.c_int, dp, C.c_double, fp, fp, fp, fp, fp, fp, fp, vp]
     _lib = lib
     return lib
 

@@ -109,6 +109,8 @@ const char* t9gb_status_string(int status)
       return "no CUDA device";
    case T9GB_NOT_READY:
       return "topology, coordinates or neighbour list missing";
+   case T9GB_TOO_LARGE:
+      return "more atoms than the fixed-capacity entry point holds";
    default:
       return "unknown status";
    }
