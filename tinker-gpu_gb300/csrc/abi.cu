@@ -30,7 +30,8 @@ static int alloc_all(Context* ctx)
    T9_CUDA(cudaMalloc(&ctx->spolar, sizeof(float) * npad));
    T9_CUDA(cudaMalloc(&ctx->spolinv, sizeof(float) * npad));
    T9_CUDA(cudaMalloc(&ctx->sdamp, sizeof(float2) * npad));
-   T9_CUDA(cudaMalloc(&ctx->srpole, sizeof(float) * 10 * npad));
+   T9_CUDA(cudaMalloc(&ctx->srpole, sizeof(float) * 12 * npad));
+   T9_CUDA(cudaMemset(ctx->srpole, 0, sizeof(float) * 12 * npad));
    T9_CUDA(cudaMalloc(&ctx->nnbr, sizeof(int) * npad));
    T9_CUDA(cudaMemset(ctx->nnbr, 0, sizeof(int) * npad));
    T9_CUDA(cudaMalloc(&ctx->nbr_over, sizeof(int)));
@@ -42,8 +43,8 @@ static int alloc_all(Context* ctx)
    float** v6[] = {&ctx->rcp6, &ctx->fld6, &ctx->udir, &ctx->efield, &ctx->uind, &ctx->rsd, &ctx->zrsd,
       &ctx->conj, &ctx->vec, &ctx->tmp6};
    for (float** p : v6) {
-      T9_CUDA(cudaMalloc(p, sizeof(float) * 6 * npad));
-      T9_CUDA(cudaMemset(*p, 0, sizeof(float) * 6 * npad));
+      T9_CUDA(cudaMalloc(p, sizeof(float) * 8 * npad));
+      T9_CUDA(cudaMemset(*p, 0, sizeof(float) * 8 * npad));
    }
    T9_CUDA(cudaMalloc(&ctx->red, sizeof(double) * RED_SLOTS * RED_MAX));
    T9_CUDA(cudaMalloc(&ctx->scal, sizeof(double) * 64));
@@ -53,10 +54,10 @@ static int alloc_all(Context* ctx)
    T9_CUDA(cudaMallocHost(&ctx->h_status, sizeof(int) * 16));
    T9_CUDA(cudaMallocHost(&ctx->h_scal, sizeof(double) * 64));
    if (ctx->cfg.predictor == 1) {
-      T9_CUDA(cudaMalloc(&ctx->aspc_hist, sizeof(float) * 16 * 6 * (size_t)npad));
-      T9_CUDA(cudaMemset(ctx->aspc_hist, 0, sizeof(float) * 16 * 6 * (size_t)npad));
+      T9_CUDA(cudaMalloc(&ctx->aspc_hist, sizeof(float) * 16 * 8 * (size_t)npad));
+      T9_CUDA(cudaMemset(ctx->aspc_hist, 0, sizeof(float) * 16 * 8 * (size_t)npad));
    }
-   ctx->h_stage_bytes = sizeof(float) * 6 * (size_t)npad;
+   ctx->h_stage_bytes = sizeof(float) * 8 * (size_t)npad;
    T9_CUDA(cudaMallocHost(&ctx->h_stage, ctx->h_stage_bytes));
    return T9GB_OK;
 }
@@ -354,8 +355,9 @@ int t9gb_induce_host(t9gb_context* h, const double* xyz, double* uind, double* u
       return st;
    const int n = ctx->n;
    // dipoles to caller order in the scratch vector, then one D2H copy
-   T9_CHECK(scatter_from_sorted3(ctx, ctx->uind, ctx->tmp6, ctx->tmp6 + 3 * n));
-   T9_CUDA(cudaMemcpyAsync(ctx->h_stage, ctx->tmp6, sizeof(float) * 6 * n, cudaMemcpyDeviceToHost, ctx->stream));
+   // (vec is scratch here; it is never read as a neighbour row)
+   T9_CHECK(scatter_from_sorted3(ctx, ctx->uind, ctx->vec, ctx->vec + 3 * n));
+   T9_CUDA(cudaMemcpyAsync(ctx->h_stage, ctx->vec, sizeof(float) * 6 * n, cudaMemcpyDeviceToHost, ctx->stream));
    T9_CUDA(cudaStreamSynchronize(ctx->stream));
    for (int i = 0; i < 3 * n; ++i) {
       if (uind)

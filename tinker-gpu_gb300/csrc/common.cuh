@@ -103,7 +103,7 @@ struct Context {
    float* spolar = nullptr;  // [npad] polarizability (0 on padding)
    float* spolinv = nullptr; // [npad] 1/max(alpha, 1e-16)
    float2* sdamp = nullptr;  // [npad] pdamp, thole
-   float* srpole = nullptr;  // [npad][10] global-frame multipoles
+   float* srpole = nullptr;  // [npad][12] global-frame multipoles, thole, polarizability
 
    // scaled partners of every slot, both directions (CSR over slots)
    int* sp_start = nullptr;  // [npad + 1]
@@ -130,7 +130,8 @@ struct Context {
    // PME
    PmeGrid pme;
 
-   // fields and PCG work, all sorted [npad][6]: d xyz, p xyz
+   // fields and PCG work, all sorted rows of 8 floats: d xyz, p xyz, thole,
+   // polarizability (32-byte rows; components 6-7 are set once per order)
    float* rcp6 = nullptr;   // reciprocal + self field
    float* fld6 = nullptr;   // total field of the last dfield/ufield
    float* udir = nullptr;
@@ -224,6 +225,7 @@ int list_update(Context* ctx);  // device: exact neighbour list
 int scatter_positions(Context* ctx);
 int rotpole_sorted(Context* ctx);
 int reset_predictor(Context* ctx);
+int fill_row_padding(Context* ctx);
 int pme_setup(Context* ctx);
 void pme_free(Context* ctx);
 

@@ -196,6 +196,7 @@ int order_build(Context* ctx)
       T9_CUDA(cudaMalloc(&ctx->nbr, sizeof(int) * (size_t)npad * cap));
       ctx->nbr_cap = cap;
    }
+   T9_CHECK(fill_row_padding(ctx));
    ctx->have_order = true;
    ctx->list_stale = true;
    if (ctx->graph_exec) {
@@ -204,6 +205,27 @@ int order_build(Context* ctx)
    }
    // a new order invalidates the predictor history
    return reset_predictor(ctx);
+}
+
+// Components 6 and 7 of every [npad][8] vector row hold the slot's thole and
+// polarizability, so a neighbour's whole row is one 32-byte load.
+__global__ void k_fill_pad(int npad, const float2* __restrict__ sdamp, const float* __restrict__ spolar,
+   float* __restrict__ a)
+{
+   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < npad; s += gridDim.x * blockDim.x) {
+      a[8 * s + 6] = sdamp[s].y;
+      a[8 * s + 7] = spolar[s];
+   }
+}
+
+int fill_row_padding(Context* ctx)
+{
+   float* rows[] = {ctx->rcp6, ctx->fld6, ctx->udir, ctx->efield, ctx->uind, ctx->rsd, ctx->zrsd, ctx->conj,
+      ctx->vec, ctx->tmp6};
+   for (float* a : rows)
+      k_fill_pad<<<grid_for(ctx->npad, 256), 256, 0, ctx->stream>>>(ctx->npad, ctx->sdamp, ctx->spolar, a);
+   T9_CUDA(cudaGetLastError());
+   return T9GB_OK;
 }
 
 // ---------------------------------------------------------------------------
@@ -522,28 +544,31 @@ int list_update(Context* ctx)
 // ---------------------------------------------------------------------------
 // positions and permutations
 
+// sorted positions, w = pdamp (read with the position by every pair kernel)
 __global__ void k_scatter_pos(int npad, const int* __restrict__ perm, const float* __restrict__ xyz,
-   float4* __restrict__ spos)
+   const float2* __restrict__ sdamp, float4* __restrict__ spos)
 {
    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < npad; s += gridDim.x * blockDim.x) {
       int a = perm[s];
       float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
       if (a >= 0)
-         v = make_float4(xyz[3 * a], xyz[3 * a + 1], xyz[3 * a + 2], 0.f);
+         v = make_float4(xyz[3 * a], xyz[3 * a + 1], xyz[3 * a + 2], sdamp[s].x);
       spos[s] = v;
    }
 }
 
 int scatter_positions(Context* ctx)
 {
-   k_scatter_pos<<<grid_for(ctx->npad, 256), 256, 0, ctx->stream>>>(ctx->npad, ctx->perm, ctx->xyz, ctx->spos);
+   k_scatter_pos<<<grid_for(ctx->npad, 256), 256, 0, ctx->stream>>>(ctx->npad, ctx->perm, ctx->xyz, ctx->sdamp,
+      ctx->spos);
    T9_CUDA(cudaGetLastError());
    ctx->list_stale = true;
    return T9GB_OK;
 }
 
+// caller-order [n][3] pair -> sorted rows of 8 (components 6, 7 untouched)
 __global__ void k_gather6(int npad, const int* __restrict__ perm, const float* __restrict__ a,
-   const float* __restrict__ b, float* __restrict__ s6)
+   const float* __restrict__ b, float* __restrict__ s8)
 {
    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < npad; s += gridDim.x * blockDim.x) {
       int at = perm[s];
@@ -555,7 +580,7 @@ __global__ void k_gather6(int npad, const int* __restrict__ perm, const float* _
          }
       }
       for (int d = 0; d < 6; ++d)
-         s6[6 * s + d] = v[d];
+         s8[8 * s + d] = v[d];
    }
 }
 
@@ -575,9 +600,9 @@ __global__ void k_scatter6(int npad, const int* __restrict__ perm, const float* 
          continue;
       for (int d = 0; d < 3; ++d) {
          if (a)
-            a[3 * at + d] = s6[6 * s + d];
+            a[3 * at + d] = s6[8 * s + d];
          if (b)
-            b[3 * at + d] = s6[6 * s + 3 + d];
+            b[3 * at + d] = s6[8 * s + 3 + d];
       }
    }
 }
@@ -626,17 +651,21 @@ __global__ void k_chkpole(int n, int4* __restrict__ frames, float* __restrict__ 
    }
 }
 
+// rows of 12: q, d xyz, qxx, qyy, qzz, qxy, qxz, qyz, thole, polarizability
 __global__ void k_rotpole(int npad, const int* __restrict__ perm, const int4* __restrict__ frames,
-   const float* __restrict__ pole, const float* __restrict__ xyz, float* __restrict__ rpole)
+   const float* __restrict__ pole, const float* __restrict__ xyz, const float2* __restrict__ sdamp,
+   const float* __restrict__ spolar, float* __restrict__ rpole)
 {
    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < npad; s += gridDim.x * blockDim.x) {
       int i = perm[s];
-      float* rp = rpole + 10 * s;
+      float* rp = rpole + 12 * s;
       if (i < 0) {
-         for (int c = 0; c < 10; ++c)
+         for (int c = 0; c < 12; ++c)
             rp[c] = 0.f;
          continue;
       }
+      rp[10] = sdamp[s].y;
+      rp[11] = spolar[s];
       int4 f = frames[i];
       float a[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
       if (f.w != 0) {
@@ -714,7 +743,7 @@ int rotpole_sorted(Context* ctx)
 {
    k_chkpole<<<grid_for(ctx->n, 256), 256, 0, ctx->stream>>>(ctx->n, ctx->frames, ctx->pole, ctx->xyz);
    k_rotpole<<<grid_for(ctx->npad, 128), 128, 0, ctx->stream>>>(ctx->npad, ctx->perm, ctx->frames, ctx->pole,
-      ctx->xyz, ctx->srpole);
+      ctx->xyz, ctx->sdamp, ctx->spolar, ctx->srpole);
    T9_CUDA(cudaGetLastError());
    return T9GB_OK;
 }

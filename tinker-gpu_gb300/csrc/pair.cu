@@ -72,16 +72,19 @@ __device__ __forceinline__ void group_reduce(float* v)
    }
 }
 
-__device__ __forceinline__ void load6(const float* __restrict__ a, int s, float* v)
+// one 32-byte row: d xyz, p xyz, thole, polarizability
+__device__ __forceinline__ void load8(const float* __restrict__ a, int s, float* v)
 {
-   const float2* p = reinterpret_cast<const float2*>(a + 6 * s);
-   float2 x = p[0], y = p[1], z = p[2];
+   const float4* p = reinterpret_cast<const float4*>(a + 8 * s);
+   const float4 x = p[0], y = p[1];
    v[0] = x.x;
    v[1] = x.y;
-   v[2] = y.x;
-   v[3] = y.y;
-   v[4] = z.x;
-   v[5] = z.y;
+   v[2] = x.z;
+   v[3] = x.w;
+   v[4] = y.x;
+   v[5] = y.y;
+   v[6] = y.z;
+   v[7] = y.w;
 }
 
 __device__ __forceinline__ float pick6(const float* f, int g)
@@ -101,8 +104,8 @@ __device__ __forceinline__ void store6(float* __restrict__ out, const float* __r
    if (g < 6) {
       float v = pick6(f, g);
       if (base)
-         v += base[6 * s + g];
-      out[6 * s + g] = v;
+         v += base[8 * s + g];
+      out[8 * s + g] = v;
    }
 }
 
@@ -142,8 +145,8 @@ __device__ __forceinline__ void ufield_i(const PairParams& P, float r2, float3 d
 template <int G>
 __global__ void __launch_bounds__(256) k_ufield_real(PairParams P, int npad, const int* __restrict__ nbr,
    const int* __restrict__ nnbr, const int* __restrict__ sp_start, const int* __restrict__ sp_j,
-   const float4* __restrict__ sp_sc, const float4* __restrict__ spos, const float* __restrict__ u6,
-   const float2* __restrict__ sdamp, const float* __restrict__ base6, float* __restrict__ out6)
+   const float4* __restrict__ sp_sc, const float4* __restrict__ spos, const float* __restrict__ u8,
+   const float* __restrict__ base8, float* __restrict__ out8)
 {
    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
    const int i = tid / G, g = tid % G;
@@ -151,26 +154,26 @@ __global__ void __launch_bounds__(256) k_ufield_real(PairParams P, int npad, con
       return;
    float f[6] = {0, 0, 0, 0, 0, 0};
    if (i < P.n) {
-      const float4 pi = spos[i];
-      const float2 di = sdamp[i];
+      const float4 pi = spos[i];  // w = pdamp
+      const float pti = u8[8 * i + 6];
       const int* row = nbr + (size_t)i * P.cap;
       const int cnt = nnbr[i];
       int k = g;
-      // two neighbours per trip: both sets of loads are in flight together
+      // two neighbours per trip: both sets of loads are in flight together;
+      // each neighbour is one 16-byte position and one 32-byte row
       for (; k + G < cnt; k += 2 * G) {
          const int j0 = row[k], j1 = row[k + G];
          const float4 p0 = spos[j0], p1 = spos[j1];
-         float u0[6], u1[6];
-         load6(u6, j0, u0);
-         load6(u6, j1, u1);
-         const float2 d0 = sdamp[j0], d1 = sdamp[j1];
+         float u0[8], u1[8];
+         load8(u8, j0, u0);
+         load8(u8, j1, u1);
          const float3 s0 = sep(P, pi, p0), s1 = sep(P, pi, p1);
          const float r0 = s0.x * s0.x + s0.y * s0.y + s0.z * s0.z;
          const float r1 = s1.x * s1.x + s1.y * s1.y + s1.z * s1.z;
          if (r0 <= P.cut2)
-            ufield_i(P, r0, s0, 1.f, di.x, di.y, d0.x, d0.y, u0, f);
+            ufield_i(P, r0, s0, 1.f, pi.w, pti, p0.w, u0[6], u0, f);
          if (r1 <= P.cut2)
-            ufield_i(P, r1, s1, 1.f, di.x, di.y, d1.x, d1.y, u1, f);
+            ufield_i(P, r1, s1, 1.f, pi.w, pti, p1.w, u1[6], u1, f);
       }
       if (k < cnt) {
          const int j = row[k];
@@ -178,10 +181,9 @@ __global__ void __launch_bounds__(256) k_ufield_real(PairParams P, int npad, con
          const float3 d = sep(P, pi, pk);
          const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
          if (r2 <= P.cut2) {
-            float uk[6];
-            load6(u6, j, uk);
-            const float2 dk = sdamp[j];
-            ufield_i(P, r2, d, 1.f, di.x, di.y, dk.x, dk.y, uk, f);
+            float uk[8];
+            load8(u8, j, uk);
+            ufield_i(P, r2, d, 1.f, pi.w, pti, pk.w, uk[6], uk, f);
          }
       }
       const int pa = sp_start[i], pb = sp_start[i + 1];
@@ -191,15 +193,14 @@ __global__ void __launch_bounds__(256) k_ufield_real(PairParams P, int npad, con
          const float3 d = sep(P, pi, pk);
          const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
          if (r2 <= P.cut2) {
-            float uk[6];
-            load6(u6, j, uk);
-            const float2 dk = sdamp[j];
-            ufield_i(P, r2, d, sp_sc[q].w, di.x, di.y, dk.x, dk.y, uk, f);
+            float uk[8];
+            load8(u8, j, uk);
+            ufield_i(P, r2, d, sp_sc[q].w, pi.w, pti, pk.w, uk[6], uk, f);
          }
       }
    }
    group_reduce<G, 6>(f);
-   store6(out6, i < P.n ? base6 : nullptr, i, g, f);
+   store6(out8, i < P.n ? base8 : nullptr, i, g, f);
 }
 
 // ---------------------------------------------------------------------------
@@ -262,14 +263,17 @@ __device__ __forceinline__ void dfield_i(const PairParams& P, float r2, float3 d
    f[5] += fz;
 }
 
-__device__ __forceinline__ void load10(const float* __restrict__ rp, int s, float* m)
+// one 48-byte multipole row: q, d xyz, qxx, qyy, qzz, qxy, qxz, qyz, thole, polarizability
+__device__ __forceinline__ void load12(const float* __restrict__ rp, int s, float* m)
 {
-   const float2* p = reinterpret_cast<const float2*>(rp + 10 * s);
+   const float4* p = reinterpret_cast<const float4*>(rp + 12 * s);
 #pragma unroll
-   for (int c = 0; c < 5; ++c) {
-      float2 v = p[c];
-      m[2 * c] = v.x;
-      m[2 * c + 1] = v.y;
+   for (int c = 0; c < 3; ++c) {
+      const float4 v = p[c];
+      m[4 * c] = v.x;
+      m[4 * c + 1] = v.y;
+      m[4 * c + 2] = v.z;
+      m[4 * c + 3] = v.w;
    }
 }
 
@@ -277,7 +281,7 @@ template <int G>
 __global__ void __launch_bounds__(256) k_dfield_real(PairParams P, int npad, const int* __restrict__ nbr,
    const int* __restrict__ nnbr, const int* __restrict__ sp_start, const int* __restrict__ sp_j,
    const float4* __restrict__ sp_sc, const float4* __restrict__ spos, const float* __restrict__ rp,
-   const float2* __restrict__ sdamp, const float* __restrict__ base6, float* __restrict__ out6)
+   const float* __restrict__ base8, float* __restrict__ out8)
 {
    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
    const int i = tid / G, g = tid % G;
@@ -286,7 +290,7 @@ __global__ void __launch_bounds__(256) k_dfield_real(PairParams P, int npad, con
    float f[6] = {0, 0, 0, 0, 0, 0};
    if (i < P.n) {
       const float4 pi = spos[i];
-      const float2 di = sdamp[i];
+      const float pti = rp[12 * i + 10];
       const int* row = nbr + (size_t)i * P.cap;
       const int cnt = nnbr[i];
       for (int k = g; k < cnt; k += G) {
@@ -295,10 +299,9 @@ __global__ void __launch_bounds__(256) k_dfield_real(PairParams P, int npad, con
          const float3 d = sep(P, pi, pk);
          const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
          if (r2 <= P.cut2) {
-            float mk[10];
-            load10(rp, j, mk);
-            const float2 dk = sdamp[j];
-            dfield_i(P, r2, d, 1.f, 1.f, di.x, di.y, dk.x, dk.y, mk, f);
+            float mk[12];
+            load12(rp, j, mk);
+            dfield_i(P, r2, d, 1.f, 1.f, pi.w, pti, pk.w, mk[10], mk, f);
          }
       }
       const int pa = sp_start[i], pb = sp_start[i + 1];
@@ -308,28 +311,28 @@ __global__ void __launch_bounds__(256) k_dfield_real(PairParams P, int npad, con
          const float3 d = sep(P, pi, pk);
          const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
          if (r2 <= P.cut2) {
-            float mk[10];
-            load10(rp, j, mk);
-            const float2 dk = sdamp[j];
+            float mk[12];
+            load12(rp, j, mk);
             const float4 sc = sp_sc[q];
-            dfield_i(P, r2, d, sc.y, sc.z, di.x, di.y, dk.x, dk.y, mk, f);
+            dfield_i(P, r2, d, sc.y, sc.z, pi.w, pti, pk.w, mk[10], mk, f);
          }
       }
    }
    group_reduce<G, 6>(f);
-   store6(out6, i < P.n ? base6 : nullptr, i, g, f);
+   store6(out8, i < P.n ? base8 : nullptr, i, g, f);
 }
 
 // ---------------------------------------------------------------------------
 // sparse preconditioner: z_i = udiag alpha_i r_i + sum_k alpha_i alpha_k T_ik r_k
 
-__device__ __forceinline__ void precond_i(float r2, float3 d, float us, float poli, float polk, float2 di, float2 dk,
+__device__ __forceinline__ void precond_i(float r2, float3 d, float us, float poli, float pdi, float pti, float pdk,
    const float* rk, float* f)
 {
+   const float polk = rk[7];
    float invr = rsqrtf(r2);
    float r = r2 * invr;
    float s3, s5, s7;
-   thole_damp(r, di.x, di.y, dk.x, dk.y, s3, s5, s7);
+   thole_damp(r, pdi, pti, pdk, rk[6], s3, s5, s7);
    const float polik = poli * polk;
    const float ir3 = invr * invr * invr;
    const float rr3 = us * s3 * polik * ir3;
@@ -348,62 +351,61 @@ template <int G>
 __global__ void __launch_bounds__(256) k_precond_sparse(PairParams P, int npad, float udiag,
    const int* __restrict__ nbr, const int* __restrict__ nnbr, const int* __restrict__ sp_start,
    const int* __restrict__ sp_j, const float4* __restrict__ sp_sc, const float4* __restrict__ spos,
-   const float* __restrict__ r6, const float2* __restrict__ sdamp, const float* __restrict__ spolar,
-   float* __restrict__ z6)
+   const float* __restrict__ r8, float* __restrict__ z8)
 {
    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
    const int i = tid / G, g = tid % G;
    if (i >= npad)
       return;
    float f[6] = {0, 0, 0, 0, 0, 0};
-   const float poli = spolar[i];
+   const float poli = r8[8 * i + 7];
    if (i < P.n) {
       const float4 pi = spos[i];
-      const float2 di = sdamp[i];
+      const float pti = r8[8 * i + 6];
       const int* row = nbr + (size_t)i * P.cap;
       const int cnt = nnbr[i];
       int k = g;
       for (; k + G < cnt; k += 2 * G) {
          const int j0 = row[k], j1 = row[k + G];
          const float4 p0 = spos[j0], p1 = spos[j1];
-         float r0v[6], r1v[6];
-         load6(r6, j0, r0v);
-         load6(r6, j1, r1v);
-         const float2 d0 = sdamp[j0], d1 = sdamp[j1];
-         const float a0 = spolar[j0], a1 = spolar[j1];
+         float r0v[8], r1v[8];
+         load8(r8, j0, r0v);
+         load8(r8, j1, r1v);
          const float3 s0 = sep(P, pi, p0), s1 = sep(P, pi, p1);
          const float q0 = s0.x * s0.x + s0.y * s0.y + s0.z * s0.z;
          const float q1 = s1.x * s1.x + s1.y * s1.y + s1.z * s1.z;
          if (q0 <= P.cut2)
-            precond_i(q0, s0, 1.f, poli, a0, di, d0, r0v, f);
+            precond_i(q0, s0, 1.f, poli, pi.w, pti, p0.w, r0v, f);
          if (q1 <= P.cut2)
-            precond_i(q1, s1, 1.f, poli, a1, di, d1, r1v, f);
+            precond_i(q1, s1, 1.f, poli, pi.w, pti, p1.w, r1v, f);
       }
       if (k < cnt) {
          const int j = row[k];
-         const float3 d = sep(P, pi, spos[j]);
+         const float4 pk = spos[j];
+         const float3 d = sep(P, pi, pk);
          const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
          if (r2 <= P.cut2) {
-            float rk[6];
-            load6(r6, j, rk);
-            precond_i(r2, d, 1.f, poli, spolar[j], di, sdamp[j], rk, f);
+            float rk[8];
+            load8(r8, j, rk);
+            precond_i(r2, d, 1.f, poli, pi.w, pti, pk.w, rk, f);
          }
       }
       const int pa = sp_start[i], pb = sp_start[i + 1];
       for (int q = pa + g; q < pb; q += G) {
          const int j = sp_j[q];
-         const float3 d = sep(P, pi, spos[j]);
+         const float4 pk = spos[j];
+         const float3 d = sep(P, pi, pk);
          const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
          if (r2 <= P.cut2) {
-            float rk[6];
-            load6(r6, j, rk);
-            precond_i(r2, d, sp_sc[q].w, poli, spolar[j], di, sdamp[j], rk, f);
+            float rk[8];
+            load8(r8, j, rk);
+            precond_i(r2, d, sp_sc[q].w, poli, pi.w, pti, pk.w, rk, f);
          }
       }
    }
    group_reduce<G, 6>(f);
    if (g < 6)
-      z6[6 * i + g] = udiag * poli * r6[6 * i + g] + pick6(f, g);
+      z8[8 * i + g] = udiag * poli * r8[8 * i + g] + pick6(f, g);
 }
 
 // ---------------------------------------------------------------------------
@@ -442,7 +444,7 @@ int launch_ufield_real(Context* ctx, const float* u6, const float* base6, float*
    PairParams P = make_params(ctx, ctx->cfg.cutoff);
    prof_begin(ctx, P_UFIELD_REAL);
    k_ufield_real<GROUP><<<grid_for((long long)ctx->npad * GROUP, PAIR_THREADS), PAIR_THREADS, 0, ctx->stream>>>(P,
-      ctx->npad, ctx->nbr, ctx->nnbr, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos, u6, ctx->sdamp, base6, out6);
+      ctx->npad, ctx->nbr, ctx->nnbr, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos, u6, base6, out6);
    prof_end(ctx);
    T9_CUDA(cudaGetLastError());
    return T9GB_OK;
@@ -453,8 +455,7 @@ int launch_dfield_real(Context* ctx, const float* base6, float* out6)
    PairParams P = make_params(ctx, ctx->cfg.cutoff);
    prof_begin(ctx, P_DFIELD_REAL);
    k_dfield_real<GROUP><<<grid_for((long long)ctx->npad * GROUP, PAIR_THREADS), PAIR_THREADS, 0, ctx->stream>>>(P,
-      ctx->npad, ctx->nbr, ctx->nnbr, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos, ctx->srpole, ctx->sdamp, base6,
-      out6);
+      ctx->npad, ctx->nbr, ctx->nnbr, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos, ctx->srpole, base6, out6);
    prof_end(ctx);
    T9_CUDA(cudaGetLastError());
    return T9GB_OK;
@@ -466,8 +467,7 @@ int launch_precond_sparse(Context* ctx, const float* r6, float* z6)
    P.ewald = 0;
    prof_begin(ctx, P_PRECOND);
    k_precond_sparse<GROUP><<<grid_for((long long)ctx->npad * GROUP, PAIR_THREADS), PAIR_THREADS, 0, ctx->stream>>>(P,
-      ctx->npad, (float)ctx->cfg.udiag, ctx->nbr, ctx->nnbr, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos, r6,
-      ctx->sdamp, ctx->spolar, z6);
+      ctx->npad, (float)ctx->cfg.udiag, ctx->nbr, ctx->nnbr, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos, r6, z6);
    prof_end(ctx);
    T9_CUDA(cudaGetLastError());
    return T9GB_OK;

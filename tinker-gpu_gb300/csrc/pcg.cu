@@ -57,13 +57,26 @@ __device__ double block_sum(double v, double* sh)
    return r;  // valid in thread 0
 }
 
-// fixed-order sum of nb partials (valid in thread 0)
-__device__ double sum_partials(const double* part, int nb, double* sh)
+// Fixed-order sums of `ns` (<= 4) consecutive partial slots, computed
+// together: 64 threads per slot stride through the nb partials, then a fixed
+// shuffle tree and one combine (blockDim must be 256).  Returns the sums in
+// out[0..ns) of every thread.
+__device__ void sum_slots(const double* red, int first, int ns, int nb, double* sh, double* out)
 {
+   const int slot = threadIdx.x >> 6, sub = threadIdx.x & 63;
    double v = 0;
-   for (int i = threadIdx.x; i < nb; i += blockDim.x)
-      v += part[i];
-   return block_sum(v, sh);
+   if (slot < ns)
+      for (int i = sub; i < nb; i += 64)
+         v += red[(first + slot) * RED_MAX + i];
+#pragma unroll
+   for (int o = 16; o > 0; o >>= 1)
+      v += __shfl_down_sync(0xffffffffu, v, o);
+   if ((threadIdx.x & 31) == 0)
+      sh[threadIdx.x >> 5] = v;
+   __syncthreads();
+   for (int k = 0; k < ns; ++k)
+      out[k] = sh[2 * k] + sh[2 * k + 1];
+   __syncthreads();
 }
 
 // store this block's partial sum of v
@@ -96,7 +109,8 @@ __device__ bool last_block(int* ticket)
 }
 
 struct VecArgs {
-   int ne;  // 6 * npad elements
+   int ne;   // 6 * npad active elements (d xyz, p xyz of each slot)
+   int ne8;  // 8 * npad floats per vector (rows padded to 32 bytes)
    int nb;  // blocks of every vector kernel
    const float* polar;
    const float* polinv;
@@ -118,21 +132,22 @@ __global__ void k_init_guess(VecArgs A, const float* __restrict__ fld, float* __
       for (int k = 0; k < 16; ++k)
          coef[k] = c_aspc[((nualt - 1 - k) % 16 + 16) % 16];
    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.ne; e += gridDim.x * blockDim.x) {
-      const float pol = A.polar[e / 6];
-      const float f = fld[e];
-      efield[e] = f;
+      const int s = e / 6, x = e + 2 * s;  // row s, component e - 6 s of [npad][8]
+      const float pol = A.polar[s];
+      const float f = fld[x];
+      efield[x] = f;
       const float ud = pol * f;
-      udir[e] = ud;
+      udir[x] = ud;
       float u = 0.f;
       if (predict) {
          double v = 0;
          for (int k = 0; k < 16; ++k)
-            v += coef[k] * (double)hist[(size_t)k * A.ne + e];
+            v += coef[k] * (double)hist[(size_t)k * A.ne8 + x];
          u = (float)v;
       } else if (pcgguess) {
          u = ud;
       }
-      uind[e] = u;
+      uind[x] = u;
    }
 }
 
@@ -142,11 +157,11 @@ __global__ void k_init_rsd(VecArgs A, const float* __restrict__ fld, const float
    const float* __restrict__ udir, const float* __restrict__ uind, float* __restrict__ rsd, int zero_guess)
 {
    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.ne; e += gridDim.x * blockDim.x) {
-      const int s = e / 6;
-      float r = zero_guess ? efield[e] : (udir[e] - uind[e]) * A.polinv[s] + fld[e];
+      const int s = e / 6, x = e + 2 * s;  // row s, component e - 6 s of [npad][8]
+      float r = zero_guess ? efield[x] : (udir[x] - uind[x]) * A.polinv[s] + fld[x];
       if (A.polar[s] == 0.f)
          r = 0.f;
-      rsd[e] = r;
+      rsd[x] = r;
    }
 }
 
@@ -160,17 +175,18 @@ __global__ void k_precond_dot(VecArgs A, const float* __restrict__ rsd, float* _
    __shared__ double sh[40];
    double rz_d = 0, rz_p = 0, rr_d = 0, rr_p = 0;
    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.ne; e += gridDim.x * blockDim.x) {
-      const float r = rsd[e];
+      const int s = e / 6, x = e + 2 * s;  // row s, component e - 6 s of [npad][8]
+      const float r = rsd[x];
       float z;
       if (A.sparse) {
-         z = zrsd[e];
+         z = zrsd[x];
       } else {
-         z = A.polar[e / 6] * r;
-         zrsd[e] = z;
+         z = A.polar[s] * r;
+         zrsd[x] = z;
       }
       if (init)
-         conj[e] = z;
-      if (e % 6 < 3) {
+         conj[x] = z;
+      if (e - 6 * s < 3) {
          rz_d += (double)r * z;
          rr_d += (double)r * r;
       } else {
@@ -184,10 +200,9 @@ __global__ void k_precond_dot(VecArgs A, const float* __restrict__ rsd, float* _
    store_partial(red, R_RR_P, rr_p, sh);
    if (!last_block(state + ST_TICKET0))
       return;
-   const double s1_d = sum_partials(red + R_RZ_D * RED_MAX, gridDim.x, sh);
-   const double s1_p = sum_partials(red + R_RZ_P * RED_MAX, gridDim.x, sh);
-   const double q_d = sum_partials(red + R_RR_D * RED_MAX, gridDim.x, sh);
-   const double q_p = sum_partials(red + R_RR_P * RED_MAX, gridDim.x, sh);
+   double tot[4];
+   sum_slots(red, R_RZ_D, 4, gridDim.x, sh, tot);
+   const double s1_d = tot[0], s1_p = tot[1], q_d = tot[2], q_p = tot[3];
    if (threadIdx.x != 0)
       return;
    if (init) {
@@ -230,10 +245,11 @@ __global__ void k_pcg_p1(VecArgs A, const float* __restrict__ fld, const float* 
    __shared__ double sh[40];
    double dd = 0, dp = 0;
    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.ne; e += gridDim.x * blockDim.x) {
-      const float p = conj[e];
-      const float v = A.polinv[e / 6] * p - fld[e];
-      vec[e] = v;
-      if (e % 6 < 3)
+      const int s = e / 6, x = e + 2 * s;  // row s, component e - 6 s of [npad][8]
+      const float p = conj[x];
+      const float v = A.polinv[s] * p - fld[x];
+      vec[x] = v;
+      if (e - 6 * s < 3)
          dd += (double)p * v;
       else
          dp += (double)p * v;
@@ -242,8 +258,9 @@ __global__ void k_pcg_p1(VecArgs A, const float* __restrict__ fld, const float* 
    store_partial(red, R_PAP_P, dp, sh);
    if (!last_block(state + ST_TICKET1))
       return;
-   const double pap_d = sum_partials(red + R_PAP_D * RED_MAX, gridDim.x, sh);
-   const double pap_p = sum_partials(red + R_PAP_P * RED_MAX, gridDim.x, sh);
+   double tot[2];
+   sum_slots(red, R_PAP_D, 2, gridDim.x, sh, tot);
+   const double pap_d = tot[0], pap_p = tot[1];
    if (threadIdx.x == 0) {
       scal[S_A_D] = pap_d == 0 ? 0.0 : scal[S_SUM_D] / pap_d;
       scal[S_A_P] = pap_p == 0 ? 0.0 : scal[S_SUM_P] / pap_p;
@@ -256,12 +273,13 @@ __global__ void k_pcg_p2(VecArgs A, const double* __restrict__ scal, float* __re
 {
    const float a = (float)scal[S_A_D], ap = (float)scal[S_A_P];
    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.ne; e += gridDim.x * blockDim.x) {
-      const float g = e % 6 < 3 ? a : ap;
-      uind[e] += g * conj[e];
-      float r = rsd[e] - g * vec[e];
-      if (A.polar[e / 6] == 0.f)
+      const int s = e / 6, x = e + 2 * s;  // row s, component e - 6 s of [npad][8]
+      const float g = e - 6 * s < 3 ? a : ap;
+      uind[x] += g * conj[x];
+      float r = rsd[x] - g * vec[x];
+      if (A.polar[s] == 0.f)
          r = 0.f;
-      rsd[e] = r;
+      rsd[x] = r;
    }
 }
 
@@ -273,10 +291,11 @@ __global__ void k_pcg_p4(VecArgs A, const double* __restrict__ scal, const int* 
    const float b = (float)scal[S_B_D], bp = (float)scal[S_B_P];
    const bool done = state[ST_DONE] != 0;
    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.ne; e += gridDim.x * blockDim.x) {
-      const float g = e % 6 < 3 ? b : bp;
-      conj[e] = zrsd[e] + g * conj[e];
+      const int s = e / 6, x = e + 2 * s;  // row s, component e - 6 s of [npad][8]
+      const float g = e - 6 * s < 3 ? b : bp;
+      conj[x] = zrsd[x] + g * conj[x];
       if (done)
-         uind[e] += pcgpeek * A.polar[e / 6] * rsd[e];
+         uind[x] += pcgpeek * A.polar[s] * rsd[x];
    }
 }
 
@@ -303,6 +322,7 @@ static VecArgs vec_args(const Context* ctx)
 {
    VecArgs A;
    A.ne = 6 * ctx->npad;
+   A.ne8 = 8 * ctx->npad;
    A.nb = std::min(RED_MAX, grid_for(A.ne, VB));
    A.polar = ctx->spolar;
    A.polinv = ctx->spolinv;
@@ -405,7 +425,7 @@ static int pcg_start(Context* ctx, const VecArgs& A, bool graph)
 static int pcg_finish(Context* ctx, const VecArgs& A)
 {
    if (ctx->cfg.predictor == 1) {
-      k_save_hist<<<A.nb, VB, 0, ctx->stream>>>(A.ne, ctx->uind, ctx->aspc_hist, ctx->status);
+      k_save_hist<<<A.nb, VB, 0, ctx->stream>>>(A.ne8, ctx->uind, ctx->aspc_hist, ctx->status);
       k_bump_nualt<<<1, 1, 0, ctx->stream>>>(ctx->status);
    }
    T9_CUDA(cudaMemcpyAsync(ctx->h_status, ctx->status, sizeof(int) * ST_NSTAT, cudaMemcpyDeviceToHost, ctx->stream));

@@ -167,90 +167,63 @@ __device__ __forceinline__ void grid_add(unsigned long long* q, size_t idx, floa
       atomicAdd(q + idx, (unsigned long long)to_fx(v));
 }
 
-// spread fractional multipoles (real part)
-__global__ void k_spread_mpole(int n, GridParams G, const float4* __restrict__ spos, const float* __restrict__ rp,
-   unsigned long long* __restrict__ q)
+// Spreading, one warp per atom: lane (jy, kz) < 25 owns one row of five x
+// points.  MODE 0 spreads fractional multipoles into the real part; MODE 1
+// spreads fractional d dipoles into the real and p dipoles into the
+// imaginary part.  rp rows are 12 floats (q, d, quadrupole, ...), u rows 8.
+template <int MODE>
+__global__ void __launch_bounds__(256) k_spread(int n, GridParams G, const float4* __restrict__ spos,
+   const float* __restrict__ src, unsigned long long* __restrict__ q)
 {
-   int s = blockIdx.x * blockDim.x + threadIdx.x;
-   if (s >= n)
+   const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+   const int lane = threadIdx.x & 31;
+   if (s >= n || lane >= 25)
       return;
    int i1, i2, i3;
    float w1, w2, w3;
    site(G, spos[s], i1, i2, i3, w1, w2, w3);
-   float t1[5][3], t2[5][3], t3[5][3];
-   bspline5<3>(w1, t1);
-   bspline5<3>(w2, t2);
-   bspline5<3>(w3, t3);
-   const float* m = rp + 10 * s;
-   // Cartesian -> fractional (orthogonal box; quadrupole off-diagonals doubled)
-   const float f0 = m[0];
-   const float fx = G.a1 * m[1], fy = G.a2 * m[2], fz = G.a3 * m[3];
-   const float fxx = G.a1 * G.a1 * m[4], fyy = G.a2 * G.a2 * m[5], fzz = G.a3 * G.a3 * m[6];
-   const float fxy = 2.f * G.a1 * G.a2 * m[7], fxz = 2.f * G.a1 * G.a3 * m[8], fyz = 2.f * G.a2 * G.a3 * m[9];
-   const int nxy = G.n1 * G.n2;
+   constexpr int L = MODE == 0 ? 3 : 2;
+   float t1[5][L], t2[5][L], t3[5][L];
+   bspline5<L>(w1, t1);
+   bspline5<L>(w2, t2);
+   bspline5<L>(w3, t3);
+   const int jy = lane % 5, kz = lane / 5;
+   int zb = i3 + kz;
+   zb -= (zb >= G.n3 ? G.n3 : 0);
+   int yb = i2 + jy;
+   yb -= (yb >= G.n2 ? G.n2 : 0);
+   const size_t row = ((size_t)zb * G.n2 + yb) * G.n1;
+   const float v0 = t3[kz][0], v1 = t3[kz][1];
+   const float u0 = t2[jy][0], u1 = t2[jy][1];
+   if (MODE == 0) {
+      const float* m = src + 12 * s;
+      // Cartesian -> fractional (orthogonal box; quadrupole off-diagonals doubled)
+      const float f0 = m[0];
+      const float fx = G.a1 * m[1], fy = G.a2 * m[2], fz = G.a3 * m[3];
+      const float fxx = G.a1 * G.a1 * m[4], fyy = G.a2 * G.a2 * m[5], fzz = G.a3 * G.a3 * m[6];
+      const float fxy = 2.f * G.a1 * G.a2 * m[7], fxz = 2.f * G.a1 * G.a3 * m[8], fyz = 2.f * G.a2 * G.a3 * m[9];
+      const float v2 = t3[kz][L - 1], u2 = t2[jy][L - 1];
+      const float term0 = f0 * u0 * v0 + fy * u1 * v0 + fz * u0 * v1 + fyy * u2 * v0 + fzz * u0 * v2 + fyz * u1 * v1;
+      const float term1 = fx * u0 * v0 + fxy * u1 * v0 + fxz * u0 * v1;
+      const float term2 = fxx * u0 * v0;
 #pragma unroll
-   for (int kz = 0; kz < 5; ++kz) {
-      int zb = i3 + kz;
-      zb -= (zb >= G.n3 ? G.n3 : 0);
-      const float v0 = t3[kz][0], v1 = t3[kz][1], v2 = t3[kz][2];
-#pragma unroll
-      for (int jy = 0; jy < 5; ++jy) {
-         int yb = i2 + jy;
-         yb -= (yb >= G.n2 ? G.n2 : 0);
-         const float u0 = t2[jy][0], u1 = t2[jy][1], u2 = t2[jy][2];
-         const float term0 = f0 * u0 * v0 + fy * u1 * v0 + fz * u0 * v1 + fyy * u2 * v0 + fzz * u0 * v2
-            + fyz * u1 * v1;
-         const float term1 = fx * u0 * v0 + fxy * u1 * v0 + fxz * u0 * v1;
-         const float term2 = fxx * u0 * v0;
-         const size_t row = (size_t)zb * nxy + (size_t)yb * G.n1;
-#pragma unroll
-         for (int ix = 0; ix < 5; ++ix) {
-            int xb = i1 + ix;
-            xb -= (xb >= G.n1 ? G.n1 : 0);
-            grid_add(q, 2 * (row + xb), term0 * t1[ix][0] + term1 * t1[ix][1] + term2 * t1[ix][2]);
-         }
+      for (int ix = 0; ix < 5; ++ix) {
+         int xb = i1 + ix;
+         xb -= (xb >= G.n1 ? G.n1 : 0);
+         grid_add(q, 2 * (row + xb), term0 * t1[ix][0] + term1 * t1[ix][1] + term2 * t1[ix][L - 1]);
       }
-   }
-}
-
-// spread fractional induced dipoles: d -> real part, p -> imaginary part
-__global__ void k_spread_uind(int n, GridParams G, const float4* __restrict__ spos, const float* __restrict__ u6,
-   unsigned long long* __restrict__ q)
-{
-   int s = blockIdx.x * blockDim.x + threadIdx.x;
-   if (s >= n)
-      return;
-   int i1, i2, i3;
-   float w1, w2, w3;
-   site(G, spos[s], i1, i2, i3, w1, w2, w3);
-   float t1[5][2], t2[5][2], t3[5][2];
-   bspline5<2>(w1, t1);
-   bspline5<2>(w2, t2);
-   bspline5<2>(w3, t3);
-   const float* u = u6 + 6 * s;
-   const float dx = G.a1 * u[0], dy = G.a2 * u[1], dz = G.a3 * u[2];
-   const float px = G.a1 * u[3], py = G.a2 * u[4], pz = G.a3 * u[5];
-   const int nxy = G.n1 * G.n2;
+   } else {
+      const float* u = src + 8 * s;
+      const float dx = G.a1 * u[0], dy = G.a2 * u[1], dz = G.a3 * u[2];
+      const float px = G.a1 * u[3], py = G.a2 * u[4], pz = G.a3 * u[5];
+      const float d01 = dy * u1 * v0 + dz * u0 * v1, d11 = dx * u0 * v0;
+      const float p01 = py * u1 * v0 + pz * u0 * v1, p11 = px * u0 * v0;
 #pragma unroll
-   for (int kz = 0; kz < 5; ++kz) {
-      int zb = i3 + kz;
-      zb -= (zb >= G.n3 ? G.n3 : 0);
-      const float v0 = t3[kz][0], v1 = t3[kz][1];
-#pragma unroll
-      for (int jy = 0; jy < 5; ++jy) {
-         int yb = i2 + jy;
-         yb -= (yb >= G.n2 ? G.n2 : 0);
-         const float u0 = t2[jy][0], u1 = t2[jy][1];
-         const float d01 = dy * u1 * v0 + dz * u0 * v1, d11 = dx * u0 * v0;
-         const float p01 = py * u1 * v0 + pz * u0 * v1, p11 = px * u0 * v0;
-         const size_t row = (size_t)zb * nxy + (size_t)yb * G.n1;
-#pragma unroll
-         for (int ix = 0; ix < 5; ++ix) {
-            int xb = i1 + ix;
-            xb -= (xb >= G.n1 ? G.n1 : 0);
-            grid_add(q, 2 * (row + xb), d01 * t1[ix][0] + d11 * t1[ix][1]);
-            grid_add(q, 2 * (row + xb) + 1, p01 * t1[ix][0] + p11 * t1[ix][1]);
-         }
+      for (int ix = 0; ix < 5; ++ix) {
+         int xb = i1 + ix;
+         xb -= (xb >= G.n1 ? G.n1 : 0);
+         grid_add(q, 2 * (row + xb), d01 * t1[ix][0] + d11 * t1[ix][1]);
+         grid_add(q, 2 * (row + xb) + 1, p01 * t1[ix][0] + p11 * t1[ix][1]);
       }
    }
 }
@@ -275,75 +248,70 @@ __global__ void k_conv(size_t ng, const float* __restrict__ infl, float2* __rest
    }
 }
 
-// gather first derivatives and store the recip + self field (plain store).
-// MODE 0 (multipoles): real part -> d and p field, self term with the
-// permanent dipole.  MODE 1 (dipoles): real -> d, imaginary -> p, self term
-// with the induced dipoles u6.
+// Gather of the first potential derivatives fused with the recip + self
+// field, one warp per atom: lane (jy, kz) < 25 reads one row of five points,
+// a fixed xor tree combines the rows.  MODE 0: real part -> d and p field,
+// self term with the permanent dipole.  MODE 1: real -> d, imaginary -> p,
+// self term with the induced dipoles.  Plain stores, rows of 8 floats.
 template <int MODE>
-__global__ void k_gather_field(int n, GridParams G, const float4* __restrict__ spos, const float2* __restrict__ g,
-   const float* __restrict__ rp, const float* __restrict__ u6, float* __restrict__ out6)
+__global__ void __launch_bounds__(256) k_gather_field(int n, GridParams G, const float4* __restrict__ spos,
+   const float2* __restrict__ g, const float* __restrict__ rp, const float* __restrict__ u8, float* __restrict__ out)
 {
-   int s = blockIdx.x * blockDim.x + threadIdx.x;
+   const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+   const int lane = threadIdx.x & 31;
    if (s >= n)
       return;
    int i1, i2, i3;
    float w1, w2, w3;
    site(G, spos[s], i1, i2, i3, w1, w2, w3);
-   float t1[5][2], t2[5][2], t3[5][2];
-   bspline5<2>(w1, t1);
-   bspline5<2>(w2, t2);
-   bspline5<2>(w3, t3);
-   float r100 = 0.f, r010 = 0.f, r001 = 0.f, i100 = 0.f, i010 = 0.f, i001 = 0.f;
-   const int nxy = G.n1 * G.n2;
-#pragma unroll
-   for (int kz = 0; kz < 5; ++kz) {
+   float acc[6] = {0, 0, 0, 0, 0, 0};
+   if (lane < 25) {
+      float t1[5][2], t2[5][2], t3[5][2];
+      bspline5<2>(w1, t1);
+      bspline5<2>(w2, t2);
+      bspline5<2>(w3, t3);
+      const int jy = lane % 5, kz = lane / 5;
       int zb = i3 + kz;
       zb -= (zb >= G.n3 ? G.n3 : 0);
-      const float v0 = t3[kz][0], v1 = t3[kz][1];
-      float ru00 = 0.f, ru10 = 0.f, ru01 = 0.f, iu00 = 0.f, iu10 = 0.f, iu01 = 0.f;
+      int yb = i2 + jy;
+      yb -= (yb >= G.n2 ? G.n2 : 0);
+      const size_t row = ((size_t)zb * G.n2 + yb) * G.n1;
+      float rt0 = 0.f, rt1 = 0.f, it0 = 0.f, it1 = 0.f;
 #pragma unroll
-      for (int jy = 0; jy < 5; ++jy) {
-         int yb = i2 + jy;
-         yb -= (yb >= G.n2 ? G.n2 : 0);
-         const float u0 = t2[jy][0], u1 = t2[jy][1];
-         const size_t row = (size_t)zb * nxy + (size_t)yb * G.n1;
-         float rt0 = 0.f, rt1 = 0.f, it0 = 0.f, it1 = 0.f;
-#pragma unroll
-         for (int ix = 0; ix < 5; ++ix) {
-            int xb = i1 + ix;
-            xb -= (xb >= G.n1 ? G.n1 : 0);
-            float2 q = g[row + xb];
-            rt0 += q.x * t1[ix][0];
-            rt1 += q.x * t1[ix][1];
-            if (MODE == 1) {
-               it0 += q.y * t1[ix][0];
-               it1 += q.y * t1[ix][1];
-            }
-         }
-         ru00 += rt0 * u0;
-         ru10 += rt1 * u0;
-         ru01 += rt0 * u1;
+      for (int ix = 0; ix < 5; ++ix) {
+         int xb = i1 + ix;
+         xb -= (xb >= G.n1 ? G.n1 : 0);
+         const float2 qv = g[row + xb];
+         rt0 += qv.x * t1[ix][0];
+         rt1 += qv.x * t1[ix][1];
          if (MODE == 1) {
-            iu00 += it0 * u0;
-            iu10 += it1 * u0;
-            iu01 += it0 * u1;
+            it0 += qv.y * t1[ix][0];
+            it1 += qv.y * t1[ix][1];
          }
       }
-      r100 += ru10 * v0;
-      r010 += ru01 * v0;
-      r001 += ru00 * v1;
+      const float u0 = t2[jy][0], u1 = t2[jy][1], v0 = t3[kz][0], v1 = t3[kz][1];
+      acc[0] = rt1 * u0 * v0;
+      acc[1] = rt0 * u1 * v0;
+      acc[2] = rt0 * u0 * v1;
       if (MODE == 1) {
-         i100 += iu10 * v0;
-         i010 += iu01 * v0;
-         i001 += iu00 * v1;
+         acc[3] = it1 * u0 * v0;
+         acc[4] = it0 * u1 * v0;
+         acc[5] = it0 * u0 * v1;
       }
    }
-   float* a = out6 + 6 * s;
+#pragma unroll
+   for (int c = 0; c < (MODE == 1 ? 6 : 3); ++c)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1)
+         acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
+   if (lane != 0)
+      return;
+   float* a = out + 8 * s;
    if (MODE == 0) {
-      const float* m = rp + 10 * s;
-      const float fx = -G.a1 * r100 + G.selfterm * m[1];
-      const float fy = -G.a2 * r010 + G.selfterm * m[2];
-      const float fz = -G.a3 * r001 + G.selfterm * m[3];
+      const float* m = rp + 12 * s;
+      const float fx = -G.a1 * acc[0] + G.selfterm * m[1];
+      const float fy = -G.a2 * acc[1] + G.selfterm * m[2];
+      const float fz = -G.a3 * acc[2] + G.selfterm * m[3];
       a[0] = fx;
       a[1] = fy;
       a[2] = fz;
@@ -351,13 +319,13 @@ __global__ void k_gather_field(int n, GridParams G, const float4* __restrict__ s
       a[4] = fy;
       a[5] = fz;
    } else {
-      const float* u = u6 + 6 * s;
-      a[0] = G.selfterm * u[0] - G.a1 * r100;
-      a[1] = G.selfterm * u[1] - G.a2 * r010;
-      a[2] = G.selfterm * u[2] - G.a3 * r001;
-      a[3] = G.selfterm * u[3] - G.a1 * i100;
-      a[4] = G.selfterm * u[4] - G.a2 * i010;
-      a[5] = G.selfterm * u[5] - G.a3 * i001;
+      const float* u = u8 + 8 * s;
+      a[0] = G.selfterm * u[0] - G.a1 * acc[0];
+      a[1] = G.selfterm * u[1] - G.a2 * acc[1];
+      a[2] = G.selfterm * u[2] - G.a3 * acc[2];
+      a[3] = G.selfterm * u[3] - G.a1 * acc[3];
+      a[4] = G.selfterm * u[4] - G.a2 * acc[4];
+      a[5] = G.selfterm * u[5] - G.a3 * acc[5];
    }
 }
 
@@ -468,13 +436,13 @@ int launch_dfield_recip(Context* ctx, float* out6)
       return T9GB_OK;
    GridParams G = grid_params(ctx);
    prof_begin(ctx, P_SPREAD_MPOLE);
-   k_spread_mpole<<<grid_for(ctx->n, 128), 128, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->srpole,
+   k_spread<0><<<grid_for((long long)ctx->n * 32, 256), 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->srpole,
       reinterpret_cast<unsigned long long*>(ctx->pme.qfx));
    prof_end(ctx);
    T9_CUDA(cudaGetLastError());
    T9_CHECK(fft_conv(ctx));
    prof_begin(ctx, P_GATHER_MPOLE);
-   k_gather_field<0><<<grid_for(ctx->n, 128), 128, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->pme.qgrid,
+   k_gather_field<0><<<grid_for((long long)ctx->n * 32, 256), 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->pme.qgrid,
       ctx->srpole, nullptr, out6);
    prof_end(ctx);
    T9_CUDA(cudaGetLastError());
@@ -487,13 +455,13 @@ int launch_ufield_recip(Context* ctx, const float* u6, float* out6)
       return T9GB_OK;
    GridParams G = grid_params(ctx);
    prof_begin(ctx, P_SPREAD_UIND);
-   k_spread_uind<<<grid_for(ctx->n, 128), 128, 0, ctx->stream>>>(ctx->n, G, ctx->spos, u6,
+   k_spread<1><<<grid_for((long long)ctx->n * 32, 256), 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, u6,
       reinterpret_cast<unsigned long long*>(ctx->pme.qfx));
    prof_end(ctx);
    T9_CUDA(cudaGetLastError());
    T9_CHECK(fft_conv(ctx));
    prof_begin(ctx, P_GATHER_UIND);
-   k_gather_field<1><<<grid_for(ctx->n, 128), 128, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->pme.qgrid, nullptr,
+   k_gather_field<1><<<grid_for((long long)ctx->n * 32, 256), 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->pme.qgrid, nullptr,
       u6, out6);
    prof_end(ctx);
    T9_CUDA(cudaGetLastError());
