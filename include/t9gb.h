@@ -131,6 +131,19 @@ int t9gb_induce_stats(const t9gb_context* ctx, int* iterations, double* eps_deby
 /* Direct dipoles alpha*E of the last induce/dfield, [n][3] device. */
 int t9gb_get_udir(t9gb_context* ctx, float* udir_device, float* udirp_device);
 
+/* Permanent-multipole energy (kcal/mol) of the current coordinates and
+ * rotated multipoles (call t9gb_mpole_init first): real-space (with the
+ * m-scaled exclusions), reciprocal and Ewald self parts in parts[3] (may be
+ * NULL).  Replaces empole(calc::energy) (src/amoeba/empole.cpp:81-138,
+ * src/cu/amoeba/empole.cu, src/cu/hippo/empole.cu:195-367,
+ * include/seq/emselfamoeba.h). */
+int t9gb_empole_energy(t9gb_context* ctx, double* energy, double* parts);
+
+/* Polarization energy -1/2 f sum_i u_d,i . E_p,i of the last induce (the
+ * dot-product form used for calc::v0).  Replaces epolar0DotProd
+ * (src/cu/amoeba/epolar.cu:14-30, called by src/amoeba/epolar.cpp:550-572). */
+int t9gb_epolar_energy(t9gb_context* ctx, double* energy);
+
 /* Run induce() as one CUDA graph (default, enable = 1: neighbour list,
  * permanent field, guess and the PCG loop as a conditional WHILE node with
  * the convergence test on the device) or as individually launched kernels

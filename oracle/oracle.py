@@ -82,6 +82,10 @@ def lib():
         _lib.or_bsmod.argtypes = [C.c_int, C.c_int, dp]
         _lib.or_bsplgen_export.argtypes = [C.c_double, C.c_int, C.c_int, dp]
         _lib.or_aspc_sum.argtypes = [C.c_int, C.c_int, dp, dp]
+        _lib.or_empole_energy.argtypes = [C.POINTER(OrSystem), dp]
+        _lib.or_empole_energy.restype = C.c_double
+        _lib.or_epolar_energy_dot.argtypes = [C.POINTER(OrSystem), dp, dp]
+        _lib.or_epolar_energy_dot.restype = C.c_double
         _lib.or_set_threads.argtypes = [C.c_int]
         _lib.or_nthreads.restype = C.c_int
     return _lib
@@ -193,6 +197,20 @@ class OracleSystem:
         o = self.opts(guess=guess, **kw)
         it = lib().or_induce(C.byref(self.s), C.byref(o), _dp(uind), _dp(uinp), _dp(udir), _dp(udirp), C.byref(eps))
         return uind, uinp, udir, udirp, it, eps.value
+
+    def empole_energy(self):
+        """(total, [real, recip, self]) permanent-multipole energy, kcal/mol."""
+        parts = np.zeros(3)
+        e = lib().or_empole_energy(C.byref(self.s), _dp(parts))
+        return e, parts
+
+    def epolar_energy(self, uind=None, udirp=None):
+        """Polarization energy by the dot product; solves induce() when no dipoles are given."""
+        if uind is None:
+            uind, _, _, udirp, *_ = self.induce()
+        uind = np.ascontiguousarray(uind, dtype=np.float64)
+        udirp = np.ascontiguousarray(udirp, dtype=np.float64)
+        return lib().or_epolar_energy_dot(C.byref(self.s), _dp(uind), _dp(udirp))
 
     def sparse_precond(self, rsd, rsdp):
         rsd = np.ascontiguousarray(rsd, dtype=np.float64)

@@ -1411,3 +1411,128 @@ double or_pme_energy_uind_check(const or_system* s, const double* fuind, const d
    or_pme_free(&p);
    return 0;
 }
+
+/* ------------------------------------------------------------------ */
+/* energies consuming the multipoles and converged dipoles              */
+
+/* pair_mpole energy (include/seq/pair_mpole.h:62-152): bn already scaled */
+static double or_mpole_pair_e(const double* bn, double xr, double yr, double zr, const double* mi, const double* mk)
+{
+   double ci = mi[0], dix = mi[1], diy = mi[2], diz = mi[3];
+   double qixx = mi[4], qiyy = mi[5], qizz = mi[6], qixy = mi[7], qixz = mi[8], qiyz = mi[9];
+   double ck = mk[0], dkx = mk[1], dky = mk[2], dkz = mk[3];
+   double qkxx = mk[4], qkyy = mk[5], qkzz = mk[6], qkxy = mk[7], qkxz = mk[8], qkyz = mk[9];
+   double dir = dix * xr + diy * yr + diz * zr;
+   double qix = qixx * xr + qixy * yr + qixz * zr;
+   double qiy = qixy * xr + qiyy * yr + qiyz * zr;
+   double qiz = qixz * xr + qiyz * yr + qizz * zr;
+   double qir = qix * xr + qiy * yr + qiz * zr;
+   double dkr = dkx * xr + dky * yr + dkz * zr;
+   double qkx = qkxx * xr + qkxy * yr + qkxz * zr;
+   double qky = qkxy * xr + qkyy * yr + qkyz * zr;
+   double qkz = qkxz * xr + qkyz * yr + qkzz * zr;
+   double qkr = qkx * xr + qky * yr + qkz * zr;
+   double dik = dix * dkx + diy * dky + diz * dkz;
+   double qik = qix * qkx + qiy * qky + qiz * qkz;
+   double diqk = dix * qkx + diy * qky + diz * qkz;
+   double dkqi = dkx * qix + dky * qiy + dkz * qiz;
+   double qiqk = 2 * (qixy * qkxy + qixz * qkxz + qiyz * qkyz) + qixx * qkxx + qiyy * qkyy + qizz * qkzz;
+   double term1 = ci * ck;
+   double term2 = ck * dir - ci * dkr + dik;
+   double term3 = ci * qkr + ck * qir - dir * dkr + 2 * (dkqi - diqk + qiqk);
+   double term4 = dir * qkr - dkr * qir - 4 * qik;
+   double term5 = qir * qkr;
+   return term1 * bn[0] + term2 * bn[1] + term3 * bn[2] + term4 * bn[3] + term5 * bn[4];
+}
+
+/* Permanent-multipole energy split into real, reciprocal and self parts
+ * (src/amoeba/empole.cpp:81-138; real space empole_cu1.cc with the
+ * exclusion correction (m - 1) x bare pair, empole_cu1.cc:110; recip
+ * 0.5 f sum fmp.fphi, src/cu/hippo/empole.cu:202-335; self
+ * include/seq/emselfamoeba.h:7-37).  Non-Ewald: parts[0] only. */
+double or_empole_energy(const or_system* s, double* parts)
+{
+   const int n = s->n;
+   const double f = s->electric;
+   double ereal = 0, erecip = 0, eself = 0;
+   or_pairs pl;
+   or_build_pairs(s, s->cutoff, &pl);
+   or_excl ex;
+   or_excl_build(s, &ex);
+#pragma omp parallel for reduction(+ : ereal) schedule(dynamic, 256)
+   for (int j = 0; j < pl.npair; ++j) {
+      int i = pl.ik[2 * j], k = pl.ik[2 * j + 1];
+      double xr = s->x[k] - s->x[i], yr = s->y[k] - s->y[i], zr = s->z[k] - s->z[i];
+      or_image(s, &xr, &yr, &zr);
+      double r2 = xr * xr + yr * yr + zr * zr;
+      double r = sqrt(r2), rr2 = 1 / r2;
+      double sc[4];
+      or_excl_get(s, &ex, i, k, sc);
+      double bare[5];
+      bare[0] = f / r;
+      bare[1] = bare[0] * rr2;
+      bare[2] = 3 * bare[1] * rr2;
+      bare[3] = 5 * bare[2] * rr2;
+      bare[4] = 7 * bare[3] * rr2;
+      double e;
+      if (s->use_ewald) {
+         double bn[5];
+         or_ewald_bn(5, bn, r, rr2, s->aewald);
+         for (int q = 0; q < 5; ++q)
+            bn[q] *= f;
+         e = or_mpole_pair_e(bn, xr, yr, zr, &s->rpole[10 * i], &s->rpole[10 * k]);
+         if (sc[0] != 1)
+            e += (sc[0] - 1) * or_mpole_pair_e(bare, xr, yr, zr, &s->rpole[10 * i], &s->rpole[10 * k]);
+      } else {
+         e = sc[0] * or_mpole_pair_e(bare, xr, yr, zr, &s->rpole[10 * i], &s->rpole[10 * k]);
+      }
+      ereal += e;
+   }
+   or_excl_free(&ex);
+   or_pairs_free(&pl);
+   if (s->use_ewald) {
+      or_pme p;
+      or_pme_init(s, &p);
+      double* fmp = (double*)malloc(sizeof(double) * 10 * n);
+      double* fphi = (double*)malloc(sizeof(double) * 20 * n);
+      or_cmp_to_fmp(&p, n, s->rpole, fmp);
+      or_grid_mpole(s, &p, fmp);
+      or_fft3d(p.grid, p.n1, p.n2, p.n3, -1);
+      or_pme_conv(s, &p, 0, NULL);
+      or_fft3d(p.grid, p.n1, p.n2, p.n3, +1);
+      or_fphi(s, &p, 0, 10, fphi, 20);
+      for (int i = 0; i < n; ++i)
+         for (int c = 0; c < 10; ++c)
+            erecip += 0.5 * f * fmp[10 * i + c] * fphi[20 * i + c];
+      free(fmp);
+      free(fphi);
+      or_pme_free(&p);
+      const double a = s->aewald, a2 = 2 * a * a;
+      const double fterm = -f * a / OR_SQRTPI;
+      for (int i = 0; i < n; ++i) {
+         const double* m = &s->rpole[10 * i];
+         double cii = m[0] * m[0];
+         double dii = m[1] * m[1] + m[2] * m[2] + m[3] * m[3];
+         double qii = 2 * (m[7] * m[7] + m[8] * m[8] + m[9] * m[9]) + m[4] * m[4] + m[5] * m[5] + m[6] * m[6];
+         eself += fterm * (cii + a2 * (dii / 3 + 2 * a2 * qii * 0.2));
+      }
+   }
+   if (parts) {
+      parts[0] = ereal;
+      parts[1] = erecip;
+      parts[2] = eself;
+   }
+   return ereal + erecip + eself;
+}
+
+/* Polarization energy by the dot product -1/2 f sum_i u_d,i . E_p,i with
+ * E_p = udirp / alpha (src/cu/amoeba/epolar.cu:14-30). */
+double or_epolar_energy_dot(const or_system* s, const double* uind, const double* udirp)
+{
+   double e = 0;
+   for (int i = 0; i < s->n; ++i) {
+      double pinv = 1.0 / fmax(s->polarity[i], 1.0e-16);
+      e += pinv * (uind[3 * i] * udirp[3 * i] + uind[3 * i + 1] * udirp[3 * i + 1] + uind[3 * i + 2] * udirp[3 * i + 2]);
+   }
+   return -0.5 * s->electric * e;
+}

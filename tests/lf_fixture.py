@@ -31,7 +31,9 @@ def system(ewald):
     st = dict(tg.systems.DEFAULT_SETTINGS)
     st["usolve_cutoff"] = fx["usolve_cutoff"]
     if ewald:
-        st.update(use_ewald=1, ewald_cutoff=fx["ewald"]["cutoff"], nfft=(24, 24, 24), pbuffer=fx["ewald"]["list_buffer"])
+        cut = fx["ewald"]["cutoff"]
+        st.update(use_ewald=1, ewald_cutoff=cut, nfft=(24, 24, 24), pbuffer=fx["ewald"]["list_buffer"],
+                  aewald=tg.systems.ewald_coefficient(cut))
     else:
         st.update(use_ewald=0, ewald_cutoff=1.0e9, nfft=(0, 0, 0), aewald=0.0, pbuffer=fx["ewald"]["list_buffer"])
     s.settings = st

@@ -73,3 +73,29 @@ def test_aspc_weights_sum_to_one(oracle):
     hist = np.ones((16, 6))
     for nualt in (16, 17, 31):
         assert np.allclose(oracle.aspc_sum(hist, nualt), 1.0, atol=1e-12)
+
+
+@pytest.mark.parametrize("ewald", [0, 1], ids=["nonewald", "pme"])
+def test_epolar_energy_golden(oracle, ewald):
+    """Polarization energy by the dot product (localframe.cpp:329-333, :500-505)."""
+    s, fx = L.system(ewald)
+    e = oracle.OracleSystem(s).epolar_energy()
+    assert abs(e - L.expected(fx, ewald)["epolar"]["ref_eng"]) < MARGIN
+
+
+def test_empole_energy_golden_nonewald(oracle):
+    """Local-Frame-1: gas phase, no cutoff (localframe.cpp:22-74), eps 1e-5."""
+    s, fx = L.system(0)
+    e, _ = oracle.OracleSystem(s).empole_energy()
+    assert abs(e - fx["expected"]["Local-Frame-1"]["empole -- gas phase, no cutoff"]["ref_eng"]) < 1e-4
+
+
+def test_empole_energy_golden_pme_parts(oracle):
+    """Local-Frame-2: PME real / recip / self parts (localframe.cpp:124-130), eps 1e-4."""
+    s, fx = L.system(1)
+    e, parts = oracle.OracleSystem(s).empole_energy()
+    ex = fx["expected"]["Local-Frame-2"]["empole -- pme"]
+    assert abs(parts[0] - ex["ref_ereal"]) < 1e-4
+    assert abs(parts[1] - ex["ref_erecip"]) < 1e-4
+    assert abs(parts[2] - ex["ref_eself"]) < 1e-4
+    assert abs(e - (ex["ref_ereal"] + ex["ref_erecip"] + ex["ref_eself"])) < 1e-4

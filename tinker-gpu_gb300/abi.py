@@ -24,7 +24,7 @@ EXPORTS = [
     "t9gb_create", "t9gb_destroy", "t9gb_status_string", "t9gb_last_error", "t9gb_set_stream",
     "t9gb_set_topology", "t9gb_set_xyz_host", "t9gb_set_xyz_device", "t9gb_nblist_build", "t9gb_mpole_init",
     "t9gb_dfield", "t9gb_ufield", "t9gb_sparse_precond_apply", "t9gb_induce", "t9gb_induce_host",
-    "t9gb_induce_stats", "t9gb_get_udir", "t9gb_use_graph", "t9gb_nblist_stats", "t9gb_profile_enable", "t9gb_profile_read", "t9gb_profile_name",
+    "t9gb_induce_stats", "t9gb_get_udir", "t9gb_empole_energy", "t9gb_epolar_energy", "t9gb_use_graph", "t9gb_nblist_stats", "t9gb_profile_enable", "t9gb_profile_read", "t9gb_profile_name",
     "t9gb_ufield_noalloc",
 ]
 
@@ -92,6 +92,8 @@ def load(path=None):
     lib.t9gb_induce_host.argtypes = [vp, dp, dp, dp]
     lib.t9gb_induce_stats.argtypes = [vp, ip, dp, ip]
     lib.t9gb_get_udir.argtypes = [vp, fp, fp]
+    lib.t9gb_empole_energy.argtypes = [vp, dp, dp]
+    lib.t9gb_epolar_energy.argtypes = [vp, dp]
     lib.t9gb_use_graph.argtypes = [vp, C.c_int]
     lib.t9gb_nblist_stats.argtypes = [vp, ip, C.POINTER(C.c_longlong), ip]
     lib.t9gb_profile_enable.argtypes = [vp, C.c_int]
@@ -263,6 +265,19 @@ class Engine:
         it, eps, st = C.c_int(), C.c_double(), C.c_int()
         self.lib.t9gb_induce_stats(self.h, C.byref(it), C.byref(eps), C.byref(st))
         return it.value, eps.value, st.value
+
+    def empole_energy(self):
+        """(total, [real, recip, self]) permanent-multipole energy, kcal/mol."""
+        e = C.c_double()
+        parts = np.zeros(3)
+        self._check(self.lib.t9gb_empole_energy(self.h, C.byref(e), _dp(parts)))
+        return e.value, parts
+
+    def epolar_energy(self):
+        """Polarization energy (dot-product form) of the last induce(), kcal/mol."""
+        e = C.c_double()
+        self._check(self.lib.t9gb_epolar_energy(self.h, C.byref(e)))
+        return e.value
 
     def use_graph(self, enable=True):
         self._check(self.lib.t9gb_use_graph(self.h, 1 if enable else 0))

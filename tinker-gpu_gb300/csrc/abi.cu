@@ -7,9 +7,6 @@
 
 #include "common.cuh"
 
-struct t9gb_context {
-   t9gb::Context c;
-};
 
 namespace t9gb {
 int induce_sorted(Context* ctx);
@@ -46,6 +43,7 @@ static int alloc_all(Context* ctx)
       T9_CUDA(cudaMalloc(p, sizeof(float) * 8 * npad));
       T9_CUDA(cudaMemset(*p, 0, sizeof(float) * 8 * npad));
    }
+   T9_CUDA(cudaMalloc(&ctx->e_atom, sizeof(double) * 3 * npad));
    T9_CUDA(cudaMalloc(&ctx->red, sizeof(double) * RED_SLOTS * RED_MAX));
    T9_CUDA(cudaMalloc(&ctx->scal, sizeof(double) * 64));
    T9_CUDA(cudaMemset(ctx->scal, 0, sizeof(double) * 64));
@@ -67,7 +65,8 @@ static void free_all(Context* ctx)
    void* dev[] = {ctx->frames, ctx->pole, ctx->xyz, ctx->perm, ctx->iperm, ctx->spos, ctx->spolar, ctx->spolinv,
       ctx->sdamp, ctx->srpole, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->nbr, ctx->nnbr, ctx->nbr_over,
       ctx->cell_count, ctx->cell_start, ctx->cell_atoms, ctx->atom_cell, ctx->rcp6, ctx->fld6, ctx->udir,
-      ctx->efield, ctx->uind, ctx->rsd, ctx->zrsd, ctx->conj, ctx->vec, ctx->tmp6, ctx->red, ctx->scal, ctx->status,
+      ctx->efield, ctx->uind, ctx->rsd, ctx->zrsd, ctx->conj, ctx->vec, ctx->tmp6, ctx->e_atom, ctx->red, ctx->scal,
+      ctx->status,
       ctx->aspc_hist};
    for (void* p : dev)
       if (p)

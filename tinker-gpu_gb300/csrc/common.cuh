@@ -142,6 +142,7 @@ struct Context {
    float* conj = nullptr;
    float* vec = nullptr;
    float* tmp6 = nullptr;
+   double* e_atom = nullptr; // [3][npad] per-atom energy terms (real, recip, self)
    double* red = nullptr;   // reduction partials [RED_SLOTS][RED_MAX]
    double* scal = nullptr;  // device scalars
    int* status = nullptr;   // device status words
@@ -222,6 +223,8 @@ inline void prof_collect(Context* ctx)
 // ---- entry points implemented across the translation units ----
 int order_build(Context* ctx);  // host: spatial order, scaled partners
 int list_update(Context* ctx);  // device: exact neighbour list
+int ensure_list(Context* ctx);  // list_update when the coordinates changed
+int check_list_overflow(Context* ctx, int* redo);  // after a sync; redo = 1: grown, repeat
 int scatter_positions(Context* ctx);
 int rotpole_sorted(Context* ctx);
 int reset_predictor(Context* ctx);
@@ -238,8 +241,17 @@ int launch_precond_sparse(Context* ctx, const float* r6, float* z6);
 int launch_dfield_recip(Context* ctx, float* out6);
 int launch_ufield_recip(Context* ctx, const float* u6, float* out6);
 
+// energies: per-atom FP64 terms (pair.cu real space, pme.cu recip + self)
+int launch_empole_real(Context* ctx, double* e_atom);
+int launch_empole_recip(Context* ctx, double* e_atom);
+
 // permutation helpers (nblist.cu)
 int gather_to_sorted3(Context* ctx, const float* a, const float* b, float* s6);
 int scatter_from_sorted3(Context* ctx, const float* s6, float* a, float* b);
 
 }  // namespace t9gb
+
+// the opaque handle of the C ABI
+struct t9gb_context {
+   t9gb::Context c;
+};

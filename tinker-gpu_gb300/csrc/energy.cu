@@ -1,0 +1,93 @@
+// Energies that consume the multipoles and the converged dipoles, with
+// deterministic FP64 reductions.
+//
+//  - t9gb_empole_energy: permanent-multipole energy, real + reciprocal + self
+//    (empole(calc::energy), src/amoeba/empole.cpp:81-138);
+//  - t9gb_epolar_energy: polarization energy by the dot product
+//    -1/2 f sum_i u_d,i . E_p,i (epolar0DotProd, src/cu/amoeba/epolar.cu:14-30).
+#include "common.cuh"
+
+namespace t9gb {
+
+// block b sums arrays[b][0..n) in a fixed order into out[b]
+__global__ void k_sum_rows(int n, int stride, const double* __restrict__ a, double* __restrict__ out)
+{
+   __shared__ double sh[1024];
+   const double* row = a + (size_t)blockIdx.x * stride;
+   double v = 0;
+   for (int i = threadIdx.x; i < n; i += blockDim.x)
+      v += row[i];
+   sh[threadIdx.x] = v;
+   __syncthreads();
+   for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+      if (threadIdx.x < o)
+         sh[threadIdx.x] += sh[threadIdx.x + o];
+      __syncthreads();
+   }
+   if (threadIdx.x == 0)
+      out[blockIdx.x] = sh[0];
+}
+
+// e[s] = -1/2 f alpha_s^-1 (u_d . udir_p)
+__global__ void k_epolar_dot(int npad, double f, const float* __restrict__ uind, const float* __restrict__ udir,
+   const float* __restrict__ polinv, double* __restrict__ e)
+{
+   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < npad; s += gridDim.x * blockDim.x) {
+      const float* u = uind + 8 * s;
+      const float* p = udir + 8 * s + 3;
+      e[s] = -0.5 * f * (double)polinv[s] * ((double)u[0] * p[0] + (double)u[1] * p[1] + (double)u[2] * p[2]);
+   }
+}
+
+}  // namespace t9gb
+
+using namespace t9gb;
+
+
+extern "C" int t9gb_empole_energy(t9gb_context* h, double* energy, double* parts)
+{
+   if (!h || !energy)
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   if (!ctx->have_order)
+      return T9GB_NOT_READY;
+   for (int attempt = 0; attempt < 2; ++attempt) {
+      T9_CHECK(ensure_list(ctx));
+      T9_CUDA(cudaMemsetAsync(ctx->e_atom, 0, sizeof(double) * 3 * ctx->npad, ctx->stream));
+      T9_CHECK(launch_empole_real(ctx, ctx->e_atom));
+      T9_CHECK(launch_empole_recip(ctx, ctx->e_atom + ctx->npad));
+      k_sum_rows<<<3, 1024, 0, ctx->stream>>>(ctx->npad, ctx->npad, ctx->e_atom, ctx->scal + 32);
+      T9_CUDA(cudaGetLastError());
+      T9_CUDA(cudaMemcpyAsync(ctx->h_scal + 32, ctx->scal + 32, sizeof(double) * 3, cudaMemcpyDeviceToHost, ctx->stream));
+      T9_CUDA(cudaStreamSynchronize(ctx->stream));
+      int redo = 0;
+      T9_CHECK(check_list_overflow(ctx, &redo));
+      if (!redo)
+         break;
+   }
+   const double* v = ctx->h_scal + 32;
+   *energy = v[0] + v[1] + v[2];
+   if (parts) {
+      parts[0] = v[0];
+      parts[1] = v[1];
+      parts[2] = v[2];
+   }
+   return T9GB_OK;
+}
+
+extern "C" int t9gb_epolar_energy(t9gb_context* h, double* energy)
+{
+   if (!h || !energy)
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   if (!ctx->have_order)
+      return T9GB_NOT_READY;
+   k_epolar_dot<<<grid_for(ctx->npad, 256), 256, 0, ctx->stream>>>(ctx->npad, ctx->cfg.electric, ctx->uind, ctx->udir,
+      ctx->spolinv, ctx->e_atom);
+   k_sum_rows<<<1, 1024, 0, ctx->stream>>>(ctx->npad, ctx->npad, ctx->e_atom, ctx->scal + 36);
+   T9_CUDA(cudaGetLastError());
+   T9_CUDA(cudaMemcpyAsync(ctx->h_scal + 36, ctx->scal + 36, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+   T9_CUDA(cudaStreamSynchronize(ctx->stream));
+   *energy = ctx->h_scal[36];
+   return T9GB_OK;
+}

@@ -27,7 +27,7 @@ struct PairParams {
    float cut2;
    int ewald;
    float aewald;
-   float ec1, ec2, ec3;  // (2a^2)^j / (sqrt(pi) a), j = 1..3
+   float ec1, ec2, ec3, ec4;  // (2a^2)^j / (sqrt(pi) a), j = 1..4
    int cap;              // list row stride
 };
 
@@ -409,6 +409,126 @@ __global__ void __launch_bounds__(256) k_precond_sparse(PairParams P, int npad, 
 }
 
 // ---------------------------------------------------------------------------
+// permanent-multipole energy, real space (pair_mpole energy terms,
+// include/seq/pair_mpole.h:62-152); exclusion correction (m - 1) x bare pair
+// as the reference's exclusion loop does (src/cu/amoeba/empole_cu1.cc:110)
+
+__device__ __forceinline__ float mpole_pair_e(const float* bn, float3 d, const float* mi, const float* mk)
+{
+   const float dir = mi[1] * d.x + mi[2] * d.y + mi[3] * d.z;
+   const float qix = mi[4] * d.x + mi[7] * d.y + mi[8] * d.z;
+   const float qiy = mi[7] * d.x + mi[5] * d.y + mi[9] * d.z;
+   const float qiz = mi[8] * d.x + mi[9] * d.y + mi[6] * d.z;
+   const float qir = qix * d.x + qiy * d.y + qiz * d.z;
+   const float dkr = mk[1] * d.x + mk[2] * d.y + mk[3] * d.z;
+   const float qkx = mk[4] * d.x + mk[7] * d.y + mk[8] * d.z;
+   const float qky = mk[7] * d.x + mk[5] * d.y + mk[9] * d.z;
+   const float qkz = mk[8] * d.x + mk[9] * d.y + mk[6] * d.z;
+   const float qkr = qkx * d.x + qky * d.y + qkz * d.z;
+   const float dik = mi[1] * mk[1] + mi[2] * mk[2] + mi[3] * mk[3];
+   const float qik = qix * qkx + qiy * qky + qiz * qkz;
+   const float diqk = mi[1] * qkx + mi[2] * qky + mi[3] * qkz;
+   const float dkqi = mk[1] * qix + mk[2] * qiy + mk[3] * qiz;
+   const float qiqk = 2.f * (mi[7] * mk[7] + mi[8] * mk[8] + mi[9] * mk[9]) + mi[4] * mk[4] + mi[5] * mk[5]
+      + mi[6] * mk[6];
+   const float t1 = mi[0] * mk[0];
+   const float t2 = mk[0] * dir - mi[0] * dkr + dik;
+   const float t3 = mi[0] * qkr + mk[0] * qir - dir * dkr + 2.f * (dkqi - diqk + qiqk);
+   const float t4 = dir * qkr - dkr * qir - 4.f * qik;
+   const float t5 = qir * qkr;
+   return t1 * bn[0] + t2 * bn[1] + t3 * bn[2] + t4 * bn[3] + t5 * bn[4];
+}
+
+__device__ __forceinline__ void bare_bn5(float f, float invr, float* bn)
+{
+   const float rr2 = invr * invr;
+   bn[0] = f * invr;
+   bn[1] = bn[0] * rr2;
+   bn[2] = 3.f * bn[1] * rr2;
+   bn[3] = 5.f * bn[2] * rr2;
+   bn[4] = 7.f * bn[3] * rr2;
+}
+
+__device__ __forceinline__ void ewald_bn5(const PairParams& P, float f, float r, float invr, float* bn)
+{
+   const float rr2 = invr * invr;
+   const float ralpha = P.aewald * r;
+   const float exp2a = __expf(-ralpha * ralpha);
+   float b0 = erfc_hastings(ralpha, exp2a) * invr;
+   float b1 = (b0 + P.ec1 * exp2a) * rr2;
+   float b2 = (3.f * b1 + P.ec2 * exp2a) * rr2;
+   float b3 = (5.f * b2 + P.ec3 * exp2a) * rr2;
+   float b4 = (7.f * b3 + P.ec4 * exp2a) * rr2;
+   bn[0] = f * b0;
+   bn[1] = f * b1;
+   bn[2] = f * b2;
+   bn[3] = f * b3;
+   bn[4] = f * b4;
+}
+
+// e_atom[i] = 1/2 sum over i's list and scaled partners (every pair is seen
+// from both atoms); FP64 accumulation of FP32 pair energies
+template <int G>
+__global__ void __launch_bounds__(256) k_empole_real(PairParams P, int npad, float f, const int* __restrict__ nbr,
+   const int* __restrict__ nnbr, const int* __restrict__ sp_start, const int* __restrict__ sp_j,
+   const float4* __restrict__ sp_sc, const float4* __restrict__ spos, const float* __restrict__ rp,
+   double* __restrict__ e_atom)
+{
+   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+   const int i = tid / G, g = tid % G;
+   if (i >= npad)
+      return;
+   double e = 0;
+   if (i < P.n) {
+      const float4 pi = spos[i];
+      float mi[12];
+      load12(rp, i, mi);
+      const int* row = nbr + (size_t)i * P.cap;
+      const int cnt = nnbr[i];
+      for (int k = g; k < cnt; k += G) {
+         const int j = row[k];
+         const float3 d = sep(P, pi, spos[j]);
+         const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
+         if (r2 <= P.cut2) {
+            float mk[12], bn[5];
+            load12(rp, j, mk);
+            const float invr = rsqrtf(r2);
+            if (P.ewald)
+               ewald_bn5(P, f, r2 * invr, invr, bn);
+            else
+               bare_bn5(f, invr, bn);
+            e += (double)mpole_pair_e(bn, d, mi, mk);
+         }
+      }
+      const int pa = sp_start[i], pb = sp_start[i + 1];
+      for (int q = pa + g; q < pb; q += G) {
+         const int j = sp_j[q];
+         const float3 d = sep(P, pi, spos[j]);
+         const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
+         if (r2 <= P.cut2) {
+            float mk[12], bn[5];
+            load12(rp, j, mk);
+            const float invr = rsqrtf(r2);
+            const float ms = sp_sc[q].x;
+            bare_bn5(f, invr, bn);
+            float eb = mpole_pair_e(bn, d, mi, mk);
+            if (P.ewald) {
+               ewald_bn5(P, f, r2 * invr, invr, bn);
+               e += (double)mpole_pair_e(bn, d, mi, mk) + (double)(ms - 1.f) * eb;
+            } else {
+               e += (double)(ms * eb);
+            }
+         }
+      }
+   }
+#pragma unroll
+   for (int o = G / 2; o > 0; o >>= 1)
+      e += __shfl_xor_sync(0xffffffffu, e, o);
+   if (g == 0)
+      e_atom[i] = i < P.n ? 0.5 * e : 0.0;
+}
+
+// ---------------------------------------------------------------------------
 // launchers
 
 static PairParams make_params(const Context* ctx, double cutoff)
@@ -433,6 +553,7 @@ static PairParams make_params(const Context* ctx, double cutoff)
    P.ec1 = (float)(base * alsq2);
    P.ec2 = (float)(base * alsq2 * alsq2);
    P.ec3 = (float)(base * alsq2 * alsq2 * alsq2);
+   P.ec4 = (float)(base * alsq2 * alsq2 * alsq2 * alsq2);
    P.cap = ctx->nbr_cap;
    return P;
 }
@@ -473,4 +594,16 @@ int launch_precond_sparse(Context* ctx, const float* r6, float* z6)
    return T9GB_OK;
 }
 
+}  // namespace t9gb
+
+namespace t9gb {
+int launch_empole_real(Context* ctx, double* e_atom)
+{
+   PairParams P = make_params(ctx, ctx->cfg.cutoff);
+   k_empole_real<GROUP><<<grid_for((long long)ctx->npad * GROUP, PAIR_THREADS), PAIR_THREADS, 0, ctx->stream>>>(P,
+      ctx->npad, (float)ctx->cfg.electric, ctx->nbr, ctx->nnbr, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos,
+      ctx->srpole, e_atom);
+   T9_CUDA(cudaGetLastError());
+   return T9GB_OK;
+}
 }  // namespace t9gb

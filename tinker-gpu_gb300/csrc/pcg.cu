@@ -337,7 +337,7 @@ static int list_now(Context* ctx)
    return T9GB_OK;
 }
 
-static int ensure_list(Context* ctx)
+int ensure_list(Context* ctx)
 {
    if (!ctx->list_stale)
       return T9GB_OK;
@@ -346,7 +346,7 @@ static int ensure_list(Context* ctx)
 
 // after a synchronisation: grow the list if an atom had more neighbours than
 // the row capacity; *redo = 1 when the caller must repeat its work
-static int check_list_overflow(Context* ctx, int* redo)
+int check_list_overflow(Context* ctx, int* redo)
 {
    *redo = 0;
    if (*ctx->h_over <= ctx->nbr_cap)

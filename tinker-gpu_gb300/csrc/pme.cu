@@ -329,6 +329,79 @@ __global__ void __launch_bounds__(256) k_gather_field(int n, GridParams G, const
    }
 }
 
+// Multipole reciprocal + self energy per atom (warp per atom, level-3
+// weights): e = 1/2 f sum_k fmp_k fphi_k (src/cu/hippo/empole.cu:202-335)
+// and the Ewald self energy (include/seq/emselfamoeba.h:7-37), stored per
+// atom in e_atom[s] and e_self[s].
+__global__ void __launch_bounds__(256) k_empole_recip_self(int n, GridParams G, float f, float aewald,
+   const float4* __restrict__ spos, const float2* __restrict__ g, const float* __restrict__ rp,
+   double* __restrict__ e_atom, double* __restrict__ e_self)
+{
+   const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+   const int lane = threadIdx.x & 31;
+   if (s >= n)
+      return;
+   int i1, i2, i3;
+   float w1, w2, w3;
+   site(G, spos[s], i1, i2, i3, w1, w2, w3);
+   float phi[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+   if (lane < 25) {
+      float t1[5][3], t2[5][3], t3[5][3];
+      bspline5<3>(w1, t1);
+      bspline5<3>(w2, t2);
+      bspline5<3>(w3, t3);
+      const int jy = lane % 5, kz = lane / 5;
+      int zb = i3 + kz;
+      zb -= (zb >= G.n3 ? G.n3 : 0);
+      int yb = i2 + jy;
+      yb -= (yb >= G.n2 ? G.n2 : 0);
+      const size_t row = ((size_t)zb * G.n2 + yb) * G.n1;
+      float t0 = 0.f, ta = 0.f, tb = 0.f;
+#pragma unroll
+      for (int ix = 0; ix < 5; ++ix) {
+         int xb = i1 + ix;
+         xb -= (xb >= G.n1 ? G.n1 : 0);
+         const float q = g[row + xb].x;
+         t0 += q * t1[ix][0];
+         ta += q * t1[ix][1];
+         tb += q * t1[ix][2];
+      }
+      const float u0 = t2[jy][0], u1 = t2[jy][1], u2 = t2[jy][2];
+      const float v0 = t3[kz][0], v1 = t3[kz][1], v2 = t3[kz][2];
+      phi[0] = t0 * u0 * v0;
+      phi[1] = ta * u0 * v0;
+      phi[2] = t0 * u1 * v0;
+      phi[3] = t0 * u0 * v1;
+      phi[4] = tb * u0 * v0;
+      phi[5] = t0 * u2 * v0;
+      phi[6] = t0 * u0 * v2;
+      phi[7] = ta * u1 * v0;
+      phi[8] = ta * u0 * v1;
+      phi[9] = t0 * u1 * v1;
+   }
+#pragma unroll
+   for (int c = 0; c < 10; ++c)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1)
+         phi[c] += __shfl_xor_sync(0xffffffffu, phi[c], o);
+   if (lane != 0)
+      return;
+   const float* m = rp + 12 * s;
+   const double fmp[10] = {m[0], G.a1 * m[1], G.a2 * m[2], G.a3 * m[3], G.a1 * G.a1 * m[4], G.a2 * G.a2 * m[5],
+      G.a3 * G.a3 * m[6], 2.f * G.a1 * G.a2 * m[7], 2.f * G.a1 * G.a3 * m[8], 2.f * G.a2 * G.a3 * m[9]};
+   double e = 0;
+   for (int c = 0; c < 10; ++c)
+      e += fmp[c] * (double)phi[c];
+   e_atom[s] = 0.5 * f * e;
+   const double a2 = 2.0 * aewald * aewald;
+   const double fterm = -(double)f * aewald / 1.77245385090551602730;
+   const double cii = (double)m[0] * m[0];
+   const double dii = (double)m[1] * m[1] + (double)m[2] * m[2] + (double)m[3] * m[3];
+   const double qii = 2.0 * ((double)m[7] * m[7] + (double)m[8] * m[8] + (double)m[9] * m[9]) + (double)m[4] * m[4]
+      + (double)m[5] * m[5] + (double)m[6] * m[6];
+   e_self[s] = fterm * (cii + a2 * (dii / 3.0 + 2.0 * a2 * qii * 0.2));
+}
+
 // ---------------------------------------------------------------------------
 
 int pme_setup(Context* ctx)
@@ -468,4 +541,22 @@ int launch_ufield_recip(Context* ctx, const float* u6, float* out6)
    return T9GB_OK;
 }
 
+}  // namespace t9gb
+
+namespace t9gb {
+int launch_empole_recip(Context* ctx, double* e_atom)
+{
+   if (!ctx->cfg.use_ewald)
+      return T9GB_OK;
+   GridParams G = grid_params(ctx);
+   k_spread<0><<<grid_for((long long)ctx->n * 32, 256), 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->srpole,
+      reinterpret_cast<unsigned long long*>(ctx->pme.qfx));
+   T9_CUDA(cudaGetLastError());
+   T9_CHECK(fft_conv(ctx));
+   k_empole_recip_self<<<grid_for((long long)ctx->n * 32, 256), 256, 0, ctx->stream>>>(ctx->n, G,
+      (float)ctx->cfg.electric, (float)ctx->cfg.aewald, ctx->spos, ctx->pme.qgrid, ctx->srpole, e_atom,
+      e_atom + ctx->npad);
+   T9_CUDA(cudaGetLastError());
+   return T9GB_OK;
+}
 }  // namespace t9gb

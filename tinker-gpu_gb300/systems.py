@@ -290,3 +290,25 @@ class Trajectory:
         ions = ~water
         xyz[starts[ions]] = c[ions]
         return xyz
+
+
+def ewald_coefficient(cutoff, eps=1.0e-8):
+    """Ewald coefficient a with erfc(a r_c) / r_c = eps: doubling then 60+
+    bisection steps, the rule Tinker applies when no coefficient is given
+    (published with Tinker's ewaldcof routine)."""
+    from math import erfc
+
+    x, i = 0.5, 0
+    ratio = eps + 1.0
+    while ratio >= eps:
+        i += 1
+        x *= 2.0
+        ratio = erfc(x * cutoff) / cutoff
+    lo, hi = 0.0, x
+    for _ in range(i + 60):
+        x = 0.5 * (lo + hi)
+        if erfc(x * cutoff) / cutoff >= eps:
+            lo = x
+        else:
+            hi = x
+    return x
