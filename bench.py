@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--predictor", default="aspc", choices=["aspc", "none"])
     ap.add_argument("--history", type=int, default=20, help="trajectory frames run before warm-up (predictor ring)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--learn-train", type=int, default=500, help="online training steps before the learned legs")
+    ap.add_argument("--no-learned", action="store_true")
     return ap.parse_args()
 
 
@@ -222,6 +224,92 @@ def cpu_baseline_sample(args, s, tr):
             "sample": f"{nsteps} induce() calls on {args.config} (FP64, direct guess, all host threads)"}
 
 
+def time_steps(eng, dev_frames, idxs, stream, flush, ud, up):
+    """CUDA-event time of induce() on the given device frames (L2 flushed
+    before each step, outside the brackets); returns (ms list, iterations,
+    learned-guess stats)."""
+    import torch
+
+    ms, its, ls = [], [], []
+    with torch.cuda.stream(stream):
+        for k, t in enumerate(idxs):
+            flush.fill_(float(k))
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            eng.set_xyz_device(dev_frames[t])
+            eng.mpole_init()
+            eng.induce(out=(ud, up))
+            b.record(stream)
+            b.synchronize()
+            ms.append(a.elapsed_time(b))
+            its.append(eng.stats()[0])
+            ls.append(eng.learn_stats())
+    return ms, its, ls
+
+
+def learned_legs(args, s, abi, stream, tr, flush, check_oracle):
+    """The learned initial guess against the plain guesses.
+
+    Two engines follow the trajectory: one with the direct guess alpha E (no
+    predictor), one with the ASPC predictor.  Each trains its network online
+    for --learn-train steps (one AdamW step per solve on its converged
+    dipoles, plain starts), then continues the trajectory through three timed
+    legs of --steps frames, each after --warmup untimed frames: the plain
+    start (network off), the learned start compared with the plain one on
+    every solve (probe 1), and the comparison on every 16th solve (probe 16).
+    Training is off in the timed legs."""
+    import torch
+
+    T, K, W = args.learn_train, args.steps, args.warmup
+    x0 = 100000  # frames after the main measurement's
+    nfr = T + 3 * (W + K)
+    dev = torch.from_numpy(np.stack([tr.frame(x0 + t) for t in range(nfr)]).astype(np.float32)).to("cuda")
+    ud = torch.zeros((s.n, 3), device="cuda")
+    up = torch.zeros((s.n, 3), device="cuda")
+    out = {"train_steps": T, "timed_steps": K, "rows_per_batch": 2 * s.n,
+           "network": "32-64-64-3 SiLU, BF16 weights/activations, FP32 accumulation, AdamW lr 1e-3 wd 1e-2"}
+    for pred, name in ((0, "direct"), (1, "aspc")):
+        eng = abi.Engine(s, predictor=pred, stream=stream)
+        eng.prepare(dev[0].double().cpu().numpy())
+        eng.learn_reset(seed=1)
+        eng.learn_config(1)
+        t0 = time.perf_counter()
+        tr_ms, tr_it, tr_ls = time_steps(eng, dev, range(T), stream, flush, ud, up)
+        res = {"train_ms_per_step": float(np.mean(tr_ms[-50:])), "train_iters_last50": float(np.mean(tr_it[-50:])),
+               "train_loss_last": tr_ls[-1][3], "train_wall_s": time.perf_counter() - t0}
+        f = T
+        for mode, probe, leg in ((0, 1, "plain"), (2, 1, "learned_probe1"), (2, 16, "learned_probe16")):
+            eng.learn_config(mode)
+            eng.learn_policy(probe)
+            time_steps(eng, dev, range(f, f + W), stream, flush, ud, up)
+            idx = list(range(f + W, f + W + K))
+            f += W + K
+            ms, its, ls = time_steps(eng, dev, idx, stream, flush, ud, up)
+            r = {"induce_ms_per_step": float(np.mean(ms)), "pcg_iterations_per_step": float(np.mean(its))}
+            if mode == 2:
+                r["learned_start_fraction"] = float(np.mean([((c & 1) + ((c >> 1) & 1)) / 2 for c, *_ in ls]))
+                r["compared_fraction"] = float(np.mean([l[4] for l in ls]))
+                cmp_ = [l for l in ls if l[4]]
+                r["start_residual_plain_debye"] = float(np.mean([l[1] for l in cmp_])) if cmp_ else None
+                r["start_residual_learned_debye"] = float(np.mean([l[2] for l in cmp_])) if cmp_ else None
+                if check_oracle and probe == 1:
+                    from oracle import oracle as O
+
+                    xyz = dev[idx[-1]].double().cpu().numpy()
+                    ou, op, *_ = O.OracleSystem(s, xyz=xyz).induce()
+                    D = importlib.import_module("tinker-gpu_gb300.units").DEBYE
+                    g_ud = ud.double().cpu().numpy()
+                    g_up = up.double().cpu().numpy()
+                    r["oracle_rms_dipole_error_debye"] = float(max(
+                        np.sqrt(((g_ud - ou) ** 2).sum(1).mean()) * D, np.sqrt(((g_up - op) ** 2).sum(1).mean()) * D))
+            res[leg] = r
+        for leg in ("learned_probe1", "learned_probe16"):
+            res[leg]["speedup_vs_plain"] = res["plain"]["induce_ms_per_step"] / res[leg]["induce_ms_per_step"]
+        out[name] = res
+        eng.close()
+    return out
+
+
 def main():
     args = parse()
     world, rank, local = dist_setup()
@@ -344,6 +432,10 @@ def main():
     # M r0 1, dots 1, history 1, output 1; per PCG iteration: ufield 5 + precond 1 + vector 4
     launches_per_step = 25 + 10 * mean_it
 
+    learned = None
+    if not args.no_learned and args.learn_train > 0:
+        learned = learned_legs(args, s, abi, stream, tr, flush, check_oracle=rank == 0 and not args.no_cpu_baseline)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline_sample(args, s, tr)
@@ -382,6 +474,7 @@ def main():
             "gpu_launches": int(round(launches_per_step * args.steps)),
             "clocks": ck,
             "cpu_baseline": cpu,
+            "learned_guess": learned,
         }
         print(json.dumps(line), flush=True)
     eng.close()

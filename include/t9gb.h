@@ -177,6 +177,53 @@ int t9gb_ufield_noalloc(int n, const double* box, double cutoff, const float* xy
    const float* thole_device, const float* uind_device, const float* uinp_device, float* field_device,
    float* fieldp_device, void* stream);
 
+/* Learned initial guess.  No counterpart in the reference, whose guesses are
+ * alpha*E (src/cu/amoeba/induce.cu pcgUdirV2) and the ASPC/GEAR/LSQR
+ * predictors (src/amoeba/induce.cpp:29-69).  A per-atom network
+ * 32 -> 64 SiLU -> 64 SiLU -> 3 (BF16 weights and activations, FP32
+ * accumulation, tensor-core GEMMs) maps rotation-invariant features of each
+ * atom -- its direct field E and polarizability, radial/charge/polarizability
+ * Gaussian descriptors and the first-order mutual field of the neighbours'
+ * direct dipoles within 6 A, all in the atom's local multipole frame -- to a
+ * correction of alpha*E.  mode bit 0: after each solve, one AdamW step
+ * (learning rate lr, decoupled weight decay) on the converged dipoles of that
+ * solve; bit 1: start each PCG solve (d and p separately) from the learned
+ * guess when its residual r.r is smaller than that of the plain guess
+ * (the predictor's when its history is full).  The PCG convergence test is
+ * unchanged.  Both bits run inside the induce() graph. */
+#define T9GB_LEARN_NFEAT 32
+#define T9GB_LEARN_NPARAM 6792 /* W1[32][64] b1[64] W2[64][64] b2[64] W3[64][8] b3[8] (cols 3-7 of W3, b3 unused) */
+int t9gb_learn_config(t9gb_context* ctx, int mode, double lr, double weight_decay);
+/* Fresh Glorot-uniform weights from `seed`; clears the optimiser moments, the
+ * frozen feature statistics and the target scale. */
+int t9gb_learn_reset(t9gb_context* ctx, unsigned seed);
+/* How often both starts are compared (bit 1 of the mode).  probe_every = 1
+ * (default): every solve computes both starting residuals and picks per
+ * system.  probe_every = k > 1: the comparison runs on every k-th solve, when
+ * the predictor history has just filled and whenever the last comparison
+ * split d and p; the solves in between start from what it chose for both
+ * systems, so they pay for one starting residual only. */
+int t9gb_learn_policy(t9gb_context* ctx, int probe_every);
+/* Last solve: choice bit 0 / 1 = the d / p solve started from the learned
+ * guess; starting RMS residuals (Debye, the PCG's definition) of the plain and
+ * the learned guess at the last comparison; training loss (mean squared error
+ * in target-scale units); compared = 1 when this solve ran the comparison. */
+int t9gb_learn_stats(t9gb_context* ctx, int* choice, double* eps0_plain, double* eps0_learned, double* loss,
+   int* compared);
+int t9gb_learn_get_weights(t9gb_context* ctx, float* w, int nparam);
+int t9gb_learn_set_weights(t9gb_context* ctx, const float* w, int nparam);
+/* Network forward and backward on caller rows, host arrays: x[rows][32]
+ * (rounded to BF16), targets t[rows][3] -> y[rows][3], grad[T9GB_LEARN_NPARAM]
+ * of the loss mean((y - t)^2), and the loss.  For gradient checks. */
+int t9gb_learn_eval(t9gb_context* ctx, int rows, const float* x, const float* t, float* y, float* grad,
+   double* loss);
+/* One AdamW step (beta 0.9/0.999, eps 1e-8) with the gradient of the last
+ * t9gb_learn_eval. */
+int t9gb_learn_adamw(t9gb_context* ctx);
+/* Raw features of the last solve, device [2n][32]: rows 0..n-1 for the d
+ * dipoles, n..2n-1 for the p dipoles, caller atom order. */
+int t9gb_learn_features(t9gb_context* ctx, float* features_device);
+
 /* Tracing: per-kernel CUDA-event timing of every launch of the listed
  * categories (the reference has only cudaProfilerStart/Stop,
  * src/cudalib.cpp:20,53).  Enabling allocates the event pool; reading

@@ -74,6 +74,7 @@ def lib():
         _lib = C.CDLL(LIB)
         dp = C.POINTER(C.c_double)
         _lib.or_rotpole.argtypes = [C.c_int, C.POINTER(C.c_int), dp, dp, dp, dp, dp]
+        _lib.or_frames.argtypes = [C.c_int, C.POINTER(C.c_int), dp, dp, dp, dp]
         _lib.or_dfield.argtypes = [C.POINTER(OrSystem), dp, dp]
         _lib.or_ufield.argtypes = [C.POINTER(OrSystem), dp, dp, dp, dp]
         _lib.or_induce.argtypes = [C.POINTER(OrSystem), C.POINTER(OrInduceOpts), dp, dp, dp, dp, dp]
@@ -116,6 +117,16 @@ def rotpole(system, xyz=None):
     out = np.zeros_like(pole)
     lib().or_rotpole(system.n, _ip(frames), _dp(pole), _dp(x), _dp(y), _dp(z), _dp(out))
     return out
+
+
+def frames(system, xyz=None):
+    """Local multipole frames [n][3][3], rows = x, y, z axes in the global frame."""
+    xyz = np.ascontiguousarray(system.xyz if xyz is None else xyz, dtype=np.float64)
+    x, y, z = [np.ascontiguousarray(xyz[:, d]) for d in range(3)]
+    fr = np.ascontiguousarray(system.frames, dtype=np.int32)
+    out = np.zeros((system.n, 9))
+    lib().or_frames(system.n, _ip(fr), _dp(x), _dp(y), _dp(z), _dp(out))
+    return out.reshape(system.n, 3, 3)
 
 
 class OracleSystem:

@@ -309,6 +309,74 @@ static void or_norm(double* a)
    a[2] *= r;
 }
 
+/* Local frame of atom i: rows of a[3][3] are the x, y, z axes in the global
+ * frame (rotpole.h:52-118). */
+static void or_frame_matrix(int i, const int* frames, const double* x, const double* y, const double* z,
+   double a[3][3])
+{
+   int iz = frames[4 * i], ix = frames[4 * i + 1], iyy = frames[4 * i + 2], ax = frames[4 * i + 3];
+   for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c)
+         a[r][c] = r == c ? 1.0 : 0.0;
+   if (ax != LF_NONE) {
+      double *xx = a[0], *yy = a[1], *zz = a[2];
+      zz[0] = x[iz] - x[i];
+      zz[1] = y[iz] - y[i];
+      zz[2] = z[iz] - z[i];
+      or_norm(zz);
+      if (ax == LF_Z_ONLY) {
+         int okay = !(fabs(zz[0]) > 0.866);
+         xx[0] = okay ? 1 : 0;
+         xx[1] = okay ? 0 : 1;
+         xx[2] = 0;
+      } else {
+         xx[0] = x[ix] - x[i];
+         xx[1] = y[ix] - y[i];
+         xx[2] = z[ix] - z[i];
+         or_norm(xx);
+      }
+      if (ax == LF_Z_BISECT || ax == LF_3_FOLD) {
+         int iy = abs(iyy) - 1;
+         yy[0] = x[iy] - x[i];
+         yy[1] = y[iy] - y[i];
+         yy[2] = z[iy] - z[i];
+         or_norm(yy);
+      }
+      if (ax == LF_BISECTOR) {
+         for (int d = 0; d < 3; ++d)
+            zz[d] += xx[d];
+         or_norm(zz);
+      } else if (ax == LF_Z_BISECT) {
+         for (int d = 0; d < 3; ++d)
+            xx[d] += yy[d];
+         or_norm(xx);
+      } else if (ax == LF_3_FOLD) {
+         for (int d = 0; d < 3; ++d)
+            zz[d] += xx[d] + yy[d];
+         or_norm(zz);
+      }
+      double dot = xx[0] * zz[0] + xx[1] * zz[1] + xx[2] * zz[2];
+      for (int d = 0; d < 3; ++d)
+         xx[d] -= dot * zz[d];
+      or_norm(xx);
+      a[1][0] = a[0][2] * a[2][1] - a[0][1] * a[2][2];
+      a[1][1] = a[0][0] * a[2][2] - a[0][2] * a[2][0];
+      a[1][2] = a[0][1] * a[2][0] - a[0][0] * a[2][1];
+   }
+}
+
+/* frames of all atoms, out[n][9] (rows x, y, z axes) */
+void or_frames(int n, const int* frames, const double* x, const double* y, const double* z, double* out)
+{
+   for (int i = 0; i < n; ++i) {
+      double a[3][3];
+      or_frame_matrix(i, frames, x, y, z, a);
+      for (int r = 0; r < 3; ++r)
+         for (int c = 0; c < 3; ++c)
+            out[9 * i + 3 * r + c] = a[r][c];
+   }
+}
+
 /* frames[n][4] = zaxis (0-based), xaxis (0-based), yaxis (1-based, signed), polaxe.
  * pole is modified in place by the chirality check, as the reference does. */
 void or_rotpole(int n, const int* frames, double* pole, const double* x, const double* y, const double* z,
@@ -330,52 +398,8 @@ void or_rotpole(int n, const int* frames, double* pole, const double* x, const d
             pole[10 * i + 9] = -pole[10 * i + 9];
          }
       }
-      double a[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
-      if (ax != LF_NONE) {
-         double *xx = a[0], *yy = a[1], *zz = a[2];
-         zz[0] = x[iz] - x[i];
-         zz[1] = y[iz] - y[i];
-         zz[2] = z[iz] - z[i];
-         or_norm(zz);
-         if (ax == LF_Z_ONLY) {
-            int okay = !(fabs(zz[0]) > 0.866);
-            xx[0] = okay ? 1 : 0;
-            xx[1] = okay ? 0 : 1;
-            xx[2] = 0;
-         } else {
-            xx[0] = x[ix] - x[i];
-            xx[1] = y[ix] - y[i];
-            xx[2] = z[ix] - z[i];
-            or_norm(xx);
-         }
-         if (ax == LF_Z_BISECT || ax == LF_3_FOLD) {
-            int iy = abs(iyy) - 1;
-            yy[0] = x[iy] - x[i];
-            yy[1] = y[iy] - y[i];
-            yy[2] = z[iy] - z[i];
-            or_norm(yy);
-         }
-         if (ax == LF_BISECTOR) {
-            for (int d = 0; d < 3; ++d)
-               zz[d] += xx[d];
-            or_norm(zz);
-         } else if (ax == LF_Z_BISECT) {
-            for (int d = 0; d < 3; ++d)
-               xx[d] += yy[d];
-            or_norm(xx);
-         } else if (ax == LF_3_FOLD) {
-            for (int d = 0; d < 3; ++d)
-               zz[d] += xx[d] + yy[d];
-            or_norm(zz);
-         }
-         double dot = xx[0] * zz[0] + xx[1] * zz[1] + xx[2] * zz[2];
-         for (int d = 0; d < 3; ++d)
-            xx[d] -= dot * zz[d];
-         or_norm(xx);
-         a[1][0] = a[0][2] * a[2][1] - a[0][1] * a[2][2];
-         a[1][1] = a[0][0] * a[2][2] - a[0][2] * a[2][0];
-         a[1][2] = a[0][1] * a[2][0] - a[0][0] * a[2][1];
-      }
+      double a[3][3];
+      or_frame_matrix(i, frames, x, y, z, a);
       const double* p = &pole[10 * i];
       double* rp = &rpole[10 * i];
       rp[0] = p[0];

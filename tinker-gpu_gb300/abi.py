@@ -25,8 +25,13 @@ EXPORTS = [
     "t9gb_set_topology", "t9gb_set_xyz_host", "t9gb_set_xyz_device", "t9gb_nblist_build", "t9gb_mpole_init",
     "t9gb_dfield", "t9gb_ufield", "t9gb_sparse_precond_apply", "t9gb_induce", "t9gb_induce_host",
     "t9gb_induce_stats", "t9gb_get_udir", "t9gb_empole_energy", "t9gb_epolar_energy", "t9gb_use_graph", "t9gb_nblist_stats", "t9gb_profile_enable", "t9gb_profile_read", "t9gb_profile_name",
-    "t9gb_ufield_noalloc",
+    "t9gb_ufield_noalloc", "t9gb_learn_config", "t9gb_learn_policy", "t9gb_learn_reset", "t9gb_learn_stats", "t9gb_learn_get_weights",
+    "t9gb_learn_set_weights", "t9gb_learn_eval", "t9gb_learn_adamw", "t9gb_learn_features",
 ]
+
+LEARN_NFEAT = 32
+LEARN_NPARAM = 6792
+LEARN_TRAIN, LEARN_USE = 1, 2
 
 
 class T9Config(C.Structure):
@@ -101,6 +106,16 @@ def load(path=None):
     lib.t9gb_profile_name.argtypes = [C.c_int]
     lib.t9gb_profile_name.restype = C.c_char_p
     lib.t9gb_ufield_noalloc.argtypes = [C.c_int, dp, C.c_double, fp, fp, fp, fp, fp, fp, fp, vp]
+    flp = C.POINTER(C.c_float)
+    lib.t9gb_learn_config.argtypes = [vp, C.c_int, C.c_double, C.c_double]
+    lib.t9gb_learn_reset.argtypes = [vp, C.c_uint]
+    lib.t9gb_learn_policy.argtypes = [vp, C.c_int]
+    lib.t9gb_learn_stats.argtypes = [vp, ip, dp, dp, dp, ip]
+    lib.t9gb_learn_get_weights.argtypes = [vp, flp, C.c_int]
+    lib.t9gb_learn_set_weights.argtypes = [vp, flp, C.c_int]
+    lib.t9gb_learn_eval.argtypes = [vp, C.c_int, flp, flp, flp, flp, dp]
+    lib.t9gb_learn_adamw.argtypes = [vp]
+    lib.t9gb_learn_features.argtypes = [vp, fp]
     _lib = lib
     return lib
 
@@ -111,6 +126,10 @@ def _dp(a):
 
 def _ip(a):
     return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def _fp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
 
 
 def make_config(system, predictor=0, **over):
@@ -303,3 +322,52 @@ class Engine:
         f, fp = self._empty3(), self._empty3()
         self._check(self.lib.t9gb_get_udir(self.h, C.c_void_p(f.data_ptr()), C.c_void_p(fp.data_ptr())))
         return f, fp
+
+    # ---- learned initial guess ----
+    def learn_config(self, mode, lr=1e-3, weight_decay=1e-2):
+        """mode: LEARN_TRAIN (1) train after each solve, LEARN_USE (2) start from
+        the learned guess with the residual fallback, 3 both, 0 off."""
+        self._check(self.lib.t9gb_learn_config(self.h, int(mode), float(lr), float(weight_decay)))
+
+    def learn_reset(self, seed=1):
+        self._check(self.lib.t9gb_learn_reset(self.h, int(seed)))
+
+    def learn_policy(self, probe_every=1):
+        self._check(self.lib.t9gb_learn_policy(self.h, int(probe_every)))
+
+    def learn_stats(self):
+        """(choice bits, eps0 plain, eps0 learned, loss, compared) of the last solve."""
+        ch, a, b, l, cmp_ = C.c_int(), C.c_double(), C.c_double(), C.c_double(), C.c_int()
+        self._check(self.lib.t9gb_learn_stats(self.h, C.byref(ch), C.byref(a), C.byref(b), C.byref(l),
+                                              C.byref(cmp_)))
+        return ch.value, a.value, b.value, l.value, cmp_.value
+
+    def learn_weights(self, w=None):
+        """Returns the FP32 master weights; sets them first when w is given."""
+        if w is not None:
+            w = np.ascontiguousarray(w, dtype=np.float32)
+            self._check(self.lib.t9gb_learn_set_weights(self.h, _fp(w), w.size))
+        out = np.zeros(LEARN_NPARAM, dtype=np.float32)
+        self._check(self.lib.t9gb_learn_get_weights(self.h, _fp(out), LEARN_NPARAM))
+        return out
+
+    def learn_eval(self, x, t):
+        """Forward + backward on host rows: returns (y [rows][3], grad, loss)."""
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        rows = x.shape[0]
+        y = np.zeros((rows, 3), dtype=np.float32)
+        g = np.zeros(LEARN_NPARAM, dtype=np.float32)
+        loss = C.c_double()
+        self._check(self.lib.t9gb_learn_eval(self.h, rows, _fp(x), _fp(t), _fp(y), _fp(g), C.byref(loss)))
+        return y, g, loss.value
+
+    def learn_adamw(self):
+        self._check(self.lib.t9gb_learn_adamw(self.h))
+
+    def learn_features(self):
+        """Raw features of the last solve, [2n][32] (d rows then p rows)."""
+        out = self.torch.zeros((2 * self.n, LEARN_NFEAT), dtype=self.torch.float32, device="cuda")
+        self._check(self.lib.t9gb_learn_features(self.h, C.c_void_p(out.data_ptr())))
+        self.torch.cuda.synchronize()
+        return out.cpu().numpy()

@@ -12,7 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(CSRC, "_build")
 LIB = os.path.join(BUILD, "libt9gb.so")
-SOURCES = ["abi.cu", "nblist.cu", "pair.cu", "pme.cu", "pcg.cu", "energy.cu", "noalloc.cu"]
+SOURCES = ["abi.cu", "nblist.cu", "pair.cu", "pme.cu", "pcg.cu", "energy.cu", "mlp.cu", "learn.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 
@@ -24,8 +24,8 @@ def _nvcc():
 
 def _compile(src, verbose_ptxas=False):
     obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
-    deps = [os.path.join(CSRC, src), os.path.join(CSRC, "common.cuh"),
-            os.path.join(HERE, "..", "include", "t9gb.h")]
+    headers = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith(".cuh")]
+    deps = [os.path.join(CSRC, src), *headers, os.path.join(HERE, "..", "include", "t9gb.h")]
     if os.path.exists(obj) and all(os.path.getmtime(obj) >= os.path.getmtime(d) for d in deps):
         return obj, ""
     cmd = [_nvcc(), *ARCH, *FLAGS, "-c", os.path.join(CSRC, src), "-o", obj]

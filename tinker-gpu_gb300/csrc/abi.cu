@@ -6,6 +6,7 @@
 #include <new>
 
 #include "common.cuh"
+#include "reduce.cuh"
 
 
 namespace t9gb {
@@ -44,6 +45,8 @@ static int alloc_all(Context* ctx)
       T9_CUDA(cudaMemset(*p, 0, sizeof(float) * 8 * npad));
    }
    T9_CUDA(cudaMalloc(&ctx->e_atom, sizeof(double) * 3 * npad));
+   T9_CUDA(cudaMalloc(&ctx->sframe, sizeof(float) * 9 * npad));
+   T9_CUDA(cudaMalloc(&ctx->hout, sizeof(float) * 6 * npad));
    T9_CUDA(cudaMalloc(&ctx->red, sizeof(double) * RED_SLOTS * RED_MAX));
    T9_CUDA(cudaMalloc(&ctx->scal, sizeof(double) * 64));
    T9_CUDA(cudaMemset(ctx->scal, 0, sizeof(double) * 64));
@@ -57,6 +60,9 @@ static int alloc_all(Context* ctx)
    }
    ctx->h_stage_bytes = sizeof(float) * 8 * (size_t)npad;
    T9_CUDA(cudaMallocHost(&ctx->h_stage, ctx->h_stage_bytes));
+   // the legacy-stream memsets above must finish before work on the caller's
+   // (possibly non-blocking) stream
+   T9_CUDA(cudaDeviceSynchronize());
    return T9GB_OK;
 }
 
@@ -65,8 +71,8 @@ static void free_all(Context* ctx)
    void* dev[] = {ctx->frames, ctx->pole, ctx->xyz, ctx->perm, ctx->iperm, ctx->spos, ctx->spolar, ctx->spolinv,
       ctx->sdamp, ctx->srpole, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->nbr, ctx->nnbr, ctx->nbr_over,
       ctx->cell_count, ctx->cell_start, ctx->cell_atoms, ctx->atom_cell, ctx->rcp6, ctx->fld6, ctx->udir,
-      ctx->efield, ctx->uind, ctx->rsd, ctx->zrsd, ctx->conj, ctx->vec, ctx->tmp6, ctx->e_atom, ctx->red, ctx->scal,
-      ctx->status,
+      ctx->efield, ctx->uind, ctx->rsd, ctx->zrsd, ctx->conj, ctx->vec, ctx->tmp6, ctx->e_atom, ctx->sframe, ctx->hout,
+      ctx->red, ctx->scal, ctx->status,
       ctx->aspc_hist};
    for (void* p : dev)
       if (p)
@@ -80,8 +86,8 @@ static void free_all(Context* ctx)
    if (ctx->h_over)
       cudaFreeHost(ctx->h_over);
    pme_free(ctx);
-   if (ctx->graph_exec)
-      cudaGraphExecDestroy(ctx->graph_exec);
+   learn_free(ctx);
+   drop_graphs(ctx);
    if (ctx->cap_stream)
       cudaStreamDestroy(ctx->cap_stream);
    for (auto& e : ctx->prof.ev)
@@ -217,6 +223,7 @@ int t9gb_set_topology(t9gb_context* h, const int* frames, const double* pole, co
       pf[i] = (float)pole[i];
    T9_CUDA(cudaMemcpy(ctx->frames, frames, sizeof(int4) * n, cudaMemcpyHostToDevice));
    T9_CUDA(cudaMemcpy(ctx->pole, pf.data(), sizeof(float) * 10 * n, cudaMemcpyHostToDevice));
+   T9_CUDA(cudaDeviceSynchronize());  // ordered before work on a non-blocking stream
    ctx->have_topology = true;
    ctx->have_order = false;
    return T9GB_OK;
@@ -354,9 +361,8 @@ int t9gb_induce_host(t9gb_context* h, const double* xyz, double* uind, double* u
       return st;
    const int n = ctx->n;
    // dipoles to caller order in the scratch vector, then one D2H copy
-   // (vec is scratch here; it is never read as a neighbour row)
-   T9_CHECK(scatter_from_sorted3(ctx, ctx->uind, ctx->vec, ctx->vec + 3 * n));
-   T9_CUDA(cudaMemcpyAsync(ctx->h_stage, ctx->vec, sizeof(float) * 6 * n, cudaMemcpyDeviceToHost, ctx->stream));
+   T9_CHECK(scatter_from_sorted3(ctx, ctx->uind, ctx->hout, ctx->hout + 3 * n));
+   T9_CUDA(cudaMemcpyAsync(ctx->h_stage, ctx->hout, sizeof(float) * 6 * n, cudaMemcpyDeviceToHost, ctx->stream));
    T9_CUDA(cudaStreamSynchronize(ctx->stream));
    for (int i = 0; i < 3 * n; ++i) {
       if (uind)
@@ -418,6 +424,133 @@ int t9gb_nblist_stats(t9gb_context* h, int* capacity, long long* entries, int* n
       }
    }
    return T9GB_OK;
+}
+
+int t9gb_learn_config(t9gb_context* h, int mode, double lr, double weight_decay)
+{
+   if (!h || mode < 0 || mode > 3 || !(lr >= 0) || !(weight_decay >= 0))
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   if (mode)
+      T9_CHECK(learn_setup(ctx));
+   if (mode != ctx->learn_mode || (float)lr != ctx->learn_lr || (float)weight_decay != ctx->learn_wd)
+      drop_graphs(ctx);  // the graphs hold the mode, rate and decay
+   if ((mode & 2) && !(ctx->learn_mode & 2))
+      ctx->learn_since_probe = 1 << 30;  // first solve compares both starts
+   ctx->learn_mode = mode;
+   ctx->learn_lr = (float)lr;
+   ctx->learn_wd = (float)weight_decay;
+   return T9GB_OK;
+}
+
+int t9gb_learn_policy(t9gb_context* h, int probe_every)
+{
+   if (!h || probe_every < 1)
+      return T9GB_BAD_ARG;
+   h->c.learn_probe = probe_every;
+   h->c.learn_since_probe = 1 << 30;
+   return T9GB_OK;
+}
+
+int t9gb_learn_reset(t9gb_context* h, unsigned seed)
+{
+   if (!h)
+      return T9GB_BAD_ARG;
+   return learn_reset(&h->c, seed);
+}
+
+int t9gb_learn_stats(t9gb_context* h, int* choice, double* eps0_plain, double* eps0_learned, double* loss,
+   int* compared)
+{
+   if (!h)
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   const double* sc = ctx->h_scal;
+   const double n = std::max(1, ctx->n), debye = ctx->cfg.debye;
+   if (choice)
+      *choice = (ctx->learn_mode & 2) ? ctx->h_status[ST_LCHOICE] : 0;
+   if (eps0_plain)
+      *eps0_plain = debye * std::sqrt(std::max(sc[S_L_PLAIN_D], sc[S_L_PLAIN_P]) / n);
+   if (eps0_learned)
+      *eps0_learned = debye * std::sqrt(std::max(sc[S_L_LEARN_D], sc[S_L_LEARN_P]) / n);
+   if (loss)
+      *loss = sc[S_L_LOSS];
+   if (compared)
+      *compared = ctx->learn_variant == 2 ? 1 : 0;
+   return T9GB_OK;
+}
+
+int t9gb_learn_get_weights(t9gb_context* h, float* w, int nparam)
+{
+   if (!h || !w || nparam != T9GB_LEARN_NPARAM)
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   T9_CHECK(learn_setup(ctx));
+   return mlp_get_weights(ctx, w);
+}
+
+int t9gb_learn_set_weights(t9gb_context* h, const float* w, int nparam)
+{
+   if (!h || !w || nparam != T9GB_LEARN_NPARAM)
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   T9_CHECK(learn_setup(ctx));
+   T9_CUDA(cudaStreamSynchronize(ctx->stream));
+   return mlp_set_weights(ctx, w);
+}
+
+int t9gb_learn_eval(t9gb_context* h, int rows, const float* x, const float* t, float* y, float* grad, double* loss)
+{
+   if (!h || rows <= 0 || !x || !t)
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   T9_CHECK(learn_setup(ctx));
+   MlpState& S = ctx->mlp;
+   if (rows > S.max_rows)
+      return T9GB_TOO_LARGE;
+   std::vector<__nv_bfloat16> xb((size_t)rows * MLP_IN);
+   for (size_t i = 0; i < xb.size(); ++i)
+      xb[i] = __float2bfloat16(x[i]);
+   cudaStream_t st = ctx->stream;
+   T9_CUDA(cudaMemcpyAsync(S.x, xb.data(), sizeof(__nv_bfloat16) * xb.size(), cudaMemcpyHostToDevice, st));
+   T9_CUDA(cudaMemcpyAsync(S.t, t, sizeof(float) * rows * MLP_OUT, cudaMemcpyHostToDevice, st));
+   T9_CHECK(mlp_forward(ctx, rows));
+   T9_CHECK(mlp_backward(ctx, rows, nullptr, 0));
+   std::vector<float> yy((size_t)rows * MLP_OUT_PAD);
+   double l = 0;
+   T9_CUDA(cudaMemcpyAsync(yy.data(), S.y, sizeof(float) * yy.size(), cudaMemcpyDeviceToHost, st));
+   if (grad)
+      T9_CUDA(cudaMemcpyAsync(grad, S.g, sizeof(float) * MLP_NPARAM, cudaMemcpyDeviceToHost, st));
+   T9_CUDA(cudaMemcpyAsync(&l, S.loss, sizeof(double), cudaMemcpyDeviceToHost, st));
+   T9_CUDA(cudaStreamSynchronize(st));
+   if (y)
+      for (int r = 0; r < rows; ++r)
+         for (int c = 0; c < MLP_OUT; ++c)
+            y[r * MLP_OUT + c] = yy[(size_t)r * MLP_OUT_PAD + c];
+   if (loss)
+      *loss = l / ((double)rows * MLP_OUT);
+   return T9GB_OK;
+}
+
+int t9gb_learn_adamw(t9gb_context* h)
+{
+   if (!h)
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   T9_CHECK(learn_setup(ctx));
+   T9_CHECK(mlp_adamw(ctx, ctx->learn_lr, ctx->learn_wd));
+   T9_CUDA(cudaStreamSynchronize(ctx->stream));
+   return T9GB_OK;
+}
+
+int t9gb_learn_features(t9gb_context* h, float* features_device)
+{
+   if (!h || !features_device)
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   if (!ctx->xf || !ctx->have_order)
+      return T9GB_NOT_READY;
+   return learn_features_out(ctx, features_device);
 }
 
 int t9gb_profile_enable(t9gb_context* h, int enable)

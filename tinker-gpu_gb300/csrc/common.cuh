@@ -2,6 +2,7 @@
 // every device buffer, fixed-point helpers, the Hastings erfc, and the
 // per-kernel event profiler.
 #pragma once
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <cufft.h>
 
@@ -71,9 +72,42 @@ struct Profiler {
    long long cnt[P_NCAT] = {0};
 };
 
+// Learned-guess network: 32 -> 64 -> 64 -> 3 (output padded to 8 columns)
+constexpr int MLP_IN = 32, MLP_HID = 64, MLP_OUT = 3, MLP_OUT_PAD = 8;
+constexpr int MLP_NPARAM = MLP_IN * MLP_HID + MLP_HID + MLP_HID * MLP_HID + MLP_HID + MLP_HID * MLP_OUT_PAD + MLP_OUT_PAD;
+
+struct MlpState {
+   int max_rows = 0;
+   int* step = nullptr; // AdamW steps taken (device, so graphs replay it)
+   int nsplit = 64;     // batch splits of the weight-gradient GEMMs
+   float* w = nullptr;  // FP32 master parameters
+   float* g = nullptr;  // gradient
+   float* m = nullptr;  // AdamW moments
+   float* v = nullptr;
+   unsigned char* mask = nullptr;
+   int* wb_index = nullptr;
+   __nv_bfloat16* wb = nullptr;  // BF16 weights used by the GEMMs
+   __nv_bfloat16* x = nullptr;   // [rows][32] inputs
+   float* z1 = nullptr;          // [rows][64] pre-activations
+   float* z2 = nullptr;
+   __nv_bfloat16* h1 = nullptr;  // [rows][64] activations
+   __nv_bfloat16* h2 = nullptr;
+   float* c = nullptr;           // [rows][64] GEMM output scratch
+   float* y = nullptr;           // [rows][8] outputs
+   float* t = nullptr;           // [rows][3] targets
+   __nv_bfloat16* dy = nullptr;  // [rows][8]
+   float* dyf = nullptr;
+   __nv_bfloat16* dz = nullptr;  // [rows][64]
+   float* dzf = nullptr;
+   double* err = nullptr;        // [rows] squared error
+   double* loss = nullptr;
+   float* split = nullptr;       // split-K / column-sum partials
+};
+
 struct Context {
    t9gb_config cfg;
    Profiler prof;
+   MlpState mlp;
    int n = 0;
    int npad = 0;  // n rounded up to 32
    int dev = 0;
@@ -104,6 +138,7 @@ struct Context {
    float* spolinv = nullptr; // [npad] 1/max(alpha, 1e-16)
    float2* sdamp = nullptr;  // [npad] pdamp, thole
    float* srpole = nullptr;  // [npad][12] global-frame multipoles, thole, polarizability
+   float* sframe = nullptr;  // [npad][9] local multipole frame (rows: x, y, z axes)
 
    // scaled partners of every slot, both directions (CSR over slots)
    int* sp_start = nullptr;  // [npad + 1]
@@ -152,9 +187,24 @@ struct Context {
    // ASPC predictor ring, sorted [16][npad][6]; the ring count is device state
    float* aspc_hist = nullptr;
 
+   // learned initial guess (learn.cu)
+   int learn_mode = 0;          // bit 0: train after each solve, bit 1: start from the learned guess
+   unsigned learn_seed = 1;
+   float learn_lr = 1e-3f, learn_wd = 1e-2f;
+   float* xf = nullptr;         // [2 npad][32] raw features, d rows then p rows
+   float* fstat = nullptr;      // feature mean[32], 1/std[32], target scale
+   float* hout = nullptr;       // [6 n] host-copy staging
+   // start policy (host): compare the plain and the learned start every
+   // learn_probe solves; in between reuse the last comparison's verdict
+   int learn_probe = 1;
+   int learn_since_probe = 1 << 30;
+   int learn_last_choice = 0;
+   int learn_variant = 0;       // start variant of the last solve
+   bool learn_ring_full = false;
+
    // whole-induce CUDA graph
    bool use_graph = true;
-   cudaGraphExec_t graph_exec = nullptr;
+   cudaGraphExec_t graph_exec[3] = {nullptr, nullptr, nullptr};  // per start variant (pcg.cu)
    cudaStream_t cap_stream = nullptr;
 
    // last induce statistics
@@ -244,6 +294,26 @@ int launch_ufield_recip(Context* ctx, const float* u6, float* out6);
 // energies: per-atom FP64 terms (pair.cu real space, pme.cu recip + self)
 int launch_empole_real(Context* ctx, double* e_atom);
 int launch_empole_recip(Context* ctx, double* e_atom);
+
+// learned-guess network (mlp.cu)
+int mlp_alloc(Context* ctx, int max_rows, unsigned seed);
+void mlp_free(Context* ctx);
+int mlp_set_weights(Context* ctx, const float* w_host);
+int mlp_get_weights(Context* ctx, float* w_host);
+int mlp_forward(Context* ctx, int rows);
+int mlp_backward(Context* ctx, int rows, const float* rowpol, int npad);
+int mlp_adamw(Context* ctx, float lr, float wd);
+// learned guess (learn.cu)
+int launch_learn_features(Context* ctx, const float* e8, const float* u8, float* xf);  // pair.cu
+int learn_setup(Context* ctx);
+void learn_free(Context* ctx);
+int learn_reset(Context* ctx, unsigned seed);
+int learn_forward(Context* ctx);
+int learn_guess(Context* ctx, float* ug8, int set_choice);
+void drop_graphs(Context* ctx);  // pcg.cu
+int learn_pick(Context* ctx, const float* ug8, const float* fld8);
+int learn_train(Context* ctx);
+int learn_features_out(Context* ctx, float* out_dev);
 
 // permutation helpers (nblist.cu)
 int gather_to_sorted3(Context* ctx, const float* a, const float* b, float* s6);

@@ -1,0 +1,454 @@
+// Per-atom MLP for the learned initial guess of the induced dipoles:
+// 32 inputs -> 64 SiLU -> 64 SiLU -> 3 outputs, BF16 weights and activations,
+// FP32 accumulation, trained online with AdamW.
+//
+// Every contraction runs on the tensor cores through one hand-written GEMM
+// (mma.sync m16n8k16 BF16 -> FP32): the forward layers, the backward input
+// gradients and the weight gradients (split over the batch, partials summed
+// in a fixed order, so training is bit-reproducible).  The reference has no
+// learned component; the closest prior art is its AMOEBA+NN CELU network
+// evaluated through cuBLAS Sgemm (src/nn.cpp:419-432).
+#include <cuda_bf16.h>
+
+#include <cmath>
+#include <random>
+
+#include "common.cuh"
+
+namespace t9gb {
+
+// ---------------------------------------------------------------------------
+// GEMM: C[z][M][N] = sum over the z-th K chunk of A(m,k) B(k,n)
+//   A(m,k) = TA ? A[k*lda + m] : A[m*lda + k]
+//   B(k,n) = TB ? B[n*ldb + k] : B[k*ldb + n]
+// Block tile 64 x 64 x 32, four warps of 16 rows x 64 columns.
+
+__device__ __forceinline__ void mma_bf16_16816(float* d, const unsigned* a, const unsigned* b)
+{
+   asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(128) k_gemm_bf16(int M, int N, int K, int kchunk, const __nv_bfloat16* __restrict__ A,
+   int lda, const __nv_bfloat16* __restrict__ B, int ldb, float* __restrict__ C)
+{
+   __shared__ __align__(16) __nv_bfloat16 As[64][40];  // [m][k], rows padded to 80 B (conflict-free)
+   __shared__ __align__(16) __nv_bfloat16 Bs[64][40];  // [n][k]
+   const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31, gq = lane >> 2, t4 = lane & 3;
+   const int m0 = blockIdx.x * 64, n0 = blockIdx.y * 64;
+   const int kbeg = blockIdx.z * kchunk, kend = min(K, kbeg + kchunk);
+   float acc[8][4];
+#pragma unroll
+   for (int j = 0; j < 8; ++j)
+      acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+   const __nv_bfloat16 zero = __float2bfloat16(0.f);
+   for (int k0 = kbeg; k0 < kend; k0 += 32) {
+      for (int e = tid; e < 64 * 32; e += 128) {
+         int r, c;
+         if (TA) {
+            r = e % 64;
+            c = e / 64;
+         } else {
+            r = e / 32;
+            c = e % 32;
+         }
+         const int gm = m0 + r, gk = k0 + c;
+         As[r][c] = (gm < M && gk < kend) ? (TA ? A[(size_t)gk * lda + gm] : A[(size_t)gm * lda + gk]) : zero;
+      }
+      for (int e = tid; e < 64 * 32; e += 128) {
+         int r, c;
+         if (TB) {
+            r = e / 32;
+            c = e % 32;
+         } else {
+            r = e % 64;
+            c = e / 64;
+         }
+         const int gn = n0 + r, gk = k0 + c;
+         Bs[r][c] = (gn < N && gk < kend) ? (TB ? B[(size_t)gn * ldb + gk] : B[(size_t)gk * ldb + gn]) : zero;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int kk = 0; kk < 32; kk += 16) {
+         unsigned a[4];
+         const int r = 16 * w + gq;
+         a[0] = *reinterpret_cast<const unsigned*>(&As[r][kk + 2 * t4]);
+         a[1] = *reinterpret_cast<const unsigned*>(&As[r + 8][kk + 2 * t4]);
+         a[2] = *reinterpret_cast<const unsigned*>(&As[r][kk + 8 + 2 * t4]);
+         a[3] = *reinterpret_cast<const unsigned*>(&As[r + 8][kk + 8 + 2 * t4]);
+#pragma unroll
+         for (int j = 0; j < 8; ++j) {
+            unsigned b[2];
+            b[0] = *reinterpret_cast<const unsigned*>(&Bs[8 * j + gq][kk + 2 * t4]);
+            b[1] = *reinterpret_cast<const unsigned*>(&Bs[8 * j + gq][kk + 8 + 2 * t4]);
+            mma_bf16_16816(acc[j], a, b);
+         }
+      }
+      __syncthreads();
+   }
+   float* Cz = C + (size_t)blockIdx.z * M * N;
+   const int r0 = m0 + 16 * w + gq;
+#pragma unroll
+   for (int j = 0; j < 8; ++j) {
+      const int c = n0 + 8 * j + 2 * t4;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+         const int r = r0 + 8 * h;
+         if (r < M) {
+            if (c < N)
+               Cz[(size_t)r * N + c] = acc[j][2 * h];
+            if (c + 1 < N)
+               Cz[(size_t)r * N + c + 1] = acc[j][2 * h + 1];
+         }
+      }
+   }
+}
+
+// out[i] = sum_z part[z][i] (fixed order)
+__global__ void k_sum_splits(int size, int nsplit, const float* __restrict__ part, float* __restrict__ out)
+{
+   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < size; i += gridDim.x * blockDim.x) {
+      float v = 0.f;
+      for (int z = 0; z < nsplit; ++z)
+         v += part[(size_t)z * size + i];
+      out[i] = v;
+   }
+}
+
+static int gemm(Context* ctx, bool ta, bool tb, int M, int N, int K, const __nv_bfloat16* A, int lda,
+   const __nv_bfloat16* B, int ldb, float* C, int nsplit)
+{
+   const int kchunk = ((K + nsplit - 1) / nsplit + 31) / 32 * 32;
+   nsplit = (K + kchunk - 1) / kchunk;
+   dim3 grid(grid_for(M, 64), grid_for(N, 64), nsplit);
+   float* out = nsplit > 1 ? ctx->mlp.split : C;
+   if (ta && !tb)
+      k_gemm_bf16<true, false><<<grid, 128, 0, ctx->stream>>>(M, N, K, kchunk, A, lda, B, ldb, out);
+   else if (!ta && tb)
+      k_gemm_bf16<false, true><<<grid, 128, 0, ctx->stream>>>(M, N, K, kchunk, A, lda, B, ldb, out);
+   else if (!ta && !tb)
+      k_gemm_bf16<false, false><<<grid, 128, 0, ctx->stream>>>(M, N, K, kchunk, A, lda, B, ldb, out);
+   else
+      k_gemm_bf16<true, true><<<grid, 128, 0, ctx->stream>>>(M, N, K, kchunk, A, lda, B, ldb, out);
+   if (nsplit > 1)
+      k_sum_splits<<<grid_for(M * N, 256), 256, 0, ctx->stream>>>(M * N, nsplit, ctx->mlp.split, C);
+   T9_CUDA(cudaGetLastError());
+   return T9GB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// elementwise pieces
+
+__device__ __forceinline__ float silu(float z) { return z / (1.f + __expf(-z)); }
+__device__ __forceinline__ float silu_grad(float z)
+{
+   const float s = 1.f / (1.f + __expf(-z));
+   return s * (1.f + z * (1.f - s));
+}
+
+// Z = C + b; H = silu(Z) (act) or Z, stored as BF16 (ldh columns, zero padded)
+__global__ void k_bias_act(int rows, int N, int ldh, const float* __restrict__ C, const float* __restrict__ b,
+   float* __restrict__ Z, __nv_bfloat16* __restrict__ H, int act)
+{
+   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < rows * ldh; e += gridDim.x * blockDim.x) {
+      const int r = e / ldh, c = e % ldh;
+      float z = 0.f;
+      if (c < N)
+         z = C[(size_t)r * N + c] + b[c];
+      if (Z)
+         Z[e] = z;
+      if (H)
+         H[e] = __float2bfloat16(act && c < N ? silu(z) : z);
+   }
+}
+
+// dZ = dH * silu'(Z), BF16 out; f32 copy for the bias gradient
+__global__ void k_silu_back(int size, const float* __restrict__ dH, const float* __restrict__ Z,
+   __nv_bfloat16* __restrict__ dZ, float* __restrict__ dZf)
+{
+   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < size; e += gridDim.x * blockDim.x) {
+      const float v = dH[e] * silu_grad(Z[e]);
+      dZ[e] = __float2bfloat16(v);
+      dZf[e] = v;
+   }
+}
+
+// MSE over the 3 outputs: dY = 2 (Y - T) / (rows * 3), zero in the padding
+// columns and in rows whose rowpol[r % npad] is 0 (padding slots); per-row
+// squared error for the loss
+__global__ void k_loss_grad(int rows, const float* __restrict__ Y, const float* __restrict__ T,
+   const float* __restrict__ rowpol, int npad, __nv_bfloat16* __restrict__ dY, float* __restrict__ dYf,
+   double* __restrict__ err)
+{
+   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
+      double s = 0;
+      const bool live = !rowpol || rowpol[r % npad] != 0.f;
+      for (int c = 0; c < MLP_OUT_PAD; ++c) {
+         float g = 0.f;
+         if (c < MLP_OUT && live) {
+            const float d = Y[(size_t)r * MLP_OUT_PAD + c] - T[(size_t)r * MLP_OUT + c];
+            s += (double)d * d;
+            g = 2.f * d / (float)(rows * MLP_OUT);
+         }
+         dY[(size_t)r * MLP_OUT_PAD + c] = __float2bfloat16(g);
+         dYf[(size_t)r * MLP_OUT_PAD + c] = g;
+      }
+      err[r] = s;
+   }
+}
+
+// column sums of a [rows][N] f32 matrix (split rows, fixed-order combine)
+__global__ void k_colsum_part(int rows, int N, int rchunk, const float* __restrict__ X, float* __restrict__ part)
+{
+   const int c = threadIdx.x;
+   if (c >= N)
+      return;
+   const int r0 = blockIdx.x * rchunk, r1 = min(rows, r0 + rchunk);
+   float v = 0.f;
+   for (int r = r0; r < r1; ++r)
+      v += X[(size_t)r * N + c];
+   part[(size_t)blockIdx.x * N + c] = v;
+}
+
+// fixed-order sum of a double array (one block)
+__global__ void k_sum_double(int n, const double* __restrict__ a, double* __restrict__ out)
+{
+   __shared__ double sh[256];
+   double v = 0;
+   for (int i = threadIdx.x; i < n; i += blockDim.x)
+      v += a[i];
+   sh[threadIdx.x] = v;
+   __syncthreads();
+   for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+      if (threadIdx.x < o)
+         sh[threadIdx.x] += sh[threadIdx.x + o];
+      __syncthreads();
+   }
+   if (threadIdx.x == 0)
+      *out = sh[0];
+}
+
+// AdamW (Loshchilov & Hutter, 2019) on the FP32 master weights; refreshes
+// the BF16 copies used by the GEMMs.  mask: parameters that stay zero (the
+// padding columns of the output layer).  One block: the step count lives on
+// the device (*step, incremented here) so a captured graph replays correctly.
+__global__ void __launch_bounds__(1024) k_adamw(int size, float lr, float beta1, float beta2, float eps, float wd,
+   int* __restrict__ step, float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
+   float* __restrict__ v, const unsigned char* __restrict__ mask, __nv_bfloat16* __restrict__ wb,
+   const int* __restrict__ wb_index)
+{
+   const int t = *step + 1;
+   const float c1 = 1.f - powf(beta1, (float)t), c2 = 1.f - powf(beta2, (float)t);
+   for (int i = threadIdx.x; i < size; i += blockDim.x) {
+      if (!mask[i])
+         continue;
+      const float gi = g[i];
+      const float mi = beta1 * m[i] + (1.f - beta1) * gi;
+      const float vi = beta2 * v[i] + (1.f - beta2) * gi * gi;
+      m[i] = mi;
+      v[i] = vi;
+      float wi = w[i];
+      wi -= lr * ((mi / c1) / (sqrtf(vi / c2) + eps) + wd * wi);
+      w[i] = wi;
+      if (wb_index[i] >= 0)
+         wb[wb_index[i]] = __float2bfloat16(wi);
+   }
+   __syncthreads();
+   if (threadIdx.x == 0)
+      *step = t;
+}
+
+// ---------------------------------------------------------------------------
+// parameter layout (FP32 master vector):
+//   W1 [32][64] | b1 [64] | W2 [64][64] | b2 [64] | W3 [64][8] | b3 [8]
+// BF16 copies: W1 | W2 | W3 in the same order (weights only).
+
+constexpr int OFF_W1 = 0;
+constexpr int OFF_B1 = OFF_W1 + MLP_IN * MLP_HID;
+constexpr int OFF_W2 = OFF_B1 + MLP_HID;
+constexpr int OFF_B2 = OFF_W2 + MLP_HID * MLP_HID;
+constexpr int OFF_W3 = OFF_B2 + MLP_HID;
+constexpr int OFF_B3 = OFF_W3 + MLP_HID * MLP_OUT_PAD;
+constexpr int OFF_END = OFF_B3 + MLP_OUT_PAD;
+constexpr int BF_W1 = 0, BF_W2 = BF_W1 + MLP_IN * MLP_HID, BF_W3 = BF_W2 + MLP_HID * MLP_HID;
+constexpr int BF_END = BF_W3 + MLP_HID * MLP_OUT_PAD;
+static_assert(OFF_END == MLP_NPARAM, "parameter count");
+
+int mlp_init(Context* ctx, unsigned seed);
+
+// allocate for max_rows rows (kept when large enough) and initialise
+int mlp_alloc(Context* ctx, int max_rows, unsigned seed)
+{
+   MlpState& S = ctx->mlp;
+   if (S.w && S.max_rows >= max_rows)
+      return mlp_init(ctx, seed);
+   mlp_free(ctx);
+   S.max_rows = max_rows;
+   T9_CUDA(cudaMalloc(&S.step, sizeof(int)));
+   T9_CUDA(cudaMalloc(&S.w, sizeof(float) * MLP_NPARAM));
+   T9_CUDA(cudaMalloc(&S.g, sizeof(float) * MLP_NPARAM));
+   T9_CUDA(cudaMalloc(&S.m, sizeof(float) * MLP_NPARAM));
+   T9_CUDA(cudaMalloc(&S.v, sizeof(float) * MLP_NPARAM));
+   T9_CUDA(cudaMalloc(&S.mask, MLP_NPARAM));
+   T9_CUDA(cudaMalloc(&S.wb_index, sizeof(int) * MLP_NPARAM));
+   T9_CUDA(cudaMalloc(&S.wb, sizeof(__nv_bfloat16) * BF_END));
+   const size_t R = max_rows;
+   T9_CUDA(cudaMalloc(&S.x, sizeof(__nv_bfloat16) * R * MLP_IN));
+   T9_CUDA(cudaMalloc(&S.z1, sizeof(float) * R * MLP_HID));
+   T9_CUDA(cudaMalloc(&S.z2, sizeof(float) * R * MLP_HID));
+   T9_CUDA(cudaMalloc(&S.h1, sizeof(__nv_bfloat16) * R * MLP_HID));
+   T9_CUDA(cudaMalloc(&S.h2, sizeof(__nv_bfloat16) * R * MLP_HID));
+   T9_CUDA(cudaMalloc(&S.c, sizeof(float) * R * MLP_HID));
+   T9_CUDA(cudaMalloc(&S.y, sizeof(float) * R * MLP_OUT_PAD));
+   T9_CUDA(cudaMalloc(&S.t, sizeof(float) * R * MLP_OUT));
+   T9_CUDA(cudaMalloc(&S.dy, sizeof(__nv_bfloat16) * R * MLP_OUT_PAD));
+   T9_CUDA(cudaMalloc(&S.dyf, sizeof(float) * R * MLP_OUT_PAD));
+   T9_CUDA(cudaMalloc(&S.dz, sizeof(__nv_bfloat16) * R * MLP_HID));
+   T9_CUDA(cudaMalloc(&S.dzf, sizeof(float) * R * MLP_HID));
+   T9_CUDA(cudaMalloc(&S.err, sizeof(double) * R));
+   T9_CUDA(cudaMalloc(&S.loss, sizeof(double)));
+   S.nsplit = 64;
+   T9_CUDA(cudaMalloc(&S.split, sizeof(float) * (size_t)std::max<size_t>(S.nsplit * MLP_HID * MLP_HID, 1024 * MLP_HID)));
+   return mlp_init(ctx, seed);
+}
+
+// seeded Glorot-uniform weights, zero biases, optimiser state cleared
+int mlp_init(Context* ctx, unsigned seed)
+{
+   MlpState& S = ctx->mlp;
+   std::vector<float> w(MLP_NPARAM, 0.f);
+   std::vector<unsigned char> mask(MLP_NPARAM, 1);
+   std::vector<int> idx(MLP_NPARAM, -1);
+   std::mt19937 rng(seed);
+   auto fill = [&](int off, int bf, int fin, int fout, int cols_used) {
+      const float lim = std::sqrt(6.f / (fin + cols_used));
+      std::uniform_real_distribution<float> U(-lim, lim);
+      for (int r = 0; r < fin; ++r)
+         for (int c = 0; c < fout; ++c) {
+            const int i = off + r * fout + c;
+            idx[i] = bf + r * fout + c;
+            if (c < cols_used)
+               w[i] = U(rng);
+            else
+               mask[i] = 0;
+         }
+   };
+   fill(OFF_W1, BF_W1, MLP_IN, MLP_HID, MLP_HID);
+   fill(OFF_W2, BF_W2, MLP_HID, MLP_HID, MLP_HID);
+   fill(OFF_W3, BF_W3, MLP_HID, MLP_OUT_PAD, MLP_OUT);
+   for (int c = MLP_OUT; c < MLP_OUT_PAD; ++c)
+      mask[OFF_B3 + c] = 0;
+   T9_CUDA(cudaMemcpyAsync(S.mask, mask.data(), MLP_NPARAM, cudaMemcpyHostToDevice, ctx->stream));
+   T9_CUDA(cudaMemcpyAsync(S.wb_index, idx.data(), sizeof(int) * MLP_NPARAM, cudaMemcpyHostToDevice, ctx->stream));
+   T9_CHECK(mlp_set_weights(ctx, w.data()));
+   return T9GB_OK;
+}
+
+void mlp_free(Context* ctx)
+{
+   MlpState& S = ctx->mlp;
+   void* p[] = {S.step, S.w, S.g, S.m, S.v, S.mask, S.wb_index, S.wb, S.x, S.z1, S.z2, S.h1, S.h2, S.c, S.y, S.t, S.dy,
+      S.dyf, S.dz, S.dzf, S.err, S.loss, S.split};
+   for (void* q : p)
+      if (q)
+         cudaFree(q);
+   S = MlpState();
+}
+
+// master weights from the host; resets the optimiser moments
+int mlp_set_weights(Context* ctx, const float* w_host)
+{
+   MlpState& S = ctx->mlp;
+   std::vector<float> w(w_host, w_host + MLP_NPARAM);
+   std::vector<__nv_bfloat16> wb(BF_END);
+   auto cp = [&](int off, int bf, int size) {
+      for (int i = 0; i < size; ++i)
+         wb[bf + i] = __float2bfloat16(w[off + i]);
+   };
+   cp(OFF_W1, BF_W1, MLP_IN * MLP_HID);
+   cp(OFF_W2, BF_W2, MLP_HID * MLP_HID);
+   cp(OFF_W3, BF_W3, MLP_HID * MLP_OUT_PAD);
+   cudaStream_t st = ctx->stream;
+   T9_CUDA(cudaMemcpyAsync(S.w, w.data(), sizeof(float) * MLP_NPARAM, cudaMemcpyHostToDevice, st));
+   T9_CUDA(cudaMemcpyAsync(S.wb, wb.data(), sizeof(__nv_bfloat16) * BF_END, cudaMemcpyHostToDevice, st));
+   T9_CUDA(cudaMemsetAsync(S.m, 0, sizeof(float) * MLP_NPARAM, st));
+   T9_CUDA(cudaMemsetAsync(S.v, 0, sizeof(float) * MLP_NPARAM, st));
+   T9_CUDA(cudaMemsetAsync(S.step, 0, sizeof(int), st));
+   T9_CUDA(cudaStreamSynchronize(st));  // the host vectors go out of scope
+   return T9GB_OK;
+}
+
+int mlp_get_weights(Context* ctx, float* w_host)
+{
+   T9_CUDA(cudaMemcpyAsync(w_host, ctx->mlp.w, sizeof(float) * MLP_NPARAM, cudaMemcpyDeviceToHost, ctx->stream));
+   T9_CUDA(cudaStreamSynchronize(ctx->stream));
+   return T9GB_OK;
+}
+
+// forward over rows of S.x; outputs in S.y [rows][8]
+int mlp_forward(Context* ctx, int rows)
+{
+   MlpState& S = ctx->mlp;
+   const __nv_bfloat16* wb = reinterpret_cast<const __nv_bfloat16*>(S.wb);
+   T9_CHECK(gemm(ctx, false, false, rows, MLP_HID, MLP_IN, S.x, MLP_IN, wb + BF_W1, MLP_HID, S.c, 1));
+   k_bias_act<<<grid_for((long long)rows * MLP_HID, 256), 256, 0, ctx->stream>>>(rows, MLP_HID, MLP_HID, S.c,
+      S.w + OFF_B1, S.z1, S.h1, 1);
+   T9_CHECK(gemm(ctx, false, false, rows, MLP_HID, MLP_HID, S.h1, MLP_HID, wb + BF_W2, MLP_HID, S.c, 1));
+   k_bias_act<<<grid_for((long long)rows * MLP_HID, 256), 256, 0, ctx->stream>>>(rows, MLP_HID, MLP_HID, S.c,
+      S.w + OFF_B2, S.z2, S.h2, 1);
+   T9_CHECK(gemm(ctx, false, false, rows, MLP_OUT_PAD, MLP_HID, S.h2, MLP_HID, wb + BF_W3, MLP_OUT_PAD, S.c, 1));
+   k_bias_act<<<grid_for((long long)rows * MLP_OUT_PAD, 256), 256, 0, ctx->stream>>>(rows, MLP_OUT_PAD,
+      MLP_OUT_PAD, S.c, S.w + OFF_B3, S.y, nullptr, 0);
+   T9_CUDA(cudaGetLastError());
+   return T9GB_OK;
+}
+
+// loss and full gradient for rows of S.x with targets S.t (after forward);
+// gradient in S.g, summed squared error in S.loss.  rowpol (may be null):
+// rows r with rowpol[r % npad] == 0 are left out.
+int mlp_backward(Context* ctx, int rows, const float* rowpol, int npad)
+{
+   MlpState& S = ctx->mlp;
+   const __nv_bfloat16* wb = reinterpret_cast<const __nv_bfloat16*>(S.wb);
+   const int ns = S.nsplit;
+   k_loss_grad<<<grid_for(rows, 256), 256, 0, ctx->stream>>>(rows, S.y, S.t, rowpol, npad, S.dy, S.dyf,
+      S.err);
+   k_sum_double<<<1, 256, 0, ctx->stream>>>(rows, S.err, S.loss);
+   T9_CUDA(cudaMemsetAsync(S.g, 0, sizeof(float) * MLP_NPARAM, ctx->stream));
+   // layer 3: dW3 = H2^T dY, db3 = colsum dY, dH2 = dY W3^T
+   T9_CHECK(gemm(ctx, true, false, MLP_HID, MLP_OUT_PAD, rows, S.h2, MLP_HID, S.dy, MLP_OUT_PAD, S.g + OFF_W3, ns));
+   const int rchunk = (rows + 1023) / 1024;
+   const int nb = grid_for(rows, rchunk);
+   k_colsum_part<<<nb, 64, 0, ctx->stream>>>(rows, MLP_OUT_PAD, rchunk, S.dyf, S.split);
+   k_sum_splits<<<1, 64, 0, ctx->stream>>>(MLP_OUT_PAD, nb, S.split, S.g + OFF_B3);
+   T9_CHECK(gemm(ctx, false, true, rows, MLP_HID, MLP_OUT_PAD, S.dy, MLP_OUT_PAD, wb + BF_W3, MLP_OUT_PAD, S.c, 1));
+   k_silu_back<<<grid_for((long long)rows * MLP_HID, 256), 256, 0, ctx->stream>>>(rows * MLP_HID, S.c, S.z2, S.dz,
+      S.dzf);
+   // layer 2: dW2 = H1^T dZ2, db2, dH1 = dZ2 W2^T
+   T9_CHECK(gemm(ctx, true, false, MLP_HID, MLP_HID, rows, S.h1, MLP_HID, S.dz, MLP_HID, S.g + OFF_W2, ns));
+   k_colsum_part<<<nb, 64, 0, ctx->stream>>>(rows, MLP_HID, rchunk, S.dzf, S.split);
+   k_sum_splits<<<1, 64, 0, ctx->stream>>>(MLP_HID, nb, S.split, S.g + OFF_B2);
+   T9_CHECK(gemm(ctx, false, true, rows, MLP_HID, MLP_HID, S.dz, MLP_HID, wb + BF_W2, MLP_HID, S.c, 1));
+   k_silu_back<<<grid_for((long long)rows * MLP_HID, 256), 256, 0, ctx->stream>>>(rows * MLP_HID, S.c, S.z1, S.dz,
+      S.dzf);
+   // layer 1: dW1 = X^T dZ1, db1
+   T9_CHECK(gemm(ctx, true, false, MLP_IN, MLP_HID, rows, S.x, MLP_IN, S.dz, MLP_HID, S.g + OFF_W1, ns));
+   k_colsum_part<<<nb, 64, 0, ctx->stream>>>(rows, MLP_HID, rchunk, S.dzf, S.split);
+   k_sum_splits<<<1, 64, 0, ctx->stream>>>(MLP_HID, nb, S.split, S.g + OFF_B1);
+   T9_CUDA(cudaGetLastError());
+   return T9GB_OK;
+}
+
+int mlp_adamw(Context* ctx, float lr, float wd)
+{
+   MlpState& S = ctx->mlp;
+   k_adamw<<<1, 1024, 0, ctx->stream>>>(MLP_NPARAM, lr, 0.9f, 0.999f, 1e-8f, wd, S.step, S.w, S.g, S.m, S.v, S.mask,
+      reinterpret_cast<__nv_bfloat16*>(S.wb), S.wb_index);
+   T9_CUDA(cudaGetLastError());
+   return T9GB_OK;
+}
+
+}  // namespace t9gb

@@ -196,13 +196,12 @@ int order_build(Context* ctx)
       T9_CUDA(cudaMalloc(&ctx->nbr, sizeof(int) * (size_t)npad * cap));
       ctx->nbr_cap = cap;
    }
+   // legacy-stream copies above finish before the stream's kernels
+   T9_CUDA(cudaDeviceSynchronize());
    T9_CHECK(fill_row_padding(ctx));
    ctx->have_order = true;
    ctx->list_stale = true;
-   if (ctx->graph_exec) {
-      cudaGraphExecDestroy(ctx->graph_exec);
-      ctx->graph_exec = nullptr;
-   }
+   drop_graphs(ctx);
    // a new order invalidates the predictor history
    return reset_predictor(ctx);
 }
@@ -652,16 +651,20 @@ __global__ void k_chkpole(int n, int4* __restrict__ frames, float* __restrict__ 
 }
 
 // rows of 12: q, d xyz, qxx, qyy, qzz, qxy, qxz, qyz, thole, polarizability
+// also stores the local frame (rows x, y, z axes) per slot in sframe[9]
 __global__ void k_rotpole(int npad, const int* __restrict__ perm, const int4* __restrict__ frames,
    const float* __restrict__ pole, const float* __restrict__ xyz, const float2* __restrict__ sdamp,
-   const float* __restrict__ spolar, float* __restrict__ rpole)
+   const float* __restrict__ spolar, float* __restrict__ rpole, float* __restrict__ sframe)
 {
    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < npad; s += gridDim.x * blockDim.x) {
       int i = perm[s];
       float* rp = rpole + 12 * s;
+      float* fr = sframe + 9 * s;
       if (i < 0) {
          for (int c = 0; c < 12; ++c)
             rp[c] = 0.f;
+         for (int c = 0; c < 9; ++c)
+            fr[c] = (c % 4 == 0) ? 1.f : 0.f;
          continue;
       }
       rp[10] = sdamp[s].y;
@@ -716,6 +719,9 @@ __global__ void k_rotpole(int npad, const int* __restrict__ perm, const int4* __
          a[1][1] = a[0][0] * a[2][2] - a[0][2] * a[2][0];
          a[1][2] = a[0][1] * a[2][0] - a[0][0] * a[2][1];
       }
+      for (int r = 0; r < 3; ++r)
+         for (int c = 0; c < 3; ++c)
+            fr[3 * r + c] = a[r][c];
       const float* p = pole + 10 * i;
       rp[0] = p[0];
       for (int c = 0; c < 3; ++c)
@@ -743,7 +749,7 @@ int rotpole_sorted(Context* ctx)
 {
    k_chkpole<<<grid_for(ctx->n, 256), 256, 0, ctx->stream>>>(ctx->n, ctx->frames, ctx->pole, ctx->xyz);
    k_rotpole<<<grid_for(ctx->npad, 128), 128, 0, ctx->stream>>>(ctx->npad, ctx->perm, ctx->frames, ctx->pole,
-      ctx->xyz, ctx->sdamp, ctx->spolar, ctx->srpole);
+      ctx->xyz, ctx->sdamp, ctx->spolar, ctx->srpole, ctx->sframe);
    T9_CUDA(cudaGetLastError());
    return T9GB_OK;
 }

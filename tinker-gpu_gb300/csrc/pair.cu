@@ -607,3 +607,181 @@ int launch_empole_real(Context* ctx, double* e_atom)
    return T9GB_OK;
 }
 }  // namespace t9gb
+
+// ---------------------------------------------------------------------------
+// Descriptors of the learned initial guess.  Per slot i two rows of 32
+// features, row i for the d dipoles and row npad + i for the p dipoles; every
+// vector is expressed in the atom's local multipole frame (rows of
+// sframe[9]), so the features are invariant under rotations of the system:
+//   0-2   direct field E (d or p)
+//   3     polarizability alpha_i
+//   4-10  sum_k fc(r) g(r; mu, 0.5), mu = 1, 1.83, ..., 6            (count)
+//   11-14 sum_k q_k fc g(r; mu, 0.75), mu = 1.5, 3, 4.5, 6           (charge)
+//   15-20 sum_k q_k fc g(r; mu, 1) r_hat, mu = 2, 4.5 (x, y, z each)  (charge
+//         direction)
+//   21-25 sum_k alpha_k fc g(r; mu, 0.6), mu = 1, 2.25, ..., 6     (polarizability)
+//   26-31 first-order mutual field of the neighbours' direct dipoles,
+//         sum_k -T_ik^Thole (alpha_k E_k) * u-scale, split r < 3.5 / r >= 3.5
+// over all partners within 6 A; fc = (1 + cos(pi r / 6)) / 2.
+// g(r; mu, s) = exp(-(r - mu)^2 / (2 s^2)).
+
+namespace t9gb {
+
+constexpr float DESC_CUT = 6.f;
+constexpr int NFEAT = 32;
+
+__device__ __forceinline__ float gauss(float r, float mu, float inv2s2)
+{
+   const float t = r - mu;
+   return __expf(-t * t * inv2s2);
+}
+
+// acc layout: gr[0..7) gq[7..11) dq[11..17) ga[17..22) fd[22..28) fp[28..34)
+constexpr int DACC = 34;
+
+__device__ __forceinline__ void desc_pair(float r2, float3 d, float us, float pdi, float pti, float pdk,
+   const float* uk, float qk, float* acc)
+{
+   const float invr = rsqrtf(r2);
+   const float r = r2 * invr;
+   const float fc = 0.5f * (__cosf(3.14159265f / DESC_CUT * r) + 1.f);
+#pragma unroll
+   for (int j = 0; j < 7; ++j)
+      acc[j] += fc * gauss(r, 1.f + (5.f / 6.f) * j, 2.f);
+#pragma unroll
+   for (int j = 0; j < 4; ++j)
+      acc[7 + j] += qk * fc * gauss(r, 1.5f * (j + 1), 1.f / (2.f * 0.75f * 0.75f));
+   const float h0 = qk * fc * gauss(r, 2.f, 0.5f) * invr, h1 = qk * fc * gauss(r, 4.5f, 0.5f) * invr;
+   acc[11] += h0 * d.x;
+   acc[12] += h0 * d.y;
+   acc[13] += h0 * d.z;
+   acc[14] += h1 * d.x;
+   acc[15] += h1 * d.y;
+   acc[16] += h1 * d.z;
+   const float polk = uk[7];
+#pragma unroll
+   for (int j = 0; j < 5; ++j)
+      acc[17 + j] += polk * fc * gauss(r, 1.f + 1.25f * j, 1.f / (2.f * 0.6f * 0.6f));
+   float s3, s5, s7;
+   thole_damp(r, pdi, pti, pdk, uk[6], s3, s5, s7);
+   const float ir3 = invr * invr * invr;
+   const float rr3 = us * s3 * ir3;
+   const float rr5 = 3.f * us * s5 * ir3 * invr * invr;
+   const int o = r < 3.5f ? 0 : 3;
+   float c = rr5 * (d.x * uk[0] + d.y * uk[1] + d.z * uk[2]);
+   acc[22 + o] += c * d.x - rr3 * uk[0];
+   acc[23 + o] += c * d.y - rr3 * uk[1];
+   acc[24 + o] += c * d.z - rr3 * uk[2];
+   c = rr5 * (d.x * uk[3] + d.y * uk[4] + d.z * uk[5]);
+   acc[28 + o] += c * d.x - rr3 * uk[3];
+   acc[29 + o] += c * d.y - rr3 * uk[4];
+   acc[30 + o] += c * d.z - rr3 * uk[5];
+}
+
+__device__ __forceinline__ void to_local(const float* F, const float* v, float* out)
+{
+#pragma unroll
+   for (int a = 0; a < 3; ++a)
+      out[a] = F[3 * a] * v[0] + F[3 * a + 1] * v[1] + F[3 * a + 2] * v[2];
+}
+
+template <int G>
+__global__ void __launch_bounds__(256) k_learn_features(PairParams P, int npad, const int* __restrict__ nbr,
+   const int* __restrict__ nnbr, const int* __restrict__ sp_start, const int* __restrict__ sp_j,
+   const float4* __restrict__ sp_sc, const float4* __restrict__ spos, const float* __restrict__ srpole,
+   const float* __restrict__ sframe, const float* __restrict__ e8, const float* __restrict__ u8,
+   float* __restrict__ xf)
+{
+   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+   const int i = tid / G, g = tid % G;
+   if (i >= npad)
+      return;
+   float acc[DACC];
+#pragma unroll
+   for (int c = 0; c < DACC; ++c)
+      acc[c] = 0.f;
+   if (i < P.n) {
+      const float4 pi = spos[i];
+      const float pti = u8[8 * i + 6];
+      const int* row = nbr + (size_t)i * P.cap;
+      const int cnt = nnbr[i];
+      for (int k = g; k < cnt; k += G) {
+         const int j = row[k];
+         const float4 pk = spos[j];
+         const float3 d = sep(P, pi, pk);
+         const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
+         if (r2 < DESC_CUT * DESC_CUT) {
+            float uk[8];
+            load8(u8, j, uk);
+            desc_pair(r2, d, 1.f, pi.w, pti, pk.w, uk, srpole[12 * j], acc);
+         }
+      }
+      const int pa = sp_start[i], pb = sp_start[i + 1];
+      for (int q = pa + g; q < pb; q += G) {
+         const int j = sp_j[q];
+         const float4 pk = spos[j];
+         const float3 d = sep(P, pi, pk);
+         const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
+         if (r2 < DESC_CUT * DESC_CUT) {
+            float uk[8];
+            load8(u8, j, uk);
+            desc_pair(r2, d, sp_sc[q].w, pi.w, pti, pk.w, uk, srpole[12 * j], acc);
+         }
+      }
+   }
+   group_reduce<G, DACC>(acc);
+   if (g >= 2)
+      return;
+   // lane 0 writes the d row, lane 1 the p row
+   float* x = xf + (size_t)(g == 0 ? i : npad + i) * NFEAT;
+   if (i >= P.n) {
+      for (int c = 0; c < NFEAT; ++c)
+         x[c] = 0.f;
+      return;
+   }
+   float F[9];
+   for (int c = 0; c < 9; ++c)
+      F[c] = sframe[9 * i + c];
+   float v[3], l[3];
+   for (int c = 0; c < 3; ++c)
+      v[c] = e8[8 * i + 3 * g + c];
+   to_local(F, v, l);
+   x[0] = l[0];
+   x[1] = l[1];
+   x[2] = l[2];
+   x[3] = u8[8 * i + 7];
+   for (int c = 0; c < 7; ++c)
+      x[4 + c] = acc[c];
+   for (int c = 0; c < 4; ++c)
+      x[11 + c] = acc[7 + c];
+   to_local(F, acc + 11, l);
+   x[15] = l[0];
+   x[16] = l[1];
+   x[17] = l[2];
+   to_local(F, acc + 14, l);
+   x[18] = l[0];
+   x[19] = l[1];
+   x[20] = l[2];
+   for (int c = 0; c < 5; ++c)
+      x[21 + c] = acc[17 + c];
+   const int fo = g == 0 ? 22 : 28;
+   to_local(F, acc + fo, l);
+   x[26] = l[0];
+   x[27] = l[1];
+   x[28] = l[2];
+   to_local(F, acc + fo + 3, l);
+   x[29] = l[0];
+   x[30] = l[1];
+   x[31] = l[2];
+}
+
+int launch_learn_features(Context* ctx, const float* e8, const float* u8, float* xf)
+{
+   PairParams P = make_params(ctx, DESC_CUT);
+   k_learn_features<GROUP><<<grid_for((long long)ctx->npad * GROUP, PAIR_THREADS), PAIR_THREADS, 0, ctx->stream>>>(P,
+      ctx->npad, ctx->nbr, ctx->nnbr, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos, ctx->srpole, ctx->sframe, e8,
+      u8, xf);
+   T9_CUDA(cudaGetLastError());
+   return T9GB_OK;
+}
+}  // namespace t9gb

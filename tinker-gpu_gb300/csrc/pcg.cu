@@ -21,13 +21,9 @@
 #include <cmath>
 
 #include "common.cuh"
+#include "reduce.cuh"
 
 namespace t9gb {
-
-// device doubles (ctx->scal) and ints (ctx->status)
-enum { S_SUM_D = 0, S_SUM_P, S_A_D, S_A_P, S_B_D, S_B_P, S_EPS, S_NSCAL = 16 };
-enum { ST_ITER = 0, ST_DONE, ST_STATUS, ST_NUALT, ST_TICKET0, ST_TICKET1, ST_NSTAT = 8 };
-enum { R_PAP_D = 0, R_PAP_P, R_RZ_D, R_RZ_P, R_RR_D, R_RR_P };
 
 constexpr int VB = 256;  // vector-kernel block size
 
@@ -36,77 +32,6 @@ constexpr int VB = 256;  // vector-kernel block size
 __constant__ double c_aspc[16] = {62. / 17., -310. / 51., 2170. / 323., -2329. / 400., 1701. / 409., -806. / 323.,
    1024. / 809., -479. / 883., 257. / 1316., -434. / 7429., 191. / 13375., -62. / 22287., 3. / 7217.,
    -3. / 67015., 2. / 646323., -1. / 9694845.};
-
-__device__ double block_sum(double v, double* sh)
-{
-#pragma unroll
-   for (int o = 16; o > 0; o >>= 1)
-      v += __shfl_down_sync(0xffffffffu, v, o);
-   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-   if (l == 0)
-      sh[w] = v;
-   __syncthreads();
-   double r = 0;
-   if (threadIdx.x < 32) {
-      r = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1)
-         r += __shfl_down_sync(0xffffffffu, r, o);
-   }
-   __syncthreads();
-   return r;  // valid in thread 0
-}
-
-// Fixed-order sums of `ns` (<= 4) consecutive partial slots, computed
-// together: 64 threads per slot stride through the nb partials, then a fixed
-// shuffle tree and one combine (blockDim must be 256).  Returns the sums in
-// out[0..ns) of every thread.
-__device__ void sum_slots(const double* red, int first, int ns, int nb, double* sh, double* out)
-{
-   const int slot = threadIdx.x >> 6, sub = threadIdx.x & 63;
-   double v = 0;
-   if (slot < ns)
-      for (int i = sub; i < nb; i += 64)
-         v += red[(first + slot) * RED_MAX + i];
-#pragma unroll
-   for (int o = 16; o > 0; o >>= 1)
-      v += __shfl_down_sync(0xffffffffu, v, o);
-   if ((threadIdx.x & 31) == 0)
-      sh[threadIdx.x >> 5] = v;
-   __syncthreads();
-   for (int k = 0; k < ns; ++k)
-      out[k] = sh[2 * k] + sh[2 * k + 1];
-   __syncthreads();
-}
-
-// store this block's partial sum of v
-__device__ void store_partial(double* red, int slot, double v, double* sh)
-{
-   v = block_sum(v, sh);
-   if (threadIdx.x == 0)
-      red[slot * RED_MAX + blockIdx.x] = v;
-}
-
-// true in the block that finishes last (threadfence + ticket); it resets the
-// ticket for the next launch
-
-__device__ bool last_block(int* ticket)
-{
-   __shared__ bool last;
-   __threadfence();
-   __syncthreads();
-   if (threadIdx.x == 0) {
-      unsigned prev = atomicAdd(reinterpret_cast<unsigned*>(ticket), 1u);
-      last = prev == gridDim.x - 1;
-   }
-   __syncthreads();
-   if (last) {
-      __threadfence();
-      if (threadIdx.x == 0)
-         *ticket = 0;
-   }
-   return last;
-}
 
 struct VecArgs {
    int ne;   // 6 * npad active elements (d xyz, p xyz of each slot)
@@ -357,12 +282,9 @@ int check_list_overflow(Context* ctx, int* redo)
    T9_CUDA(cudaMalloc(&ctx->nbr, sizeof(int) * (size_t)ctx->npad * cap));
    ctx->nbr_cap = cap;
    *ctx->h_over = 0;
-   T9_CUDA(cudaMemset(ctx->nbr_over, 0, sizeof(int)));
+   T9_CUDA(cudaMemsetAsync(ctx->nbr_over, 0, sizeof(int), ctx->stream));
    ctx->list_stale = true;
-   if (ctx->graph_exec) {
-      cudaGraphExecDestroy(ctx->graph_exec);
-      ctx->graph_exec = nullptr;
-   }
+   drop_graphs(ctx);
    *redo = 1;
    return T9GB_OK;
 }
@@ -401,19 +323,35 @@ static int pcg_body(Context* ctx, const VecArgs& A, cudaGraphConditionalHandle h
    return T9GB_OK;
 }
 
+// start variants: the plain guess (ASPC / alpha E / zero), the learned guess
+// for both systems, or both with the per-system residual comparison
+enum { V_PLAIN = 0, V_LEARNED = 1, V_COMPARE = 2 };
+
 // neighbour list, permanent field, guess, r0, M r0 and s = r.z
-static int pcg_start(Context* ctx, const VecArgs& A, bool graph)
+static int pcg_start(Context* ctx, const VecArgs& A, bool graph, int variant)
 {
    const t9gb_config& c = ctx->cfg;
    T9_CHECK(graph ? list_now(ctx) : ensure_list(ctx));
    T9_CHECK(dfield6(ctx, ctx->fld6));
    k_init_guess<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->fld6, ctx->efield, ctx->udir, ctx->uind, c.pcgguess,
       c.predictor == 1 ? 1 : 0, ctx->aspc_hist, ctx->status);
-   const bool zero_guess = !c.pcgguess && c.predictor != 1;
+   // the network runs when its guess is used or when this solve trains it
+   if ((ctx->learn_mode & 1) || variant != V_PLAIN)
+      T9_CHECK(learn_forward(ctx));
+   if (variant == V_LEARNED)
+      T9_CHECK(learn_guess(ctx, ctx->uind, 1));
+   else if (variant == V_COMPARE)
+      T9_CHECK(learn_guess(ctx, ctx->tmp6, 0));
+   const bool zero_guess = !c.pcgguess && c.predictor != 1 && variant != V_LEARNED;
    if (!zero_guess)
       T9_CHECK(ufield6(ctx, ctx->uind, ctx->fld6));
    k_init_rsd<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->fld6, ctx->efield, ctx->udir, ctx->uind, ctx->rsd,
       zero_guess ? 1 : 0);
+   if (variant == V_COMPARE) {
+      // residual of the learned guess; each of d, p starts from the smaller
+      T9_CHECK(ufield6(ctx, ctx->tmp6, ctx->vec));
+      T9_CHECK(learn_pick(ctx, ctx->tmp6, ctx->vec));
+   }
    if (A.sparse)
       T9_CHECK(launch_precond_sparse(ctx, ctx->rsd, ctx->zrsd));
    k_precond_dot<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->rsd, ctx->zrsd, ctx->conj, ctx->red, ctx->scal, ctx->status,
@@ -424,6 +362,8 @@ static int pcg_start(Context* ctx, const VecArgs& A, bool graph)
 
 static int pcg_finish(Context* ctx, const VecArgs& A)
 {
+   if (ctx->learn_mode & 1)
+      T9_CHECK(learn_train(ctx));
    if (ctx->cfg.predictor == 1) {
       k_save_hist<<<A.nb, VB, 0, ctx->stream>>>(A.ne8, ctx->uind, ctx->aspc_hist, ctx->status);
       k_bump_nualt<<<1, 1, 0, ctx->stream>>>(ctx->status);
@@ -435,10 +375,10 @@ static int pcg_finish(Context* ctx, const VecArgs& A)
 }
 
 // host-driven loop (used while profiling: every launch is bracketed)
-static int induce_stepwise(Context* ctx)
+static int induce_stepwise(Context* ctx, int variant)
 {
    const VecArgs A = vec_args(ctx);
-   T9_CHECK(pcg_start(ctx, A, false));
+   T9_CHECK(pcg_start(ctx, A, false, variant));
    const int politer = std::max(1, ctx->cfg.politer);
    for (int it = 0; it < politer; ++it) {
       T9_CHECK(pcg_body(ctx, A, 0, 0));
@@ -454,7 +394,7 @@ static int induce_stepwise(Context* ctx)
 }
 
 // capture the whole induce() into one graph with a conditional WHILE loop
-static int induce_capture(Context* ctx)
+static int induce_capture(Context* ctx, int variant)
 {
    const VecArgs A = vec_args(ctx);
    cudaStream_t s0 = ctx->stream;
@@ -462,7 +402,7 @@ static int induce_capture(Context* ctx)
       T9_CUDA(cudaStreamCreateWithFlags(&ctx->cap_stream, cudaStreamNonBlocking));
    cudaGraph_t graph = nullptr;
    T9_CUDA(cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal));
-   int rc = pcg_start(ctx, A, true);
+   int rc = pcg_start(ctx, A, true, variant);
    cudaStreamCaptureStatus cs;
    cudaGraph_t cap = nullptr;
    const cudaGraphNode_t* deps = nullptr;
@@ -507,11 +447,11 @@ static int induce_capture(Context* ctx)
       rc = T9GB_CUDA_ERR;
    }
    if (rc == T9GB_OK) {
-      e = cudaGraphInstantiate(&ctx->graph_exec, graph, 0);
+      e = cudaGraphInstantiate(&ctx->graph_exec[variant], graph, 0);
       if (e != cudaSuccess) {
          ctx->last_error = std::string("graph instantiate: ") + cudaGetErrorString(e);
          rc = T9GB_CUDA_ERR;
-         ctx->graph_exec = nullptr;
+         ctx->graph_exec[variant] = nullptr;
       }
    }
    if (graph)
@@ -522,21 +462,47 @@ static int induce_capture(Context* ctx)
    return rc;
 }
 
-static int induce_graph(Context* ctx)
+static int induce_graph(Context* ctx, int variant)
 {
-   if (!ctx->graph_exec)
-      T9_CHECK(induce_capture(ctx));
-   T9_CUDA(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+   if (!ctx->graph_exec[variant])
+      T9_CHECK(induce_capture(ctx, variant));
+   T9_CUDA(cudaGraphLaunch(ctx->graph_exec[variant], ctx->stream));
    T9_CUDA(cudaStreamSynchronize(ctx->stream));
    ctx->list_stale = false;
    return T9GB_OK;
 }
 
+void drop_graphs(Context* ctx)
+{
+   for (auto& g : ctx->graph_exec)
+      if (g) {
+         cudaGraphExecDestroy(g);
+         g = nullptr;
+      }
+}
+
+// host policy for the start variant: compare both starts every learn_probe
+// solves (and when the predictor history has just filled); in between start
+// from what the last comparison chose for both systems
+static int pick_variant(Context* ctx)
+{
+   if (!(ctx->learn_mode & 2))
+      return V_PLAIN;
+   if (ctx->learn_since_probe >= ctx->learn_probe)
+      return V_COMPARE;
+   if (ctx->learn_last_choice == 3)
+      return V_LEARNED;
+   if (ctx->learn_last_choice == 0)
+      return V_PLAIN;
+   return V_COMPARE;
+}
+
 int induce_sorted(Context* ctx)
 {
    const bool graph = ctx->use_graph && !ctx->prof.on;
+   const int variant = pick_variant(ctx);
    for (int attempt = 0; attempt < 2; ++attempt) {
-      T9_CHECK(graph ? induce_graph(ctx) : induce_stepwise(ctx));
+      T9_CHECK(graph ? induce_graph(ctx, variant) : induce_stepwise(ctx, variant));
       int redo = 0;
       T9_CHECK(check_list_overflow(ctx, &redo));
       if (!redo)
@@ -552,6 +518,18 @@ int induce_sorted(Context* ctx)
    ctx->last_iter = ctx->h_status[ST_ITER];
    ctx->last_eps = ctx->h_scal[S_EPS];
    ctx->last_status = ctx->h_status[ST_STATUS];
+   ctx->learn_variant = variant;
+   if (variant == V_COMPARE) {
+      ctx->learn_last_choice = ctx->h_status[ST_LCHOICE];
+      ctx->learn_since_probe = 1;
+   } else {
+      ctx->learn_since_probe += 1;
+   }
+   // the plain start changes character once the predictor history is full
+   const bool full = ctx->cfg.predictor == 1 && ctx->h_status[ST_NUALT] >= 16;
+   if (full != ctx->learn_ring_full)
+      ctx->learn_since_probe = 1 << 30;
+   ctx->learn_ring_full = full;
    return ctx->last_status;
 }
 
