@@ -144,6 +144,40 @@ int t9gb_empole_energy(t9gb_context* ctx, double* energy, double* parts);
  * (src/cu/amoeba/epolar.cu:14-30, called by src/amoeba/epolar.cpp:550-572). */
 int t9gb_epolar_energy(t9gb_context* ctx, double* energy);
 
+/* Calc flags of the energy/gradient entry points, the reference's calc::
+ * bits (include/tool/rcman.h:105-155). */
+#define T9GB_CALC_ENERGY 0x010
+#define T9GB_CALC_GRAD 0x020
+#define T9GB_CALC_VIRIAL 0x040 /* not available yet: returns T9GB_BAD_ARG */
+
+/* Permanent-multipole energy (kcal/mol) and gradient (kcal/mol/A, device
+ * float [n][3], caller order, written -- not accumulated) of the current
+ * coordinates and rotated multipoles (call t9gb_mpole_init first), including
+ * the forces on the frame atoms from the multipole torques.  Replaces
+ * empole(int vers) (src/amoeba/empole.cpp:81-138) with its torque step
+ * (src/cu/amoeba/torque.cu:8-383).  vers: T9GB_CALC_ENERGY and/or
+ * T9GB_CALC_GRAD. */
+int t9gb_empole(t9gb_context* ctx, int vers, double* energy, float* grad_device, double* virial);
+
+/* Polarization: solves induce() on the current coordinates, then the energy
+ * (dot-product form) and/or the gradient at the converged dipoles.  Replaces
+ * epolar(int vers) (src/amoeba/epolar.cpp:550-649): epolar_cu1 /
+ * epolarEwaldRecipSelf_cu1 / epolar0DotProd / torque.  Returns the induce
+ * status (T9GB_NOT_CONVERGED ...) when the solve fails. */
+int t9gb_epolar(t9gb_context* ctx, int vers, double* energy, float* grad_device, double* virial);
+
+/* Both terms in one pass over the pair list (the MD path), energy = empole +
+ * epolar.  Replaces emplar(int vers) (src/amoeba/emplar.cpp:10-28,
+ * src/cu/amoeba/emplar.cu:505-606). */
+int t9gb_emplar(t9gb_context* ctx, int vers, double* energy, float* grad_device, double* virial);
+
+/* Components of the last energy evaluation (t9gb_empole_energy, t9gb_empole,
+ * t9gb_epolar, t9gb_emplar with T9GB_CALC_ENERGY): parts[4] = multipole
+ * real-space, reciprocal and self energy, polarization energy (kcal/mol),
+ * the reference's separate em/ep accumulators (src/amoeba/empole.cpp,
+ * src/amoeba/epolar.cpp). */
+int t9gb_energy_components(t9gb_context* ctx, double* parts);
+
 /* Run induce() as one CUDA graph (default, enable = 1: neighbour list,
  * permanent field, guess and the PCG loop as a conditional WHILE node with
  * the convergence test on the device) or as individually launched kernels

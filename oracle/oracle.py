@@ -234,6 +234,54 @@ class OracleSystem:
         return z, zp
 
 
+# ---------------------------------------------------------------------------
+# gradients by central differences of the FP64 energies
+#
+# empole: E(x) with the multipoles re-rotated into each displaced geometry,
+# so the frame (torque) terms are included.  epolar: the reference's
+# polarization gradient (src/amoeba/epolar.cpp, include/seq/pair_polar.h,
+# src/cu/epolarrecip.cu) is the gradient at fixed induced dipoles of
+#   G(x) = -1/2 f [ u_p . E_d(x) + u_d . E_p(x) + u_d . E_u(u_p)(x) ]
+# with E_d / E_p the d- / p-scaled permanent fields (dfield) and E_u the
+# mutual field (ufield); the permanent multipoles again follow the frames.
+# Both reproduce the reference's golden gradients (test/localframe.cpp).
+
+
+def _fd(fun, xyz, atoms, h):
+    g = np.zeros((len(atoms), 3))
+    for j, a in enumerate(atoms):
+        for d in range(3):
+            xp = xyz.copy()
+            xp[a, d] += h
+            xm = xyz.copy()
+            xm[a, d] -= h
+            g[j, d] = (fun(xp) - fun(xm)) / (2 * h)
+    return g
+
+
+def empole_gradient_fd(system, xyz=None, atoms=None, h=1e-5, **kw):
+    """dE_mpole/dx [len(atoms)][3], kcal/mol/A."""
+    xyz = np.array(system.xyz if xyz is None else xyz, dtype=np.float64)
+    atoms = range(system.n) if atoms is None else atoms
+    return _fd(lambda x: OracleSystem(system, x, **kw).empole_energy()[0], xyz, list(atoms), h)
+
+
+def epolar_g(system, xyz, uind, uinp, **kw):
+    o = OracleSystem(system, xyz, **kw)
+    fd, fp = o.dfield()
+    _, fu = o.ufield(np.zeros_like(uinp), uinp)
+    return -0.5 * o.s.electric * ((uinp * fd).sum() + (uind * fp).sum() + (uind * fu).sum())
+
+
+def epolar_gradient_fd(system, uind, uinp, xyz=None, atoms=None, h=1e-5, **kw):
+    """Polarization gradient at fixed dipoles [len(atoms)][3], kcal/mol/A."""
+    xyz = np.array(system.xyz if xyz is None else xyz, dtype=np.float64)
+    atoms = range(system.n) if atoms is None else atoms
+    ud = np.asarray(uind, dtype=np.float64)
+    up = np.asarray(uinp, dtype=np.float64)
+    return _fd(lambda x: epolar_g(system, x, ud, up, **kw), xyz, list(atoms), h)
+
+
 def bsmod(nfft, order=5):
     out = np.zeros(nfft)
     lib().or_bsmod(nfft, order, _dp(out))

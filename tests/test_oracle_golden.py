@@ -99,3 +99,30 @@ def test_empole_energy_golden_pme_parts(oracle):
     assert abs(parts[1] - ex["ref_erecip"]) < 1e-4
     assert abs(parts[2] - ex["ref_eself"]) < 1e-4
     assert abs(e - (ex["ref_ereal"] + ex["ref_erecip"] + ex["ref_eself"])) < 1e-4
+
+
+# The reference skips the last molecule (a planar NH3) in its gradient
+# comparisons (test/localframe.cpp:12-21, do_ij); so do these tests.
+GRAD_ATOMS = 18
+
+
+@pytest.mark.parametrize("ewald", [0, 1], ids=["gas", "pme"])
+def test_empole_gradient_golden(oracle, ewald):
+    """Local-Frame-1/2 empole gradients (localframe.cpp:49-72, :133-151), eps 5e-4."""
+    s, fx = L.system(ewald)
+    case = fx["expected"]["Local-Frame-2" if ewald else "Local-Frame-1"]
+    ex = case["empole -- pme" if ewald else "empole -- gas phase, no cutoff"]
+    g = oracle.empole_gradient_fd(s, atoms=range(GRAD_ATOMS))
+    ref = np.array(ex["ref_grad"])[:GRAD_ATOMS]
+    assert np.abs(g - ref).max() < ex["eps_g"]
+
+
+@pytest.mark.parametrize("ewald", [0, 1], ids=["nonewald", "pme"])
+def test_epolar_gradient_golden(oracle, ewald):
+    """Local-Frame-3/4 epolar gradients at the converged dipoles
+    (localframe.cpp:344-366, :521-543), eps 5e-4."""
+    s, fx = L.system(ewald)
+    ud, up, *_ = oracle.OracleSystem(s).induce()
+    g = oracle.epolar_gradient_fd(s, ud, up, atoms=range(GRAD_ATOMS))
+    ref = np.array(L.expected(fx, ewald)["epolar"]["ref_grad"])[:GRAD_ATOMS]
+    assert np.abs(g - ref).max() < 5e-4

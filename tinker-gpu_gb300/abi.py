@@ -27,7 +27,9 @@ EXPORTS = [
     "t9gb_induce_stats", "t9gb_get_udir", "t9gb_empole_energy", "t9gb_epolar_energy", "t9gb_use_graph", "t9gb_nblist_stats", "t9gb_profile_enable", "t9gb_profile_read", "t9gb_profile_name",
     "t9gb_ufield_noalloc", "t9gb_learn_config", "t9gb_learn_policy", "t9gb_learn_reset", "t9gb_learn_stats", "t9gb_learn_get_weights",
     "t9gb_learn_set_weights", "t9gb_learn_eval", "t9gb_learn_adamw", "t9gb_learn_features",
+    "t9gb_empole", "t9gb_epolar", "t9gb_emplar", "t9gb_energy_components",
 ]
+CALC_ENERGY, CALC_GRAD, CALC_VIRIAL = 0x010, 0x020, 0x040
 
 LEARN_NFEAT = 32
 LEARN_NPARAM = 6792
@@ -116,6 +118,9 @@ def load(path=None):
     lib.t9gb_learn_eval.argtypes = [vp, C.c_int, flp, flp, flp, flp, dp]
     lib.t9gb_learn_adamw.argtypes = [vp]
     lib.t9gb_learn_features.argtypes = [vp, fp]
+    lib.t9gb_energy_components.argtypes = [vp, dp]
+    for name in ("t9gb_empole", "t9gb_epolar", "t9gb_emplar"):
+        getattr(lib, name).argtypes = [vp, C.c_int, dp, fp, dp]
     _lib = lib
     return lib
 
@@ -371,3 +376,29 @@ class Engine:
         self._check(self.lib.t9gb_learn_features(self.h, C.c_void_p(out.data_ptr())))
         self.torch.cuda.synchronize()
         return out.cpu().numpy()
+
+    # ---- energies and gradients (calc flags of the reference) ----
+    def _eg(self, fn, vers):
+        e = C.c_double()
+        g = self._empty3() if vers & CALC_GRAD else None
+        rc = fn(self.h, int(vers), C.byref(e), C.c_void_p(g.data_ptr()) if g is not None else None, None)
+        self._check(rc, allow=(T9GB_NOT_CONVERGED,))
+        return e.value, g
+
+    def energy_components(self):
+        """[multipole real, recip, self, polarization] of the last energy evaluation."""
+        out = np.zeros(4)
+        self._check(self.lib.t9gb_energy_components(self.h, _dp(out)))
+        return out
+
+    def empole(self, vers=CALC_ENERGY | CALC_GRAD):
+        """(energy, gradient [n][3] device) of the permanent multipoles."""
+        return self._eg(self.lib.t9gb_empole, vers)
+
+    def epolar(self, vers=CALC_ENERGY | CALC_GRAD):
+        """Solves induce(), then (energy, gradient) of the polarization."""
+        return self._eg(self.lib.t9gb_epolar, vers)
+
+    def emplar(self, vers=CALC_ENERGY | CALC_GRAD):
+        """Both terms in one pass: (energy, gradient)."""
+        return self._eg(self.lib.t9gb_emplar, vers)

@@ -87,6 +87,7 @@ static void free_all(Context* ctx)
       cudaFreeHost(ctx->h_over);
    pme_free(ctx);
    learn_free(ctx);
+   force_free(ctx);
    drop_graphs(ctx);
    if (ctx->cap_stream)
       cudaStreamDestroy(ctx->cap_stream);
@@ -222,6 +223,7 @@ int t9gb_set_topology(t9gb_context* h, const int* frames, const double* pole, co
    for (size_t i = 0; i < pf.size(); ++i)
       pf[i] = (float)pole[i];
    T9_CUDA(cudaMemcpy(ctx->frames, frames, sizeof(int4) * n, cudaMemcpyHostToDevice));
+   ctx->h_frames.assign(frames, frames + 4 * (size_t)n);
    T9_CUDA(cudaMemcpy(ctx->pole, pf.data(), sizeof(float) * 10 * n, cudaMemcpyHostToDevice));
    T9_CUDA(cudaDeviceSynchronize());  // ordered before work on a non-blocking stream
    ctx->have_topology = true;

@@ -194,6 +194,15 @@ struct Context {
    float* xf = nullptr;         // [2 npad][32] raw features, d rows then p rows
    float* fstat = nullptr;      // feature mean[32], 1/std[32], target scale
    float* hout = nullptr;       // [6 n] host-copy staging
+
+   // forces (force.cu): per-slot real / reciprocal (permanent grid,
+   // dipole grid) forces and torque fields, frame forces by role, and the
+   // reverse frame map (slot j -> (slot i, role) entries)
+   float *freal = nullptr, *frecp = nullptr, *frecu = nullptr;
+   float *treal = nullptr, *trecp = nullptr, *trecu = nullptr;
+   float* fbuf = nullptr;
+   int *rev_start = nullptr, *rev_ent = nullptr;
+   std::vector<int> h_frames;  // [n][4] caller order
    // start policy (host): compare the plain and the learned start every
    // learn_probe solves; in between reuse the last comparison's verdict
    int learn_probe = 1;
@@ -305,6 +314,13 @@ int mlp_backward(Context* ctx, int rows, const float* rowpol, int npad);
 int mlp_adamw(Context* ctx, float lr, float wd);
 // learned guess (learn.cu)
 int launch_learn_features(Context* ctx, const float* e8, const float* u8, float* xf);  // pair.cu
+// forces (force.cu, pme.cu)
+int force_setup(Context* ctx);
+void force_free(Context* ctx);
+int frame_map_build(Context* ctx);
+int elec_forces(Context* ctx, bool mpole, bool polar, float* grad);
+int launch_force_recip(Context* ctx, bool mpole, bool polar);
+int induce_sorted(Context* ctx);
 int learn_setup(Context* ctx);
 void learn_free(Context* ctx);
 int learn_reset(Context* ctx, unsigned seed);

@@ -4,7 +4,10 @@
 //  - t9gb_empole_energy: permanent-multipole energy, real + reciprocal + self
 //    (empole(calc::energy), src/amoeba/empole.cpp:81-138);
 //  - t9gb_epolar_energy: polarization energy by the dot product
-//    -1/2 f sum_i u_d,i . E_p,i (epolar0DotProd, src/cu/amoeba/epolar.cu:14-30).
+//    -1/2 f sum_i u_d,i . E_p,i (epolar0DotProd, src/cu/amoeba/epolar.cu:14-30);
+//  - t9gb_empole / t9gb_epolar / t9gb_emplar: energy and gradient with the
+//    reference's calc flags (include/tool/rcman.h:105-155), forces from
+//    force.cu.
 #include "common.cuh"
 
 namespace t9gb {
@@ -90,4 +93,111 @@ extern "C" int t9gb_epolar_energy(t9gb_context* h, double* energy)
    T9_CUDA(cudaStreamSynchronize(ctx->stream));
    *energy = ctx->h_scal[36];
    return T9GB_OK;
+}
+
+namespace t9gb {
+
+static int sum_empole(Context* ctx, double* energy)
+{
+   k_sum_rows<<<3, 1024, 0, ctx->stream>>>(ctx->npad, ctx->npad, ctx->e_atom, ctx->scal + 32);
+   T9_CUDA(cudaGetLastError());
+   T9_CUDA(cudaMemcpyAsync(ctx->h_scal + 32, ctx->scal + 32, sizeof(double) * 3, cudaMemcpyDeviceToHost, ctx->stream));
+   T9_CUDA(cudaStreamSynchronize(ctx->stream));
+   *energy = ctx->h_scal[32] + ctx->h_scal[33] + ctx->h_scal[34];
+   return T9GB_OK;
+}
+
+static int check_vers(Context* ctx, int vers, double* energy, float* grad, double* virial)
+{
+   if ((vers & T9GB_CALC_ENERGY) && !energy)
+      return T9GB_BAD_ARG;
+   if ((vers & T9GB_CALC_GRAD) && !grad)
+      return T9GB_BAD_ARG;
+   if (vers & T9GB_CALC_VIRIAL) {
+      (void)virial;
+      ctx->last_error = "virial is not available";
+      return T9GB_BAD_ARG;
+   }
+   if (!(vers & (T9GB_CALC_ENERGY | T9GB_CALC_GRAD)))
+      return T9GB_BAD_ARG;
+   if (!ctx->have_order)
+      return T9GB_NOT_READY;
+   return T9GB_OK;
+}
+
+// mpole / polar terms on the current coordinates and rotated multipoles
+static int elec_terms(Context* ctx, bool mpole, bool polar, int vers, double* energy, float* grad)
+{
+   double e = 0;
+   if (polar) {
+      int rc = induce_sorted(ctx);
+      if (rc != T9GB_OK)
+         return rc;
+   }
+   for (int attempt = 0; attempt < 2; ++attempt) {
+      T9_CHECK(ensure_list(ctx));
+      T9_CUDA(cudaMemsetAsync(ctx->e_atom, 0, sizeof(double) * 3 * ctx->npad, ctx->stream));
+      if (vers & T9GB_CALC_GRAD) {
+         T9_CHECK(elec_forces(ctx, mpole, polar, grad));
+      } else if (mpole) {
+         T9_CHECK(launch_empole_real(ctx, ctx->e_atom));
+         T9_CHECK(launch_empole_recip(ctx, ctx->e_atom + ctx->npad));
+      }
+      T9_CUDA(cudaStreamSynchronize(ctx->stream));
+      int redo = 0;
+      T9_CHECK(check_list_overflow(ctx, &redo));
+      if (!redo)
+         break;
+   }
+   if (vers & T9GB_CALC_ENERGY) {
+      if (mpole)
+         T9_CHECK(sum_empole(ctx, &e));
+      if (polar) {
+         k_epolar_dot<<<grid_for(ctx->npad, 256), 256, 0, ctx->stream>>>(ctx->npad, ctx->cfg.electric, ctx->uind,
+            ctx->udir, ctx->spolinv, ctx->e_atom);
+         k_sum_rows<<<1, 1024, 0, ctx->stream>>>(ctx->npad, ctx->npad, ctx->e_atom, ctx->scal + 36);
+         T9_CUDA(cudaGetLastError());
+         T9_CUDA(cudaMemcpyAsync(ctx->h_scal + 36, ctx->scal + 36, sizeof(double), cudaMemcpyDeviceToHost,
+            ctx->stream));
+         T9_CUDA(cudaStreamSynchronize(ctx->stream));
+         e += ctx->h_scal[36];
+      }
+      *energy = e;
+   }
+   return T9GB_OK;
+}
+
+}  // namespace t9gb
+
+extern "C" int t9gb_energy_components(t9gb_context* h, double* parts)
+{
+   if (!h || !parts)
+      return T9GB_BAD_ARG;
+   for (int c = 0; c < 4; ++c)
+      parts[c] = h->c.h_scal[32 + c + (c == 3 ? 1 : 0)];
+   return T9GB_OK;
+}
+
+extern "C" int t9gb_empole(t9gb_context* h, int vers, double* energy, float* grad, double* virial)
+{
+   if (!h)
+      return T9GB_BAD_ARG;
+   T9_CHECK(check_vers(&h->c, vers, energy, grad, virial));
+   return elec_terms(&h->c, true, false, vers, energy, grad);
+}
+
+extern "C" int t9gb_epolar(t9gb_context* h, int vers, double* energy, float* grad, double* virial)
+{
+   if (!h)
+      return T9GB_BAD_ARG;
+   T9_CHECK(check_vers(&h->c, vers, energy, grad, virial));
+   return elec_terms(&h->c, false, true, vers, energy, grad);
+}
+
+extern "C" int t9gb_emplar(t9gb_context* h, int vers, double* energy, float* grad, double* virial)
+{
+   if (!h)
+      return T9GB_BAD_ARG;
+   T9_CHECK(check_vers(&h->c, vers, energy, grad, virial));
+   return elec_terms(&h->c, true, true, vers, energy, grad);
 }

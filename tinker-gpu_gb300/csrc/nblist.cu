@@ -199,6 +199,7 @@ int order_build(Context* ctx)
    // legacy-stream copies above finish before the stream's kernels
    T9_CUDA(cudaDeviceSynchronize());
    T9_CHECK(fill_row_padding(ctx));
+   T9_CHECK(frame_map_build(ctx));
    ctx->have_order = true;
    ctx->list_stale = true;
    drop_graphs(ctx);

@@ -403,6 +403,269 @@ __global__ void __launch_bounds__(256) k_empole_recip_self(int n, GridParams G, 
 }
 
 // ---------------------------------------------------------------------------
+// Force gathers: the 20 fractional derivatives of the reciprocal potential
+// (level-4 weights; the reference's fphi order: 0, x, y, z, xx, yy, zz, xy,
+// xz, yz, xxx, yyy, zzz, xxy, xxz, xyy, yyz, xzz, yzz, xyz), made Cartesian
+// (orthogonal box: one factor nfft/L per derivative) and contracted on the
+// spot.  Replaces fphiMpole/fphiUind (src/cu/pme.cu:383-906) followed by the
+// force/torque parts of empoleEwaldRecipGeneric_cu (src/cu/hippo/empole.cu)
+// and epolarEwaldRecipSelf_cu1 (src/cu/epolarrecip.cu:414-511).
+
+__device__ __forceinline__ void row_sums20(const float2* __restrict__ g, const GridParams& G, int i1, size_t row,
+   const float (*t1)[4], bool imag, float* t)
+{
+   t[0] = t[1] = t[2] = t[3] = 0.f;
+#pragma unroll
+   for (int ix = 0; ix < 5; ++ix) {
+      int xb = i1 + ix;
+      xb -= (xb >= G.n1 ? G.n1 : 0);
+      const float2 qv = g[row + xb];
+      const float q = imag ? qv.y : qv.x;
+#pragma unroll
+      for (int l = 0; l < 4; ++l)
+         t[l] += q * t1[ix][l];
+   }
+}
+
+__device__ __forceinline__ void fphi20(const float* t, const float* u, const float* v, float* phi)
+{
+   phi[0] = t[0] * u[0] * v[0];
+   phi[1] = t[1] * u[0] * v[0];
+   phi[2] = t[0] * u[1] * v[0];
+   phi[3] = t[0] * u[0] * v[1];
+   phi[4] = t[2] * u[0] * v[0];
+   phi[5] = t[0] * u[2] * v[0];
+   phi[6] = t[0] * u[0] * v[2];
+   phi[7] = t[1] * u[1] * v[0];
+   phi[8] = t[1] * u[0] * v[1];
+   phi[9] = t[0] * u[1] * v[1];
+   phi[10] = t[3] * u[0] * v[0];
+   phi[11] = t[0] * u[3] * v[0];
+   phi[12] = t[0] * u[0] * v[3];
+   phi[13] = t[2] * u[1] * v[0];
+   phi[14] = t[2] * u[0] * v[1];
+   phi[15] = t[1] * u[2] * v[0];
+   phi[16] = t[0] * u[2] * v[1];
+   phi[17] = t[1] * u[0] * v[2];
+   phi[18] = t[0] * u[1] * v[2];
+   phi[19] = t[1] * u[1] * v[1];
+}
+
+// fractional -> Cartesian for the 20 derivatives
+__device__ __forceinline__ void to_cart20(const GridParams& G, float* c)
+{
+   const float a = G.a1, b = G.a2, d = G.a3;
+   c[1] *= a;
+   c[2] *= b;
+   c[3] *= d;
+   c[4] *= a * a;
+   c[5] *= b * b;
+   c[6] *= d * d;
+   c[7] *= a * b;
+   c[8] *= a * d;
+   c[9] *= b * d;
+   c[10] *= a * a * a;
+   c[11] *= b * b * b;
+   c[12] *= d * d * d;
+   c[13] *= a * a * b;
+   c[14] *= a * a * d;
+   c[15] *= a * b * b;
+   c[16] *= b * b * d;
+   c[17] *= a * d * d;
+   c[18] *= b * d * d;
+   c[19] *= a * b * d;
+}
+
+__device__ __forceinline__ int ix2(int a, int b)
+{
+   return a == b ? 4 + a : (a + b == 1 ? 7 : (a + b == 2 ? 8 : 9));
+}
+
+__device__ __forceinline__ int ix3(int a, int b, int c)
+{
+   int n[3] = {0, 0, 0};
+   n[a]++;
+   n[b]++;
+   n[c]++;
+   if (n[0] == 3)
+      return 10;
+   if (n[1] == 3)
+      return 11;
+   if (n[2] == 3)
+      return 12;
+   if (n[0] == 2)
+      return n[1] ? 13 : 14;
+   if (n[1] == 2)
+      return n[0] ? 15 : 16;
+   if (n[2] == 2)
+      return n[0] ? 17 : 18;
+   return 19;
+}
+
+// -(q phi_a + d_b phi_ab + Theta_bc phi_abc) for a multipole row m (12 floats)
+__device__ __forceinline__ void mpole_force(const float* m, const float* c, float* F)
+{
+   const float Q[3][3] = {{m[4], m[7], m[8]}, {m[7], m[5], m[9]}, {m[8], m[9], m[6]}};
+   for (int a = 0; a < 3; ++a) {
+      float v = m[0] * c[1 + a];
+      for (int b = 0; b < 3; ++b) {
+         v += m[1 + b] * c[ix2(a, b)];
+         for (int cc = 0; cc < 3; ++cc)
+            v += Q[b][cc] * c[ix3(a, b, cc)];
+      }
+      F[a] = -v;
+   }
+}
+
+// permanent grid: multipole forces, torque field and energies (MPOLE), the
+// polarization force on the dipoles in the permanent field gradient and the
+// Ewald self torque (POLAR)
+template <bool MPOLE, bool POLAR>
+__global__ void __launch_bounds__(256) k_gather_force_perm(int n, GridParams G, float f, float aewald,
+   const float4* __restrict__ spos, const float2* __restrict__ g, const float* __restrict__ rp,
+   const float* __restrict__ u8, float* __restrict__ fout, float* __restrict__ tout, double* __restrict__ e_atom,
+   double* __restrict__ e_self)
+{
+   const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+   const int lane = threadIdx.x & 31;
+   if (s >= n)
+      return;
+   int i1, i2, i3;
+   float w1, w2, w3;
+   site(G, spos[s], i1, i2, i3, w1, w2, w3);
+   float phi[20];
+#pragma unroll
+   for (int c = 0; c < 20; ++c)
+      phi[c] = 0.f;
+   if (lane < 25) {
+      float t1[5][4], t2[5][4], t3[5][4];
+      bspline5<4>(w1, t1);
+      bspline5<4>(w2, t2);
+      bspline5<4>(w3, t3);
+      const int jy = lane % 5, kz = lane / 5;
+      int zb = i3 + kz;
+      zb -= (zb >= G.n3 ? G.n3 : 0);
+      int yb = i2 + jy;
+      yb -= (yb >= G.n2 ? G.n2 : 0);
+      const size_t row = ((size_t)zb * G.n2 + yb) * G.n1;
+      float t[4];
+      row_sums20(g, G, i1, row, t1, false, t);
+      fphi20(t, t2[jy], t3[kz], phi);
+   }
+#pragma unroll
+   for (int c = 0; c < 20; ++c)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1)
+         phi[c] += __shfl_xor_sync(0xffffffffu, phi[c], o);
+   if (lane != 0)
+      return;
+   to_cart20(G, phi);
+   const float* m = rp + 12 * s;
+   float F[3] = {0.f, 0.f, 0.f}, T[10];
+#pragma unroll
+   for (int c = 0; c < 10; ++c)
+      T[c] = 0.f;
+   if (MPOLE) {
+      mpole_force(m, phi, F);
+      for (int c = 0; c < 3; ++c)
+         F[c] *= f;
+      for (int c = 0; c < 10; ++c)
+         T[c] = f * phi[c];
+      double e = (double)m[0] * phi[0] + (double)m[1] * phi[1] + (double)m[2] * phi[2] + (double)m[3] * phi[3];
+      e += (double)m[4] * phi[4] + (double)m[5] * phi[5] + (double)m[6] * phi[6];
+      e += 2.0 * ((double)m[7] * phi[7] + (double)m[8] * phi[8] + (double)m[9] * phi[9]);
+      if (e_atom)
+         e_atom[s] = 0.5 * f * e;
+      if (e_self) {
+         const double a2 = 2.0 * aewald * aewald;
+         const double fterm = -(double)f * aewald / 1.77245385090551602730;
+         const double cii = (double)m[0] * m[0];
+         const double dii = (double)m[1] * m[1] + (double)m[2] * m[2] + (double)m[3] * m[3];
+         const double qii = 2.0 * ((double)m[7] * m[7] + (double)m[8] * m[8] + (double)m[9] * m[9])
+            + (double)m[4] * m[4] + (double)m[5] * m[5] + (double)m[6] * m[6];
+         e_self[s] = fterm * (cii + a2 * (dii / 3.0 + 2.0 * a2 * qii * 0.2));
+      }
+   }
+   if (POLAR) {
+      const float* u = u8 + 8 * s;
+      const float us[3] = {u[0] + u[3], u[1] + u[4], u[2] + u[5]};
+      for (int a = 0; a < 3; ++a) {
+         float v = 0.f;
+         for (int b = 0; b < 3; ++b)
+            v += us[b] * phi[ix2(a, b)];
+         F[a] -= 0.5f * f * v;
+         T[1 + a] -= 0.5f * f * G.selfterm * us[a];
+      }
+   }
+   for (int c = 0; c < 3; ++c)
+      fout[3 * s + c] = F[c];
+   for (int c = 0; c < 10; ++c)
+      tout[10 * s + c] = T[c];
+}
+
+// induced-dipole grid (d real, p imaginary): force on the multipoles in the
+// dipoles' potential, the mutual dipole force and the torque field
+__global__ void __launch_bounds__(256) k_gather_force_uind(int n, GridParams G, float f,
+   const float4* __restrict__ spos, const float2* __restrict__ g, const float* __restrict__ rp,
+   const float* __restrict__ u8, float* __restrict__ fout, float* __restrict__ tout)
+{
+   const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+   const int lane = threadIdx.x & 31;
+   if (s >= n)
+      return;
+   int i1, i2, i3;
+   float w1, w2, w3;
+   site(G, spos[s], i1, i2, i3, w1, w2, w3);
+   float pd[20], pp[20];
+#pragma unroll
+   for (int c = 0; c < 20; ++c)
+      pd[c] = pp[c] = 0.f;
+   if (lane < 25) {
+      float t1[5][4], t2[5][4], t3[5][4];
+      bspline5<4>(w1, t1);
+      bspline5<4>(w2, t2);
+      bspline5<4>(w3, t3);
+      const int jy = lane % 5, kz = lane / 5;
+      int zb = i3 + kz;
+      zb -= (zb >= G.n3 ? G.n3 : 0);
+      int yb = i2 + jy;
+      yb -= (yb >= G.n2 ? G.n2 : 0);
+      const size_t row = ((size_t)zb * G.n2 + yb) * G.n1;
+      float t[4];
+      row_sums20(g, G, i1, row, t1, false, t);
+      fphi20(t, t2[jy], t3[kz], pd);
+      row_sums20(g, G, i1, row, t1, true, t);
+      fphi20(t, t2[jy], t3[kz], pp);
+   }
+#pragma unroll
+   for (int c = 0; c < 20; ++c)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+         pd[c] += __shfl_xor_sync(0xffffffffu, pd[c], o);
+         pp[c] += __shfl_xor_sync(0xffffffffu, pp[c], o);
+      }
+   if (lane != 0)
+      return;
+   to_cart20(G, pd);
+   to_cart20(G, pp);
+   float ps[20];
+   for (int c = 0; c < 20; ++c)
+      ps[c] = pd[c] + pp[c];
+   const float* m = rp + 12 * s;
+   const float* u = u8 + 8 * s;
+   float F[3];
+   mpole_force(m, ps, F);
+   for (int a = 0; a < 3; ++a) {
+      float v = 0.f;
+      for (int b = 0; b < 3; ++b)
+         v += u[b] * pp[ix2(a, b)] + u[3 + b] * pd[ix2(a, b)];
+      fout[3 * s + a] = 0.5f * f * (F[a] - v);
+   }
+   for (int c = 0; c < 10; ++c)
+      tout[10 * s + c] = 0.5f * f * ps[c];
+}
+
+// ---------------------------------------------------------------------------
 
 int pme_setup(Context* ctx)
 {
@@ -557,6 +820,42 @@ int launch_empole_recip(Context* ctx, double* e_atom)
       (float)ctx->cfg.electric, (float)ctx->cfg.aewald, ctx->spos, ctx->pme.qgrid, ctx->srpole, e_atom,
       e_atom + ctx->npad);
    T9_CUDA(cudaGetLastError());
+   return T9GB_OK;
+}
+}  // namespace t9gb
+
+namespace t9gb {
+// reciprocal forces for elec_forces (force.cu)
+int launch_force_recip(Context* ctx, bool mpole, bool polar)
+{
+   GridParams G = grid_params(ctx);
+   const int nb = grid_for((long long)ctx->n * 32, 256);
+   const float f = (float)ctx->cfg.electric, a = (float)ctx->cfg.aewald;
+   k_spread<0><<<nb, 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->srpole,
+      reinterpret_cast<unsigned long long*>(ctx->pme.qfx));
+   T9_CUDA(cudaGetLastError());
+   T9_CHECK(fft_conv(ctx));
+   double* er = ctx->e_atom + ctx->npad;
+   double* es = ctx->e_atom + 2 * ctx->npad;
+   if (mpole && polar)
+      k_gather_force_perm<true, true><<<nb, 256, 0, ctx->stream>>>(ctx->n, G, f, a, ctx->spos, ctx->pme.qgrid,
+         ctx->srpole, ctx->uind, ctx->frecp, ctx->trecp, er, es);
+   else if (mpole)
+      k_gather_force_perm<true, false><<<nb, 256, 0, ctx->stream>>>(ctx->n, G, f, a, ctx->spos, ctx->pme.qgrid,
+         ctx->srpole, ctx->uind, ctx->frecp, ctx->trecp, er, es);
+   else
+      k_gather_force_perm<false, true><<<nb, 256, 0, ctx->stream>>>(ctx->n, G, f, a, ctx->spos, ctx->pme.qgrid,
+         ctx->srpole, ctx->uind, ctx->frecp, ctx->trecp, nullptr, nullptr);
+   T9_CUDA(cudaGetLastError());
+   if (polar) {
+      k_spread<1><<<nb, 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->uind,
+         reinterpret_cast<unsigned long long*>(ctx->pme.qfx));
+      T9_CUDA(cudaGetLastError());
+      T9_CHECK(fft_conv(ctx));
+      k_gather_force_uind<<<nb, 256, 0, ctx->stream>>>(ctx->n, G, f, ctx->spos, ctx->pme.qgrid, ctx->srpole,
+         ctx->uind, ctx->frecu, ctx->trecu);
+      T9_CUDA(cudaGetLastError());
+   }
    return T9GB_OK;
 }
 }  // namespace t9gb
