@@ -148,15 +148,17 @@ int t9gb_epolar_energy(t9gb_context* ctx, double* energy);
  * bits (include/tool/rcman.h:105-155). */
 #define T9GB_CALC_ENERGY 0x010
 #define T9GB_CALC_GRAD 0x020
-#define T9GB_CALC_VIRIAL 0x040 /* not available yet: returns T9GB_BAD_ARG */
+#define T9GB_CALC_VIRIAL 0x040
 
 /* Permanent-multipole energy (kcal/mol) and gradient (kcal/mol/A, device
  * float [n][3], caller order, written -- not accumulated) of the current
  * coordinates and rotated multipoles (call t9gb_mpole_init first), including
  * the forces on the frame atoms from the multipole torques.  Replaces
  * empole(int vers) (src/amoeba/empole.cpp:81-138) with its torque step
- * (src/cu/amoeba/torque.cu:8-383).  vers: T9GB_CALC_ENERGY and/or
- * T9GB_CALC_GRAD. */
+ * (src/cu/amoeba/torque.cu:8-383).  vers: any of T9GB_CALC_ENERGY,
+ * T9GB_CALC_GRAD, T9GB_CALC_VIRIAL; virial[9] (row-major, kcal/mol) is the
+ * strain derivative dE/d(eps)_ab of the energy, symmetrised, the reference's
+ * vir_em + vir_trq convention. */
 int t9gb_empole(t9gb_context* ctx, int vers, double* energy, float* grad_device, double* virial);
 
 /* Polarization: solves induce() on the current coordinates, then the energy

@@ -282,6 +282,40 @@ def epolar_gradient_fd(system, uind, uinp, xyz=None, atoms=None, h=1e-5, **kw):
     return _fd(lambda x: epolar_g(system, x, ud, up, **kw), xyz, list(atoms), h)
 
 
+def _strain_fd(system, fun, diag_only, h):
+    """dF/d(eps)_ab for x -> (I + eps) x (box edges scaled with the diagonal)."""
+    import dataclasses
+
+    S = np.zeros((3, 3))
+    for a in range(3):
+        for b in range(3):
+            if diag_only and a != b:
+                S[a, b] = np.nan
+                continue
+            vals = []
+            for sg in (1, -1):
+                eps = np.zeros((3, 3))
+                eps[a, b] = sg * h
+                x = np.asarray(system.xyz, dtype=np.float64) @ (np.eye(3) + eps).T
+                box = None if system.box is None else np.asarray(system.box, dtype=np.float64) * (1 + np.diag(eps))
+                vals.append(fun(dataclasses.replace(system, xyz=x, box=box)))
+            S[a, b] = (vals[0] - vals[1]) / (2 * h)
+    return S
+
+
+def empole_virial_fd(system, diag_only=False, h=1e-6, **kw):
+    """Virial dE_mpole/d(eps) [3][3] (orthorhombic PBC: diagonal only, the
+    off-diagonal entries are NaN)."""
+    return _strain_fd(system, lambda s2: OracleSystem(s2, **kw).empole_energy()[0], diag_only, h)
+
+
+def epolar_virial_fd(system, uind, uinp, diag_only=False, h=1e-6, **kw):
+    """Polarization virial at fixed dipoles, dG/d(eps) [3][3]."""
+    ud = np.asarray(uind, dtype=np.float64)
+    up = np.asarray(uinp, dtype=np.float64)
+    return _strain_fd(system, lambda s2: epolar_g(s2, s2.xyz, ud, up, **kw), diag_only, h)
+
+
 def bsmod(nfft, order=5):
     out = np.zeros(nfft)
     lib().or_bsmod(nfft, order, _dp(out))

@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 import lf_fixture as L
-from gpu_util import cpu, engine_for
+from gpu_util import cpu, engine_for, water_cluster
 
 pytestmark = pytest.mark.gpu
 
@@ -107,3 +107,41 @@ def test_gas_phase_net_force_vanishes(gpu_lib):
     e = engine_for(s)
     g = cpu(e.emplar()[1])
     assert np.abs(g.sum(axis=0)).max() < 1e-3
+
+
+CALC_ALL = 0x070  # energy | gradient | virial
+VIR_ABS = 2e-3   # kcal/mol
+VIR_REL = 2e-5
+
+
+def _vir_close(w, ref):
+    m = ~np.isnan(ref)
+    err = np.abs(w - ref)[m].max()
+    print("virial\n", w, "\noracle\n", ref, "\nmax err", err)
+    return err < VIR_ABS + VIR_REL * np.abs(ref[m]).max()
+
+
+def test_virial_gas_cluster_vs_oracle(gpu_lib, oracle, tg):
+    """Full 3 x 3 virial without PBC (real space and frame terms)."""
+    s = water_cluster(tg)
+    e = engine_for(s)
+    _, _, w1 = e.empole(CALC_ALL)
+    assert _vir_close(w1, oracle.empole_virial_fd(s))
+    _, _, w2 = e.epolar(CALC_ALL)
+    ud, up, *_ = oracle.OracleSystem(s).induce()
+    assert _vir_close(w2, oracle.epolar_virial_fd(s, ud, up))
+
+
+def test_virial_pme_diagonal_vs_oracle(gpu_lib, oracle, tg):
+    """PME water box: the diagonal components (box and coordinates scaled
+    along one axis) include the k-space and fractional-transform terms."""
+    s = tg.systems.make_config("water648")
+    e = engine_for(s)
+    _, _, w1 = e.empole(CALC_ALL)
+    assert _vir_close(w1, oracle.empole_virial_fd(s, diag_only=True, cutoff=9.0))
+    _, _, w2 = e.epolar(CALC_ALL)
+    ud, up, *_ = oracle.OracleSystem(s).induce()
+    assert _vir_close(w2, oracle.epolar_virial_fd(s, ud, up, diag_only=True, cutoff=9.0))
+    # symmetric by construction; emplar = empole + epolar
+    _, _, w3 = e.emplar(CALC_ALL)
+    assert np.abs(w3 - w1 - w2).max() < 1e-3

@@ -126,3 +126,14 @@ def test_epolar_gradient_golden(oracle, ewald):
     g = oracle.epolar_gradient_fd(s, ud, up, atoms=range(GRAD_ATOMS))
     ref = np.array(L.expected(fx, ewald)["epolar"]["ref_grad"])[:GRAD_ATOMS]
     assert np.abs(g - ref).max() < 5e-4
+
+
+def test_virial_fd_gas_symmetric(oracle, tg):
+    """Without PBC the strain derivative of the energy is symmetric
+    (rotational invariance): a check of the finite-difference virial that the
+    GPU virial tests compare against."""
+    from gpu_util import water_cluster
+
+    s = water_cluster(tg, nmol=12)
+    w = oracle.empole_virial_fd(s)
+    assert np.abs(w - w.T).max() < 1e-5 * max(1.0, np.abs(w).max())

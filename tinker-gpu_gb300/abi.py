@@ -381,8 +381,12 @@ class Engine:
     def _eg(self, fn, vers):
         e = C.c_double()
         g = self._empty3() if vers & CALC_GRAD else None
-        rc = fn(self.h, int(vers), C.byref(e), C.c_void_p(g.data_ptr()) if g is not None else None, None)
+        v = np.zeros(9)
+        rc = fn(self.h, int(vers), C.byref(e), C.c_void_p(g.data_ptr()) if g is not None else None,
+                _dp(v) if vers & CALC_VIRIAL else None)
         self._check(rc, allow=(T9GB_NOT_CONVERGED,))
+        if vers & CALC_VIRIAL:
+            return e.value, g, v.reshape(3, 3)
         return e.value, g
 
     def energy_components(self):

@@ -46,6 +46,7 @@ struct PmeGrid {
    float2* qgrid = nullptr;   // complex grid [n3][n2][n1]
    long long* qfx = nullptr;  // fixed-point accumulation grid [n3][n2][n1][2]
    float* infl = nullptr;     // influence function [n3][n2][n1]
+   float2* qstash = nullptr;  // transformed permanent grid kept for the virial cross terms
 };
 
 // Per-kernel event timing (tracing): categories of timed launches.
@@ -201,6 +202,8 @@ struct Context {
    float *freal = nullptr, *frecp = nullptr, *frecu = nullptr;
    float *treal = nullptr, *trecp = nullptr, *trecu = nullptr;
    float* fbuf = nullptr;
+   float* wvir = nullptr;  // [27][npad] virial rows: real, frame, reciprocal
+   double* vsum = nullptr; // their sums
    int *rev_start = nullptr, *rev_ent = nullptr;
    std::vector<int> h_frames;  // [n][4] caller order
    // start policy (host): compare the plain and the learned start every
@@ -318,8 +321,8 @@ int launch_learn_features(Context* ctx, const float* e8, const float* u8, float*
 int force_setup(Context* ctx);
 void force_free(Context* ctx);
 int frame_map_build(Context* ctx);
-int elec_forces(Context* ctx, bool mpole, bool polar, float* grad);
-int launch_force_recip(Context* ctx, bool mpole, bool polar);
+int elec_forces(Context* ctx, bool mpole, bool polar, float* grad, bool vir);
+int launch_force_recip(Context* ctx, bool mpole, bool polar, float* wrec);
 int induce_sorted(Context* ctx);
 int learn_setup(Context* ctx);
 void learn_free(Context* ctx);

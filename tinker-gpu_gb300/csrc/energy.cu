@@ -31,6 +31,25 @@ __global__ void k_sum_rows(int n, int stride, const double* __restrict__ a, doub
       out[blockIdx.x] = sh[0];
 }
 
+// block b sums the float row a[b][0..n) in a fixed order (double) into out[b]
+__global__ void k_sum_rows_f(int n, int stride, const float* __restrict__ a, double* __restrict__ out)
+{
+   __shared__ double sh[1024];
+   const float* row = a + (size_t)blockIdx.x * stride;
+   double v = 0;
+   for (int i = threadIdx.x; i < n; i += blockDim.x)
+      v += row[i];
+   sh[threadIdx.x] = v;
+   __syncthreads();
+   for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+      if (threadIdx.x < o)
+         sh[threadIdx.x] += sh[threadIdx.x + o];
+      __syncthreads();
+   }
+   if (threadIdx.x == 0)
+      out[blockIdx.x] = sh[0];
+}
+
 // e[s] = -1/2 f alpha_s^-1 (u_d . udir_p)
 __global__ void k_epolar_dot(int npad, double f, const float* __restrict__ uind, const float* __restrict__ udir,
    const float* __restrict__ polinv, double* __restrict__ e)
@@ -113,12 +132,9 @@ static int check_vers(Context* ctx, int vers, double* energy, float* grad, doubl
       return T9GB_BAD_ARG;
    if ((vers & T9GB_CALC_GRAD) && !grad)
       return T9GB_BAD_ARG;
-   if (vers & T9GB_CALC_VIRIAL) {
-      (void)virial;
-      ctx->last_error = "virial is not available";
+   if ((vers & T9GB_CALC_VIRIAL) && !virial)
       return T9GB_BAD_ARG;
-   }
-   if (!(vers & (T9GB_CALC_ENERGY | T9GB_CALC_GRAD)))
+   if (!(vers & (T9GB_CALC_ENERGY | T9GB_CALC_GRAD | T9GB_CALC_VIRIAL)))
       return T9GB_BAD_ARG;
    if (!ctx->have_order)
       return T9GB_NOT_READY;
@@ -126,7 +142,37 @@ static int check_vers(Context* ctx, int vers, double* energy, float* grad, doubl
 }
 
 // mpole / polar terms on the current coordinates and rotated multipoles
-static int elec_terms(Context* ctx, bool mpole, bool polar, int vers, double* energy, float* grad)
+// virial: sum of the per-slot rows (real, frame, reciprocal transform) and
+// the k-space sums, symmetrised; row-major 3 x 3
+static int sum_virial(Context* ctx, double* virial)
+{
+   k_sum_rows_f<<<27, 1024, 0, ctx->stream>>>(ctx->npad, ctx->npad, ctx->wvir, ctx->vsum);
+   T9_CUDA(cudaGetLastError());
+   double v[27], k[12];
+   T9_CUDA(cudaMemcpyAsync(v, ctx->vsum, sizeof(double) * 27, cudaMemcpyDeviceToHost, ctx->stream));
+   T9_CUDA(cudaMemcpyAsync(k, ctx->scal + 40, sizeof(double) * 12, cudaMemcpyDeviceToHost, ctx->stream));
+   T9_CUDA(cudaStreamSynchronize(ctx->stream));
+   if (!ctx->cfg.use_ewald)
+      for (double& x : k)
+         x = 0;
+   const int ab[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
+   double W[3][3];
+   for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b)
+         W[a][b] = v[3 * a + b] + v[9 + 3 * a + b] + v[18 + 3 * a + b];
+   for (int c = 0; c < 6; ++c) {
+      const double kv = k[c] + k[6 + c];
+      W[ab[c][0]][ab[c][1]] += c < 3 ? kv : 0.5 * kv;
+      if (c >= 3)
+         W[ab[c][1]][ab[c][0]] += 0.5 * kv;
+   }
+   for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b)
+         virial[3 * a + b] = 0.5 * (W[a][b] + W[b][a]);
+   return T9GB_OK;
+}
+
+static int elec_terms(Context* ctx, bool mpole, bool polar, int vers, double* energy, float* grad, double* virial)
 {
    double e = 0;
    if (polar) {
@@ -137,8 +183,9 @@ static int elec_terms(Context* ctx, bool mpole, bool polar, int vers, double* en
    for (int attempt = 0; attempt < 2; ++attempt) {
       T9_CHECK(ensure_list(ctx));
       T9_CUDA(cudaMemsetAsync(ctx->e_atom, 0, sizeof(double) * 3 * ctx->npad, ctx->stream));
-      if (vers & T9GB_CALC_GRAD) {
-         T9_CHECK(elec_forces(ctx, mpole, polar, grad));
+      if (vers & (T9GB_CALC_GRAD | T9GB_CALC_VIRIAL)) {
+         T9_CHECK(elec_forces(ctx, mpole, polar, (vers & T9GB_CALC_GRAD) ? grad : nullptr,
+            (vers & T9GB_CALC_VIRIAL) != 0));
       } else if (mpole) {
          T9_CHECK(launch_empole_real(ctx, ctx->e_atom));
          T9_CHECK(launch_empole_recip(ctx, ctx->e_atom + ctx->npad));
@@ -164,6 +211,8 @@ static int elec_terms(Context* ctx, bool mpole, bool polar, int vers, double* en
       }
       *energy = e;
    }
+   if (vers & T9GB_CALC_VIRIAL)
+      T9_CHECK(sum_virial(ctx, virial));
    return T9GB_OK;
 }
 
@@ -183,7 +232,7 @@ extern "C" int t9gb_empole(t9gb_context* h, int vers, double* energy, float* gra
    if (!h)
       return T9GB_BAD_ARG;
    T9_CHECK(check_vers(&h->c, vers, energy, grad, virial));
-   return elec_terms(&h->c, true, false, vers, energy, grad);
+   return elec_terms(&h->c, true, false, vers, energy, grad, virial);
 }
 
 extern "C" int t9gb_epolar(t9gb_context* h, int vers, double* energy, float* grad, double* virial)
@@ -191,7 +240,7 @@ extern "C" int t9gb_epolar(t9gb_context* h, int vers, double* energy, float* gra
    if (!h)
       return T9GB_BAD_ARG;
    T9_CHECK(check_vers(&h->c, vers, energy, grad, virial));
-   return elec_terms(&h->c, false, true, vers, energy, grad);
+   return elec_terms(&h->c, false, true, vers, energy, grad, virial);
 }
 
 extern "C" int t9gb_emplar(t9gb_context* h, int vers, double* energy, float* grad, double* virial)
@@ -199,5 +248,5 @@ extern "C" int t9gb_emplar(t9gb_context* h, int vers, double* energy, float* gra
    if (!h)
       return T9GB_BAD_ARG;
    T9_CHECK(check_vers(&h->c, vers, energy, grad, virial));
-   return elec_terms(&h->c, true, true, vers, energy, grad);
+   return elec_terms(&h->c, true, true, vers, energy, grad, virial);
 }

@@ -209,10 +209,11 @@ struct PairOut {
    double e;      // empole pair energy (i side, halved later)
    double f[3];   // force on i
    double t[10];  // torque field at i
+   double w[9];   // virial dE/d(strain)_ab, i side of the pair (halved)
 };
 
 // one pair seen from i: R = x_i - x_k, scales sc = (m, d, p, u)
-template <bool MPOLE, bool POLAR>
+template <bool MPOLE, bool POLAR, bool VIR>
 __device__ __forceinline__ void elec_pair(const PairParams& P, float3 Rv, float r2, float4 sc, const Mp& mi,
    const float* ui, float pdi, float pti, const Mp& mk, const float* uk, float pdk, float ptk, PairOut& o)
 {
@@ -237,6 +238,14 @@ __device__ __forceinline__ void elec_pair(const PairParams& P, float3 Rv, float 
       o.f[0] -= e.x;
       o.f[1] -= e.y;
       o.f[2] -= e.z;
+      if (VIR) {
+         const float ge[3] = {e.x, e.y, e.z}, rv[3] = {Rv.x, Rv.y, Rv.z};
+#pragma unroll
+         for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b)
+               o.w[3 * a + b] += 0.5f * ge[a] * rv[b];
+      }
       o.t[0] += pk.p0.v;
 #pragma unroll
       for (int a = 0; a < 3; ++a)
@@ -297,6 +306,14 @@ __device__ __forceinline__ void elec_pair(const PairParams& P, float3 Rv, float 
       o.f[0] -= 0.5f * g.x;
       o.f[1] -= 0.5f * g.y;
       o.f[2] -= 0.5f * g.z;
+      if (VIR) {
+         const float gg[3] = {g.x, g.y, g.z}, rv[3] = {Rv.x, Rv.y, Rv.z};
+#pragma unroll
+         for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b)
+               o.w[3 * a + b] += 0.25f * gg[a] * rv[b];
+      }
       o.t[0] += 0.5f * (pa.p0.v + pb.p0.v);
 #pragma unroll
       for (int c = 0; c < 3; ++c)
@@ -321,11 +338,12 @@ __device__ __forceinline__ void group_reduce_d(double* v)
 // Real-space forces and torque fields, G lanes per atom i over the list and
 // the scaled partners.  f: electric; outputs per slot: force [npad][3],
 // torque field [npad][10], empole real energy (MPOLE).
-template <int G, bool MPOLE, bool POLAR>
+template <int G, bool MPOLE, bool POLAR, bool VIR>
 __global__ void __launch_bounds__(128) k_elec_real(PairParams P, int npad, float f, const int* __restrict__ nbr,
    const int* __restrict__ nnbr, const int* __restrict__ sp_start, const int* __restrict__ sp_j,
    const float4* __restrict__ sp_sc, const float4* __restrict__ spos, const float* __restrict__ rp,
-   const float* __restrict__ u8, float* __restrict__ fout, float* __restrict__ tout, double* __restrict__ e_atom)
+   const float* __restrict__ u8, float* __restrict__ fout, float* __restrict__ tout, double* __restrict__ e_atom,
+   float* __restrict__ wout)
 {
    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
    const int i = tid / G, g = tid % G;
@@ -337,6 +355,9 @@ __global__ void __launch_bounds__(128) k_elec_real(PairParams P, int npad, float
 #pragma unroll
    for (int c = 0; c < 10; ++c)
       o.t[c] = 0;
+#pragma unroll
+   for (int c = 0; c < 9; ++c)
+      o.w[c] = 0;
    if (i < P.n) {
       const float4 pi = spos[i];
       Mp mi;
@@ -358,7 +379,7 @@ __global__ void __launch_bounds__(128) k_elec_real(PairParams P, int npad, float
             float uk[8] = {0, 0, 0, 0, 0, 0, 0, 0};
             if (POLAR)
                load8(u8, j, uk);
-            elec_pair<MPOLE, POLAR>(P, make_float3(-d.x, -d.y, -d.z), r2, make_float4(1.f, 1.f, 1.f, 1.f), mi, ui,
+            elec_pair<MPOLE, POLAR, VIR>(P, make_float3(-d.x, -d.y, -d.z), r2, make_float4(1.f, 1.f, 1.f, 1.f), mi, ui,
                pi.w, pti, mk, uk, pk.w, rp[12 * j + 10], o);
          }
       }
@@ -374,7 +395,7 @@ __global__ void __launch_bounds__(128) k_elec_real(PairParams P, int npad, float
             float uk[8] = {0, 0, 0, 0, 0, 0, 0, 0};
             if (POLAR)
                load8(u8, j, uk);
-            elec_pair<MPOLE, POLAR>(P, make_float3(-d.x, -d.y, -d.z), r2, sp_sc[q], mi, ui, pi.w, pti, mk, uk, pk.w,
+            elec_pair<MPOLE, POLAR, VIR>(P, make_float3(-d.x, -d.y, -d.z), r2, sp_sc[q], mi, ui, pi.w, pti, mk, uk, pk.w,
                rp[12 * j + 10], o);
          }
       }
@@ -388,7 +409,13 @@ __global__ void __launch_bounds__(128) k_elec_real(PairParams P, int npad, float
    for (int c = 0; c < 10; ++c)
       acc[4 + c] = o.t[c];
    group_reduce_d<G, 14>(acc);
+   if (VIR)
+      group_reduce_d<G, 9>(o.w);
    if (g == 0) {
+      if (VIR)
+#pragma unroll
+         for (int c = 0; c < 9; ++c)
+            wout[c * npad + i] = (float)(f * o.w[c]);
       if (MPOLE && e_atom)
          e_atom[i] = 0.5 * f * acc[0];
 #pragma unroll
@@ -479,14 +506,18 @@ __device__ void frame_rot(const float* xi, const float* xz, const float* xx, con
 }
 
 // fbuf[s][3 role + c] = -dE/dx(role atom, c) through the rotation of slot s
+// wout (may be null): the frame part of the virial, -sum_role F_role (x_role - x_i)
 __global__ void k_frame_force(int npad, const int* __restrict__ perm, const int4* __restrict__ frames,
    const float* __restrict__ pole, const float* __restrict__ xyz, const float* __restrict__ t0,
-   const float* __restrict__ t1, const float* __restrict__ t2, float* __restrict__ fbuf)
+   const float* __restrict__ t1, const float* __restrict__ t2, float* __restrict__ fbuf, float* __restrict__ wout)
 {
    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < npad; s += gridDim.x * blockDim.x) {
       float* out = fbuf + 12 * s;
       for (int m = 0; m < 12; ++m)
          out[m] = 0.f;
+      if (wout)
+         for (int c = 0; c < 9; ++c)
+            wout[c * npad + s] = 0.f;
       const int i = perm[s];
       if (i < 0)
          continue;
@@ -531,6 +562,16 @@ __global__ void k_frame_force(int npad, const int* __restrict__ perm, const int4
                }
             out[3 * role + c] = -dE;
          }
+      if (wout) {
+         const float* pos[4] = {xi, xz, xx, xy};
+         for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) {
+               float w = 0.f;
+               for (int role = 1; role < nrole; ++role)
+                  w -= out[3 * role + a] * (pos[role][b] - xi[b]);
+               wout[(3 * a + b) * npad + s] = w;
+            }
+      }
    }
 }
 
@@ -569,18 +610,22 @@ int force_setup(Context* ctx)
    T9_CUDA(cudaMalloc(&ctx->trecp, sizeof(float) * 10 * np));
    T9_CUDA(cudaMalloc(&ctx->trecu, sizeof(float) * 10 * np));
    T9_CUDA(cudaMalloc(&ctx->fbuf, sizeof(float) * 12 * np));
+   T9_CUDA(cudaMalloc(&ctx->wvir, sizeof(float) * 27 * np));
+   T9_CUDA(cudaMalloc(&ctx->vsum, sizeof(double) * 32));
    return T9GB_OK;
 }
 
 void force_free(Context* ctx)
 {
    void* p[] = {ctx->freal, ctx->frecp, ctx->frecu, ctx->treal, ctx->trecp, ctx->trecu, ctx->fbuf, ctx->rev_start,
-      ctx->rev_ent};
+      ctx->rev_ent, ctx->wvir, ctx->vsum};
    for (void* q : p)
       if (q)
          cudaFree(q);
    ctx->freal = ctx->frecp = ctx->frecu = ctx->treal = ctx->trecp = ctx->trecu = ctx->fbuf = nullptr;
    ctx->rev_start = ctx->rev_ent = nullptr;
+   ctx->wvir = nullptr;
+   ctx->vsum = nullptr;
 }
 
 // reverse frame map: for slot j, the (slot i, role) pairs whose frame uses j
@@ -623,7 +668,17 @@ int frame_map_build(Context* ctx)
 // Forces of the permanent multipoles (mpole) and/or of the polarization at
 // the last induce's dipoles (polar).  grad: caller order [n][3] device.
 // e_atom receives the multipole energy terms (real, recip, self) when mpole.
-int elec_forces(Context* ctx, bool mpole, bool polar, float* grad)
+// vir: per-slot virial rows wvir [27][npad] (real, frame, reciprocal) and the
+// k-space sums in scal[40..51].
+template <bool MPOLE, bool POLAR, bool VIR>
+static void launch_real(Context* ctx, const PairParams& P, float f, int grid)
+{
+   k_elec_real<GROUP, MPOLE, POLAR, VIR><<<grid, 128, 0, ctx->stream>>>(P, ctx->npad, f, ctx->nbr, ctx->nnbr,
+      ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos, ctx->srpole, ctx->uind, ctx->freal, ctx->treal,
+      MPOLE ? ctx->e_atom : nullptr, ctx->wvir);
+}
+
+int elec_forces(Context* ctx, bool mpole, bool polar, float* grad, bool vir)
 {
    T9_CHECK(force_setup(ctx));
    if (!ctx->rev_start)
@@ -631,23 +686,34 @@ int elec_forces(Context* ctx, bool mpole, bool polar, float* grad)
    const PairParams P = make_params(ctx, ctx->cfg.cutoff);
    const float f = (float)ctx->cfg.electric;
    const int grid = grid_for((long long)ctx->npad * GROUP, 128);
-   if (mpole && polar)
-      k_elec_real<GROUP, true, true><<<grid, 128, 0, ctx->stream>>>(P, ctx->npad, f, ctx->nbr, ctx->nnbr, ctx->sp_start,
-         ctx->sp_j, ctx->sp_sc, ctx->spos, ctx->srpole, ctx->uind, ctx->freal, ctx->treal, ctx->e_atom);
-   else if (mpole)
-      k_elec_real<GROUP, true, false><<<grid, 128, 0, ctx->stream>>>(P, ctx->npad, f, ctx->nbr, ctx->nnbr,
-         ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos, ctx->srpole, ctx->uind, ctx->freal, ctx->treal, ctx->e_atom);
-   else
-      k_elec_real<GROUP, false, true><<<grid, 128, 0, ctx->stream>>>(P, ctx->npad, f, ctx->nbr, ctx->nnbr,
-         ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos, ctx->srpole, ctx->uind, ctx->freal, ctx->treal, nullptr);
+   if (vir) {
+      if (mpole && polar)
+         launch_real<true, true, true>(ctx, P, f, grid);
+      else if (mpole)
+         launch_real<true, false, true>(ctx, P, f, grid);
+      else
+         launch_real<false, true, true>(ctx, P, f, grid);
+   } else {
+      if (mpole && polar)
+         launch_real<true, true, false>(ctx, P, f, grid);
+      else if (mpole)
+         launch_real<true, false, false>(ctx, P, f, grid);
+      else
+         launch_real<false, true, false>(ctx, P, f, grid);
+   }
    T9_CUDA(cudaGetLastError());
    const bool ew = ctx->cfg.use_ewald != 0;
+   const size_t np = ctx->npad;
    if (ew)
-      T9_CHECK(launch_force_recip(ctx, mpole, polar));
+      T9_CHECK(launch_force_recip(ctx, mpole, polar, vir ? ctx->wvir + 18 * np : nullptr));
+   else if (vir)
+      T9_CUDA(cudaMemsetAsync(ctx->wvir + 18 * np, 0, sizeof(float) * 9 * np, ctx->stream));
    k_frame_force<<<grid_for(ctx->npad, 128), 128, 0, ctx->stream>>>(ctx->npad, ctx->perm, ctx->frames, ctx->pole,
-      ctx->xyz, ctx->treal, ew ? ctx->trecp : nullptr, ew && polar ? ctx->trecu : nullptr, ctx->fbuf);
-   k_force_combine<<<grid_for(ctx->n, 128), 128, 0, ctx->stream>>>(ctx->n, ctx->iperm, ctx->freal,
-      ew ? ctx->frecp : nullptr, ew && polar ? ctx->frecu : nullptr, ctx->rev_start, ctx->rev_ent, ctx->fbuf, grad);
+      ctx->xyz, ctx->treal, ew ? ctx->trecp : nullptr, ew && polar ? ctx->trecu : nullptr, ctx->fbuf,
+      vir ? ctx->wvir + 9 * np : nullptr);
+   if (grad)
+      k_force_combine<<<grid_for(ctx->n, 128), 128, 0, ctx->stream>>>(ctx->n, ctx->iperm, ctx->freal,
+         ew ? ctx->frecp : nullptr, ew && polar ? ctx->frecu : nullptr, ctx->rev_start, ctx->rev_ent, ctx->fbuf, grad);
    T9_CUDA(cudaGetLastError());
    return T9GB_OK;
 }

@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "reduce.cuh"
 
 namespace t9gb {
 
@@ -403,6 +404,78 @@ __global__ void __launch_bounds__(256) k_empole_recip_self(int n, GridParams G, 
 }
 
 // ---------------------------------------------------------------------------
+// k-space part of the reciprocal virial (the strain derivative of the
+// influence function), read-only on the forward-transformed grid:
+//   W_ab += sum_m w(m) G(m) [-delta_ab + 2 h_a h_b (1 + pi^2 h^2 / a^2) / h^2]
+// MODE 1 (permanent grid): w = wE |F(m)|^2, and the grid is kept in qstash
+// when stash != null.  MODE 2 (d real, p imaginary): with
+// Q_d = (F(m) + F*(-m)) / 2, Q_p = (F(m) - F*(-m)) / 2i and the kept
+// permanent Q_M, w = wP Re[Q_M (Q_d + Q_p)* + Q_d Q_p*].  The reference's
+// counterpart is pmeConv_cu1<Do_V> (src/cu/pme.cu:908-1031).  Six sums in a
+// fixed order; the last block writes them to out[0..6) (xx yy zz xy xz yz).
+template <int MODE>
+__global__ void k_conv_virial(int n1, int n2, int n3, float L1, float L2, float L3, float pterm,
+   const float* __restrict__ infl, const float2* __restrict__ g, float2* __restrict__ stash, float wE, float wP,
+   double* __restrict__ red, double* __restrict__ out, int* __restrict__ state)
+{
+   __shared__ double sh[40];
+   double v[6] = {0, 0, 0, 0, 0, 0};
+   const size_t ng = (size_t)n1 * n2 * n3;
+   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < ng; i += (size_t)gridDim.x * blockDim.x) {
+      const int k1 = (int)(i % n1), k2 = (int)((i / n1) % n2), k3 = (int)(i / ((size_t)n1 * n2));
+      const float2 F = g[i];
+      float2 QM = make_float2(0.f, 0.f);
+      if (MODE == 1 && stash)
+         stash[i] = F;
+      if (MODE == 2)
+         QM = stash[i];
+      if (i == 0)
+         continue;
+      const int r1 = (k1 < (n1 + 1) / 2) ? k1 : k1 - n1;
+      const int r2 = (k2 < (n2 + 1) / 2) ? k2 : k2 - n2;
+      const int r3 = (k3 < (n3 + 1) / 2) ? k3 : k3 - n3;
+      const float h[3] = {r1 / L1, r2 / L2, r3 / L3};
+      const float hsq = h[0] * h[0] + h[1] * h[1] + h[2] * h[2];
+      double w;
+      if (MODE == 1) {
+         w = (double)wE * ((double)F.x * F.x + (double)F.y * F.y);
+      } else {
+         const int m1 = k1 == 0 ? 0 : n1 - k1, m2 = k2 == 0 ? 0 : n2 - k2, m3 = k3 == 0 ? 0 : n3 - k3;
+         const float2 Fm = g[((size_t)m3 * n2 + m2) * n1 + m1];
+         // Q_d = (F + conj(Fm)) / 2, Q_p = (F - conj(Fm)) / (2i)
+         const double dx = 0.5 * ((double)F.x + Fm.x), dy = 0.5 * ((double)F.y - Fm.y);
+         const double px = 0.5 * ((double)F.y + Fm.y), py = -0.5 * ((double)F.x - Fm.x);
+         const double ux = dx + px, uy = dy + py;
+         w = (double)wP * (((double)QM.x * ux + (double)QM.y * uy) + (dx * px + dy * py));
+      }
+      w *= infl[i];
+      const double vf = 2.0 * (1.0 + (double)pterm * hsq) / hsq;
+      v[0] += w * (vf * h[0] * h[0] - 1.0);
+      v[1] += w * (vf * h[1] * h[1] - 1.0);
+      v[2] += w * (vf * h[2] * h[2] - 1.0);
+      v[3] += w * vf * h[0] * h[1];
+      v[4] += w * vf * h[0] * h[2];
+      v[5] += w * vf * h[1] * h[2];
+   }
+   for (int c = 0; c < 6; ++c)
+      store_partial(red, c, v[c], sh);
+   if (!last_block(state + ST_TICKET0))
+      return;
+   double t[4];
+   sum_slots(red, 0, 4, gridDim.x, sh, t);
+   double t2[4];
+   sum_slots(red, 4, 2, gridDim.x, sh, t2);
+   if (threadIdx.x == 0) {
+      out[0] = t[0];
+      out[1] = t[1];
+      out[2] = t[2];
+      out[3] = t[3];
+      out[4] = t2[0];
+      out[5] = t2[1];
+   }
+}
+
+// ---------------------------------------------------------------------------
 // Force gathers: the 20 fractional derivatives of the reciprocal potential
 // (level-4 weights; the reference's fphi order: 0, x, y, z, xx, yy, zz, xy,
 // xz, yz, xxx, yyy, zzz, xxy, xxz, xyy, yyz, xzz, yzz, xyz), made Cartesian
@@ -520,11 +593,13 @@ __device__ __forceinline__ void mpole_force(const float* m, const float* c, floa
 // permanent grid: multipole forces, torque field and energies (MPOLE), the
 // polarization force on the dipoles in the permanent field gradient and the
 // Ewald self torque (POLAR)
+// wout (may be null): the fractional-transform part of the virial per slot,
+// [9][npad]; the dipole-grid gather adds to the same rows
 template <bool MPOLE, bool POLAR>
-__global__ void __launch_bounds__(256) k_gather_force_perm(int n, GridParams G, float f, float aewald,
+__global__ void __launch_bounds__(256) k_gather_force_perm(int n, int npad, GridParams G, float f, float aewald,
    const float4* __restrict__ spos, const float2* __restrict__ g, const float* __restrict__ rp,
    const float* __restrict__ u8, float* __restrict__ fout, float* __restrict__ tout, double* __restrict__ e_atom,
-   double* __restrict__ e_self)
+   double* __restrict__ e_self, float* __restrict__ wout)
 {
    const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
    const int lane = threadIdx.x & 31;
@@ -586,9 +661,12 @@ __global__ void __launch_bounds__(256) k_gather_force_perm(int n, GridParams G, 
          e_self[s] = fterm * (cii + a2 * (dii / 3.0 + 2.0 * a2 * qii * 0.2));
       }
    }
+   float us[3] = {0.f, 0.f, 0.f};
    if (POLAR) {
       const float* u = u8 + 8 * s;
-      const float us[3] = {u[0] + u[3], u[1] + u[4], u[2] + u[5]};
+      us[0] = u[0] + u[3];
+      us[1] = u[1] + u[4];
+      us[2] = u[2] + u[5];
       for (int a = 0; a < 3; ++a) {
          float v = 0.f;
          for (int b = 0; b < 3; ++b)
@@ -601,13 +679,30 @@ __global__ void __launch_bounds__(256) k_gather_force_perm(int n, GridParams G, 
       fout[3 * s + c] = F[c];
    for (int c = 0; c < 10; ++c)
       tout[10 * s + c] = T[c];
+   if (wout) {
+      // -f [phi_a d_b + 2 (phi2 Theta)_ab] (MPOLE), -f/2 phi_a u_b (POLAR)
+      const float Q[3][3] = {{m[4], m[7], m[8]}, {m[7], m[5], m[9]}, {m[8], m[9], m[6]}};
+      for (int a = 0; a < 3; ++a)
+         for (int b = 0; b < 3; ++b) {
+            float w = 0.f;
+            if (MPOLE) {
+               float pq = 0.f;
+               for (int c = 0; c < 3; ++c)
+                  pq += phi[ix2(a, c)] * Q[c][b];
+               w -= f * (phi[1 + a] * m[1 + b] + 2.f * pq);
+            }
+            if (POLAR)
+               w -= 0.5f * f * phi[1 + a] * us[b];
+            wout[(3 * a + b) * npad + s] = w;
+         }
+   }
 }
 
 // induced-dipole grid (d real, p imaginary): force on the multipoles in the
 // dipoles' potential, the mutual dipole force and the torque field
-__global__ void __launch_bounds__(256) k_gather_force_uind(int n, GridParams G, float f,
+__global__ void __launch_bounds__(256) k_gather_force_uind(int n, int npad, GridParams G, float f,
    const float4* __restrict__ spos, const float2* __restrict__ g, const float* __restrict__ rp,
-   const float* __restrict__ u8, float* __restrict__ fout, float* __restrict__ tout)
+   const float* __restrict__ u8, float* __restrict__ fout, float* __restrict__ tout, float* __restrict__ wout)
 {
    const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
    const int lane = threadIdx.x & 31;
@@ -663,6 +758,18 @@ __global__ void __launch_bounds__(256) k_gather_force_uind(int n, GridParams G, 
    }
    for (int c = 0; c < 10; ++c)
       tout[10 * s + c] = 0.5f * f * ps[c];
+   if (wout) {
+      // -f/2 [psi_a d_b + 2 (psi2 Theta)_ab + psi^p_a u_d,b + psi^d_a u_p,b]
+      const float Q[3][3] = {{m[4], m[7], m[8]}, {m[7], m[5], m[9]}, {m[8], m[9], m[6]}};
+      for (int a = 0; a < 3; ++a)
+         for (int b = 0; b < 3; ++b) {
+            float pq = 0.f;
+            for (int c = 0; c < 3; ++c)
+               pq += ps[ix2(a, c)] * Q[c][b];
+            const float w = ps[1 + a] * m[1 + b] + 2.f * pq + pp[1 + a] * u[b] + pd[1 + a] * u[3 + b];
+            wout[(3 * a + b) * npad + s] -= 0.5f * f * w;
+         }
+   }
 }
 
 // ---------------------------------------------------------------------------
@@ -723,6 +830,7 @@ void pme_free(Context* ctx)
    cudaFree(P.qgrid);
    cudaFree(P.qfx);
    cudaFree(P.infl);
+   cudaFree(P.qstash);
    P = PmeGrid();
 }
 
@@ -743,7 +851,10 @@ static GridParams grid_params(const Context* ctx)
    return G;
 }
 
-static int fft_conv(Context* ctx)
+// vir: 0 none, 1 permanent-grid k-space virial (wE, stash), 2 dipole-grid
+// cross terms (wP); the sums go to out[0..6)
+static int fft_conv(Context* ctx, int vir = 0, float wE = 0.f, float wP = 0.f, bool stash = false,
+   double* out = nullptr)
 {
    PmeGrid& P = ctx->pme;
    const size_t ng = (size_t)P.n1 * P.n2 * P.n3;
@@ -755,6 +866,20 @@ static int fft_conv(Context* ctx)
    if (cufftExecC2C(P.plan, (cufftComplex*)P.qgrid, (cufftComplex*)P.qgrid, CUFFT_FORWARD) != CUFFT_SUCCESS) {
       ctx->last_error = "cufftExecC2C forward failed";
       return T9GB_CUDA_ERR;
+   }
+   if (vir) {
+      const t9gb_config& c = ctx->cfg;
+      const float pterm = (float)((3.14159265358979323846 / c.aewald) * (3.14159265358979323846 / c.aewald));
+      if ((stash || vir == 2) && !P.qstash)
+         T9_CUDA(cudaMalloc(&P.qstash, sizeof(float2) * ng));
+      const int vb = (int)std::min<size_t>((ng + 255) / 256, RED_MAX);
+      if (vir == 1)
+         k_conv_virial<1><<<vb, 256, 0, ctx->stream>>>(P.n1, P.n2, P.n3, (float)c.box[0], (float)c.box[1],
+            (float)c.box[2], pterm, P.infl, P.qgrid, stash ? P.qstash : nullptr, wE, wP, ctx->red, out, ctx->status);
+      else
+         k_conv_virial<2><<<vb, 256, 0, ctx->stream>>>(P.n1, P.n2, P.n3, (float)c.box[0], (float)c.box[1],
+            (float)c.box[2], pterm, P.infl, P.qgrid, P.qstash, wE, wP, ctx->red, out, ctx->status);
+      T9_CUDA(cudaGetLastError());
    }
    k_conv<<<cb, 256, 0, ctx->stream>>>(ng, P.infl, P.qgrid);
    T9_CUDA(cudaGetLastError());
@@ -825,35 +950,42 @@ int launch_empole_recip(Context* ctx, double* e_atom)
 }  // namespace t9gb
 
 namespace t9gb {
-// reciprocal forces for elec_forces (force.cu)
-int launch_force_recip(Context* ctx, bool mpole, bool polar)
+// reciprocal forces for elec_forces (force.cu); wrec (may be null): the
+// per-slot fractional-transform virial rows, k-space sums in scal[40..52)
+int launch_force_recip(Context* ctx, bool mpole, bool polar, float* wrec)
 {
    GridParams G = grid_params(ctx);
    const int nb = grid_for((long long)ctx->n * 32, 256);
+   const int np = ctx->npad;
    const float f = (float)ctx->cfg.electric, a = (float)ctx->cfg.aewald;
+   const bool vir = wrec != nullptr;
+   if (vir) {
+      T9_CUDA(cudaMemsetAsync(wrec, 0, sizeof(float) * 9 * np, ctx->stream));
+      T9_CUDA(cudaMemsetAsync(ctx->scal + 40, 0, sizeof(double) * 12, ctx->stream));
+   }
    k_spread<0><<<nb, 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->srpole,
       reinterpret_cast<unsigned long long*>(ctx->pme.qfx));
    T9_CUDA(cudaGetLastError());
-   T9_CHECK(fft_conv(ctx));
-   double* er = ctx->e_atom + ctx->npad;
-   double* es = ctx->e_atom + 2 * ctx->npad;
+   T9_CHECK(fft_conv(ctx, vir ? 1 : 0, mpole ? 0.5f * f : 0.f, 0.f, vir && polar, ctx->scal + 40));
+   double* er = ctx->e_atom + np;
+   double* es = ctx->e_atom + 2 * np;
    if (mpole && polar)
-      k_gather_force_perm<true, true><<<nb, 256, 0, ctx->stream>>>(ctx->n, G, f, a, ctx->spos, ctx->pme.qgrid,
-         ctx->srpole, ctx->uind, ctx->frecp, ctx->trecp, er, es);
+      k_gather_force_perm<true, true><<<nb, 256, 0, ctx->stream>>>(ctx->n, np, G, f, a, ctx->spos, ctx->pme.qgrid,
+         ctx->srpole, ctx->uind, ctx->frecp, ctx->trecp, er, es, wrec);
    else if (mpole)
-      k_gather_force_perm<true, false><<<nb, 256, 0, ctx->stream>>>(ctx->n, G, f, a, ctx->spos, ctx->pme.qgrid,
-         ctx->srpole, ctx->uind, ctx->frecp, ctx->trecp, er, es);
+      k_gather_force_perm<true, false><<<nb, 256, 0, ctx->stream>>>(ctx->n, np, G, f, a, ctx->spos, ctx->pme.qgrid,
+         ctx->srpole, ctx->uind, ctx->frecp, ctx->trecp, er, es, wrec);
    else
-      k_gather_force_perm<false, true><<<nb, 256, 0, ctx->stream>>>(ctx->n, G, f, a, ctx->spos, ctx->pme.qgrid,
-         ctx->srpole, ctx->uind, ctx->frecp, ctx->trecp, nullptr, nullptr);
+      k_gather_force_perm<false, true><<<nb, 256, 0, ctx->stream>>>(ctx->n, np, G, f, a, ctx->spos, ctx->pme.qgrid,
+         ctx->srpole, ctx->uind, ctx->frecp, ctx->trecp, nullptr, nullptr, wrec);
    T9_CUDA(cudaGetLastError());
    if (polar) {
       k_spread<1><<<nb, 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->uind,
          reinterpret_cast<unsigned long long*>(ctx->pme.qfx));
       T9_CUDA(cudaGetLastError());
-      T9_CHECK(fft_conv(ctx));
-      k_gather_force_uind<<<nb, 256, 0, ctx->stream>>>(ctx->n, G, f, ctx->spos, ctx->pme.qgrid, ctx->srpole,
-         ctx->uind, ctx->frecu, ctx->trecu);
+      T9_CHECK(fft_conv(ctx, vir ? 2 : 0, 0.f, 0.5f * f, false, ctx->scal + 46));
+      k_gather_force_uind<<<nb, 256, 0, ctx->stream>>>(ctx->n, np, G, f, ctx->spos, ctx->pme.qgrid, ctx->srpole,
+         ctx->uind, ctx->frecu, ctx->trecu, wrec);
       T9_CUDA(cudaGetLastError());
    }
    return T9GB_OK;
