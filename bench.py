@@ -339,7 +339,10 @@ def main():
     stream = torch.cuda.Stream()
     eng = abi.Engine(s, predictor=pred, stream=stream)
     eng.prepare(tr.frame(0))
-    nsteps = args.history + args.warmup + args.steps
+    # frames: predictor history, warm-up, then the timed, e2e and per-kernel
+    # passes, each continuing the trajectory (no time jumps for the predictor)
+    f0 = args.history + args.warmup
+    nsteps = f0 + 3 * args.steps
     frames = np.stack([tr.frame(t) for t in range(nsteps)]).astype(np.float32)
     # device-resident inputs for the kernel-only measurement
     dev_frames = torch.from_numpy(frames).to("cuda")
@@ -395,7 +398,7 @@ def main():
     hp = np.zeros((s.n, 3))
     e2e_t = []
     for k in range(args.steps):
-        x = frames[args.history + args.warmup + k].astype(np.float64)
+        x = frames[f0 + args.steps + k].astype(np.float64)
         flush.fill_(float(k))
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -414,7 +417,7 @@ def main():
     prof_iters = []
     with torch.cuda.stream(stream):
         for k in range(args.steps):
-            step_device(args.history + args.warmup + k)
+            step_device(f0 + 2 * args.steps + k)
             prof_iters.append(eng.stats()[0])
     prof = eng.profile_read(reset=True)
     eng.profile(False)

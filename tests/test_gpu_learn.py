@@ -133,7 +133,9 @@ def test_fallback_rejects_a_bad_network(gpu_lib, tg, LO):
     e.learn_weights(w * 40.0)
     rec = []
     _run(e, traj, [10], 2, rec)
+    # the same frames without a network (same neighbour-list history)
     ref = engine_for(s)
+    _run(ref, traj, [0, 1, 2, 10, 10], 0)
     ud_ref, up_ref, _ = ref.induce_host(traj.frame(10))
     ud, up, _ = e.induce_host(traj.frame(10))
     it, eps, st, choice, eps0_p, eps0_l, _, compared = rec[0]
@@ -144,24 +146,28 @@ def test_fallback_rejects_a_bad_network(gpu_lib, tg, LO):
 def test_probe_policy(gpu_lib, tg):
     """probe_every = 4: the comparison runs on every 4th solve; the solves in
     between start from the learned guess without computing the plain
-    residual and give the same bits as a solve that compares and picks it."""
+    residual and give the same bits as a solve that compares and picks it
+    (two engines with the same history, probe 4 and probe 1)."""
     s = tg.systems.make_config("water648")
     traj = tg.systems.Trajectory(s)
-    e = engine_for(s)
-    e.learn_reset(seed=2)
-    _run(e, traj, range(100), 1)
-    e.learn_policy(4)
-    rec, sol = [], []
-    e.learn_config(2)
+    engines = []
+    for probe in (4, 1):
+        e = engine_for(s)
+        e.learn_reset(seed=2)
+        _run(e, traj, range(100), 1)
+        e.learn_policy(probe)
+        e.learn_config(2)
+        engines.append(e)
+    rec, sol = [[], []], [[], []]
     for k in range(100, 106):
-        sol.append(e.induce_host(traj.frame(k))[:2])
-        rec.append(e.learn_stats())
-    assert [r[4] for r in rec] == [1, 0, 0, 0, 1, 0]
-    assert all(r[0] == 3 for r in rec)
-    e.learn_policy(1)
-    ud, up, _ = e.induce_host(traj.frame(101))
-    assert e.learn_stats()[4] == 1 and e.learn_stats()[0] == 3
-    assert np.array_equal(ud, sol[1][0]) and np.array_equal(up, sol[1][1])
+        for j, e in enumerate(engines):
+            sol[j].append(e.induce_host(traj.frame(k))[:2])
+            rec[j].append(e.learn_stats())
+    assert [r[4] for r in rec[0]] == [1, 0, 0, 0, 1, 0]
+    assert [r[4] for r in rec[1]] == [1] * 6
+    assert all(r[0] == 3 for r in rec[0] + rec[1])
+    for k in range(6):
+        assert np.array_equal(sol[0][k][0], sol[1][k][0]) and np.array_equal(sol[0][k][1], sol[1][k][1])
 
 
 def test_learned_graph_matches_stepwise(gpu_lib, tg):

@@ -46,6 +46,11 @@ static int alloc_all(Context* ctx)
    }
    T9_CUDA(cudaMalloc(&ctx->e_atom, sizeof(double) * 3 * npad));
    T9_CUDA(cudaMalloc(&ctx->sframe, sizeof(float) * 9 * npad));
+   T9_CUDA(cudaMalloc(&ctx->sref, sizeof(float4) * npad));
+   T9_CUDA(cudaMemset(ctx->sref, 0, sizeof(float4) * npad));
+   T9_CUDA(cudaMalloc(&ctx->lflag, sizeof(int)));
+   T9_CUDA(cudaMemset(ctx->lflag, 0, sizeof(int)));
+   T9_CUDA(cudaMallocHost(&ctx->h_lflag, sizeof(int)));
    T9_CUDA(cudaMalloc(&ctx->hout, sizeof(float) * 6 * npad));
    T9_CUDA(cudaMalloc(&ctx->red, sizeof(double) * RED_SLOTS * RED_MAX));
    T9_CUDA(cudaMalloc(&ctx->scal, sizeof(double) * 64));
@@ -72,7 +77,7 @@ static void free_all(Context* ctx)
       ctx->sdamp, ctx->srpole, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->nbr, ctx->nnbr, ctx->nbr_over,
       ctx->cell_count, ctx->cell_start, ctx->cell_atoms, ctx->atom_cell, ctx->rcp6, ctx->fld6, ctx->udir,
       ctx->efield, ctx->uind, ctx->rsd, ctx->zrsd, ctx->conj, ctx->vec, ctx->tmp6, ctx->e_atom, ctx->sframe, ctx->hout,
-      ctx->red, ctx->scal, ctx->status,
+      ctx->red, ctx->scal, ctx->status, ctx->sref, ctx->lflag,
       ctx->aspc_hist};
    for (void* p : dev)
       if (p)
@@ -85,6 +90,8 @@ static void free_all(Context* ctx)
       cudaFreeHost(ctx->h_stage);
    if (ctx->h_over)
       cudaFreeHost(ctx->h_over);
+   if (ctx->h_lflag)
+      cudaFreeHost(ctx->h_lflag);
    pme_free(ctx);
    learn_free(ctx);
    force_free(ctx);
@@ -417,7 +424,7 @@ int t9gb_nblist_stats(t9gb_context* h, int* capacity, long long* entries, int* n
       *nscaled = ctx->nsp / 2;
    if (entries) {
       *entries = 0;
-      if (ctx->have_order && !ctx->list_stale) {
+      if (ctx->have_order && !ctx->list_need_build) {
          std::vector<int> cnt(ctx->npad);
          T9_CUDA(cudaMemcpyAsync(cnt.data(), ctx->nnbr, sizeof(int) * ctx->npad, cudaMemcpyDeviceToHost, ctx->stream));
          T9_CUDA(cudaStreamSynchronize(ctx->stream));

@@ -154,7 +154,11 @@ struct Context {
    int* nnbr = nullptr;      // [npad]
    int* nbr_over = nullptr;  // device max count seen (overflow check)
    int* h_over = nullptr;    // pinned mirror
-   bool list_stale = true;
+   bool list_stale = true;        // positions changed since the last list check
+   bool list_need_build = true;   // no valid list for the current order / capacity
+   float4* sref = nullptr;        // [npad] positions at the last list build
+   int* lflag = nullptr;          // device: rebuild requested / an atom moved too far
+   int* h_lflag = nullptr;        // pinned mirror
    bool use_cells = false;
    int nc[3] = {0, 0, 0};
    int ncell = 0;

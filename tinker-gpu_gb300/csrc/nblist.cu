@@ -202,6 +202,7 @@ int order_build(Context* ctx)
    T9_CHECK(frame_map_build(ctx));
    ctx->have_order = true;
    ctx->list_stale = true;
+   ctx->list_need_build = true;
    drop_graphs(ctx);
    // a new order invalidates the predictor history
    return reset_predictor(ctx);
@@ -537,7 +538,6 @@ int list_update(Context* ctx)
    }
    prof_end(ctx);
    T9_CUDA(cudaGetLastError());
-   ctx->list_stale = false;
    return T9GB_OK;
 }
 

@@ -255,18 +255,123 @@ static VecArgs vec_args(const Context* ctx)
    return A;
 }
 
-static int list_now(Context* ctx)
+// ---------------------------------------------------------------------------
+// Verlet reuse of the neighbour list.  The list holds the pairs within
+// cutoff + buffer at its build; it stays valid while every atom is within
+// half the buffer of its position at the build.  It is rebuilt when the host
+// requests it (new order, grown capacity, overflow) or when the device check
+// finds an atom that moved further.  Inside the induce() graph the decision
+// is a conditional IF node set by the check kernel; the host-driven path
+// reads the same flag, so both paths make the same decisions.
+
+__global__ void k_disp_check(int npad, const float4* __restrict__ spos, const float4* __restrict__ sref, float lx,
+   float ly, float lz, float ilx, float ily, float ilz, float lim2, int* __restrict__ flag, int* __restrict__ state,
+   cudaGraphConditionalHandle handle, int use_handle)
 {
-   T9_CHECK(list_update(ctx));
-   T9_CUDA(cudaMemcpyAsync(ctx->h_over, ctx->nbr_over, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < npad; s += gridDim.x * blockDim.x) {
+      const float4 a = spos[s], b = sref[s];
+      const float dx = image1(a.x - b.x, lx, ilx), dy = image1(a.y - b.y, ly, ily), dz = image1(a.z - b.z, lz, ilz);
+      if (dx * dx + dy * dy + dz * dz > lim2)
+         atomicOr(flag, 1);
+   }
+   if (!last_block(state + ST_TICKET0))
+      return;
+   if (threadIdx.x == 0 && use_handle)
+      cudaGraphSetConditional(handle, *(volatile int*)flag ? 1u : 0u);
+}
+
+__global__ void k_list_done(int npad, const float4* __restrict__ spos, float4* __restrict__ sref, int* __restrict__ flag)
+{
+   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < npad; s += gridDim.x * blockDim.x)
+      sref[s] = spos[s];
+   if (blockIdx.x == 0 && threadIdx.x == 0)
+      *flag = 0;
+}
+
+static int list_request(Context* ctx)
+{
+   if (ctx->list_need_build) {
+      T9_CUDA(cudaMemsetAsync(ctx->lflag, 0xff, sizeof(int), ctx->stream));
+      ctx->list_need_build = false;
+   }
    return T9GB_OK;
 }
 
+static int launch_disp_check(Context* ctx, cudaGraphConditionalHandle handle, int use_handle)
+{
+   const t9gb_config& c = ctx->cfg;
+   const bool pbc = c.box[0] > 0 && c.box[1] > 0 && c.box[2] > 0;
+   const float half = 0.5f * (float)c.list_buffer;
+   const int nb = std::min(RED_MAX, grid_for(ctx->npad, 256));
+   k_disp_check<<<nb, 256, 0, ctx->stream>>>(ctx->npad, ctx->spos, ctx->sref, pbc ? (float)c.box[0] : 0.f,
+      pbc ? (float)c.box[1] : 0.f, pbc ? (float)c.box[2] : 0.f, pbc ? (float)(1.0 / c.box[0]) : 0.f,
+      pbc ? (float)(1.0 / c.box[1]) : 0.f, pbc ? (float)(1.0 / c.box[2]) : 0.f, half * half, ctx->lflag, ctx->status,
+      handle, use_handle);
+   T9_CUDA(cudaGetLastError());
+   return T9GB_OK;
+}
+
+static int list_build_body(Context* ctx)
+{
+   T9_CHECK(list_update(ctx));
+   k_list_done<<<grid_for(ctx->npad, 256), 256, 0, ctx->stream>>>(ctx->npad, ctx->spos, ctx->sref, ctx->lflag);
+   T9_CUDA(cudaGetLastError());
+   return T9GB_OK;
+}
+
+// host-driven refresh (one synchronisation)
 int ensure_list(Context* ctx)
 {
-   if (!ctx->list_stale)
+   if (!ctx->list_stale && !ctx->list_need_build)
       return T9GB_OK;
-   return list_now(ctx);
+   T9_CHECK(list_request(ctx));
+   T9_CHECK(launch_disp_check(ctx, 0, 0));
+   T9_CUDA(cudaMemcpyAsync(ctx->h_lflag, ctx->lflag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+   T9_CUDA(cudaStreamSynchronize(ctx->stream));
+   if (*ctx->h_lflag)
+      T9_CHECK(list_build_body(ctx));
+   T9_CUDA(cudaMemcpyAsync(ctx->h_over, ctx->nbr_over, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+   ctx->list_stale = false;
+   return T9GB_OK;
+}
+
+// the same inside a stream capture: check kernel, then a conditional IF node
+// whose body rebuilds the list
+static int list_refresh_graph(Context* ctx)
+{
+   cudaStream_t s0 = ctx->stream;
+   cudaStreamCaptureStatus cs;
+   cudaGraph_t cap = nullptr;
+   const cudaGraphNode_t* deps = nullptr;
+   size_t ndeps = 0;
+   if (cudaStreamGetCaptureInfo(s0, &cs, nullptr, &cap, &deps, nullptr, &ndeps) != cudaSuccess)
+      return T9GB_CUDA_ERR;
+   cudaGraphConditionalHandle handle = 0;
+   T9_CUDA(cudaGraphConditionalHandleCreate(&handle, cap, 0, cudaGraphCondAssignDefault));
+   T9_CHECK(launch_disp_check(ctx, handle, 1));
+   if (cudaStreamGetCaptureInfo(s0, &cs, nullptr, &cap, &deps, nullptr, &ndeps) != cudaSuccess)
+      return T9GB_CUDA_ERR;
+   cudaGraphNodeParams cp = {};
+   cp.type = cudaGraphNodeTypeConditional;
+   cp.conditional.handle = handle;
+   cp.conditional.type = cudaGraphCondTypeIf;
+   cp.conditional.size = 1;
+   cudaGraphNode_t node = nullptr;
+   T9_CUDA(cudaGraphAddNode(&node, cap, deps, nullptr, ndeps, &cp));
+   T9_CUDA(cudaStreamUpdateCaptureDependencies(s0, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+   if (!ctx->cap_stream)
+      T9_CUDA(cudaStreamCreateWithFlags(&ctx->cap_stream, cudaStreamNonBlocking));
+   cudaGraph_t body = cp.conditional.phGraph_out[0];
+   T9_CUDA(cudaStreamBeginCaptureToGraph(ctx->cap_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+   ctx->stream = ctx->cap_stream;
+   int rc = list_build_body(ctx);
+   ctx->stream = s0;
+   cudaGraph_t tmp = nullptr;
+   if (cudaStreamEndCapture(ctx->cap_stream, &tmp) != cudaSuccess && rc == T9GB_OK)
+      rc = T9GB_CUDA_ERR;
+   T9_CHECK(rc);
+   T9_CUDA(cudaMemcpyAsync(ctx->h_over, ctx->nbr_over, sizeof(int), cudaMemcpyDeviceToHost, s0));
+   return T9GB_OK;
 }
 
 // after a synchronisation: grow the list if an atom had more neighbours than
@@ -283,7 +388,7 @@ int check_list_overflow(Context* ctx, int* redo)
    ctx->nbr_cap = cap;
    *ctx->h_over = 0;
    T9_CUDA(cudaMemsetAsync(ctx->nbr_over, 0, sizeof(int), ctx->stream));
-   ctx->list_stale = true;
+   ctx->list_need_build = true;
    drop_graphs(ctx);
    *redo = 1;
    return T9GB_OK;
@@ -331,7 +436,7 @@ enum { V_PLAIN = 0, V_LEARNED = 1, V_COMPARE = 2 };
 static int pcg_start(Context* ctx, const VecArgs& A, bool graph, int variant)
 {
    const t9gb_config& c = ctx->cfg;
-   T9_CHECK(graph ? list_now(ctx) : ensure_list(ctx));
+   T9_CHECK(graph ? list_refresh_graph(ctx) : ensure_list(ctx));
    T9_CHECK(dfield6(ctx, ctx->fld6));
    k_init_guess<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->fld6, ctx->efield, ctx->udir, ctx->uind, c.pcgguess,
       c.predictor == 1 ? 1 : 0, ctx->aspc_hist, ctx->status);
@@ -466,6 +571,7 @@ static int induce_graph(Context* ctx, int variant)
 {
    if (!ctx->graph_exec[variant])
       T9_CHECK(induce_capture(ctx, variant));
+   T9_CHECK(list_request(ctx));
    T9_CUDA(cudaGraphLaunch(ctx->graph_exec[variant], ctx->stream));
    T9_CUDA(cudaStreamSynchronize(ctx->stream));
    ctx->list_stale = false;
