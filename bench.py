@@ -46,6 +46,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--learn-train", type=int, default=500, help="online training steps before the learned legs")
     ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--no-forces", action="store_true")
+    ap.add_argument("--no-flush", action="store_true",
+                    help="skip the 512 MB L2 flush buffer (for ncu captures only; numbers are not bench values)")
     return ap.parse_args()
 
 
@@ -339,16 +342,16 @@ def main():
     stream = torch.cuda.Stream()
     eng = abi.Engine(s, predictor=pred, stream=stream)
     eng.prepare(tr.frame(0))
-    # frames: predictor history, warm-up, then the timed, e2e and per-kernel
-    # passes, each continuing the trajectory (no time jumps for the predictor)
+    # frames: predictor history, warm-up, then the timed, e2e, per-kernel and
+    # force passes, each continuing the trajectory (no time jumps for the predictor)
     f0 = args.history + args.warmup
-    nsteps = f0 + 3 * args.steps
+    nsteps = f0 + 4 * args.steps
     frames = np.stack([tr.frame(t) for t in range(nsteps)]).astype(np.float32)
     # device-resident inputs for the kernel-only measurement
     dev_frames = torch.from_numpy(frames).to("cuda")
     ud = torch.zeros((s.n, 3), device="cuda")
     up = torch.zeros((s.n, 3), device="cuda")
-    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    flush = torch.empty((16 if args.no_flush else 512 * 1024 * 1024) // 4, dtype=torch.float32, device="cuda")
 
     def step_device(t):
         eng.set_xyz_device(dev_frames[t])
@@ -435,6 +438,26 @@ def main():
     # M r0 1, dots 1, history 1, output 1; per PCG iteration: ufield 5 + precond 1 + vector 4
     launches_per_step = 25 + 10 * mean_it
 
+    # ---- forces: emplar (induce + multipole and polarization energy, gradient, virial) ----
+    forces = None
+    if not args.no_forces:
+        fms = []
+        with torch.cuda.stream(stream):
+            for k in range(args.steps):
+                eng.set_xyz_device(dev_frames[f0 + 3 * args.steps + k])
+                eng.mpole_init()
+                flush.fill_(float(k))
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                eng.emplar(abi.CALC_ENERGY | abi.CALC_GRAD | abi.CALC_VIRIAL)
+                b.record(stream)
+                b.synchronize()
+                fms.append(a.elapsed_time(b))
+        em = float(np.mean(fms))
+        forces = {"emplar_ms_per_step": em, "induce_ms_per_step": 1000 * dev_sec / args.steps,
+                  "forces_virial_ms_per_step": em - 1000 * dev_sec / args.steps,
+                  "note": "t9gb_emplar(energy|grad|virial): induce + real-space and PME forces, torques, virial"}
+
     learned = None
     if not args.no_learned and args.learn_train > 0:
         learned = learned_legs(args, s, abi, stream, tr, flush, check_oracle=rank == 0 and not args.no_cpu_baseline)
@@ -460,7 +483,8 @@ def main():
             "config": {
                 "workload": args.config, "atoms": s.n, "pme_grid": list(s.settings["nfft"]), "cutoff_A": 7.0,
                 "poleps_debye": s.settings["poleps"], "predictor": args.predictor, "history_frames": args.history,
-                "l2": "flushed (512 MB write) between timed steps", "parallelism": f"replicas x{world}",
+                "l2": "not flushed (profiling run)" if args.no_flush else "flushed (512 MB write) between timed steps",
+                "parallelism": f"replicas x{world}",
             },
             "induce_ms_per_step": 1000 * dev_sec / args.steps,
             "pcg_iterations_per_step": mean_it,
@@ -478,6 +502,7 @@ def main():
             "clocks": ck,
             "cpu_baseline": cpu,
             "learned_guess": learned,
+            "forces": forces,
         }
         print(json.dumps(line), flush=True)
     eng.close()

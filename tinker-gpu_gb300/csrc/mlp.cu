@@ -112,6 +112,7 @@ __global__ void k_sum_splits(int size, int nsplit, const float* __restrict__ par
 {
    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < size; i += gridDim.x * blockDim.x) {
       float v = 0.f;
+#pragma unroll 8
       for (int z = 0; z < nsplit; ++z)
          v += part[(size_t)z * size + i];
       out[i] = v;
@@ -200,29 +201,69 @@ __global__ void k_loss_grad(int rows, const float* __restrict__ Y, const float* 
    }
 }
 
-// column sums of a [rows][N] f32 matrix (split rows, fixed-order combine)
-__global__ void k_colsum_part(int rows, int N, int rchunk, const float* __restrict__ X, float* __restrict__ part)
+// Column sums of a [rows][N] f32 matrix (N <= 64), two fixed-order levels:
+// COLSUM_BLOCKS blocks of 4 x 64 threads (column c = thread % 64, row group
+// thread / 64) stride over the rows, then one block per column combines the
+// block partials with a shared-memory tree.
+constexpr int COLSUM_BLOCKS = 64;
+
+__global__ void __launch_bounds__(256) k_colsum_part(int rows, int N, const float* __restrict__ X,
+   float* __restrict__ part)
 {
-   const int c = threadIdx.x;
-   if (c >= N)
-      return;
-   const int r0 = blockIdx.x * rchunk, r1 = min(rows, r0 + rchunk);
+   __shared__ float sh[4][64];
+   const int c = threadIdx.x & 63, g = threadIdx.x >> 6;
    float v = 0.f;
-   for (int r = r0; r < r1; ++r)
-      v += X[(size_t)r * N + c];
-   part[(size_t)blockIdx.x * N + c] = v;
+   if (c < N)
+      for (int r = blockIdx.x * 4 + g; r < rows; r += COLSUM_BLOCKS * 4)
+         v += X[(size_t)r * N + c];
+   sh[g][c] = v;
+   __syncthreads();
+   if (g == 0 && c < N)
+      part[(size_t)blockIdx.x * N + c] = (sh[0][c] + sh[1][c]) + (sh[2][c] + sh[3][c]);
 }
 
-// fixed-order sum of a double array (one block)
-__global__ void k_sum_double(int n, const double* __restrict__ a, double* __restrict__ out)
+__global__ void __launch_bounds__(COLSUM_BLOCKS) k_colsum_final(int N, const float* __restrict__ part,
+   float* __restrict__ out)
+{
+   __shared__ float sh[COLSUM_BLOCKS];
+   const int c = blockIdx.x;
+   sh[threadIdx.x] = part[(size_t)threadIdx.x * N + c];
+   __syncthreads();
+   for (int o = COLSUM_BLOCKS / 2; o > 0; o >>= 1) {
+      if (threadIdx.x < o)
+         sh[threadIdx.x] += sh[threadIdx.x + o];
+      __syncthreads();
+   }
+   if (threadIdx.x == 0)
+      out[c] = sh[0];
+}
+
+// fixed-order sum of a double array: block partials, then one block
+__global__ void __launch_bounds__(256) k_sum_double_part(int n, const double* __restrict__ a,
+   double* __restrict__ part)
 {
    __shared__ double sh[256];
    double v = 0;
-   for (int i = threadIdx.x; i < n; i += blockDim.x)
+   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
       v += a[i];
    sh[threadIdx.x] = v;
    __syncthreads();
    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+      if (threadIdx.x < o)
+         sh[threadIdx.x] += sh[threadIdx.x + o];
+      __syncthreads();
+   }
+   if (threadIdx.x == 0)
+      part[blockIdx.x] = sh[0];
+}
+
+__global__ void __launch_bounds__(64) k_sum_double_final(int nb, const double* __restrict__ part,
+   double* __restrict__ out)
+{
+   __shared__ double sh[64];
+   sh[threadIdx.x] = threadIdx.x < nb ? part[threadIdx.x] : 0.0;
+   __syncthreads();
+   for (int o = 32; o > 0; o >>= 1) {
       if (threadIdx.x < o)
          sh[threadIdx.x] += sh[threadIdx.x + o];
       __syncthreads();
@@ -310,7 +351,7 @@ int mlp_alloc(Context* ctx, int max_rows, unsigned seed)
    T9_CUDA(cudaMalloc(&S.dzf, sizeof(float) * R * MLP_HID));
    T9_CUDA(cudaMalloc(&S.err, sizeof(double) * R));
    T9_CUDA(cudaMalloc(&S.loss, sizeof(double)));
-   S.nsplit = 64;
+   S.nsplit = 128;
    T9_CUDA(cudaMalloc(&S.split, sizeof(float) * (size_t)std::max<size_t>(S.nsplit * MLP_HID * MLP_HID, 1024 * MLP_HID)));
    return mlp_init(ctx, seed);
 }
@@ -416,28 +457,29 @@ int mlp_backward(Context* ctx, int rows, const float* rowpol, int npad)
    const int ns = S.nsplit;
    k_loss_grad<<<grid_for(rows, 256), 256, 0, ctx->stream>>>(rows, S.y, S.t, rowpol, npad, S.dy, S.dyf,
       S.err);
-   k_sum_double<<<1, 256, 0, ctx->stream>>>(rows, S.err, S.loss);
+   double* dpart = reinterpret_cast<double*>(S.split);
+   k_sum_double_part<<<64, 256, 0, ctx->stream>>>(rows, S.err, dpart);
+   k_sum_double_final<<<1, 64, 0, ctx->stream>>>(64, dpart, S.loss);
    T9_CUDA(cudaMemsetAsync(S.g, 0, sizeof(float) * MLP_NPARAM, ctx->stream));
+   auto colsum = [&](int N, const float* X, float* out) {
+      k_colsum_part<<<COLSUM_BLOCKS, 256, 0, ctx->stream>>>(rows, N, X, S.split);
+      k_colsum_final<<<N, COLSUM_BLOCKS, 0, ctx->stream>>>(N, S.split, out);
+   };
    // layer 3: dW3 = H2^T dY, db3 = colsum dY, dH2 = dY W3^T
    T9_CHECK(gemm(ctx, true, false, MLP_HID, MLP_OUT_PAD, rows, S.h2, MLP_HID, S.dy, MLP_OUT_PAD, S.g + OFF_W3, ns));
-   const int rchunk = (rows + 1023) / 1024;
-   const int nb = grid_for(rows, rchunk);
-   k_colsum_part<<<nb, 64, 0, ctx->stream>>>(rows, MLP_OUT_PAD, rchunk, S.dyf, S.split);
-   k_sum_splits<<<1, 64, 0, ctx->stream>>>(MLP_OUT_PAD, nb, S.split, S.g + OFF_B3);
+   colsum(MLP_OUT_PAD, S.dyf, S.g + OFF_B3);
    T9_CHECK(gemm(ctx, false, true, rows, MLP_HID, MLP_OUT_PAD, S.dy, MLP_OUT_PAD, wb + BF_W3, MLP_OUT_PAD, S.c, 1));
    k_silu_back<<<grid_for((long long)rows * MLP_HID, 256), 256, 0, ctx->stream>>>(rows * MLP_HID, S.c, S.z2, S.dz,
       S.dzf);
    // layer 2: dW2 = H1^T dZ2, db2, dH1 = dZ2 W2^T
    T9_CHECK(gemm(ctx, true, false, MLP_HID, MLP_HID, rows, S.h1, MLP_HID, S.dz, MLP_HID, S.g + OFF_W2, ns));
-   k_colsum_part<<<nb, 64, 0, ctx->stream>>>(rows, MLP_HID, rchunk, S.dzf, S.split);
-   k_sum_splits<<<1, 64, 0, ctx->stream>>>(MLP_HID, nb, S.split, S.g + OFF_B2);
+   colsum(MLP_HID, S.dzf, S.g + OFF_B2);
    T9_CHECK(gemm(ctx, false, true, rows, MLP_HID, MLP_HID, S.dz, MLP_HID, wb + BF_W2, MLP_HID, S.c, 1));
    k_silu_back<<<grid_for((long long)rows * MLP_HID, 256), 256, 0, ctx->stream>>>(rows * MLP_HID, S.c, S.z1, S.dz,
       S.dzf);
    // layer 1: dW1 = X^T dZ1, db1
    T9_CHECK(gemm(ctx, true, false, MLP_IN, MLP_HID, rows, S.x, MLP_IN, S.dz, MLP_HID, S.g + OFF_W1, ns));
-   k_colsum_part<<<nb, 64, 0, ctx->stream>>>(rows, MLP_HID, rchunk, S.dzf, S.split);
-   k_sum_splits<<<1, 64, 0, ctx->stream>>>(MLP_HID, nb, S.split, S.g + OFF_B1);
+   colsum(MLP_HID, S.dzf, S.g + OFF_B1);
    T9_CUDA(cudaGetLastError());
    return T9GB_OK;
 }
