@@ -47,6 +47,7 @@ def parse():
     ap.add_argument("--learn-train", type=int, default=500, help="online training steps before the learned legs")
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--no-forces", action="store_true")
+    ap.add_argument("--own-fft", action="store_true", help="the library's fused transform instead of cuFFT")
     ap.add_argument("--no-flush", action="store_true",
                     help="skip the 512 MB L2 flush buffer (for ncu captures only; numbers are not bench values)")
     return ap.parse_args()
@@ -342,6 +343,8 @@ def main():
     stream = torch.cuda.Stream()
     eng = abi.Engine(s, predictor=pred, stream=stream)
     eng.prepare(tr.frame(0))
+    if args.own_fft:
+        eng.pme_own_fft(True)
     # frames: predictor history, warm-up, then the timed, e2e, per-kernel and
     # force passes, each continuing the trajectory (no time jumps for the predictor)
     f0 = args.history + args.warmup
@@ -483,6 +486,7 @@ def main():
             "config": {
                 "workload": args.config, "atoms": s.n, "pme_grid": list(s.settings["nfft"]), "cutoff_A": 7.0,
                 "poleps_debye": s.settings["poleps"], "predictor": args.predictor, "history_frames": args.history,
+                "fft": "fused power-of-two transform (library)" if args.own_fft else "cuFFT C2C",
                 "l2": "not flushed (profiling run)" if args.no_flush else "flushed (512 MB write) between timed steps",
                 "parallelism": f"replicas x{world}",
             },

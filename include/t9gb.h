@@ -187,6 +187,15 @@ int t9gb_energy_components(t9gb_context* ctx, double* parts);
  * pattern, pcg.cu:144-145).  Both give bit-identical dipoles. */
 int t9gb_use_graph(t9gb_context* ctx, int enable);
 
+/* PME 3-D FFT: the library's fused transform (enable = 1; power-of-two grids
+ * of 16..128 points per edge: five single-axis radix-2 passes in shared
+ * memory, the fixed-point conversion in the first and the influence function
+ * between the z passes) or cuFFT C2C (enable = 0, the default; always used
+ * for other grid sizes).  Replaces fftfront/fftback + pmeConv
+ * (src/cudart/fft.cpp:65-95, src/cu/pme.cu:908-1031).  Enabling on an
+ * unsupported grid returns T9GB_BAD_ARG. */
+int t9gb_pme_own_fft(t9gb_context* ctx, int enable);
+
 /* Neighbour-list sizes: row capacity, entries of the current list (both
  * directions) and scaled pairs (the reference's Spatial::nakpl/niak,
  * include/ff/spatial.h:15-140). */

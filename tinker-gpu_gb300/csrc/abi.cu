@@ -452,6 +452,19 @@ int t9gb_learn_config(t9gb_context* h, int mode, double lr, double weight_decay)
    return T9GB_OK;
 }
 
+int t9gb_pme_own_fft(t9gb_context* h, int enable)
+{
+   if (!h)
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   if (enable && !ctx->pme.own_fft_ok)
+      return T9GB_BAD_ARG;
+   if ((enable != 0) != ctx->pme.own_fft)
+      drop_graphs(ctx);
+   ctx->pme.own_fft = enable != 0;
+   return T9GB_OK;
+}
+
 int t9gb_learn_policy(t9gb_context* h, int probe_every)
 {
    if (!h || probe_every < 1)

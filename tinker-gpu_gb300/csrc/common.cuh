@@ -42,6 +42,8 @@ __device__ __forceinline__ float image1(float d, float l, float linv) { return d
 
 struct PmeGrid {
    int n1 = 0, n2 = 0, n3 = 0;
+   bool own_fft = false;      // power-of-two grid: the library's fused FFT path
+   bool own_fft_ok = false;   // the grid qualifies
    cufftHandle plan = 0;
    float2* qgrid = nullptr;   // complex grid [n3][n2][n1]
    long long* qfx = nullptr;  // fixed-point accumulation grid [n3][n2][n1][2]
