@@ -47,7 +47,10 @@ def parse():
     ap.add_argument("--learn-train", type=int, default=500, help="online training steps before the learned legs")
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--no-forces", action="store_true")
+    ap.add_argument("--no-large", action="store_true", help="skip the 98,304-atom leg")
+    ap.add_argument("--large-config", default="water98304")
     ap.add_argument("--own-fft", action="store_true", help="the library's fused transform instead of cuFFT")
+    ap.add_argument("--lanes", type=int, default=8, help="lanes per atom in the real-space field kernels")
     ap.add_argument("--no-flush", action="store_true",
                     help="skip the 512 MB L2 flush buffer (for ncu captures only; numbers are not bench values)")
     return ap.parse_args()
@@ -228,6 +231,55 @@ def cpu_baseline_sample(args, s, tr):
             "sample": f"{nsteps} induce() calls on {args.config} (FP64, direct guess, all host threads)"}
 
 
+def kernel_rooflines(kernels, n, entries, nfft, peak):
+    """Algorithmic bytes per launch / average event time of each profiled kernel."""
+    out = {}
+    for k, v in kernels.items():
+        if not v.get("ms_per_launch"):
+            continue
+        alg = algorithmic_bytes(k, n, entries, nfft)
+        gbs = alg / (v["ms_per_launch"] / 1000.0) / 1e9
+        out[k] = {"algorithmic_bytes": alg, "achieved_gbs": gbs, "frac": gbs / peak}
+    return out
+
+
+def large_leg(args, abi, tg, stream, flush, peak):
+    """The 98,304-atom box (PME 128^3): induce ms/step in the graph, per-kernel
+    rooflines from a profiled pass, and the learned-guess legs."""
+    import torch
+
+    s = tg.systems.make_config(args.large_config)
+    tr = tg.systems.Trajectory(s, seed=17)
+    eng = abi.Engine(s, predictor=1, stream=stream)
+    eng.prepare(tr.frame(0))
+    K, W, H = args.steps, args.warmup, args.history
+    dev = torch.from_numpy(np.stack([tr.frame(t) for t in range(H + W + 2 * K)]).astype(np.float32)).to("cuda")
+    ud = torch.zeros((s.n, 3), device="cuda")
+    up = torch.zeros((s.n, 3), device="cuda")
+    time_steps(eng, dev, range(H + W), stream, flush, ud, up)
+    ms, its, _ = time_steps(eng, dev, range(H + W, H + W + K), stream, flush, ud, up)
+    eng.profile(True)
+    eng.profile_read(reset=True)
+    with torch.cuda.stream(stream):
+        for t in range(H + W + K, H + W + 2 * K):
+            eng.set_xyz_device(dev[t])
+            eng.mpole_init()
+            eng.induce(out=(ud, up))
+    prof = eng.profile_read(reset=True)
+    eng.profile(False)
+    kernels = {k: {"ms_total": v[0], "launches": v[1], "ms_per_launch": (v[0] / v[1] if v[1] else None)}
+               for k, v in prof.items() if v[1]}
+    ls = eng.list_stats()
+    out = {"workload": args.large_config, "atoms": s.n, "pme_grid": list(s.settings["nfft"]),
+           "induce_ms_per_step": float(np.mean(ms)), "pcg_iterations_per_step": float(np.mean(its)),
+           "kernels": kernels,
+           "rooflines": kernel_rooflines(kernels, s.n, ls["entries"], s.settings["nfft"][0], peak)}
+    eng.close()
+    if not args.no_learned and args.learn_train > 0:
+        out["learned_guess"] = learned_legs(args, s, abi, stream, tr, flush, check_oracle=False)
+    return out
+
+
 def time_steps(eng, dev_frames, idxs, stream, flush, ud, up):
     """CUDA-event time of induce() on the given device frames (L2 flushed
     before each step, outside the brackets); returns (ms list, iterations,
@@ -345,6 +397,7 @@ def main():
     eng.prepare(tr.frame(0))
     if args.own_fft:
         eng.pme_own_fft(True)
+    eng.pair_lanes(args.lanes)
     # frames: predictor history, warm-up, then the timed, e2e, per-kernel and
     # force passes, each continuing the trajectory (no time jumps for the predictor)
     f0 = args.history + args.warmup
@@ -465,6 +518,10 @@ def main():
     if not args.no_learned and args.learn_train > 0:
         learned = learned_legs(args, s, abi, stream, tr, flush, check_oracle=rank == 0 and not args.no_cpu_baseline)
 
+    large = None
+    if not args.no_large:
+        large = large_leg(args, abi, tg, stream, flush, peak)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline_sample(args, s, tr)
@@ -487,6 +544,7 @@ def main():
                 "workload": args.config, "atoms": s.n, "pme_grid": list(s.settings["nfft"]), "cutoff_A": 7.0,
                 "poleps_debye": s.settings["poleps"], "predictor": args.predictor, "history_frames": args.history,
                 "fft": "fused power-of-two transform (library)" if args.own_fft else "cuFFT C2C",
+                "lanes_per_atom": args.lanes,
                 "l2": "not flushed (profiling run)" if args.no_flush else "flushed (512 MB write) between timed steps",
                 "parallelism": f"replicas x{world}",
             },
@@ -501,12 +559,14 @@ def main():
                          "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
                          "algorithmic_bytes_per_launch": alg},
             "kernels": kernels,
+            "kernel_rooflines": kernel_rooflines(kernels, s.n, ls["entries"], nfft, peak),
             "lists": ls,
             "gpu_launches": int(round(launches_per_step * args.steps)),
             "clocks": ck,
             "cpu_baseline": cpu,
             "learned_guess": learned,
             "forces": forces,
+            "large_box": large,
         }
         print(json.dumps(line), flush=True)
     eng.close()

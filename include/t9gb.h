@@ -196,6 +196,11 @@ int t9gb_use_graph(t9gb_context* ctx, int enable);
  * unsupported grid returns T9GB_BAD_ARG. */
 int t9gb_pme_own_fft(t9gb_context* ctx, int enable);
 
+/* Lanes of a warp that share one atom's neighbour row in the real-space
+ * field and preconditioner kernels: 8 (default), 16 or 32.  A tuning knob;
+ * results are identical up to the order of the per-lane partial sums. */
+int t9gb_pair_lanes(t9gb_context* ctx, int lanes);
+
 /* Neighbour-list sizes: row capacity, entries of the current list (both
  * directions) and scaled pairs (the reference's Spatial::nakpl/niak,
  * include/ff/spatial.h:15-140). */

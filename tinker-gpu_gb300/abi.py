@@ -28,6 +28,7 @@ EXPORTS = [
     "t9gb_ufield_noalloc", "t9gb_learn_config", "t9gb_learn_policy", "t9gb_learn_reset", "t9gb_learn_stats", "t9gb_learn_get_weights",
     "t9gb_learn_set_weights", "t9gb_learn_eval", "t9gb_learn_adamw", "t9gb_learn_features",
     "t9gb_empole", "t9gb_epolar", "t9gb_emplar", "t9gb_energy_components", "t9gb_pme_own_fft",
+    "t9gb_pair_lanes",
 ]
 CALC_ENERGY, CALC_GRAD, CALC_VIRIAL = 0x010, 0x020, 0x040
 
@@ -120,6 +121,7 @@ def load(path=None):
     lib.t9gb_learn_features.argtypes = [vp, fp]
     lib.t9gb_energy_components.argtypes = [vp, dp]
     lib.t9gb_pme_own_fft.argtypes = [vp, C.c_int]
+    lib.t9gb_pair_lanes.argtypes = [vp, C.c_int]
     for name in ("t9gb_empole", "t9gb_epolar", "t9gb_emplar"):
         getattr(lib, name).argtypes = [vp, C.c_int, dp, fp, dp]
     _lib = lib
@@ -307,6 +309,9 @@ class Engine:
     def pme_own_fft(self, enable=True):
         """Fused power-of-two FFT (default where supported) or cuFFT."""
         self._check(self.lib.t9gb_pme_own_fft(self.h, 1 if enable else 0))
+
+    def pair_lanes(self, lanes=16):
+        self._check(self.lib.t9gb_pair_lanes(self.h, int(lanes)))
 
     def use_graph(self, enable=True):
         self._check(self.lib.t9gb_use_graph(self.h, 1 if enable else 0))

@@ -452,6 +452,16 @@ int t9gb_learn_config(t9gb_context* h, int mode, double lr, double weight_decay)
    return T9GB_OK;
 }
 
+int t9gb_pair_lanes(t9gb_context* h, int lanes)
+{
+   if (!h || (lanes != 8 && lanes != 16 && lanes != 32))
+      return T9GB_BAD_ARG;
+   if (lanes != h->c.pair_lanes)
+      drop_graphs(&h->c);
+   h->c.pair_lanes = lanes;
+   return T9GB_OK;
+}
+
 int t9gb_pme_own_fft(t9gb_context* h, int enable)
 {
    if (!h)

@@ -156,6 +156,7 @@ struct Context {
    int* nnbr = nullptr;      // [npad]
    int* nbr_over = nullptr;  // device max count seen (overflow check)
    int* h_over = nullptr;    // pinned mirror
+   int pair_lanes = 8;            // lanes per atom in the field kernels
    bool list_stale = true;        // positions changed since the last list check
    bool list_need_build = true;   // no valid list for the current order / capacity
    float4* sref = nullptr;        // [npad] positions at the last list build

@@ -495,12 +495,25 @@ __global__ void __launch_bounds__(256) k_empole_real(PairParams P, int npad, flo
 
 static constexpr int PAIR_THREADS = 256;
 
+// lanes per atom of the three field kernels (8, 16 or 32; t9gb_pair_lanes)
+#define T9_LANES_DISPATCH(KERNEL, ...)                                                                                 \
+   do {                                                                                                                \
+      const int g_ = ctx->pair_lanes;                                                                                  \
+      const int nb_ = grid_for((long long)ctx->npad * g_, PAIR_THREADS);                                               \
+      if (g_ == 8)                                                                                                     \
+         KERNEL<8><<<nb_, PAIR_THREADS, 0, ctx->stream>>>(__VA_ARGS__);                                                \
+      else if (g_ == 32)                                                                                               \
+         KERNEL<32><<<nb_, PAIR_THREADS, 0, ctx->stream>>>(__VA_ARGS__);                                               \
+      else                                                                                                             \
+         KERNEL<16><<<nb_, PAIR_THREADS, 0, ctx->stream>>>(__VA_ARGS__);                                               \
+   } while (0)
+
 int launch_ufield_real(Context* ctx, const float* u6, const float* base6, float* out6)
 {
    PairParams P = make_params(ctx, ctx->cfg.cutoff);
    prof_begin(ctx, P_UFIELD_REAL);
-   k_ufield_real<GROUP><<<grid_for((long long)ctx->npad * GROUP, PAIR_THREADS), PAIR_THREADS, 0, ctx->stream>>>(P,
-      ctx->npad, ctx->nbr, ctx->nnbr, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos, u6, base6, out6);
+   T9_LANES_DISPATCH(k_ufield_real, P, ctx->npad, ctx->nbr, ctx->nnbr, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos,
+      u6, base6, out6);
    prof_end(ctx);
    T9_CUDA(cudaGetLastError());
    return T9GB_OK;
@@ -510,8 +523,8 @@ int launch_dfield_real(Context* ctx, const float* base6, float* out6)
 {
    PairParams P = make_params(ctx, ctx->cfg.cutoff);
    prof_begin(ctx, P_DFIELD_REAL);
-   k_dfield_real<GROUP><<<grid_for((long long)ctx->npad * GROUP, PAIR_THREADS), PAIR_THREADS, 0, ctx->stream>>>(P,
-      ctx->npad, ctx->nbr, ctx->nnbr, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos, ctx->srpole, base6, out6);
+   T9_LANES_DISPATCH(k_dfield_real, P, ctx->npad, ctx->nbr, ctx->nnbr, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos,
+      ctx->srpole, base6, out6);
    prof_end(ctx);
    T9_CUDA(cudaGetLastError());
    return T9GB_OK;
@@ -522,8 +535,8 @@ int launch_precond_sparse(Context* ctx, const float* r6, float* z6)
    PairParams P = make_params(ctx, ctx->cfg.usolve_cutoff + ctx->cfg.pbuffer);
    P.ewald = 0;
    prof_begin(ctx, P_PRECOND);
-   k_precond_sparse<GROUP><<<grid_for((long long)ctx->npad * GROUP, PAIR_THREADS), PAIR_THREADS, 0, ctx->stream>>>(P,
-      ctx->npad, (float)ctx->cfg.udiag, ctx->nbr, ctx->nnbr, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos, r6, z6);
+   T9_LANES_DISPATCH(k_precond_sparse, P, ctx->npad, (float)ctx->cfg.udiag, ctx->nbr, ctx->nnbr, ctx->sp_start,
+      ctx->sp_j, ctx->sp_sc, ctx->spos, r6, z6);
    prof_end(ctx);
    T9_CUDA(cudaGetLastError());
    return T9GB_OK;
