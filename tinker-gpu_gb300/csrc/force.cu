@@ -205,11 +205,13 @@ __device__ __forceinline__ void radial(const PairParams& P, float r, float* bn, 
    }
 }
 
+// per-lane partial sums over the lane's few pairs (FP32); the lanes of an
+// atom are combined in FP64
 struct PairOut {
-   double e;      // empole pair energy (i side, halved later)
-   double f[3];   // force on i
-   double t[10];  // torque field at i
-   double w[9];   // virial dE/d(strain)_ab, i side of the pair (halved)
+   float e;      // empole pair energy (i side, halved later)
+   float f[3];   // force on i
+   float t[10];  // torque field at i
+   float w[9];   // virial dE/d(strain)_ab, i side of the pair (halved)
 };
 
 // one pair seen from i: R = x_i - x_k, scales sc = (m, d, p, u)
@@ -409,13 +411,18 @@ __global__ void __launch_bounds__(128) k_elec_real(PairParams P, int npad, float
    for (int c = 0; c < 10; ++c)
       acc[4 + c] = o.t[c];
    group_reduce_d<G, 14>(acc);
-   if (VIR)
-      group_reduce_d<G, 9>(o.w);
+   double wv[9];
+   if (VIR) {
+#pragma unroll
+      for (int c = 0; c < 9; ++c)
+         wv[c] = o.w[c];
+      group_reduce_d<G, 9>(wv);
+   }
    if (g == 0) {
       if (VIR)
 #pragma unroll
          for (int c = 0; c < 9; ++c)
-            wout[c * npad + i] = (float)(f * o.w[c]);
+            wout[c * npad + i] = (float)(f * wv[c]);
       if (MPOLE && e_atom)
          e_atom[i] = 0.5 * f * acc[0];
 #pragma unroll

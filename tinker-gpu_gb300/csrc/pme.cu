@@ -587,26 +587,27 @@ __global__ void k_conv_virial(int n1, int n2, int n3, float L1, float L2, float 
       const int r3 = (k3 < (n3 + 1) / 2) ? k3 : k3 - n3;
       const float h[3] = {r1 / L1, r2 / L2, r3 / L3};
       const float hsq = h[0] * h[0] + h[1] * h[1] + h[2] * h[2];
-      double w;
+      // per-point terms in FP32, sums in FP64
+      float w;
       if (MODE == 1) {
-         w = (double)wE * ((double)F.x * F.x + (double)F.y * F.y);
+         w = wE * (F.x * F.x + F.y * F.y);
       } else {
          const int m1 = k1 == 0 ? 0 : n1 - k1, m2 = k2 == 0 ? 0 : n2 - k2, m3 = k3 == 0 ? 0 : n3 - k3;
          const float2 Fm = g[((size_t)m3 * n2 + m2) * n1 + m1];
          // Q_d = (F + conj(Fm)) / 2, Q_p = (F - conj(Fm)) / (2i)
-         const double dx = 0.5 * ((double)F.x + Fm.x), dy = 0.5 * ((double)F.y - Fm.y);
-         const double px = 0.5 * ((double)F.y + Fm.y), py = -0.5 * ((double)F.x - Fm.x);
-         const double ux = dx + px, uy = dy + py;
-         w = (double)wP * (((double)QM.x * ux + (double)QM.y * uy) + (dx * px + dy * py));
+         const float dx = 0.5f * (F.x + Fm.x), dy = 0.5f * (F.y - Fm.y);
+         const float px = 0.5f * (F.y + Fm.y), py = -0.5f * (F.x - Fm.x);
+         const float ux = dx + px, uy = dy + py;
+         w = wP * ((QM.x * ux + QM.y * uy) + (dx * px + dy * py));
       }
       w *= infl[i];
-      const double vf = 2.0 * (1.0 + (double)pterm * hsq) / hsq;
-      v[0] += w * (vf * h[0] * h[0] - 1.0);
-      v[1] += w * (vf * h[1] * h[1] - 1.0);
-      v[2] += w * (vf * h[2] * h[2] - 1.0);
-      v[3] += w * vf * h[0] * h[1];
-      v[4] += w * vf * h[0] * h[2];
-      v[5] += w * vf * h[1] * h[2];
+      const float wf = w * (2.f * (1.f + pterm * hsq) / hsq);
+      v[0] += (double)(wf * h[0] * h[0] - w);
+      v[1] += (double)(wf * h[1] * h[1] - w);
+      v[2] += (double)(wf * h[2] * h[2] - w);
+      v[3] += (double)(wf * h[0] * h[1]);
+      v[4] += (double)(wf * h[0] * h[2]);
+      v[5] += (double)(wf * h[1] * h[2]);
    }
    for (int c = 0; c < 6; ++c)
       store_partial(red, c, v[c], sh);
@@ -649,6 +650,22 @@ __device__ __forceinline__ void row_sums20(const float2* __restrict__ g, const G
       for (int l = 0; l < 4; ++l)
          t[l] += q * t1[ix][l];
    }
+}
+
+// row idx of a [5][L] weight table without dynamic indexing (keeps the
+// table in registers)
+template <int L>
+__device__ __forceinline__ void pick_row(const float (*t)[L], int idx, float* out)
+{
+#pragma unroll
+   for (int l = 0; l < L; ++l)
+      out[l] = t[0][l];
+#pragma unroll
+   for (int j = 1; j < 5; ++j)
+      if (idx == j)
+#pragma unroll
+         for (int l = 0; l < L; ++l)
+            out[l] = t[j][l];
 }
 
 __device__ __forceinline__ void fphi20(const float* t, const float* u, const float* v, float* phi)
@@ -730,10 +747,13 @@ __device__ __forceinline__ int ix3(int a, int b, int c)
 __device__ __forceinline__ void mpole_force(const float* m, const float* c, float* F)
 {
    const float Q[3][3] = {{m[4], m[7], m[8]}, {m[7], m[5], m[9]}, {m[8], m[9], m[6]}};
+#pragma unroll
    for (int a = 0; a < 3; ++a) {
       float v = m[0] * c[1 + a];
+#pragma unroll
       for (int b = 0; b < 3; ++b) {
          v += m[1 + b] * c[ix2(a, b)];
+#pragma unroll
          for (int cc = 0; cc < 3; ++cc)
             v += Q[b][cc] * c[ix3(a, b, cc)];
       }
@@ -774,9 +794,11 @@ __global__ void __launch_bounds__(256) k_gather_force_perm(int n, int npad, Grid
       int yb = i2 + jy;
       yb -= (yb >= G.n2 ? G.n2 : 0);
       const size_t row = ((size_t)zb * G.n2 + yb) * G.n1;
-      float t[4];
+      float t[4], uy[4], vz[4];
+      pick_row<4>(t2, jy, uy);
+      pick_row<4>(t3, kz, vz);
       row_sums20(g, G, i1, row, t1, false, t);
-      fphi20(t, t2[jy], t3[kz], phi);
+      fphi20(t, uy, vz, phi);
    }
 #pragma unroll
    for (int c = 0; c < 20; ++c)
@@ -793,8 +815,10 @@ __global__ void __launch_bounds__(256) k_gather_force_perm(int n, int npad, Grid
       T[c] = 0.f;
    if (MPOLE) {
       mpole_force(m, phi, F);
+      #pragma unroll
       for (int c = 0; c < 3; ++c)
          F[c] *= f;
+      #pragma unroll
       for (int c = 0; c < 10; ++c)
          T[c] = f * phi[c];
       double e = (double)m[0] * phi[0] + (double)m[1] * phi[1] + (double)m[2] * phi[2] + (double)m[3] * phi[3];
@@ -818,26 +842,33 @@ __global__ void __launch_bounds__(256) k_gather_force_perm(int n, int npad, Grid
       us[0] = u[0] + u[3];
       us[1] = u[1] + u[4];
       us[2] = u[2] + u[5];
+#pragma unroll
       for (int a = 0; a < 3; ++a) {
          float v = 0.f;
+#pragma unroll
          for (int b = 0; b < 3; ++b)
             v += us[b] * phi[ix2(a, b)];
          F[a] -= 0.5f * f * v;
          T[1 + a] -= 0.5f * f * G.selfterm * us[a];
       }
    }
+   #pragma unroll
    for (int c = 0; c < 3; ++c)
       fout[3 * s + c] = F[c];
+   #pragma unroll
    for (int c = 0; c < 10; ++c)
       tout[10 * s + c] = T[c];
    if (wout) {
       // -f [phi_a d_b + 2 (phi2 Theta)_ab] (MPOLE), -f/2 phi_a u_b (POLAR)
       const float Q[3][3] = {{m[4], m[7], m[8]}, {m[7], m[5], m[9]}, {m[8], m[9], m[6]}};
+#pragma unroll
       for (int a = 0; a < 3; ++a)
+#pragma unroll
          for (int b = 0; b < 3; ++b) {
             float w = 0.f;
             if (MPOLE) {
                float pq = 0.f;
+#pragma unroll
                for (int c = 0; c < 3; ++c)
                   pq += phi[ix2(a, c)] * Q[c][b];
                w -= f * (phi[1 + a] * m[1 + b] + 2.f * pq);
@@ -877,11 +908,13 @@ __global__ void __launch_bounds__(256) k_gather_force_uind(int n, int npad, Grid
       int yb = i2 + jy;
       yb -= (yb >= G.n2 ? G.n2 : 0);
       const size_t row = ((size_t)zb * G.n2 + yb) * G.n1;
-      float t[4];
+      float t[4], uy[4], vz[4];
+      pick_row<4>(t2, jy, uy);
+      pick_row<4>(t3, kz, vz);
       row_sums20(g, G, i1, row, t1, false, t);
-      fphi20(t, t2[jy], t3[kz], pd);
+      fphi20(t, uy, vz, pd);
       row_sums20(g, G, i1, row, t1, true, t);
-      fphi20(t, t2[jy], t3[kz], pp);
+      fphi20(t, uy, vz, pp);
    }
 #pragma unroll
    for (int c = 0; c < 20; ++c)
@@ -895,26 +928,33 @@ __global__ void __launch_bounds__(256) k_gather_force_uind(int n, int npad, Grid
    to_cart20(G, pd);
    to_cart20(G, pp);
    float ps[20];
+   #pragma unroll
    for (int c = 0; c < 20; ++c)
       ps[c] = pd[c] + pp[c];
    const float* m = rp + 12 * s;
    const float* u = u8 + 8 * s;
    float F[3];
    mpole_force(m, ps, F);
+#pragma unroll
    for (int a = 0; a < 3; ++a) {
       float v = 0.f;
+#pragma unroll
       for (int b = 0; b < 3; ++b)
          v += u[b] * pp[ix2(a, b)] + u[3 + b] * pd[ix2(a, b)];
       fout[3 * s + a] = 0.5f * f * (F[a] - v);
    }
+   #pragma unroll
    for (int c = 0; c < 10; ++c)
       tout[10 * s + c] = 0.5f * f * ps[c];
    if (wout) {
       // -f/2 [psi_a d_b + 2 (psi2 Theta)_ab + psi^p_a u_d,b + psi^d_a u_p,b]
       const float Q[3][3] = {{m[4], m[7], m[8]}, {m[7], m[5], m[9]}, {m[8], m[9], m[6]}};
+#pragma unroll
       for (int a = 0; a < 3; ++a)
+#pragma unroll
          for (int b = 0; b < 3; ++b) {
             float pq = 0.f;
+#pragma unroll
             for (int c = 0; c < 3; ++c)
                pq += ps[ix2(a, c)] * Q[c][b];
             const float w = ps[1 + a] * m[1 + b] + 2.f * pq + pp[1 + a] * u[b] + pd[1 + a] * u[3 + b];
