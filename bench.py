@@ -375,6 +375,9 @@ def main():
 
             dist.init_process_group("gloo")
         run_reference(args, world, rank)
+        if world > 1:
+            dist.barrier()
+            dist.destroy_process_group()
         return
 
     import torch
