@@ -32,6 +32,10 @@ static int alloc_all(Context* ctx)
    T9_CUDA(cudaMemset(ctx->srpole, 0, sizeof(float) * 12 * npad));
    T9_CUDA(cudaMalloc(&ctx->nnbr, sizeof(int) * npad));
    T9_CUDA(cudaMemset(ctx->nnbr, 0, sizeof(int) * npad));
+   T9_CUDA(cudaMalloc(&ctx->nnbrc, sizeof(int) * npad));
+   T9_CUDA(cudaMemset(ctx->nnbrc, 0, sizeof(int) * npad));
+   T9_CUDA(cudaMalloc(&ctx->nnbrp, sizeof(int) * npad));
+   T9_CUDA(cudaMemset(ctx->nnbrp, 0, sizeof(int) * npad));
    T9_CUDA(cudaMalloc(&ctx->nbr_over, sizeof(int)));
    T9_CUDA(cudaMemset(ctx->nbr_over, 0, sizeof(int)));
    T9_CUDA(cudaMallocHost(&ctx->h_over, sizeof(int)));
@@ -74,7 +78,7 @@ static int alloc_all(Context* ctx)
 static void free_all(Context* ctx)
 {
    void* dev[] = {ctx->frames, ctx->pole, ctx->xyz, ctx->perm, ctx->iperm, ctx->spos, ctx->spolar, ctx->spolinv,
-      ctx->sdamp, ctx->srpole, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->nbr, ctx->nnbr, ctx->nbr_over,
+      ctx->sdamp, ctx->srpole, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->nbr, ctx->nnbr, ctx->nbr_over, ctx->nbrc, ctx->nnbrc, ctx->nbrp, ctx->nnbrp,
       ctx->cell_count, ctx->cell_start, ctx->cell_atoms, ctx->atom_cell, ctx->rcp6, ctx->fld6, ctx->udir,
       ctx->efield, ctx->uind, ctx->rsd, ctx->zrsd, ctx->conj, ctx->vec, ctx->tmp6, ctx->e_atom, ctx->sframe, ctx->hout,
       ctx->red, ctx->scal, ctx->status, ctx->sref, ctx->lflag,

@@ -154,6 +154,12 @@ struct Context {
    int nbr_cap = 0;
    int* nbr = nullptr;       // [npad][nbr_cap]
    int* nnbr = nullptr;      // [npad]
+   // per-step sub-lists of nbr (same order): pairs within the cutoff and
+   // within the preconditioner cutoff
+   int* nbrc = nullptr;
+   int* nnbrc = nullptr;
+   int* nbrp = nullptr;
+   int* nnbrp = nullptr;
    int* nbr_over = nullptr;  // device max count seen (overflow check)
    int* h_over = nullptr;    // pinned mirror
    int pair_lanes = 8;            // lanes per atom in the field kernels
@@ -293,7 +299,9 @@ inline void prof_collect(Context* ctx)
 int order_build(Context* ctx);  // host: spatial order, scaled partners
 int list_update(Context* ctx);  // device: exact neighbour list
 int ensure_list(Context* ctx);  // list_update when the coordinates changed
-int check_list_overflow(Context* ctx, int* redo);  // after a sync; redo = 1: grown, repeat
+int check_list_overflow(Context* ctx, int* redo);
+int alloc_lists(Context* ctx, int cap);          // nbr, nbrc, nbrp with row capacity cap
+int launch_list_filter(Context* ctx);             // pair.cu  // after a sync; redo = 1: grown, repeat
 int scatter_positions(Context* ctx);
 int rotpole_sorted(Context* ctx);
 int reset_predictor(Context* ctx);

@@ -680,7 +680,7 @@ int frame_map_build(Context* ctx)
 template <bool MPOLE, bool POLAR, bool VIR>
 static void launch_real(Context* ctx, const PairParams& P, float f, int grid)
 {
-   k_elec_real<GROUP, MPOLE, POLAR, VIR><<<grid, 128, 0, ctx->stream>>>(P, ctx->npad, f, ctx->nbr, ctx->nnbr,
+   k_elec_real<GROUP, MPOLE, POLAR, VIR><<<grid, 128, 0, ctx->stream>>>(P, ctx->npad, f, ctx->nbrc, ctx->nnbrc,
       ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos, ctx->srpole, ctx->uind, ctx->freal, ctx->treal,
       MPOLE ? ctx->e_atom : nullptr, ctx->wvir);
 }

@@ -104,7 +104,7 @@ __global__ void k_resid_cmp(int ne, const float* __restrict__ polar, const float
    const float* __restrict__ udir, const float* __restrict__ uL, const float* __restrict__ fldL,
    const float* __restrict__ rsd, double* __restrict__ red, double* __restrict__ scal, int* __restrict__ state)
 {
-   __shared__ double sh[40];
+   __shared__ double sh[64];
    double pd = 0, pp = 0, ld = 0, lp = 0;
    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += gridDim.x * blockDim.x) {
       const int s = e / 6, x = e + 2 * s;
@@ -120,10 +120,8 @@ __global__ void k_resid_cmp(int ne, const float* __restrict__ polar, const float
          lp += (double)r1 * r1;
       }
    }
-   store_partial(red, 0, pd, sh);
-   store_partial(red, 1, pp, sh);
-   store_partial(red, 2, ld, sh);
-   store_partial(red, 3, lp, sh);
+   const double pv[4] = {pd, pp, ld, lp};
+   store_partials<4>(red, 0, pv, sh);
    if (!last_block(state + ST_TICKET0))
       return;
    double tot[4];

@@ -47,6 +47,18 @@ static double list_cutoff(const t9gb_config& c)
 
 // Host: Morton order of the current coordinates, per-slot parameters, the
 // scaled-partner table and the neighbour-list storage.
+// the list and its two per-step sub-lists, all with row capacity cap
+int alloc_lists(Context* ctx, int cap)
+{
+   for (int** p : {&ctx->nbr, &ctx->nbrc, &ctx->nbrp}) {
+      cudaFree(*p);
+      *p = nullptr;
+      T9_CUDA(cudaMalloc(p, sizeof(int) * (size_t)ctx->npad * cap));
+   }
+   ctx->nbr_cap = cap;
+   return T9GB_OK;
+}
+
 int order_build(Context* ctx)
 {
    const int n = ctx->n, npad = ctx->npad;
@@ -190,12 +202,8 @@ int order_build(Context* ctx)
       T9_CUDA(cudaMalloc(&ctx->cell_count, sizeof(int) * ctx->ncell));
       T9_CUDA(cudaMalloc(&ctx->cell_start, sizeof(int) * (ctx->ncell + 1)));
    }
-   if (cap != ctx->nbr_cap) {
-      cudaFree(ctx->nbr);
-      ctx->nbr = nullptr;
-      T9_CUDA(cudaMalloc(&ctx->nbr, sizeof(int) * (size_t)npad * cap));
-      ctx->nbr_cap = cap;
-   }
+   if (cap != ctx->nbr_cap)
+      T9_CHECK(alloc_lists(ctx, cap));
    // legacy-stream copies above finish before the stream's kernels
    T9_CUDA(cudaDeviceSynchronize());
    T9_CHECK(fill_row_padding(ctx));

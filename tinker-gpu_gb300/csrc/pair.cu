@@ -495,6 +495,65 @@ __global__ void __launch_bounds__(256) k_empole_real(PairParams P, int npad, flo
 
 static constexpr int PAIR_THREADS = 256;
 
+// ---------------------------------------------------------------------------
+// Per-step sub-lists: warp per atom, each row of the (reused, buffered) list
+// is filtered into the pairs within the cutoff and those within the
+// preconditioner cutoff, in the row's order (ballot compaction), so the field
+// and preconditioner kernels visit only pairs they use.  The kernels repeat
+// the same r^2 test with the same arithmetic.
+__global__ void __launch_bounds__(256) k_list_filter(PairParams P, float cutp2, int npad, const int* __restrict__ nbr,
+   const int* __restrict__ nnbr, const float4* __restrict__ spos, int* __restrict__ nbrc, int* __restrict__ nnbrc,
+   int* __restrict__ nbrp, int* __restrict__ nnbrp)
+{
+   const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+   const int lane = threadIdx.x & 31;
+   if (i >= npad)
+      return;
+   int oc = 0, op = 0;
+   if (i < P.n) {
+      const float4 pi = spos[i];
+      const int* row = nbr + (size_t)i * P.cap;
+      int* rc = nbrc + (size_t)i * P.cap;
+      int* rp = nbrp + (size_t)i * P.cap;
+      const int cnt = nnbr[i];
+      const unsigned lt = (1u << lane) - 1u;
+      for (int k0 = 0; k0 < cnt; k0 += 32) {
+         const int k = k0 + lane;
+         bool inc = false, inp = false;
+         int j = 0;
+         if (k < cnt) {
+            j = row[k];
+            const float3 d = sep(P, pi, spos[j]);
+            const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
+            inc = r2 <= P.cut2;
+            inp = r2 <= cutp2;
+         }
+         const unsigned mc = __ballot_sync(0xffffffffu, inc), mp = __ballot_sync(0xffffffffu, inp);
+         if (inc)
+            rc[oc + __popc(mc & lt)] = j;
+         if (inp)
+            rp[op + __popc(mp & lt)] = j;
+         oc += __popc(mc);
+         op += __popc(mp);
+      }
+   }
+   if (lane == 0) {
+      nnbrc[i] = oc;
+      nnbrp[i] = op;
+   }
+}
+
+int launch_list_filter(Context* ctx)
+{
+   PairParams P = make_params(ctx, ctx->cfg.cutoff);
+   const double cp = ctx->cfg.usolve_cutoff + ctx->cfg.pbuffer;
+   const float cutp2 = cp * cp > 3.0e38 ? 3.0e38f : (float)(cp * cp);
+   k_list_filter<<<grid_for((long long)ctx->npad * 32, 256), 256, 0, ctx->stream>>>(P, cutp2, ctx->npad, ctx->nbr,
+      ctx->nnbr, ctx->spos, ctx->nbrc, ctx->nnbrc, ctx->nbrp, ctx->nnbrp);
+   T9_CUDA(cudaGetLastError());
+   return T9GB_OK;
+}
+
 // lanes per atom of the three field kernels (8, 16 or 32; t9gb_pair_lanes)
 #define T9_LANES_DISPATCH(KERNEL, ...)                                                                                 \
    do {                                                                                                                \
@@ -512,7 +571,7 @@ int launch_ufield_real(Context* ctx, const float* u6, const float* base6, float*
 {
    PairParams P = make_params(ctx, ctx->cfg.cutoff);
    prof_begin(ctx, P_UFIELD_REAL);
-   T9_LANES_DISPATCH(k_ufield_real, P, ctx->npad, ctx->nbr, ctx->nnbr, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos,
+   T9_LANES_DISPATCH(k_ufield_real, P, ctx->npad, ctx->nbrc, ctx->nnbrc, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos,
       u6, base6, out6);
    prof_end(ctx);
    T9_CUDA(cudaGetLastError());
@@ -523,7 +582,7 @@ int launch_dfield_real(Context* ctx, const float* base6, float* out6)
 {
    PairParams P = make_params(ctx, ctx->cfg.cutoff);
    prof_begin(ctx, P_DFIELD_REAL);
-   T9_LANES_DISPATCH(k_dfield_real, P, ctx->npad, ctx->nbr, ctx->nnbr, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos,
+   T9_LANES_DISPATCH(k_dfield_real, P, ctx->npad, ctx->nbrc, ctx->nnbrc, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos,
       ctx->srpole, base6, out6);
    prof_end(ctx);
    T9_CUDA(cudaGetLastError());
@@ -535,7 +594,7 @@ int launch_precond_sparse(Context* ctx, const float* r6, float* z6)
    PairParams P = make_params(ctx, ctx->cfg.usolve_cutoff + ctx->cfg.pbuffer);
    P.ewald = 0;
    prof_begin(ctx, P_PRECOND);
-   T9_LANES_DISPATCH(k_precond_sparse, P, ctx->npad, (float)ctx->cfg.udiag, ctx->nbr, ctx->nnbr, ctx->sp_start,
+   T9_LANES_DISPATCH(k_precond_sparse, P, ctx->npad, (float)ctx->cfg.udiag, ctx->nbrp, ctx->nnbrp, ctx->sp_start,
       ctx->sp_j, ctx->sp_sc, ctx->spos, r6, z6);
    prof_end(ctx);
    T9_CUDA(cudaGetLastError());
@@ -549,7 +608,7 @@ int launch_empole_real(Context* ctx, double* e_atom)
 {
    PairParams P = make_params(ctx, ctx->cfg.cutoff);
    k_empole_real<GROUP><<<grid_for((long long)ctx->npad * GROUP, PAIR_THREADS), PAIR_THREADS, 0, ctx->stream>>>(P,
-      ctx->npad, (float)ctx->cfg.electric, ctx->nbr, ctx->nnbr, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos,
+      ctx->npad, (float)ctx->cfg.electric, ctx->nbrc, ctx->nnbrc, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos,
       ctx->srpole, e_atom);
    T9_CUDA(cudaGetLastError());
    return T9GB_OK;
@@ -727,7 +786,8 @@ int launch_learn_features(Context* ctx, const float* e8, const float* u8, float*
 {
    PairParams P = make_params(ctx, DESC_CUT);
    k_learn_features<GROUP><<<grid_for((long long)ctx->npad * GROUP, PAIR_THREADS), PAIR_THREADS, 0, ctx->stream>>>(P,
-      ctx->npad, ctx->nbr, ctx->nnbr, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos, ctx->srpole, ctx->sframe, e8,
+      ctx->npad, ctx->cfg.cutoff >= DESC_CUT ? ctx->nbrc : ctx->nbr, ctx->cfg.cutoff >= DESC_CUT ? ctx->nnbrc : ctx->nnbr,
+      ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos, ctx->srpole, ctx->sframe, e8,
       u8, xf);
    T9_CUDA(cudaGetLastError());
    return T9GB_OK;

@@ -97,7 +97,7 @@ __global__ void k_precond_dot(VecArgs A, const float* __restrict__ rsd, float* _
    float* __restrict__ conj, double* __restrict__ red, double* __restrict__ scal, int* __restrict__ state, int init,
    int n, double debye, double poleps, int politer, int miniter, cudaGraphConditionalHandle handle, int use_handle)
 {
-   __shared__ double sh[40];
+   __shared__ double sh[64];
    double rz_d = 0, rz_p = 0, rr_d = 0, rr_p = 0;
    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.ne; e += gridDim.x * blockDim.x) {
       const int s = e / 6, x = e + 2 * s;  // row s, component e - 6 s of [npad][8]
@@ -119,10 +119,8 @@ __global__ void k_precond_dot(VecArgs A, const float* __restrict__ rsd, float* _
          rr_p += (double)r * r;
       }
    }
-   store_partial(red, R_RZ_D, rz_d, sh);
-   store_partial(red, R_RZ_P, rz_p, sh);
-   store_partial(red, R_RR_D, rr_d, sh);
-   store_partial(red, R_RR_P, rr_p, sh);
+   const double pv[4] = {rz_d, rz_p, rr_d, rr_p};
+   store_partials<4>(red, R_RZ_D, pv, sh);
    if (!last_block(state + ST_TICKET0))
       return;
    double tot[4];
@@ -167,7 +165,7 @@ __global__ void k_precond_dot(VecArgs A, const float* __restrict__ rsd, float* _
 __global__ void k_pcg_p1(VecArgs A, const float* __restrict__ fld, const float* __restrict__ conj,
    float* __restrict__ vec, double* __restrict__ red, double* __restrict__ scal, int* __restrict__ state)
 {
-   __shared__ double sh[40];
+   __shared__ double sh[64];
    double dd = 0, dp = 0;
    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.ne; e += gridDim.x * blockDim.x) {
       const int s = e / 6, x = e + 2 * s;  // row s, component e - 6 s of [npad][8]
@@ -179,8 +177,8 @@ __global__ void k_pcg_p1(VecArgs A, const float* __restrict__ fld, const float* 
       else
          dp += (double)p * v;
    }
-   store_partial(red, R_PAP_D, dd, sh);
-   store_partial(red, R_PAP_P, dp, sh);
+   const double pv[2] = {dd, dp};
+   store_partials<2>(red, R_PAP_D, pv, sh);
    if (!last_block(state + ST_TICKET1))
       return;
    double tot[2];
@@ -330,6 +328,7 @@ int ensure_list(Context* ctx)
    T9_CUDA(cudaStreamSynchronize(ctx->stream));
    if (*ctx->h_lflag)
       T9_CHECK(list_build_body(ctx));
+   T9_CHECK(launch_list_filter(ctx));
    T9_CUDA(cudaMemcpyAsync(ctx->h_over, ctx->nbr_over, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
    ctx->list_stale = false;
    return T9GB_OK;
@@ -370,6 +369,7 @@ static int list_refresh_graph(Context* ctx)
    if (cudaStreamEndCapture(ctx->cap_stream, &tmp) != cudaSuccess && rc == T9GB_OK)
       rc = T9GB_CUDA_ERR;
    T9_CHECK(rc);
+   T9_CHECK(launch_list_filter(ctx));
    T9_CUDA(cudaMemcpyAsync(ctx->h_over, ctx->nbr_over, sizeof(int), cudaMemcpyDeviceToHost, s0));
    return T9GB_OK;
 }
@@ -382,10 +382,7 @@ int check_list_overflow(Context* ctx, int* redo)
    if (*ctx->h_over <= ctx->nbr_cap)
       return T9GB_OK;
    int cap = ((int)(*ctx->h_over * 1.25) + 31) / 32 * 32;
-   cudaFree(ctx->nbr);
-   ctx->nbr = nullptr;
-   T9_CUDA(cudaMalloc(&ctx->nbr, sizeof(int) * (size_t)ctx->npad * cap));
-   ctx->nbr_cap = cap;
+   T9_CHECK(alloc_lists(ctx, cap));
    *ctx->h_over = 0;
    T9_CUDA(cudaMemsetAsync(ctx->nbr_over, 0, sizeof(int), ctx->stream));
    ctx->list_need_build = true;

@@ -569,7 +569,7 @@ __global__ void k_conv_virial(int n1, int n2, int n3, float L1, float L2, float 
    const float* __restrict__ infl, const float2* __restrict__ g, float2* __restrict__ stash, float wE, float wP,
    double* __restrict__ red, double* __restrict__ out, int* __restrict__ state)
 {
-   __shared__ double sh[40];
+   __shared__ double sh[64];
    double v[6] = {0, 0, 0, 0, 0, 0};
    const size_t ng = (size_t)n1 * n2 * n3;
    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < ng; i += (size_t)gridDim.x * blockDim.x) {
@@ -609,8 +609,7 @@ __global__ void k_conv_virial(int n1, int n2, int n3, float L1, float L2, float 
       v[4] += (double)(wf * h[0] * h[2]);
       v[5] += (double)(wf * h[1] * h[2]);
    }
-   for (int c = 0; c < 6; ++c)
-      store_partial(red, c, v[c], sh);
+   store_partials<6>(red, 0, v, sh);
    if (!last_block(state + ST_TICKET0))
       return;
    double t[4];

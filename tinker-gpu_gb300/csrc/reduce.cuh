@@ -65,6 +65,42 @@ static __device__ __forceinline__ void store_partial(double* red, int slot, doub
       red[slot * RED_MAX + blockIdx.x] = v;
 }
 
+// store this block's partial sums of N values into slots first..first+N-1:
+// the same shuffle trees as block_sum for each value (identical results), with
+// the N values interleaved and one barrier pair instead of N (sh: >= 8 N
+// doubles; blockDim <= 256)
+template <int N>
+static __device__ __forceinline__ void store_partials(double* red, int first, const double* v, double* sh)
+{
+   double x[N];
+#pragma unroll
+   for (int c = 0; c < N; ++c)
+      x[c] = v[c];
+#pragma unroll
+   for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+      for (int c = 0; c < N; ++c)
+         x[c] += __shfl_down_sync(0xffffffffu, x[c], o);
+   const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+   if (l == 0)
+#pragma unroll
+      for (int c = 0; c < N; ++c)
+         sh[c * 8 + w] = x[c];
+   __syncthreads();
+   if (threadIdx.x < 32) {
+#pragma unroll
+      for (int c = 0; c < N; ++c) {
+         double r = threadIdx.x < nw ? sh[c * 8 + threadIdx.x] : 0.0;
+#pragma unroll
+         for (int o = 16; o > 0; o >>= 1)
+            r += __shfl_down_sync(0xffffffffu, r, o);
+         if (threadIdx.x == 0)
+            red[(first + c) * RED_MAX + blockIdx.x] = r;
+      }
+   }
+   __syncthreads();
+}
+
 // true in the block that finishes last (threadfence + ticket); it resets the
 // ticket for the next launch
 static __device__ __forceinline__ bool last_block(int* ticket)
