@@ -69,6 +69,8 @@ static int alloc_all(Context* ctx)
    }
    ctx->h_stage_bytes = sizeof(float) * 8 * (size_t)npad;
    T9_CUDA(cudaMallocHost(&ctx->h_stage, ctx->h_stage_bytes));
+   T9_CUDA(cudaMallocHost(&ctx->h_in, sizeof(float) * 3 * (size_t)npad));
+   T9_CUDA(cudaEventCreateWithFlags(&ctx->ev_in, cudaEventDisableTiming));
    // the legacy-stream memsets above must finish before work on the caller's
    // (possibly non-blocking) stream
    T9_CUDA(cudaDeviceSynchronize());
@@ -92,6 +94,10 @@ static void free_all(Context* ctx)
       cudaFreeHost(ctx->h_scal);
    if (ctx->h_stage)
       cudaFreeHost(ctx->h_stage);
+   if (ctx->h_in)
+      cudaFreeHost(ctx->h_in);
+   if (ctx->ev_in)
+      cudaEventDestroy(ctx->ev_in);
    if (ctx->h_over)
       cudaFreeHost(ctx->h_over);
    if (ctx->h_lflag)
@@ -248,19 +254,21 @@ int t9gb_set_xyz_host(t9gb_context* h, const double* xyz)
       return T9GB_BAD_ARG;
    Context* ctx = &h->c;
    const int n = ctx->n;
-   ctx->h_xyz.assign(xyz, xyz + 3 * n);
-   float* st = ctx->h_stage;
-   for (int i = 0; i < 3 * n; ++i) {
+   for (int i = 0; i < 3 * n; ++i)
       if (!std::isfinite(xyz[i]))
          return T9GB_BAD_ARG;
+   // the previous copy out of the staging buffer must have finished
+   if (ctx->ev_in_pending)
+      T9_CUDA(cudaEventSynchronize(ctx->ev_in));
+   float* st = ctx->h_in;
+   for (int i = 0; i < 3 * n; ++i)
       st[i] = (float)xyz[i];
-   }
    T9_CUDA(cudaMemcpyAsync(ctx->xyz, st, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
+   T9_CUDA(cudaEventRecord(ctx->ev_in, ctx->stream));
+   ctx->ev_in_pending = true;
    ctx->have_xyz = true;
    if (ctx->have_order)
       T9_CHECK(scatter_positions(ctx));
-   // the staging buffer is reused by the next call: finish the copy
-   T9_CUDA(cudaStreamSynchronize(ctx->stream));
    return T9GB_OK;
 }
 
@@ -270,13 +278,6 @@ int t9gb_set_xyz_device(t9gb_context* h, const float* xyz_device)
       return T9GB_BAD_ARG;
    Context* ctx = &h->c;
    T9_CUDA(cudaMemcpyAsync(ctx->xyz, xyz_device, sizeof(float) * 3 * ctx->n, cudaMemcpyDeviceToDevice, ctx->stream));
-   if (!ctx->have_xyz || ctx->h_xyz.empty()) {
-      // the host list builder needs a host copy of the first coordinates
-      std::vector<float> tmp(3 * (size_t)ctx->n);
-      T9_CUDA(cudaMemcpyAsync(tmp.data(), xyz_device, sizeof(float) * 3 * ctx->n, cudaMemcpyDeviceToHost, ctx->stream));
-      T9_CUDA(cudaStreamSynchronize(ctx->stream));
-      ctx->h_xyz.assign(tmp.begin(), tmp.end());
-   }
    ctx->have_xyz = true;
    if (ctx->have_order)
       T9_CHECK(scatter_positions(ctx));
@@ -290,13 +291,13 @@ int t9gb_nblist_build(t9gb_context* h)
    Context* ctx = &h->c;
    if (!ctx->have_topology || !ctx->have_xyz)
       return T9GB_NOT_READY;
-   if (ctx->h_xyz.empty() || (int)ctx->h_xyz.size() != 3 * ctx->n) {
+   {
+      // the ordering uses the current device coordinates
       std::vector<float> tmp(3 * (size_t)ctx->n);
       T9_CUDA(cudaMemcpyAsync(tmp.data(), ctx->xyz, sizeof(float) * 3 * ctx->n, cudaMemcpyDeviceToHost, ctx->stream));
       T9_CUDA(cudaStreamSynchronize(ctx->stream));
       ctx->h_xyz.assign(tmp.begin(), tmp.end());
    }
-   T9_CUDA(cudaStreamSynchronize(ctx->stream));
    T9_CHECK(order_build(ctx));
    T9_CHECK(scatter_positions(ctx));
    return T9GB_OK;

@@ -127,7 +127,10 @@ struct Context {
 
    // coordinates, caller order
    float* xyz = nullptr;       // [n][3]
-   std::vector<double> h_xyz;  // copy for the host-side ordering
+   std::vector<double> h_xyz;  // host copy for the ordering, refreshed by t9gb_nblist_build
+   float* h_in = nullptr;      // pinned staging of host coordinates
+   cudaEvent_t ev_in = nullptr; // its last copy to the device
+   bool ev_in_pending = false;
    bool have_xyz = false;
    bool have_topology = false;
    bool have_order = false;
