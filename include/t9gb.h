@@ -82,6 +82,18 @@ int t9gb_set_stream(t9gb_context* ctx, void* stream);
 int t9gb_set_topology(t9gb_context* ctx, const int* frames, const double* pole, const double* polarity,
    const double* thole, const double* pdamp, int nexcl, const int* excl_ik, const double* excl_scale);
 
+/* Per-type-pair Thole coefficients.  ptype[n] in 0..ntypes-1 is each atom's
+ * polarization type and thlval[ntypes][ntypes] (symmetric, finite, >= 0) the
+ * coefficient of a pair of types, as the reference's CUDA pair kernels read
+ * thlval[njpolar * jpolar[i] + jpolar[k]] (src/cu/amoeba/ufield_cu1.cc,
+ * dfield_cu1.cc, sparsePrecond_cu1.cc, epolar_cu1.cc).  Replaces the jpolar /
+ * thlval INIT of epolarData (src/amoeba/epolar.cpp:393-398, 486-491); Tinker
+ * fills the table from the thole values and its POLPAIR keywords.
+ * ntypes = 0 returns to min(thole_i, thole_k) (damp_thole2/3,
+ * include/seq/damp.h:19-44).  Like t9gb_set_topology, call before
+ * t9gb_nblist_build; ntypes <= 256. */
+int t9gb_set_thole_pairs(t9gb_context* ctx, int ntypes, const int* ptype, const double* thlval);
+
 /* Coordinates [n][3].  Replace copyPosToXyz (src/atom.cpp:161-166). */
 int t9gb_set_xyz_host(t9gb_context* ctx, const double* xyz);
 int t9gb_set_xyz_device(t9gb_context* ctx, const float* xyz_device);

@@ -48,6 +48,9 @@ class OrSystem(C.Structure):
         ("bsorder", C.c_int),
         ("cutoff", C.c_double),
         ("electric", C.c_double),
+        ("nthl", C.c_int),
+        ("ptype", C.POINTER(C.c_int)),
+        ("thl", C.POINTER(C.c_double)),
     ]
 
 
@@ -164,6 +167,11 @@ class OracleSystem:
         s.cutoff = float(st.get("ewald_cutoff", 1.0e9) if cutoff is None else cutoff)
         from_units = __import__("importlib").import_module("tinker-gpu_gb300.units")
         s.electric = from_units.ELECTRIC
+        if getattr(system, "ptype", None) is not None:
+            self.ptype = np.ascontiguousarray(system.ptype, dtype=np.int32)
+            self.thl = np.ascontiguousarray(system.thole_table, dtype=np.float64)
+            s.nthl = int(self.thl.shape[0])
+            s.ptype, s.thl = _ip(self.ptype), _dp(self.thl)
         self.s = s
         self.n = system.n
         self.settings = st

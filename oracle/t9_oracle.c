@@ -65,6 +65,9 @@ typedef struct {
    int bsorder;
    double cutoff;           /* real-space cutoff (Ewald) or multipole cutoff */
    double electric;
+   int nthl;                /* > 0: per-type-pair Thole table (jpolar / thlval) */
+   const int* ptype;        /* [n] polarization type, 0..nthl-1 */
+   const double* thl;       /* [nthl][nthl] */
 } or_system;
 
 typedef struct {
@@ -268,6 +271,17 @@ static inline void or_excl_get(const or_system* s, const or_excl* e, int i, int 
 
 /* ------------------------------------------------------------------ */
 /* damping (include/seq/damp.h)                                        */
+
+/* Thole coefficient of pair (i, k): thlval[jpolar_i][jpolar_k] when a table
+ * is set (src/cu/amoeba/ufield_cu1.cc, dfield_cu1.cc, sparsePrecond_cu1.cc,
+ * epolar_cu1.cc), else min(thole_i, thole_k) (damp_thole2/3, damp.h:19-44).
+ * Passed as both pti and ptk to the pair routines below. */
+static inline double or_pair_gamma(const or_system* s, int i, int k)
+{
+   if (s->nthl > 0)
+      return s->thl[s->ptype[i] * s->nthl + s->ptype[k]];
+   return fmin(s->thole[i], s->thole[k]);
+}
 
 static inline void or_thole3(double r, double pdi, double pti, double pdk, double ptk, double* s3, double* s5,
    double* s7)
@@ -1068,9 +1082,9 @@ void or_dfield(const or_system* s, double* field, double* fieldp)
       double r2 = xr * xr + yr * yr + zr * zr;
       double sc[4];
       or_excl_get(s, &ex, i, k, sc);
+      const double pga = or_pair_gamma(s, i, k);
       or_pair_dfield(s->use_ewald, s->aewald, r2, xr, yr, zr, sc[1], sc[2], &s->rpole[10 * i], s->pdamp[i],
-         s->thole[i], &s->rpole[10 * k], s->pdamp[k], s->thole[k], &fd[3 * i], &fp[3 * i], &fd[3 * k],
-         &fp[3 * k]);
+         pga, &s->rpole[10 * k], s->pdamp[k], pga, &fd[3 * i], &fp[3 * i], &fd[3 * k], &fp[3 * k]);
    }
    or_acc_reduce(&acc, n, field, fieldp);
    or_excl_free(&ex);
@@ -1158,9 +1172,9 @@ static void or_ufield_c(const or_system* s, or_ucache* c, const double* uind, co
       double r2 = xr * xr + yr * yr + zr * zr;
       double sc[4];
       or_excl_get(s, &c->ex, i, k, sc);
+      const double pga = or_pair_gamma(s, i, k);
       or_pair_ufield(s->use_ewald, s->aewald, r2, xr, yr, zr, sc[3], &uind[3 * i], &uinp[3 * i], s->pdamp[i],
-         s->thole[i], &uind[3 * k], &uinp[3 * k], s->pdamp[k], s->thole[k], &fd[3 * i], &fp[3 * i], &fd[3 * k],
-         &fp[3 * k]);
+         pga, &uind[3 * k], &uinp[3 * k], s->pdamp[k], pga, &fd[3 * i], &fp[3 * i], &fd[3 * k], &fp[3 * k]);
    }
    or_acc_reduce(&acc, n, field, fieldp);
 }
@@ -1201,7 +1215,8 @@ static void or_sparse_precond(const or_system* s, const or_pairs* pl, const or_e
       double sc[4];
       or_excl_get(s, ex, i, k, sc);
       double s3, s5;
-      or_thole3(r, s->pdamp[i], s->thole[i], s->pdamp[k], s->thole[k], &s3, &s5, NULL);
+      const double pga = or_pair_gamma(s, i, k);
+      or_thole3(r, s->pdamp[i], pga, s->pdamp[k], pga, &s3, &s5, NULL);
       s3 *= sc[3];
       s5 *= sc[3];
       double polik = s->polarity[i] * s->polarity[k];

@@ -1,0 +1,35 @@
+"""Two-ion known answers (Tinker9 test/nacl.cpp NaCl-2, NaCl-3) from the
+committed fixture tests/golden/nacl.json."""
+import importlib
+import json
+import os
+
+tg = importlib.import_module("tinker-gpu_gb300")
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def load():
+    with open(os.path.join(HERE, "golden", "nacl.json")) as f:
+        return json.load(f)
+
+
+def system(name, fx=None):
+    c = (load() if fx is None else fx)[name]
+    atoms = c["atoms"]
+    xyz = [a["xyz"] for a in atoms]
+    types = [a["type"] for a in atoms]
+    bonds = sorted({(min(a["index"], b) - 1, max(a["index"], b) - 1) for a in atoms for b in a["bonds"]})
+    records = {
+        int(t): [(r["axes"][0], r["axes"][1], r["axes"][2], r["values"]) for r in recs]
+        for t, recs in c["multipole"].items()
+    }
+    polar = {int(t): (p["alpha"], p["thole"], tuple(p["group"])) for t, p in c["polarize"].items()}
+    s = tg.systems.build_system(xyz, types, bonds, records, polar, scales=c["scales"], box=[c["box"]] * 3, name=name)
+    st = dict(tg.systems.DEFAULT_SETTINGS)
+    if c["ewald"]:
+        st.update(use_ewald=1, ewald_cutoff=c["cutoff"], nfft=tuple(c["nfft"]),
+                  aewald=tg.systems.ewald_coefficient(c["cutoff"]))
+    else:
+        st.update(use_ewald=0, ewald_cutoff=c["cutoff"], nfft=(0, 0, 0), aewald=0.0)
+    s.settings = st
+    return s, c["expected"]

@@ -137,3 +137,67 @@ def test_virial_fd_gas_symmetric(oracle, tg):
     s = water_cluster(tg, nmol=12)
     w = oracle.empole_virial_fd(s)
     assert np.abs(w - w.T).max() < 1e-5 * max(1.0, np.abs(w).max())
+
+
+TN_MAX = 1e-4   # Debye, every atom (the reference test's own margin is 1e-3 on four atoms)
+TN_RMS = 2e-5   # Debye: the files' 1e-6 rounding plus the reference run's 1e-5 RMS convergence
+
+
+@pytest.mark.parametrize("frame", [0, 1])
+def test_tinkernist_dipoles_golden(oracle, tg, frame):
+    """2,684-atom water/ion box, PME 36^3 (test/tinkernist.cpp): the oracle's
+    induced and direct dipoles against the reference's .uind / .udir files."""
+    import tn_fixture as T
+
+    s, fx = T.system(frame=frame)
+    o = oracle.OracleSystem(s)
+    ud, _, *_ = o.induce()
+    fd, _ = o.dfield()
+    D = tg.units.DEBYE
+    for got, ref in ((ud * D, fx["uind"][frame]), (fd * s.polarity[:, None] * D, fx["udir"][frame])):
+        d = got - ref
+        assert np.abs(d).max() < TN_MAX and np.sqrt((d ** 2).mean()) < TN_RMS
+
+
+@pytest.mark.parametrize("name", ["NaCl-2", "NaCl-3"])
+def test_nacl_empole_golden(oracle, name):
+    """Two ions (test/nacl.cpp): multipole energy, gradient (central
+    differences) and virial (strain derivatives; the diagonal under PME)
+    against the reference's known answers at its own margins."""
+    import nacl_fixture as N
+
+    s, ex = N.system(name)
+    eps = ex["eps"]
+    cut = s.settings["ewald_cutoff"]
+    e, _ = oracle.OracleSystem(s).empole_energy()
+    assert abs(e - ex["ref_eng"]) < eps + 5e-5  # known answers carry four decimals
+    g = oracle.empole_gradient_fd(s, atoms=np.arange(2), cutoff=cut)
+    assert np.abs(g - np.array(ex["ref_grad"])).max() < eps + 5e-5
+    w = oracle.empole_virial_fd(s, diag_only=bool(s.settings["use_ewald"]), cutoff=cut)
+    m = ~np.isnan(w)
+    assert np.abs(w - np.array(ex["ref_v"]))[m].max() < eps + 5e-4  # three decimals
+
+
+@pytest.mark.parametrize("ewald", [1, 0], ids=["ewald", "nonewald"])
+def test_polpair_golden(oracle, ewald):
+    """Na+/Cl- with a per-type-pair Thole coefficient (test/polpair.cpp):
+    total energy, gradient and virial (diagonal under PME) of the multipole
+    plus polarization terms against the reference's known answers."""
+    import pp_fixture as P
+
+    s, ex, eps = P.system(ewald)
+    cut = s.settings["ewald_cutoff"]
+    o = oracle.OracleSystem(s)
+    ud, up, *_ = o.induce()
+    e = o.empole_energy()[0] + o.epolar_energy()
+    assert abs(e - ex["energy"]) < eps["energy"]
+    g = oracle.empole_gradient_fd(s, atoms=np.arange(2), cutoff=cut) + oracle.epolar_gradient_fd(
+        s, ud, up, atoms=np.arange(2), cutoff=cut)
+    assert np.abs(g - np.array(ex["gradient"])).max() < eps["gradient"]
+    w = oracle.empole_virial_fd(s, diag_only=bool(ewald), cutoff=cut) + oracle.epolar_virial_fd(
+        s, ud, up, diag_only=bool(ewald), cutoff=cut)
+    m = ~np.isnan(w)
+    assert np.abs(w - np.array(ex["virial"]))[m].max() < eps["virial"]
+    # the pair coefficient matters: min(thole) gives another answer
+    s.ptype = None
+    assert abs(oracle.OracleSystem(s).epolar_energy() - (ex["energy"] - o.empole_energy()[0])) > 1.0

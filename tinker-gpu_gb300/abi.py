@@ -28,7 +28,7 @@ EXPORTS = [
     "t9gb_ufield_noalloc", "t9gb_learn_config", "t9gb_learn_policy", "t9gb_learn_reset", "t9gb_learn_stats", "t9gb_learn_get_weights",
     "t9gb_learn_set_weights", "t9gb_learn_eval", "t9gb_learn_adamw", "t9gb_learn_features",
     "t9gb_empole", "t9gb_epolar", "t9gb_emplar", "t9gb_energy_components", "t9gb_pme_own_fft",
-    "t9gb_pair_lanes",
+    "t9gb_pair_lanes", "t9gb_set_thole_pairs",
 ]
 CALC_ENERGY, CALC_GRAD, CALC_VIRIAL = 0x010, 0x020, 0x040
 
@@ -122,6 +122,7 @@ def load(path=None):
     lib.t9gb_energy_components.argtypes = [vp, dp]
     lib.t9gb_pme_own_fft.argtypes = [vp, C.c_int]
     lib.t9gb_pair_lanes.argtypes = [vp, C.c_int]
+    lib.t9gb_set_thole_pairs.argtypes = [vp, C.c_int, ip, dp]
     for name in ("t9gb_empole", "t9gb_epolar", "t9gb_emplar"):
         getattr(lib, name).argtypes = [vp, C.c_int, dp, fp, dp]
     _lib = lib
@@ -199,6 +200,18 @@ class Engine:
                 self.h, _ip(frames), _dp(pole), _dp(pol), _dp(thl), _dp(pdm), len(eik) // 2, _ip(eik), _dp(esc)
             )
         )
+        if getattr(system, "ptype", None) is not None:
+            self.set_thole_pairs(system.ptype, system.thole_table)
+
+    def set_thole_pairs(self, ptype, table):
+        """Per-type-pair Thole coefficients (ptype [n] 0-based, table [t][t]);
+        ptype None restores min(thole_i, thole_k)."""
+        if ptype is None:
+            self._check(self.lib.t9gb_set_thole_pairs(self.h, 0, None, None))
+            return
+        pt = np.ascontiguousarray(ptype, dtype=np.int32)
+        tb = np.ascontiguousarray(table, dtype=np.float64)
+        self._check(self.lib.t9gb_set_thole_pairs(self.h, int(tb.shape[0]), _ip(pt), _dp(tb)))
 
     def _check(self, rc, h=-1, allow=()):
         if rc == T9GB_OK or rc in allow:

@@ -84,7 +84,7 @@ static void free_all(Context* ctx)
       ctx->cell_count, ctx->cell_start, ctx->cell_atoms, ctx->atom_cell, ctx->rcp6, ctx->fld6, ctx->udir,
       ctx->efield, ctx->uind, ctx->rsd, ctx->zrsd, ctx->conj, ctx->vec, ctx->tmp6, ctx->e_atom, ctx->sframe, ctx->hout,
       ctx->red, ctx->scal, ctx->status, ctx->sref, ctx->lflag,
-      ctx->aspc_hist};
+      ctx->aspc_hist, ctx->thl};
    for (void* p : dev)
       if (p)
          cudaFree(p);
@@ -245,6 +245,45 @@ int t9gb_set_topology(t9gb_context* h, const int* frames, const double* pole, co
    T9_CUDA(cudaDeviceSynchronize());  // ordered before work on a non-blocking stream
    ctx->have_topology = true;
    ctx->have_order = false;
+   return T9GB_OK;
+}
+
+int t9gb_set_thole_pairs(t9gb_context* h, int ntypes, const int* ptype, const double* thlval)
+{
+   if (!h || ntypes < 0 || ntypes > 256 || (ntypes > 0 && (!ptype || !thlval)))
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   if (!ctx->have_topology)
+      return T9GB_NOT_READY;
+   const int n = ctx->n;
+   for (int i = 0; i < n && ntypes > 0; ++i)
+      if (ptype[i] < 0 || ptype[i] >= ntypes)
+         return T9GB_BAD_ARG;
+   std::vector<float> tab((size_t)ntypes * ntypes);
+   for (int a = 0; a < ntypes; ++a)
+      for (int b = 0; b < ntypes; ++b) {
+         const double v = thlval[(size_t)a * ntypes + b];
+         // each side of a pair reads its own row: the table must be symmetric
+         if (!std::isfinite(v) || v < 0 || v != thlval[(size_t)b * ntypes + a])
+            return T9GB_BAD_ARG;
+         tab[(size_t)a * ntypes + b] = (float)v;
+      }
+   if (ctx->thl) {
+      T9_CUDA(cudaFree(ctx->thl));
+      ctx->thl = nullptr;
+   }
+   ctx->nthl = 0;
+   ctx->h_ptype.clear();
+   if (ntypes > 0) {
+      T9_CUDA(cudaMalloc(&ctx->thl, sizeof(float) * tab.size()));
+      T9_CUDA(cudaMemcpy(ctx->thl, tab.data(), sizeof(float) * tab.size(), cudaMemcpyHostToDevice));
+      T9_CUDA(cudaDeviceSynchronize());
+      ctx->h_ptype.assign(ptype, ptype + n);
+      ctx->nthl = ntypes;
+   }
+   // the per-slot rows carry the type from the next ordering on
+   ctx->have_order = false;
+   drop_graphs(ctx);
    return T9GB_OK;
 }
 

@@ -122,6 +122,11 @@ struct Context {
    int4* frames = nullptr;  // zaxis, xaxis, yaxis (1-based signed), kind
    float* pole = nullptr;   // [n][10] local frame
    std::vector<double> h_polarity, h_thole, h_pdamp;
+   // per-type-pair Thole table (reference jpolar / thlval): when set, the
+   // thole slot of every row holds the atom's polarization type instead
+   std::vector<int> h_ptype;
+   float* thl = nullptr;  // [nthl][nthl], device
+   int nthl = 0;
    std::vector<int> h_excl_ik;
    std::vector<double> h_excl_scale;
 

@@ -160,11 +160,12 @@ static int sum_virial(Context* ctx, double* virial)
    for (int a = 0; a < 3; ++a)
       for (int b = 0; b < 3; ++b)
          W[a][b] = v[3 * a + b] + v[9 + 3 * a + b] + v[18 + 3 * a + b];
+   // the influence-function sums are symmetric: component ab is also ba
    for (int c = 0; c < 6; ++c) {
       const double kv = k[c] + k[6 + c];
-      W[ab[c][0]][ab[c][1]] += c < 3 ? kv : 0.5 * kv;
+      W[ab[c][0]][ab[c][1]] += kv;
       if (c >= 3)
-         W[ab[c][1]][ab[c][0]] += 0.5 * kv;
+         W[ab[c][1]][ab[c][0]] += kv;
    }
    for (int a = 0; a < 3; ++a)
       for (int b = 0; b < 3; ++b)

@@ -258,7 +258,7 @@ __device__ __forceinline__ void elec_pair(const PairParams& P, float3 Rv, float 
    }
    if (POLAR) {
       // Thole damping lambda_3/5/7 and d lambda / dr
-      const float pg = fminf(pti, ptk);
+      const float pg = pair_gamma(P, pti, ptk);
       const float dmp = pdi * pdk;
       float a = 0.f, ea = 0.f;
       if (dmp != 0.f) {

@@ -140,7 +140,8 @@ int order_build(Context* ctx)
       int a = ctx->h_perm[s];
       pol[s] = (float)ctx->h_polarity[a];
       pinv[s] = (float)(1.0 / std::max(ctx->h_polarity[a], 1.0e-16));
-      dmp[s] = make_float2((float)ctx->h_pdamp[a], (float)ctx->h_thole[a]);
+      const float tl = ctx->h_ptype.empty() ? (float)ctx->h_thole[a] : (float)ctx->h_ptype[a];
+      dmp[s] = make_float2((float)ctx->h_pdamp[a], tl);
    }
 
    // cell grid and list capacity

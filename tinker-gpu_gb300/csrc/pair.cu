@@ -21,10 +21,9 @@
 namespace t9gb {
 
 
-__device__ __forceinline__ void thole_damp(float r, float pdi, float pti, float pdk, float ptk, float& s3, float& s5,
+__device__ __forceinline__ void thole_damp(float r, float pdi, float pgamma, float pdk, float& s3, float& s5,
    float& s7)
 {
-   float pgamma = fminf(pti, ptk);
    float damp = pdi * pdk;
    float ratio = r * __frcp_rn(damp);
    damp = (damp == 0.f) ? -1.0e16f : -pgamma * ratio * ratio * ratio;
@@ -82,7 +81,7 @@ __device__ __forceinline__ void ufield_i(const PairParams& P, float r2, float3 d
    float rr3 = invr * rr2;
    float rr5 = 3.f * rr3 * rr2;
    float s3, s5, s7;
-   thole_damp(r, pdi, pti, pdk, ptk, s3, s5, s7);
+   thole_damp(r, pdi, pair_gamma(P, pti, ptk), pdk, s3, s5, s7);
    float b1, b2;
    if (P.ewald) {
       float e1, e2, e3;
@@ -177,7 +176,7 @@ __device__ __forceinline__ void dfield_i(const PairParams& P, float r2, float3 d
    float rr5 = 3.f * rr3 * rr2;
    float rr7 = 5.f * rr5 * rr2;
    float s3, s5, s7;
-   thole_damp(r, pdi, pti, pdk, ptk, s3, s5, s7);
+   thole_damp(r, pdi, pair_gamma(P, pti, ptk), pdk, s3, s5, s7);
    float e1 = 0.f, e2 = 0.f, e3 = 0.f;
    if (P.ewald)
       ewald_bn(P, r, invr, rr2, e1, e2, e3);
@@ -286,14 +285,14 @@ __global__ void __launch_bounds__(256) k_dfield_real(PairParams P, int npad, con
 // ---------------------------------------------------------------------------
 // sparse preconditioner: z_i = udiag alpha_i r_i + sum_k alpha_i alpha_k T_ik r_k
 
-__device__ __forceinline__ void precond_i(float r2, float3 d, float us, float poli, float pdi, float pti, float pdk,
+__device__ __forceinline__ void precond_i(const PairParams& P, float r2, float3 d, float us, float poli, float pdi, float pti, float pdk,
    const float* rk, float* f)
 {
    const float polk = rk[7];
    float invr = rsqrtf(r2);
    float r = r2 * invr;
    float s3, s5, s7;
-   thole_damp(r, pdi, pti, pdk, rk[6], s3, s5, s7);
+   thole_damp(r, pdi, pair_gamma(P, pti, rk[6]), pdk, s3, s5, s7);
    const float polik = poli * polk;
    const float ir3 = invr * invr * invr;
    const float rr3 = us * s3 * polik * ir3;
@@ -336,9 +335,9 @@ __global__ void __launch_bounds__(256) k_precond_sparse(PairParams P, int npad, 
          const float q0 = s0.x * s0.x + s0.y * s0.y + s0.z * s0.z;
          const float q1 = s1.x * s1.x + s1.y * s1.y + s1.z * s1.z;
          if (q0 <= P.cut2)
-            precond_i(q0, s0, 1.f, poli, pi.w, pti, p0.w, r0v, f);
+            precond_i(P, q0, s0, 1.f, poli, pi.w, pti, p0.w, r0v, f);
          if (q1 <= P.cut2)
-            precond_i(q1, s1, 1.f, poli, pi.w, pti, p1.w, r1v, f);
+            precond_i(P, q1, s1, 1.f, poli, pi.w, pti, p1.w, r1v, f);
       }
       if (k < cnt) {
          const int j = row[k];
@@ -348,7 +347,7 @@ __global__ void __launch_bounds__(256) k_precond_sparse(PairParams P, int npad, 
          if (r2 <= P.cut2) {
             float rk[8];
             load8(r8, j, rk);
-            precond_i(r2, d, 1.f, poli, pi.w, pti, pk.w, rk, f);
+            precond_i(P, r2, d, 1.f, poli, pi.w, pti, pk.w, rk, f);
          }
       }
       const int pa = sp_start[i], pb = sp_start[i + 1];
@@ -360,7 +359,7 @@ __global__ void __launch_bounds__(256) k_precond_sparse(PairParams P, int npad, 
          if (r2 <= P.cut2) {
             float rk[8];
             load8(r8, j, rk);
-            precond_i(r2, d, sp_sc[q].w, poli, pi.w, pti, pk.w, rk, f);
+            precond_i(P, r2, d, sp_sc[q].w, poli, pi.w, pti, pk.w, rk, f);
          }
       }
    }
@@ -646,7 +645,7 @@ __device__ __forceinline__ float gauss(float r, float mu, float inv2s2)
 // acc layout: gr[0..7) gq[7..11) dq[11..17) ga[17..22) fd[22..28) fp[28..34)
 constexpr int DACC = 34;
 
-__device__ __forceinline__ void desc_pair(float r2, float3 d, float us, float pdi, float pti, float pdk,
+__device__ __forceinline__ void desc_pair(const PairParams& P, float r2, float3 d, float us, float pdi, float pti, float pdk,
    const float* uk, float qk, float* acc)
 {
    const float invr = rsqrtf(r2);
@@ -670,7 +669,7 @@ __device__ __forceinline__ void desc_pair(float r2, float3 d, float us, float pd
    for (int j = 0; j < 5; ++j)
       acc[17 + j] += polk * fc * gauss(r, 1.f + 1.25f * j, 1.f / (2.f * 0.6f * 0.6f));
    float s3, s5, s7;
-   thole_damp(r, pdi, pti, pdk, uk[6], s3, s5, s7);
+   thole_damp(r, pdi, pair_gamma(P, pti, uk[6]), pdk, s3, s5, s7);
    const float ir3 = invr * invr * invr;
    const float rr3 = us * s3 * ir3;
    const float rr5 = 3.f * us * s5 * ir3 * invr * invr;
@@ -720,7 +719,7 @@ __global__ void __launch_bounds__(256) k_learn_features(PairParams P, int npad, 
          if (r2 < DESC_CUT * DESC_CUT) {
             float uk[8];
             load8(u8, j, uk);
-            desc_pair(r2, d, 1.f, pi.w, pti, pk.w, uk, srpole[12 * j], acc);
+            desc_pair(P, r2, d, 1.f, pi.w, pti, pk.w, uk, srpole[12 * j], acc);
          }
       }
       const int pa = sp_start[i], pb = sp_start[i + 1];
@@ -732,7 +731,7 @@ __global__ void __launch_bounds__(256) k_learn_features(PairParams P, int npad, 
          if (r2 < DESC_CUT * DESC_CUT) {
             float uk[8];
             load8(u8, j, uk);
-            desc_pair(r2, d, sp_sc[q].w, pi.w, pti, pk.w, uk, srpole[12 * j], acc);
+            desc_pair(P, r2, d, sp_sc[q].w, pi.w, pti, pk.w, uk, srpole[12 * j], acc);
          }
       }
    }

@@ -15,12 +15,24 @@ struct PairParams {
    float aewald;
    float ec1, ec2, ec3, ec4;  // (2a^2)^j / (sqrt(pi) a), j = 1..4
    int cap;              // list row stride
+   const float* thl;     // per-type-pair Thole table [nthl][nthl], or null
+   int nthl;
 };
 
 __device__ __forceinline__ float3 sep(const PairParams& P, float4 pi, float4 pk)
 {
    return make_float3(image1(pk.x - pi.x, P.lx, P.ilx), image1(pk.y - pi.y, P.ly, P.ily),
       image1(pk.z - pi.z, P.lz, P.ilz));
+}
+
+// Thole coefficient of a pair from the two rows' thole slots: the
+// per-type-pair table thlval[jpolar_i][jpolar_k] when one is set (the
+// reference's CUDA pair kernels, src/cu/amoeba/ufield_cu1.cc, dfield_cu1.cc,
+// sparsePrecond_cu1.cc, epolar_cu1.cc), else min(thole_i, thole_k)
+// (damp_thole2/3, include/seq/damp.h:19-44)
+__device__ __forceinline__ float pair_gamma(const PairParams& P, float ti, float tk)
+{
+   return P.thl ? __ldg(P.thl + (int)ti * P.nthl + (int)tk) : fminf(ti, tk);
 }
 
 template <int G, int N>
@@ -73,6 +85,8 @@ static inline PairParams make_params(const Context* ctx, double cutoff)
    P.ec3 = (float)(base * alsq2 * alsq2 * alsq2);
    P.ec4 = (float)(base * alsq2 * alsq2 * alsq2 * alsq2);
    P.cap = ctx->nbr_cap;
+   P.thl = ctx->nthl > 0 ? ctx->thl : nullptr;
+   P.nthl = ctx->nthl;
    return P;
 }
 

@@ -55,6 +55,8 @@ class System:
     mol_size: Optional[np.ndarray] = None
     name: str = ""
     settings: dict = field(default_factory=dict)
+    ptype: Optional[np.ndarray] = None  # [n] polarization type, with thole_table
+    thole_table: Optional[np.ndarray] = None  # [t][t] per-type-pair Thole coefficient
 
     @property
     def n(self):
