@@ -94,6 +94,20 @@ int t9gb_set_topology(t9gb_context* ctx, const int* frames, const double* pole, 
  * t9gb_nblist_build; ntypes <= 256. */
 int t9gb_set_thole_pairs(t9gb_context* ctx, int ntypes, const int* ptype, const double* thlval);
 
+/* Uniform external electric field field[3] in e/A^2 (Tinker's MV/cm value
+ * divided by 1439.96455), or NULL for none.  Replaces extfld::texfld and
+ * its consumers: the permanent field of both dipole sets gains the field
+ * (extfieldModifyDField, src/elec.cpp:836-842, src/cu/amoeba/empole.cu:
+ * 139-167), and the multipole terms gain -f (q r.E + d.E) per atom with its
+ * force, torque and virial (exfieldDipole, src/elec.cpp:820-833,
+ * src/cu/amoeba/empole.cu:79-137), counted in the one-body part of
+ * t9gb_empole_energy.  r is the coordinate as given: the reference wraps
+ * molecules into the primary cell first (bounds(), src/atom.cpp:169-176),
+ * which the caller does before passing coordinates.  The polarization
+ * energy includes the field through the dot product.  May change between
+ * solves (a time-dependent field); takes effect in stream order. */
+int t9gb_set_external_field(t9gb_context* ctx, const double* field);
+
 /* Coordinates [n][3].  Replace copyPosToXyz (src/atom.cpp:161-166). */
 int t9gb_set_xyz_host(t9gb_context* ctx, const double* xyz);
 int t9gb_set_xyz_device(t9gb_context* ctx, const float* xyz_device);

@@ -51,6 +51,7 @@ class OrSystem(C.Structure):
         ("nthl", C.c_int),
         ("ptype", C.POINTER(C.c_int)),
         ("thl", C.POINTER(C.c_double)),
+        ("exfld", C.c_double * 3),
     ]
 
 
@@ -167,6 +168,10 @@ class OracleSystem:
         s.cutoff = float(st.get("ewald_cutoff", 1.0e9) if cutoff is None else cutoff)
         from_units = __import__("importlib").import_module("tinker-gpu_gb300.units")
         s.electric = from_units.ELECTRIC
+        ef = getattr(system, "exfld", None)
+        if ef is not None:
+            for d in range(3):
+                s.exfld[d] = float(ef[d])
         if getattr(system, "ptype", None) is not None:
             self.ptype = np.ascontiguousarray(system.ptype, dtype=np.int32)
             self.thl = np.ascontiguousarray(system.thole_table, dtype=np.float64)

@@ -68,6 +68,7 @@ typedef struct {
    int nthl;                /* > 0: per-type-pair Thole table (jpolar / thlval) */
    const int* ptype;        /* [n] polarization type, 0..nthl-1 */
    const double* thl;       /* [nthl][nthl] */
+   double exfld[3];         /* uniform external field, e/A^2 (zero: none) */
 } or_system;
 
 typedef struct {
@@ -1089,6 +1090,12 @@ void or_dfield(const or_system* s, double* field, double* fieldp)
    or_acc_reduce(&acc, n, field, fieldp);
    or_excl_free(&ex);
    or_pairs_free(&pl);
+   /* external field on both sets (extfieldModifyDField, src/cu/amoeba/empole.cu:139-159) */
+   for (int i = 0; i < n; ++i)
+      for (int d = 0; d < 3; ++d) {
+         field[3 * i + d] += s->exfld[d];
+         fieldp[3 * i + d] += s->exfld[d];
+      }
 }
 
 /* cached pair list and PME state for repeated ufield calls */
@@ -1555,6 +1562,15 @@ double or_empole_energy(const or_system* s, double* parts)
          double qii = 2 * (m[7] * m[7] + m[8] * m[8] + m[9] * m[9]) + m[4] * m[4] + m[5] * m[5] + m[6] * m[6];
          eself += fterm * (cii + a2 * (dii / 3 + 2 * a2 * qii * 0.2));
       }
+   }
+   /* permanent multipoles in the external field, -f (q r.E + d.E) per atom
+    * with unwrapped coordinates (exfieldDipole_cu1, src/cu/amoeba/empole.cu:79-130);
+    * counted with the one-body self part */
+   for (int i = 0; i < n; ++i) {
+      const double* m = &s->rpole[10 * i];
+      const double* E = s->exfld;
+      eself -= f * (m[0] * (s->x[i] * E[0] + s->y[i] * E[1] + s->z[i] * E[2]) + m[1] * E[0] + m[2] * E[1] +
+                      m[3] * E[2]);
    }
    if (parts) {
       parts[0] = ereal;

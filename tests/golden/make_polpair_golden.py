@@ -19,12 +19,13 @@ from make_localframe_golden import REF, read_prm  # noqa: E402
 
 
 def read_xyz(path):
-    """Tinker .xyz with a box line after the title."""
+    """Tinker .xyz, with or without a box line after the title."""
     with open(path) as f:
         lines = f.read().splitlines()
     n = int(lines[0].split()[0])
+    first = 2 if not lines[1].split()[0].isdigit() else 1
     atoms = []
-    for ln in lines[2 : 2 + n]:
+    for ln in lines[first : first + n]:
         t = ln.split()
         atoms.append({"index": int(t[0]), "name": t[1], "xyz": [float(v) for v in t[2:5]], "type": int(t[5]),
                       "bonds": [int(v) for v in t[6:]]})

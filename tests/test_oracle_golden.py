@@ -201,3 +201,30 @@ def test_polpair_golden(oracle, ewald):
     # the pair coefficient matters: min(thole) gives another answer
     s.ptype = None
     assert abs(oracle.OracleSystem(s).epolar_energy() - (ex["energy"] - o.empole_energy()[0])) > 1.0
+
+
+def test_extfield_golden(oracle):
+    """Four waters and a Na+ in a uniform external field (test/extfield.cpp,
+    amoebabio18): multipole, polarization and total energies, gradients and
+    virials (diagonal under PME) against the reference's known answers."""
+    import ef_fixture as F
+
+    s, fx = F.system()
+    ex, eps = fx["expected"], fx["eps"]
+    cut = s.settings["ewald_cutoff"]
+    o = oracle.OracleSystem(s)
+    em = o.empole_energy()[0]
+    ud, up, *_ = o.induce()
+    ep = o.epolar_energy()
+    assert abs(em - ex["mpole"]["energy"]) < eps["energy"]
+    assert abs(ep - ex["polar"]["energy"]) < eps["energy"]
+    assert abs(em + ep - ex["mplar"]["energy"]) < eps["energy"]
+    atoms = np.arange(s.n)
+    gm = oracle.empole_gradient_fd(s, atoms=atoms, cutoff=cut)
+    gp = oracle.epolar_gradient_fd(s, ud, up, atoms=atoms, cutoff=cut)
+    for g, key in ((gm, "mpole"), (gp, "polar"), (gm + gp, "mplar")):
+        assert np.abs(g - np.array(ex[key]["gradient"])).max() < eps["gradient"]
+    wm = np.diag(oracle.empole_virial_fd(s, diag_only=True, cutoff=cut))
+    wp = np.diag(oracle.epolar_virial_fd(s, ud, up, diag_only=True, cutoff=cut))
+    for w, key in ((wm, "mpole"), (wp, "polar"), (wm + wp, "mplar")):
+        assert np.abs(w - np.diag(np.array(ex[key]["virial"]))).max() < eps["virial"]

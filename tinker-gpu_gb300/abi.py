@@ -28,7 +28,7 @@ EXPORTS = [
     "t9gb_ufield_noalloc", "t9gb_learn_config", "t9gb_learn_policy", "t9gb_learn_reset", "t9gb_learn_stats", "t9gb_learn_get_weights",
     "t9gb_learn_set_weights", "t9gb_learn_eval", "t9gb_learn_adamw", "t9gb_learn_features",
     "t9gb_empole", "t9gb_epolar", "t9gb_emplar", "t9gb_energy_components", "t9gb_pme_own_fft",
-    "t9gb_pair_lanes", "t9gb_set_thole_pairs",
+    "t9gb_pair_lanes", "t9gb_set_thole_pairs", "t9gb_set_external_field",
 ]
 CALC_ENERGY, CALC_GRAD, CALC_VIRIAL = 0x010, 0x020, 0x040
 
@@ -123,6 +123,7 @@ def load(path=None):
     lib.t9gb_pme_own_fft.argtypes = [vp, C.c_int]
     lib.t9gb_pair_lanes.argtypes = [vp, C.c_int]
     lib.t9gb_set_thole_pairs.argtypes = [vp, C.c_int, ip, dp]
+    lib.t9gb_set_external_field.argtypes = [vp, dp]
     for name in ("t9gb_empole", "t9gb_epolar", "t9gb_emplar"):
         getattr(lib, name).argtypes = [vp, C.c_int, dp, fp, dp]
     _lib = lib
@@ -202,6 +203,16 @@ class Engine:
         )
         if getattr(system, "ptype", None) is not None:
             self.set_thole_pairs(system.ptype, system.thole_table)
+        if getattr(system, "exfld", None) is not None:
+            self.set_external_field(system.exfld)
+
+    def set_external_field(self, field):
+        """Uniform external field [3] in e/A^2, or None."""
+        if field is None:
+            self._check(self.lib.t9gb_set_external_field(self.h, None))
+            return
+        ef = np.ascontiguousarray(field, dtype=np.float64)
+        self._check(self.lib.t9gb_set_external_field(self.h, _dp(ef)))
 
     def set_thole_pairs(self, ptype, table):
         """Per-type-pair Thole coefficients (ptype [n] 0-based, table [t][t]);

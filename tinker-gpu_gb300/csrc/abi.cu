@@ -30,6 +30,8 @@ static int alloc_all(Context* ctx)
    T9_CUDA(cudaMalloc(&ctx->sdamp, sizeof(float2) * npad));
    T9_CUDA(cudaMalloc(&ctx->srpole, sizeof(float) * 12 * npad));
    T9_CUDA(cudaMemset(ctx->srpole, 0, sizeof(float) * 12 * npad));
+   T9_CUDA(cudaMalloc(&ctx->exfld, sizeof(float) * 4));
+   T9_CUDA(cudaMemset(ctx->exfld, 0, sizeof(float) * 4));
    T9_CUDA(cudaMalloc(&ctx->nnbr, sizeof(int) * npad));
    T9_CUDA(cudaMemset(ctx->nnbr, 0, sizeof(int) * npad));
    T9_CUDA(cudaMalloc(&ctx->nnbrc, sizeof(int) * npad));
@@ -84,7 +86,7 @@ static void free_all(Context* ctx)
       ctx->cell_count, ctx->cell_start, ctx->cell_atoms, ctx->atom_cell, ctx->rcp6, ctx->fld6, ctx->udir,
       ctx->efield, ctx->uind, ctx->rsd, ctx->zrsd, ctx->conj, ctx->vec, ctx->tmp6, ctx->e_atom, ctx->sframe, ctx->hout,
       ctx->red, ctx->scal, ctx->status, ctx->sref, ctx->lflag,
-      ctx->aspc_hist, ctx->thl};
+      ctx->aspc_hist, ctx->thl, ctx->exfld};
    for (void* p : dev)
       if (p)
          cudaFree(p);
@@ -284,6 +286,27 @@ int t9gb_set_thole_pairs(t9gb_context* h, int ntypes, const int* ptype, const do
    // the per-slot rows carry the type from the next ordering on
    ctx->have_order = false;
    drop_graphs(ctx);
+   return T9GB_OK;
+}
+
+int t9gb_set_external_field(t9gb_context* h, const double* field)
+{
+   if (!h)
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   float e[4] = {0.f, 0.f, 0.f, 0.f};
+   if (field)
+      for (int d = 0; d < 3; ++d) {
+         if (!std::isfinite(field[d]))
+            return T9GB_BAD_ARG;
+         e[d] = (float)field[d];
+      }
+   // stream-ordered: solves already queued keep the field they were queued
+   // with; the pageable source is consumed before the call returns
+   for (int d = 0; d < 4; ++d)
+      ctx->h_exfld[d] = e[d];
+   T9_CUDA(cudaMemcpyAsync(ctx->exfld, ctx->h_exfld, sizeof(float) * 4, cudaMemcpyHostToDevice, ctx->stream));
+   ctx->use_exfld = e[0] != 0.f || e[1] != 0.f || e[2] != 0.f;
    return T9GB_OK;
 }
 

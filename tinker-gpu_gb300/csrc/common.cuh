@@ -127,6 +127,11 @@ struct Context {
    std::vector<int> h_ptype;
    float* thl = nullptr;  // [nthl][nthl], device
    int nthl = 0;
+   // uniform external field (reference extfld::texfld), e/A^2: device copy
+   // read by the permanent-field kernel, host copy for the force path
+   float* exfld = nullptr;  // [4], device
+   float h_exfld[4] = {0.f, 0.f, 0.f, 0.f};
+   bool use_exfld = false;
    std::vector<int> h_excl_ik;
    std::vector<double> h_excl_scale;
 
@@ -345,6 +350,9 @@ int force_setup(Context* ctx);
 void force_free(Context* ctx);
 int frame_map_build(Context* ctx);
 int elec_forces(Context* ctx, bool mpole, bool polar, float* grad, bool vir);
+// external-field multipole terms after the pair / reciprocal kernels:
+// energy into the one-body block of e_atom, forces, torque field, virial rows
+int launch_extfield_mpole(Context* ctx, bool forces, bool vir);
 int launch_force_recip(Context* ctx, bool mpole, bool polar, float* wrec);
 int induce_sorted(Context* ctx);
 int learn_setup(Context* ctx);

@@ -2,7 +2,8 @@
 // deterministic FP64 reductions.
 //
 //  - t9gb_empole_energy: permanent-multipole energy, real + reciprocal + self
-//    (empole(calc::energy), src/amoeba/empole.cpp:81-138);
+//    (empole(calc::energy), src/amoeba/empole.cpp:81-138); the one-body
+//    "self" part also holds the external-field term when a field is set;
 //  - t9gb_epolar_energy: polarization energy by the dot product
 //    -1/2 f sum_i u_d,i . E_p,i (epolar0DotProd, src/cu/amoeba/epolar.cu:14-30);
 //  - t9gb_empole / t9gb_epolar / t9gb_emplar: energy and gradient with the
@@ -78,6 +79,7 @@ extern "C" int t9gb_empole_energy(t9gb_context* h, double* energy, double* parts
       T9_CUDA(cudaMemsetAsync(ctx->e_atom, 0, sizeof(double) * 3 * ctx->npad, ctx->stream));
       T9_CHECK(launch_empole_real(ctx, ctx->e_atom));
       T9_CHECK(launch_empole_recip(ctx, ctx->e_atom + ctx->npad));
+      T9_CHECK(launch_extfield_mpole(ctx, false, false));
       k_sum_rows<<<3, 1024, 0, ctx->stream>>>(ctx->npad, ctx->npad, ctx->e_atom, ctx->scal + 32);
       T9_CUDA(cudaGetLastError());
       T9_CUDA(cudaMemcpyAsync(ctx->h_scal + 32, ctx->scal + 32, sizeof(double) * 3, cudaMemcpyDeviceToHost, ctx->stream));
@@ -190,6 +192,7 @@ static int elec_terms(Context* ctx, bool mpole, bool polar, int vers, double* en
       } else if (mpole) {
          T9_CHECK(launch_empole_real(ctx, ctx->e_atom));
          T9_CHECK(launch_empole_recip(ctx, ctx->e_atom + ctx->npad));
+         T9_CHECK(launch_extfield_mpole(ctx, false, false));
       }
       T9_CUDA(cudaStreamSynchronize(ctx->stream));
       int redo = 0;

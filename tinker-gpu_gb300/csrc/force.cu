@@ -582,6 +582,53 @@ __global__ void k_frame_force(int npad, const int* __restrict__ perm, const int4
    }
 }
 
+// Permanent multipoles in a uniform external field E (e/A^2): energy
+// -f (q r.E + d.E) per atom at the caller's coordinates, force f q E, torque
+// field dE/dd = -f E (the frame chain rule turns it into frame forces), and
+// virial rows dE/d(eps_ab) = -f q E_a r_b (exfieldDipole_cu1,
+// src/cu/amoeba/empole.cu:79-130).  Adds to what the pair and reciprocal
+// kernels stored; any output may be null.
+__global__ void k_extfield_mpole(int npad, const int* __restrict__ perm, const float* __restrict__ xyz,
+   const float* __restrict__ rp, float e0, float e1, float e2, float f, float* __restrict__ fout,
+   float* __restrict__ tout, float* __restrict__ wout, double* __restrict__ e_one)
+{
+   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < npad; s += gridDim.x * blockDim.x) {
+      const int i = perm[s];
+      if (i < 0)
+         continue;
+      const float E[3] = {e0, e1, e2};
+      const float r[3] = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
+      const float* m = rp + 12 * s;
+      const float rE = r[0] * E[0] + r[1] * E[1] + r[2] * E[2];
+      if (e_one)
+         e_one[s] += -(double)f * ((double)m[0] * rE + (double)m[1] * E[0] + (double)m[2] * E[1] + (double)m[3] * E[2]);
+      if (fout)
+         for (int c = 0; c < 3; ++c)
+            fout[3 * s + c] += f * m[0] * E[c];
+      if (tout) {
+         tout[10 * s] += -f * rE;
+         for (int c = 0; c < 3; ++c)
+            tout[10 * s + 1 + c] += -f * E[c];
+      }
+      if (wout)
+         for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b)
+               wout[(3 * a + b) * npad + s] += -f * m[0] * E[a] * r[b];
+   }
+}
+
+int launch_extfield_mpole(Context* ctx, bool forces, bool vir)
+{
+   if (!ctx->use_exfld)
+      return T9GB_OK;
+   const float* E = ctx->h_exfld;
+   k_extfield_mpole<<<grid_for(ctx->npad, 256), 256, 0, ctx->stream>>>(ctx->npad, ctx->perm, ctx->xyz, ctx->srpole,
+      E[0], E[1], E[2], (float)ctx->cfg.electric, forces ? ctx->freal : nullptr, forces ? ctx->treal : nullptr,
+      vir ? ctx->wvir : nullptr, ctx->e_atom + 2 * (size_t)ctx->npad);
+   T9_CUDA(cudaGetLastError());
+   return T9GB_OK;
+}
+
 // gradient (caller order) = -(sum of the per-slot forces + frame forces)
 __global__ void k_force_combine(int n, const int* __restrict__ iperm, const float* __restrict__ f0,
    const float* __restrict__ f1, const float* __restrict__ f2, const int* __restrict__ rev_start,
@@ -715,6 +762,8 @@ int elec_forces(Context* ctx, bool mpole, bool polar, float* grad, bool vir)
       T9_CHECK(launch_force_recip(ctx, mpole, polar, vir ? ctx->wvir + 18 * np : nullptr));
    else if (vir)
       T9_CUDA(cudaMemsetAsync(ctx->wvir + 18 * np, 0, sizeof(float) * 9 * np, ctx->stream));
+   if (mpole)
+      T9_CHECK(launch_extfield_mpole(ctx, true, vir));
    k_frame_force<<<grid_for(ctx->npad, 128), 128, 0, ctx->stream>>>(ctx->npad, ctx->perm, ctx->frames, ctx->pole,
       ctx->xyz, ctx->treal, ew ? ctx->trecp : nullptr, ew && polar ? ctx->trecu : nullptr, ctx->fbuf,
       vir ? ctx->wvir + 9 * np : nullptr);

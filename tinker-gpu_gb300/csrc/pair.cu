@@ -241,7 +241,7 @@ template <int G>
 __global__ void __launch_bounds__(256) k_dfield_real(PairParams P, int npad, const int* __restrict__ nbr,
    const int* __restrict__ nnbr, const int* __restrict__ sp_start, const int* __restrict__ sp_j,
    const float4* __restrict__ sp_sc, const float4* __restrict__ spos, const float* __restrict__ rp,
-   const float* __restrict__ base8, float* __restrict__ out8)
+   const float* __restrict__ base8, const float* __restrict__ exfld, float* __restrict__ out8)
 {
    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
    const int i = tid / G, g = tid % G;
@@ -279,6 +279,17 @@ __global__ void __launch_bounds__(256) k_dfield_real(PairParams P, int npad, con
       }
    }
    group_reduce<G, 6>(f);
+   if (i < P.n) {
+      // uniform external field on both sets (extfieldModifyDField_cu1,
+      // src/cu/amoeba/empole.cu:139-159); zero when none is set
+      const float e0 = exfld[0], e1 = exfld[1], e2 = exfld[2];
+      f[0] += e0;
+      f[1] += e1;
+      f[2] += e2;
+      f[3] += e0;
+      f[4] += e1;
+      f[5] += e2;
+   }
    store6(out8, i < P.n ? base8 : nullptr, i, g, f);
 }
 
@@ -582,7 +593,7 @@ int launch_dfield_real(Context* ctx, const float* base6, float* out6)
    PairParams P = make_params(ctx, ctx->cfg.cutoff);
    prof_begin(ctx, P_DFIELD_REAL);
    T9_LANES_DISPATCH(k_dfield_real, P, ctx->npad, ctx->nbrc, ctx->nnbrc, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos,
-      ctx->srpole, base6, out6);
+      ctx->srpole, base6, ctx->exfld, out6);
    prof_end(ctx);
    T9_CUDA(cudaGetLastError());
    return T9GB_OK;

@@ -57,6 +57,7 @@ class System:
     settings: dict = field(default_factory=dict)
     ptype: Optional[np.ndarray] = None  # [n] polarization type, with thole_table
     thole_table: Optional[np.ndarray] = None  # [t][t] per-type-pair Thole coefficient
+    exfld: Optional[np.ndarray] = None  # uniform external field [3], e/A^2
 
     @property
     def n(self):
