@@ -58,7 +58,8 @@ typedef struct {
    double udiag;        /* polpot::uaccel */
    int pcgprec;         /* 1: sparse preconditioner, 0: diagonal (polpcg::pcgprec) */
    int pcgguess;        /* 1: direct guess alpha*E, 0: zero (polpcg::pcgguess) */
-   int predictor;       /* 0: none, 1: ASPC (uprior::polpred) */
+   int predictor;       /* 0: none, 1: ASPC (16 frames), 2: GEAR (6) (uprior::polpred;
+                           LSQR has no CUDA path in the reference: T9GB_BAD_ARG) */
    double electric;     /* kcal*A/(mol*e^2) (units::electric) */
    double debye;        /* Debye per e*A (units::debye) */
 } t9gb_config;

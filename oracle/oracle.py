@@ -87,6 +87,7 @@ def lib():
         _lib.or_bsmod.argtypes = [C.c_int, C.c_int, dp]
         _lib.or_bsplgen_export.argtypes = [C.c_double, C.c_int, C.c_int, dp]
         _lib.or_aspc_sum.argtypes = [C.c_int, C.c_int, dp, dp]
+        _lib.or_gear_sum.argtypes = [C.c_int, C.c_int, dp, dp]
         _lib.or_empole_energy.argtypes = [C.POINTER(OrSystem), dp]
         _lib.or_empole_energy.restype = C.c_double
         _lib.or_epolar_energy_dot.argtypes = [C.POINTER(OrSystem), dp, dp]
@@ -346,4 +347,12 @@ def aspc_sum(hist, nualt):
     n3 = hist[0].size
     out = np.zeros(n3)
     lib().or_aspc_sum(n3, int(nualt), _dp(hist), _dp(out))
+    return out
+
+
+def gear_sum(hist, nualt):
+    hist = np.ascontiguousarray(hist, dtype=np.float64)
+    n3 = hist[0].size
+    out = np.zeros(n3)
+    lib().or_gear_sum(n3, int(nualt), _dp(hist), _dp(out))
     return out

@@ -1440,6 +1440,22 @@ void or_aspc_sum(int n3, int nualt, const double* hist, double* u)
    }
 }
 
+/* Gear 6-point extrapolation, the binomial weights of the fifth difference
+ * (exact for a quintic history); the reference's table is in
+ * src/cu/upredict.cu:141-146 and its ring of 6 in src/amoeba/epolar.cpp:461-468.
+ * hist[6][n3], slot s gets gear[(nualt-1-s) mod 6]. */
+static const double or_gear[6] = {6., -15., 20., -15., 6., -1.};
+
+void or_gear_sum(int n3, int nualt, const double* hist, double* u)
+{
+   for (int i = 0; i < n3; ++i) {
+      double acc = 0;
+      for (int s = 0; s < 6; ++s)
+         acc += or_gear[((nualt - 1 - s) % 6 + 6) % 6] * hist[(size_t)s * n3 + i];
+      u[i] = acc;
+   }
+}
+
 /* exported wrappers for tests: PME pieces */
 void or_bsplgen_export(double w, int order, int level, double* theta) { or_bsplgen(w, order, level, theta); }
 

@@ -118,3 +118,29 @@ def test_graph_predictor_steps_match_stepwise(gpu_lib, tg):
         ub, _, _ = b.induce_host(x)
         assert a.stats()[0] == b.stats()[0]
         assert np.array_equal(ua, ub)
+
+
+def test_gear_predictor_trajectory(gpu_lib, oracle, tg):
+    """Gear guess after 6 saved steps: fewer iterations than alpha E, the
+    converged answer unchanged; graph and host-driven loops agree."""
+    s = tg.systems.make_config("water648")
+    tr = tg.systems.Trajectory(s)
+    plain = engine_for(s)
+    gear = engine_for(s, predictor=2)
+    step = engine_for(s, predictor=2)
+    step.use_graph(False)
+    its_plain, its_gear = [], []
+    for k in range(12):
+        x = tr.frame(k)
+        ud0, _, _ = plain.induce_host(x)
+        its_plain.append(plain.stats()[0])
+        ud1, _, rc = gear.induce_host(x)
+        assert rc == 0
+        its_gear.append(gear.stats()[0])
+        ud2, _, _ = step.induce_host(x)
+        assert np.array_equal(ud1, ud2) and gear.stats()[0] == step.stats()[0]
+    print("iterations plain", its_plain, "gear", its_gear)
+    D = tg.units.DEBYE
+    assert rms_err(ud1 * D, ud0 * D) < DIPOLE_RMS_DEBYE
+    assert its_gear[:6] == its_plain[:6]
+    assert np.mean(its_gear[7:]) < np.mean(its_plain[7:])

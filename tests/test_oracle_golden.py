@@ -75,6 +75,19 @@ def test_aspc_weights_sum_to_one(oracle):
         assert np.allclose(oracle.aspc_sum(hist, nualt), 1.0, atol=1e-12)
 
 
+def test_gear_extrapolates_a_quintic(oracle):
+    """Gear's six weights continue any polynomial of degree <= 5; the ring
+    slot of frame t is t mod 6 (ulspredSave, src/amoeba/induce.cpp:37)."""
+    rng = np.random.default_rng(3)
+    c = rng.normal(size=(6, 4))
+    p = lambda t: sum(c[k] * t ** k for k in range(6))
+    for nualt in (6, 7, 11):
+        hist = np.zeros((6, 4))
+        for t in range(nualt - 6, nualt):
+            hist[t % 6] = p(t)
+        assert np.allclose(oracle.gear_sum(hist, nualt), p(nualt), rtol=1e-9, atol=1e-6)
+
+
 @pytest.mark.parametrize("ewald", [0, 1], ids=["nonewald", "pme"])
 def test_epolar_energy_golden(oracle, ewald):
     """Polarization energy by the dot product (localframe.cpp:329-333, :500-505)."""

@@ -65,9 +65,10 @@ static int alloc_all(Context* ctx)
    T9_CUDA(cudaMemset(ctx->status, 0, sizeof(int) * 16));
    T9_CUDA(cudaMallocHost(&ctx->h_status, sizeof(int) * 16));
    T9_CUDA(cudaMallocHost(&ctx->h_scal, sizeof(double) * 64));
-   if (ctx->cfg.predictor == 1) {
-      T9_CUDA(cudaMalloc(&ctx->aspc_hist, sizeof(float) * 16 * 8 * (size_t)npad));
-      T9_CUDA(cudaMemset(ctx->aspc_hist, 0, sizeof(float) * 16 * 8 * (size_t)npad));
+   if (pred_depth(ctx->cfg) > 0) {
+      const size_t bytes = sizeof(float) * pred_depth(ctx->cfg) * 8 * (size_t)npad;
+      T9_CUDA(cudaMalloc(&ctx->aspc_hist, bytes));
+      T9_CUDA(cudaMemset(ctx->aspc_hist, 0, bytes));
    }
    ctx->h_stage_bytes = sizeof(float) * 8 * (size_t)npad;
    T9_CUDA(cudaMallocHost(&ctx->h_stage, ctx->h_stage_bytes));
@@ -156,6 +157,10 @@ int t9gb_create(const t9gb_config* cfg, t9gb_context** out)
       return T9GB_BAD_ARG;
    const bool pbc = cfg->box[0] > 0 && cfg->box[1] > 0 && cfg->box[2] > 0;
    if (cfg->use_ewald && (!pbc || cfg->nfft[0] < 8 || cfg->nfft[1] < 8 || cfg->nfft[2] < 8 || cfg->aewald <= 0))
+      return T9GB_BAD_ARG;
+   // ASPC or Gear; the reference's CUDA path has no LSQR predictor
+   // (throwExceptionMissingFunction, src/cu/upredict.cu:198-201)
+   if (cfg->predictor < 0 || cfg->predictor > 2)
       return T9GB_BAD_ARG;
    if (cfg->politer < 1 || cfg->poleps <= 0)
       return T9GB_BAD_ARG;

@@ -211,7 +211,8 @@ struct Context {
    int* h_status = nullptr; // pinned mirrors
    double* h_scal = nullptr;
 
-   // ASPC predictor ring, sorted [16][npad][6]; the ring count is device state
+   // predictor ring (ASPC 16 / Gear 6 frames), sorted [depth][npad][8]; the
+   // ring count is device state
    float* aspc_hist = nullptr;
 
    // learned initial guess (learn.cu)
@@ -318,6 +319,9 @@ int launch_list_filter(Context* ctx);             // pair.cu  // after a sync; r
 int scatter_positions(Context* ctx);
 int rotpole_sorted(Context* ctx);
 int reset_predictor(Context* ctx);
+// ring depth of the dipole predictor: ASPC 16, Gear 6, none 0
+// (maxualt, src/amoeba/epolar.cpp:446-470)
+static inline int pred_depth(const t9gb_config& c) { return c.predictor == 1 ? 16 : c.predictor == 2 ? 6 : 0; }
 int fill_row_padding(Context* ctx);
 int pme_setup(Context* ctx);
 void pme_free(Context* ctx);

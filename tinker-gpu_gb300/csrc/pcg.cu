@@ -33,6 +33,10 @@ __constant__ double c_aspc[16] = {62. / 17., -310. / 51., 2170. / 323., -2329. /
    1024. / 809., -479. / 883., 257. / 1316., -434. / 7429., 191. / 13375., -62. / 22287., 3. / 7217.,
    -3. / 67015., 2. / 646323., -1. / 9694845.};
 
+// Gear 6-point extrapolation weights (the binomial coefficients of the
+// fifth difference); the reference tabulates them in src/cu/upredict.cu:141-146.
+__constant__ double c_gear[6] = {6., -15., 20., -15., 6., -1.};
+
 struct VecArgs {
    int ne;   // 6 * npad active elements (d xyz, p xyz of each slot)
    int ne8;  // 8 * npad floats per vector (rows padded to 32 bytes)
@@ -44,18 +48,22 @@ struct VecArgs {
 
 // ---- start of induce ----
 
-// E = field, udir = alpha E, guess: ASPC when 16 frames are saved, else the
-// direct guess alpha E (pcgguess) or zero
+// E = field, udir = alpha E, guess: the predictor's extrapolation once its
+// ring (depth 16 for ASPC, 6 for Gear) is full, else the direct guess
+// alpha E (pcgguess) or zero
 __global__ void k_init_guess(VecArgs A, const float* __restrict__ fld, float* __restrict__ efield,
    float* __restrict__ udir, float* __restrict__ uind, int pcgguess, int predictor, const float* __restrict__ hist,
    const int* __restrict__ state)
 {
    const int nualt = state[ST_NUALT];
-   const bool predict = predictor && nualt >= 16;
+   const int depth = predictor == 1 ? 16 : predictor == 2 ? 6 : 0;
+   const bool predict = depth > 0 && nualt >= depth;
    double coef[16];
    if (predict)
-      for (int k = 0; k < 16; ++k)
-         coef[k] = c_aspc[((nualt - 1 - k) % 16 + 16) % 16];
+      for (int k = 0; k < depth; ++k) {
+         const int j = ((nualt - 1 - k) % depth + depth) % depth;
+         coef[k] = predictor == 1 ? c_aspc[j] : c_gear[j];
+      }
    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.ne; e += gridDim.x * blockDim.x) {
       const int s = e / 6, x = e + 2 * s;  // row s, component e - 6 s of [npad][8]
       const float pol = A.polar[s];
@@ -66,7 +74,7 @@ __global__ void k_init_guess(VecArgs A, const float* __restrict__ fld, float* __
       float u = 0.f;
       if (predict) {
          double v = 0;
-         for (int k = 0; k < 16; ++k)
+         for (int k = 0; k < depth; ++k)
             v += coef[k] * (double)hist[(size_t)k * A.ne8 + x];
          u = (float)v;
       } else if (pcgguess) {
@@ -223,19 +231,20 @@ __global__ void k_pcg_p4(VecArgs A, const double* __restrict__ scal, const int* 
 }
 
 // predictor ring save (ulspredSave, src/amoeba/induce.cpp:29-63)
-__global__ void k_save_hist(int ne, const float* __restrict__ uind, float* __restrict__ hist, int* __restrict__ state)
+__global__ void k_save_hist(int ne, int depth, const float* __restrict__ uind, float* __restrict__ hist,
+   int* __restrict__ state)
 {
-   const int slot = state[ST_NUALT] % 16;
+   const int slot = state[ST_NUALT] % depth;
    float* dst = hist + (size_t)slot * ne;
    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ne; i += gridDim.x * blockDim.x)
       dst[i] = uind[i];
 }
 
-__global__ void k_bump_nualt(int* state)
+__global__ void k_bump_nualt(int* state, int depth)
 {
    int v = state[ST_NUALT] + 1;
-   if (v > 32)
-      v -= 16;
+   if (v > 2 * depth)
+      v -= depth;
    state[ST_NUALT] = v;
 }
 
@@ -436,7 +445,7 @@ static int pcg_start(Context* ctx, const VecArgs& A, bool graph, int variant)
    T9_CHECK(graph ? list_refresh_graph(ctx) : ensure_list(ctx));
    T9_CHECK(dfield6(ctx, ctx->fld6));
    k_init_guess<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->fld6, ctx->efield, ctx->udir, ctx->uind, c.pcgguess,
-      c.predictor == 1 ? 1 : 0, ctx->aspc_hist, ctx->status);
+      c.predictor, ctx->aspc_hist, ctx->status);
    // the network runs when its guess is used or when this solve trains it
    if ((ctx->learn_mode & 1) || variant != V_PLAIN)
       T9_CHECK(learn_forward(ctx));
@@ -444,7 +453,7 @@ static int pcg_start(Context* ctx, const VecArgs& A, bool graph, int variant)
       T9_CHECK(learn_guess(ctx, ctx->uind, 1));
    else if (variant == V_COMPARE)
       T9_CHECK(learn_guess(ctx, ctx->tmp6, 0));
-   const bool zero_guess = !c.pcgguess && c.predictor != 1 && variant != V_LEARNED;
+   const bool zero_guess = !c.pcgguess && pred_depth(c) == 0 && variant != V_LEARNED;
    if (!zero_guess)
       T9_CHECK(ufield6(ctx, ctx->uind, ctx->fld6));
    k_init_rsd<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->fld6, ctx->efield, ctx->udir, ctx->uind, ctx->rsd,
@@ -466,9 +475,9 @@ static int pcg_finish(Context* ctx, const VecArgs& A)
 {
    if (ctx->learn_mode & 1)
       T9_CHECK(learn_train(ctx));
-   if (ctx->cfg.predictor == 1) {
-      k_save_hist<<<A.nb, VB, 0, ctx->stream>>>(A.ne8, ctx->uind, ctx->aspc_hist, ctx->status);
-      k_bump_nualt<<<1, 1, 0, ctx->stream>>>(ctx->status);
+   if (pred_depth(ctx->cfg) > 0) {
+      k_save_hist<<<A.nb, VB, 0, ctx->stream>>>(A.ne8, pred_depth(ctx->cfg), ctx->uind, ctx->aspc_hist, ctx->status);
+      k_bump_nualt<<<1, 1, 0, ctx->stream>>>(ctx->status, pred_depth(ctx->cfg));
    }
    T9_CUDA(cudaMemcpyAsync(ctx->h_status, ctx->status, sizeof(int) * ST_NSTAT, cudaMemcpyDeviceToHost, ctx->stream));
    T9_CUDA(cudaMemcpyAsync(ctx->h_scal, ctx->scal, sizeof(double) * S_NSCAL, cudaMemcpyDeviceToHost, ctx->stream));
@@ -611,7 +620,7 @@ int induce_sorted(Context* ctx)
       if (!redo)
          break;
       // the overflowed solve saved a history frame: drop it
-      if (ctx->cfg.predictor == 1) {
+      if (pred_depth(ctx->cfg) > 0) {
          T9_CUDA(cudaMemcpy(ctx->h_status, ctx->status, sizeof(int) * ST_NSTAT, cudaMemcpyDeviceToHost));
          int v = ctx->h_status[ST_NUALT] - 1;
          T9_CUDA(cudaMemcpy(ctx->status + ST_NUALT, &v, sizeof(int), cudaMemcpyHostToDevice));
@@ -629,7 +638,7 @@ int induce_sorted(Context* ctx)
       ctx->learn_since_probe += 1;
    }
    // the plain start changes character once the predictor history is full
-   const bool full = ctx->cfg.predictor == 1 && ctx->h_status[ST_NUALT] >= 16;
+   const bool full = pred_depth(ctx->cfg) > 0 && ctx->h_status[ST_NUALT] >= pred_depth(ctx->cfg);
    if (full != ctx->learn_ring_full)
       ctx->learn_since_probe = 1 << 30;
    ctx->learn_ring_full = full;
