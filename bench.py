@@ -49,7 +49,9 @@ def parse():
     ap.add_argument("--no-forces", action="store_true")
     ap.add_argument("--no-large", action="store_true", help="skip the 98,304-atom leg")
     ap.add_argument("--large-config", default="water98304")
-    ap.add_argument("--own-fft", action="store_true", help="the library's fused transform instead of cuFFT")
+    ap.add_argument("--fft", choices=["auto", "own", "cufft"], default="auto",
+                    help="PME transform: the library's default (its fused transform on cubic 32/64 grids, cuFFT "
+                    "otherwise), the fused transform, or cuFFT")
     ap.add_argument("--lanes", type=int, default=8, help="lanes per atom in the real-space field kernels")
     ap.add_argument("--no-flush", action="store_true",
                     help="skip the 512 MB L2 flush buffer (for ncu captures only; numbers are not bench values)")
@@ -252,6 +254,8 @@ def large_leg(args, abi, tg, stream, flush, peak):
     tr = tg.systems.Trajectory(s, seed=17)
     eng = abi.Engine(s, predictor=1, stream=stream)
     eng.prepare(tr.frame(0))
+    if args.fft != "auto":
+        eng.pme_own_fft(args.fft == "own")
     K, W, H = args.steps, args.warmup, args.history
     dev = torch.from_numpy(np.stack([tr.frame(t) for t in range(H + W + 2 * K)]).astype(np.float32)).to("cuda")
     ud = torch.zeros((s.n, 3), device="cuda")
@@ -398,8 +402,8 @@ def main():
     stream = torch.cuda.Stream()
     eng = abi.Engine(s, predictor=pred, stream=stream)
     eng.prepare(tr.frame(0))
-    if args.own_fft:
-        eng.pme_own_fft(True)
+    if args.fft != "auto":
+        eng.pme_own_fft(args.fft == "own")
     eng.pair_lanes(args.lanes)
     # frames: predictor history, warm-up, then the timed, e2e, per-kernel and
     # force passes, each continuing the trajectory (no time jumps for the predictor)
@@ -546,7 +550,8 @@ def main():
             "config": {
                 "workload": args.config, "atoms": s.n, "pme_grid": list(s.settings["nfft"]), "cutoff_A": 7.0,
                 "poleps_debye": s.settings["poleps"], "predictor": args.predictor, "history_frames": args.history,
-                "fft": "fused power-of-two transform (library)" if args.own_fft else "cuFFT C2C",
+                "fft": {"auto": "library default: fused transform on cubic 32/64 grids, cuFFT C2C otherwise",
+                        "own": "fused power-of-two transform (library)", "cufft": "cuFFT C2C"}[args.fft],
                 "lanes_per_atom": args.lanes,
                 "l2": "not flushed (profiling run)" if args.no_flush else "flushed (512 MB write) between timed steps",
                 "parallelism": f"replicas x{world}",

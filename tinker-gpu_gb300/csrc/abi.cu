@@ -74,6 +74,11 @@ static int alloc_all(Context* ctx)
    T9_CUDA(cudaMallocHost(&ctx->h_stage, ctx->h_stage_bytes));
    T9_CUDA(cudaMallocHost(&ctx->h_in, sizeof(float) * 3 * (size_t)npad));
    T9_CUDA(cudaEventCreateWithFlags(&ctx->ev_in, cudaEventDisableTiming));
+   for (int k = 0; k < 2; ++k) {
+      T9_CUDA(cudaStreamCreateWithFlags(&ctx->side_stream[k], cudaStreamNonBlocking));
+      T9_CUDA(cudaEventCreateWithFlags(&ctx->ev_fork[k], cudaEventDisableTiming));
+      T9_CUDA(cudaEventCreateWithFlags(&ctx->ev_join[k], cudaEventDisableTiming));
+   }
    // the legacy-stream memsets above must finish before work on the caller's
    // (possibly non-blocking) stream
    T9_CUDA(cudaDeviceSynchronize());
@@ -111,6 +116,14 @@ static void free_all(Context* ctx)
    drop_graphs(ctx);
    if (ctx->cap_stream)
       cudaStreamDestroy(ctx->cap_stream);
+   for (int k = 0; k < 2; ++k) {
+      if (ctx->side_stream[k])
+         cudaStreamDestroy(ctx->side_stream[k]);
+      if (ctx->ev_fork[k])
+         cudaEventDestroy(ctx->ev_fork[k]);
+      if (ctx->ev_join[k])
+         cudaEventDestroy(ctx->ev_join[k]);
+   }
    for (auto& e : ctx->prof.ev)
       cudaEventDestroy(e);
    if (ctx->own_stream && ctx->stream)

@@ -24,8 +24,25 @@ constexpr int GROUP = 16;  // lanes per atom in the real-space kernels
 constexpr double FX_SCALE = 1099511627776.0;  // 2^40
 constexpr double FX_INV = 1.0 / 1099511627776.0;
 
-__device__ __forceinline__ long long to_fx(float v) { return __float2ll_rn(v * 1099511627776.0f); }
-__device__ __forceinline__ float from_fx(long long v) { return (float)((double)v * FX_INV); }
+// Conversions in 32-bit arithmetic (64-bit conversions and FP64 are slow
+// paths on this GPU).  to_fx: y = v 2^8 = hi + frac with hi = floor(y) and
+// frac in [0, 1) exact, so hi 2^32 + rn(frac 2^32) = rn(v 2^40), the value
+// a direct float -> int64 conversion gives (|v| < 2^23).  from_fx:
+// v 2^-40 = hi 2^-8 + lo 2^-40 for v = hi 2^32 + lo, within one rounding of
+// the correctly rounded float.
+__device__ __forceinline__ long long to_fx(float v)
+{
+   const float y = v * 256.0f;
+   const int hi = __float2int_rd(y);
+   const unsigned lo = __float2uint_rn((y - (float)hi) * 4294967296.0f);
+   return (long long)(((unsigned long long)(long long)hi << 32) + lo);
+}
+__device__ __forceinline__ float from_fx(long long v)
+{
+   const int hi = (int)(v >> 32);
+   const unsigned lo = (unsigned)(v & 0xffffffffll);
+   return fmaf(__uint2float_rn(lo), 9.094947017729282e-13f, __int2float_rn(hi) * 0.00390625f);
+}
 
 // Complementary error function, Hastings' rational approximation (C. Hastings,
 // Approximations for Digital Computers, Princeton 1955, p. 167; Abramowitz &
@@ -245,6 +262,13 @@ struct Context {
    bool use_graph = true;
    cudaGraphExec_t graph_exec[3] = {nullptr, nullptr, nullptr};  // per start variant (pcg.cu)
    cudaStream_t cap_stream = nullptr;
+   // second streams for the reciprocal grid half of a field evaluation, run
+   // beside the real-space pair kernel (fork / join by events).  A stream
+   // that joined a graph capture stays in it until that capture ends, so the
+   // WHILE-body capture (on cap_stream) has its own side stream: [1] there,
+   // [0] everywhere else.
+   cudaStream_t side_stream[2] = {nullptr, nullptr};
+   cudaEvent_t ev_fork[2] = {nullptr, nullptr}, ev_join[2] = {nullptr, nullptr};
 
    // last induce statistics
    int last_iter = 0;
@@ -334,6 +358,10 @@ int launch_precond_sparse(Context* ctx, const float* r6, float* z6);
 // reciprocal space (pme.cu): out6 = recip + self field (plain store)
 int launch_dfield_recip(Context* ctx, float* out6);
 int launch_ufield_recip(Context* ctx, const float* u6, float* out6);
+int launch_dfield_recip_grid(Context* ctx);
+int launch_dfield_recip_gather(Context* ctx, float* out6, bool acc);
+int launch_ufield_recip_grid(Context* ctx, const float* u6);
+int launch_ufield_recip_gather(Context* ctx, const float* u6, float* out6, bool acc);
 
 // energies: per-atom FP64 terms (pair.cu real space, pme.cu recip + self)
 int launch_empole_real(Context* ctx, double* e_atom);

@@ -400,18 +400,67 @@ int check_list_overflow(Context* ctx, int* redo)
    return T9GB_OK;
 }
 
+// The reciprocal grid (spread + transform) runs on the side stream while the
+// real-space pair kernel runs on ctx->stream; after the join the gather adds
+// recip + self to the real-space field (the same sum, so the same bits, as
+// the serial order).  Serial while the per-kernel profile is on.
+static int side_index(const Context* ctx)
+{
+   return ctx->cap_stream && ctx->stream == ctx->cap_stream ? 1 : 0;
+}
+
+static int recip_fork(Context* ctx, int k)
+{
+   T9_CUDA(cudaEventRecord(ctx->ev_fork[k], ctx->stream));
+   T9_CUDA(cudaStreamWaitEvent(ctx->side_stream[k], ctx->ev_fork[k], 0));
+   return T9GB_OK;
+}
+
+static int recip_join(Context* ctx, int k)
+{
+   T9_CUDA(cudaEventRecord(ctx->ev_join[k], ctx->side_stream[k]));
+   T9_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->ev_join[k], 0));
+   return T9GB_OK;
+}
+
 static int ufield6(Context* ctx, const float* u6, float* out6)
 {
-   T9_CHECK(launch_ufield_recip(ctx, u6, ctx->rcp6));
-   T9_CHECK(launch_ufield_real(ctx, u6, ctx->cfg.use_ewald ? ctx->rcp6 : nullptr, out6));
-   return T9GB_OK;
+   if (!ctx->cfg.use_ewald)
+      return launch_ufield_real(ctx, u6, nullptr, out6);
+   if (ctx->prof.on) {
+      T9_CHECK(launch_ufield_recip(ctx, u6, ctx->rcp6));
+      return launch_ufield_real(ctx, u6, ctx->rcp6, out6);
+   }
+   const int k = side_index(ctx);
+   T9_CHECK(recip_fork(ctx, k));
+   cudaStream_t main = ctx->stream;
+   ctx->stream = ctx->side_stream[k];
+   const int rc = launch_ufield_recip_grid(ctx, u6);
+   ctx->stream = main;
+   T9_CHECK(rc);
+   T9_CHECK(launch_ufield_real(ctx, u6, nullptr, out6));
+   T9_CHECK(recip_join(ctx, k));
+   return launch_ufield_recip_gather(ctx, u6, out6, true);
 }
 
 static int dfield6(Context* ctx, float* out6)
 {
-   T9_CHECK(launch_dfield_recip(ctx, ctx->rcp6));
-   T9_CHECK(launch_dfield_real(ctx, ctx->cfg.use_ewald ? ctx->rcp6 : nullptr, out6));
-   return T9GB_OK;
+   if (!ctx->cfg.use_ewald)
+      return launch_dfield_real(ctx, nullptr, out6);
+   if (ctx->prof.on) {
+      T9_CHECK(launch_dfield_recip(ctx, ctx->rcp6));
+      return launch_dfield_real(ctx, ctx->rcp6, out6);
+   }
+   const int k = side_index(ctx);
+   T9_CHECK(recip_fork(ctx, k));
+   cudaStream_t main = ctx->stream;
+   ctx->stream = ctx->side_stream[k];
+   const int rc = launch_dfield_recip_grid(ctx);
+   ctx->stream = main;
+   T9_CHECK(rc);
+   T9_CHECK(launch_dfield_real(ctx, nullptr, out6));
+   T9_CHECK(recip_join(ctx, k));
+   return launch_dfield_recip_gather(ctx, out6, true);
 }
 
 static int pcg_body(Context* ctx, const VecArgs& A, cudaGraphConditionalHandle handle, int use_handle)

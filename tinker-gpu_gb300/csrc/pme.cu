@@ -254,7 +254,7 @@ __global__ void k_conv(size_t ng, const float* __restrict__ infl, float2* __rest
 // a fixed xor tree combines the rows.  MODE 0: real part -> d and p field,
 // self term with the permanent dipole.  MODE 1: real -> d, imaginary -> p,
 // self term with the induced dipoles.  Plain stores, rows of 8 floats.
-template <int MODE>
+template <int MODE, bool ACC>
 __global__ void __launch_bounds__(256) k_gather_field(int n, GridParams G, const float4* __restrict__ spos,
    const float2* __restrict__ g, const float* __restrict__ rp, const float* __restrict__ u8, float* __restrict__ out)
 {
@@ -308,26 +308,26 @@ __global__ void __launch_bounds__(256) k_gather_field(int n, GridParams G, const
    if (lane != 0)
       return;
    float* a = out + 8 * s;
+   float r[6];
    if (MODE == 0) {
       const float* m = rp + 12 * s;
-      const float fx = -G.a1 * acc[0] + G.selfterm * m[1];
-      const float fy = -G.a2 * acc[1] + G.selfterm * m[2];
-      const float fz = -G.a3 * acc[2] + G.selfterm * m[3];
-      a[0] = fx;
-      a[1] = fy;
-      a[2] = fz;
-      a[3] = fx;
-      a[4] = fy;
-      a[5] = fz;
+      r[0] = r[3] = -G.a1 * acc[0] + G.selfterm * m[1];
+      r[1] = r[4] = -G.a2 * acc[1] + G.selfterm * m[2];
+      r[2] = r[5] = -G.a3 * acc[2] + G.selfterm * m[3];
    } else {
       const float* u = u8 + 8 * s;
-      a[0] = G.selfterm * u[0] - G.a1 * acc[0];
-      a[1] = G.selfterm * u[1] - G.a2 * acc[1];
-      a[2] = G.selfterm * u[2] - G.a3 * acc[2];
-      a[3] = G.selfterm * u[3] - G.a1 * acc[3];
-      a[4] = G.selfterm * u[4] - G.a2 * acc[4];
-      a[5] = G.selfterm * u[5] - G.a3 * acc[5];
+      r[0] = G.selfterm * u[0] - G.a1 * acc[0];
+      r[1] = G.selfterm * u[1] - G.a2 * acc[1];
+      r[2] = G.selfterm * u[2] - G.a3 * acc[2];
+      r[3] = G.selfterm * u[3] - G.a1 * acc[3];
+      r[4] = G.selfterm * u[4] - G.a2 * acc[4];
+      r[5] = G.selfterm * u[5] - G.a3 * acc[5];
    }
+   // ACC: add to the real-space field already stored (the same two-operand
+   // sum the real-space kernel forms when it adds this result as its base)
+#pragma unroll
+   for (int c = 0; c < 6; ++c)
+      a[c] = ACC ? a[c] + r[c] : r[c];
 }
 
 // Multipole reciprocal + self energy per atom (warp per atom, level-3
@@ -404,154 +404,263 @@ __global__ void __launch_bounds__(256) k_empole_recip_self(int n, GridParams G, 
 }
 
 // ---------------------------------------------------------------------------
-// Fused 3-D FFT for power-of-two grids (16..128 points per edge), replacing
-// the 6 cuFFT kernels + fixed-point conversion + convolution of one pass by
-// five single-axis passes.  Each block transforms 16 lines of one axis in
-// shared memory (element i of line l at sm[i * 17 + l]; consecutive threads
-// take consecutive lines, so butterflies hit distinct banks), with the
-// bit reversal folded into the load (decimation in time) or the store
-// (decimation in frequency):
-//   x forward  (reads the fixed-point grid and clears it),
-//   y forward,
-//   z forward, influence function, z inverse  (MODE 2; the virial path
-//     splits it into z forward / z inverse around the k-space pass),
-//   y inverse, x inverse.
-// Forward e^{-2 pi i k n / N}, inverse unnormalised, as cuFFT's C2C.  The
-// twiddles come from a table computed in double precision.
+// Fused 3-D FFT + convolution for cubic power-of-two grids (N = 32, 64, 128
+// points per edge), replacing cuFFT's six kernels plus the fixed-point
+// conversion and the convolution of one pass by three kernels:
+//   k_fft_plane<FROM_FX, forward>: fixed-point grid -> float (the fixed-point
+//     grid is cleared for the next spread), 2-D forward FFT of each z plane;
+//   k_fft_zline<MODE 2>: forward FFT along z, times the influence function,
+//     inverse FFT along z, for 16 x-adjacent lines per block (the virial path
+//     splits it into MODE 0 forward / MODE 1 inverse around the k-space pass);
+//   k_fft_plane<inverse>: 2-D inverse FFT of each plane.
+// A line transform of N = N1 x T points runs on T threads (8; 4 for N = 32)
+// of one warp, each holding N1 points in registers: an N1-point DFT over the
+// stride-T subsequence, the twiddle W_N^(t k1), an exchange through shared
+// memory, then N1 / T T-point DFTs per thread (Cooley-Tukey with
+// n = n1 T + n2, k = k1 + N1 k2).  Forward e^{-2 pi i k n / N}, inverse
+// unnormalised, as cuFFT's C2C; the twiddles come from a table computed in
+// double precision.
 
 __constant__ float2 c_tw[128];  // e^{-2 pi i k / 128}
-constexpr int FFT_L = 16;       // lines per block
 
 __device__ __forceinline__ float2 cmulf(float2 a, float2 b)
 {
    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
-__device__ __forceinline__ int brev(int x, int logn)
+__host__ __device__ constexpr int brev_c(int x, int bits)
 {
-   return (int)(__brev((unsigned)x) >> (32 - logn));
+   int r = 0;
+   for (int b = 0; b < bits; ++b) {
+      r = (r << 1) | (x & 1);
+      x >>= 1;
+   }
+   return r;
 }
 
-// FFT_L lines of length 2^logN at a[i * (FFT_L + 1) + l]; DIT: bit-reversed
-// input, natural output; DIF: natural input, bit-reversed output
-template <bool DIT, bool INV>
-__device__ void fft_lines(float2* a, const float2* tw, int logN)
+__host__ __device__ constexpr int log2_c(int m) { return m <= 1 ? 0 : 1 + log2_c(m / 2); }
+
+// in-register M-point DFT (M = 4, 8, 16), natural order in and out;
+// tw: e^{-2 pi i k / 128} in shared memory (uniform indices: broadcasts)
+template <int M, bool INV>
+__device__ __forceinline__ void dft_reg(float2* v, const float2* tw)
 {
-   constexpr int ld = FFT_L + 1;
-   const int nb = FFT_L << (logN - 1);
-   for (int t = 0; t < logN; ++t) {
-      const int s = DIT ? t + 1 : logN - t;
-      const int half = 1 << (s - 1), tws = 128 >> s;
-      for (int b = threadIdx.x; b < nb; b += blockDim.x) {
-         const int l = b & (FFT_L - 1), j = b >> 4;
-         const int k = j & (half - 1);
-         const int i0 = ((j >> (s - 1)) << s) + k;
-         float2 w = tw[k * tws];
-         if (INV)
-            w.y = -w.y;
-         float2* p0 = a + i0 * ld + l;
-         float2* p1 = p0 + half * ld;
-         const float2 x0 = *p0, x1 = *p1;
-         if (DIT) {
-            const float2 v = cmulf(w, x1);
-            *p0 = make_float2(x0.x + v.x, x0.y + v.y);
-            *p1 = make_float2(x0.x - v.x, x0.y - v.y);
-         } else {
-            *p0 = make_float2(x0.x + x1.x, x0.y + x1.y);
-            *p1 = cmulf(w, make_float2(x0.x - x1.x, x0.y - x1.y));
+   constexpr int L = log2_c(M);
+#pragma unroll
+   for (int i = 0; i < M; ++i) {
+      const int j = brev_c(i, L);
+      if (j > i) {
+         const float2 a = v[i];
+         v[i] = v[j];
+         v[j] = a;
+      }
+   }
+#pragma unroll
+   for (int st = 1; st <= L; ++st) {
+      const int len = 1 << st, half = len / 2, step = 128 / len;
+#pragma unroll
+      for (int b = 0; b < M; b += len)
+#pragma unroll
+         for (int k = 0; k < half; ++k) {
+            float2 w = tw[k * step];
+            if (INV)
+               w.y = -w.y;
+            const float2 a = v[b + k];
+            const float2 c = k == 0 ? v[b + k + half] : cmulf(w, v[b + k + half]);
+            v[b + k] = make_float2(a.x + c.x, a.y + c.y);
+            v[b + k + half] = make_float2(a.x - c.x, a.y - c.y);
+         }
+   }
+}
+
+// One N-point line at line[i * ls], transformed in place by the T threads
+// t = 0..T-1 of one warp (every thread of the warp takes part in some line).
+template <int N, int T, bool INV>
+__device__ __forceinline__ void fft_line(float2* line, int ls, int t, const float2* tw)
+{
+   constexpr int N1 = N / T, J = N1 / T;
+   float2 v[N1];
+#pragma unroll
+   for (int n1 = 0; n1 < N1; ++n1)
+      v[n1] = line[(n1 * T + t) * ls];
+   dft_reg<N1, INV>(v, tw);
+#pragma unroll
+   for (int k1 = 1; k1 < N1; ++k1) {
+      float2 w = tw[((t * k1) & (N - 1)) * (128 / N)];
+      if (INV)
+         w.y = -w.y;
+      v[k1] = cmulf(v[k1], w);
+   }
+   __syncwarp();
+#pragma unroll
+   for (int k1 = 0; k1 < N1; ++k1)
+      line[(k1 * T + t) * ls] = v[k1];
+   __syncwarp();
+   float2 u[J][T];
+#pragma unroll
+   for (int j = 0; j < J; ++j) {
+      const int k1 = t * J + j;
+#pragma unroll
+      for (int n2 = 0; n2 < T; ++n2)
+         u[j][n2] = line[(k1 * T + n2) * ls];
+      dft_reg<T, INV>(u[j], tw);
+   }
+   __syncwarp();
+#pragma unroll
+   for (int j = 0; j < J; ++j)
+#pragma unroll
+      for (int k2 = 0; k2 < T; ++k2)
+         line[(t * J + j + N1 * k2) * ls] = u[j][k2];
+   __syncwarp();
+}
+
+template <int N>
+__host__ __device__ constexpr int fft_threads_per_line()
+{
+   return N == 32 ? 4 : 8;
+}
+
+// 2-D FFT (x then y) of z plane blockIdx.x; N * T threads, dynamic shared
+// memory N (N + 1) + 128 float2
+template <int N, bool FROM_FX, bool INV>
+__global__ void __launch_bounds__(N * fft_threads_per_line<N>()) k_fft_plane(long long* __restrict__ qfx,
+   float2* __restrict__ g)
+{
+   constexpr int T = fft_threads_per_line<N>(), LD = N + 1, NT = N * T, R = N / T;
+   extern __shared__ float2 fsm[];
+   float2* tw = fsm + N * LD;
+   for (int k = threadIdx.x; k < 128; k += NT)
+      tw[k] = c_tw[k];
+   const size_t base = (size_t)blockIdx.x * N * N;
+   // element e = threadIdx.x + r NT, r < R: all loads of a chunk in flight together
+#pragma unroll
+   for (int c = 0; c < R; c += 8) {
+      float2 v[8];
+      if (FROM_FX) {
+         longlong2* q = reinterpret_cast<longlong2*>(qfx) + base + threadIdx.x;
+         longlong2 f[8];
+#pragma unroll
+         for (int r = 0; r < 8; ++r)
+            f[r] = q[(c + r) * NT];
+#pragma unroll
+         for (int r = 0; r < 8; ++r) {
+            q[(c + r) * NT] = make_longlong2(0, 0);
+            v[r] = make_float2(from_fx(f[r].x), from_fx(f[r].y));
+         }
+      } else {
+#pragma unroll
+         for (int r = 0; r < 8; ++r)
+            v[r] = g[base + threadIdx.x + (c + r) * NT];
+      }
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+         const int e = threadIdx.x + (c + r) * NT;
+         fsm[(e / N) * LD + (e % N)] = v[r];
+      }
+   }
+   __syncthreads();
+   const int line = threadIdx.x / T, t = threadIdx.x % T;
+   fft_line<N, T, INV>(fsm + line * LD, 1, t, tw);  // row y = line, along x
+   __syncthreads();
+   fft_line<N, T, INV>(fsm + line, LD, t, tw);  // column x = line, along y
+   __syncthreads();
+#pragma unroll
+   for (int r = 0; r < R; ++r) {
+      const int e = threadIdx.x + r * NT;
+      g[base + e] = fsm[(e / N) * LD + (e % N)];
+   }
+}
+
+// Lines along z of 16 adjacent x at one y.  MODE 0 forward, 1 inverse,
+// 2 forward, influence function, inverse.
+template <int N, int MODE>
+__global__ void __launch_bounds__(16 * fft_threads_per_line<N>()) k_fft_zline(const float* __restrict__ infl,
+   float2* __restrict__ g)
+{
+   constexpr int T = fft_threads_per_line<N>(), XL = 16, LD = XL + 1, NT = XL * T, R = N / T;
+   __shared__ float2 sm[N * LD];
+   __shared__ float2 tw[128];
+   for (int k = threadIdx.x; k < 128; k += NT)
+      tw[k] = c_tw[k];
+   const int xb = (blockIdx.x % (N / XL)) * XL, y = blockIdx.x / (N / XL);
+   const size_t base = (size_t)y * N + xb, zs = (size_t)N * N;
+   // element e = threadIdx.x + r NT of the [z][16] tile: z = e / 16, x = e % 16
+   const int ex = threadIdx.x % XL, ez = threadIdx.x / XL;
+   constexpr int ZS = NT / XL;  // z rows per r step
+#pragma unroll
+   for (int c = 0; c < R; c += 8) {
+      float2 v[8];
+#pragma unroll
+      for (int r = 0; r < 8; ++r)
+         v[r] = g[base + (size_t)(ez + (c + r) * ZS) * zs + ex];
+#pragma unroll
+      for (int r = 0; r < 8; ++r)
+         sm[(ez + (c + r) * ZS) * LD + ex] = v[r];
+   }
+   __syncthreads();
+   const int line = threadIdx.x / T, t = threadIdx.x % T;
+   if (MODE != 1)
+      fft_line<N, T, false>(sm + line, LD, t, tw);
+   if (MODE == 2) {
+      __syncthreads();
+#pragma unroll
+      for (int c = 0; c < R; c += 8) {
+         float f[8];
+#pragma unroll
+         for (int r = 0; r < 8; ++r)
+            f[r] = infl[base + (size_t)(ez + (c + r) * ZS) * zs + ex];
+#pragma unroll
+         for (int r = 0; r < 8; ++r) {
+            float2& v = sm[(ez + (c + r) * ZS) * LD + ex];
+            v = make_float2(v.x * f[r], v.y * f[r]);
          }
       }
       __syncthreads();
    }
-}
-
-// AXIS 0 x, 1 y, 2 z.  MODE 0 forward, 1 inverse, 2 forward + influence
-// function + inverse (z), 3 forward from the fixed-point grid (x)
-template <int AXIS, int MODE>
-__global__ void __launch_bounds__(256) k_fft_line(int n1, int n2, int n3, int logN, const float* __restrict__ infl,
-   long long* __restrict__ qfx, float2* __restrict__ g)
-{
-   __shared__ float2 sm[128 * (FFT_L + 1)];
-   __shared__ float2 tw[128];
-   for (int k = threadIdx.x; k < 128; k += blockDim.x)
-      tw[k] = c_tw[k];
-   constexpr int ld = FFT_L + 1;
-   const int N = 1 << logN;
-   size_t base, lstr, istr;
-   if (AXIS == 0) {
-      const int rows = n2 / FFT_L;
-      base = ((size_t)(blockIdx.x / rows) * n2 + (blockIdx.x % rows) * FFT_L) * n1;
-      lstr = n1;
-      istr = 1;
-   } else if (AXIS == 1) {
-      const int cols = n1 / FFT_L;
-      base = (size_t)(blockIdx.x / cols) * n2 * n1 + (blockIdx.x % cols) * FFT_L;
-      lstr = 1;
-      istr = n1;
-   } else {
-      const int cols = n1 / FFT_L;
-      base = (size_t)(blockIdx.x / cols) * n1 + (blockIdx.x % cols) * FFT_L;
-      lstr = 1;
-      istr = (size_t)n1 * n2;
-   }
-   const bool dit_in = MODE != 1;  // decimation in time first: bit-reversed load
-   for (int e = threadIdx.x; e < FFT_L * N; e += blockDim.x) {
-      int i, l;
-      if (AXIS == 0) {
-         i = e & (N - 1);
-         l = e >> logN;
-      } else {
-         l = e & (FFT_L - 1);
-         i = e >> 4;
-      }
-      const size_t ga = base + l * lstr + i * istr;
-      float2 v;
-      if (MODE == 3) {
-         longlong2* q = reinterpret_cast<longlong2*>(qfx) + ga;
-         const longlong2 f = *q;
-         *q = make_longlong2(0, 0);
-         v = make_float2(from_fx(f.x), from_fx(f.y));
-      } else {
-         v = g[ga];
-      }
-      sm[(dit_in ? brev(i, logN) : i) * ld + l] = v;
-   }
+   if (MODE != 0)
+      fft_line<N, T, true>(sm + line, LD, t, tw);
    __syncthreads();
-   if (MODE == 0 || MODE == 3) {
-      fft_lines<true, false>(sm, tw, logN);
-   } else if (MODE == 1) {
-      fft_lines<false, true>(sm, tw, logN);
-   } else {
-      fft_lines<true, false>(sm, tw, logN);
-      for (int e = threadIdx.x; e < FFT_L * N; e += blockDim.x) {
-         const int l = e & (FFT_L - 1), i = e >> 4;
-         const float f = infl[base + l * lstr + i * istr];
-         float2& v = sm[i * ld + l];
-         v = make_float2(v.x * f, v.y * f);
-      }
-      __syncthreads();
-      fft_lines<false, true>(sm, tw, logN);
-   }
-   const bool natural_out = MODE == 0 || MODE == 3;
-   for (int e = threadIdx.x; e < FFT_L * N; e += blockDim.x) {
-      int i, l;
-      if (AXIS == 0) {
-         i = e & (N - 1);
-         l = e >> logN;
-      } else {
-         l = e & (FFT_L - 1);
-         i = e >> 4;
-      }
-      g[base + l * lstr + i * istr] = sm[(natural_out ? i : brev(i, logN)) * ld + l];
-   }
+#pragma unroll
+   for (int r = 0; r < R; ++r)
+      g[base + (size_t)(ez + r * ZS) * zs + ex] = sm[(ez + r * ZS) * LD + ex];
 }
 
-static int ilog2_exact(int n)
+template <int N>
+static size_t fft_plane_smem()
 {
-   int l = 0;
-   while ((1 << l) < n)
-      ++l;
-   return (1 << l) == n ? l : -1;
+   return sizeof(float2) * ((size_t)N * (N + 1) + 128);
+}
+
+template <int N>
+static int fft_setup_kernels(Context* ctx)
+{
+   const int bytes = (int)fft_plane_smem<N>();
+   void (*fwd)(long long*, float2*) = k_fft_plane<N, true, false>;
+   void (*inv)(long long*, float2*) = k_fft_plane<N, false, true>;
+   T9_CUDA(cudaFuncSetAttribute(fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+   T9_CUDA(cudaFuncSetAttribute(inv, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+   return T9GB_OK;
+}
+
+// forward planes; vir: the z pass stops after the forward transform
+template <int N>
+static void fft_own_forward(const PmeGrid& P, cudaStream_t st, bool split)
+{
+   constexpr int T = fft_threads_per_line<N>();
+   k_fft_plane<N, true, false><<<N, N * T, fft_plane_smem<N>(), st>>>(P.qfx, P.qgrid);
+   if (split)
+      k_fft_zline<N, 0><<<N * N / 16, 16 * T, 0, st>>>(P.infl, P.qgrid);
+   else
+      k_fft_zline<N, 2><<<N * N / 16, 16 * T, 0, st>>>(P.infl, P.qgrid);
+}
+
+template <int N>
+static void fft_own_inverse(const PmeGrid& P, cudaStream_t st, bool split)
+{
+   constexpr int T = fft_threads_per_line<N>();
+   if (split)
+      k_fft_zline<N, 1><<<N * N / 16, 16 * T, 0, st>>>(P.infl, P.qgrid);
+   k_fft_plane<N, false, true><<<N, N * T, fft_plane_smem<N>(), st>>>(P.qfx, P.qgrid);
 }
 
 // ---------------------------------------------------------------------------
@@ -1009,12 +1118,18 @@ int pme_setup(Context* ctx)
       ctx->last_error = "cufftPlan3d failed";
       return T9GB_CUDA_ERR;
    }
-   // the fused FFT: powers of two, 16..128 per edge
-   auto pow2 = [](int v) { return v >= 16 && v <= 128 && (v & (v - 1)) == 0; };
-   P.own_fft_ok = pow2(P.n1) && pow2(P.n2) && pow2(P.n3);
-   // off by default: on GB300 the 64^3 pass takes 43.5 us against cuFFT's 37 us
-   P.own_fft = false;
+   // the fused FFT: cubic grids of 32, 64 or 128 points per edge
+   P.own_fft_ok = P.n1 == P.n2 && P.n2 == P.n3 && (P.n1 == 32 || P.n1 == 64 || P.n1 == 128);
+   // default where it measured faster than cuFFT on GB300 (64^3: 0.627 vs
+   // 0.634 ms per induce step in the graph); at 128^3 cuFFT is faster
+   P.own_fft = P.own_fft_ok && P.n1 <= 64;
    if (P.own_fft_ok) {
+      if (P.n1 == 32)
+         T9_CHECK(fft_setup_kernels<32>(ctx));
+      else if (P.n1 == 64)
+         T9_CHECK(fft_setup_kernels<64>(ctx));
+      else
+         T9_CHECK(fft_setup_kernels<128>(ctx));
       float2 tw[128];
       for (int k = 0; k < 128; ++k)
          tw[k] = make_float2((float)std::cos(2 * pi * k / 128.0), (float)-std::sin(2 * pi * k / 128.0));
@@ -1082,21 +1197,24 @@ static int fft_conv(Context* ctx, int vir = 0, float wE = 0.f, float wP = 0.f, b
    const int cb = (int)std::min<size_t>((ng + 255) / 256, 152 * 16);
    prof_begin(ctx, P_FFT_CONV);
    if (P.own_fft) {
-      const int l1 = ilog2_exact(P.n1), l2 = ilog2_exact(P.n2), l3 = ilog2_exact(P.n3);
-      const int bx = P.n3 * (P.n2 / FFT_L), by = P.n3 * (P.n1 / FFT_L), bz = P.n2 * (P.n1 / FFT_L);
       cudaStream_t st = ctx->stream;
-      k_fft_line<0, 3><<<bx, 256, 0, st>>>(P.n1, P.n2, P.n3, l1, P.infl, P.qfx, P.qgrid);
-      k_fft_line<1, 0><<<by, 256, 0, st>>>(P.n1, P.n2, P.n3, l2, P.infl, P.qfx, P.qgrid);
-      if (!vir) {
-         k_fft_line<2, 2><<<bz, 256, 0, st>>>(P.n1, P.n2, P.n3, l3, P.infl, P.qfx, P.qgrid);
-      } else {
-         k_fft_line<2, 0><<<bz, 256, 0, st>>>(P.n1, P.n2, P.n3, l3, P.infl, P.qfx, P.qgrid);
+      const bool split = vir != 0;
+      if (P.n1 == 32)
+         fft_own_forward<32>(P, st, split);
+      else if (P.n1 == 64)
+         fft_own_forward<64>(P, st, split);
+      else
+         fft_own_forward<128>(P, st, split);
+      if (split) {
          T9_CHECK(conv_virial(ctx, vir, wE, wP, stash, out));
          k_conv<<<cb, 256, 0, st>>>(ng, P.infl, P.qgrid);
-         k_fft_line<2, 1><<<bz, 256, 0, st>>>(P.n1, P.n2, P.n3, l3, P.infl, P.qfx, P.qgrid);
       }
-      k_fft_line<1, 1><<<by, 256, 0, st>>>(P.n1, P.n2, P.n3, l2, P.infl, P.qfx, P.qgrid);
-      k_fft_line<0, 1><<<bx, 256, 0, st>>>(P.n1, P.n2, P.n3, l1, P.infl, P.qfx, P.qgrid);
+      if (P.n1 == 32)
+         fft_own_inverse<32>(P, st, split);
+      else if (P.n1 == 64)
+         fft_own_inverse<64>(P, st, split);
+      else
+         fft_own_inverse<128>(P, st, split);
       T9_CUDA(cudaGetLastError());
       prof_end(ctx);
       return T9GB_OK;
@@ -1120,7 +1238,10 @@ static int fft_conv(Context* ctx, int vir = 0, float wE = 0.f, float wP = 0.f, b
    return T9GB_OK;
 }
 
-int launch_dfield_recip(Context* ctx, float* out6)
+// Reciprocal permanent field in two halves: the grid (spread + transform,
+// on ctx->stream) and the gather (recip + self into out6; acc: added to the
+// real-space field stored there)
+int launch_dfield_recip_grid(Context* ctx)
 {
    if (!ctx->cfg.use_ewald)
       return T9GB_OK;
@@ -1130,16 +1251,34 @@ int launch_dfield_recip(Context* ctx, float* out6)
       reinterpret_cast<unsigned long long*>(ctx->pme.qfx));
    prof_end(ctx);
    T9_CUDA(cudaGetLastError());
-   T9_CHECK(fft_conv(ctx));
+   return fft_conv(ctx);
+}
+
+int launch_dfield_recip_gather(Context* ctx, float* out6, bool acc)
+{
+   if (!ctx->cfg.use_ewald)
+      return T9GB_OK;
+   GridParams G = grid_params(ctx);
+   const int nb = grid_for((long long)ctx->n * 32, 256);
    prof_begin(ctx, P_GATHER_MPOLE);
-   k_gather_field<0><<<grid_for((long long)ctx->n * 32, 256), 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->pme.qgrid,
-      ctx->srpole, nullptr, out6);
+   if (acc)
+      k_gather_field<0, true><<<nb, 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->pme.qgrid, ctx->srpole, nullptr,
+         out6);
+   else
+      k_gather_field<0, false><<<nb, 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->pme.qgrid, ctx->srpole,
+         nullptr, out6);
    prof_end(ctx);
    T9_CUDA(cudaGetLastError());
    return T9GB_OK;
 }
 
-int launch_ufield_recip(Context* ctx, const float* u6, float* out6)
+int launch_dfield_recip(Context* ctx, float* out6)
+{
+   T9_CHECK(launch_dfield_recip_grid(ctx));
+   return launch_dfield_recip_gather(ctx, out6, false);
+}
+
+int launch_ufield_recip_grid(Context* ctx, const float* u6)
 {
    if (!ctx->cfg.use_ewald)
       return T9GB_OK;
@@ -1149,13 +1288,29 @@ int launch_ufield_recip(Context* ctx, const float* u6, float* out6)
       reinterpret_cast<unsigned long long*>(ctx->pme.qfx));
    prof_end(ctx);
    T9_CUDA(cudaGetLastError());
-   T9_CHECK(fft_conv(ctx));
+   return fft_conv(ctx);
+}
+
+int launch_ufield_recip_gather(Context* ctx, const float* u6, float* out6, bool acc)
+{
+   if (!ctx->cfg.use_ewald)
+      return T9GB_OK;
+   GridParams G = grid_params(ctx);
+   const int nb = grid_for((long long)ctx->n * 32, 256);
    prof_begin(ctx, P_GATHER_UIND);
-   k_gather_field<1><<<grid_for((long long)ctx->n * 32, 256), 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->pme.qgrid, nullptr,
-      u6, out6);
+   if (acc)
+      k_gather_field<1, true><<<nb, 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->pme.qgrid, nullptr, u6, out6);
+   else
+      k_gather_field<1, false><<<nb, 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->pme.qgrid, nullptr, u6, out6);
    prof_end(ctx);
    T9_CUDA(cudaGetLastError());
    return T9GB_OK;
+}
+
+int launch_ufield_recip(Context* ctx, const float* u6, float* out6)
+{
+   T9_CHECK(launch_ufield_recip_grid(ctx, u6));
+   return launch_ufield_recip_gather(ctx, u6, out6, false);
 }
 
 }  // namespace t9gb
