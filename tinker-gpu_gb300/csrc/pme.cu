@@ -162,10 +162,12 @@ __device__ __forceinline__ void site(const GridParams& G, float4 p, int& i1, int
    i3 += (i3 < 0 ? G.n3 : 0);
 }
 
+// fire-and-forget 64-bit reduction (no value returned, so the warp does not
+// wait on it)
 __device__ __forceinline__ void grid_add(unsigned long long* q, size_t idx, float v)
 {
    if (v != 0.f)
-      atomicAdd(q + idx, (unsigned long long)to_fx(v));
+      asm volatile("red.global.add.u64 [%0], %1;" ::"l"(q + idx), "l"((unsigned long long)to_fx(v)) : "memory");
 }
 
 // Spreading, one warp per atom: lane (jy, kz) < 25 owns one row of five x
