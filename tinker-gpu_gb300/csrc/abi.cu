@@ -14,6 +14,14 @@ int induce_sorted(Context* ctx);
 int public_dfield(Context* ctx, float* field, float* fieldp);
 int public_ufield(Context* ctx, const float* uind, const float* uinp, float* field, float* fieldp);
 int public_precond(Context* ctx, const float* rsd, const float* rsdp, float* zrsd, float* zrsdp);
+
+int stage_dipoles(Context* ctx)
+{
+   const int n = ctx->n;
+   T9_CHECK(scatter_from_sorted3(ctx, ctx->uind, ctx->hout, ctx->hout + 3 * n));
+   T9_CUDA(cudaMemcpyAsync(ctx->h_stage, ctx->hout, sizeof(float) * 6 * n, cudaMemcpyDeviceToHost, ctx->stream));
+   return T9GB_OK;
+}
 }  // namespace t9gb
 
 using namespace t9gb;
@@ -450,14 +458,13 @@ int t9gb_induce_host(t9gb_context* h, const double* xyz, double* uind, double* u
    if (!ctx->have_order)
       T9_CHECK(t9gb_nblist_build(h));
    T9_CHECK(t9gb_mpole_init(h));
+   // the dipoles' caller-order copy rides in the solve's synchronisation
+   ctx->stage_out = true;
    int st = induce_sorted(ctx);
+   ctx->stage_out = false;
    if (st != T9GB_OK && st != T9GB_NOT_CONVERGED && st != T9GB_NAN_DETECTED)
       return st;
    const int n = ctx->n;
-   // dipoles to caller order in the scratch vector, then one D2H copy
-   T9_CHECK(scatter_from_sorted3(ctx, ctx->uind, ctx->hout, ctx->hout + 3 * n));
-   T9_CUDA(cudaMemcpyAsync(ctx->h_stage, ctx->hout, sizeof(float) * 6 * n, cudaMemcpyDeviceToHost, ctx->stream));
-   T9_CUDA(cudaStreamSynchronize(ctx->stream));
    for (int i = 0; i < 3 * n; ++i) {
       if (uind)
          uind[i] = ctx->h_stage[i];

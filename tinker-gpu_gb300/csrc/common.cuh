@@ -262,6 +262,9 @@ struct Context {
    bool use_graph = true;
    cudaGraphExec_t graph_exec[3] = {nullptr, nullptr, nullptr};  // per start variant (pcg.cu)
    cudaStream_t cap_stream = nullptr;
+   // t9gb_induce_host: enqueue the caller-order dipole copy before the
+   // solve's one synchronisation
+   bool stage_out = false;
    // second streams for the reciprocal grid half of a field evaluation, run
    // beside the real-space pair kernel (fork / join by events).  A stream
    // that joined a graph capture stays in it until that capture ends, so the
@@ -400,6 +403,9 @@ int learn_features_out(Context* ctx, float* out_dev);
 // permutation helpers (nblist.cu)
 int gather_to_sorted3(Context* ctx, const float* a, const float* b, float* s6);
 int scatter_from_sorted3(Context* ctx, const float* s6, float* a, float* b);
+// the converged dipoles in caller order into the pinned h_stage ([2][n][3]),
+// enqueued before a solve's synchronisation when stage_out is set
+int stage_dipoles(Context* ctx);
 
 }  // namespace t9gb
 

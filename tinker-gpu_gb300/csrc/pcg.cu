@@ -549,6 +549,8 @@ static int induce_stepwise(Context* ctx, int variant)
          break;
    }
    T9_CHECK(pcg_finish(ctx, A));
+   if (ctx->stage_out)
+      T9_CHECK(stage_dipoles(ctx));
    T9_CUDA(cudaStreamSynchronize(ctx->stream));
    return T9GB_OK;
 }
@@ -628,6 +630,8 @@ static int induce_graph(Context* ctx, int variant)
       T9_CHECK(induce_capture(ctx, variant));
    T9_CHECK(list_request(ctx));
    T9_CUDA(cudaGraphLaunch(ctx->graph_exec[variant], ctx->stream));
+   if (ctx->stage_out)
+      T9_CHECK(stage_dipoles(ctx));
    T9_CUDA(cudaStreamSynchronize(ctx->stream));
    ctx->list_stale = false;
    return T9GB_OK;
