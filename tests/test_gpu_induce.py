@@ -144,3 +144,22 @@ def test_gear_predictor_trajectory(gpu_lib, oracle, tg):
     assert rms_err(ud1 * D, ud0 * D) < DIPOLE_RMS_DEBYE
     assert its_gear[:6] == its_plain[:6]
     assert np.mean(its_gear[7:]) < np.mean(its_plain[7:])
+
+
+@pytest.mark.parametrize("bad", [np.nan, np.inf, -np.inf])
+def test_non_finite_coordinates_rejected(gpu_lib, tg, bad):
+    """A non-finite coordinate is refused before any copy or launch; the
+    context keeps working and gives the same dipoles as before."""
+    import importlib
+
+    abi = importlib.import_module("tinker-gpu_gb300.abi")
+    s = tg.systems.make_config("water648")
+    e = engine_for(s)
+    ref, _, _ = e.induce_host(s.xyz)
+    x = s.xyz.copy()
+    x[100, 1] = bad
+    with pytest.raises(abi.T9Error) as err:
+        e.induce_host(x)
+    assert err.value.code == abi.T9GB_BAD_ARG
+    again, _, _ = e.induce_host(s.xyz)
+    assert np.array_equal(ref, again)

@@ -342,15 +342,19 @@ int t9gb_set_xyz_host(t9gb_context* h, const double* xyz)
       return T9GB_BAD_ARG;
    Context* ctx = &h->c;
    const int n = ctx->n;
-   for (int i = 0; i < 3 * n; ++i)
-      if (!std::isfinite(xyz[i]))
-         return T9GB_BAD_ARG;
    // the previous copy out of the staging buffer must have finished
    if (ctx->ev_in_pending)
       T9_CUDA(cudaEventSynchronize(ctx->ev_in));
+   // one pass: convert and check (|x| < inf and not NaN: x - x == 0)
    float* st = ctx->h_in;
-   for (int i = 0; i < 3 * n; ++i)
-      st[i] = (float)xyz[i];
+   double bad = 0.0;
+   for (int i = 0; i < 3 * n; ++i) {
+      const double v = xyz[i];
+      bad += v - v;
+      st[i] = (float)v;
+   }
+   if (bad != 0.0 || bad != bad)
+      return T9GB_BAD_ARG;
    T9_CUDA(cudaMemcpyAsync(ctx->xyz, st, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
    T9_CUDA(cudaEventRecord(ctx->ev_in, ctx->stream));
    ctx->ev_in_pending = true;

@@ -635,12 +635,13 @@ __device__ __forceinline__ void norm3(float* a)
 }
 
 // chirality check (rotpole.h:7-50): flips y-odd components once, in place
-__global__ void k_chkpole(int n, int4* __restrict__ frames, float* __restrict__ pole, const float* __restrict__ xyz)
+__device__ __forceinline__ void chkpole_one(int i, int4* __restrict__ frames, float* __restrict__ pole,
+   const float* __restrict__ xyz)
 {
-   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+   {
       int4 f = frames[i];
       if (f.w != 2 || f.z == 0)
-         continue;
+         return;
       int id = abs(f.z) - 1;
       const float* pa = xyz + 3 * i;
       const float* pb = xyz + 3 * f.x;
@@ -662,9 +663,11 @@ __global__ void k_chkpole(int n, int4* __restrict__ frames, float* __restrict__ 
 
 // rows of 12: q, d xyz, qxx, qyy, qzz, qxy, qxz, qyz, thole, polarizability
 // also stores the local frame (rows x, y, z axes) per slot in sframe[9]
-__global__ void k_rotpole(int npad, const int* __restrict__ perm, const int4* __restrict__ frames,
-   const float* __restrict__ pole, const float* __restrict__ xyz, const float2* __restrict__ sdamp,
-   const float* __restrict__ spolar, float* __restrict__ rpole, float* __restrict__ sframe)
+// The chirality check of the slot's own atom runs first (chkpole): the
+// thread is the only one touching that atom, and it reads back what it wrote.
+__global__ void k_rotpole(int npad, const int* __restrict__ perm, int4* __restrict__ frames, float* __restrict__ pole,
+   const float* __restrict__ xyz, const float2* __restrict__ sdamp, const float* __restrict__ spolar,
+   float* __restrict__ rpole, float* __restrict__ sframe)
 {
    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < npad; s += gridDim.x * blockDim.x) {
       int i = perm[s];
@@ -677,6 +680,7 @@ __global__ void k_rotpole(int npad, const int* __restrict__ perm, const int4* __
             fr[c] = (c % 4 == 0) ? 1.f : 0.f;
          continue;
       }
+      chkpole_one(i, frames, pole, xyz);
       rp[10] = sdamp[s].y;
       rp[11] = spolar[s];
       int4 f = frames[i];
@@ -757,7 +761,6 @@ __global__ void k_rotpole(int npad, const int* __restrict__ perm, const int4* __
 
 int rotpole_sorted(Context* ctx)
 {
-   k_chkpole<<<grid_for(ctx->n, 256), 256, 0, ctx->stream>>>(ctx->n, ctx->frames, ctx->pole, ctx->xyz);
    k_rotpole<<<grid_for(ctx->npad, 128), 128, 0, ctx->stream>>>(ctx->npad, ctx->perm, ctx->frames, ctx->pole,
       ctx->xyz, ctx->sdamp, ctx->spolar, ctx->srpole, ctx->sframe);
    T9_CUDA(cudaGetLastError());
