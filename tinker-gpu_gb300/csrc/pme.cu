@@ -475,8 +475,18 @@ __device__ __forceinline__ void dft_reg(float2* v, const float2* tw)
    }
 }
 
-// One N-point line at line[i * ls], transformed in place by the T threads
-// t = 0..T-1 of one warp (every thread of the warp takes part in some line).
+// Shared-memory swizzle of a line index: the low bits within each block of T
+// are XORed with the block number (and the block group), so the strided
+// step-2 reads of fft_line and the column passes spread over the banks.
+template <int T>
+__device__ __forceinline__ int fsig(int i)
+{
+   return i ^ (((i / T) + (i / (T * T))) & (T - 1));
+}
+
+// One N-point line, element i at line[fsig(i) * ls], transformed in place by
+// the T threads t = 0..T-1 of one warp (every thread of the warp takes part
+// in some line).
 template <int N, int T, bool INV>
 __device__ __forceinline__ void fft_line(float2* line, int ls, int t, const float2* tw)
 {
@@ -484,7 +494,7 @@ __device__ __forceinline__ void fft_line(float2* line, int ls, int t, const floa
    float2 v[N1];
 #pragma unroll
    for (int n1 = 0; n1 < N1; ++n1)
-      v[n1] = line[(n1 * T + t) * ls];
+      v[n1] = line[fsig<T>(n1 * T + t) * ls];
    dft_reg<N1, INV>(v, tw);
 #pragma unroll
    for (int k1 = 1; k1 < N1; ++k1) {
@@ -496,7 +506,7 @@ __device__ __forceinline__ void fft_line(float2* line, int ls, int t, const floa
    __syncwarp();
 #pragma unroll
    for (int k1 = 0; k1 < N1; ++k1)
-      line[(k1 * T + t) * ls] = v[k1];
+      line[fsig<T>(k1 * T + t) * ls] = v[k1];
    __syncwarp();
    float2 u[J][T];
 #pragma unroll
@@ -504,7 +514,7 @@ __device__ __forceinline__ void fft_line(float2* line, int ls, int t, const floa
       const int k1 = t * J + j;
 #pragma unroll
       for (int n2 = 0; n2 < T; ++n2)
-         u[j][n2] = line[(k1 * T + n2) * ls];
+         u[j][n2] = line[fsig<T>(k1 * T + n2) * ls];
       dft_reg<T, INV>(u[j], tw);
    }
    __syncwarp();
@@ -512,7 +522,7 @@ __device__ __forceinline__ void fft_line(float2* line, int ls, int t, const floa
    for (int j = 0; j < J; ++j)
 #pragma unroll
       for (int k2 = 0; k2 < T; ++k2)
-         line[(t * J + j + N1 * k2) * ls] = u[j][k2];
+         line[fsig<T>(t * J + j + N1 * k2) * ls] = u[j][k2];
    __syncwarp();
 }
 
@@ -522,13 +532,28 @@ __host__ __device__ constexpr int fft_threads_per_line()
    return N == 32 ? 4 : 8;
 }
 
+// row pitch of the plane (float2) and of the z-line tile
+template <int N>
+__host__ __device__ constexpr int fft_plane_ld()
+{
+   return N == 32 ? N + 4 : N + 2;
+}
+
+template <int N>
+__host__ __device__ constexpr int fft_zline_ld()
+{
+   return N == 32 ? 20 : 18;
+}
+
 // 2-D FFT (x then y) of z plane blockIdx.x; N * T threads, dynamic shared
 // memory N (N + 1) + 128 float2
 template <int N, bool FROM_FX, bool INV>
 __global__ void __launch_bounds__(N * fft_threads_per_line<N>()) k_fft_plane(long long* __restrict__ qfx,
    float2* __restrict__ g)
 {
-   constexpr int T = fft_threads_per_line<N>(), LD = N + 1, NT = N * T, R = N / T;
+   // element (y, x) at fsm[fsig(y) LD + fsig(x)]; the padding keeps the two
+   // lines of a 16-thread shared-memory phase on different banks
+   constexpr int T = fft_threads_per_line<N>(), LD = fft_plane_ld<N>(), NT = N * T, R = N / T;
    extern __shared__ float2 fsm[];
    float2* tw = fsm + N * LD;
    for (int k = threadIdx.x; k < 128; k += NT)
@@ -557,19 +582,19 @@ __global__ void __launch_bounds__(N * fft_threads_per_line<N>()) k_fft_plane(lon
 #pragma unroll
       for (int r = 0; r < 8; ++r) {
          const int e = threadIdx.x + (c + r) * NT;
-         fsm[(e / N) * LD + (e % N)] = v[r];
+         fsm[fsig<T>(e / N) * LD + fsig<T>(e % N)] = v[r];
       }
    }
    __syncthreads();
    const int line = threadIdx.x / T, t = threadIdx.x % T;
-   fft_line<N, T, INV>(fsm + line * LD, 1, t, tw);  // row y = line, along x
+   fft_line<N, T, INV>(fsm + fsig<T>(line) * LD, 1, t, tw);  // row y = line, along x
    __syncthreads();
-   fft_line<N, T, INV>(fsm + line, LD, t, tw);  // column x = line, along y
+   fft_line<N, T, INV>(fsm + fsig<T>(line), LD, t, tw);  // column x = line, along y
    __syncthreads();
 #pragma unroll
    for (int r = 0; r < R; ++r) {
       const int e = threadIdx.x + r * NT;
-      g[base + e] = fsm[(e / N) * LD + (e % N)];
+      g[base + e] = fsm[fsig<T>(e / N) * LD + fsig<T>(e % N)];
    }
 }
 
@@ -579,7 +604,8 @@ template <int N, int MODE>
 __global__ void __launch_bounds__(16 * fft_threads_per_line<N>()) k_fft_zline(const float* __restrict__ infl,
    float2* __restrict__ g)
 {
-   constexpr int T = fft_threads_per_line<N>(), XL = 16, LD = XL + 1, NT = XL * T, R = N / T;
+   // element z of line l at sm[fsig(z) LD + l]
+   constexpr int T = fft_threads_per_line<N>(), XL = 16, LD = fft_zline_ld<N>(), NT = XL * T, R = N / T;
    __shared__ float2 sm[N * LD];
    __shared__ float2 tw[128];
    for (int k = threadIdx.x; k < 128; k += NT)
@@ -597,7 +623,7 @@ __global__ void __launch_bounds__(16 * fft_threads_per_line<N>()) k_fft_zline(co
          v[r] = g[base + (size_t)(ez + (c + r) * ZS) * zs + ex];
 #pragma unroll
       for (int r = 0; r < 8; ++r)
-         sm[(ez + (c + r) * ZS) * LD + ex] = v[r];
+         sm[fsig<T>(ez + (c + r) * ZS) * LD + ex] = v[r];
    }
    __syncthreads();
    const int line = threadIdx.x / T, t = threadIdx.x % T;
@@ -613,7 +639,7 @@ __global__ void __launch_bounds__(16 * fft_threads_per_line<N>()) k_fft_zline(co
             f[r] = infl[base + (size_t)(ez + (c + r) * ZS) * zs + ex];
 #pragma unroll
          for (int r = 0; r < 8; ++r) {
-            float2& v = sm[(ez + (c + r) * ZS) * LD + ex];
+            float2& v = sm[fsig<T>(ez + (c + r) * ZS) * LD + ex];
             v = make_float2(v.x * f[r], v.y * f[r]);
          }
       }
@@ -624,13 +650,13 @@ __global__ void __launch_bounds__(16 * fft_threads_per_line<N>()) k_fft_zline(co
    __syncthreads();
 #pragma unroll
    for (int r = 0; r < R; ++r)
-      g[base + (size_t)(ez + r * ZS) * zs + ex] = sm[(ez + r * ZS) * LD + ex];
+      g[base + (size_t)(ez + r * ZS) * zs + ex] = sm[fsig<T>(ez + r * ZS) * LD + ex];
 }
 
 template <int N>
 static size_t fft_plane_smem()
 {
-   return sizeof(float2) * ((size_t)N * (N + 1) + 128);
+   return sizeof(float2) * ((size_t)N * fft_plane_ld<N>() + 128);
 }
 
 template <int N>
