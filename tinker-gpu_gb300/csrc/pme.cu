@@ -487,8 +487,20 @@ __device__ __forceinline__ int fsig(int i)
 // One N-point line, element i at line[fsig(i) * ls], transformed in place by
 // the T threads t = 0..T-1 of one warp (every thread of the warp takes part
 // in some line).
+// wt[k1] = W_N^(t k1) for this thread's t, read once per kernel from the
+// table (its thread-dependent indices would conflict on every line).
+template <int N, int T>
+__device__ __forceinline__ void fft_twiddles(int t, const float2* tw, float2* wt)
+{
+   if (N / T <= 8) {
+#pragma unroll
+      for (int k1 = 0; k1 < N / T; ++k1)
+         wt[k1] = tw[((t * k1) & (N - 1)) * (128 / N)];
+   }
+}
+
 template <int N, int T, bool INV>
-__device__ __forceinline__ void fft_line(float2* line, int ls, int t, const float2* tw)
+__device__ __forceinline__ void fft_line(float2* line, int ls, int t, const float2* tw, const float2* wt)
 {
    constexpr int N1 = N / T, J = N1 / T;
    float2 v[N1];
@@ -498,7 +510,9 @@ __device__ __forceinline__ void fft_line(float2* line, int ls, int t, const floa
    dft_reg<N1, INV>(v, tw);
 #pragma unroll
    for (int k1 = 1; k1 < N1; ++k1) {
-      float2 w = tw[((t * k1) & (N - 1)) * (128 / N)];
+      // registers for up to 8 twiddles; the 128-point lines (1024-thread
+      // planes) read the table rather than spill
+      float2 w = N1 <= 8 ? wt[k1] : tw[((t * k1) & (N - 1)) * (128 / N)];
       if (INV)
          w.y = -w.y;
       v[k1] = cmulf(v[k1], w);
@@ -587,9 +601,11 @@ __global__ void __launch_bounds__(N * fft_threads_per_line<N>()) k_fft_plane(lon
    }
    __syncthreads();
    const int line = threadIdx.x / T, t = threadIdx.x % T;
-   fft_line<N, T, INV>(fsm + fsig<T>(line) * LD, 1, t, tw);  // row y = line, along x
+   float2 wt[N / T];
+   fft_twiddles<N, T>(t, tw, wt);
+   fft_line<N, T, INV>(fsm + fsig<T>(line) * LD, 1, t, tw, wt);  // row y = line, along x
    __syncthreads();
-   fft_line<N, T, INV>(fsm + fsig<T>(line), LD, t, tw);  // column x = line, along y
+   fft_line<N, T, INV>(fsm + fsig<T>(line), LD, t, tw, wt);  // column x = line, along y
    __syncthreads();
 #pragma unroll
    for (int r = 0; r < R; ++r) {
@@ -627,8 +643,10 @@ __global__ void __launch_bounds__(16 * fft_threads_per_line<N>()) k_fft_zline(co
    }
    __syncthreads();
    const int line = threadIdx.x / T, t = threadIdx.x % T;
+   float2 wt[N / T];
+   fft_twiddles<N, T>(t, tw, wt);
    if (MODE != 1)
-      fft_line<N, T, false>(sm + line, LD, t, tw);
+      fft_line<N, T, false>(sm + line, LD, t, tw, wt);
    if (MODE == 2) {
       __syncthreads();
 #pragma unroll
@@ -646,7 +664,7 @@ __global__ void __launch_bounds__(16 * fft_threads_per_line<N>()) k_fft_zline(co
       __syncthreads();
    }
    if (MODE != 0)
-      fft_line<N, T, true>(sm + line, LD, t, tw);
+      fft_line<N, T, true>(sm + line, LD, t, tw, wt);
    __syncthreads();
 #pragma unroll
    for (int r = 0; r < R; ++r)
