@@ -37,12 +37,16 @@ static inline uint64_t spread_bits(uint64_t v)
 
 static bool is_pbc(const t9gb_config& c) { return c.box[0] > 0 && c.box[1] > 0 && c.box[2] > 0; }
 
+// The stored list holds the pairs within the largest per-step filter radius
+// plus the list buffer: it is reused until an atom has moved more than half
+// the buffer, so no pair inside a filter radius can be missing from it
+// (neigh::lbuffer, src/nblist.cpp:312-530).
 static double list_cutoff(const t9gb_config& c)
 {
    double r = c.cutoff;
    if (c.pcgprec)
       r = std::max(r, c.usolve_cutoff + c.pbuffer);
-   return r;
+   return r + std::max(0.0, c.list_buffer);
 }
 
 // Host: Morton order of the current coordinates, per-slot parameters, the
