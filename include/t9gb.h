@@ -109,6 +109,27 @@ int t9gb_set_thole_pairs(t9gb_context* ctx, int ntypes, const int* ptype, const 
  * solves (a time-dependent field); takes effect in stream order. */
 int t9gb_set_external_field(t9gb_context* ctx, const double* field);
 
+/* ---- Buffered 14-7 van der Waals (the MD path around induce) ---- */
+
+/* Per-atom van der Waals data, copied once.  Replaces the ehal INIT of
+ * vdwData (src/evdw.cpp, jvdw / radmin / epsilon / ired / kred).
+ * vtype[n] in 0..ntypes-1; radmin[ntypes][ntypes] (A) and
+ * epsilon[ntypes][ntypes] (kcal/mol) after the combining rules, symmetric;
+ * red[n] reduction factor toward parent[n] (0-based; parent = the atom
+ * itself for none); scaled pairs scaled_ik[nscaled][2] with their
+ * vdw-1x-scale values; the fifth-order taper starts at `taper` and ends at
+ * `off` (A).  Like t9gb_set_topology, call before t9gb_nblist_build: the
+ * stored neighbour list grows to cover `off`.  ntypes = 0 removes the term. */
+int t9gb_set_vdw(t9gb_context* ctx, int ntypes, const int* vtype, const double* radmin, const double* epsilon,
+   const double* red, const int* parent, int nscaled, const int* scaled_ik, const double* scaled_v, double taper,
+   double off);
+
+/* Buffered 14-7 energy (kcal/mol), gradient [n][3] (device, kcal/mol/A,
+ * caller order) and virial (3 x 3, row-major, kcal/mol) with the calc flags.
+ * Replaces void ehal(int vers) (src/ehal.cpp; src/cu/ehal.cu,
+ * include/seq/pair_hal.h:52-96). */
+int t9gb_ehal(t9gb_context* ctx, int vers, double* energy, float* grad_device, double* virial);
+
 /* Coordinates [n][3].  Replace copyPosToXyz (src/atom.cpp:161-166). */
 int t9gb_set_xyz_host(t9gb_context* ctx, const double* xyz);
 int t9gb_set_xyz_device(t9gb_context* ctx, const float* xyz_device);

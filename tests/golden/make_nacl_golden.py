@@ -61,6 +61,38 @@ def parse_case(src, case):
     return out
 
 
+def parse_sections(src, case_name):
+    """{section title: {ref_eng, ref_grad, ref_v, eps}} of one TEST_CASE."""
+    body = src.split('TEST_CASE("%s"' % case_name, 1)[1].split("TEST_CASE(", 1)[0]
+    body = "\n".join(ln.split("//", 1)[0] for ln in body.splitlines())
+    eps = re.search(r"const double eps = (-?[\d.]+(?:e-?\d+)?);", body)
+    out = {}
+    for part in body.split('SECTION("')[1:]:
+        title = part.split('"', 1)[0].strip()
+        vals = {"eps": float(eps.group(1))}
+        for m in re.finditer(r"const double (\w+)\[\]\[3\] = \{(.*?)\};", part, re.S):
+            nums = [float(v) for v in re.findall(r"-?\d+\.\d+(?:e-?\d+)?", m.group(2))]
+            vals[m.group(1)] = [nums[j : j + 3] for j in range(0, len(nums), 3)]
+        for m in re.finditer(r"const double (\w+) = (-?[\d.]+(?:e-?\d+)?);", part):
+            vals[m.group(1)] = float(m.group(2))
+        x = re.search(r'test/file/nacl/(nacl\d\.xyz)', part)
+        vals["xyz_file"] = x.group(1) if x else None
+        vals["extra_keys"] = re.findall(r'key\d \+= "([^"]*)\\n"', part)
+        out[title] = vals
+    return out
+
+
+def read_vdw(path, types):
+    """vdw records (radius, epsilon[, reduction]) of the given types/classes."""
+    out = {}
+    with open(path) as f:
+        for ln in f:
+            t = ln.split()
+            if len(t) >= 4 and t[0] == "vdw" and int(t[1]) in types:
+                out[t[1]] = [float(v) for v in t[2:]]
+    return out
+
+
 def case(xyz_file, key_file, src, name, ewald):
     atoms = read_xyz(os.path.join(REF, "test/file/nacl", xyz_file))
     types = sorted({a["type"] for a in atoms})
@@ -86,9 +118,23 @@ def case(xyz_file, key_file, src, name, ewald):
 def main():
     with open(os.path.join(REF, "test/nacl.cpp")) as f:
         src = f.read()
+    kw, _ = read_key(os.path.join(REF, "test/file/nacl/nacl.key"))
+    secs = parse_sections(src, "NaCl-1")
+    ehal = {}
+    for title, v in secs.items():
+        if v["xyz_file"] is None or v["extra_keys"]:
+            continue  # the long-range correction sections (vdw-correction) are not restated
+        ehal[title] = {"atoms": read_xyz(os.path.join(REF, "test/file/nacl", v["xyz_file"])),
+                       "ref_eng": v["ref_eng"], "ref_grad": v["ref_grad"], "ref_v": v["ref_v"], "eps": v["eps"]}
     fixture = {
-        "source": "Tinker9 test/nacl.cpp, test/file/nacl/{nacl1.xyz,nacl4.xyz,nacl.key,nacl4.key}, "
-        "test/file/commit_6fe8e913/amoeba09.prm",
+        "source": "Tinker9 test/nacl.cpp, test/file/nacl/{nacl1.xyz,nacl2.xyz,nacl3.xyz,nacl4.xyz,nacl.key,"
+        "nacl4.key}, test/file/commit_6fe8e913/amoeba09.prm",
+        "NaCl-1": {
+            "box": float(kw["a-axis"][0]),
+            "vdw_cutoff": float(kw["vdw-cutoff"][0]),
+            "vdw": read_vdw(os.path.join(REF, "test/file/commit_6fe8e913/amoeba09.prm"), {7, 15}),
+            "cases": ehal,
+        },
         "NaCl-2": case("nacl1.xyz", "nacl.key", src, "NaCl-2", False),
         "NaCl-3": case("nacl4.xyz", "nacl4.key", src, "NaCl-3", True),
     }

@@ -33,3 +33,24 @@ def system(name, fx=None):
         st.update(use_ewald=0, ewald_cutoff=c["cutoff"], nfft=(0, 0, 0), aewald=0.0)
     s.settings = st
     return s, c["expected"]
+
+
+def hal_system(title, fx=None):
+    """NaCl-1 (test/nacl.cpp:35-190): a Na+/Cl- pair in an 18.643 A box with
+    only the buffered 14-7 term, vdw-cutoff 2.6 A."""
+    c = (load() if fx is None else fx)["NaCl-1"]
+    case = c["cases"][title]
+    atoms = case["atoms"]
+    xyz = [a["xyz"] for a in atoms]
+    types = [a["type"] for a in atoms]
+    # multipole / polarize records are not used by this term: a neutral,
+    # non-polarizable placeholder keeps the context valid
+    records = {t: [(0, 0, 0, [0.0] * 10)] for t in types}
+    polar = {t: (0.0, 0.39, ()) for t in types}
+    s = tg.systems.build_system(xyz, types, [], records, polar, box=[c["box"]] * 3, name="nacl-hal")
+    vrec = {int(t): tuple(v) for t, v in c["vdw"].items()}
+    s.vdw = tg.systems.hal_params(types, [], vrec, {}, c["vdw_cutoff"])
+    st = dict(tg.systems.DEFAULT_SETTINGS)
+    st.update(use_ewald=0, ewald_cutoff=c["vdw_cutoff"], nfft=(0, 0, 0), aewald=0.0)
+    s.settings = st
+    return s, case

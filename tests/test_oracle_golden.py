@@ -241,3 +241,24 @@ def test_extfield_golden(oracle):
     wp = np.diag(oracle.epolar_virial_fd(s, ud, up, diag_only=True, cutoff=cut))
     for w, key in ((wm, "mpole"), (wp, "polar"), (wm + wp, "mplar")):
         assert np.abs(w - np.diag(np.array(ex[key]["virial"]))).max() < eps["virial"]
+
+
+HAL_TITLES = ["- ehal -- no switch", "- ehal -- switch, near cut", "- ehal -- switch, near off"]
+
+
+@pytest.mark.parametrize("title", HAL_TITLES)
+def test_hal_golden(oracle, title):
+    """Buffered 14-7 energy, gradient and virial of the NaCl-1 pair at 2.2,
+    2.38 and 2.5 A (no taper, taper near its start, near the cutoff)."""
+    import dataclasses
+
+    import nacl_fixture as N
+    from oracle import mm_oracle
+
+    s, ex = N.hal_system(title)
+    e = mm_oracle.hal_energy(s)
+    assert abs(e - ex["ref_eng"]) < ex["eps"]
+    g = oracle._fd(lambda x: mm_oracle.hal_energy(s, x), np.asarray(s.xyz, dtype=np.float64), [0, 1], 1e-6)
+    assert np.abs(g - np.array(ex["ref_grad"])).max() < ex["eps"]
+    w = oracle._strain_fd(s, lambda s2: mm_oracle.hal_energy(s2), False, 1e-6)
+    assert np.abs(w - np.array(ex["ref_v"])).max() < ex["eps"] * 10  # known answers with three decimals

@@ -28,7 +28,7 @@ EXPORTS = [
     "t9gb_ufield_noalloc", "t9gb_learn_config", "t9gb_learn_policy", "t9gb_learn_reset", "t9gb_learn_stats", "t9gb_learn_get_weights",
     "t9gb_learn_set_weights", "t9gb_learn_eval", "t9gb_learn_adamw", "t9gb_learn_features",
     "t9gb_empole", "t9gb_epolar", "t9gb_emplar", "t9gb_energy_components", "t9gb_pme_own_fft",
-    "t9gb_pair_lanes", "t9gb_set_thole_pairs", "t9gb_set_external_field",
+    "t9gb_pair_lanes", "t9gb_set_thole_pairs", "t9gb_set_external_field", "t9gb_set_vdw", "t9gb_ehal",
 ]
 CALC_ENERGY, CALC_GRAD, CALC_VIRIAL = 0x010, 0x020, 0x040
 
@@ -124,6 +124,8 @@ def load(path=None):
     lib.t9gb_pair_lanes.argtypes = [vp, C.c_int]
     lib.t9gb_set_thole_pairs.argtypes = [vp, C.c_int, ip, dp]
     lib.t9gb_set_external_field.argtypes = [vp, dp]
+    lib.t9gb_set_vdw.argtypes = [vp, C.c_int, ip, dp, dp, dp, ip, C.c_int, ip, dp, C.c_double, C.c_double]
+    lib.t9gb_ehal.argtypes = [vp, C.c_int, dp, fp, dp]
     for name in ("t9gb_empole", "t9gb_epolar", "t9gb_emplar"):
         getattr(lib, name).argtypes = [vp, C.c_int, dp, fp, dp]
     _lib = lib
@@ -205,6 +207,25 @@ class Engine:
             self.set_thole_pairs(system.ptype, system.thole_table)
         if getattr(system, "exfld", None) is not None:
             self.set_external_field(system.exfld)
+        if getattr(system, "vdw", None) is not None:
+            self.set_vdw(system.vdw)
+
+    def set_vdw(self, v):
+        """v: systems.VdwParams (per-atom types, pair tables, reduction,
+        scaled pairs, taper and cutoff), or None to remove the term."""
+        if v is None:
+            self._check(self.lib.t9gb_set_vdw(self.h, 0, None, None, None, None, None, 0, None, None, 0.0, 0.0))
+            return
+        vt = np.ascontiguousarray(v.vtype, dtype=np.int32)
+        rm = np.ascontiguousarray(v.radmin, dtype=np.float64)
+        ep = np.ascontiguousarray(v.epsilon, dtype=np.float64)
+        rd = np.ascontiguousarray(v.red, dtype=np.float64)
+        pa = np.ascontiguousarray(v.parent, dtype=np.int32)
+        ik = np.ascontiguousarray(v.scaled_ik, dtype=np.int32).reshape(-1)
+        sv = np.ascontiguousarray(v.scaled_v, dtype=np.float64)
+        self._vdw_keep = (vt, rm, ep, rd, pa, ik, sv)
+        self._check(self.lib.t9gb_set_vdw(self.h, int(rm.shape[0]), _ip(vt), _dp(rm), _dp(ep), _dp(rd), _ip(pa),
+                                          len(sv), _ip(ik), _dp(sv), float(v.taper), float(v.off)))
 
     def set_external_field(self, field):
         """Uniform external field [3] in e/A^2, or None."""
@@ -422,6 +443,11 @@ class Engine:
         if vers & CALC_VIRIAL:
             return e.value, g, v.reshape(3, 3)
         return e.value, g
+
+    def ehal(self, vers=CALC_ENERGY | CALC_GRAD):
+        """Buffered 14-7 van der Waals: (energy, gradient) or with CALC_VIRIAL
+        (energy, gradient, virial)."""
+        return self._eg(self.lib.t9gb_ehal, vers)
 
     def energy_components(self):
         """[multipole real, recip, self, polarization] of the last energy evaluation."""

@@ -121,6 +121,7 @@ static void free_all(Context* ctx)
    pme_free(ctx);
    learn_free(ctx);
    force_free(ctx);
+   vdw_release(ctx);
    drop_graphs(ctx);
    if (ctx->cap_stream)
       cudaStreamDestroy(ctx->cap_stream);

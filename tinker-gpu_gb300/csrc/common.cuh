@@ -152,6 +152,25 @@ struct Context {
    std::vector<int> h_excl_ik;
    std::vector<double> h_excl_scale;
 
+   // buffered 14-7 van der Waals (t9gb_set_vdw): per-type-pair radius and
+   // well depth, reduction toward a parent atom, scaled pairs, taper / cutoff
+   bool use_vdw = false;
+   int nvt = 0;
+   double vdw_taper = 0, vdw_off = 0;
+   std::vector<int> h_vtype, h_vparent;
+   std::vector<double> h_vred;
+   std::vector<int> h_vexcl_ik;
+   std::vector<double> h_vexcl_scale;
+   float2* vtab = nullptr;     // [nvt][nvt] (radmin, epsilon), device
+   int* vtype = nullptr;       // [n]
+   int* vparent = nullptr;     // [n]
+   float* vred = nullptr;      // [n]
+   int* vch_start = nullptr;   // [n + 1] children (atoms reduced toward this one)
+   int* vch = nullptr;
+   float4* vpos = nullptr;     // [npad] reduced sites, sorted; w = type (int bits)
+   float* fvdw = nullptr;      // [npad][3] dE/dx of each reduced site
+   float* sp_v = nullptr;      // [nsp] van der Waals scale of each scaled pair
+
    // coordinates, caller order
    float* xyz = nullptr;       // [n][3]
    std::vector<double> h_xyz;  // host copy for the ordering, refreshed by t9gb_nblist_build
@@ -284,6 +303,11 @@ struct Context {
 };
 
 // reductions: up to RED_MAX block partials per slot
+// Largest separation between the two reduced van der Waals sites of a pair
+// and their atoms' separation that the stored list allows for (each site lies
+// (1 - red) of a bond from its atom: 0.09 A for AMOEBA water hydrogens).
+constexpr double VDW_SITE_MARGIN = 0.25;
+
 constexpr int RED_MAX = 1024;
 constexpr int RED_SLOTS = 8;
 
@@ -396,6 +420,14 @@ int learn_reset(Context* ctx, unsigned seed);
 int learn_forward(Context* ctx);
 int learn_guess(Context* ctx, float* ug8, int set_choice);
 void drop_graphs(Context* ctx);  // pcg.cu
+// energy.cu: fixed-order sums of per-slot rows (nrows <= 8 FP64 rows; nblocks
+// <= 3 blocks of 9 FP32 virial rows, summed and symmetrised)
+int sum_rows_d(Context* ctx, const double* rows, int nrows, double* out);
+int sum_rows_virial(Context* ctx, const float* rows, int nblocks, double* virial);
+// vdw.cu: reduced sites, pair kernel and per-atom gather (grad: dE/dx added
+// to or stored in grad when not null); energy rows in e_atom[2 npad ..)
+int vdw_forces(Context* ctx, float* grad, bool add, bool vir, double* energy);
+void vdw_release(Context* ctx);
 int learn_pick(Context* ctx, const float* ug8, const float* fld8);
 int learn_train(Context* ctx);
 int learn_features_out(Context* ctx, float* out_dev);

@@ -118,6 +118,39 @@ extern "C" int t9gb_epolar_energy(t9gb_context* h, double* energy)
 
 namespace t9gb {
 
+// fixed-order sum of nrows FP64 rows of npad per-slot terms
+int sum_rows_d(Context* ctx, const double* rows, int nrows, double* out)
+{
+   k_sum_rows<<<nrows, 1024, 0, ctx->stream>>>(ctx->npad, ctx->npad, rows, ctx->scal + 52);
+   T9_CUDA(cudaGetLastError());
+   double v[8];
+   T9_CUDA(cudaMemcpyAsync(v, ctx->scal + 52, sizeof(double) * nrows, cudaMemcpyDeviceToHost, ctx->stream));
+   T9_CUDA(cudaStreamSynchronize(ctx->stream));
+   double t = 0;
+   for (int r = 0; r < nrows; ++r)
+      t += v[r];
+   *out = t;
+   return T9GB_OK;
+}
+
+// nblocks blocks of 9 FP32 virial rows [9][npad], summed and symmetrised
+int sum_rows_virial(Context* ctx, const float* rows, int nblocks, double* virial)
+{
+   k_sum_rows_f<<<9 * nblocks, 1024, 0, ctx->stream>>>(ctx->npad, ctx->npad, rows, ctx->vsum);
+   T9_CUDA(cudaGetLastError());
+   double v[27];
+   T9_CUDA(cudaMemcpyAsync(v, ctx->vsum, sizeof(double) * 9 * nblocks, cudaMemcpyDeviceToHost, ctx->stream));
+   T9_CUDA(cudaStreamSynchronize(ctx->stream));
+   double W[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+   for (int b = 0; b < nblocks; ++b)
+      for (int c = 0; c < 9; ++c)
+         W[c] += v[9 * b + c];
+   for (int a = 0; a < 3; ++a)
+      for (int c = 0; c < 3; ++c)
+         virial[3 * a + c] = 0.5 * (W[3 * a + c] + W[3 * c + a]);
+   return T9GB_OK;
+}
+
 static int sum_empole(Context* ctx, double* energy)
 {
    k_sum_rows<<<3, 1024, 0, ctx->stream>>>(ctx->npad, ctx->npad, ctx->e_atom, ctx->scal + 32);

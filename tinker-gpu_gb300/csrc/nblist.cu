@@ -41,11 +41,14 @@ static bool is_pbc(const t9gb_config& c) { return c.box[0] > 0 && c.box[1] > 0 &
 // plus the list buffer: it is reused until an atom has moved more than half
 // the buffer, so no pair inside a filter radius can be missing from it
 // (neigh::lbuffer, src/nblist.cpp:312-530).
-static double list_cutoff(const t9gb_config& c)
+static double list_cutoff(const Context* ctx)
 {
+   const t9gb_config& c = ctx->cfg;
    double r = c.cutoff;
    if (c.pcgprec)
       r = std::max(r, c.usolve_cutoff + c.pbuffer);
+   if (ctx->use_vdw)
+      r = std::max(r, ctx->vdw_off + VDW_SITE_MARGIN);
    return r + std::max(0.0, c.list_buffer);
 }
 
@@ -111,28 +114,54 @@ int order_build(Context* ctx)
       ctx->h_iperm[key[s].second] = s;
    }
 
-   // scaled partners per slot, both directions, ascending partner slot
+   // scaled partners per slot, both directions, ascending partner slot: the
+   // union of the electrostatic (m, d, p, u) and van der Waals scaled pairs,
+   // each scale 1 where the other list does not name the pair
+   struct Scales {
+      float4 e;
+      float v;
+   };
+   std::map<std::pair<int, int>, Scales> pairs;
    const int nex = (int)ctx->h_excl_scale.size() / 4;
-   std::vector<std::vector<std::pair<int, float4>>> part(npad);
    for (int j = 0; j < nex; ++j) {
-      int si = ctx->h_iperm[ctx->h_excl_ik[2 * j]];
-      int sk = ctx->h_iperm[ctx->h_excl_ik[2 * j + 1]];
+      int a = ctx->h_excl_ik[2 * j], b = ctx->h_excl_ik[2 * j + 1];
       const double* v = &ctx->h_excl_scale[4 * j];
-      float4 sc = make_float4((float)v[0], (float)v[1], (float)v[2], (float)v[3]);
-      part[si].push_back({sk, sc});
-      part[sk].push_back({si, sc});
+      pairs[{std::min(a, b), std::max(a, b)}] = {make_float4((float)v[0], (float)v[1], (float)v[2], (float)v[3]), 1.f};
+   }
+   if (ctx->use_vdw) {
+      const int nv = (int)ctx->h_vexcl_scale.size();
+      for (int j = 0; j < nv; ++j) {
+         int a = ctx->h_vexcl_ik[2 * j], b = ctx->h_vexcl_ik[2 * j + 1];
+         auto key = std::make_pair(std::min(a, b), std::max(a, b));
+         auto it = pairs.find(key);
+         if (it == pairs.end())
+            pairs[key] = {make_float4(1.f, 1.f, 1.f, 1.f), (float)ctx->h_vexcl_scale[j]};
+         else
+            it->second.v = (float)ctx->h_vexcl_scale[j];
+      }
+   }
+   struct Part {
+      int k;
+      float4 sc;
+      float v;
+   };
+   std::vector<std::vector<Part>> part(npad);
+   for (const auto& pr : pairs) {
+      const int si = ctx->h_iperm[pr.first.first], sk = ctx->h_iperm[pr.first.second];
+      part[si].push_back({sk, pr.second.e, pr.second.v});
+      part[sk].push_back({si, pr.second.e, pr.second.v});
    }
    std::vector<int> sp_start(npad + 1, 0), sp_j;
    std::vector<float4> sp_sc;
+   std::vector<float> sp_v;
    for (int s = 0; s < npad; ++s) {
       auto& v = part[s];
-      std::sort(v.begin(), v.end(), [](const std::pair<int, float4>& a, const std::pair<int, float4>& b) {
-         return a.first < b.first;
-      });
+      std::sort(v.begin(), v.end(), [](const Part& a, const Part& b) { return a.k < b.k; });
       sp_start[s + 1] = sp_start[s] + (int)v.size();
       for (auto& e : v) {
-         sp_j.push_back(e.first);
-         sp_sc.push_back(e.second);
+         sp_j.push_back(e.k);
+         sp_sc.push_back(e.sc);
+         sp_v.push_back(e.v);
       }
    }
    ctx->nsp = (int)sp_j.size();
@@ -149,7 +178,7 @@ int order_build(Context* ctx)
    }
 
    // cell grid and list capacity
-   const double R = list_cutoff(cfg);
+   const double R = list_cutoff(ctx);
    ctx->list_cut = (float)R;
    ctx->use_cells = false;
    if (pbc && R < 1.0e6) {
@@ -184,6 +213,8 @@ int order_build(Context* ctx)
    cudaFree(ctx->sp_start);
    cudaFree(ctx->sp_j);
    cudaFree(ctx->sp_sc);
+   cudaFree(ctx->sp_v);
+   ctx->sp_v = nullptr;
    cudaFree(ctx->cell_count);
    cudaFree(ctx->cell_start);
    ctx->perm = ctx->iperm = ctx->sp_start = ctx->sp_j = ctx->cell_count = ctx->cell_start = nullptr;
@@ -193,12 +224,14 @@ int order_build(Context* ctx)
    T9_CUDA(cudaMalloc(&ctx->sp_start, sizeof(int) * (npad + 1)));
    T9_CUDA(cudaMalloc(&ctx->sp_j, sizeof(int) * std::max(1, ctx->nsp)));
    T9_CUDA(cudaMalloc(&ctx->sp_sc, sizeof(float4) * std::max(1, ctx->nsp)));
+   T9_CUDA(cudaMalloc(&ctx->sp_v, sizeof(float) * std::max(1, ctx->nsp)));
    T9_CUDA(cudaMemcpy(ctx->perm, ctx->h_perm.data(), sizeof(int) * npad, cudaMemcpyHostToDevice));
    T9_CUDA(cudaMemcpy(ctx->iperm, ctx->h_iperm.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
    T9_CUDA(cudaMemcpy(ctx->sp_start, sp_start.data(), sizeof(int) * (npad + 1), cudaMemcpyHostToDevice));
    if (ctx->nsp) {
       T9_CUDA(cudaMemcpy(ctx->sp_j, sp_j.data(), sizeof(int) * ctx->nsp, cudaMemcpyHostToDevice));
       T9_CUDA(cudaMemcpy(ctx->sp_sc, sp_sc.data(), sizeof(float4) * ctx->nsp, cudaMemcpyHostToDevice));
+      T9_CUDA(cudaMemcpy(ctx->sp_v, sp_v.data(), sizeof(float) * ctx->nsp, cudaMemcpyHostToDevice));
    }
    T9_CUDA(cudaMemcpy(ctx->spolar, pol.data(), sizeof(float) * npad, cudaMemcpyHostToDevice));
    T9_CUDA(cudaMemcpy(ctx->spolinv, pinv.data(), sizeof(float) * npad, cudaMemcpyHostToDevice));

@@ -33,8 +33,80 @@ AMOEBA_POLAR = {
     CL_ION: (4.0, 0.39, ()),
 }
 
+# buffered 14-7 records (R0 diameter A, eps kcal/mol, reduction): water03.prm
+# vdw 1 / 2 (= amoeba09.prm classes 34 / 35, :481-482), ions amoeba09.prm
+# :454 and :462; vdw-12/13/14 scales 0 / 0 / 1 (amoeba09.prm:31-33)
+AMOEBA_VDW = {
+    WATER_O: (3.405, 0.110, 0.0),
+    WATER_H: (2.655, 0.0135, 0.91),
+    NA_ION: (2.955, 0.280, 0.0),
+    CL_ION: (4.120, 0.340, 0.0),
+}
+AMOEBA_VDW_SCALES = {"vdw-12-scale": 0.0, "vdw-13-scale": 0.0, "vdw-14-scale": 1.0, "vdw-15-scale": 1.0}
+VDW_CUTOFF = 9.0  # A, the benchmark configurations' van der Waals cutoff
+
 OH_BOND = 0.9572
 HOH_ANGLE = 104.52
+
+
+@dataclass
+class VdwParams:
+    """Buffered 14-7 van der Waals data for t9gb_set_vdw."""
+
+    vtype: np.ndarray  # [n] index into the pair tables
+    radmin: np.ndarray  # [t][t] combined R0, A
+    epsilon: np.ndarray  # [t][t] combined well depth, kcal/mol
+    red: np.ndarray  # [n] reduction factor toward parent (0: none)
+    parent: np.ndarray  # [n] 0-based; the atom itself without reduction
+    scaled_ik: np.ndarray  # [m][2]
+    scaled_v: np.ndarray  # [m]
+    taper: float
+    off: float
+
+
+def hal_params(types, bonds, records, scales, off, taper=None):
+    """Tinker's buffered 14-7 set-up (kvdw): per-atom (R, eps, red) records
+    keyed by atom type, CUBIC-MEAN radii and HHG well depths, the reduction
+    parent = the first bonded neighbour, vdw-1x-scale pairs by bond
+    separation, taper = 0.9 x cutoff unless given.
+    records: type -> (radius, epsilon, reduction); scales: {'vdw-12-scale': ...}."""
+    n = len(types)
+    kinds = sorted(set(int(t) for t in types))
+    idx = {t: j for j, t in enumerate(kinds)}
+    R = np.array([records[t][0] for t in kinds], dtype=np.float64)
+    E = np.array([records[t][1] for t in kinds], dtype=np.float64)
+    r3, r2 = R[:, None] ** 3 + R[None, :] ** 3, R[:, None] ** 2 + R[None, :] ** 2
+    radmin = np.where(r2 > 0, r3 / np.where(r2 > 0, r2, 1.0), 0.0)
+    se = np.sqrt(E)
+    den = (se[:, None] + se[None, :]) ** 2
+    epsilon = np.where(den > 0, 4.0 * E[:, None] * E[None, :] / np.where(den > 0, den, 1.0), 0.0)
+    adj, sep = topo.bond_distance_lists(n, bonds, 4)
+    red = np.zeros(n)
+    parent = np.arange(n, dtype=np.int32)
+    for i, t in enumerate(types):
+        r = records[int(t)][2] if len(records[int(t)]) > 2 else 0.0
+        if r and adj[i]:
+            red[i] = r
+            parent[i] = adj[i][0]
+    ik, sv = [], []
+    for i in range(n):
+        for k, d in sep[i].items():
+            if k > i and 1 <= d <= 4:
+                v = scales.get(f"vdw-1{d + 1}-scale", 1.0)
+                if v != 1.0:
+                    ik.append((i, k))
+                    sv.append(v)
+    return VdwParams(
+        vtype=np.array([idx[int(t)] for t in types], dtype=np.int32),
+        radmin=radmin,
+        epsilon=epsilon,
+        red=red,
+        parent=parent,
+        scaled_ik=np.array(ik, dtype=np.int32).reshape(-1, 2),
+        scaled_v=np.array(sv, dtype=np.float64),
+        taper=0.9 * off if taper is None else taper,
+        off=off,
+    )
 
 
 @dataclass
@@ -58,6 +130,7 @@ class System:
     ptype: Optional[np.ndarray] = None  # [n] polarization type, with thole_table
     thole_table: Optional[np.ndarray] = None  # [t][t] per-type-pair Thole coefficient
     exfld: Optional[np.ndarray] = None  # uniform external field [3], e/A^2
+    vdw: Optional[VdwParams] = None  # buffered 14-7 van der Waals
 
     @property
     def n(self):
@@ -225,7 +298,9 @@ DEFAULT_SETTINGS = dict(
 )
 
 
-def make_config(name, **over):
+def make_config(name, vdw=False, **over):
+    """A benchmark configuration; vdw=True also attaches the buffered 14-7
+    term (9 A cutoff, taper from 8.1 A)."""
     cfg = dict(CONFIGS[name])
     cfg.update(over)
     lat = make_lattice(
@@ -240,7 +315,19 @@ def make_config(name, **over):
     s.settings["nfft"] = (cfg["nfft"],) * 3
     s.settings["use_ewald"] = 1
     s.lattice = lat
+    if vdw:
+        bonds = lattice_bonds(s)
+        s.vdw = hal_params(s.types.tolist(), bonds, AMOEBA_VDW, AMOEBA_VDW_SCALES, VDW_CUTOFF)
     return s
+
+
+def lattice_bonds(s):
+    """O-H bonds of the lattice waters (molecule starts and sizes)."""
+    bonds = []
+    for st, sz in zip(s.mol_start, s.mol_size):
+        if sz == 3:
+            bonds.extend([(int(st), int(st) + 1), (int(st), int(st) + 2)])
+    return bonds
 
 
 class Trajectory:
