@@ -130,6 +130,25 @@ int t9gb_set_vdw(t9gb_context* ctx, int ntypes, const int* vtype, const double* 
  * include/seq/pair_hal.h:52-96). */
 int t9gb_ehal(t9gb_context* ctx, int vers, double* energy, float* grad_device, double* virial);
 
+/* Bond, angle and Urey-Bradley terms.  Replaces the ebond / eangle / eurey
+ * INIT of evalence (src/evalence.cpp; include/seq/bond.h, angle.h, urey.h):
+ * harmonic bonds ibnd[nbond][2] with force constants bk and ideal lengths
+ * bl and the global bond-cubic / bond-quartic; harmonic angles
+ * iang[nangle][3] (vertex in the middle) with ak, ideal angles anat
+ * (degrees) and angle_terms[4] = angle-cubic, -quartic, -pentic, -sextic;
+ * Urey-Bradley pairs iury[nurey][3] (the 1-3 distance of the ends) with uk,
+ * ul and urey-cubic / -quartic.  bondunit 1, angunit (pi/180)^2, ureyunit 1
+ * (Tinker's defaults).  May be called any time after t9gb_create. */
+int t9gb_set_valence(t9gb_context* ctx, int nbond, const int* ibnd, const double* bk, const double* bl,
+   double bond_cubic, double bond_quartic, int nangle, const int* iang, const double* ak, const double* anat,
+   const double* angle_terms, int nurey, const int* iury, const double* uk, const double* ul, double urey_cubic,
+   double urey_quartic);
+
+/* Valence energy, gradient [n][3] (device) and virial with the calc flags
+ * (calls the coordinates set by t9gb_set_xyz_*).  Replaces void
+ * evalence(int vers) for these three terms. */
+int t9gb_evalence(t9gb_context* ctx, int vers, double* energy, float* grad_device, double* virial);
+
 /* Coordinates [n][3].  Replace copyPosToXyz (src/atom.cpp:161-166). */
 int t9gb_set_xyz_host(t9gb_context* ctx, const double* xyz);
 int t9gb_set_xyz_device(t9gb_context* ctx, const float* xyz_device);

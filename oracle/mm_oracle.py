@@ -7,6 +7,11 @@ gradients and virials come from central differences of these energies
   hal_energy      include/seq/pair_hal.h:52-96 (pair_hal_v2, vlambda = 1),
                   include/math/switch.h:22-33 (switchTaper5), reduced sites as
                   src/cu/ehal.cu (xred = red (x - x_parent) + x_parent)
+  bond_energy     include/seq/bond.h:44-59 (HARMONIC with cubic / quartic,
+                  bondunit 1)
+  angle_energy    include/seq/angle.h:88-115 (HARMONIC, angle in degrees,
+                  angunit (pi/180)^2, cubic ... sextic)
+  urey_energy     include/seq/urey.h:44-53 (ureyunit 1, cubic / quartic)
 """
 import numpy as np
 
@@ -56,3 +61,41 @@ def hal_energy(system, xyz=None, box="system"):
     eps = np.asarray(v.epsilon)[t[iu], t[ku]] * scale[iu, ku]
     m = (r <= v.off) & (eps != 0)
     return float(hal_pair(r[m], rv[m], eps[m], v.taper, v.off).sum())
+
+
+def _image_opt(d, box):
+    return d if box is None else _image(d, box)
+
+
+def bond_energy(xyz, bonds, cubic, quartic, box=None):
+    """bonds: rows (i, k, force constant, ideal length)."""
+    b = np.asarray(bonds, dtype=np.float64).reshape(-1, 4)
+    i, k = b[:, 0].astype(int), b[:, 1].astype(int)
+    x = np.asarray(xyz, dtype=np.float64)
+    r = np.sqrt((_image_opt(x[i] - x[k], box) ** 2).sum(1))
+    dt = r - b[:, 3]
+    return float((b[:, 2] * dt * dt * (1 + cubic * dt + quartic * dt * dt)).sum())
+
+
+def angle_energy(xyz, angles, cubic, quartic, pentic, sextic, box=None):
+    """angles: rows (a, vertex, c, force constant, ideal angle in degrees)."""
+    g = np.asarray(angles, dtype=np.float64).reshape(-1, 5)
+    a, m, c = (g[:, j].astype(int) for j in range(3))
+    x = np.asarray(xyz, dtype=np.float64)
+    u = _image_opt(x[a] - x[m], box)
+    v = _image_opt(x[c] - x[m], box)
+    cos = (u * v).sum(1) / np.sqrt((u * u).sum(1) * (v * v).sum(1))
+    ang = np.degrees(np.arccos(np.clip(cos, -1, 1)))
+    dt = ang - g[:, 4]
+    unit = (np.pi / 180) ** 2
+    return float((unit * g[:, 3] * dt ** 2 * (1 + cubic * dt + quartic * dt ** 2 + pentic * dt ** 3 + sextic * dt ** 4)).sum())
+
+
+def urey_energy(xyz, ureys, cubic, quartic, box=None):
+    """ureys: rows (a, vertex, c, force constant, ideal a-c distance)."""
+    u = np.asarray(ureys, dtype=np.float64).reshape(-1, 5)
+    a, c = u[:, 0].astype(int), u[:, 2].astype(int)
+    x = np.asarray(xyz, dtype=np.float64)
+    r = np.sqrt((_image_opt(x[a] - x[c], box) ** 2).sum(1))
+    dt = r - u[:, 4]
+    return float((u[:, 3] * dt * dt * (1 + cubic * dt + quartic * dt * dt)).sum())

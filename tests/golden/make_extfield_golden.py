@@ -35,7 +35,7 @@ def read_ref(path):
         s = ln.strip()
         if s.startswith("Total Potential Energy"):
             out["energy"] = float(t[-2])
-        elif s.startswith("Atomic Multipoles") or s.startswith("Polarization"):
+        elif s.startswith(("Atomic Multipoles", "Polarization", "Bond Stretching", "Urey-Bradley")):
             out["energy"] = float(t[-2])
         elif s.startswith("Internal Virial Tensor"):
             rows = [t[-3:], lines[i + 1].split(), lines[i + 2].split()]

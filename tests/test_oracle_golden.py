@@ -262,3 +262,33 @@ def test_hal_golden(oracle, title):
     assert np.abs(g - np.array(ex["ref_grad"])).max() < ex["eps"]
     w = oracle._strain_fd(s, lambda s2: mm_oracle.hal_energy(s2), False, 1e-6)
     assert np.abs(w - np.array(ex["ref_v"])).max() < ex["eps"] * 10  # known answers with three decimals
+
+
+def _valence_golden():
+    import json
+    import os
+
+    with open(os.path.join(os.path.dirname(__file__), "golden", "valence.json")) as f:
+        return json.load(f)
+
+
+@pytest.mark.parametrize("term", ["bond", "urey"])
+def test_valence_golden(oracle, term):
+    """Anharmonic bonds of a 304-atom protein (test/bond.cpp) and the
+    Urey-Bradley term of ten waters (test/urey.cpp): energy, gradient,
+    virial of the oracle against the reference's known answers."""
+    from oracle import mm_oracle
+
+    d = _valence_golden()[term]
+    x = np.asarray(d["xyz"], dtype=np.float64)
+    if term == "bond":
+        f = lambda y: mm_oracle.bond_energy(y, d["bonds"], d["cubic"], d["quartic"])
+    else:
+        f = lambda y: mm_oracle.urey_energy(y, d["ureys"], d["cubic"], d["quartic"])
+    ex, eps = d["expected"], d["eps"]
+    assert abs(f(x) - ex["energy"]) < eps["energy"]
+    g = oracle._fd(f, x, list(range(len(x))), 1e-6)
+    assert np.abs(g - np.array(ex["gradient"])).max() < eps["gradient"]
+    # virial: dE/d(eps_ab) = sum_i g_ia x_ib (a translation-invariant sum)
+    w = g.T @ x
+    assert np.abs(0.5 * (w + w.T) - np.array(ex["virial"])).max() < eps["virial"]

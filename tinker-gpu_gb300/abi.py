@@ -29,6 +29,7 @@ EXPORTS = [
     "t9gb_learn_set_weights", "t9gb_learn_eval", "t9gb_learn_adamw", "t9gb_learn_features",
     "t9gb_empole", "t9gb_epolar", "t9gb_emplar", "t9gb_energy_components", "t9gb_pme_own_fft",
     "t9gb_pair_lanes", "t9gb_set_thole_pairs", "t9gb_set_external_field", "t9gb_set_vdw", "t9gb_ehal",
+    "t9gb_set_valence", "t9gb_evalence",
 ]
 CALC_ENERGY, CALC_GRAD, CALC_VIRIAL = 0x010, 0x020, 0x040
 
@@ -126,6 +127,9 @@ def load(path=None):
     lib.t9gb_set_external_field.argtypes = [vp, dp]
     lib.t9gb_set_vdw.argtypes = [vp, C.c_int, ip, dp, dp, dp, ip, C.c_int, ip, dp, C.c_double, C.c_double]
     lib.t9gb_ehal.argtypes = [vp, C.c_int, dp, fp, dp]
+    lib.t9gb_set_valence.argtypes = [vp, C.c_int, ip, dp, dp, C.c_double, C.c_double, C.c_int, ip, dp, dp, dp,
+                                     C.c_int, ip, dp, dp, C.c_double, C.c_double]
+    lib.t9gb_evalence.argtypes = [vp, C.c_int, dp, fp, dp]
     for name in ("t9gb_empole", "t9gb_epolar", "t9gb_emplar"):
         getattr(lib, name).argtypes = [vp, C.c_int, dp, fp, dp]
     _lib = lib
@@ -209,6 +213,24 @@ class Engine:
             self.set_external_field(system.exfld)
         if getattr(system, "vdw", None) is not None:
             self.set_vdw(system.vdw)
+        if getattr(system, "valence", None) is not None:
+            self.set_valence(system.valence)
+
+    def set_valence(self, v):
+        """v: systems.ValenceParams (bonds, angles, Urey-Bradley pairs)."""
+        b = np.asarray(v.bonds, dtype=np.float64).reshape(-1, 4)
+        a = np.asarray(v.angles, dtype=np.float64).reshape(-1, 5)
+        u = np.asarray(v.ureys, dtype=np.float64).reshape(-1, 5)
+        keep = (np.ascontiguousarray(b[:, :2], dtype=np.int32), np.ascontiguousarray(b[:, 2]),
+                np.ascontiguousarray(b[:, 3]), np.ascontiguousarray(a[:, :3], dtype=np.int32),
+                np.ascontiguousarray(a[:, 3]), np.ascontiguousarray(a[:, 4]),
+                np.ascontiguousarray(v.angle_terms, dtype=np.float64), np.ascontiguousarray(u[:, :3], dtype=np.int32),
+                np.ascontiguousarray(u[:, 3]), np.ascontiguousarray(u[:, 4]))
+        self._val_keep = keep
+        self._check(self.lib.t9gb_set_valence(
+            self.h, len(b), _ip(keep[0]), _dp(keep[1]), _dp(keep[2]), float(v.bond_cubic), float(v.bond_quartic),
+            len(a), _ip(keep[3]), _dp(keep[4]), _dp(keep[5]), _dp(keep[6]),
+            len(u), _ip(keep[7]), _dp(keep[8]), _dp(keep[9]), float(v.urey_cubic), float(v.urey_quartic)))
 
     def set_vdw(self, v):
         """v: systems.VdwParams (per-atom types, pair tables, reduction,
@@ -443,6 +465,10 @@ class Engine:
         if vers & CALC_VIRIAL:
             return e.value, g, v.reshape(3, 3)
         return e.value, g
+
+    def evalence(self, vers=CALC_ENERGY | CALC_GRAD):
+        """Bond + angle + Urey-Bradley: (energy, gradient[, virial])."""
+        return self._eg(self.lib.t9gb_evalence, vers)
 
     def ehal(self, vers=CALC_ENERGY | CALC_GRAD):
         """Buffered 14-7 van der Waals: (energy, gradient) or with CALC_VIRIAL

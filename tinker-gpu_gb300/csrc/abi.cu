@@ -122,6 +122,7 @@ static void free_all(Context* ctx)
    learn_free(ctx);
    force_free(ctx);
    vdw_release(ctx);
+   valence_release(ctx);
    drop_graphs(ctx);
    if (ctx->cap_stream)
       cudaStreamDestroy(ctx->cap_stream);

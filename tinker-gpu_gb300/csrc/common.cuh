@@ -171,6 +171,18 @@ struct Context {
    float* fvdw = nullptr;      // [npad][3] dE/dx of each reduced site
    float* sp_v = nullptr;      // [nsp] van der Waals scale of each scaled pair
 
+   // bond / angle / Urey-Bradley terms (t9gb_set_valence), caller order
+   int nval = 0;
+   double val_glob[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // bond c/q, angle c/q/p/s, Urey c/q
+   int4* val_idx = nullptr;    // [nval] (a, b, c, kind)
+   float2* val_par = nullptr;  // [nval] (force constant, ideal)
+   float* val_g = nullptr;     // [nval][3][3] gradient slots
+   double* val_e = nullptr;    // [nval]
+   float* val_w = nullptr;     // [9][nval] virial rows
+   int* val_start = nullptr;   // [n + 1] per-atom slot lists
+   int* val_ent = nullptr;
+   double* val_sum = nullptr;  // [10]
+
    // coordinates, caller order
    float* xyz = nullptr;       // [n][3]
    std::vector<double> h_xyz;  // host copy for the ordering, refreshed by t9gb_nblist_build
@@ -428,6 +440,11 @@ int sum_rows_virial(Context* ctx, const float* rows, int nblocks, double* virial
 // to or stored in grad when not null); energy rows in e_atom[2 npad ..)
 int vdw_forces(Context* ctx, float* grad, bool add, bool vir, double* energy);
 void vdw_release(Context* ctx);
+// valence.cu: bond / angle / Urey-Bradley gradient (into or added to grad),
+// then their energy and virial sums
+int valence_forces(Context* ctx, float* grad, bool add, bool vir);
+int valence_sums(Context* ctx, double* energy, double* virial);
+void valence_release(Context* ctx);
 int learn_pick(Context* ctx, const float* ug8, const float* fld8);
 int learn_train(Context* ctx);
 int learn_features_out(Context* ctx, float* out_dev);

@@ -45,6 +45,14 @@ AMOEBA_VDW = {
 AMOEBA_VDW_SCALES = {"vdw-12-scale": 0.0, "vdw-13-scale": 0.0, "vdw-14-scale": 1.0, "vdw-15-scale": 1.0}
 VDW_CUTOFF = 9.0  # A, the benchmark configurations' van der Waals cutoff
 
+# water valence (water03.prm :107, :118, :129 and its global terms :11-17):
+# O-H bond, H-O-H angle, H-H Urey-Bradley
+WATER_BOND = (556.85, 0.9572)
+WATER_ANGLE = (48.70, 108.50)
+WATER_UREY = (-7.60, 1.5537)
+BOND_CUBIC, BOND_QUARTIC = -2.55, 3.793125
+ANGLE_TERMS = (-0.014, 0.000056, -0.0000007, 0.000000022)
+
 OH_BOND = 0.9572
 HOH_ANGLE = 104.52
 
@@ -110,6 +118,20 @@ def hal_params(types, bonds, records, scales, off, taper=None):
 
 
 @dataclass
+class ValenceParams:
+    """Bond / angle / Urey-Bradley terms for t9gb_set_valence."""
+
+    bonds: np.ndarray  # [nb][4]: i, k, force constant, ideal length
+    angles: np.ndarray  # [na][5]: a, vertex, c, force constant, ideal degrees
+    ureys: np.ndarray  # [nu][5]: a, vertex, c, force constant, ideal 1-3 length
+    bond_cubic: float = 0.0
+    bond_quartic: float = 0.0
+    angle_terms: tuple = (0.0, 0.0, 0.0, 0.0)  # cubic, quartic, pentic, sextic
+    urey_cubic: float = 0.0
+    urey_quartic: float = 0.0
+
+
+@dataclass
 class System:
     """Everything the polarization path needs about one system."""
 
@@ -131,6 +153,7 @@ class System:
     thole_table: Optional[np.ndarray] = None  # [t][t] per-type-pair Thole coefficient
     exfld: Optional[np.ndarray] = None  # uniform external field [3], e/A^2
     vdw: Optional[VdwParams] = None  # buffered 14-7 van der Waals
+    valence: Optional[ValenceParams] = None  # bond / angle / Urey-Bradley
 
     @property
     def n(self):
@@ -298,9 +321,10 @@ DEFAULT_SETTINGS = dict(
 )
 
 
-def make_config(name, vdw=False, **over):
+def make_config(name, vdw=False, valence=False, **over):
     """A benchmark configuration; vdw=True also attaches the buffered 14-7
-    term (9 A cutoff, taper from 8.1 A)."""
+    term (9 A cutoff, taper from 8.1 A), valence=True the water bond, angle
+    and Urey-Bradley terms (the MD force field)."""
     cfg = dict(CONFIGS[name])
     cfg.update(over)
     lat = make_lattice(
@@ -318,7 +342,25 @@ def make_config(name, vdw=False, **over):
     if vdw:
         bonds = lattice_bonds(s)
         s.vdw = hal_params(s.types.tolist(), bonds, AMOEBA_VDW, AMOEBA_VDW_SCALES, VDW_CUTOFF)
+    if valence:
+        s.valence = water_valence(s)
     return s
+
+
+def water_valence(s, bond=WATER_BOND, angle=WATER_ANGLE, urey=WATER_UREY):
+    """Valence terms of the waters of a system (molecules of three atoms,
+    oxygen first)."""
+    b, a, u = [], [], []
+    for st, sz in zip(s.mol_start, s.mol_size):
+        if sz == 3:
+            o, h1, h2 = int(st), int(st) + 1, int(st) + 2
+            b += [(o, h1) + bond, (o, h2) + bond]
+            a.append((h1, o, h2) + angle)
+            u.append((h1, o, h2) + urey)
+    return ValenceParams(bonds=np.array(b, dtype=np.float64).reshape(-1, 4),
+                         angles=np.array(a, dtype=np.float64).reshape(-1, 5),
+                         ureys=np.array(u, dtype=np.float64).reshape(-1, 5), bond_cubic=BOND_CUBIC,
+                         bond_quartic=BOND_QUARTIC, angle_terms=ANGLE_TERMS)
 
 
 def lattice_bonds(s):
