@@ -149,6 +149,29 @@ int t9gb_set_valence(t9gb_context* ctx, int nbond, const int* ibnd, const double
  * evalence(int vers) for these three terms. */
 int t9gb_evalence(t9gb_context* ctx, int vers, double* energy, float* grad_device, double* virial);
 
+/* ---- Molecular dynamics ---- */
+
+/* Start a trajectory at positions xyz[n][3] (A) with masses[n] (g/mol) and
+ * velocities vel[n][3] (A/ps, NULL for zero): sets the coordinates, builds
+ * the spatial order if needed and evaluates the first gradient (the
+ * integrator's KickOff, src/md/integrator.cpp:186-190).  Forces are the
+ * multipole + polarization terms (induce included), plus the van der Waals
+ * and valence terms when set. */
+int t9gb_md_init(t9gb_context* ctx, const double* xyz, const double* mass, const double* vel);
+
+/* nsteps velocity-Verlet steps of dt ps (BasicIntegrator::dynamic with
+ * nrespa 1, src/md/integrator.cpp:70-170).  thermostat 0: none (NVE);
+ * 1: Bussi velocity rescaling toward kelvin with coupling time tau ps and
+ * nfree degrees of freedom (<= 0: 3n - 3), variates from a generator seeded
+ * by seed (bussiThermostat, src/mdpt.cpp:41-71).  Returns the last kinetic
+ * energy (kcal/mol) and temperature (K) when the pointers are not NULL. */
+int t9gb_md_run(t9gb_context* ctx, int nsteps, double dt_ps, int thermostat, double kelvin, double tau_ps, int nfree,
+   unsigned long long seed, double* ekin, double* temperature);
+
+/* Current positions / velocities (host, [n][3], may be NULL) and the
+ * gradient at them (device [n][3], may be NULL). */
+int t9gb_md_state(t9gb_context* ctx, double* xyz, double* vel, float* grad_device);
+
 /* Coordinates [n][3].  Replace copyPosToXyz (src/atom.cpp:161-166). */
 int t9gb_set_xyz_host(t9gb_context* ctx, const double* xyz);
 int t9gb_set_xyz_device(t9gb_context* ctx, const float* xyz_device);

@@ -27,6 +27,9 @@ def load():
         "xyz": z["xyz_e6"] * 1e-6,
         "uind": z["uind_e6"] * 1e-6,
         "udir": z["udir_e6"] * 1e-6,
+        "vel": z["vel_e6"] * 1e-6,
+        "dyn_x": z["dyn_x"],
+        "dyn_v": z["dyn_v"],
     }
 
 
@@ -45,3 +48,38 @@ def system(fx=None, frame=0):
     st.update(use_ewald=1, ewald_cutoff=cut, nfft=(NFFT,) * 3, aewald=tg.systems.ewald_coefficient(cut))
     s.settings = st
     return s, fx
+
+
+def md_system(fx=None):
+    """The water30 restart (positions and velocities of test/file/tinkernist/
+    water30.dyn) with the whole amoeba09 force field of the MD test: the
+    electrostatics above, buffered 14-7 van der Waals (12 A cutoff, taper
+    from 10.8 A) and the water bond / angle / Urey-Bradley terms.
+    Returns (system, masses, velocities, fixture)."""
+    fx = load() if fx is None else fx
+    m = fx["meta"]
+    md = m["md"]
+    s, _ = system(fx, 0)
+    s.xyz = np.array(fx["dyn_x"], dtype=np.float64)
+    types = fx["types"]
+    vrec = {int(t): tuple(v) + ((0.0,) if len(v) == 2 else ()) for t, v in md["vdw"].items()}
+    # vdw-12 / -13 / -14 scales 0 / 0 / 1 (amoeba09.prm:31-34)
+    s.vdw = tg.systems.hal_params(types, fx["bonds"], vrec, tg.systems.AMOEBA_VDW_SCALES, m["vdw_cutoff"])
+    b, a, u = [], [], []
+    adj = {}
+    for i, k in fx["bonds"]:
+        adj.setdefault(i, []).append(k)
+        adj.setdefault(k, []).append(i)
+    for o, hs in sorted(adj.items()):
+        if types[o] == 36 and len(hs) == 2:
+            h1, h2 = sorted(hs)
+            b += [(o, h1) + tuple(md["bond"]), (o, h2) + tuple(md["bond"])]
+            a.append((h1, o, h2) + tuple(md["angle"]))
+            u.append((h1, o, h2) + tuple(md["urey"]))
+    g = md["globals"]
+    s.valence = tg.systems.ValenceParams(
+        bonds=np.array(b), angles=np.array(a), ureys=np.array(u), bond_cubic=g["bond-cubic"],
+        bond_quartic=g["bond-quartic"],
+        angle_terms=(g["angle-cubic"], g["angle-quartic"], g["angle-pentic"], g["angle-sextic"]))
+    mass = np.array([md["mass"][str(t)] for t in types])
+    return s, mass, np.array(fx["dyn_v"], dtype=np.float64), fx

@@ -29,7 +29,7 @@ EXPORTS = [
     "t9gb_learn_set_weights", "t9gb_learn_eval", "t9gb_learn_adamw", "t9gb_learn_features",
     "t9gb_empole", "t9gb_epolar", "t9gb_emplar", "t9gb_energy_components", "t9gb_pme_own_fft",
     "t9gb_pair_lanes", "t9gb_set_thole_pairs", "t9gb_set_external_field", "t9gb_set_vdw", "t9gb_ehal",
-    "t9gb_set_valence", "t9gb_evalence",
+    "t9gb_set_valence", "t9gb_evalence", "t9gb_md_init", "t9gb_md_run", "t9gb_md_state",
 ]
 CALC_ENERGY, CALC_GRAD, CALC_VIRIAL = 0x010, 0x020, 0x040
 
@@ -130,6 +130,10 @@ def load(path=None):
     lib.t9gb_set_valence.argtypes = [vp, C.c_int, ip, dp, dp, C.c_double, C.c_double, C.c_int, ip, dp, dp, dp,
                                      C.c_int, ip, dp, dp, C.c_double, C.c_double]
     lib.t9gb_evalence.argtypes = [vp, C.c_int, dp, fp, dp]
+    lib.t9gb_md_init.argtypes = [vp, dp, dp, dp]
+    lib.t9gb_md_run.argtypes = [vp, C.c_int, C.c_double, C.c_int, C.c_double, C.c_double, C.c_int, C.c_ulonglong, dp,
+                                dp]
+    lib.t9gb_md_state.argtypes = [vp, dp, dp, fp]
     for name in ("t9gb_empole", "t9gb_epolar", "t9gb_emplar"):
         getattr(lib, name).argtypes = [vp, C.c_int, dp, fp, dp]
     _lib = lib
@@ -465,6 +469,29 @@ class Engine:
         if vers & CALC_VIRIAL:
             return e.value, g, v.reshape(3, 3)
         return e.value, g
+
+    # ---- molecular dynamics ----
+    def md_init(self, xyz, mass, vel=None):
+        x = np.ascontiguousarray(xyz, dtype=np.float64)
+        m = np.ascontiguousarray(mass, dtype=np.float64)
+        v = None if vel is None else np.ascontiguousarray(vel, dtype=np.float64)
+        self._check(self.lib.t9gb_md_init(self.h, _dp(x), _dp(m), None if v is None else _dp(v)))
+
+    def md_run(self, nsteps, dt_ps=0.001, thermostat=0, kelvin=298.0, tau_ps=0.1, nfree=0, seed=1):
+        """Returns (kinetic energy kcal/mol, temperature K, status)."""
+        ek, t = C.c_double(), C.c_double()
+        rc = self.lib.t9gb_md_run(self.h, int(nsteps), float(dt_ps), int(thermostat), float(kelvin), float(tau_ps),
+                                  int(nfree), int(seed), C.byref(ek), C.byref(t))
+        self._check(rc, allow=(T9GB_NOT_CONVERGED,))
+        return ek.value, t.value, rc
+
+    def md_state(self):
+        """(positions, velocities, gradient) of the trajectory."""
+        x = np.zeros((self.n, 3))
+        v = np.zeros((self.n, 3))
+        g = self._empty3()
+        self._check(self.lib.t9gb_md_state(self.h, _dp(x), _dp(v), C.c_void_p(g.data_ptr())))
+        return x, v, g
 
     def evalence(self, vers=CALC_ENERGY | CALC_GRAD):
         """Bond + angle + Urey-Bradley: (energy, gradient[, virial])."""

@@ -12,7 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(CSRC, "_build")
 LIB = os.path.join(BUILD, "libt9gb.so")
-SOURCES = ["abi.cu", "nblist.cu", "pair.cu", "pme.cu", "pcg.cu", "energy.cu", "mlp.cu", "learn.cu", "force.cu", "vdw.cu", "valence.cu", "noalloc.cu"]
+SOURCES = ["abi.cu", "nblist.cu", "pair.cu", "pme.cu", "pcg.cu", "energy.cu", "mlp.cu", "learn.cu", "force.cu", "vdw.cu", "valence.cu", "md.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 

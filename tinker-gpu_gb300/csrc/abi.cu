@@ -123,6 +123,7 @@ static void free_all(Context* ctx)
    force_free(ctx);
    vdw_release(ctx);
    valence_release(ctx);
+   md_release(ctx);
    drop_graphs(ctx);
    if (ctx->cap_stream)
       cudaStreamDestroy(ctx->cap_stream);

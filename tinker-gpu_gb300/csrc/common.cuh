@@ -7,6 +7,7 @@
 #include <cufft.h>
 
 #include <cstdint>
+#include <random>
 #include <string>
 #include <vector>
 
@@ -182,6 +183,18 @@ struct Context {
    int* val_start = nullptr;   // [n + 1] per-atom slot lists
    int* val_ent = nullptr;
    double* val_sum = nullptr;  // [10]
+
+   // molecular dynamics state (t9gb_md_init / t9gb_md_run), caller order
+   double* md_x = nullptr;     // [n][3] positions, FP64
+   double* md_v = nullptr;     // [n][3] velocities, A/ps
+   double* md_minv = nullptr;  // [n] 1 / mass
+   float* md_g = nullptr;      // [n][3] total gradient at md_x
+   double* md_red = nullptr;   // kinetic-energy partials
+   double* md_out = nullptr;   // [2] + ticket
+   int* md_ticket = nullptr;
+   bool md_ready = false;
+   std::mt19937_64 md_rng;     // Bussi thermostat variates (host)
+   unsigned long long md_seed = ~0ull;
 
    // coordinates, caller order
    float* xyz = nullptr;       // [n][3]
@@ -445,6 +458,7 @@ void vdw_release(Context* ctx);
 int valence_forces(Context* ctx, float* grad, bool add, bool vir);
 int valence_sums(Context* ctx, double* energy, double* virial);
 void valence_release(Context* ctx);
+void md_release(Context* ctx);  // md.cu
 int learn_pick(Context* ctx, const float* ug8, const float* fld8);
 int learn_train(Context* ctx);
 int learn_features_out(Context* ctx, float* out_dev);

@@ -1,0 +1,233 @@
+// Molecular dynamics around induce(): velocity Verlet with an optional Bussi
+// thermostat, forces from the multipole + polarization terms (t9gb_emplar's
+// path, induce included), the buffered 14-7 van der Waals and the valence
+// terms, whichever the context holds.
+//
+// Restates the reference's VerletIntegrator (src/md/integrator.cpp:70-190:
+// KickOff energy, vel1(dt/2), pos(dt), energy, vel2(dt/2), thermostat
+// control2) and bussiThermostat (src/mdpt.cpp:41-71).  Positions and
+// velocities are FP64 on the device (caller order); forces come in FP32 as
+// in the reference's mixed build.  a = -g / m * ekcal, ekcal = 418.4
+// (kcal/mol -> g/mol A^2/ps^2).
+#include "common.cuh"
+#include "reduce.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <random>
+
+namespace t9gb {
+
+constexpr double EKCAL = 418.4;
+constexpr double GASCONST = 1.987204259e-3;  // kcal/mol/K (Tinker's units::gasconst)
+
+// v += -g ekcal / m * h
+__global__ void k_md_kick(int n, double h, const float* __restrict__ g, const double* __restrict__ minv,
+   double* __restrict__ v)
+{
+   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < 3 * n; e += gridDim.x * blockDim.x)
+      v[e] -= h * EKCAL * minv[e / 3] * (double)g[e];
+}
+
+// x += v dt; the force kernels' float copy
+__global__ void k_md_drift(int n, double dt, const double* __restrict__ v, double* __restrict__ x,
+   float* __restrict__ xf)
+{
+   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < 3 * n; e += gridDim.x * blockDim.x) {
+      const double y = x[e] + dt * v[e];
+      x[e] = y;
+      xf[e] = (float)y;
+   }
+}
+
+// 1/2 sum m v^2 (g/mol A^2/ps^2), fixed order: block partials then one block
+__global__ void k_md_kinetic(int n, const double* __restrict__ v, const double* __restrict__ minv,
+   double* __restrict__ red, double* __restrict__ out, int* __restrict__ ticket)
+{
+   __shared__ double sh[64];
+   double s = 0;
+   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+      const double* w = v + 3 * i;
+      s += (w[0] * w[0] + w[1] * w[1] + w[2] * w[2]) / minv[i];
+   }
+   store_partial(red, 0, s, sh);
+   if (!last_block(ticket))
+      return;
+   double t[1];
+   sum_slots(red, 0, 1, gridDim.x, sh, t);
+   if (threadIdx.x == 0)
+      *out = 0.5 * t[0];
+}
+
+__global__ void k_md_scale(int n, double s, double* __restrict__ v)
+{
+   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < 3 * n; e += gridDim.x * blockDim.x)
+      v[e] *= s;
+}
+
+static int md_free(Context* ctx)
+{
+   void* p[] = {ctx->md_x, ctx->md_v, ctx->md_minv, ctx->md_g, ctx->md_red, ctx->md_out};
+   for (void* q : p)
+      if (q)
+         cudaFree(q);
+   ctx->md_x = ctx->md_v = ctx->md_minv = ctx->md_red = ctx->md_out = nullptr;
+   ctx->md_g = nullptr;
+   ctx->md_ready = false;
+   return T9GB_OK;
+}
+
+void md_release(Context* ctx) { md_free(ctx); }
+
+// total gradient at ctx->xyz into md_g
+static int md_forces(Context* ctx, t9gb_context* h)
+{
+   T9_CHECK(scatter_positions(ctx));
+   T9_CHECK(rotpole_sorted(ctx));
+   int st = t9gb_emplar(h, T9GB_CALC_GRAD, nullptr, ctx->md_g, nullptr);
+   if (st != T9GB_OK)
+      return st;
+   T9_CHECK(vdw_forces(ctx, ctx->md_g, true, false, nullptr));
+   T9_CHECK(valence_forces(ctx, ctx->md_g, true, false));
+   return T9GB_OK;
+}
+
+static int md_kinetic(Context* ctx, double* ekin)
+{
+   const int nb = std::min(RED_MAX, grid_for(ctx->n, 256));
+   k_md_kinetic<<<nb, 256, 0, ctx->stream>>>(ctx->n, ctx->md_v, ctx->md_minv, ctx->md_red, ctx->md_out,
+      ctx->md_ticket);
+   T9_CUDA(cudaGetLastError());
+   double e;
+   T9_CUDA(cudaMemcpyAsync(&e, ctx->md_out, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+   T9_CUDA(cudaStreamSynchronize(ctx->stream));
+   *ekin = e / EKCAL;  // kcal/mol
+   return T9GB_OK;
+}
+
+}  // namespace t9gb
+
+using namespace t9gb;
+
+extern "C" int t9gb_md_init(t9gb_context* h, const double* xyz, const double* mass, const double* vel)
+{
+   if (!h || !xyz || !mass)
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   if (!ctx->have_topology)
+      return T9GB_NOT_READY;
+   const int n = ctx->n;
+   std::vector<double> minv(n);
+   for (int i = 0; i < n; ++i) {
+      if (!(mass[i] > 0) || !std::isfinite(mass[i]))
+         return T9GB_BAD_ARG;
+      minv[i] = 1.0 / mass[i];
+   }
+   for (int i = 0; i < 3 * n; ++i)
+      if (!std::isfinite(xyz[i]) || (vel && !std::isfinite(vel[i])))
+         return T9GB_BAD_ARG;
+   md_free(ctx);
+   T9_CUDA(cudaMalloc(&ctx->md_x, sizeof(double) * 3 * n));
+   T9_CUDA(cudaMalloc(&ctx->md_v, sizeof(double) * 3 * n));
+   T9_CUDA(cudaMalloc(&ctx->md_minv, sizeof(double) * n));
+   T9_CUDA(cudaMalloc(&ctx->md_g, sizeof(float) * 3 * n));
+   T9_CUDA(cudaMalloc(&ctx->md_red, sizeof(double) * RED_MAX));
+   T9_CUDA(cudaMalloc(&ctx->md_out, sizeof(double) * 2 + sizeof(int) * 2));
+   ctx->md_ticket = reinterpret_cast<int*>(ctx->md_out + 2);
+   T9_CUDA(cudaMemset(ctx->md_out, 0, sizeof(double) * 2 + sizeof(int) * 2));
+   T9_CUDA(cudaMemcpy(ctx->md_x, xyz, sizeof(double) * 3 * n, cudaMemcpyHostToDevice));
+   T9_CUDA(cudaMemcpy(ctx->md_minv, minv.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+   if (vel)
+      T9_CUDA(cudaMemcpy(ctx->md_v, vel, sizeof(double) * 3 * n, cudaMemcpyHostToDevice));
+   else
+      T9_CUDA(cudaMemset(ctx->md_v, 0, sizeof(double) * 3 * n));
+   T9_CUDA(cudaDeviceSynchronize());
+   // the force kernels' coordinates, the spatial order, and the first forces
+   // (the integrator's KickOff)
+   T9_CHECK(t9gb_set_xyz_host(h, xyz));
+   if (!ctx->have_order)
+      T9_CHECK(t9gb_nblist_build(h));
+   T9_CHECK(md_forces(ctx, h));
+   ctx->md_ready = true;
+   return T9GB_OK;
+}
+
+extern "C" int t9gb_md_run(t9gb_context* h, int nsteps, double dt, int thermostat, double kelvin, double tau,
+   int nfree, unsigned long long seed, double* ekin_out, double* temp_out)
+{
+   if (!h || nsteps < 0 || !(dt > 0) || thermostat < 0 || thermostat > 1)
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   if (!ctx->md_ready)
+      return T9GB_NOT_READY;
+   const int n = ctx->n;
+   if (nfree <= 0)
+      nfree = 3 * n - 3;
+   if (thermostat == 1 && (!(kelvin > 0) || !(tau > 0) || nfree < 2))
+      return T9GB_BAD_ARG;
+   if (thermostat == 1 && ctx->md_seed != seed) {
+      ctx->md_rng.seed(seed);
+      ctx->md_seed = seed;
+   }
+   const int nb = grid_for(3 * n, 256);
+   for (int step = 0; step < nsteps; ++step) {
+      k_md_kick<<<nb, 256, 0, ctx->stream>>>(n, 0.5 * dt, ctx->md_g, ctx->md_minv, ctx->md_v);
+      k_md_drift<<<nb, 256, 0, ctx->stream>>>(n, dt, ctx->md_v, ctx->md_x, ctx->xyz);
+      T9_CUDA(cudaGetLastError());
+      // a solve that fails to converge leaves no forces: the trajectory stops
+      // there, as the reference's induce throws (src/cu/amoeba/pcg.cu:180-184)
+      const int st = md_forces(ctx, h);
+      if (st != T9GB_OK)
+         return st;
+      k_md_kick<<<nb, 256, 0, ctx->stream>>>(n, 0.5 * dt, ctx->md_g, ctx->md_minv, ctx->md_v);
+      T9_CUDA(cudaGetLastError());
+      if (thermostat == 1) {
+         double ek;
+         T9_CHECK(md_kinetic(ctx, &ek));
+         double temp = 2.0 * ek / (nfree * GASCONST);
+         if (temp == 0)
+            temp = 0.1;
+         const double c = std::exp(-dt / tau);
+         const double d = (1 - c) * (kelvin / temp) / nfree;
+         std::normal_distribution<double> gauss(0.0, 1.0);
+         std::gamma_distribution<double> gam(0.5 * (nfree - 1), 2.0);  // chi-squared, nfree - 1
+         const double r = gauss(ctx->md_rng);
+         const double s = gam(ctx->md_rng);
+         double scale = std::sqrt(c + (s + r * r) * d + 2 * r * std::sqrt(c * d));
+         if (r + std::sqrt(c / d) < 0)
+            scale = -scale;
+         k_md_scale<<<nb, 256, 0, ctx->stream>>>(n, scale, ctx->md_v);
+         T9_CUDA(cudaGetLastError());
+      }
+   }
+   // the context's host coordinates follow the trajectory (t9gb_nblist_build
+   // orders from them)
+   if (ekin_out || temp_out) {
+      double ek;
+      T9_CHECK(md_kinetic(ctx, &ek));
+      if (ekin_out)
+         *ekin_out = ek;
+      if (temp_out)
+         *temp_out = 2.0 * ek / (nfree * GASCONST);
+   }
+   T9_CUDA(cudaStreamSynchronize(ctx->stream));
+   return T9GB_OK;
+}
+
+extern "C" int t9gb_md_state(t9gb_context* h, double* xyz, double* vel, float* grad_device)
+{
+   if (!h)
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   if (!ctx->md_ready)
+      return T9GB_NOT_READY;
+   const int n = ctx->n;
+   if (xyz)
+      T9_CUDA(cudaMemcpyAsync(xyz, ctx->md_x, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
+   if (vel)
+      T9_CUDA(cudaMemcpyAsync(vel, ctx->md_v, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
+   if (grad_device)
+      T9_CUDA(cudaMemcpyAsync(grad_device, ctx->md_g, sizeof(float) * 3 * n, cudaMemcpyDeviceToDevice, ctx->stream));
+   T9_CUDA(cudaStreamSynchronize(ctx->stream));
+   return T9GB_OK;
+}
