@@ -47,6 +47,7 @@ def parse():
     ap.add_argument("--learn-train", type=int, default=500, help="online training steps before the learned legs")
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--no-forces", action="store_true")
+    ap.add_argument("--no-md", action="store_true", help="skip the MD leg (ns/day)")
     ap.add_argument("--no-large", action="store_true", help="skip the 98,304-atom leg")
     ap.add_argument("--large-config", default="water98304")
     ap.add_argument("--fft", choices=["auto", "own", "cufft"], default="auto",
@@ -243,6 +244,50 @@ def kernel_rooflines(kernels, n, entries, nfft, peak):
         gbs = alg / (v["ms_per_launch"] / 1000.0) / 1e9
         out[k] = {"algorithmic_bytes": alg, "achieved_gbs": gbs, "frac": gbs / peak}
     return out
+
+
+def md_leg(args, abi, tg, stream):
+    """ns/day: velocity-Verlet MD of the configuration with the whole water
+    force field -- multipole + polarization (induce with the ASPC predictor,
+    PCG to 1e-6 D), buffered 14-7 van der Waals (9 A, taper from 8.1 A) and
+    the water bond / angle / Urey-Bradley terms -- under the Bussi thermostat
+    at 298 K, 1 fs steps.  Starts from seeded Maxwell-Boltzmann velocities on
+    the synthetic lattice (no 2 ps relaxation)."""
+    import torch
+
+    s = tg.systems.make_config(args.config, vdw=True, valence=True)
+    mass = np.where(s.types == tg.systems.WATER_O, 15.999,
+                    np.where(s.types == tg.systems.WATER_H, 1.008,
+                             np.where(s.types == tg.systems.NA_ION, 22.99, 35.453)))
+    rng = np.random.default_rng(29)
+    v0 = rng.normal(size=(s.n, 3)) * np.sqrt(1.987204259e-3 * 298.0 * 418.4 / mass)[:, None]
+    eng = abi.Engine(s, predictor=1, stream=stream)
+    eng.prepare(s.xyz)
+    if args.fft != "auto":
+        eng.pme_own_fft(args.fft == "own")
+    dt_fs = 1.0
+    eng.md_init(s.xyz, mass, v0)
+    with torch.cuda.stream(stream):
+        eng.md_run(max(args.warmup, 20), dt_fs * 1e-3, thermostat=1, kelvin=298.0, tau_ps=0.1, seed=3)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        w0 = time.perf_counter()
+        a.record(stream)
+        ek, temp, _ = eng.md_run(args.steps, dt_fs * 1e-3, thermostat=1, kelvin=298.0, tau_ps=0.1, seed=3)
+        b.record(stream)
+        b.synchronize()
+        wall = time.perf_counter() - w0
+    ms = a.elapsed_time(b) / args.steps
+    eng.close()
+    return {
+        "ms_per_step": ms,
+        "wall_ms_per_step": 1000 * wall / args.steps,
+        "ns_per_day": 86.4 * dt_fs / ms,
+        "steps": args.steps,
+        "temperature_k": temp,
+        "config": f"{args.config}: multipole + polarization (ASPC, PCG 1e-6 D), HAL 9 A, water valence; "
+                  "Bussi 298 K (tau 0.1 ps), 1 fs velocity Verlet",
+    }
 
 
 def large_leg(args, abi, tg, stream, flush, peak):
@@ -529,6 +574,10 @@ def main():
     if not args.no_large:
         large = large_leg(args, abi, tg, stream, flush, peak)
 
+    md = None
+    if not args.no_md:
+        md = md_leg(args, abi, tg, stream)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline_sample(args, s, tr)
@@ -558,8 +607,9 @@ def main():
             },
             "induce_ms_per_step": 1000 * dev_sec / args.steps,
             "pcg_iterations_per_step": mean_it,
-            "ns_per_day": None,
-            "ns_per_day_note": "needs the MD rows (HAL vdW, valence, integrator); not built",
+            "ns_per_day": None if md is None else md["ns_per_day"],
+            "ns_per_day_note": "MD leg (see md)" if md is not None else "MD leg skipped (--no-md)",
+            "md": md,
             "wall_s_timed": wall,
             "e2e": {"value": e2e_value, "unit": "induce() calls/s", "ms_per_step": 1000 * e2e_sec / args.steps,
                     "h2d_bytes_per_step": 3 * s.n * 4, "d2h_bytes_per_step": 6 * s.n * 4},
