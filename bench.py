@@ -4,8 +4,9 @@ A step is one induce() call -- permanent field (PME + real space), PCG to a
 1e-6 Debye RMS residual with the sparse preconditioner and the ASPC predictor
 -- on one frame of a seeded 1 fs trajectory of the 12,288-atom AMOEBA water
 box (49.31 A, PME 64^3, order 5, a = 0.5446, 7 A cutoff).  Frames are
-synthetic: molecules librate and rattle about seeded lattice sites (the
-reference's 2 ps NVT relaxation needs the MD rows that are not built yet).
+synthetic: molecules librate and rattle about seeded lattice sites, so the
+induce legs time the same coordinates on every run.  The MD leg (ns/day)
+integrates the same box with the whole water force field.
 
 value: induce() calls per second over all ranks, inputs resident in HBM.
 e2e:   the same through t9gb_induce_host: host coordinates in, host dipoles
@@ -252,7 +253,9 @@ def md_leg(args, abi, tg, stream):
     PCG to 1e-6 D), buffered 14-7 van der Waals (9 A, taper from 8.1 A) and
     the water bond / angle / Urey-Bradley terms -- under the Bussi thermostat
     at 298 K, 1 fs steps.  Starts from seeded Maxwell-Boltzmann velocities on
-    the synthetic lattice (no 2 ps relaxation)."""
+    the synthetic lattice, relaxed first by 500 untimed steps under a strong
+    coupling (tau 0.01 ps): the lattice's randomly oriented waters release
+    their packing energy as heat within the first tenths of a picosecond."""
     import torch
 
     s = tg.systems.make_config(args.config, vdw=True, valence=True)
@@ -268,6 +271,7 @@ def md_leg(args, abi, tg, stream):
     dt_fs = 1.0
     eng.md_init(s.xyz, mass, v0)
     with torch.cuda.stream(stream):
+        _, t_relax, _ = eng.md_run(500, dt_fs * 1e-3, thermostat=1, kelvin=298.0, tau_ps=0.01, seed=3)
         eng.md_run(max(args.warmup, 20), dt_fs * 1e-3, thermostat=1, kelvin=298.0, tau_ps=0.1, seed=3)
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
@@ -285,6 +289,7 @@ def md_leg(args, abi, tg, stream):
         "ns_per_day": 86.4 * dt_fs / ms,
         "steps": args.steps,
         "temperature_k": temp,
+        "relaxation": {"steps": 500, "tau_ps": 0.01, "temperature_k": t_relax},
         "config": f"{args.config}: multipole + polarization (ASPC, PCG 1e-6 D), HAL 9 A, water valence; "
                   "Bussi 298 K (tau 0.1 ps), 1 fs velocity Verlet",
     }

@@ -194,6 +194,8 @@ struct Context {
    int* md_ticket = nullptr;
    bool md_ready = false;
    std::mt19937_64 md_rng;     // Bussi thermostat variates (host)
+   double* md_rs = nullptr;    // [2][nsteps] variates of the current run
+   int md_rs_cap = 0;
    unsigned long long md_seed = ~0ull;
 
    // coordinates, caller order

@@ -217,6 +217,10 @@ static int elec_terms(Context* ctx, bool mpole, bool polar, int vers, double* en
          return rc;
    }
    for (int attempt = 0; attempt < 2; ++attempt) {
+      // a list refreshed here needs its capacity checked; one already checked
+      // (after the solve above, or an earlier call) does not, and the gradient
+      // then stays in stream order without a synchronisation
+      const bool fresh = ctx->list_stale || ctx->list_need_build;
       T9_CHECK(ensure_list(ctx));
       T9_CUDA(cudaMemsetAsync(ctx->e_atom, 0, sizeof(double) * 3 * ctx->npad, ctx->stream));
       if (vers & (T9GB_CALC_GRAD | T9GB_CALC_VIRIAL)) {
@@ -227,6 +231,8 @@ static int elec_terms(Context* ctx, bool mpole, bool polar, int vers, double* en
          T9_CHECK(launch_empole_recip(ctx, ctx->e_atom + ctx->npad));
          T9_CHECK(launch_extfield_mpole(ctx, false, false));
       }
+      if (!fresh)
+         break;
       T9_CUDA(cudaStreamSynchronize(ctx->stream));
       int redo = 0;
       T9_CHECK(check_list_overflow(ctx, &redo));

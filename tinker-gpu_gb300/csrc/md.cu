@@ -59,20 +59,40 @@ __global__ void k_md_kinetic(int n, const double* __restrict__ v, const double* 
       *out = 0.5 * t[0];
 }
 
-__global__ void k_md_scale(int n, double s, double* __restrict__ v)
+// Bussi factor of one step from the kinetic energy in md_out[0] and the
+// step's variates (normal r, chi-squared s), stored in md_out[1]
+__global__ void k_md_bussi(const double* __restrict__ rs, int step, double c, double kelvin, int nfree,
+   double* __restrict__ out)
 {
+   const double ek = out[0] / EKCAL;
+   double temp = 2.0 * ek / (nfree * GASCONST);
+   if (temp == 0)
+      temp = 0.1;
+   const double d = (1 - c) * (kelvin / temp) / nfree;
+   const double r = rs[2 * step], s = rs[2 * step + 1];
+   double scale = sqrt(c + (s + r * r) * d + 2 * r * sqrt(c * d));
+   if (r + sqrt(c / d) < 0)
+      scale = -scale;
+   out[1] = scale;
+}
+
+__global__ void k_md_scale(int n, const double* __restrict__ s, double* __restrict__ v)
+{
+   const double f = *s;
    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < 3 * n; e += gridDim.x * blockDim.x)
-      v[e] *= s;
+      v[e] *= f;
 }
 
 static int md_free(Context* ctx)
 {
-   void* p[] = {ctx->md_x, ctx->md_v, ctx->md_minv, ctx->md_g, ctx->md_red, ctx->md_out};
+   void* p[] = {ctx->md_x, ctx->md_v, ctx->md_minv, ctx->md_g, ctx->md_red, ctx->md_out, ctx->md_rs};
    for (void* q : p)
       if (q)
          cudaFree(q);
    ctx->md_x = ctx->md_v = ctx->md_minv = ctx->md_red = ctx->md_out = nullptr;
    ctx->md_g = nullptr;
+   ctx->md_rs = nullptr;
+   ctx->md_rs_cap = 0;
    ctx->md_ready = false;
    return T9GB_OK;
 }
@@ -170,6 +190,26 @@ extern "C" int t9gb_md_run(t9gb_context* h, int nsteps, double dt, int thermosta
       ctx->md_seed = seed;
    }
    const int nb = grid_for(3 * n, 256);
+   if (thermostat == 1 && nsteps > 0) {
+      // the run's thermostat variates, drawn in the reference's order (one
+      // normal, then one chi-squared with nfree - 1 degrees, per step)
+      std::vector<double> rs(2 * (size_t)nsteps);
+      std::normal_distribution<double> gauss(0.0, 1.0);
+      std::gamma_distribution<double> gam(0.5 * (nfree - 1), 2.0);
+      for (int k = 0; k < nsteps; ++k) {
+         rs[2 * k] = gauss(ctx->md_rng);
+         rs[2 * k + 1] = gam(ctx->md_rng);
+      }
+      if (ctx->md_rs_cap < nsteps) {
+         if (ctx->md_rs)
+            T9_CUDA(cudaFree(ctx->md_rs));
+         T9_CUDA(cudaMalloc(&ctx->md_rs, sizeof(double) * 2 * nsteps));
+         ctx->md_rs_cap = nsteps;
+      }
+      T9_CUDA(cudaMemcpyAsync(ctx->md_rs, rs.data(), sizeof(double) * 2 * nsteps, cudaMemcpyHostToDevice,
+         ctx->stream));
+      T9_CUDA(cudaStreamSynchronize(ctx->stream));
+   }
    for (int step = 0; step < nsteps; ++step) {
       k_md_kick<<<nb, 256, 0, ctx->stream>>>(n, 0.5 * dt, ctx->md_g, ctx->md_minv, ctx->md_v);
       k_md_drift<<<nb, 256, 0, ctx->stream>>>(n, dt, ctx->md_v, ctx->md_x, ctx->xyz);
@@ -182,21 +222,12 @@ extern "C" int t9gb_md_run(t9gb_context* h, int nsteps, double dt, int thermosta
       k_md_kick<<<nb, 256, 0, ctx->stream>>>(n, 0.5 * dt, ctx->md_g, ctx->md_minv, ctx->md_v);
       T9_CUDA(cudaGetLastError());
       if (thermostat == 1) {
-         double ek;
-         T9_CHECK(md_kinetic(ctx, &ek));
-         double temp = 2.0 * ek / (nfree * GASCONST);
-         if (temp == 0)
-            temp = 0.1;
-         const double c = std::exp(-dt / tau);
-         const double d = (1 - c) * (kelvin / temp) / nfree;
-         std::normal_distribution<double> gauss(0.0, 1.0);
-         std::gamma_distribution<double> gam(0.5 * (nfree - 1), 2.0);  // chi-squared, nfree - 1
-         const double r = gauss(ctx->md_rng);
-         const double s = gam(ctx->md_rng);
-         double scale = std::sqrt(c + (s + r * r) * d + 2 * r * std::sqrt(c * d));
-         if (r + std::sqrt(c / d) < 0)
-            scale = -scale;
-         k_md_scale<<<nb, 256, 0, ctx->stream>>>(n, scale, ctx->md_v);
+         // kinetic energy, factor and rescale on the device: no synchronisation
+         const int kb = std::min(RED_MAX, grid_for(n, 256));
+         k_md_kinetic<<<kb, 256, 0, ctx->stream>>>(n, ctx->md_v, ctx->md_minv, ctx->md_red, ctx->md_out,
+            ctx->md_ticket);
+         k_md_bussi<<<1, 1, 0, ctx->stream>>>(ctx->md_rs, step, std::exp(-dt / tau), kelvin, nfree, ctx->md_out);
+         k_md_scale<<<nb, 256, 0, ctx->stream>>>(n, ctx->md_out + 1, ctx->md_v);
          T9_CUDA(cudaGetLastError());
       }
    }
