@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--no-forces", action="store_true")
     ap.add_argument("--no-md", action="store_true", help="skip the MD leg (ns/day)")
+    ap.add_argument("--md-steps", type=int, default=1000, help="timed MD steps (after 2 ps of relaxation)")
     ap.add_argument("--no-large", action="store_true", help="skip the 98,304-atom leg")
     ap.add_argument("--large-config", default="water98304")
     ap.add_argument("--fft", choices=["auto", "own", "cufft"], default="auto",
@@ -247,15 +248,17 @@ def kernel_rooflines(kernels, n, entries, nfft, peak):
     return out
 
 
-def md_leg(args, abi, tg, stream):
+def md_leg(args, abi, tg, stream, nrec, local):
     """ns/day: velocity-Verlet MD of the configuration with the whole water
     force field -- multipole + polarization (induce with the ASPC predictor,
     PCG to 1e-6 D), buffered 14-7 van der Waals (9 A, taper from 8.1 A) and
     the water bond / angle / Urey-Bradley terms -- under the Bussi thermostat
-    at 298 K, 1 fs steps.  Starts from seeded Maxwell-Boltzmann velocities on
-    the synthetic lattice, relaxed first by 500 untimed steps under a strong
-    coupling (tau 0.01 ps): the lattice's randomly oriented waters release
-    their packing energy as heat within the first tenths of a picosecond."""
+    at 298 K, 1 fs steps.  From seeded Maxwell-Boltzmann velocities on the
+    synthetic lattice: 2 ps of untimed NVT relaxation (the first 0.2 ps at a
+    tau of 0.01 ps, while the randomly oriented waters release their packing
+    energy as heat, then tau 0.1 ps), --md-steps timed steps, then nrec more
+    steps recorded frame by frame on the device for the induce legs.
+    Returns (result, recorded frames [nrec][n][3] float32 or None, system)."""
     import torch
 
     s = tg.systems.make_config(args.config, vdw=True, valence=True)
@@ -268,31 +271,55 @@ def md_leg(args, abi, tg, stream):
     eng.prepare(s.xyz)
     if args.fft != "auto":
         eng.pme_own_fft(args.fft == "own")
-    dt_fs = 1.0
+    dt = 1e-3
+    K = args.md_steps
     eng.md_init(s.xyz, mass, v0)
+
+    def run(n, tau):
+        return eng.md_run(n, dt, thermostat=1, kelvin=298.0, tau_ps=tau, seed=3)
+
     with torch.cuda.stream(stream):
-        _, t_relax, _ = eng.md_run(500, dt_fs * 1e-3, thermostat=1, kelvin=298.0, tau_ps=0.01, seed=3)
-        eng.md_run(max(args.warmup, 20), dt_fs * 1e-3, thermostat=1, kelvin=298.0, tau_ps=0.1, seed=3)
+        run(200, 0.01)
+        _, t_relax, _ = run(1800, 0.1)
+        run(max(args.warmup, 3), 0.1)
+        st0, it0 = eng.md_stats()
+        clocks = ClockSampler(local)
+        clocks.start()
+        time.sleep(0.3)
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
         w0 = time.perf_counter()
         a.record(stream)
-        ek, temp, _ = eng.md_run(args.steps, dt_fs * 1e-3, thermostat=1, kelvin=298.0, tau_ps=0.1, seed=3)
+        ek, temp, _ = run(K, 0.1)
         b.record(stream)
         b.synchronize()
         wall = time.perf_counter() - w0
-    ms = a.elapsed_time(b) / args.steps
+        ck = clocks.stop()
+        st1, it1 = eng.md_stats()
+        frames = None
+        if nrec > 0:
+            frames = torch.empty((nrec, s.n, 3), dtype=torch.float32, device="cuda")
+            torch.cuda.synchronize()
+            for k in range(nrec):
+                run(1, 0.1)
+                eng.md_positions_device(frames[k])
+            torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / K
     eng.close()
     return {
         "ms_per_step": ms,
-        "wall_ms_per_step": 1000 * wall / args.steps,
-        "ns_per_day": 86.4 * dt_fs / ms,
-        "steps": args.steps,
+        "wall_ms_per_step": 1000 * wall / K,
+        "ns_per_day": 86.4 * dt * 1000 / ms,
+        "steps": K,
+        "pcg_iterations_per_step": (it1 - it0) / max(1, st1 - st0),
         "temperature_k": temp,
-        "relaxation": {"steps": 500, "tau_ps": 0.01, "temperature_k": t_relax},
+        "relaxation": {"ps": 2.0, "temperature_k": t_relax,
+                       "schedule": "0.2 ps Bussi tau 0.01 ps, 1.8 ps Bussi tau 0.1 ps, 298 K"},
+        "clocks": ck,
+        "recorded_frames": nrec,
         "config": f"{args.config}: multipole + polarization (ASPC, PCG 1e-6 D), HAL 9 A, water valence; "
                   "Bussi 298 K (tau 0.1 ps), 1 fs velocity Verlet",
-    }
+    }, frames, s
 
 
 def large_leg(args, abi, tg, stream, flush, peak):
@@ -330,7 +357,11 @@ def large_leg(args, abi, tg, stream, flush, peak):
            "rooflines": kernel_rooflines(kernels, s.n, ls["entries"], s.settings["nfft"][0], peak)}
     eng.close()
     if not args.no_learned and args.learn_train > 0:
-        out["learned_guess"] = learned_legs(args, s, abi, stream, tr, flush, check_oracle=False)
+        nfr = args.learn_train + 3 * (args.warmup + args.steps)
+        x0 = 100000  # frames after the measurement's
+        lf = torch.from_numpy(np.stack([tr.frame(x0 + t) for t in range(nfr)]).astype(np.float32)).to("cuda")
+        out["learned_guess"] = learned_legs(args, s, abi, stream, lf, flush, check_oracle=False)
+        out["learned_guess"]["frames"] = "synthetic librating trajectory"
     return out
 
 
@@ -357,7 +388,7 @@ def time_steps(eng, dev_frames, idxs, stream, flush, ud, up):
     return ms, its, ls
 
 
-def learned_legs(args, s, abi, stream, tr, flush, check_oracle):
+def learned_legs(args, s, abi, stream, dev, flush, check_oracle):
     """The learned initial guess against the plain guesses.
 
     Two engines follow the trajectory: one with the direct guess alpha E (no
@@ -367,13 +398,11 @@ def learned_legs(args, s, abi, stream, tr, flush, check_oracle):
     legs of --steps frames, each after --warmup untimed frames: the plain
     start (network off), the learned start compared with the plain one on
     every solve (probe 1), and the comparison on every 16th solve (probe 16).
-    Training is off in the timed legs."""
+    Training is off in the timed legs.  dev: device frames [>= T + 3 (W + K)][n][3]."""
     import torch
 
     T, K, W = args.learn_train, args.steps, args.warmup
-    x0 = 100000  # frames after the main measurement's
-    nfr = T + 3 * (W + K)
-    dev = torch.from_numpy(np.stack([tr.frame(x0 + t) for t in range(nfr)]).astype(np.float32)).to("cuda")
+    assert dev.shape[0] >= T + 3 * (W + K)
     ud = torch.zeros((s.n, 3), device="cuda")
     up = torch.zeros((s.n, 3), device="cuda")
     out = {"train_steps": T, "timed_steps": K, "rows_per_batch": 2 * s.n,
@@ -571,17 +600,28 @@ def main():
                   "forces_virial_ms_per_step": em - 1000 * dev_sec / args.steps,
                   "note": "t9gb_emplar(energy|grad|virial): induce + real-space and PME forces, torques, virial"}
 
+    # ---- MD (ns/day), recording the frames of the learned-guess legs ----
+    want_learned = not args.no_learned and args.learn_train > 0
+    nrec = args.learn_train + 3 * (args.warmup + args.steps) if want_learned else 0
+    md, md_frames, md_sys = None, None, None
+    if not args.no_md:
+        md, md_frames, md_sys = md_leg(args, abi, tg, stream, nrec, local)
+
     learned = None
-    if not args.no_learned and args.learn_train > 0:
-        learned = learned_legs(args, s, abi, stream, tr, flush, check_oracle=rank == 0 and not args.no_cpu_baseline)
+    if want_learned:
+        check = rank == 0 and not args.no_cpu_baseline
+        if md_frames is not None:
+            learned = learned_legs(args, md_sys, abi, stream, md_frames, flush, check_oracle=check)
+            learned["frames"] = "MD trajectory of the relaxed box (the MD leg's, continued)"
+        else:
+            lf = torch.from_numpy(np.stack([tr.frame(100000 + t) for t in range(nrec)]).astype(np.float32)).to("cuda")
+            learned = learned_legs(args, s, abi, stream, lf, flush, check_oracle=check)
+            learned["frames"] = "synthetic librating trajectory"
+        del md_frames
 
     large = None
     if not args.no_large:
         large = large_leg(args, abi, tg, stream, flush, peak)
-
-    md = None
-    if not args.no_md:
-        md = md_leg(args, abi, tg, stream)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

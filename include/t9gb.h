@@ -172,6 +172,15 @@ int t9gb_md_run(t9gb_context* ctx, int nsteps, double dt_ps, int thermostat, dou
  * gradient at them (device [n][3], may be NULL). */
 int t9gb_md_state(t9gb_context* ctx, double* xyz, double* vel, float* grad_device);
 
+/* The current positions as float [n][3] into device memory, ordered on the
+ * context's stream (no synchronisation): a caller records a trajectory
+ * frame by frame without a host round trip (the reference writes archive
+ * frames from host copies, src/md/misc.cpp mdsave). */
+int t9gb_md_positions_device(t9gb_context* ctx, float* xyz_device);
+
+/* Steps integrated and PCG iterations spent in them since t9gb_md_init. */
+int t9gb_md_stats(t9gb_context* ctx, long long* steps, long long* pcg_iterations);
+
 /* Coordinates [n][3].  Replace copyPosToXyz (src/atom.cpp:161-166). */
 int t9gb_set_xyz_host(t9gb_context* ctx, const double* xyz);
 int t9gb_set_xyz_device(t9gb_context* ctx, const float* xyz_device);

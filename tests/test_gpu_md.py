@@ -57,3 +57,27 @@ def test_bussi_thermostat_heats_a_cold_box(gpu_lib, tg):
     temps = [e.md_run(40, 0.001, thermostat=1, kelvin=298.0, tau_ps=0.01, seed=7)[1] for _ in range(5)]
     print("temperatures", [round(t, 1) for t in temps])
     assert 200.0 < np.mean(temps[2:]) < 400.0
+
+
+def test_trajectory_recording_and_iteration_counts(gpu_lib, tg):
+    """Frames copied on the device match the host state, and the step and
+    PCG-iteration counters add up the solves of the steps."""
+    import torch
+
+    s = tg.systems.make_config("water648", vdw=True, valence=True)
+    mass = np.where(s.types == tg.systems.WATER_O, 15.999, 1.008)
+    e = engine_for(s, predictor=1)
+    e.md_init(s.xyz, mass, None)
+    frames = torch.zeros((3, s.n, 3), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()  # the engine copies on its own stream
+    iters = 0
+    for k in range(3):
+        e.md_run(1, 0.001, thermostat=1, kelvin=298.0, tau_ps=0.1, seed=2)
+        iters += e.stats()[0]
+        e.md_positions_device(frames[k])
+    x, _, _ = e.md_state()
+    torch.cuda.synchronize()
+    assert np.array_equal(frames[2].cpu().numpy(), x.astype(np.float32))
+    assert not np.array_equal(frames[0].cpu().numpy(), frames[2].cpu().numpy())
+    steps, its = e.md_stats()
+    assert steps == 3 and its == iters and its > 0

@@ -30,6 +30,7 @@ EXPORTS = [
     "t9gb_empole", "t9gb_epolar", "t9gb_emplar", "t9gb_energy_components", "t9gb_pme_own_fft",
     "t9gb_pair_lanes", "t9gb_set_thole_pairs", "t9gb_set_external_field", "t9gb_set_vdw", "t9gb_ehal",
     "t9gb_set_valence", "t9gb_evalence", "t9gb_md_init", "t9gb_md_run", "t9gb_md_state",
+    "t9gb_md_positions_device", "t9gb_md_stats",
 ]
 CALC_ENERGY, CALC_GRAD, CALC_VIRIAL = 0x010, 0x020, 0x040
 
@@ -134,6 +135,8 @@ def load(path=None):
     lib.t9gb_md_run.argtypes = [vp, C.c_int, C.c_double, C.c_int, C.c_double, C.c_double, C.c_int, C.c_ulonglong, dp,
                                 dp]
     lib.t9gb_md_state.argtypes = [vp, dp, dp, fp]
+    lib.t9gb_md_positions_device.argtypes = [vp, fp]
+    lib.t9gb_md_stats.argtypes = [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
     for name in ("t9gb_empole", "t9gb_epolar", "t9gb_emplar"):
         getattr(lib, name).argtypes = [vp, C.c_int, dp, fp, dp]
     _lib = lib
@@ -492,6 +495,19 @@ class Engine:
         g = self._empty3()
         self._check(self.lib.t9gb_md_state(self.h, _dp(x), _dp(v), C.c_void_p(g.data_ptr())))
         return x, v, g
+
+    def md_positions_device(self, out):
+        """Current positions into a float32 CUDA tensor [n][3], in stream order."""
+        if not (out.is_cuda and out.dtype == self.torch.float32 and out.is_contiguous()
+                and tuple(out.shape) == (self.n, 3)):
+            raise ValueError("md_positions_device: want a contiguous float32 CUDA tensor [n][3]")
+        self._check(self.lib.t9gb_md_positions_device(self.h, C.c_void_p(out.data_ptr())))
+
+    def md_stats(self):
+        """(steps, PCG iterations) since md_init."""
+        st, it = C.c_longlong(), C.c_longlong()
+        self._check(self.lib.t9gb_md_stats(self.h, C.byref(st), C.byref(it)))
+        return st.value, it.value
 
     def evalence(self, vers=CALC_ENERGY | CALC_GRAD):
         """Bond + angle + Urey-Bradley: (energy, gradient[, virial])."""

@@ -197,6 +197,7 @@ struct Context {
    double* md_rs = nullptr;    // [2][nsteps] variates of the current run
    int md_rs_cap = 0;
    unsigned long long md_seed = ~0ull;
+   long long md_steps = 0, md_iters = 0;  // since t9gb_md_init
 
    // coordinates, caller order
    float* xyz = nullptr;       // [n][3]
@@ -395,6 +396,11 @@ int check_list_overflow(Context* ctx, int* redo);
 int alloc_lists(Context* ctx, int cap);          // nbr, nbrc, nbrp with row capacity cap
 int launch_list_filter(Context* ctx);             // pair.cu  // after a sync; redo = 1: grown, repeat
 int scatter_positions(Context* ctx);
+// side stream of the current capture level, and the fork / join of work on
+// it with the main stream (events, no host synchronisation)
+int side_index(const Context* ctx);
+int recip_fork(Context* ctx, int k);
+int recip_join(Context* ctx, int k);
 int rotpole_sorted(Context* ctx);
 int reset_predictor(Context* ctx);
 // ring depth of the dipole predictor: ASPC 16, Gear 6, none 0

@@ -740,6 +740,21 @@ int elec_forces(Context* ctx, bool mpole, bool polar, float* grad, bool vir)
    const PairParams P = make_params(ctx, ctx->cfg.cutoff);
    const float f = (float)ctx->cfg.electric;
    const int grid = grid_for((long long)ctx->npad * GROUP, 128);
+   const bool ew = ctx->cfg.use_ewald != 0;
+   const size_t np = ctx->npad;
+   float* wrec = vir ? ctx->wvir + 18 * np : nullptr;
+   // the reciprocal forces (spread, transform, gather: their own outputs)
+   // run on the side stream beside the real-space kernel
+   const bool side = ew && !ctx->prof.on;
+   const int k = side_index(ctx);
+   if (side) {
+      T9_CHECK(recip_fork(ctx, k));
+      cudaStream_t main = ctx->stream;
+      ctx->stream = ctx->side_stream[k];
+      const int rc = launch_force_recip(ctx, mpole, polar, wrec);
+      ctx->stream = main;
+      T9_CHECK(rc);
+   }
    if (vir) {
       if (mpole && polar)
          launch_real<true, true, true>(ctx, P, f, grid);
@@ -756,10 +771,10 @@ int elec_forces(Context* ctx, bool mpole, bool polar, float* grad, bool vir)
          launch_real<false, true, false>(ctx, P, f, grid);
    }
    T9_CUDA(cudaGetLastError());
-   const bool ew = ctx->cfg.use_ewald != 0;
-   const size_t np = ctx->npad;
-   if (ew)
-      T9_CHECK(launch_force_recip(ctx, mpole, polar, vir ? ctx->wvir + 18 * np : nullptr));
+   if (side)
+      T9_CHECK(recip_join(ctx, k));
+   else if (ew)
+      T9_CHECK(launch_force_recip(ctx, mpole, polar, wrec));
    else if (vir)
       T9_CUDA(cudaMemsetAsync(ctx->wvir + 18 * np, 0, sizeof(float) * 9 * np, ctx->stream));
    if (mpole)

@@ -168,6 +168,7 @@ extern "C" int t9gb_md_init(t9gb_context* h, const double* xyz, const double* ma
    if (!ctx->have_order)
       T9_CHECK(t9gb_nblist_build(h));
    T9_CHECK(md_forces(ctx, h));
+   ctx->md_steps = ctx->md_iters = 0;
    ctx->md_ready = true;
    return T9GB_OK;
 }
@@ -219,6 +220,8 @@ extern "C" int t9gb_md_run(t9gb_context* h, int nsteps, double dt, int thermosta
       const int st = md_forces(ctx, h);
       if (st != T9GB_OK)
          return st;
+      ctx->md_steps += 1;
+      ctx->md_iters += ctx->last_iter;
       k_md_kick<<<nb, 256, 0, ctx->stream>>>(n, 0.5 * dt, ctx->md_g, ctx->md_minv, ctx->md_v);
       T9_CUDA(cudaGetLastError());
       if (thermostat == 1) {
@@ -260,5 +263,32 @@ extern "C" int t9gb_md_state(t9gb_context* h, double* xyz, double* vel, float* g
    if (grad_device)
       T9_CUDA(cudaMemcpyAsync(grad_device, ctx->md_g, sizeof(float) * 3 * n, cudaMemcpyDeviceToDevice, ctx->stream));
    T9_CUDA(cudaStreamSynchronize(ctx->stream));
+   return T9GB_OK;
+}
+
+extern "C" int t9gb_md_positions_device(t9gb_context* h, float* xyz_device)
+{
+   if (!h || !xyz_device)
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   if (!ctx->md_ready)
+      return T9GB_NOT_READY;
+   // the drift kernel keeps the float copy of the trajectory in caller order
+   T9_CUDA(cudaMemcpyAsync(xyz_device, ctx->xyz, sizeof(float) * 3 * ctx->n, cudaMemcpyDeviceToDevice,
+      ctx->stream));
+   return T9GB_OK;
+}
+
+extern "C" int t9gb_md_stats(t9gb_context* h, long long* steps, long long* pcg_iterations)
+{
+   if (!h)
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   if (!ctx->md_ready)
+      return T9GB_NOT_READY;
+   if (steps)
+      *steps = ctx->md_steps;
+   if (pcg_iterations)
+      *pcg_iterations = ctx->md_iters;
    return T9GB_OK;
 }

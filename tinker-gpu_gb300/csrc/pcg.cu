@@ -404,19 +404,19 @@ int check_list_overflow(Context* ctx, int* redo)
 // real-space pair kernel runs on ctx->stream; after the join the gather adds
 // recip + self to the real-space field (the same sum, so the same bits, as
 // the serial order).  Serial while the per-kernel profile is on.
-static int side_index(const Context* ctx)
+int side_index(const Context* ctx)
 {
    return ctx->cap_stream && ctx->stream == ctx->cap_stream ? 1 : 0;
 }
 
-static int recip_fork(Context* ctx, int k)
+int recip_fork(Context* ctx, int k)
 {
    T9_CUDA(cudaEventRecord(ctx->ev_fork[k], ctx->stream));
    T9_CUDA(cudaStreamWaitEvent(ctx->side_stream[k], ctx->ev_fork[k], 0));
    return T9GB_OK;
 }
 
-static int recip_join(Context* ctx, int k)
+int recip_join(Context* ctx, int k)
 {
    T9_CUDA(cudaEventRecord(ctx->ev_join[k], ctx->side_stream[k]));
    T9_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->ev_join[k], 0));
