@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--no-forces", action="store_true")
     ap.add_argument("--no-md", action="store_true", help="skip the MD leg (ns/day)")
     ap.add_argument("--md-steps", type=int, default=1000, help="timed MD steps (after 2 ps of relaxation)")
+    ap.add_argument("--md-extra", default="nacl23142,water98304",
+                    help="further configurations timed as MD (comma separated; empty: none)")
     ap.add_argument("--no-large", action="store_true", help="skip the 98,304-atom leg")
     ap.add_argument("--large-config", default="water98304")
     ap.add_argument("--fft", choices=["auto", "own", "cufft"], default="auto",
@@ -248,7 +250,7 @@ def kernel_rooflines(kernels, n, entries, nfft, peak):
     return out
 
 
-def md_leg(args, abi, tg, stream, nrec, local):
+def md_leg(args, abi, tg, stream, nrec, local, config):
     """ns/day: velocity-Verlet MD of the configuration with the whole water
     force field -- multipole + polarization (induce with the ASPC predictor,
     PCG to 1e-6 D), buffered 14-7 van der Waals (9 A, taper from 8.1 A) and
@@ -261,7 +263,7 @@ def md_leg(args, abi, tg, stream, nrec, local):
     Returns (result, recorded frames [nrec][n][3] float32 or None, system)."""
     import torch
 
-    s = tg.systems.make_config(args.config, vdw=True, valence=True)
+    s = tg.systems.make_config(config, vdw=True, valence=True)
     mass = np.where(s.types == tg.systems.WATER_O, 15.999,
                     np.where(s.types == tg.systems.WATER_H, 1.008,
                              np.where(s.types == tg.systems.NA_ION, 22.99, 35.453)))
@@ -275,8 +277,13 @@ def md_leg(args, abi, tg, stream, nrec, local):
     K = args.md_steps
     eng.md_init(s.xyz, mass, v0)
 
+    bad = []
+
     def run(n, tau):
-        return eng.md_run(n, dt, thermostat=1, kelvin=298.0, tau_ps=tau, seed=3)
+        ek, t, rc = eng.md_run(n, dt, thermostat=1, kelvin=298.0, tau_ps=tau, seed=3)
+        if rc != 0:
+            bad.append(rc)
+        return ek, t, rc
 
     with torch.cuda.stream(stream):
         run(200, 0.01)
@@ -317,8 +324,9 @@ def md_leg(args, abi, tg, stream, nrec, local):
                        "schedule": "0.2 ps Bussi tau 0.01 ps, 1.8 ps Bussi tau 0.1 ps, 298 K"},
         "clocks": ck,
         "recorded_frames": nrec,
-        "config": f"{args.config}: multipole + polarization (ASPC, PCG 1e-6 D), HAL 9 A, water valence; "
-                  "Bussi 298 K (tau 0.1 ps), 1 fs velocity Verlet",
+        "status": "ok" if not bad else f"solver status {bad[0]} in {len(bad)} run(s): trajectory stopped early",
+        "config": f"{config}: {s.n} atoms, PME {s.settings['nfft'][0]}^3; multipole + polarization (ASPC, PCG "
+                  "1e-6 D), HAL 9 A, water valence; Bussi 298 K (tau 0.1 ps), 1 fs velocity Verlet",
     }, frames, s
 
 
@@ -605,7 +613,7 @@ def main():
     nrec = args.learn_train + 3 * (args.warmup + args.steps) if want_learned else 0
     md, md_frames, md_sys = None, None, None
     if not args.no_md:
-        md, md_frames, md_sys = md_leg(args, abi, tg, stream, nrec, local)
+        md, md_frames, md_sys = md_leg(args, abi, tg, stream, nrec, local, args.config)
 
     learned = None
     if want_learned:
@@ -622,6 +630,12 @@ def main():
     large = None
     if not args.no_large:
         large = large_leg(args, abi, tg, stream, flush, peak)
+
+    # ---- MD of the other configurations (ns/day only) ----
+    md_other = {}
+    if not args.no_md:
+        for name in [c for c in args.md_extra.split(",") if c and c != args.config]:
+            md_other[name] = md_leg(args, abi, tg, stream, 0, local, name)[0]
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -655,6 +669,7 @@ def main():
             "ns_per_day": None if md is None else md["ns_per_day"],
             "ns_per_day_note": "MD leg (see md)" if md is not None else "MD leg skipped (--no-md)",
             "md": md,
+            "md_other_configs": md_other,
             "wall_s_timed": wall,
             "e2e": {"value": e2e_value, "unit": "induce() calls/s", "ms_per_step": 1000 * e2e_sec / args.steps,
                     "h2d_bytes_per_step": 3 * s.n * 4, "d2h_bytes_per_step": 6 * s.n * 4},
