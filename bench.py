@@ -584,9 +584,11 @@ def main():
     per_launch_s = kernels[dom]["ms_per_launch"] / 1000.0
     achieved = alg / per_launch_s / 1e9
     mean_it = float(np.mean(iters))
-    # own kernels per step: positions 1, rotpole 2, list 5, reset 1, dfield 5, guess 1, ufield 5, r0 1,
-    # M r0 1, dots 1, history 1, output 1; per PCG iteration: ufield 5 + precond 1 + vector 4
-    launches_per_step = 25 + 10 * mean_it
+    # own kernels per step (fused FFT, default CG fusion): positions 1, rotpole 2, list 5, permanent
+    # field 6 (real, spread, 3 transform, gather), guess 1, field of the guess 6, r0 1, M r0 with the
+    # dots 1, peek + predictor save 1, predictor index 1, output 1; per PCG iteration: field 6,
+    # Ap 1, update 1, M r with the dots 1
+    launches_per_step = 26 + 9 * mean_it
 
     # ---- forces: emplar (induce + multipole and polarization energy, gradient, virial) ----
     forces = None

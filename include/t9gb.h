@@ -300,6 +300,19 @@ int t9gb_pme_own_fft(t9gb_context* ctx, int enable);
  * results are identical up to the order of the per-lane partial sums. */
 int t9gb_pair_lanes(t9gb_context* ctx, int lanes);
 
+/* Kernel fusion of the CG iteration (bit mask; default 1).  Bit 0: the
+ * sparse preconditioner also forms r.z, r.r and the CG scalars (else a
+ * separate dot kernel, sparsePrecondApply + the dot products of
+ * src/cu/amoeba/pcg.cu:120-150).  Bit 1 (PME only): the search direction
+ * p = z + b p is formed by the kernels that read it and the mutual-field
+ * gather also forms Ap, p.Ap and the step length (else a direction kernel
+ * and a separate Ap kernel).  A tuning knob: the same iteration, results
+ * equal up to the order of the partial sums.  Measured on GB300: bit 0
+ * saves a launch per iteration; bit 1 costs more than it saves, since the
+ * fused gather holds more registers and hides less of its grid-load
+ * latency. */
+int t9gb_set_pcg_fusion(t9gb_context* ctx, int mask);
+
 /* Neighbour-list sizes: row capacity, entries of the current list (both
  * directions) and scaled pairs (the reference's Spatial::nakpl/niak,
  * include/ff/spatial.h:15-140). */

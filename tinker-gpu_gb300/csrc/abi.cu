@@ -561,6 +561,16 @@ int t9gb_pair_lanes(t9gb_context* h, int lanes)
    return T9GB_OK;
 }
 
+int t9gb_set_pcg_fusion(t9gb_context* h, int mask)
+{
+   if (!h || mask < 0 || mask > 3)
+      return T9GB_BAD_ARG;
+   if (mask != h->c.pcg_fuse)
+      drop_graphs(&h->c);
+   h->c.pcg_fuse = mask;
+   return T9GB_OK;
+}
+
 int t9gb_pme_own_fft(t9gb_context* h, int enable)
 {
    if (!h)

@@ -240,6 +240,7 @@ struct Context {
    int* nbr_over = nullptr;  // device max count seen (overflow check)
    int* h_over = nullptr;    // pinned mirror
    int pair_lanes = 8;            // lanes per atom in the field kernels
+   int pcg_fuse = 1;              // t9gb_set_pcg_fusion
    bool list_stale = true;        // positions changed since the last list check
    bool list_need_build = true;   // no valid list for the current order / capacity
    float4* sref = nullptr;        // [npad] positions at the last list build
@@ -336,7 +337,7 @@ struct Context {
 // (1 - red) of a bond from its atom: 0.09 A for AMOEBA water hydrogens).
 constexpr double VDW_SITE_MARGIN = 0.25;
 
-constexpr int RED_MAX = 1024;
+constexpr int RED_MAX = 2048;
 constexpr int RED_SLOTS = 8;
 
 #define T9_CUDA(call)                                                                                                  \
@@ -395,6 +396,33 @@ int ensure_list(Context* ctx);  // list_update when the coordinates changed
 int check_list_overflow(Context* ctx, int* redo);
 int alloc_lists(Context* ctx, int cap);          // nbr, nbrc, nbrp with row capacity cap
 int launch_list_filter(Context* ctx);             // pair.cu  // after a sync; redo = 1: grown, repeat
+// The fused kernels of a CG iteration: the sparse preconditioner with the
+// r.z / r.r sums and the CG scalars (pair.cu), and the mutual-field gather
+// with Ap = p/alpha - field, p.Ap and the step length (pme.cu).
+struct PcgDots {
+   float* conj;  // init: the first search direction p = z
+   double* red;
+   double* scal;
+   int* state;
+   int init, n;
+   double debye, poleps;
+   int politer, miniter;
+   cudaGraphConditionalHandle handle;
+   int use_handle;
+};
+struct PcgAp {
+   const float* zrsd;    // z: p = z + b p_old
+   float* conj;          // p_old in, p out
+   const float* polinv;  // 1/alpha per slot
+   float* vec;           // Ap out
+   double* red;
+   double* scal;
+   int* state;
+};
+int launch_precond_sparse_dots(Context* ctx, const float* r6, float* z6, const PcgDots& D);
+int launch_ufield_real_dir(Context* ctx, const float* p6, const float* z6, const double* scal, float* out6);
+int launch_ufield_recip_grid_dir(Context* ctx, const float* p6, const float* z6, const double* scal);
+int launch_ufield_recip_gather_ap(Context* ctx, float* out6, const PcgAp& P);
 int scatter_positions(Context* ctx);
 // side stream of the current capture level, and the fork / join of work on
 // it with the main stream (events, no host synchronisation)

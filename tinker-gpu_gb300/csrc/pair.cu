@@ -17,6 +17,7 @@
 // of the reference's pair functions equals the i-side formula evaluated from
 // atom k with the separation reversed, which is what the full list does.
 #include "pair.cuh"
+#include "reduce.cuh"
 
 namespace t9gb {
 
@@ -102,16 +103,34 @@ __device__ __forceinline__ void ufield_i(const PairParams& P, float r2, float3 d
    f[5] += c * d.z - b1 * uk[5];
 }
 
-template <int G>
+// DIR: the dipoles are the CG search direction p = z + b p_old, formed
+// from u8 = p_old, z8 and b (scal) as each row is read
+template <int G, bool DIR>
+__device__ __forceinline__ void urow(const float* __restrict__ u8, const float* __restrict__ z8, int j, float bd,
+   float bp, float* v)
+{
+   if (DIR)
+      dir_row(u8, z8, j, bd, bp, v);
+   else
+      load8(u8, j, v);
+}
+
+template <int G, bool DIR>
 __global__ void __launch_bounds__(256) k_ufield_real(PairParams P, int npad, const int* __restrict__ nbr,
    const int* __restrict__ nnbr, const int* __restrict__ sp_start, const int* __restrict__ sp_j,
    const float4* __restrict__ sp_sc, const float4* __restrict__ spos, const float* __restrict__ u8,
-   const float* __restrict__ base8, float* __restrict__ out8)
+   const float* __restrict__ z8, const double* __restrict__ scal, const float* __restrict__ base8,
+   float* __restrict__ out8)
 {
    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
    const int i = tid / G, g = tid % G;
    if (i >= npad)
       return;
+   float bd = 0.f, bp = 0.f;
+   if (DIR) {
+      bd = (float)scal[S_B_D];
+      bp = (float)scal[S_B_P];
+   }
    float f[6] = {0, 0, 0, 0, 0, 0};
    if (i < P.n) {
       const float4 pi = spos[i];  // w = pdamp
@@ -125,8 +144,8 @@ __global__ void __launch_bounds__(256) k_ufield_real(PairParams P, int npad, con
          const int j0 = row[k], j1 = row[k + G];
          const float4 p0 = spos[j0], p1 = spos[j1];
          float u0[8], u1[8];
-         load8(u8, j0, u0);
-         load8(u8, j1, u1);
+         urow<G, DIR>(u8, z8, j0, bd, bp, u0);
+         urow<G, DIR>(u8, z8, j1, bd, bp, u1);
          const float3 s0 = sep(P, pi, p0), s1 = sep(P, pi, p1);
          const float r0 = s0.x * s0.x + s0.y * s0.y + s0.z * s0.z;
          const float r1 = s1.x * s1.x + s1.y * s1.y + s1.z * s1.z;
@@ -142,7 +161,7 @@ __global__ void __launch_bounds__(256) k_ufield_real(PairParams P, int npad, con
          const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
          if (r2 <= P.cut2) {
             float uk[8];
-            load8(u8, j, uk);
+            urow<G, DIR>(u8, z8, j, bd, bp, uk);
             ufield_i(P, r2, d, 1.f, pi.w, pti, pk.w, uk[6], uk, f);
          }
       }
@@ -154,7 +173,7 @@ __global__ void __launch_bounds__(256) k_ufield_real(PairParams P, int npad, con
          const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
          if (r2 <= P.cut2) {
             float uk[8];
-            load8(u8, j, uk);
+            urow<G, DIR>(u8, z8, j, bd, bp, uk);
             ufield_i(P, r2, d, sp_sc[q].w, pi.w, pti, pk.w, uk[6], uk, f);
          }
       }
@@ -318,16 +337,13 @@ __device__ __forceinline__ void precond_i(const PairParams& P, float r2, float3 
    f[5] += c * d.z - rr3 * rk[5];
 }
 
+// the preconditioner row of slot i: lane g < 6 returns z component g
 template <int G>
-__global__ void __launch_bounds__(256) k_precond_sparse(PairParams P, int npad, float udiag,
+__device__ __forceinline__ float precond_row(const PairParams& P, int i, int g, float udiag,
    const int* __restrict__ nbr, const int* __restrict__ nnbr, const int* __restrict__ sp_start,
    const int* __restrict__ sp_j, const float4* __restrict__ sp_sc, const float4* __restrict__ spos,
-   const float* __restrict__ r8, float* __restrict__ z8)
+   const float* __restrict__ r8)
 {
-   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-   const int i = tid / G, g = tid % G;
-   if (i >= npad)
-      return;
    float f[6] = {0, 0, 0, 0, 0, 0};
    const float poli = r8[8 * i + 7];
    if (i < P.n) {
@@ -375,8 +391,63 @@ __global__ void __launch_bounds__(256) k_precond_sparse(PairParams P, int npad, 
       }
    }
    group_reduce<G, 6>(f);
+   return g < 6 ? udiag * poli * r8[8 * i + g] + pick6(f, g) : 0.f;
+}
+
+template <int G>
+__global__ void __launch_bounds__(256) k_precond_sparse(PairParams P, int npad, float udiag,
+   const int* __restrict__ nbr, const int* __restrict__ nnbr, const int* __restrict__ sp_start,
+   const int* __restrict__ sp_j, const float4* __restrict__ sp_sc, const float4* __restrict__ spos,
+   const float* __restrict__ r8, float* __restrict__ z8)
+{
+   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+   const int i = tid / G, g = tid % G;
+   if (i >= npad)
+      return;
+   const float z = precond_row<G>(P, i, g, udiag, nbr, nnbr, sp_start, sp_j, sp_sc, spos, r8);
    if (g < 6)
-      z8[8 * i + g] = udiag * poli * r8[8 * i + g] + pick6(f, g);
+      z8[8 * i + g] = z;
+}
+
+// z = M r fused with the partial sums r.z, r.r (d and p) and, in the last
+// block, the CG scalars.  Slots are visited block-strided, 256 / G per
+// block per trip (npad is a multiple of 32, so every lane of a block makes
+// the same trips); at most RED_MAX blocks.
+template <int G>
+__global__ void __launch_bounds__(256, 4) k_precond_sparse_dots(PairParams P, int npad, float udiag,
+   const int* __restrict__ nbr, const int* __restrict__ nnbr, const int* __restrict__ sp_start,
+   const int* __restrict__ sp_j, const float4* __restrict__ sp_sc, const float4* __restrict__ spos,
+   const float* __restrict__ r8, float* __restrict__ z8, PcgDots D)
+{
+   __shared__ double sh[64];
+   constexpr int PER = 256 / G;
+   const int g = threadIdx.x % G;
+   double rz_d = 0, rz_p = 0, rr_d = 0, rr_p = 0;
+   for (int i = blockIdx.x * PER + threadIdx.x / G; i < npad; i += gridDim.x * PER) {
+      const float z = precond_row<G>(P, i, g, udiag, nbr, nnbr, sp_start, sp_j, sp_sc, spos, r8);
+      if (g < 6) {
+         const float r = r8[8 * i + g];
+         z8[8 * i + g] = z;
+         if (D.init)
+            D.conj[8 * i + g] = z;
+         if (g < 3) {
+            rz_d += (double)r * z;
+            rr_d += (double)r * r;
+         } else {
+            rz_p += (double)r * z;
+            rr_p += (double)r * r;
+         }
+      }
+   }
+   const double pv[4] = {rz_d, rz_p, rr_d, rr_p};
+   store_partials<4>(D.red, R_RZ_D, pv, sh);
+   if (!last_block(D.state + ST_TICKET0))
+      return;
+   double tot[4];
+   sum_slots(D.red, R_RZ_D, 4, gridDim.x, sh, tot);
+   if (threadIdx.x == 0)
+      pcg_scalars(tot, D.scal, D.state, D.init, D.n, D.debye, D.poleps, D.politer, D.miniter, D.handle,
+         D.use_handle);
 }
 
 // ---------------------------------------------------------------------------
@@ -577,12 +648,36 @@ int launch_list_filter(Context* ctx)
          KERNEL<16><<<nb_, PAIR_THREADS, 0, ctx->stream>>>(__VA_ARGS__);                                               \
    } while (0)
 
+// the same for kernels with a second template parameter
+#define T9_LANES_DISPATCH2(KERNEL, ARG, ...)                                                                           \
+   do {                                                                                                                \
+      const int g_ = ctx->pair_lanes;                                                                                  \
+      const int nb_ = grid_for((long long)ctx->npad * g_, PAIR_THREADS);                                               \
+      if (g_ == 8)                                                                                                     \
+         KERNEL<8, ARG><<<nb_, PAIR_THREADS, 0, ctx->stream>>>(__VA_ARGS__);                                           \
+      else if (g_ == 32)                                                                                               \
+         KERNEL<32, ARG><<<nb_, PAIR_THREADS, 0, ctx->stream>>>(__VA_ARGS__);                                          \
+      else                                                                                                             \
+         KERNEL<16, ARG><<<nb_, PAIR_THREADS, 0, ctx->stream>>>(__VA_ARGS__);                                          \
+   } while (0)
+
 int launch_ufield_real(Context* ctx, const float* u6, const float* base6, float* out6)
 {
    PairParams P = make_params(ctx, ctx->cfg.cutoff);
    prof_begin(ctx, P_UFIELD_REAL);
-   T9_LANES_DISPATCH(k_ufield_real, P, ctx->npad, ctx->nbrc, ctx->nnbrc, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos,
-      u6, base6, out6);
+   T9_LANES_DISPATCH2(k_ufield_real, false, P, ctx->npad, ctx->nbrc, ctx->nnbrc, ctx->sp_start, ctx->sp_j, ctx->sp_sc,
+      ctx->spos, u6, nullptr, nullptr, base6, out6);
+   prof_end(ctx);
+   T9_CUDA(cudaGetLastError());
+   return T9GB_OK;
+}
+
+int launch_ufield_real_dir(Context* ctx, const float* p6, const float* z6, const double* scal, float* out6)
+{
+   PairParams P = make_params(ctx, ctx->cfg.cutoff);
+   prof_begin(ctx, P_UFIELD_REAL);
+   T9_LANES_DISPATCH2(k_ufield_real, true, P, ctx->npad, ctx->nbrc, ctx->nnbrc, ctx->sp_start, ctx->sp_j, ctx->sp_sc,
+      ctx->spos, p6, z6, scal, nullptr, out6);
    prof_end(ctx);
    T9_CUDA(cudaGetLastError());
    return T9GB_OK;
@@ -594,6 +689,28 @@ int launch_dfield_real(Context* ctx, const float* base6, float* out6)
    prof_begin(ctx, P_DFIELD_REAL);
    T9_LANES_DISPATCH(k_dfield_real, P, ctx->npad, ctx->nbrc, ctx->nnbrc, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos,
       ctx->srpole, base6, ctx->exfld, out6);
+   prof_end(ctx);
+   T9_CUDA(cudaGetLastError());
+   return T9GB_OK;
+}
+
+int launch_precond_sparse_dots(Context* ctx, const float* r6, float* z6, const PcgDots& D)
+{
+   PairParams P = make_params(ctx, ctx->cfg.usolve_cutoff + ctx->cfg.pbuffer);
+   P.ewald = 0;
+   const int g = ctx->pair_lanes;
+   const int per = PAIR_THREADS / g;
+   const int nb = std::min(RED_MAX, (ctx->npad + per - 1) / per);
+   prof_begin(ctx, P_PRECOND);
+   if (g == 8)
+      k_precond_sparse_dots<8><<<nb, PAIR_THREADS, 0, ctx->stream>>>(P, ctx->npad, (float)ctx->cfg.udiag, ctx->nbrp,
+         ctx->nnbrp, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos, r6, z6, D);
+   else if (g == 32)
+      k_precond_sparse_dots<32><<<nb, PAIR_THREADS, 0, ctx->stream>>>(P, ctx->npad, (float)ctx->cfg.udiag, ctx->nbrp,
+         ctx->nnbrp, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos, r6, z6, D);
+   else
+      k_precond_sparse_dots<16><<<nb, PAIR_THREADS, 0, ctx->stream>>>(P, ctx->npad, (float)ctx->cfg.udiag, ctx->nbrp,
+         ctx->nnbrp, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos, r6, z6, D);
    prof_end(ctx);
    T9_CUDA(cudaGetLastError());
    return T9GB_OK;

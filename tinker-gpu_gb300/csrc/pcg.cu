@@ -133,38 +133,8 @@ __global__ void k_precond_dot(VecArgs A, const float* __restrict__ rsd, float* _
       return;
    double tot[4];
    sum_slots(red, R_RZ_D, 4, gridDim.x, sh, tot);
-   const double s1_d = tot[0], s1_p = tot[1], q_d = tot[2], q_p = tot[3];
-   if (threadIdx.x != 0)
-      return;
-   if (init) {
-      scal[S_SUM_D] = s1_d;
-      scal[S_SUM_P] = s1_p;
-      state[ST_ITER] = 0;
-      state[ST_DONE] = 0;
-      state[ST_STATUS] = T9GB_OK;
-      return;
-   }
-   const double s_d = scal[S_SUM_D], s_p = scal[S_SUM_P];
-   scal[S_B_D] = s_d == 0 ? 0.0 : s1_d / s_d;
-   scal[S_B_P] = s_p == 0 ? 0.0 : s1_p / s_p;
-   scal[S_SUM_D] = s1_d;
-   scal[S_SUM_P] = s1_p;
-   const double eps = debye * sqrt(fmax(q_d, q_p) / n);
-   const int iter = state[ST_ITER] + 1;
-   state[ST_ITER] = iter;
-   bool done = eps < poleps;
-   if (iter < miniter)
-      done = false;
-   if (iter >= politer)
-      done = true;
-   const bool nan = !(eps == eps);
-   if (nan)
-      done = true;
-   scal[S_EPS] = eps;
-   state[ST_DONE] = done ? 1 : 0;
-   state[ST_STATUS] = nan ? T9GB_NAN_DETECTED : (done && !(eps < poleps) ? T9GB_NOT_CONVERGED : T9GB_OK);
-   if (use_handle)
-      cudaGraphSetConditional(handle, done ? 0u : 1u);
+   if (threadIdx.x == 0)
+      pcg_scalars(tot, scal, state, init, n, debye, poleps, politer, miniter, handle, use_handle);
 }
 
 // ---- loop body ----
@@ -214,30 +184,31 @@ __global__ void k_pcg_p2(VecArgs A, const double* __restrict__ scal, float* __re
    }
 }
 
-// p = z + b p; peek on the last iteration
-__global__ void k_pcg_p4(VecArgs A, const double* __restrict__ scal, const int* __restrict__ state,
-   float* __restrict__ conj, const float* __restrict__ zrsd, float* __restrict__ uind, const float* __restrict__ rsd,
-   float pcgpeek)
+// p = z + b p in place (the paths that do not form p where it is read)
+__global__ void k_pcg_dir(VecArgs A, const double* __restrict__ scal, float* __restrict__ conj,
+   const float* __restrict__ zrsd)
 {
    const float b = (float)scal[S_B_D], bp = (float)scal[S_B_P];
-   const bool done = state[ST_DONE] != 0;
    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.ne; e += gridDim.x * blockDim.x) {
       const int s = e / 6, x = e + 2 * s;  // row s, component e - 6 s of [npad][8]
-      const float g = e - 6 * s < 3 ? b : bp;
-      conj[x] = zrsd[x] + g * conj[x];
-      if (done)
-         uind[x] += pcgpeek * A.polar[s] * rsd[x];
+      conj[x] = __fmaf_rn(e - 6 * s < 3 ? b : bp, conj[x], zrsd[x]);
    }
 }
 
-// predictor ring save (ulspredSave, src/amoeba/induce.cpp:29-63)
-__global__ void k_save_hist(int ne, int depth, const float* __restrict__ uind, float* __restrict__ hist,
-   int* __restrict__ state)
+// after the loop: u += pcgpeek alpha r (induceMutualPcg1_cu,
+// src/cu/amoeba/pcg.cu:170-178), and with a predictor the converged
+// dipoles saved into its ring (ulspredSave, src/amoeba/induce.cpp:29-63)
+__global__ void k_pcg_peek_save(VecArgs A, float* __restrict__ uind, const float* __restrict__ rsd, float pcgpeek,
+   int depth, float* __restrict__ hist, const int* __restrict__ state)
 {
-   const int slot = state[ST_NUALT] % depth;
-   float* dst = hist + (size_t)slot * ne;
-   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ne; i += gridDim.x * blockDim.x)
-      dst[i] = uind[i];
+   float* dst = depth > 0 ? hist + (size_t)(state[ST_NUALT] % depth) * A.ne8 : nullptr;
+   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.ne; e += gridDim.x * blockDim.x) {
+      const int s = e / 6, x = e + 2 * s;  // row s, component e - 6 s of [npad][8]
+      const float u = uind[x] + pcgpeek * A.polar[s] * rsd[x];
+      uind[x] = u;
+      if (dst)
+         dst[x] = u;
+   }
 }
 
 __global__ void k_bump_nualt(int* state, int depth)
@@ -463,24 +434,61 @@ static int dfield6(Context* ctx, float* out6)
    return launch_dfield_recip_gather(ctx, out6, true);
 }
 
-static int pcg_body(Context* ctx, const VecArgs& A, cudaGraphConditionalHandle handle, int use_handle)
+// z = M r with r.z, r.r and the CG scalars: one fused kernel for the sparse
+// preconditioner, else the preconditioner and the dot kernel
+static int precond_dots(Context* ctx, const VecArgs& A, int init, cudaGraphConditionalHandle handle,
+   int use_handle)
 {
    const t9gb_config& c = ctx->cfg;
-   T9_CHECK(ufield6(ctx, ctx->conj, ctx->fld6));
-   prof_begin(ctx, P_VECTOR);
-   k_pcg_p1<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->fld6, ctx->conj, ctx->vec, ctx->red, ctx->scal, ctx->status);
-   k_pcg_p2<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->scal, ctx->uind, ctx->conj, ctx->rsd, ctx->vec);
-   prof_end(ctx);
+   const int miniter = init ? 3 : std::min(3, ctx->n);
+   if (A.sparse && (ctx->pcg_fuse & 1) && !ctx->prof.on) {
+      PcgDots D{ctx->conj, ctx->red, ctx->scal, ctx->status, init, ctx->n, c.debye, c.poleps, c.politer, miniter,
+         handle, use_handle};
+      return launch_precond_sparse_dots(ctx, ctx->rsd, ctx->zrsd, D);
+   }
    if (A.sparse)
       T9_CHECK(launch_precond_sparse(ctx, ctx->rsd, ctx->zrsd));
    prof_begin(ctx, P_VECTOR);
    k_precond_dot<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->rsd, ctx->zrsd, ctx->conj, ctx->red, ctx->scal, ctx->status,
-      0, ctx->n, c.debye, c.poleps, c.politer, std::min(3, ctx->n), handle, use_handle);
-   k_pcg_p4<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->scal, ctx->status, ctx->conj, ctx->zrsd, ctx->uind, ctx->rsd,
-      (float)c.pcgpeek);
+      init, ctx->n, c.debye, c.poleps, c.politer, miniter, handle, use_handle);
    prof_end(ctx);
    T9_CUDA(cudaGetLastError());
    return T9GB_OK;
+}
+
+// One CG iteration.  With PME outside profiling the search direction
+// p = z + b p_old is formed by its readers (spread, real-space field,
+// gather) and the gather also forms Ap = p/alpha - ufield(p), p.Ap and a,
+// storing p; elsewhere p is formed first and Ap by its own kernel.  Then
+// u += a p, r -= a Ap, and the preconditioner with the dots.
+static int pcg_body(Context* ctx, const VecArgs& A, cudaGraphConditionalHandle handle, int use_handle)
+{
+   if (ctx->cfg.use_ewald && (ctx->pcg_fuse & 2) && !ctx->prof.on) {
+      const int k = side_index(ctx);
+      T9_CHECK(recip_fork(ctx, k));
+      cudaStream_t main = ctx->stream;
+      ctx->stream = ctx->side_stream[k];
+      const int rc = launch_ufield_recip_grid_dir(ctx, ctx->conj, ctx->zrsd, ctx->scal);
+      ctx->stream = main;
+      T9_CHECK(rc);
+      T9_CHECK(launch_ufield_real_dir(ctx, ctx->conj, ctx->zrsd, ctx->scal, ctx->fld6));
+      T9_CHECK(recip_join(ctx, k));
+      PcgAp P{ctx->zrsd, ctx->conj, A.polinv, ctx->vec, ctx->red, ctx->scal, ctx->status};
+      T9_CHECK(launch_ufield_recip_gather_ap(ctx, ctx->fld6, P));
+   } else {
+      prof_begin(ctx, P_VECTOR);
+      k_pcg_dir<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->scal, ctx->conj, ctx->zrsd);
+      prof_end(ctx);
+      T9_CHECK(ufield6(ctx, ctx->conj, ctx->fld6));
+      prof_begin(ctx, P_VECTOR);
+      k_pcg_p1<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->fld6, ctx->conj, ctx->vec, ctx->red, ctx->scal, ctx->status);
+      prof_end(ctx);
+   }
+   prof_begin(ctx, P_VECTOR);
+   k_pcg_p2<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->scal, ctx->uind, ctx->conj, ctx->rsd, ctx->vec);
+   prof_end(ctx);
+   T9_CUDA(cudaGetLastError());
+   return precond_dots(ctx, A, 0, handle, use_handle);
 }
 
 // start variants: the plain guess (ASPC / alpha E / zero), the learned guess
@@ -512,22 +520,21 @@ static int pcg_start(Context* ctx, const VecArgs& A, bool graph, int variant)
       T9_CHECK(ufield6(ctx, ctx->tmp6, ctx->vec));
       T9_CHECK(learn_pick(ctx, ctx->tmp6, ctx->vec));
    }
-   if (A.sparse)
-      T9_CHECK(launch_precond_sparse(ctx, ctx->rsd, ctx->zrsd));
-   k_precond_dot<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->rsd, ctx->zrsd, ctx->conj, ctx->red, ctx->scal, ctx->status,
-      1, ctx->n, c.debye, c.poleps, c.politer, 3, 0, 0);
-   T9_CUDA(cudaGetLastError());
-   return T9GB_OK;
+   return precond_dots(ctx, A, 1, 0, 0);
 }
 
 static int pcg_finish(Context* ctx, const VecArgs& A)
 {
+   const int depth = pred_depth(ctx->cfg);
+   if (ctx->cfg.pcgpeek != 0.0 || depth > 0) {
+      k_pcg_peek_save<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->uind, ctx->rsd, (float)ctx->cfg.pcgpeek, depth,
+         ctx->aspc_hist, ctx->status);
+      T9_CUDA(cudaGetLastError());
+   }
+   if (depth > 0)
+      k_bump_nualt<<<1, 1, 0, ctx->stream>>>(ctx->status, depth);
    if (ctx->learn_mode & 1)
       T9_CHECK(learn_train(ctx));
-   if (pred_depth(ctx->cfg) > 0) {
-      k_save_hist<<<A.nb, VB, 0, ctx->stream>>>(A.ne8, pred_depth(ctx->cfg), ctx->uind, ctx->aspc_hist, ctx->status);
-      k_bump_nualt<<<1, 1, 0, ctx->stream>>>(ctx->status, pred_depth(ctx->cfg));
-   }
    T9_CUDA(cudaMemcpyAsync(ctx->h_status, ctx->status, sizeof(int) * ST_NSTAT, cudaMemcpyDeviceToHost, ctx->stream));
    T9_CUDA(cudaMemcpyAsync(ctx->h_scal, ctx->scal, sizeof(double) * S_NSCAL, cudaMemcpyDeviceToHost, ctx->stream));
    T9_CUDA(cudaGetLastError());

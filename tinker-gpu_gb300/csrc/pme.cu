@@ -174,9 +174,12 @@ __device__ __forceinline__ void grid_add(unsigned long long* q, size_t idx, floa
 // points.  MODE 0 spreads fractional multipoles into the real part; MODE 1
 // spreads fractional d dipoles into the real and p dipoles into the
 // imaginary part.  rp rows are 12 floats (q, d, quadrupole, ...), u rows 8.
-template <int MODE>
+// DIR (MODE 1): the dipoles are the CG search direction p = z + b p_old
+// (src = p_old, z8 = z, b from scal), formed as each row is read.
+template <int MODE, bool DIR = false>
 __global__ void __launch_bounds__(256) k_spread(int n, GridParams G, const float4* __restrict__ spos,
-   const float* __restrict__ src, unsigned long long* __restrict__ q)
+   const float* __restrict__ src, const float* __restrict__ z8, const double* __restrict__ scal,
+   unsigned long long* __restrict__ q)
 {
    const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
    const int lane = threadIdx.x & 31;
@@ -216,7 +219,13 @@ __global__ void __launch_bounds__(256) k_spread(int n, GridParams G, const float
          grid_add(q, 2 * (row + xb), term0 * t1[ix][0] + term1 * t1[ix][1] + term2 * t1[ix][L - 1]);
       }
    } else {
-      const float* u = src + 8 * s;
+      float u[8];
+      if (DIR)
+         dir_row(src, z8, s, (float)scal[S_B_D], (float)scal[S_B_P], u);
+      else
+#pragma unroll
+         for (int c = 0; c < 6; ++c)
+            u[c] = src[8 * s + c];
       const float dx = G.a1 * u[0], dy = G.a2 * u[1], dz = G.a3 * u[2];
       const float px = G.a1 * u[3], py = G.a2 * u[4], pz = G.a3 * u[5];
       const float d01 = dy * u1 * v0 + dz * u0 * v1, d11 = dx * u0 * v0;
@@ -256,14 +265,16 @@ __global__ void k_conv(size_t ng, const float* __restrict__ infl, float2* __rest
 // a fixed xor tree combines the rows.  MODE 0: real part -> d and p field,
 // self term with the permanent dipole.  MODE 1: real -> d, imaginary -> p,
 // self term with the induced dipoles.  Plain stores, rows of 8 floats.
-template <int MODE, bool ACC>
-__global__ void __launch_bounds__(256) k_gather_field(int n, GridParams G, const float4* __restrict__ spos,
-   const float2* __restrict__ g, const float* __restrict__ rp, const float* __restrict__ u8, float* __restrict__ out)
+// AP (MODE 1, ACC): the dipoles are the CG search direction p = z + b p_old
+// (P.conj = p_old, P.zrsd = z); instead of the field, lane 0 stores
+// p and Ap = p/alpha - field, and the block partials of p.Ap give, in the
+// last block, the step length a = s / p.Ap.  Atoms are visited warp-strided
+// over at most RED_MAX blocks.
+template <int MODE, bool ACC, bool AP>
+__device__ __forceinline__ void gather_atom(int s, int lane, const GridParams& G, const float4* __restrict__ spos,
+   const float2* __restrict__ g, const float* __restrict__ rp, const float* __restrict__ u8, float* __restrict__ out,
+   const PcgAp& P, float bd, float bp, double* pap)
 {
-   const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-   const int lane = threadIdx.x & 31;
-   if (s >= n)
-      return;
    int i1, i2, i3;
    float w1, w2, w3;
    site(G, spos[s], i1, i2, i3, w1, w2, w3);
@@ -307,6 +318,26 @@ __global__ void __launch_bounds__(256) k_gather_field(int n, GridParams G, const
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1)
          acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
+   if (AP) {
+      // lane c < 6 finishes component c: p, its recip + self field added to
+      // the real-space field, Ap = p/alpha - field, and p.Ap
+      if (lane < 6) {
+         float ac = acc[0];
+#pragma unroll
+         for (int k = 1; k < 6; ++k)
+            if (lane == k)
+               ac = acc[k];
+         const int c = lane, x = 8 * s + c;
+         const float gc = c % 3 == 0 ? G.a1 : (c % 3 == 1 ? G.a2 : G.a3);
+         const float p = __fmaf_rn(c < 3 ? bd : bp, P.conj[x], P.zrsd[x]);
+         const float fld = out[x] + (G.selfterm * p - gc * ac);
+         const float v = P.polinv[s] * p - fld;
+         P.vec[x] = v;
+         P.conj[x] = p;
+         pap[c < 3 ? 0 : 1] += (double)p * v;
+      }
+      return;
+   }
    if (lane != 0)
       return;
    float* a = out + 8 * s;
@@ -330,6 +361,35 @@ __global__ void __launch_bounds__(256) k_gather_field(int n, GridParams G, const
 #pragma unroll
    for (int c = 0; c < 6; ++c)
       a[c] = ACC ? a[c] + r[c] : r[c];
+}
+
+template <int MODE, bool ACC, bool AP = false>
+__global__ void __launch_bounds__(256, 6) k_gather_field(int n, GridParams G, const float4* __restrict__ spos,
+   const float2* __restrict__ g, const float* __restrict__ rp, const float* __restrict__ u8, float* __restrict__ out,
+   PcgAp P)
+{
+   const int lane = threadIdx.x & 31;
+   if (!AP) {
+      const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+      if (s < n)
+         gather_atom<MODE, ACC, false>(s, lane, G, spos, g, rp, u8, out, P, 0.f, 0.f, nullptr);
+      return;
+   }
+   __shared__ double sh[64];
+   const float bd = (float)P.scal[S_B_D], bp = (float)P.scal[S_B_P];
+   double pap[2] = {0, 0};
+   const int nw = (gridDim.x * blockDim.x) >> 5;
+   for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < n; s += nw)
+      gather_atom<MODE, ACC, true>(s, lane, G, spos, g, rp, u8, out, P, bd, bp, pap);
+   store_partials<2>(P.red, R_PAP_D, pap, sh);
+   if (!last_block(P.state + ST_TICKET1))
+      return;
+   double tot[2];
+   sum_slots(P.red, R_PAP_D, 2, gridDim.x, sh, tot);
+   if (threadIdx.x == 0) {
+      P.scal[S_A_D] = tot[0] == 0 ? 0.0 : P.scal[S_SUM_D] / tot[0];
+      P.scal[S_A_P] = tot[1] == 0 ? 0.0 : P.scal[S_SUM_P] / tot[1];
+   }
 }
 
 // Multipole reciprocal + self energy per atom (warp per atom, level-3
@@ -1294,7 +1354,7 @@ int launch_dfield_recip_grid(Context* ctx)
    GridParams G = grid_params(ctx);
    prof_begin(ctx, P_SPREAD_MPOLE);
    k_spread<0><<<grid_for((long long)ctx->n * 32, 256), 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->srpole,
-      reinterpret_cast<unsigned long long*>(ctx->pme.qfx));
+      nullptr, nullptr, reinterpret_cast<unsigned long long*>(ctx->pme.qfx));
    prof_end(ctx);
    T9_CUDA(cudaGetLastError());
    return fft_conv(ctx);
@@ -1309,10 +1369,10 @@ int launch_dfield_recip_gather(Context* ctx, float* out6, bool acc)
    prof_begin(ctx, P_GATHER_MPOLE);
    if (acc)
       k_gather_field<0, true><<<nb, 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->pme.qgrid, ctx->srpole, nullptr,
-         out6);
+         out6, PcgAp{});
    else
       k_gather_field<0, false><<<nb, 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->pme.qgrid, ctx->srpole,
-         nullptr, out6);
+         nullptr, out6, PcgAp{});
    prof_end(ctx);
    T9_CUDA(cudaGetLastError());
    return T9GB_OK;
@@ -1331,7 +1391,7 @@ int launch_ufield_recip_grid(Context* ctx, const float* u6)
    GridParams G = grid_params(ctx);
    prof_begin(ctx, P_SPREAD_UIND);
    k_spread<1><<<grid_for((long long)ctx->n * 32, 256), 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, u6,
-      reinterpret_cast<unsigned long long*>(ctx->pme.qfx));
+      nullptr, nullptr, reinterpret_cast<unsigned long long*>(ctx->pme.qfx));
    prof_end(ctx);
    T9_CUDA(cudaGetLastError());
    return fft_conv(ctx);
@@ -1345,9 +1405,11 @@ int launch_ufield_recip_gather(Context* ctx, const float* u6, float* out6, bool 
    const int nb = grid_for((long long)ctx->n * 32, 256);
    prof_begin(ctx, P_GATHER_UIND);
    if (acc)
-      k_gather_field<1, true><<<nb, 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->pme.qgrid, nullptr, u6, out6);
+      k_gather_field<1, true><<<nb, 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->pme.qgrid, nullptr, u6, out6,
+         PcgAp{});
    else
-      k_gather_field<1, false><<<nb, 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->pme.qgrid, nullptr, u6, out6);
+      k_gather_field<1, false><<<nb, 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->pme.qgrid, nullptr, u6, out6,
+         PcgAp{});
    prof_end(ctx);
    T9_CUDA(cudaGetLastError());
    return T9GB_OK;
@@ -1359,6 +1421,34 @@ int launch_ufield_recip(Context* ctx, const float* u6, float* out6)
    return launch_ufield_recip_gather(ctx, u6, out6, false);
 }
 
+// the CG search direction's grid: p = z + b p_old formed by the spread
+int launch_ufield_recip_grid_dir(Context* ctx, const float* p6, const float* z6, const double* scal)
+{
+   if (!ctx->cfg.use_ewald)
+      return T9GB_OK;
+   GridParams G = grid_params(ctx);
+   prof_begin(ctx, P_SPREAD_UIND);
+   k_spread<1, true><<<grid_for((long long)ctx->n * 32, 256), 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, p6, z6,
+      scal, reinterpret_cast<unsigned long long*>(ctx->pme.qfx));
+   prof_end(ctx);
+   T9_CUDA(cudaGetLastError());
+   return fft_conv(ctx);
+}
+
+// recip + self field of the search direction added to the real-space field
+// in out6, then p, Ap and the step length (PcgAp)
+int launch_ufield_recip_gather_ap(Context* ctx, float* out6, const PcgAp& P)
+{
+   GridParams G = grid_params(ctx);
+   const int nb = std::min(RED_MAX, grid_for((long long)ctx->n * 32, 256));
+   prof_begin(ctx, P_GATHER_UIND);
+   k_gather_field<1, true, true><<<nb, 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->pme.qgrid, nullptr, nullptr,
+      out6, P);
+   prof_end(ctx);
+   T9_CUDA(cudaGetLastError());
+   return T9GB_OK;
+}
+
 }  // namespace t9gb
 
 namespace t9gb {
@@ -1368,7 +1458,7 @@ int launch_empole_recip(Context* ctx, double* e_atom)
       return T9GB_OK;
    GridParams G = grid_params(ctx);
    k_spread<0><<<grid_for((long long)ctx->n * 32, 256), 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->srpole,
-      reinterpret_cast<unsigned long long*>(ctx->pme.qfx));
+      nullptr, nullptr, reinterpret_cast<unsigned long long*>(ctx->pme.qfx));
    T9_CUDA(cudaGetLastError());
    T9_CHECK(fft_conv(ctx));
    k_empole_recip_self<<<grid_for((long long)ctx->n * 32, 256), 256, 0, ctx->stream>>>(ctx->n, G,
@@ -1394,7 +1484,7 @@ int launch_force_recip(Context* ctx, bool mpole, bool polar, float* wrec)
       T9_CUDA(cudaMemsetAsync(ctx->scal + 40, 0, sizeof(double) * 12, ctx->stream));
    }
    k_spread<0><<<nb, 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->srpole,
-      reinterpret_cast<unsigned long long*>(ctx->pme.qfx));
+      nullptr, nullptr, reinterpret_cast<unsigned long long*>(ctx->pme.qfx));
    T9_CUDA(cudaGetLastError());
    T9_CHECK(fft_conv(ctx, vir ? 1 : 0, mpole ? 0.5f * f : 0.f, 0.f, vir && polar, ctx->scal + 40));
    double* er = ctx->e_atom + np;
@@ -1411,7 +1501,7 @@ int launch_force_recip(Context* ctx, bool mpole, bool polar, float* wrec)
    T9_CUDA(cudaGetLastError());
    if (polar) {
       k_spread<1><<<nb, 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->uind,
-         reinterpret_cast<unsigned long long*>(ctx->pme.qfx));
+         nullptr, nullptr, reinterpret_cast<unsigned long long*>(ctx->pme.qfx));
       T9_CUDA(cudaGetLastError());
       T9_CHECK(fft_conv(ctx, vir ? 2 : 0, 0.f, 0.5f * f, false, ctx->scal + 46));
       k_gather_force_uind<<<nb, 256, 0, ctx->stream>>>(ctx->n, np, G, f, ctx->spos, ctx->pme.qgrid, ctx->srpole,

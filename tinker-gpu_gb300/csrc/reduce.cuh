@@ -43,9 +43,22 @@ static __device__ __forceinline__ void sum_slots(const double* red, int first, i
 {
    const int slot = threadIdx.x >> 6, sub = threadIdx.x & 63;
    double v = 0;
-   if (slot < ns)
-      for (int i = sub; i < nb; i += 64)
-         v += red[(first + slot) * RED_MAX + i];
+   if (slot < ns) {
+      // eight loads in flight per round; the additions keep the order of i
+      const double* p = red + (first + slot) * RED_MAX;
+      int i = sub;
+      for (; i + 7 * 64 < nb; i += 8 * 64) {
+         double t[8];
+#pragma unroll
+         for (int k = 0; k < 8; ++k)
+            t[k] = p[i + k * 64];
+#pragma unroll
+         for (int k = 0; k < 8; ++k)
+            v += t[k];
+      }
+      for (; i < nb; i += 64)
+         v += p[i];
+   }
 #pragma unroll
    for (int o = 16; o > 0; o >>= 1)
       v += __shfl_down_sync(0xffffffffu, v, o);
@@ -119,6 +132,69 @@ static __device__ __forceinline__ bool last_block(int* ticket)
          *ticket = 0;
    }
    return last;
+}
+
+// The CG scalars after the r.z / r.r sums (thread 0 of the last block).
+// tot = {r.z d, r.z p, r.r d, r.r p}.  init: s = r.z, the first search
+// direction is z itself (b = 0), counters reset.  Loop: b = s1 / s, s = s1,
+// eps = debye sqrt(max(r.r) / n), iteration count, convergence (at least
+// miniter, at most politer iterations), status, and the graph's WHILE
+// condition (induceMutualPcg1_cu, src/cu/amoeba/pcg.cu:120-168).
+__device__ __forceinline__ void pcg_scalars(const double* tot, double* scal, int* state, int init, int n,
+   double debye, double poleps, int politer, int miniter, cudaGraphConditionalHandle handle, int use_handle)
+{
+   const double s1_d = tot[0], s1_p = tot[1], q_d = tot[2], q_p = tot[3];
+   if (init) {
+      scal[S_SUM_D] = s1_d;
+      scal[S_SUM_P] = s1_p;
+      scal[S_B_D] = 0.0;
+      scal[S_B_P] = 0.0;
+      state[ST_ITER] = 0;
+      state[ST_DONE] = 0;
+      state[ST_STATUS] = T9GB_OK;
+      return;
+   }
+   const double s_d = scal[S_SUM_D], s_p = scal[S_SUM_P];
+   scal[S_B_D] = s_d == 0 ? 0.0 : s1_d / s_d;
+   scal[S_B_P] = s_p == 0 ? 0.0 : s1_p / s_p;
+   scal[S_SUM_D] = s1_d;
+   scal[S_SUM_P] = s1_p;
+   const double eps = debye * sqrt(fmax(q_d, q_p) / n);
+   const int iter = state[ST_ITER] + 1;
+   state[ST_ITER] = iter;
+   bool done = eps < poleps;
+   if (iter < miniter)
+      done = false;
+   if (iter >= politer)
+      done = true;
+   const bool nan = !(eps == eps);
+   if (nan)
+      done = true;
+   scal[S_EPS] = eps;
+   state[ST_DONE] = done ? 1 : 0;
+   state[ST_STATUS] = nan ? T9GB_NAN_DETECTED : (done && !(eps < poleps) ? T9GB_NOT_CONVERGED : T9GB_OK);
+   if (use_handle)
+      cudaGraphSetConditional(handle, done ? 0u : 1u);
+}
+
+// Row s of the search direction p = z + b p_old formed where it is read
+// (components 0-5: d with b_d, p with b_p; 6-7: the row's tags from p_old).
+// Every reader forms it with the same fused multiply-add, so all see the
+// same values.
+__device__ __forceinline__ void dir_row(const float* __restrict__ p8, const float* __restrict__ z8, int s, float bd,
+   float bp, float* v)
+{
+   const float4* p = reinterpret_cast<const float4*>(p8 + 8 * s);
+   const float4* z = reinterpret_cast<const float4*>(z8 + 8 * s);
+   const float4 p0 = p[0], p1 = p[1], z0 = z[0], z1 = z[1];
+   v[0] = __fmaf_rn(bd, p0.x, z0.x);
+   v[1] = __fmaf_rn(bd, p0.y, z0.y);
+   v[2] = __fmaf_rn(bd, p0.z, z0.z);
+   v[3] = __fmaf_rn(bp, p0.w, z0.w);
+   v[4] = __fmaf_rn(bp, p1.x, z1.x);
+   v[5] = __fmaf_rn(bp, p1.y, z1.y);
+   v[6] = p1.z;
+   v[7] = p1.w;
 }
 
 }  // namespace t9gb
