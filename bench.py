@@ -586,9 +586,9 @@ def main():
     mean_it = float(np.mean(iters))
     # own kernels per step (fused FFT, default CG fusion): positions 1, rotpole 2, list 5, permanent
     # field 6 (real, spread, 3 transform, gather), guess 1, field of the guess 6, r0 1, M r0 with the
-    # dots 1, peek + predictor save 1, predictor index 1, output 1; per PCG iteration: field 6,
-    # Ap 1, update 1, M r with the dots 1
-    launches_per_step = 26 + 9 * mean_it
+    # dots 1, peek + predictor save 1, predictor index 1, output 1; per PCG iteration: direction 1,
+    # field 6, Ap 1, update 1, M r with the dots 1
+    launches_per_step = 26 + 10 * mean_it
 
     # ---- forces: emplar (induce + multipole and polarization energy, gradient, virial) ----
     forces = None

@@ -304,13 +304,16 @@ int t9gb_pair_lanes(t9gb_context* ctx, int lanes);
  * sparse preconditioner also forms r.z, r.r and the CG scalars (else a
  * separate dot kernel, sparsePrecondApply + the dot products of
  * src/cu/amoeba/pcg.cu:120-150).  Bit 1 (PME only): the search direction
- * p = z + b p is formed by the kernels that read it and the mutual-field
- * gather also forms Ap, p.Ap and the step length (else a direction kernel
- * and a separate Ap kernel).  A tuning knob: the same iteration, results
- * equal up to the order of the partial sums.  Measured on GB300: bit 0
- * saves a launch per iteration; bit 1 costs more than it saves, since the
- * fused gather holds more registers and hides less of its grid-load
- * latency. */
+ * p = z + b p is formed by the kernels that read it (spread, real-space
+ * field, gather, and the Ap kernel, which stores it) instead of by a
+ * kernel of its own.  Bit 2 (with bit 1): the gather also forms Ap, p.Ap
+ * and the step length.  A tuning knob: the same iteration, results equal
+ * up to the order of the partial sums.  Measured on GB300 (induce ms per
+ * step, 12,288 / 98,304 atoms): mask 0 0.612 / 2.889, 1 0.609 / 2.853,
+ * 3 0.606 / 2.959, 7 0.632 / 2.962.  Bit 1 makes the real-space kernel read
+ * two rows per neighbour, which costs where that kernel is the longer arm
+ * of the iteration; bit 2 makes the gather hold more registers and hide
+ * less of its grid-load latency. */
 int t9gb_set_pcg_fusion(t9gb_context* ctx, int mask);
 
 /* Neighbour-list sizes: row capacity, entries of the current list (both

@@ -187,7 +187,7 @@ def test_reused_list_keeps_every_pair_within_cutoff(gpu_lib, oracle, tg):
     assert abs(en - eo) < 1e-5 * np.abs(parts).sum() + 1e-4
 
 
-@pytest.mark.parametrize("mask", [0, 2, 3])
+@pytest.mark.parametrize("mask", [0, 3, 7])
 def test_pcg_fusion_variants_agree(gpu_lib, tg, mask):
     """Every kernel-fusion setting of the CG iteration solves the same
     system: dipoles equal to rounding of the reordered partial sums, over a

@@ -390,7 +390,7 @@ class Engine:
 
     def pcg_fusion(self, mask=1):
         """Fusion of the CG iteration's kernels (bit 0 preconditioner + dots,
-        bit 1 direction formed by its readers + fused Ap)."""
+        bit 1 direction formed by its readers, bit 2 Ap fused into the gather)."""
         self._check(self.lib.t9gb_set_pcg_fusion(self.h, int(mask)))
 
     def use_graph(self, enable=True):

@@ -423,6 +423,7 @@ int launch_precond_sparse_dots(Context* ctx, const float* r6, float* z6, const P
 int launch_ufield_real_dir(Context* ctx, const float* p6, const float* z6, const double* scal, float* out6);
 int launch_ufield_recip_grid_dir(Context* ctx, const float* p6, const float* z6, const double* scal);
 int launch_ufield_recip_gather_ap(Context* ctx, float* out6, const PcgAp& P);
+int launch_ufield_recip_gather_dir(Context* ctx, float* out6, const PcgAp& P);
 int scatter_positions(Context* ctx);
 // side stream of the current capture level, and the fork / join of work on
 // it with the main stream (events, no host synchronisation)

@@ -139,15 +139,28 @@ __global__ void k_precond_dot(VecArgs A, const float* __restrict__ rsd, float* _
 
 // ---- loop body ----
 
-// Ap = p/alpha - ufield(p); partials p.Ap; last block: a = s / p.Ap
-__global__ void k_pcg_p1(VecArgs A, const float* __restrict__ fld, const float* __restrict__ conj,
-   float* __restrict__ vec, double* __restrict__ red, double* __restrict__ scal, int* __restrict__ state)
+// Ap = p/alpha - ufield(p); partials p.Ap; last block: a = s / p.Ap.
+// DIR: p = z + b p_old is formed here (as the field kernels formed it) and
+// stored.
+template <bool DIR>
+__global__ void k_pcg_p1(VecArgs A, const float* __restrict__ fld, float* __restrict__ conj,
+   const float* __restrict__ zrsd, float* __restrict__ vec, double* __restrict__ red, double* __restrict__ scal,
+   int* __restrict__ state)
 {
    __shared__ double sh[64];
    double dd = 0, dp = 0;
+   float bd = 0.f, bp = 0.f;
+   if (DIR) {
+      bd = (float)scal[S_B_D];
+      bp = (float)scal[S_B_P];
+   }
    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.ne; e += gridDim.x * blockDim.x) {
       const int s = e / 6, x = e + 2 * s;  // row s, component e - 6 s of [npad][8]
-      const float p = conj[x];
+      float p = conj[x];
+      if (DIR) {
+         p = __fmaf_rn(e - 6 * s < 3 ? bd : bp, p, zrsd[x]);
+         conj[x] = p;
+      }
       const float v = A.polinv[s] * p - fld[x];
       vec[x] = v;
       if (e - 6 * s < 3)
@@ -441,7 +454,7 @@ static int precond_dots(Context* ctx, const VecArgs& A, int init, cudaGraphCondi
 {
    const t9gb_config& c = ctx->cfg;
    const int miniter = init ? 3 : std::min(3, ctx->n);
-   if (A.sparse && (ctx->pcg_fuse & 1) && !ctx->prof.on) {
+   if (A.sparse && (ctx->pcg_fuse & 1)) {
       PcgDots D{ctx->conj, ctx->red, ctx->scal, ctx->status, init, ctx->n, c.debye, c.poleps, c.politer, miniter,
          handle, use_handle};
       return launch_precond_sparse_dots(ctx, ctx->rsd, ctx->zrsd, D);
@@ -474,14 +487,21 @@ static int pcg_body(Context* ctx, const VecArgs& A, cudaGraphConditionalHandle h
       T9_CHECK(launch_ufield_real_dir(ctx, ctx->conj, ctx->zrsd, ctx->scal, ctx->fld6));
       T9_CHECK(recip_join(ctx, k));
       PcgAp P{ctx->zrsd, ctx->conj, A.polinv, ctx->vec, ctx->red, ctx->scal, ctx->status};
-      T9_CHECK(launch_ufield_recip_gather_ap(ctx, ctx->fld6, P));
+      if (ctx->pcg_fuse & 4) {
+         T9_CHECK(launch_ufield_recip_gather_ap(ctx, ctx->fld6, P));
+      } else {
+         T9_CHECK(launch_ufield_recip_gather_dir(ctx, ctx->fld6, P));
+         k_pcg_p1<true><<<A.nb, VB, 0, ctx->stream>>>(A, ctx->fld6, ctx->conj, ctx->zrsd, ctx->vec, ctx->red,
+            ctx->scal, ctx->status);
+      }
    } else {
       prof_begin(ctx, P_VECTOR);
       k_pcg_dir<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->scal, ctx->conj, ctx->zrsd);
       prof_end(ctx);
       T9_CHECK(ufield6(ctx, ctx->conj, ctx->fld6));
       prof_begin(ctx, P_VECTOR);
-      k_pcg_p1<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->fld6, ctx->conj, ctx->vec, ctx->red, ctx->scal, ctx->status);
+      k_pcg_p1<false><<<A.nb, VB, 0, ctx->stream>>>(A, ctx->fld6, ctx->conj, nullptr, ctx->vec, ctx->red, ctx->scal,
+         ctx->status);
       prof_end(ctx);
    }
    prof_begin(ctx, P_VECTOR);

@@ -270,7 +270,7 @@ __global__ void k_conv(size_t ng, const float* __restrict__ infl, float2* __rest
 // p and Ap = p/alpha - field, and the block partials of p.Ap give, in the
 // last block, the step length a = s / p.Ap.  Atoms are visited warp-strided
 // over at most RED_MAX blocks.
-template <int MODE, bool ACC, bool AP>
+template <int MODE, bool ACC, bool AP, bool DIR>
 __device__ __forceinline__ void gather_atom(int s, int lane, const GridParams& G, const float4* __restrict__ spos,
    const float2* __restrict__ g, const float* __restrict__ rp, const float* __restrict__ u8, float* __restrict__ out,
    const PcgAp& P, float bd, float bp, double* pap)
@@ -348,7 +348,13 @@ __device__ __forceinline__ void gather_atom(int s, int lane, const GridParams& G
       r[1] = r[4] = -G.a2 * acc[1] + G.selfterm * m[2];
       r[2] = r[5] = -G.a3 * acc[2] + G.selfterm * m[3];
    } else {
-      const float* u = u8 + 8 * s;
+      float u[8];
+      if (DIR)
+         dir_row(P.conj, P.zrsd, s, bd, bp, u);
+      else
+#pragma unroll
+         for (int c = 0; c < 6; ++c)
+            u[c] = u8[8 * s + c];
       r[0] = G.selfterm * u[0] - G.a1 * acc[0];
       r[1] = G.selfterm * u[1] - G.a2 * acc[1];
       r[2] = G.selfterm * u[2] - G.a3 * acc[2];
@@ -363,7 +369,7 @@ __device__ __forceinline__ void gather_atom(int s, int lane, const GridParams& G
       a[c] = ACC ? a[c] + r[c] : r[c];
 }
 
-template <int MODE, bool ACC, bool AP = false>
+template <int MODE, bool ACC, bool AP = false, bool DIR = false>
 __global__ void __launch_bounds__(256, 6) k_gather_field(int n, GridParams G, const float4* __restrict__ spos,
    const float2* __restrict__ g, const float* __restrict__ rp, const float* __restrict__ u8, float* __restrict__ out,
    PcgAp P)
@@ -371,8 +377,13 @@ __global__ void __launch_bounds__(256, 6) k_gather_field(int n, GridParams G, co
    const int lane = threadIdx.x & 31;
    if (!AP) {
       const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+      float bd = 0.f, bp = 0.f;
+      if (DIR) {
+         bd = (float)P.scal[S_B_D];
+         bp = (float)P.scal[S_B_P];
+      }
       if (s < n)
-         gather_atom<MODE, ACC, false>(s, lane, G, spos, g, rp, u8, out, P, 0.f, 0.f, nullptr);
+         gather_atom<MODE, ACC, false, DIR>(s, lane, G, spos, g, rp, u8, out, P, bd, bp, nullptr);
       return;
    }
    __shared__ double sh[64];
@@ -380,7 +391,7 @@ __global__ void __launch_bounds__(256, 6) k_gather_field(int n, GridParams G, co
    double pap[2] = {0, 0};
    const int nw = (gridDim.x * blockDim.x) >> 5;
    for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < n; s += nw)
-      gather_atom<MODE, ACC, true>(s, lane, G, spos, g, rp, u8, out, P, bd, bp, pap);
+      gather_atom<MODE, ACC, true, false>(s, lane, G, spos, g, rp, u8, out, P, bd, bp, pap);
    store_partials<2>(P.red, R_PAP_D, pap, sh);
    if (!last_block(P.state + ST_TICKET1))
       return;
@@ -1433,6 +1444,20 @@ int launch_ufield_recip_grid_dir(Context* ctx, const float* p6, const float* z6,
    prof_end(ctx);
    T9_CUDA(cudaGetLastError());
    return fft_conv(ctx);
+}
+
+// recip + self field of the search direction p = z + b p_old (P.conj =
+// p_old, P.zrsd = z, P.scal = b) added to the real-space field in out6
+int launch_ufield_recip_gather_dir(Context* ctx, float* out6, const PcgAp& P)
+{
+   GridParams G = grid_params(ctx);
+   const int nb = grid_for((long long)ctx->n * 32, 256);
+   prof_begin(ctx, P_GATHER_UIND);
+   k_gather_field<1, true, false, true><<<nb, 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->pme.qgrid, nullptr,
+      nullptr, out6, P);
+   prof_end(ctx);
+   T9_CUDA(cudaGetLastError());
+   return T9GB_OK;
 }
 
 // recip + self field of the search direction added to the real-space field
