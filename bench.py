@@ -164,7 +164,8 @@ def algorithmic_bytes(kernel, n, entries, nfft):
     if kernel in ("gather_uind", "gather_mpole"):
         return 8 * ng + n * (16 + 24 + 24)
     if kernel == "pcg_vector":
-        return n * 6 * 4 * 8
+        # per iteration: direction (3 vectors), Ap (3 + 1/alpha), update (6): 4 vectors of 6 floats per launch
+        return n * 6 * 4 * 4
     if kernel == "nblist":
         return n * 16 + 4 * entries
     return n * 16
