@@ -348,15 +348,29 @@ int t9gb_set_xyz_host(t9gb_context* h, const double* xyz)
    // the previous copy out of the staging buffer must have finished
    if (ctx->ev_in_pending)
       T9_CUDA(cudaEventSynchronize(ctx->ev_in));
-   // one pass: convert and check (|x| < inf and not NaN: x - x == 0)
+   // one pass: convert and check finiteness (exponent field not all ones),
+   // four independent integer accumulators so the loop vectorizes
    float* st = ctx->h_in;
-   double bad = 0.0;
-   for (int i = 0; i < 3 * n; ++i) {
+   const int m = 3 * n;
+   constexpr uint64_t EXP = 0x7ff0000000000000ull;
+   uint64_t bad[4] = {0, 0, 0, 0};
+   int i = 0;
+   for (; i + 4 <= m; i += 4)
+      for (int k = 0; k < 4; ++k) {
+         const double v = xyz[i + k];
+         uint64_t b;
+         std::memcpy(&b, &v, sizeof b);
+         bad[k] |= (b & EXP) == EXP;
+         st[i + k] = (float)v;
+      }
+   for (; i < m; ++i) {
       const double v = xyz[i];
-      bad += v - v;
+      uint64_t b;
+      std::memcpy(&b, &v, sizeof b);
+      bad[0] |= (b & EXP) == EXP;
       st[i] = (float)v;
    }
-   if (bad != 0.0 || bad != bad)
+   if (bad[0] | bad[1] | bad[2] | bad[3])
       return T9GB_BAD_ARG;
    T9_CUDA(cudaMemcpyAsync(ctx->xyz, st, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
    T9_CUDA(cudaEventRecord(ctx->ev_in, ctx->stream));
@@ -471,13 +485,14 @@ int t9gb_induce_host(t9gb_context* h, const double* xyz, double* uind, double* u
    ctx->stage_out = false;
    if (st != T9GB_OK && st != T9GB_NOT_CONVERGED && st != T9GB_NAN_DETECTED)
       return st;
-   const int n = ctx->n;
-   for (int i = 0; i < 3 * n; ++i) {
-      if (uind)
-         uind[i] = ctx->h_stage[i];
-      if (uinp)
-         uinp[i] = ctx->h_stage[3 * n + i];
-   }
+   const int m = 3 * ctx->n;
+   const float* hs = ctx->h_stage;
+   if (uind)
+      for (int i = 0; i < m; ++i)
+         uind[i] = hs[i];
+   if (uinp)
+      for (int i = 0; i < m; ++i)
+         uinp[i] = hs[m + i];
    return st;
 }
 
