@@ -300,6 +300,14 @@ int t9gb_pme_own_fft(t9gb_context* ctx, int enable);
  * results are identical up to the order of the per-lane partial sums. */
 int t9gb_pair_lanes(t9gb_context* ctx, int lanes);
 
+/* Lanes of a warp that share one atom's neighbour row in the real-space
+ * force kernel (empole / epolar / emplar gradients): 8 (default), 16 or
+ * 32.  A tuning knob; results are identical up to the order of the
+ * per-lane partial sums.  Measured on GB300 (emplar with energy, gradient
+ * and virial, 12,288 / 98,304 atoms): 0.986 / 4.72 ms at 8 lanes, 1.004 /
+ * 5.01 at 16, 1.062 / 5.82 at 32. */
+int t9gb_force_lanes(t9gb_context* ctx, int lanes);
+
 /* Kernel fusion of the CG iteration (bit mask; default 1).  Bit 0: the
  * sparse preconditioner also forms r.z, r.r and the CG scalars (else a
  * separate dot kernel, sparsePrecondApply + the dot products of

@@ -28,9 +28,9 @@ EXPORTS = [
     "t9gb_profile_read", "t9gb_profile_name", "t9gb_ufield_noalloc", "t9gb_learn_config", "t9gb_learn_policy",
     "t9gb_learn_reset", "t9gb_learn_stats", "t9gb_learn_get_weights", "t9gb_learn_set_weights", "t9gb_learn_eval",
     "t9gb_learn_adamw", "t9gb_learn_features", "t9gb_empole", "t9gb_epolar", "t9gb_emplar", "t9gb_energy_components",
-    "t9gb_pme_own_fft", "t9gb_pair_lanes", "t9gb_set_pcg_fusion", "t9gb_set_thole_pairs", "t9gb_set_external_field",
-    "t9gb_set_vdw", "t9gb_ehal", "t9gb_set_valence", "t9gb_evalence", "t9gb_md_init", "t9gb_md_run", "t9gb_md_state",
-    "t9gb_md_positions_device", "t9gb_md_stats",
+    "t9gb_pme_own_fft", "t9gb_pair_lanes", "t9gb_force_lanes", "t9gb_set_pcg_fusion", "t9gb_set_thole_pairs",
+    "t9gb_set_external_field", "t9gb_set_vdw", "t9gb_ehal", "t9gb_set_valence", "t9gb_evalence", "t9gb_md_init",
+    "t9gb_md_run", "t9gb_md_state", "t9gb_md_positions_device", "t9gb_md_stats",
 ]
 CALC_ENERGY, CALC_GRAD, CALC_VIRIAL = 0x010, 0x020, 0x040
 
@@ -125,6 +125,7 @@ def load(path=None):
     lib.t9gb_pme_own_fft.argtypes = [vp, C.c_int]
     lib.t9gb_pair_lanes.argtypes = [vp, C.c_int]
     lib.t9gb_set_pcg_fusion.argtypes = [vp, C.c_int]
+    lib.t9gb_force_lanes.argtypes = [vp, C.c_int]
     lib.t9gb_set_thole_pairs.argtypes = [vp, C.c_int, ip, dp]
     lib.t9gb_set_external_field.argtypes = [vp, dp]
     lib.t9gb_set_vdw.argtypes = [vp, C.c_int, ip, dp, dp, dp, ip, C.c_int, ip, dp, C.c_double, C.c_double]
@@ -387,6 +388,9 @@ class Engine:
 
     def pair_lanes(self, lanes=16):
         self._check(self.lib.t9gb_pair_lanes(self.h, int(lanes)))
+
+    def force_lanes(self, lanes=8):
+        self._check(self.lib.t9gb_force_lanes(self.h, int(lanes)))
 
     def pcg_fusion(self, mask=1):
         """Fusion of the CG iteration's kernels (bit 0 preconditioner + dots,

@@ -576,6 +576,14 @@ int t9gb_pair_lanes(t9gb_context* h, int lanes)
    return T9GB_OK;
 }
 
+int t9gb_force_lanes(t9gb_context* h, int lanes)
+{
+   if (!h || (lanes != 8 && lanes != 16 && lanes != 32))
+      return T9GB_BAD_ARG;
+   h->c.force_lanes = lanes;
+   return T9GB_OK;
+}
+
 int t9gb_set_pcg_fusion(t9gb_context* h, int mask)
 {
    if (!h || mask < 0 || mask > 7)

@@ -724,12 +724,25 @@ int frame_map_build(Context* ctx)
 // e_atom receives the multipole energy terms (real, recip, self) when mpole.
 // vir: per-slot virial rows wvir [27][npad] (real, frame, reciprocal) and the
 // k-space sums in scal[40..51].
-template <bool MPOLE, bool POLAR, bool VIR>
-static void launch_real(Context* ctx, const PairParams& P, float f, int grid)
+template <int G, bool MPOLE, bool POLAR, bool VIR>
+static void launch_real_g(Context* ctx, const PairParams& P, float f)
 {
-   k_elec_real<GROUP, MPOLE, POLAR, VIR><<<grid, 128, 0, ctx->stream>>>(P, ctx->npad, f, ctx->nbrc, ctx->nnbrc,
+   const int grid = grid_for((long long)ctx->npad * G, 128);
+   k_elec_real<G, MPOLE, POLAR, VIR><<<grid, 128, 0, ctx->stream>>>(P, ctx->npad, f, ctx->nbrc, ctx->nnbrc,
       ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos, ctx->srpole, ctx->uind, ctx->freal, ctx->treal,
       MPOLE ? ctx->e_atom : nullptr, ctx->wvir);
+}
+
+// lanes per atom: t9gb_force_lanes (8, 16 or 32)
+template <bool MPOLE, bool POLAR, bool VIR>
+static void launch_real(Context* ctx, const PairParams& P, float f, int)
+{
+   if (ctx->force_lanes == 8)
+      launch_real_g<8, MPOLE, POLAR, VIR>(ctx, P, f);
+   else if (ctx->force_lanes == 32)
+      launch_real_g<32, MPOLE, POLAR, VIR>(ctx, P, f);
+   else
+      launch_real_g<16, MPOLE, POLAR, VIR>(ctx, P, f);
 }
 
 int elec_forces(Context* ctx, bool mpole, bool polar, float* grad, bool vir)
