@@ -301,11 +301,11 @@ int t9gb_pme_own_fft(t9gb_context* ctx, int enable);
 int t9gb_pair_lanes(t9gb_context* ctx, int lanes);
 
 /* Lanes of a warp that share one atom's neighbour row in the real-space
- * force kernel (empole / epolar / emplar gradients): 8 (default), 16 or
- * 32.  A tuning knob; results are identical up to the order of the
- * per-lane partial sums.  Measured on GB300 (emplar with energy, gradient
- * and virial, 12,288 / 98,304 atoms): 0.986 / 4.72 ms at 8 lanes, 1.004 /
- * 5.01 at 16, 1.062 / 5.82 at 32. */
+ * force kernel (empole / epolar / emplar gradients): a power of two from
+ * 1 to 32, default 4.  A tuning knob; results are identical up to the
+ * order of the per-lane partial sums.  Measured on GB300 (emplar gradient,
+ * 12,288 / 98,304 atoms, ms): 1 lane 0.817 / 4.031, 2 0.781 / 4.051,
+ * 4 0.758 / 4.071, 8 0.768 / 4.148, 16 0.797 / 4.355. */
 int t9gb_force_lanes(t9gb_context* ctx, int lanes);
 
 /* Kernel fusion of the CG iteration (bit mask; default 1).  Bit 0: the

@@ -389,7 +389,7 @@ class Engine:
     def pair_lanes(self, lanes=16):
         self._check(self.lib.t9gb_pair_lanes(self.h, int(lanes)))
 
-    def force_lanes(self, lanes=8):
+    def force_lanes(self, lanes=4):
         self._check(self.lib.t9gb_force_lanes(self.h, int(lanes)))
 
     def pcg_fusion(self, mask=1):

@@ -578,7 +578,7 @@ int t9gb_pair_lanes(t9gb_context* h, int lanes)
 
 int t9gb_force_lanes(t9gb_context* h, int lanes)
 {
-   if (!h || (lanes != 8 && lanes != 16 && lanes != 32))
+   if (!h || lanes < 1 || lanes > 32 || (lanes & (lanes - 1)))
       return T9GB_BAD_ARG;
    h->c.force_lanes = lanes;
    return T9GB_OK;

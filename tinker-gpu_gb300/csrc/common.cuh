@@ -241,7 +241,7 @@ struct Context {
    int* h_over = nullptr;    // pinned mirror
    int pair_lanes = 8;            // lanes per atom in the field kernels
    int pcg_fuse = 1;              // t9gb_set_pcg_fusion
-   int force_lanes = 8;           // lanes per atom in the real-space force kernel
+   int force_lanes = 4;           // lanes per atom in the real-space force kernel
    bool list_stale = true;        // positions changed since the last list check
    bool list_need_build = true;   // no valid list for the current order / capacity
    float4* sref = nullptr;        // [npad] positions at the last list build
