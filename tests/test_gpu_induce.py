@@ -203,3 +203,23 @@ def test_pcg_fusion_variants_agree(gpu_lib, tg, mask):
         ub, pb, _ = b.induce_host(x)
         assert abs(a.stats()[0] - b.stats()[0]) <= 1
         assert np.abs(ua - ub).max() < 1e-6 and np.abs(pa - pb).max() < 1e-6
+
+
+def test_dipole_grid_range_fallback(gpu_lib, tg):
+    """The dipole grids pack d and p as 32-bit fixed point; dipoles large
+    enough to reach the packing guard make the context widen the range and
+    recompute, so the mutual field stays linear in the dipoles."""
+    s = tg.systems.make_config("water648")
+    e = engine_for(s)
+    rng = np.random.default_rng(3)
+    u = rng.normal(scale=0.1, size=(s.n, 3))
+    f1, p1 = e.ufield(u, -u)
+    big = 1000.0
+    f2, p2 = e.ufield(big * u, -big * u)
+    f1, p1, f2, p2 = (cpu(t) for t in (f1, p1, f2, p2))
+    scale = np.abs(f1).max()
+    assert np.abs(f2 / big - f1).max() < 1e-4 * scale
+    assert np.abs(p2 / big - p1).max() < 1e-4 * scale
+    # the widened context keeps solving
+    ud, _, _ = e.induce()
+    assert np.isfinite(cpu(ud)).all()

@@ -67,6 +67,9 @@ struct PmeGrid {
    long long* qfx = nullptr;  // fixed-point accumulation grid [n3][n2][n1][2]
    float* infl = nullptr;     // influence function [n3][n2][n1]
    float2* qstash = nullptr;  // transformed permanent grid kept for the virial cross terms
+   bool packed = false;       // the fixed-point grid holds packed d / p dipole values
+   int pack_shift = 24;       // their 32-bit fixed-point scale 2^pack_shift (16 after a range fallback)
+   bool probe = false;        // spreads of the learned guess's residual: their own range flag
 };
 
 // Per-kernel event timing (tracing): categories of timed launches.

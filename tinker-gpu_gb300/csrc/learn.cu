@@ -127,11 +127,15 @@ __global__ void k_resid_cmp(int ne, const float* __restrict__ polar, const float
    double tot[4];
    sum_slots(red, 0, 4, gridDim.x, sh, tot);
    if (threadIdx.x == 0) {
+      // a learned guess whose field left the grid's fixed-point range has no
+      // valid residual: the plain start is kept
+      const bool out = state[ST_RANGE_L] != 0;
+      state[ST_RANGE_L] = 0;
       scal[S_L_PLAIN_D] = tot[0];
       scal[S_L_PLAIN_P] = tot[1];
-      scal[S_L_LEARN_D] = tot[2];
-      scal[S_L_LEARN_P] = tot[3];
-      state[ST_LCHOICE] = (tot[2] < tot[0] ? 1 : 0) | (tot[3] < tot[1] ? 2 : 0);
+      scal[S_L_LEARN_D] = out ? INFINITY : tot[2];
+      scal[S_L_LEARN_P] = out ? INFINITY : tot[3];
+      state[ST_LCHOICE] = out ? 0 : (tot[2] < tot[0] ? 1 : 0) | (tot[3] < tot[1] ? 2 : 0);
    }
 }
 

@@ -537,7 +537,11 @@ static int pcg_start(Context* ctx, const VecArgs& A, bool graph, int variant)
       zero_guess ? 1 : 0);
    if (variant == V_COMPARE) {
       // residual of the learned guess; each of d, p starts from the smaller
-      T9_CHECK(ufield6(ctx, ctx->tmp6, ctx->vec));
+      // (a learned guess beyond the grid's fixed-point range is rejected)
+      ctx->pme.probe = true;
+      const int rc = ufield6(ctx, ctx->tmp6, ctx->vec);
+      ctx->pme.probe = false;
+      T9_CHECK(rc);
       T9_CHECK(learn_pick(ctx, ctx->tmp6, ctx->vec));
    }
    return precond_dots(ctx, A, 1, 0, 0);
@@ -693,13 +697,27 @@ int induce_sorted(Context* ctx)
 {
    const bool graph = ctx->use_graph && !ctx->prof.on;
    const int variant = pick_variant(ctx);
-   for (int attempt = 0; attempt < 2; ++attempt) {
+   bool range_failed = false;
+   for (int attempt = 0; attempt < 3; ++attempt) {
       T9_CHECK(graph ? induce_graph(ctx, variant) : induce_stepwise(ctx, variant));
       int redo = 0;
       T9_CHECK(check_list_overflow(ctx, &redo));
+      if (ctx->h_status[ST_RANGE]) {
+         // a dipole-grid contribution reached the packed fixed-point guard:
+         // widen the range (2^24 -> 2^16 scale) and solve again
+         T9_CUDA(cudaMemsetAsync(ctx->status + ST_RANGE, 0, sizeof(int), ctx->stream));
+         ctx->h_status[ST_RANGE] = 0;
+         if (ctx->pme.pack_shift > 16) {
+            ctx->pme.pack_shift = 16;
+            drop_graphs(ctx);
+            redo = 1;
+         } else {
+            range_failed = true;
+         }
+      }
       if (!redo)
          break;
-      // the overflowed solve saved a history frame: drop it
+      // the repeated solve saved a history frame: drop it
       if (pred_depth(ctx->cfg) > 0) {
          T9_CUDA(cudaMemcpy(ctx->h_status, ctx->status, sizeof(int) * ST_NSTAT, cudaMemcpyDeviceToHost));
          int v = ctx->h_status[ST_NUALT] - 1;
@@ -710,6 +728,10 @@ int induce_sorted(Context* ctx)
    ctx->last_iter = ctx->h_status[ST_ITER];
    ctx->last_eps = ctx->h_scal[S_EPS];
    ctx->last_status = ctx->h_status[ST_STATUS];
+   if (range_failed) {
+      ctx->last_error = "induced dipoles beyond the PME grid's fixed-point range (|alpha E| of order 10^3 e A)";
+      ctx->last_status = T9GB_NAN_DETECTED;
+   }
    ctx->learn_variant = variant;
    if (variant == V_COMPARE) {
       ctx->learn_last_choice = ctx->h_status[ST_LCHOICE];
@@ -737,12 +759,24 @@ int reset_predictor(Context* ctx)
 template <class F>
 static int with_list(Context* ctx, F&& body)
 {
-   for (int attempt = 0; attempt < 2; ++attempt) {
+   for (int attempt = 0; attempt < 3; ++attempt) {
       T9_CHECK(ensure_list(ctx));
       T9_CHECK(body());
       T9_CUDA(cudaStreamSynchronize(ctx->stream));
       int redo = 0;
       T9_CHECK(check_list_overflow(ctx, &redo));
+      int range = 0;
+      T9_CUDA(cudaMemcpy(&range, ctx->status + ST_RANGE, sizeof(int), cudaMemcpyDeviceToHost));
+      if (range) {
+         T9_CUDA(cudaMemset(ctx->status + ST_RANGE, 0, sizeof(int)));
+         if (ctx->pme.pack_shift <= 16) {
+            ctx->last_error = "dipoles beyond the PME grid's fixed-point range";
+            return T9GB_BAD_ARG;
+         }
+         ctx->pme.pack_shift = 16;
+         drop_graphs(ctx);
+         redo = 1;
+      }
       if (!redo)
          return T9GB_OK;
    }

@@ -134,6 +134,8 @@ struct GridParams {
    float r1, r2, r3;  // 1/box
    float a1, a2, a3;  // nfft / box
    float selfterm;    // 4 a^3 / (3 sqrt(pi))
+   float pk_s, pk_lim;  // dipole grids: 32-bit fixed-point scale, per-contribution guard
+   int* range;          // set when a contribution reaches pk_lim
 };
 
 __device__ __forceinline__ void site(const GridParams& G, float4 p, int& i1, int& i2, int& i3, float& w1, float& w2,
@@ -162,12 +164,48 @@ __device__ __forceinline__ void site(const GridParams& G, float4 p, int& i1, int
    i3 += (i3 < 0 ? G.n3 : 0);
 }
 
+// Fixed-point grid: one 64-bit word per point.  Multipole grids hold the
+// real part at scale 2^40 (to_fx).  Dipole grids pack the d value (high 32
+// bits) and the p value (low 32 bits) as 32-bit fixed point at scale pk_s
+// (2^24, or 2^16 after a range fallback): the word sum is A 2^32 + B for the
+// sums A, B of the halves, and both are recovered exactly while each stays
+// within the signed 32-bit range, so one reduction carries both grids.
+
 // fire-and-forget 64-bit reduction (no value returned, so the warp does not
 // wait on it)
+__device__ __forceinline__ void red_u64(unsigned long long* q, size_t idx, unsigned long long v)
+{
+   asm volatile("red.global.add.u64 [%0], %1;" ::"l"(q + idx), "l"(v) : "memory");
+}
+
 __device__ __forceinline__ void grid_add(unsigned long long* q, size_t idx, float v)
 {
    if (v != 0.f)
-      asm volatile("red.global.add.u64 [%0], %1;" ::"l"(q + idx), "l"((unsigned long long)to_fx(v)) : "memory");
+      red_u64(q, idx, (unsigned long long)to_fx(v));
+}
+
+// d and p values of one point into one word; a value at or above pk_lim in
+// magnitude (1/32 of the half's range) raises the range flag
+__device__ __forceinline__ void grid_add2(unsigned long long* q, size_t idx, float vd, float vp, const GridParams& G)
+{
+   if (vd == 0.f && vp == 0.f)
+      return;
+   if (!(fabsf(vd) < G.pk_lim && fabsf(vp) < G.pk_lim)) {
+      atomicOr(G.range, 1);
+      return;
+   }
+   const long long a = __float2int_rn(vd * G.pk_s), b = __float2int_rn(vp * G.pk_s);
+   red_u64(q, idx, (unsigned long long)(a * 4294967296ll + b));
+}
+
+// one word of the fixed-point grid as a complex value
+__device__ __forceinline__ float2 grid_word(long long w, int packed, float inv)
+{
+   if (!packed)
+      return make_float2(from_fx(w), 0.f);
+   const int b = (int)(unsigned)(unsigned long long)w;
+   const int a = (int)((w - (long long)b) >> 32);
+   return make_float2((float)a * inv, (float)b * inv);
 }
 
 // Spreading, one warp per atom: lane (jy, kz) < 25 owns one row of five x
@@ -216,7 +254,7 @@ __global__ void __launch_bounds__(256) k_spread(int n, GridParams G, const float
       for (int ix = 0; ix < 5; ++ix) {
          int xb = i1 + ix;
          xb -= (xb >= G.n1 ? G.n1 : 0);
-         grid_add(q, 2 * (row + xb), term0 * t1[ix][0] + term1 * t1[ix][1] + term2 * t1[ix][L - 1]);
+         grid_add(q, row + xb, term0 * t1[ix][0] + term1 * t1[ix][1] + term2 * t1[ix][L - 1]);
       }
    } else {
       float u[8];
@@ -234,19 +272,17 @@ __global__ void __launch_bounds__(256) k_spread(int n, GridParams G, const float
       for (int ix = 0; ix < 5; ++ix) {
          int xb = i1 + ix;
          xb -= (xb >= G.n1 ? G.n1 : 0);
-         grid_add(q, 2 * (row + xb), d01 * t1[ix][0] + d11 * t1[ix][1]);
-         grid_add(q, 2 * (row + xb) + 1, p01 * t1[ix][0] + p11 * t1[ix][1]);
+         grid_add2(q, row + xb, d01 * t1[ix][0] + d11 * t1[ix][1], p01 * t1[ix][0] + p11 * t1[ix][1], G);
       }
    }
 }
 
 // fixed -> complex float, clearing the fixed grid for the next spread
-__global__ void k_fx_to_grid(size_t ng, long long* __restrict__ q, float2* __restrict__ g)
+__global__ void k_fx_to_grid(size_t ng, long long* __restrict__ q, float2* __restrict__ g, int packed, float inv)
 {
    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < ng; i += (size_t)gridDim.x * blockDim.x) {
-      longlong2 v = reinterpret_cast<longlong2*>(q)[i];
-      g[i] = make_float2(from_fx(v.x), from_fx(v.y));
-      reinterpret_cast<longlong2*>(q)[i] = make_longlong2(0, 0);
+      g[i] = grid_word(q[i], packed, inv);
+      q[i] = 0;
    }
 }
 
@@ -634,7 +670,7 @@ __host__ __device__ constexpr int fft_zline_ld()
 // memory N (N + 1) + 128 float2
 template <int N, bool FROM_FX, bool INV>
 __global__ void __launch_bounds__(N * fft_threads_per_line<N>()) k_fft_plane(long long* __restrict__ qfx,
-   float2* __restrict__ g)
+   float2* __restrict__ g, int packed, float inv)
 {
    // element (y, x) at fsm[fsig(y) LD + fsig(x)]; the padding keeps the two
    // lines of a 16-thread shared-memory phase on different banks
@@ -649,15 +685,15 @@ __global__ void __launch_bounds__(N * fft_threads_per_line<N>()) k_fft_plane(lon
    for (int c = 0; c < R; c += 8) {
       float2 v[8];
       if (FROM_FX) {
-         longlong2* q = reinterpret_cast<longlong2*>(qfx) + base + threadIdx.x;
-         longlong2 f[8];
+         long long* q = qfx + base + threadIdx.x;
+         long long f[8];
 #pragma unroll
          for (int r = 0; r < 8; ++r)
             f[r] = q[(c + r) * NT];
 #pragma unroll
          for (int r = 0; r < 8; ++r) {
-            q[(c + r) * NT] = make_longlong2(0, 0);
-            v[r] = make_float2(from_fx(f[r].x), from_fx(f[r].y));
+            q[(c + r) * NT] = 0;
+            v[r] = grid_word(f[r], packed, inv);
          }
       } else {
 #pragma unroll
@@ -752,8 +788,8 @@ template <int N>
 static int fft_setup_kernels(Context* ctx)
 {
    const int bytes = (int)fft_plane_smem<N>();
-   void (*fwd)(long long*, float2*) = k_fft_plane<N, true, false>;
-   void (*inv)(long long*, float2*) = k_fft_plane<N, false, true>;
+   void (*fwd)(long long*, float2*, int, float) = k_fft_plane<N, true, false>;
+   void (*inv)(long long*, float2*, int, float) = k_fft_plane<N, false, true>;
    T9_CUDA(cudaFuncSetAttribute(fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
    T9_CUDA(cudaFuncSetAttribute(inv, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
    return T9GB_OK;
@@ -764,7 +800,8 @@ template <int N>
 static void fft_own_forward(const PmeGrid& P, cudaStream_t st, bool split)
 {
    constexpr int T = fft_threads_per_line<N>();
-   k_fft_plane<N, true, false><<<N, N * T, fft_plane_smem<N>(), st>>>(P.qfx, P.qgrid);
+   k_fft_plane<N, true, false><<<N, N * T, fft_plane_smem<N>(), st>>>(P.qfx, P.qgrid, P.packed ? 1 : 0,
+      1.0f / (float)(1 << P.pack_shift));
    if (split)
       k_fft_zline<N, 0><<<N * N / 16, 16 * T, 0, st>>>(P.infl, P.qgrid);
    else
@@ -777,7 +814,7 @@ static void fft_own_inverse(const PmeGrid& P, cudaStream_t st, bool split)
    constexpr int T = fft_threads_per_line<N>();
    if (split)
       k_fft_zline<N, 1><<<N * N / 16, 16 * T, 0, st>>>(P.infl, P.qgrid);
-   k_fft_plane<N, false, true><<<N, N * T, fft_plane_smem<N>(), st>>>(P.qfx, P.qgrid);
+   k_fft_plane<N, false, true><<<N, N * T, fft_plane_smem<N>(), st>>>(P.qfx, P.qgrid, 0, 0.f);
 }
 
 // ---------------------------------------------------------------------------
@@ -1201,8 +1238,8 @@ int pme_setup(Context* ctx)
    P.n3 = c.nfft[2];
    const size_t ng = (size_t)P.n1 * P.n2 * P.n3;
    T9_CUDA(cudaMalloc(&P.qgrid, sizeof(float2) * ng));
-   T9_CUDA(cudaMalloc(&P.qfx, sizeof(long long) * 2 * ng));
-   T9_CUDA(cudaMemset(P.qfx, 0, sizeof(long long) * 2 * ng));
+   T9_CUDA(cudaMalloc(&P.qfx, sizeof(long long) * ng));
+   T9_CUDA(cudaMemset(P.qfx, 0, sizeof(long long) * ng));
    // influence function in double precision, stored as float
    std::vector<double> m1, m2, m3;
    bspline_moduli(P.n1, c.bsorder, m1);
@@ -1282,6 +1319,9 @@ static GridParams grid_params(const Context* ctx)
    G.a2 = (float)(c.nfft[1] / c.box[1]);
    G.a3 = (float)(c.nfft[2] / c.box[2]);
    G.selfterm = (float)(4.0 * c.aewald * c.aewald * c.aewald / (3.0 * 1.77245385090551602730));
+   G.pk_s = (float)(1 << ctx->pme.pack_shift);
+   G.pk_lim = (float)(1 << (31 - 5 - ctx->pme.pack_shift));
+   G.range = ctx->status + (ctx->pme.probe ? ST_RANGE_L : ST_RANGE);
    return G;
 }
 
@@ -1336,7 +1376,8 @@ static int fft_conv(Context* ctx, int vir = 0, float wE = 0.f, float wP = 0.f, b
       prof_end(ctx);
       return T9GB_OK;
    }
-   k_fx_to_grid<<<cb, 256, 0, ctx->stream>>>(ng, P.qfx, P.qgrid);
+   k_fx_to_grid<<<cb, 256, 0, ctx->stream>>>(ng, P.qfx, P.qgrid, P.packed ? 1 : 0,
+      1.0f / (float)(1 << P.pack_shift));
    T9_CUDA(cudaGetLastError());
    cufftSetStream(P.plan, ctx->stream);
    if (cufftExecC2C(P.plan, (cufftComplex*)P.qgrid, (cufftComplex*)P.qgrid, CUFFT_FORWARD) != CUFFT_SUCCESS) {
@@ -1364,6 +1405,7 @@ int launch_dfield_recip_grid(Context* ctx)
       return T9GB_OK;
    GridParams G = grid_params(ctx);
    prof_begin(ctx, P_SPREAD_MPOLE);
+   ctx->pme.packed = false;
    k_spread<0><<<grid_for((long long)ctx->n * 32, 256), 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->srpole,
       nullptr, nullptr, reinterpret_cast<unsigned long long*>(ctx->pme.qfx));
    prof_end(ctx);
@@ -1401,6 +1443,7 @@ int launch_ufield_recip_grid(Context* ctx, const float* u6)
       return T9GB_OK;
    GridParams G = grid_params(ctx);
    prof_begin(ctx, P_SPREAD_UIND);
+   ctx->pme.packed = true;
    k_spread<1><<<grid_for((long long)ctx->n * 32, 256), 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, u6,
       nullptr, nullptr, reinterpret_cast<unsigned long long*>(ctx->pme.qfx));
    prof_end(ctx);
@@ -1439,6 +1482,7 @@ int launch_ufield_recip_grid_dir(Context* ctx, const float* p6, const float* z6,
       return T9GB_OK;
    GridParams G = grid_params(ctx);
    prof_begin(ctx, P_SPREAD_UIND);
+   ctx->pme.packed = true;
    k_spread<1, true><<<grid_for((long long)ctx->n * 32, 256), 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, p6, z6,
       scal, reinterpret_cast<unsigned long long*>(ctx->pme.qfx));
    prof_end(ctx);
@@ -1482,6 +1526,7 @@ int launch_empole_recip(Context* ctx, double* e_atom)
    if (!ctx->cfg.use_ewald)
       return T9GB_OK;
    GridParams G = grid_params(ctx);
+   ctx->pme.packed = false;
    k_spread<0><<<grid_for((long long)ctx->n * 32, 256), 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->srpole,
       nullptr, nullptr, reinterpret_cast<unsigned long long*>(ctx->pme.qfx));
    T9_CUDA(cudaGetLastError());
@@ -1508,6 +1553,7 @@ int launch_force_recip(Context* ctx, bool mpole, bool polar, float* wrec)
       T9_CUDA(cudaMemsetAsync(wrec, 0, sizeof(float) * 9 * np, ctx->stream));
       T9_CUDA(cudaMemsetAsync(ctx->scal + 40, 0, sizeof(double) * 12, ctx->stream));
    }
+   ctx->pme.packed = false;
    k_spread<0><<<nb, 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->srpole,
       nullptr, nullptr, reinterpret_cast<unsigned long long*>(ctx->pme.qfx));
    T9_CUDA(cudaGetLastError());
@@ -1525,6 +1571,7 @@ int launch_force_recip(Context* ctx, bool mpole, bool polar, float* wrec)
          ctx->srpole, ctx->uind, ctx->frecp, ctx->trecp, nullptr, nullptr, wrec);
    T9_CUDA(cudaGetLastError());
    if (polar) {
+      ctx->pme.packed = true;
       k_spread<1><<<nb, 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->uind,
          nullptr, nullptr, reinterpret_cast<unsigned long long*>(ctx->pme.qfx));
       T9_CUDA(cudaGetLastError());

@@ -12,7 +12,10 @@ enum { S_SUM_D = 0, S_SUM_P, S_A_D, S_A_P, S_B_D, S_B_P, S_EPS, S_L_PLAIN_D = 8,
    S_L_LEARN_P, S_L_LOSS, S_NSCAL = 16 };
 // ST_LCHOICE: bit 0 / 1 set when the d / p solve started from the learned
 // guess; ST_LREADY: bit 0 feature statistics, bit 1 target scale fixed
-enum { ST_ITER = 0, ST_DONE, ST_STATUS, ST_NUALT, ST_TICKET0, ST_TICKET1, ST_LCHOICE, ST_LREADY, ST_NSTAT = 8 };
+// ST_RANGE: a dipole-grid contribution reached the packed fixed-point guard;
+// ST_RANGE_L: the same while evaluating the learned guess's residual
+enum { ST_ITER = 0, ST_DONE, ST_STATUS, ST_NUALT, ST_TICKET0, ST_TICKET1, ST_LCHOICE, ST_LREADY, ST_RANGE,
+   ST_RANGE_L, ST_NSTAT };
 enum { R_PAP_D = 0, R_PAP_P, R_RZ_D, R_RZ_P, R_RR_D, R_RR_P };
 
 static __device__ __forceinline__ double block_sum(double v, double* sh)
