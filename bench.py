@@ -154,13 +154,13 @@ def algorithmic_bytes(kernel, n, entries, nfft):
     if kernel == "precond_sparse":
         return n * (16 + 24 + 8 + 4 + 24) + 4 * entries
     if kernel == "spread_uind":
-        # pos + dipoles in, fixed-point grid (16 B per point) written once
-        return n * (16 + 24) + 16 * ng
+        # pos + dipoles in, fixed-point grid (one 8-byte word per point: d and p packed) written once
+        return n * (16 + 24) + 8 * ng
     if kernel == "spread_mpole":
-        return n * (16 + 40) + 16 * ng
+        return n * (16 + 40) + 8 * ng
     if kernel == "fft_conv":
-        # fixed grid read + clear 32 B/pt, float grid write 8, conv r/w 16 + table 4, two FFTs r/w 32
-        return ng * (32 + 8 + 16 + 4 + 32)
+        # fixed grid read + clear 16 B/pt, float grid write 8, conv r/w 16 + table 4, two FFTs r/w 32
+        return ng * (16 + 8 + 16 + 4 + 32)
     if kernel in ("gather_uind", "gather_mpole"):
         return 8 * ng + n * (16 + 24 + 24)
     if kernel == "pcg_vector":
