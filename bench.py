@@ -57,7 +57,8 @@ def parse():
     ap.add_argument("--fft", choices=["auto", "own", "cufft"], default="auto",
                     help="PME transform: the library's default (its fused transform on cubic 32/64 grids, cuFFT "
                     "otherwise), the fused transform, or cuFFT")
-    ap.add_argument("--lanes", type=int, default=8, help="lanes per atom in the real-space field kernels")
+    ap.add_argument("--lanes", type=int, default=0,
+                    help="lanes per atom in the real-space field kernels (0: the library's choice by box size)")
     ap.add_argument("--no-flush", action="store_true",
                     help="skip the 512 MB L2 flush buffer (for ncu captures only; numbers are not bench values)")
     return ap.parse_args()
@@ -492,7 +493,8 @@ def main():
     eng.prepare(tr.frame(0))
     if args.fft != "auto":
         eng.pme_own_fft(args.fft == "own")
-    eng.pair_lanes(args.lanes)
+    if args.lanes:
+        eng.pair_lanes(args.lanes)
     # frames: predictor history, warm-up, then the timed, e2e, per-kernel and
     # force passes, each continuing the trajectory (no time jumps for the predictor)
     f0 = args.history + args.warmup
@@ -663,7 +665,7 @@ def main():
                 "poleps_debye": s.settings["poleps"], "predictor": args.predictor, "history_frames": args.history,
                 "fft": {"auto": "library default: fused transform on cubic 32/64 grids, cuFFT C2C otherwise",
                         "own": "fused power-of-two transform (library)", "cufft": "cuFFT C2C"}[args.fft],
-                "lanes_per_atom": args.lanes,
+                "lanes_per_atom": args.lanes or "library default (8 up to 32,768 atoms, 4 above)",
                 "l2": "not flushed (profiling run)" if args.no_flush else "flushed (512 MB write) between timed steps",
                 "parallelism": f"replicas x{world}",
             },

@@ -296,8 +296,9 @@ int t9gb_use_graph(t9gb_context* ctx, int enable);
 int t9gb_pme_own_fft(t9gb_context* ctx, int enable);
 
 /* Lanes of a warp that share one atom's neighbour row in the real-space
- * field and preconditioner kernels: 8 (default), 16 or 32.  A tuning knob;
- * results are identical up to the order of the per-lane partial sums. */
+ * field and preconditioner kernels: 4, 8, 16 or 32 (default 8 up to 32,768
+ * atoms, 4 above).  A tuning knob; results are identical up to the order of
+ * the per-lane partial sums. */
 int t9gb_pair_lanes(t9gb_context* ctx, int lanes);
 
 /* Lanes of a warp that share one atom's neighbour row in the real-space

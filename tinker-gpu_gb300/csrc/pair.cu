@@ -58,15 +58,20 @@ __device__ __forceinline__ float pick6(const float* f, int g)
    return v;
 }
 
-// lanes g < 6 of the group store component g: out = base + f
+// lane g of a group of G stores components g, g + G, ... < 6: out = base + f
+template <int G>
 __device__ __forceinline__ void store6(float* __restrict__ out, const float* __restrict__ base, int s, int g,
    const float* f)
 {
-   if (g < 6) {
-      float v = pick6(f, g);
-      if (base)
-         v += base[8 * s + g];
-      out[8 * s + g] = v;
+#pragma unroll
+   for (int c0 = 0; c0 < 6; c0 += G) {
+      const int c = c0 + g;
+      if (c < 6) {
+         float v = pick6(f, c);
+         if (base)
+            v += base[8 * s + c];
+         out[8 * s + c] = v;
+      }
    }
 }
 
@@ -179,7 +184,7 @@ __global__ void __launch_bounds__(256) k_ufield_real(PairParams P, int npad, con
       }
    }
    group_reduce<G, 6>(f);
-   store6(out8, i < P.n ? base8 : nullptr, i, g, f);
+   store6<G>(out8, i < P.n ? base8 : nullptr, i, g, f);
 }
 
 // ---------------------------------------------------------------------------
@@ -309,7 +314,7 @@ __global__ void __launch_bounds__(256) k_dfield_real(PairParams P, int npad, con
       f[4] += e1;
       f[5] += e2;
    }
-   store6(out8, i < P.n ? base8 : nullptr, i, g, f);
+   store6<G>(out8, i < P.n ? base8 : nullptr, i, g, f);
 }
 
 // ---------------------------------------------------------------------------
@@ -337,14 +342,17 @@ __device__ __forceinline__ void precond_i(const PairParams& P, float r2, float3 
    f[5] += c * d.z - rr3 * rk[5];
 }
 
-// the preconditioner row of slot i: lane g < 6 returns z component g
+// the preconditioner row of slot i: the off-diagonal sums f[6] (reduced
+// over the group); z_c = udiag alpha_i r_c + f_c
 template <int G>
-__device__ __forceinline__ float precond_row(const PairParams& P, int i, int g, float udiag,
+__device__ __forceinline__ void precond_row(const PairParams& P, int i, int g, float* f,
    const int* __restrict__ nbr, const int* __restrict__ nnbr, const int* __restrict__ sp_start,
    const int* __restrict__ sp_j, const float4* __restrict__ sp_sc, const float4* __restrict__ spos,
    const float* __restrict__ r8)
 {
-   float f[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll
+   for (int c = 0; c < 6; ++c)
+      f[c] = 0.f;
    const float poli = r8[8 * i + 7];
    if (i < P.n) {
       const float4 pi = spos[i];
@@ -391,7 +399,6 @@ __device__ __forceinline__ float precond_row(const PairParams& P, int i, int g, 
       }
    }
    group_reduce<G, 6>(f);
-   return g < 6 ? udiag * poli * r8[8 * i + g] + pick6(f, g) : 0.f;
 }
 
 template <int G>
@@ -404,9 +411,15 @@ __global__ void __launch_bounds__(256) k_precond_sparse(PairParams P, int npad, 
    const int i = tid / G, g = tid % G;
    if (i >= npad)
       return;
-   const float z = precond_row<G>(P, i, g, udiag, nbr, nnbr, sp_start, sp_j, sp_sc, spos, r8);
-   if (g < 6)
-      z8[8 * i + g] = z;
+   float f[6];
+   precond_row<G>(P, i, g, f, nbr, nnbr, sp_start, sp_j, sp_sc, spos, r8);
+   const float poli = r8[8 * i + 7];
+#pragma unroll
+   for (int c0 = 0; c0 < 6; c0 += G) {
+      const int c = c0 + g;
+      if (c < 6)
+         z8[8 * i + c] = udiag * poli * r8[8 * i + c] + pick6(f, c);
+   }
 }
 
 // z = M r fused with the partial sums r.z, r.r (d and p) and, in the last
@@ -424,18 +437,25 @@ __global__ void __launch_bounds__(256, 4) k_precond_sparse_dots(PairParams P, in
    const int g = threadIdx.x % G;
    double rz_d = 0, rz_p = 0, rr_d = 0, rr_p = 0;
    for (int i = blockIdx.x * PER + threadIdx.x / G; i < npad; i += gridDim.x * PER) {
-      const float z = precond_row<G>(P, i, g, udiag, nbr, nnbr, sp_start, sp_j, sp_sc, spos, r8);
-      if (g < 6) {
-         const float r = r8[8 * i + g];
-         z8[8 * i + g] = z;
-         if (D.init)
-            D.conj[8 * i + g] = z;
-         if (g < 3) {
-            rz_d += (double)r * z;
-            rr_d += (double)r * r;
-         } else {
-            rz_p += (double)r * z;
-            rr_p += (double)r * r;
+      float f[6];
+      precond_row<G>(P, i, g, f, nbr, nnbr, sp_start, sp_j, sp_sc, spos, r8);
+      const float poli = r8[8 * i + 7];
+#pragma unroll
+      for (int c0 = 0; c0 < 6; c0 += G) {
+         const int c = c0 + g;
+         if (c < 6) {
+            const float r = r8[8 * i + c];
+            const float z = udiag * poli * r + pick6(f, c);
+            z8[8 * i + c] = z;
+            if (D.init)
+               D.conj[8 * i + c] = z;
+            if (c < 3) {
+               rz_d += (double)r * z;
+               rr_d += (double)r * r;
+            } else {
+               rz_p += (double)r * z;
+               rr_p += (double)r * r;
+            }
          }
       }
    }
@@ -640,7 +660,9 @@ int launch_list_filter(Context* ctx)
    do {                                                                                                                \
       const int g_ = ctx->pair_lanes;                                                                                  \
       const int nb_ = grid_for((long long)ctx->npad * g_, PAIR_THREADS);                                               \
-      if (g_ == 8)                                                                                                     \
+      if (g_ == 4)                                                                                                     \
+         KERNEL<4><<<nb_, PAIR_THREADS, 0, ctx->stream>>>(__VA_ARGS__);                                                \
+      else if (g_ == 8)                                                                                                \
          KERNEL<8><<<nb_, PAIR_THREADS, 0, ctx->stream>>>(__VA_ARGS__);                                                \
       else if (g_ == 32)                                                                                               \
          KERNEL<32><<<nb_, PAIR_THREADS, 0, ctx->stream>>>(__VA_ARGS__);                                               \
@@ -653,7 +675,9 @@ int launch_list_filter(Context* ctx)
    do {                                                                                                                \
       const int g_ = ctx->pair_lanes;                                                                                  \
       const int nb_ = grid_for((long long)ctx->npad * g_, PAIR_THREADS);                                               \
-      if (g_ == 8)                                                                                                     \
+      if (g_ == 4)                                                                                                     \
+         KERNEL<4, ARG><<<nb_, PAIR_THREADS, 0, ctx->stream>>>(__VA_ARGS__);                                           \
+      else if (g_ == 8)                                                                                                \
          KERNEL<8, ARG><<<nb_, PAIR_THREADS, 0, ctx->stream>>>(__VA_ARGS__);                                           \
       else if (g_ == 32)                                                                                               \
          KERNEL<32, ARG><<<nb_, PAIR_THREADS, 0, ctx->stream>>>(__VA_ARGS__);                                          \
@@ -702,7 +726,10 @@ int launch_precond_sparse_dots(Context* ctx, const float* r6, float* z6, const P
    const int per = PAIR_THREADS / g;
    const int nb = std::min(RED_MAX, (ctx->npad + per - 1) / per);
    prof_begin(ctx, P_PRECOND);
-   if (g == 8)
+   if (g == 4)
+      k_precond_sparse_dots<4><<<nb, PAIR_THREADS, 0, ctx->stream>>>(P, ctx->npad, (float)ctx->cfg.udiag, ctx->nbrp,
+         ctx->nnbrp, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos, r6, z6, D);
+   else if (g == 8)
       k_precond_sparse_dots<8><<<nb, PAIR_THREADS, 0, ctx->stream>>>(P, ctx->npad, (float)ctx->cfg.udiag, ctx->nbrp,
          ctx->nnbrp, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos, r6, z6, D);
    else if (g == 32)
