@@ -13,6 +13,7 @@ atom.  Coordinates and dipoles are stored as the files' six-decimal integers.
 Run in a checkout that has the reference at REFERENCE_ROOT (default
 /root/reference); the GPU machine never runs this.
 """
+import importlib
 import json
 import os
 import sys
@@ -21,70 +22,41 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 from make_localframe_golden import REF, read_prm  # noqa: E402
+
+tio = importlib.import_module("tinker-gpu_gb300.tinkerio")
 
 
 def read_frames(path):
     """Every frame of a Tinker .arc-style file: (box, names, xyz[f][n][3], types, bonds)."""
-    with open(path) as f:
-        lines = f.read().splitlines()
-    frames, names, types, bonds, boxes = [], None, None, None, []
-    i = 0
-    while i < len(lines) and lines[i].strip():
-        n = int(lines[i].split()[0])
-        boxes.append([float(v) for v in lines[i + 1].split()[:3]])
-        rows = [ln.split() for ln in lines[i + 2 : i + 2 + n]]
-        frames.append([[float(t[2]), float(t[3]), float(t[4])] for t in rows])
-        if names is None:
-            names = [t[1] for t in rows]
-            types = [int(t[5]) for t in rows]
-            bonds = sorted({(min(int(t[0]), int(b)) - 1, max(int(t[0]), int(b)) - 1) for t in rows for b in t[6:]})
-        i += 2 + n
-    return boxes, names, np.array(frames), types, bonds
+    frames = tio.read_xyz(path)
+    f0 = frames[0]
+    return ([list(f.box[:3]) for f in frames], f0.names, np.array([f.xyz for f in frames]), f0.types.tolist(),
+            f0.bonds)
 
 
 def read_dyn(path):
-    """Positions and velocities of a Tinker .dyn restart (Fortran D exponents)."""
-    with open(path) as f:
-        lines = f.read().splitlines()
-    n = int(lines[1].split()[0])
-    def block(title):
-        i = next(j for j, ln in enumerate(lines) if ln.strip().startswith(title)) + 1
-        return np.array([[float(v.replace("D", "E")) for v in ln.split()] for ln in lines[i : i + n]])
-    return block("Current Atomic Positions"), block("Current Atomic Velocities")
+    """Positions and velocities of a Tinker .dyn restart."""
+    x, v, _, _, _ = tio.read_dyn(path)
+    return x, v
 
 
 def read_md_params(path, types):
     """Masses by type, van der Waals records by class and the water valence
     records (bond 34-35, angle 35-34-35, Urey-Bradley 35-34-35)."""
-    mass, cls, vdw, bond, angle, urey, glob = {}, {}, {}, {}, {}, {}, {}
-    with open(path) as f:
-        for ln in f:
-            t = ln.split()
-            if not t:
-                continue
-            k = t[0].lower()
-            if k == "atom" and int(t[1]) in types:
-                cls[int(t[1])] = int(t[2])
-                mass[int(t[1])] = float(t[-2])
-            elif k == "vdw":
-                vdw[int(t[1])] = [float(v) for v in t[2:]]
-            elif k == "bond":
-                bond[(int(t[1]), int(t[2]))] = [float(t[3]), float(t[4])]
-            elif k == "angle":
-                angle[(int(t[1]), int(t[2]), int(t[3]))] = [float(t[4]), float(t[5])]
-            elif k == "ureybrad":
-                urey[(int(t[1]), int(t[2]), int(t[3]))] = [float(t[4]), float(t[5])]
-            elif k in ("bond-cubic", "bond-quartic", "angle-cubic", "angle-quartic", "angle-pentic", "angle-sextic",
-                       "urey-cubic", "urey-quartic"):
-                glob[k] = float(t[1])
+    P = tio.read_prm(path)
+    cls = {t: P.atoms[t][0] for t in types}
     o, hyd = cls[36], cls[37]
+    glob = {k: float(v[0]) for k, v in P.keywords.items()
+            if k in ("bond-cubic", "bond-quartic", "angle-cubic", "angle-quartic", "angle-pentic", "angle-sextic",
+                     "urey-cubic", "urey-quartic")}
     return {
-        "mass": {str(t): mass[t] for t in types},
-        "vdw": {str(t): vdw[cls[t]] for t in types},
-        "bond": bond[(min(o, hyd), max(o, hyd))],
-        "angle": angle[(hyd, o, hyd)],
-        "urey": urey[(hyd, o, hyd)],
+        "mass": {str(t): P.atoms[t][3] for t in types},
+        "vdw": {str(t): P.vdw[cls[t]] for t in types},
+        "bond": list(P.bond[(min(o, hyd), max(o, hyd))]),
+        "angle": list(P.angle[(hyd, o, hyd)]),
+        "urey": list(P.urey[(hyd, o, hyd)]),
         "globals": glob,
     }
 
