@@ -230,6 +230,10 @@ int t9gb_induce_stats(const t9gb_context* ctx, int* iterations, double* eps_deby
 /* Direct dipoles alpha*E of the last induce/dfield, [n][3] device. */
 int t9gb_get_udir(t9gb_context* ctx, float* udir_device, float* udirp_device);
 
+/* Induced dipoles of the last solve (induce, emplar, an MD step), [n][3]
+ * device, e A; either pointer may be NULL. */
+int t9gb_get_uind(t9gb_context* ctx, float* uind_device, float* uinp_device);
+
 /* Permanent-multipole energy (kcal/mol) of the current coordinates and
  * rotated multipoles (call t9gb_mpole_init first): real-space (with the
  * m-scaled exclusions), reciprocal and Ewald self parts in parts[3] (may be
@@ -302,11 +306,11 @@ int t9gb_pme_own_fft(t9gb_context* ctx, int enable);
 int t9gb_pair_lanes(t9gb_context* ctx, int lanes);
 
 /* Lanes of a warp that share one atom's neighbour row in the real-space
- * force kernel (empole / epolar / emplar gradients): a power of two from
- * 1 to 32, default 4.  A tuning knob; results are identical up to the
- * order of the per-lane partial sums.  Measured on GB300 (emplar gradient,
- * 12,288 / 98,304 atoms, ms): 1 lane 0.817 / 4.031, 2 0.781 / 4.051,
- * 4 0.758 / 4.071, 8 0.768 / 4.148, 16 0.797 / 4.355. */
+ * force kernel (empole / epolar / emplar gradients): 4 (default), 8 or
+ * 16.  A tuning knob; results are identical up to the order of the
+ * per-lane partial sums.  Measured on GB300 (emplar gradient, 12,288 /
+ * 98,304 atoms, ms): 1 lane 0.817 / 4.031, 2 0.781 / 4.051, 4 0.758 /
+ * 4.071, 8 0.768 / 4.148, 16 0.797 / 4.355 (1 and 2 are not built). */
 int t9gb_force_lanes(t9gb_context* ctx, int lanes);
 
 /* Kernel fusion of the CG iteration (bit mask; default 1).  Bit 0: the

@@ -24,13 +24,13 @@ EXPORTS = [
     "t9gb_create", "t9gb_destroy", "t9gb_status_string", "t9gb_last_error", "t9gb_set_stream", "t9gb_set_topology",
     "t9gb_set_xyz_host", "t9gb_set_xyz_device", "t9gb_nblist_build", "t9gb_mpole_init", "t9gb_dfield", "t9gb_ufield",
     "t9gb_sparse_precond_apply", "t9gb_induce", "t9gb_induce_host", "t9gb_induce_stats", "t9gb_get_udir",
-    "t9gb_empole_energy", "t9gb_epolar_energy", "t9gb_use_graph", "t9gb_nblist_stats", "t9gb_profile_enable",
-    "t9gb_profile_read", "t9gb_profile_name", "t9gb_ufield_noalloc", "t9gb_learn_config", "t9gb_learn_policy",
-    "t9gb_learn_reset", "t9gb_learn_stats", "t9gb_learn_get_weights", "t9gb_learn_set_weights", "t9gb_learn_eval",
-    "t9gb_learn_adamw", "t9gb_learn_features", "t9gb_empole", "t9gb_epolar", "t9gb_emplar", "t9gb_energy_components",
-    "t9gb_pme_own_fft", "t9gb_pair_lanes", "t9gb_force_lanes", "t9gb_set_pcg_fusion", "t9gb_set_thole_pairs",
-    "t9gb_set_external_field", "t9gb_set_vdw", "t9gb_ehal", "t9gb_set_valence", "t9gb_evalence", "t9gb_md_init",
-    "t9gb_md_run", "t9gb_md_state", "t9gb_md_positions_device", "t9gb_md_stats",
+    "t9gb_get_uind", "t9gb_empole_energy", "t9gb_epolar_energy", "t9gb_use_graph", "t9gb_nblist_stats",
+    "t9gb_profile_enable", "t9gb_profile_read", "t9gb_profile_name", "t9gb_ufield_noalloc", "t9gb_learn_config",
+    "t9gb_learn_policy", "t9gb_learn_reset", "t9gb_learn_stats", "t9gb_learn_get_weights", "t9gb_learn_set_weights",
+    "t9gb_learn_eval", "t9gb_learn_adamw", "t9gb_learn_features", "t9gb_empole", "t9gb_epolar", "t9gb_emplar",
+    "t9gb_energy_components", "t9gb_pme_own_fft", "t9gb_pair_lanes", "t9gb_force_lanes", "t9gb_set_pcg_fusion",
+    "t9gb_set_thole_pairs", "t9gb_set_external_field", "t9gb_set_vdw", "t9gb_ehal", "t9gb_set_valence",
+    "t9gb_evalence", "t9gb_md_init", "t9gb_md_run", "t9gb_md_state", "t9gb_md_positions_device", "t9gb_md_stats",
 ]
 CALC_ENERGY, CALC_GRAD, CALC_VIRIAL = 0x010, 0x020, 0x040
 
@@ -102,6 +102,7 @@ def load(path=None):
     lib.t9gb_induce_host.argtypes = [vp, dp, dp, dp]
     lib.t9gb_induce_stats.argtypes = [vp, ip, dp, ip]
     lib.t9gb_get_udir.argtypes = [vp, fp, fp]
+    lib.t9gb_get_uind.argtypes = [vp, fp, fp]
     lib.t9gb_empole_energy.argtypes = [vp, dp, dp]
     lib.t9gb_epolar_energy.argtypes = [vp, dp]
     lib.t9gb_use_graph.argtypes = [vp, C.c_int]
@@ -420,6 +421,12 @@ class Engine:
     def udir(self):
         f, fp = self._empty3(), self._empty3()
         self._check(self.lib.t9gb_get_udir(self.h, C.c_void_p(f.data_ptr()), C.c_void_p(fp.data_ptr())))
+        return f, fp
+
+    def uind(self):
+        """Induced dipoles (d, p) of the last solve, [n][3] CUDA tensors, e A."""
+        f, fp = self._empty3(), self._empty3()
+        self._check(self.lib.t9gb_get_uind(self.h, C.c_void_p(f.data_ptr()), C.c_void_p(fp.data_ptr())))
         return f, fp
 
     # ---- learned initial guess ----

@@ -523,6 +523,16 @@ int t9gb_get_udir(t9gb_context* h, float* udir, float* udirp)
    return scatter_from_sorted3(ctx, ctx->udir, udir, udirp);
 }
 
+int t9gb_get_uind(t9gb_context* h, float* uind, float* uinp)
+{
+   if (!h || (!uind && !uinp))
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   if (!ctx->have_order)
+      return T9GB_NOT_READY;
+   return scatter_from_sorted3(ctx, ctx->uind, uind, uinp);
+}
+
 int t9gb_use_graph(t9gb_context* h, int enable)
 {
    if (!h)
@@ -582,7 +592,7 @@ int t9gb_pair_lanes(t9gb_context* h, int lanes)
 
 int t9gb_force_lanes(t9gb_context* h, int lanes)
 {
-   if (!h || lanes < 1 || lanes > 32 || (lanes & (lanes - 1)))
+   if (!h || (lanes != 4 && lanes != 8 && lanes != 16))
       return T9GB_BAD_ARG;
    h->c.force_lanes = lanes;
    return T9GB_OK;

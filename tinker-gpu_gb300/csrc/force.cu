@@ -733,20 +733,14 @@ static void launch_real_g(Context* ctx, const PairParams& P, float f)
       MPOLE ? ctx->e_atom : nullptr, ctx->wvir);
 }
 
-// lanes per atom: t9gb_force_lanes (1, 2, 4, 8, 16 or 32)
+// lanes per atom: t9gb_force_lanes (4, 8 or 16)
 template <bool MPOLE, bool POLAR, bool VIR>
 static void launch_real(Context* ctx, const PairParams& P, float f, int)
 {
-   if (ctx->force_lanes == 1)
-      launch_real_g<1, MPOLE, POLAR, VIR>(ctx, P, f);
-   else if (ctx->force_lanes == 2)
-      launch_real_g<2, MPOLE, POLAR, VIR>(ctx, P, f);
-   else if (ctx->force_lanes == 4)
+   if (ctx->force_lanes == 4)
       launch_real_g<4, MPOLE, POLAR, VIR>(ctx, P, f);
    else if (ctx->force_lanes == 8)
       launch_real_g<8, MPOLE, POLAR, VIR>(ctx, P, f);
-   else if (ctx->force_lanes == 32)
-      launch_real_g<32, MPOLE, POLAR, VIR>(ctx, P, f);
    else
       launch_real_g<16, MPOLE, POLAR, VIR>(ctx, P, f);
 }

@@ -306,6 +306,25 @@ def _scales(params, keys):
     return sc
 
 
+def resolve_files(xyz_path, key_path=None, prm_path=None):
+    """(key path or None, parameter-file path) for a coordinate file: the
+    .key beside the .xyz unless given, and the parameter file that the key
+    names (relative to the key, .prm added when missing) unless given."""
+    if key_path is None:
+        cand = os.path.splitext(xyz_path)[0] + ".key"
+        key_path = cand if os.path.exists(cand) else None
+    if prm_path is None:
+        pv = read_key(key_path).get("parameters") if key_path else None
+        if not pv:
+            raise ValueError("no parameter file: give prm_path or a 'parameters' keyword")
+        prm_path = pv[0]
+        if not os.path.isabs(prm_path):
+            prm_path = os.path.join(os.path.dirname(key_path), prm_path)
+        if not os.path.exists(prm_path) and os.path.exists(prm_path + ".prm"):
+            prm_path += ".prm"
+    return key_path, prm_path
+
+
 def system_from_tinker(xyz_path, key_path=None, prm_path=None, frame=0, vdw=True, valence=True):
     """A System from a Tinker coordinate file, its keyword file (default: the
     .key beside the .xyz) and the parameter file the key names (or prm_path).
@@ -315,19 +334,8 @@ def system_from_tinker(xyz_path, key_path=None, prm_path=None, frame=0, vdw=True
     a-axis / b-axis / c-axis (else the file's box line), vdw-cutoff,
     vdw-taper; Tinker's defaults otherwise."""
     fr = read_xyz(xyz_path)[frame]
-    if key_path is None:
-        cand = os.path.splitext(xyz_path)[0] + ".key"
-        key_path = cand if os.path.exists(cand) else None
+    key_path, prm_path = resolve_files(xyz_path, key_path, prm_path)
     keys = read_key(key_path) if key_path else {}
-    if prm_path is None:
-        pv = keys.get("parameters")
-        if not pv:
-            raise ValueError("no parameter file: give prm_path or a 'parameters' keyword")
-        prm_path = pv[0]
-        if not os.path.isabs(prm_path) and key_path:
-            prm_path = os.path.join(os.path.dirname(key_path), prm_path)
-        if not os.path.exists(prm_path) and os.path.exists(prm_path + ".prm"):
-            prm_path += ".prm"
     P = read_prm(prm_path)
     types = [int(t) for t in fr.types]
     kinds = sorted(set(types))
