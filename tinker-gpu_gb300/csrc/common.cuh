@@ -62,9 +62,11 @@ struct PmeGrid {
    int n1 = 0, n2 = 0, n3 = 0;
    bool own_fft = false;      // power-of-two grid: the library's fused FFT path
    bool own_fft_ok = false;   // the grid qualifies
-   cufftHandle plan = 0;
+   cufftHandle plan = 0, plan2 = 0;
    float2* qgrid = nullptr;   // complex grid [n3][n2][n1]
-   long long* qfx = nullptr;  // fixed-point accumulation grid [n3][n2][n1][2]
+   long long* qfx = nullptr;  // fixed-point accumulation grid [n3][n2][n1], one word per point
+   float2* qgrid2 = nullptr;  // the second grid pair (induced-dipole reciprocal forces)
+   long long* qfx2 = nullptr;
    float* infl = nullptr;     // influence function [n3][n2][n1]
    float2* qstash = nullptr;  // transformed permanent grid kept for the virial cross terms
    bool packed = false;       // the fixed-point grid holds packed d / p dipole values
@@ -322,8 +324,10 @@ struct Context {
    // that joined a graph capture stays in it until that capture ends, so the
    // WHILE-body capture (on cap_stream) has its own side stream: [1] there,
    // [0] everywhere else.
-   cudaStream_t side_stream[2] = {nullptr, nullptr};
-   cudaEvent_t ev_fork[2] = {nullptr, nullptr}, ev_join[2] = {nullptr, nullptr};
+   // side streams: [0] eager forks, [1] forks inside a graph capture, [2] the
+   // second reciprocal half of the forces
+   cudaStream_t side_stream[3] = {nullptr, nullptr, nullptr};
+   cudaEvent_t ev_fork[3] = {nullptr, nullptr, nullptr}, ev_join[3] = {nullptr, nullptr, nullptr};
 
    // last induce statistics
    int last_iter = 0;
@@ -479,6 +483,8 @@ int elec_forces(Context* ctx, bool mpole, bool polar, float* grad, bool vir);
 // energy into the one-body block of e_atom, forces, torque field, virial rows
 int launch_extfield_mpole(Context* ctx, bool forces, bool vir);
 int launch_force_recip(Context* ctx, bool mpole, bool polar, float* wrec);
+int launch_force_recip_perm(Context* ctx, bool mpole, bool polar, float* wrec);
+int launch_force_recip_uind(Context* ctx, float* wrec, bool alt);
 int induce_sorted(Context* ctx);
 int learn_setup(Context* ctx);
 void learn_free(Context* ctx);

@@ -745,6 +745,13 @@ static void launch_real(Context* ctx, const PairParams& P, float f, int)
       launch_real_g<16, MPOLE, POLAR, VIR>(ctx, P, f);
 }
 
+// the second reciprocal half needs the third side stream (eager calls only:
+// inside a graph capture the side streams belong to the capture levels)
+static bool two_halves_ok(const Context* ctx)
+{
+   return ctx->side_stream[2] != nullptr && ctx->pme.qgrid2 != nullptr && side_index(ctx) == 0;
+}
+
 int elec_forces(Context* ctx, bool mpole, bool polar, float* grad, bool vir)
 {
    T9_CHECK(force_setup(ctx));
@@ -757,14 +764,23 @@ int elec_forces(Context* ctx, bool mpole, bool polar, float* grad, bool vir)
    const size_t np = ctx->npad;
    float* wrec = vir ? ctx->wvir + 18 * np : nullptr;
    // the reciprocal forces (spread, transform, gather: their own outputs)
-   // run on the side stream beside the real-space kernel
+   // run on side streams beside the real-space kernel; without the virial
+   // the permanent and the induced-dipole halves run beside each other too
+   // (the dipole half on the second grid)
    const bool side = ew && !ctx->prof.on;
+   const bool two = side && polar && !vir && two_halves_ok(ctx);
    const int k = side_index(ctx);
    if (side) {
       T9_CHECK(recip_fork(ctx, k));
+      if (two)
+         T9_CHECK(recip_fork(ctx, 2));
       cudaStream_t main = ctx->stream;
       ctx->stream = ctx->side_stream[k];
-      const int rc = launch_force_recip(ctx, mpole, polar, wrec);
+      int rc = two ? launch_force_recip_perm(ctx, mpole, polar, wrec) : launch_force_recip(ctx, mpole, polar, wrec);
+      if (rc == T9GB_OK && two) {
+         ctx->stream = ctx->side_stream[2];
+         rc = launch_force_recip_uind(ctx, wrec, true);
+      }
       ctx->stream = main;
       T9_CHECK(rc);
    }
@@ -784,8 +800,11 @@ int elec_forces(Context* ctx, bool mpole, bool polar, float* grad, bool vir)
          launch_real<false, true, false>(ctx, P, f, grid);
    }
    T9_CUDA(cudaGetLastError());
-   if (side)
+   if (side) {
       T9_CHECK(recip_join(ctx, k));
+      if (two)
+         T9_CHECK(recip_join(ctx, 2));
+   }
    else if (ew)
       T9_CHECK(launch_force_recip(ctx, mpole, polar, wrec));
    else if (vir)

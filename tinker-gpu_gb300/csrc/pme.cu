@@ -19,6 +19,7 @@
 //  - the grid accumulates in 64-bit fixed point (order-independent), then one
 //    pass converts it to the complex float grid and clears the fixed grid.
 #include <cmath>
+#include <utility>
 #include <vector>
 
 #include "common.cuh"
@@ -1240,6 +1241,11 @@ int pme_setup(Context* ctx)
    T9_CUDA(cudaMalloc(&P.qgrid, sizeof(float2) * ng));
    T9_CUDA(cudaMalloc(&P.qfx, sizeof(long long) * ng));
    T9_CUDA(cudaMemset(P.qfx, 0, sizeof(long long) * ng));
+   // the second grid: the induced-dipole half of the reciprocal forces runs
+   // beside the permanent half
+   T9_CUDA(cudaMalloc(&P.qgrid2, sizeof(float2) * ng));
+   T9_CUDA(cudaMalloc(&P.qfx2, sizeof(long long) * ng));
+   T9_CUDA(cudaMemset(P.qfx2, 0, sizeof(long long) * ng));
    // influence function in double precision, stored as float
    std::vector<double> m1, m2, m3;
    bspline_moduli(P.n1, c.bsorder, m1);
@@ -1268,7 +1274,8 @@ int pme_setup(Context* ctx)
    T9_CUDA(cudaMalloc(&d_infl, sizeof(float) * ng));
    T9_CUDA(cudaMemcpy(d_infl, infl.data(), sizeof(float) * ng, cudaMemcpyHostToDevice));
    P.infl = d_infl;
-   if (cufftPlan3d(&P.plan, P.n3, P.n2, P.n1, CUFFT_C2C) != CUFFT_SUCCESS) {
+   if (cufftPlan3d(&P.plan, P.n3, P.n2, P.n1, CUFFT_C2C) != CUFFT_SUCCESS ||
+      cufftPlan3d(&P.plan2, P.n3, P.n2, P.n1, CUFFT_C2C) != CUFFT_SUCCESS) {
       ctx->last_error = "cufftPlan3d failed";
       return T9GB_CUDA_ERR;
    }
@@ -1298,6 +1305,10 @@ void pme_free(Context* ctx)
    PmeGrid& P = ctx->pme;
    if (P.plan)
       cufftDestroy(P.plan);
+   if (P.plan2)
+      cufftDestroy(P.plan2);
+   cudaFree(P.qgrid2);
+   cudaFree(P.qfx2);
    cudaFree(P.qgrid);
    cudaFree(P.qfx);
    cudaFree(P.infl);
@@ -1540,9 +1551,13 @@ int launch_empole_recip(Context* ctx, double* e_atom)
 }  // namespace t9gb
 
 namespace t9gb {
-// reciprocal forces for elec_forces (force.cu); wrec (may be null): the
-// per-slot fractional-transform virial rows, k-space sums in scal[40..52)
-int launch_force_recip(Context* ctx, bool mpole, bool polar, float* wrec)
+// reciprocal forces for elec_forces (force.cu), in two halves: the
+// permanent-multipole grid (forces and torque fields of the multipoles, the
+// induced dipoles' force in the permanent field) and the induced-dipole
+// grid.  wrec (may be null): the per-slot fractional-transform virial rows,
+// k-space sums in scal[40..52); with the virial the dipole half reads the
+// permanent half's transformed grid, so the two run in order.
+int launch_force_recip_perm(Context* ctx, bool mpole, bool polar, float* wrec)
 {
    GridParams G = grid_params(ctx);
    const int nb = grid_for((long long)ctx->n * 32, 256);
@@ -1570,16 +1585,48 @@ int launch_force_recip(Context* ctx, bool mpole, bool polar, float* wrec)
       k_gather_force_perm<false, true><<<nb, 256, 0, ctx->stream>>>(ctx->n, np, G, f, a, ctx->spos, ctx->pme.qgrid,
          ctx->srpole, ctx->uind, ctx->frecp, ctx->trecp, nullptr, nullptr, wrec);
    T9_CUDA(cudaGetLastError());
-   if (polar) {
-      ctx->pme.packed = true;
-      k_spread<1><<<nb, 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->uind,
-         nullptr, nullptr, reinterpret_cast<unsigned long long*>(ctx->pme.qfx));
-      T9_CUDA(cudaGetLastError());
-      T9_CHECK(fft_conv(ctx, vir ? 2 : 0, 0.f, 0.5f * f, false, ctx->scal + 46));
-      k_gather_force_uind<<<nb, 256, 0, ctx->stream>>>(ctx->n, np, G, f, ctx->spos, ctx->pme.qgrid, ctx->srpole,
-         ctx->uind, ctx->frecu, ctx->trecu, wrec);
-      T9_CUDA(cudaGetLastError());
+   return T9GB_OK;
+}
+
+// alt: on the second grid (and FFT plan), so that it can run beside the
+// permanent half on another stream (no virial)
+int launch_force_recip_uind(Context* ctx, float* wrec, bool alt)
+{
+   PmeGrid& P = ctx->pme;
+   if (alt) {
+      std::swap(P.qfx, P.qfx2);
+      std::swap(P.qgrid, P.qgrid2);
+      std::swap(P.plan, P.plan2);
    }
+   GridParams G = grid_params(ctx);
+   const int nb = grid_for((long long)ctx->n * 32, 256);
+   const float f = (float)ctx->cfg.electric;
+   const bool vir = wrec != nullptr;
+   P.packed = true;
+   k_spread<1><<<nb, 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->uind,
+      nullptr, nullptr, reinterpret_cast<unsigned long long*>(P.qfx));
+   int rc = cudaGetLastError() == cudaSuccess ? T9GB_OK : T9GB_CUDA_ERR;
+   if (rc == T9GB_OK)
+      rc = fft_conv(ctx, vir ? 2 : 0, 0.f, 0.5f * f, false, ctx->scal + 46);
+   if (rc == T9GB_OK) {
+      k_gather_force_uind<<<nb, 256, 0, ctx->stream>>>(ctx->n, ctx->npad, G, f, ctx->spos, P.qgrid, ctx->srpole,
+         ctx->uind, ctx->frecu, ctx->trecu, wrec);
+      if (cudaGetLastError() != cudaSuccess)
+         rc = T9GB_CUDA_ERR;
+   }
+   if (alt) {
+      std::swap(P.qfx, P.qfx2);
+      std::swap(P.qgrid, P.qgrid2);
+      std::swap(P.plan, P.plan2);
+   }
+   return rc;
+}
+
+int launch_force_recip(Context* ctx, bool mpole, bool polar, float* wrec)
+{
+   T9_CHECK(launch_force_recip_perm(ctx, mpole, polar, wrec));
+   if (polar)
+      T9_CHECK(launch_force_recip_uind(ctx, wrec, false));
    return T9GB_OK;
 }
 }  // namespace t9gb
