@@ -82,7 +82,7 @@ static int alloc_all(Context* ctx)
    T9_CUDA(cudaMallocHost(&ctx->h_stage, ctx->h_stage_bytes));
    T9_CUDA(cudaMallocHost(&ctx->h_in, sizeof(float) * 3 * (size_t)npad));
    T9_CUDA(cudaEventCreateWithFlags(&ctx->ev_in, cudaEventDisableTiming));
-   for (int k = 0; k < 3; ++k) {
+   for (int k = 0; k < 4; ++k) {
       T9_CUDA(cudaStreamCreateWithFlags(&ctx->side_stream[k], cudaStreamNonBlocking));
       T9_CUDA(cudaEventCreateWithFlags(&ctx->ev_fork[k], cudaEventDisableTiming));
       T9_CUDA(cudaEventCreateWithFlags(&ctx->ev_join[k], cudaEventDisableTiming));
@@ -127,7 +127,7 @@ static void free_all(Context* ctx)
    drop_graphs(ctx);
    if (ctx->cap_stream)
       cudaStreamDestroy(ctx->cap_stream);
-   for (int k = 0; k < 3; ++k) {
+   for (int k = 0; k < 4; ++k) {
       if (ctx->side_stream[k])
          cudaStreamDestroy(ctx->side_stream[k]);
       if (ctx->ev_fork[k])

@@ -7,6 +7,7 @@
 #include <cufft.h>
 
 #include <cstdint>
+#include <functional>
 #include <random>
 #include <string>
 #include <vector>
@@ -175,6 +176,7 @@ struct Context {
    int* vch = nullptr;
    float4* vpos = nullptr;     // [npad] reduced sites, sorted; w = type (int bits)
    float* fvdw = nullptr;      // [npad][3] dE/dx of each reduced site
+   double* e_vdw = nullptr;    // [npad] van der Waals energy per site
    float* sp_v = nullptr;      // [nsp] van der Waals scale of each scaled pair
 
    // bond / angle / Urey-Bradley terms (t9gb_set_valence), caller order
@@ -194,6 +196,7 @@ struct Context {
    double* md_v = nullptr;     // [n][3] velocities, A/ps
    double* md_minv = nullptr;  // [n] 1 / mass
    float* md_g = nullptr;      // [n][3] total gradient at md_x
+   float* md_g2 = nullptr;     // [n][3] its van der Waals + valence part
    double* md_red = nullptr;   // kinetic-energy partials
    double* md_out = nullptr;   // [2] + ticket
    int* md_ticket = nullptr;
@@ -325,9 +328,10 @@ struct Context {
    // WHILE-body capture (on cap_stream) has its own side stream: [1] there,
    // [0] everywhere else.
    // side streams: [0] eager forks, [1] forks inside a graph capture, [2] the
-   // second reciprocal half of the forces
-   cudaStream_t side_stream[3] = {nullptr, nullptr, nullptr};
-   cudaEvent_t ev_fork[3] = {nullptr, nullptr, nullptr}, ev_join[3] = {nullptr, nullptr, nullptr};
+   // second reciprocal half of the forces, [3] the MD step's van der Waals
+   // and valence terms beside the electrostatic forces
+   cudaStream_t side_stream[4] = {nullptr, nullptr, nullptr, nullptr};
+   cudaEvent_t ev_fork[4] = {nullptr, nullptr, nullptr, nullptr}, ev_join[4] = {nullptr, nullptr, nullptr, nullptr};
 
    // last induce statistics
    int last_iter = 0;
@@ -433,6 +437,9 @@ int launch_ufield_recip_grid_dir(Context* ctx, const float* p6, const float* z6,
 int launch_ufield_recip_gather_ap(Context* ctx, float* out6, const PcgAp& P);
 int launch_ufield_recip_gather_dir(Context* ctx, float* out6, const PcgAp& P);
 int scatter_positions(Context* ctx);
+// t9gb_emplar(grad) with `beside` called once the dipoles are solved and the
+// list is current, before the electrostatic forces are launched
+int emplar_grad_beside(Context* ctx, float* grad, const std::function<int()>& beside);
 // side stream of the current capture level, and the fork / join of work on
 // it with the main stream (events, no host synchronisation)
 int side_index(const Context* ctx);

@@ -208,7 +208,8 @@ static int sum_virial(Context* ctx, double* virial)
    return T9GB_OK;
 }
 
-static int elec_terms(Context* ctx, bool mpole, bool polar, int vers, double* energy, float* grad, double* virial)
+static int elec_terms(Context* ctx, bool mpole, bool polar, int vers, double* energy, float* grad, double* virial,
+   const std::function<int()>* beside = nullptr)
 {
    double e = 0;
    if (polar) {
@@ -216,12 +217,19 @@ static int elec_terms(Context* ctx, bool mpole, bool polar, int vers, double* en
       if (rc != T9GB_OK)
          return rc;
    }
+   bool beside_done = false;
    for (int attempt = 0; attempt < 2; ++attempt) {
       // a list refreshed here needs its capacity checked; one already checked
       // (after the solve above, or an earlier call) does not, and the gradient
       // then stays in stream order without a synchronisation
       const bool fresh = ctx->list_stale || ctx->list_need_build;
       T9_CHECK(ensure_list(ctx));
+      // work that reads the list starts once the list is final: here when it
+      // was current already, else after the capacity check below
+      if (beside && !beside_done && !fresh) {
+         T9_CHECK((*beside)());
+         beside_done = true;
+      }
       T9_CUDA(cudaMemsetAsync(ctx->e_atom, 0, sizeof(double) * 3 * ctx->npad, ctx->stream));
       if (vers & (T9GB_CALC_GRAD | T9GB_CALC_VIRIAL)) {
          T9_CHECK(elec_forces(ctx, mpole, polar, (vers & T9GB_CALC_GRAD) ? grad : nullptr,
@@ -239,6 +247,8 @@ static int elec_terms(Context* ctx, bool mpole, bool polar, int vers, double* en
       if (!redo)
          break;
    }
+   if (beside && !beside_done)
+      T9_CHECK((*beside)());
    if (vers & T9GB_CALC_ENERGY) {
       if (mpole)
          T9_CHECK(sum_empole(ctx, &e));
@@ -257,6 +267,11 @@ static int elec_terms(Context* ctx, bool mpole, bool polar, int vers, double* en
    if (vers & T9GB_CALC_VIRIAL)
       T9_CHECK(sum_virial(ctx, virial));
    return T9GB_OK;
+}
+
+int emplar_grad_beside(Context* ctx, float* grad, const std::function<int()>& beside)
+{
+   return elec_terms(ctx, true, true, T9GB_CALC_GRAD, nullptr, grad, nullptr, &beside);
 }
 
 }  // namespace t9gb

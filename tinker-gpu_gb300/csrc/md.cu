@@ -22,11 +22,23 @@ constexpr double EKCAL = 418.4;
 constexpr double GASCONST = 1.987204259e-3;  // kcal/mol/K (Tinker's units::gasconst)
 
 // v += -g ekcal / m * h
-__global__ void k_md_kick(int n, double h, const float* __restrict__ g, const double* __restrict__ minv,
-   double* __restrict__ v)
+// v -= h g / m for the gradient g + g2 (g2: the van der Waals and valence
+// part, computed beside the electrostatic forces; may be null)
+__global__ void k_md_kick(int n, double h, const float* __restrict__ g, const float* __restrict__ g2,
+   const double* __restrict__ minv, double* __restrict__ v)
+{
+   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < 3 * n; e += gridDim.x * blockDim.x) {
+      const double gt = g2 ? (double)g[e] + (double)g2[e] : (double)g[e];
+      v[e] -= h * EKCAL * minv[e / 3] * gt;
+   }
+}
+
+// the step's total gradient g + g2 (g2 may be null)
+__global__ void k_md_grad_total(int n, const float* __restrict__ g, const float* __restrict__ g2,
+   float* __restrict__ out)
 {
    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < 3 * n; e += gridDim.x * blockDim.x)
-      v[e] -= h * EKCAL * minv[e / 3] * (double)g[e];
+      out[e] = g2 ? g[e] + g2[e] : g[e];
 }
 
 // x += v dt; the force kernels' float copy
@@ -85,12 +97,12 @@ __global__ void k_md_scale(int n, const double* __restrict__ s, double* __restri
 
 static int md_free(Context* ctx)
 {
-   void* p[] = {ctx->md_x, ctx->md_v, ctx->md_minv, ctx->md_g, ctx->md_red, ctx->md_out, ctx->md_rs};
+   void* p[] = {ctx->md_x, ctx->md_v, ctx->md_minv, ctx->md_g, ctx->md_g2, ctx->md_red, ctx->md_out, ctx->md_rs};
    for (void* q : p)
       if (q)
          cudaFree(q);
    ctx->md_x = ctx->md_v = ctx->md_minv = ctx->md_red = ctx->md_out = nullptr;
-   ctx->md_g = nullptr;
+   ctx->md_g = ctx->md_g2 = nullptr;
    ctx->md_rs = nullptr;
    ctx->md_rs_cap = 0;
    ctx->md_ready = false;
@@ -99,17 +111,38 @@ static int md_free(Context* ctx)
 
 void md_release(Context* ctx) { md_free(ctx); }
 
-// total gradient at ctx->xyz into md_g
+// gradient at ctx->xyz: electrostatics into md_g and, on side stream 3
+// beside the electrostatic forces (after the dipole solve, with the list
+// fixed), the van der Waals and valence terms into md_g2; the kicks add them
 static int md_forces(Context* ctx, t9gb_context* h)
 {
+   (void)h;
    T9_CHECK(scatter_positions(ctx));
    T9_CHECK(rotpole_sorted(ctx));
-   int st = t9gb_emplar(h, T9GB_CALC_GRAD, nullptr, ctx->md_g, nullptr);
-   if (st != T9GB_OK)
-      return st;
-   T9_CHECK(vdw_forces(ctx, ctx->md_g, true, false, nullptr));
-   T9_CHECK(valence_forces(ctx, ctx->md_g, true, false));
-   return T9GB_OK;
+   const bool extra = ctx->use_vdw || ctx->nval > 0;
+   if (extra)
+      T9_CUDA(cudaMemsetAsync(ctx->md_g2, 0, sizeof(float) * 3 * ctx->n, ctx->stream));
+   bool forked = false;
+   const std::function<int()> beside = [&]() -> int {
+      if (!extra)
+         return T9GB_OK;
+      T9_CUDA(cudaEventRecord(ctx->ev_fork[3], ctx->stream));
+      T9_CUDA(cudaStreamWaitEvent(ctx->side_stream[3], ctx->ev_fork[3], 0));
+      forked = true;
+      cudaStream_t main = ctx->stream;
+      ctx->stream = ctx->side_stream[3];
+      int rc = vdw_forces(ctx, ctx->md_g2, true, false, nullptr);
+      if (rc == T9GB_OK)
+         rc = valence_forces(ctx, ctx->md_g2, true, false);
+      ctx->stream = main;
+      return rc;
+   };
+   const int st = emplar_grad_beside(ctx, ctx->md_g, beside);
+   if (forked) {
+      T9_CUDA(cudaEventRecord(ctx->ev_join[3], ctx->side_stream[3]));
+      T9_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->ev_join[3], 0));
+   }
+   return st;
 }
 
 static int md_kinetic(Context* ctx, double* ekin)
@@ -151,6 +184,7 @@ extern "C" int t9gb_md_init(t9gb_context* h, const double* xyz, const double* ma
    T9_CUDA(cudaMalloc(&ctx->md_v, sizeof(double) * 3 * n));
    T9_CUDA(cudaMalloc(&ctx->md_minv, sizeof(double) * n));
    T9_CUDA(cudaMalloc(&ctx->md_g, sizeof(float) * 3 * n));
+   T9_CUDA(cudaMalloc(&ctx->md_g2, sizeof(float) * 3 * n));
    T9_CUDA(cudaMalloc(&ctx->md_red, sizeof(double) * RED_MAX));
    T9_CUDA(cudaMalloc(&ctx->md_out, sizeof(double) * 2 + sizeof(int) * 2));
    ctx->md_ticket = reinterpret_cast<int*>(ctx->md_out + 2);
@@ -191,6 +225,7 @@ extern "C" int t9gb_md_run(t9gb_context* h, int nsteps, double dt, int thermosta
       ctx->md_seed = seed;
    }
    const int nb = grid_for(3 * n, 256);
+   const bool extra = ctx->use_vdw || ctx->nval > 0;
    if (thermostat == 1 && nsteps > 0) {
       // the run's thermostat variates, drawn in the reference's order (one
       // normal, then one chi-squared with nfree - 1 degrees, per step)
@@ -212,7 +247,8 @@ extern "C" int t9gb_md_run(t9gb_context* h, int nsteps, double dt, int thermosta
       T9_CUDA(cudaStreamSynchronize(ctx->stream));
    }
    for (int step = 0; step < nsteps; ++step) {
-      k_md_kick<<<nb, 256, 0, ctx->stream>>>(n, 0.5 * dt, ctx->md_g, ctx->md_minv, ctx->md_v);
+      k_md_kick<<<nb, 256, 0, ctx->stream>>>(n, 0.5 * dt, ctx->md_g, extra ? ctx->md_g2 : nullptr, ctx->md_minv,
+         ctx->md_v);
       k_md_drift<<<nb, 256, 0, ctx->stream>>>(n, dt, ctx->md_v, ctx->md_x, ctx->xyz);
       T9_CUDA(cudaGetLastError());
       // a solve that fails to converge leaves no forces: the trajectory stops
@@ -222,7 +258,8 @@ extern "C" int t9gb_md_run(t9gb_context* h, int nsteps, double dt, int thermosta
          return st;
       ctx->md_steps += 1;
       ctx->md_iters += ctx->last_iter;
-      k_md_kick<<<nb, 256, 0, ctx->stream>>>(n, 0.5 * dt, ctx->md_g, ctx->md_minv, ctx->md_v);
+      k_md_kick<<<nb, 256, 0, ctx->stream>>>(n, 0.5 * dt, ctx->md_g, extra ? ctx->md_g2 : nullptr, ctx->md_minv,
+         ctx->md_v);
       T9_CUDA(cudaGetLastError());
       if (thermostat == 1) {
          // kinetic energy, factor and rescale on the device: no synchronisation
@@ -260,8 +297,12 @@ extern "C" int t9gb_md_state(t9gb_context* h, double* xyz, double* vel, float* g
       T9_CUDA(cudaMemcpyAsync(xyz, ctx->md_x, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
    if (vel)
       T9_CUDA(cudaMemcpyAsync(vel, ctx->md_v, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
-   if (grad_device)
-      T9_CUDA(cudaMemcpyAsync(grad_device, ctx->md_g, sizeof(float) * 3 * n, cudaMemcpyDeviceToDevice, ctx->stream));
+   if (grad_device) {
+      const bool extra = ctx->use_vdw || ctx->nval > 0;
+      k_md_grad_total<<<grid_for(3 * n, 256), 256, 0, ctx->stream>>>(n, ctx->md_g, extra ? ctx->md_g2 : nullptr,
+         grad_device);
+      T9_CUDA(cudaGetLastError());
+   }
    T9_CUDA(cudaStreamSynchronize(ctx->stream));
    return T9GB_OK;
 }

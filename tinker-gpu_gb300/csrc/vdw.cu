@@ -193,7 +193,8 @@ __global__ void k_vdw_combine(int n, const int* __restrict__ iperm, const int* _
 
 static void vdw_free(Context* ctx)
 {
-   void* p[] = {ctx->vtab, ctx->vtype, ctx->vparent, ctx->vred, ctx->vch_start, ctx->vch, ctx->vpos, ctx->fvdw};
+   void* p[] = {ctx->vtab, ctx->vtype, ctx->vparent, ctx->vred, ctx->vch_start, ctx->vch, ctx->vpos, ctx->fvdw,
+      ctx->e_vdw};
    for (void* q : p)
       if (q)
          cudaFree(q);
@@ -201,6 +202,7 @@ static void vdw_free(Context* ctx)
    ctx->vtype = ctx->vparent = ctx->vch_start = ctx->vch = nullptr;
    ctx->vred = ctx->fvdw = nullptr;
    ctx->vpos = nullptr;
+   ctx->e_vdw = nullptr;
 }
 
 void vdw_release(Context* ctx) { vdw_free(ctx); }
@@ -225,7 +227,7 @@ int vdw_forces(Context* ctx, float* grad, bool add, bool vir, double* energy)
    PairParams P = make_params(ctx, ctx->vdw_off);
    k_vdw_pos<<<grid_for(ctx->npad, 256), 256, 0, ctx->stream>>>(ctx->npad, P, ctx->perm, ctx->xyz, ctx->vtype,
       ctx->vparent, ctx->vred, ctx->vpos);
-   double* ev = ctx->e_atom + 2 * (size_t)ctx->npad;  // reused block: cleared by the caller
+   double* ev = ctx->e_vdw;  // every site's row written
    float* wv = vir ? ctx->wvir : nullptr;
    // lanes per atom: 16 on small boxes (more warps to hide the row loads),
    // 8 where the box fills the GPU anyway (GB300, ehal energy + gradient:
@@ -310,6 +312,7 @@ extern "C" int t9gb_set_vdw(t9gb_context* h, int ntypes, const int* vtype, const
    T9_CUDA(cudaMalloc(&ctx->vch, sizeof(int) * std::max<size_t>(1, cl.size())));
    T9_CUDA(cudaMalloc(&ctx->vpos, sizeof(float4) * npad));
    T9_CUDA(cudaMalloc(&ctx->fvdw, sizeof(float) * 3 * npad));
+   T9_CUDA(cudaMalloc(&ctx->e_vdw, sizeof(double) * npad));
    T9_CUDA(cudaMemcpy(ctx->vtab, tab.data(), sizeof(float2) * tab.size(), cudaMemcpyHostToDevice));
    T9_CUDA(cudaMemcpy(ctx->vtype, vtype, sizeof(int) * n, cudaMemcpyHostToDevice));
    T9_CUDA(cudaMemcpy(ctx->vparent, parent, sizeof(int) * n, cudaMemcpyHostToDevice));
@@ -365,7 +368,7 @@ extern "C" int t9gb_ehal(t9gb_context* h, int vers, double* energy, float* grad,
          break;
    }
    if (vers & T9GB_CALC_ENERGY)
-      T9_CHECK(sum_rows_d(ctx, ctx->e_atom + 2 * (size_t)ctx->npad, 1, energy));
+      T9_CHECK(sum_rows_d(ctx, ctx->e_vdw, 1, energy));
    if (vir)
       T9_CHECK(sum_rows_virial(ctx, ctx->wvir, 1, virial));
    return T9GB_OK;
