@@ -1,13 +1,14 @@
 // Real-space pair kernels over the per-step neighbour list.
 //
-// GROUP (16) consecutive lanes own one atom i: lane g walks the list entries
-// g, g+16, g+32, ... of atom i (consecutive addresses per step, two entries
-// in flight per trip), then the scaled partners of i the same way; the
-// partial fields are combined with a fixed xor-shuffle tree and written with
-// plain stores.  Every pair is
+// G consecutive lanes own one atom i (t9gb_pair_lanes: 8 up to 32,768 atoms,
+// 4 above): lane g walks the list entries g, g+G, g+2G, ... of atom i
+// (consecutive addresses per step, two entries in flight per trip), then the
+// scaled partners of i the same way; the partial fields are combined with a
+// fixed xor-shuffle tree and written with plain stores.  Every pair is
 // evaluated from both sides (full list), so no atomics are needed and each
 // field component is a sum in a fixed order: results are bit-reproducible.
-// 12,288 atoms give 196,608 threads, ~40 warps on each of the 152 SMs.
+// 12,288 atoms at 8 lanes give 98,304 threads, ~20 warps on each of the 152
+// SMs.
 //
 // Pair arithmetic restates the reference's pair_dfield_v2 / pair_ufield_v2
 // (include/seq/pair_field.h:127-256, :333-420) for the atom-i side, Thole
