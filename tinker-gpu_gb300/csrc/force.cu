@@ -735,7 +735,7 @@ static void launch_real_g(Context* ctx, const PairParams& P, float f)
 
 // lanes per atom: t9gb_force_lanes (4, 8 or 16)
 template <bool MPOLE, bool POLAR, bool VIR>
-static void launch_real(Context* ctx, const PairParams& P, float f, int)
+static void launch_real(Context* ctx, const PairParams& P, float f)
 {
    if (ctx->force_lanes == 4)
       launch_real_g<4, MPOLE, POLAR, VIR>(ctx, P, f);
@@ -759,7 +759,6 @@ int elec_forces(Context* ctx, bool mpole, bool polar, float* grad, bool vir)
       T9_CHECK(frame_map_build(ctx));
    const PairParams P = make_params(ctx, ctx->cfg.cutoff);
    const float f = (float)ctx->cfg.electric;
-   const int grid = grid_for((long long)ctx->npad * GROUP, 128);
    const bool ew = ctx->cfg.use_ewald != 0;
    const size_t np = ctx->npad;
    float* wrec = vir ? ctx->wvir + 18 * np : nullptr;
@@ -786,18 +785,18 @@ int elec_forces(Context* ctx, bool mpole, bool polar, float* grad, bool vir)
    }
    if (vir) {
       if (mpole && polar)
-         launch_real<true, true, true>(ctx, P, f, grid);
+         launch_real<true, true, true>(ctx, P, f);
       else if (mpole)
-         launch_real<true, false, true>(ctx, P, f, grid);
+         launch_real<true, false, true>(ctx, P, f);
       else
-         launch_real<false, true, true>(ctx, P, f, grid);
+         launch_real<false, true, true>(ctx, P, f);
    } else {
       if (mpole && polar)
-         launch_real<true, true, false>(ctx, P, f, grid);
+         launch_real<true, true, false>(ctx, P, f);
       else if (mpole)
-         launch_real<true, false, false>(ctx, P, f, grid);
+         launch_real<true, false, false>(ctx, P, f);
       else
-         launch_real<false, true, false>(ctx, P, f, grid);
+         launch_real<false, true, false>(ctx, P, f);
    }
    T9_CUDA(cudaGetLastError());
    if (side) {
