@@ -313,14 +313,18 @@ int t9gb_pair_lanes(t9gb_context* ctx, int lanes);
  * 4.071, 8 0.768 / 4.148, 16 0.797 / 4.355 (1 and 2 are not built). */
 int t9gb_force_lanes(t9gb_context* ctx, int lanes);
 
-/* Kernel fusion of the CG iteration (bit mask; default 1).  Bit 0: the
+/* Kernel fusion and overlap of the CG solve (bit mask; default 9).  Bit 0: the
  * sparse preconditioner also forms r.z, r.r and the CG scalars (else a
  * separate dot kernel, sparsePrecondApply + the dot products of
  * src/cu/amoeba/pcg.cu:120-150).  Bit 1 (PME only): the search direction
  * p = z + b p is formed by the kernels that read it (spread, real-space
  * field, gather, and the Ap kernel, which stores it) instead of by a
  * kernel of its own.  Bit 2 (with bit 1): the gather also forms Ap, p.Ap
- * and the step length.  A tuning knob: the same iteration, results equal
+ * and the step length.  Bit 3 (PME with a predictor): once the predictor's
+ * ring is full the field of the extrapolated guess is computed beside the
+ * permanent field (the guess does not depend on it), on the second grid and
+ * two more streams, with the same kernels and sums as in order.  A tuning
+ * knob: the same iteration, results equal
  * up to the order of the partial sums.  Measured on GB300 (induce ms per
  * step, 12,288 / 98,304 atoms): mask 0 0.612 / 2.889, 1 0.609 / 2.853,
  * 3 0.606 / 2.959, 7 0.632 / 2.962.  Bit 1 makes the real-space kernel read

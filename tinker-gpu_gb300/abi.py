@@ -393,9 +393,10 @@ class Engine:
     def force_lanes(self, lanes=4):
         self._check(self.lib.t9gb_force_lanes(self.h, int(lanes)))
 
-    def pcg_fusion(self, mask=1):
-        """Fusion of the CG iteration's kernels (bit 0 preconditioner + dots,
-        bit 1 direction formed by its readers, bit 2 Ap fused into the gather)."""
+    def pcg_fusion(self, mask=9):
+        """Fusion and overlap of the CG solve (bit 0 preconditioner + dots,
+        bit 1 direction formed by its readers, bit 2 Ap fused into the gather,
+        bit 3 the predicted guess's field beside the permanent field)."""
         self._check(self.lib.t9gb_set_pcg_fusion(self.h, int(mask)))
 
     def use_graph(self, enable=True):

@@ -248,7 +248,7 @@ struct Context {
    int* nbr_over = nullptr;  // device max count seen (overflow check)
    int* h_over = nullptr;    // pinned mirror
    int pair_lanes = 8;            // lanes per atom in the field kernels
-   int pcg_fuse = 1;              // t9gb_set_pcg_fusion
+   int pcg_fuse = 9;              // t9gb_set_pcg_fusion
    int force_lanes = 4;           // lanes per atom in the real-space force kernel
    bool list_stale = true;        // positions changed since the last list check
    bool list_need_build = true;   // no valid list for the current order / capacity
@@ -317,7 +317,7 @@ struct Context {
 
    // whole-induce CUDA graph
    bool use_graph = true;
-   cudaGraphExec_t graph_exec[3] = {nullptr, nullptr, nullptr};  // per start variant (pcg.cu)
+   cudaGraphExec_t graph_exec[4] = {nullptr, nullptr, nullptr, nullptr};  // per start variant (pcg.cu)
    cudaStream_t cap_stream = nullptr;
    // t9gb_induce_host: enqueue the caller-order dipole copy before the
    // solve's one synchronisation
@@ -436,6 +436,9 @@ int launch_ufield_real_dir(Context* ctx, const float* p6, const float* z6, const
 int launch_ufield_recip_grid_dir(Context* ctx, const float* p6, const float* z6, const double* scal);
 int launch_ufield_recip_gather_ap(Context* ctx, float* out6, const PcgAp& P);
 int launch_ufield_recip_gather_dir(Context* ctx, float* out6, const PcgAp& P);
+// the same on the second grid (and FFT plan)
+int launch_ufield_recip_grid_alt(Context* ctx, const float* u6);
+int launch_ufield_recip_gather_alt(Context* ctx, const float* u6, float* out6);
 int scatter_positions(Context* ctx);
 // t9gb_emplar(grad) with `beside` called once the dipoles are solved and the
 // list is current, before the electrostatic forces are launched

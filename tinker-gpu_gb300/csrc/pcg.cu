@@ -53,7 +53,7 @@ struct VecArgs {
 // alpha E (pcgguess) or zero
 __global__ void k_init_guess(VecArgs A, const float* __restrict__ fld, float* __restrict__ efield,
    float* __restrict__ udir, float* __restrict__ uind, int pcgguess, int predictor, const float* __restrict__ hist,
-   const int* __restrict__ state)
+   const int* __restrict__ state, int set_uind)
 {
    const int nualt = state[ST_NUALT];
    const int depth = predictor == 1 ? 16 : predictor == 2 ? 6 : 0;
@@ -79,6 +79,34 @@ __global__ void k_init_guess(VecArgs A, const float* __restrict__ fld, float* __
          u = (float)v;
       } else if (pcgguess) {
          u = ud;
+      }
+      if (set_uind)
+         uind[x] = u;
+   }
+}
+
+// the predictor's guess alone (zero while its ring is not full), before the
+// permanent field is known: the same extrapolation as k_init_guess
+__global__ void k_predict(VecArgs A, int predictor, const float* __restrict__ hist, const int* __restrict__ state,
+   float* __restrict__ uind)
+{
+   const int nualt = state[ST_NUALT];
+   const int depth = predictor == 1 ? 16 : predictor == 2 ? 6 : 0;
+   const bool predict = depth > 0 && nualt >= depth;
+   double coef[16];
+   if (predict)
+      for (int k = 0; k < depth; ++k) {
+         const int j = ((nualt - 1 - k) % depth + depth) % depth;
+         coef[k] = predictor == 1 ? c_aspc[j] : c_gear[j];
+      }
+   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.ne; e += gridDim.x * blockDim.x) {
+      const int s = e / 6, x = e + 2 * s;  // row s, component e - 6 s of [npad][8]
+      float u = 0.f;
+      if (predict) {
+         double v = 0;
+         for (int k = 0; k < depth; ++k)
+            v += coef[k] * (double)hist[(size_t)k * A.ne8 + x];
+         u = (float)v;
       }
       uind[x] = u;
    }
@@ -513,16 +541,58 @@ static int pcg_body(Context* ctx, const VecArgs& A, cudaGraphConditionalHandle h
 
 // start variants: the plain guess (ASPC / alpha E / zero), the learned guess
 // for both systems, or both with the per-system residual comparison
-enum { V_PLAIN = 0, V_LEARNED = 1, V_COMPARE = 2 };
+// V_PREDICT: the plain start with the predictor's ring full, the field of
+// the extrapolated guess computed beside the permanent field
+enum { V_PLAIN = 0, V_LEARNED = 1, V_COMPARE = 2, V_PREDICT = 3 };
+
+// V_PREDICT: the guess does not depend on this step's permanent field, so
+// its mutual field (real space on side stream 2, the reciprocal grid on side
+// stream 3 and the second grid, the gather back on stream 2) runs beside the
+// permanent field (main and side stream 0); the same kernels and sums as the
+// plain start, so the same bits
+static int pcg_start_predict(Context* ctx, const VecArgs& A, bool graph)
+{
+   const t9gb_config& c = ctx->cfg;
+   T9_CHECK(graph ? list_refresh_graph(ctx) : ensure_list(ctx));
+   k_predict<<<A.nb, VB, 0, ctx->stream>>>(A, c.predictor, ctx->aspc_hist, ctx->status, ctx->uind);
+   T9_CUDA(cudaGetLastError());
+   T9_CHECK(recip_fork(ctx, 2));
+   T9_CHECK(recip_fork(ctx, 3));
+   cudaStream_t main = ctx->stream;
+   ctx->stream = ctx->side_stream[3];
+   int rc = launch_ufield_recip_grid_alt(ctx, ctx->uind);
+   if (rc == T9GB_OK) {
+      ctx->stream = ctx->side_stream[2];
+      rc = launch_ufield_real(ctx, ctx->uind, nullptr, ctx->tmp6);
+   }
+   if (rc == T9GB_OK && cudaEventRecord(ctx->ev_join[3], ctx->side_stream[3]) == cudaSuccess &&
+      cudaStreamWaitEvent(ctx->side_stream[2], ctx->ev_join[3], 0) == cudaSuccess)
+      rc = launch_ufield_recip_gather_alt(ctx, ctx->uind, ctx->tmp6);
+   else if (rc == T9GB_OK)
+      rc = T9GB_CUDA_ERR;
+   ctx->stream = main;
+   T9_CHECK(rc);
+   T9_CHECK(dfield6(ctx, ctx->fld6));
+   T9_CHECK(recip_join(ctx, 2));
+   k_init_guess<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->fld6, ctx->efield, ctx->udir, ctx->uind, c.pcgguess,
+      c.predictor, ctx->aspc_hist, ctx->status, 0);
+   if (ctx->learn_mode & 1)
+      T9_CHECK(learn_forward(ctx));
+   k_init_rsd<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->tmp6, ctx->efield, ctx->udir, ctx->uind, ctx->rsd, 0);
+   T9_CUDA(cudaGetLastError());
+   return precond_dots(ctx, A, 1, 0, 0);
+}
 
 // neighbour list, permanent field, guess, r0, M r0 and s = r.z
 static int pcg_start(Context* ctx, const VecArgs& A, bool graph, int variant)
 {
    const t9gb_config& c = ctx->cfg;
+   if (variant == V_PREDICT)
+      return pcg_start_predict(ctx, A, graph);
    T9_CHECK(graph ? list_refresh_graph(ctx) : ensure_list(ctx));
    T9_CHECK(dfield6(ctx, ctx->fld6));
    k_init_guess<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->fld6, ctx->efield, ctx->udir, ctx->uind, c.pcgguess,
-      c.predictor, ctx->aspc_hist, ctx->status);
+      c.predictor, ctx->aspc_hist, ctx->status, 1);
    // the network runs when its guess is used or when this solve trains it
    if ((ctx->learn_mode & 1) || variant != V_PLAIN)
       T9_CHECK(learn_forward(ctx));
@@ -680,7 +750,7 @@ void drop_graphs(Context* ctx)
 // host policy for the start variant: compare both starts every learn_probe
 // solves (and when the predictor history has just filled); in between start
 // from what the last comparison chose for both systems
-static int pick_variant(Context* ctx)
+static int pick_variant_learn(Context* ctx)
 {
    if (!(ctx->learn_mode & 2))
       return V_PLAIN;
@@ -691,6 +761,17 @@ static int pick_variant(Context* ctx)
    if (ctx->learn_last_choice == 0)
       return V_PLAIN;
    return V_COMPARE;
+}
+
+// the plain start with the predictor's ring full (as of the last solve)
+// overlaps the guess's field with the permanent field (PME, the second grid)
+static int pick_variant(Context* ctx)
+{
+   const int v = pick_variant_learn(ctx);
+   if (v == V_PLAIN && ctx->learn_ring_full && pred_depth(ctx->cfg) > 0 && ctx->cfg.use_ewald && !ctx->prof.on &&
+      (ctx->pcg_fuse & 8) && ctx->pme.qgrid2 != nullptr && ctx->side_stream[3] != nullptr)
+      return V_PREDICT;
+   return v;
 }
 
 int induce_sorted(Context* ctx)
@@ -749,6 +830,7 @@ int induce_sorted(Context* ctx)
 
 int reset_predictor(Context* ctx)
 {
+   ctx->learn_ring_full = false;
    T9_CUDA(cudaMemsetAsync(ctx->status + ST_NUALT, 0, sizeof(int), ctx->stream));
    return T9GB_OK;
 }

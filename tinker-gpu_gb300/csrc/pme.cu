@@ -1486,6 +1486,29 @@ int launch_ufield_recip(Context* ctx, const float* u6, float* out6)
    return launch_ufield_recip_gather(ctx, u6, out6, false);
 }
 
+static void swap_grids(PmeGrid& P)
+{
+   std::swap(P.qfx, P.qfx2);
+   std::swap(P.qgrid, P.qgrid2);
+   std::swap(P.plan, P.plan2);
+}
+
+int launch_ufield_recip_grid_alt(Context* ctx, const float* u6)
+{
+   swap_grids(ctx->pme);
+   const int rc = launch_ufield_recip_grid(ctx, u6);
+   swap_grids(ctx->pme);
+   return rc;
+}
+
+int launch_ufield_recip_gather_alt(Context* ctx, const float* u6, float* out6)
+{
+   swap_grids(ctx->pme);
+   const int rc = launch_ufield_recip_gather(ctx, u6, out6, true);
+   swap_grids(ctx->pme);
+   return rc;
+}
+
 // the CG search direction's grid: p = z + b p_old formed by the spread
 int launch_ufield_recip_grid_dir(Context* ctx, const float* p6, const float* z6, const double* scal)
 {
