@@ -223,3 +223,25 @@ def test_dipole_grid_range_fallback(gpu_lib, tg):
     # the widened context keeps solving
     ud, _, _ = e.induce()
     assert np.isfinite(cpu(ud)).all()
+
+
+def test_predicted_start_overlap_is_bit_identical(gpu_lib, tg):
+    """With the predictor's ring full the guess's field runs beside the
+    permanent field (fusion bit 3): the same kernels and sums, so the same
+    bits as the start in order; a reset of the predictor (a new neighbour
+    order) falls back to the plain start and refills the ring."""
+    s = tg.systems.make_config("water648")
+    tr = tg.systems.Trajectory(s)
+    a = engine_for(s, predictor=1)
+    b = engine_for(s, predictor=1)
+    b.pcg_fusion(1)
+    for step in range(40):
+        x = tr.frame(step)
+        if step == 24:
+            for e in (a, b):
+                e.set_xyz(x)
+                e.nblist_build()  # new spatial order: the predictor starts over
+        ua, pa, _ = a.induce_host(x)
+        ub, pb, _ = b.induce_host(x)
+        assert a.stats()[0] == b.stats()[0], step
+        assert np.array_equal(ua, ub) and np.array_equal(pa, pb), step
