@@ -548,23 +548,34 @@ enum { V_PLAIN = 0, V_LEARNED = 1, V_COMPARE = 2, V_PREDICT = 3 };
 // V_PREDICT: the guess does not depend on this step's permanent field, so
 // its mutual field (real space on side stream 2, the reciprocal grid on side
 // stream 3 and the second grid, the gather back on stream 2) runs beside the
-// permanent field (main and side stream 0); the same kernels and sums as the
-// plain start, so the same bits
+// permanent field (main and side stream 0), and both reciprocal grids beside
+// the neighbour-list refresh; the same kernels and sums as the plain start,
+// so the same bits
 static int pcg_start_predict(Context* ctx, const VecArgs& A, bool graph)
 {
    const t9gb_config& c = ctx->cfg;
-   T9_CHECK(graph ? list_refresh_graph(ctx) : ensure_list(ctx));
    k_predict<<<A.nb, VB, 0, ctx->stream>>>(A, c.predictor, ctx->aspc_hist, ctx->status, ctx->uind);
    T9_CUDA(cudaGetLastError());
-   T9_CHECK(recip_fork(ctx, 2));
+   // the two reciprocal grids need no neighbour list: they start first and
+   // run beside the list refresh (side 0: the permanent grid; side 3: the
+   // guess's grid on the second grid pair)
+   T9_CHECK(recip_fork(ctx, 0));
    T9_CHECK(recip_fork(ctx, 3));
    cudaStream_t main = ctx->stream;
-   ctx->stream = ctx->side_stream[3];
-   int rc = launch_ufield_recip_grid_alt(ctx, ctx->uind);
+   ctx->stream = ctx->side_stream[0];
+   int rc = launch_dfield_recip_grid(ctx);
    if (rc == T9GB_OK) {
-      ctx->stream = ctx->side_stream[2];
-      rc = launch_ufield_real(ctx, ctx->uind, nullptr, ctx->tmp6);
+      ctx->stream = ctx->side_stream[3];
+      rc = launch_ufield_recip_grid_alt(ctx, ctx->uind);
    }
+   ctx->stream = main;
+   T9_CHECK(rc);
+   T9_CHECK(graph ? list_refresh_graph(ctx) : ensure_list(ctx));
+   // the real-space fields: the guess's on side 2 (then its gather, after the
+   // grid), the permanent one here (then its gather)
+   T9_CHECK(recip_fork(ctx, 2));
+   ctx->stream = ctx->side_stream[2];
+   rc = launch_ufield_real(ctx, ctx->uind, nullptr, ctx->tmp6);
    if (rc == T9GB_OK && cudaEventRecord(ctx->ev_join[3], ctx->side_stream[3]) == cudaSuccess &&
       cudaStreamWaitEvent(ctx->side_stream[2], ctx->ev_join[3], 0) == cudaSuccess)
       rc = launch_ufield_recip_gather_alt(ctx, ctx->uind, ctx->tmp6);
@@ -572,7 +583,9 @@ static int pcg_start_predict(Context* ctx, const VecArgs& A, bool graph)
       rc = T9GB_CUDA_ERR;
    ctx->stream = main;
    T9_CHECK(rc);
-   T9_CHECK(dfield6(ctx, ctx->fld6));
+   T9_CHECK(launch_dfield_real(ctx, nullptr, ctx->fld6));
+   T9_CHECK(recip_join(ctx, 0));
+   T9_CHECK(launch_dfield_recip_gather(ctx, ctx->fld6, true));
    T9_CHECK(recip_join(ctx, 2));
    k_init_guess<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->fld6, ctx->efield, ctx->udir, ctx->uind, c.pcgguess,
       c.predictor, ctx->aspc_hist, ctx->status, 0);
@@ -589,8 +602,22 @@ static int pcg_start(Context* ctx, const VecArgs& A, bool graph, int variant)
    const t9gb_config& c = ctx->cfg;
    if (variant == V_PREDICT)
       return pcg_start_predict(ctx, A, graph);
-   T9_CHECK(graph ? list_refresh_graph(ctx) : ensure_list(ctx));
-   T9_CHECK(dfield6(ctx, ctx->fld6));
+   if (c.use_ewald && !ctx->prof.on) {
+      // the permanent grid needs no neighbour list: it runs beside the refresh
+      T9_CHECK(recip_fork(ctx, 0));
+      cudaStream_t main = ctx->stream;
+      ctx->stream = ctx->side_stream[0];
+      const int rc = launch_dfield_recip_grid(ctx);
+      ctx->stream = main;
+      T9_CHECK(rc);
+      T9_CHECK(graph ? list_refresh_graph(ctx) : ensure_list(ctx));
+      T9_CHECK(launch_dfield_real(ctx, nullptr, ctx->fld6));
+      T9_CHECK(recip_join(ctx, 0));
+      T9_CHECK(launch_dfield_recip_gather(ctx, ctx->fld6, true));
+   } else {
+      T9_CHECK(graph ? list_refresh_graph(ctx) : ensure_list(ctx));
+      T9_CHECK(dfield6(ctx, ctx->fld6));
+   }
    k_init_guess<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->fld6, ctx->efield, ctx->udir, ctx->uind, c.pcgguess,
       c.predictor, ctx->aspc_hist, ctx->status, 1);
    // the network runs when its guess is used or when this solve trains it
