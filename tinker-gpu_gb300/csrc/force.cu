@@ -326,17 +326,6 @@ __device__ __forceinline__ void elec_pair(const PairParams& P, float3 Rv, float 
    }
 }
 
-template <int G, int N>
-__device__ __forceinline__ void group_reduce_d(double* v)
-{
-#pragma unroll
-   for (int c = 0; c < N; ++c) {
-#pragma unroll
-      for (int o = G / 2; o > 0; o >>= 1)
-         v[c] += __shfl_xor_sync(0xffffffffu, v[c], o);
-   }
-}
-
 // Real-space forces and torque fields, G lanes per atom i over the list and
 // the scaled partners.  f: electric; outputs per slot: force [npad][3],
 // torque field [npad][10], empole real energy (MPOLE).
@@ -402,7 +391,9 @@ __global__ void __launch_bounds__(128) k_elec_real(PairParams P, int npad, float
          }
       }
    }
-   double acc[14];
+   // the lane partials are FP32: their group sum stays FP32 (this GPU's FP64
+   // pipe is far narrower), the outputs are scaled from it
+   float acc[14];
    acc[0] = o.e;
    acc[1] = o.f[0];
    acc[2] = o.f[1];
@@ -410,27 +401,27 @@ __global__ void __launch_bounds__(128) k_elec_real(PairParams P, int npad, float
 #pragma unroll
    for (int c = 0; c < 10; ++c)
       acc[4 + c] = o.t[c];
-   group_reduce_d<G, 14>(acc);
-   double wv[9];
+   group_reduce<G, 14>(acc);
+   float wv[9];
    if (VIR) {
 #pragma unroll
       for (int c = 0; c < 9; ++c)
          wv[c] = o.w[c];
-      group_reduce_d<G, 9>(wv);
+      group_reduce<G, 9>(wv);
    }
    if (g == 0) {
       if (VIR)
 #pragma unroll
          for (int c = 0; c < 9; ++c)
-            wout[c * npad + i] = (float)(f * wv[c]);
+            wout[c * npad + i] = f * wv[c];
       if (MPOLE && e_atom)
-         e_atom[i] = 0.5 * f * acc[0];
+         e_atom[i] = 0.5 * (double)f * (double)acc[0];
 #pragma unroll
       for (int c = 0; c < 3; ++c)
-         fout[3 * i + c] = (float)(f * acc[1 + c]);
+         fout[3 * i + c] = f * acc[1 + c];
 #pragma unroll
       for (int c = 0; c < 10; ++c)
-         tout[10 * i + c] = (float)(f * acc[4 + c]);
+         tout[10 * i + c] = f * acc[4 + c];
    }
 }
 

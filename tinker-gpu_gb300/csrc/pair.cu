@@ -436,7 +436,7 @@ __global__ void __launch_bounds__(256, 4) k_precond_sparse_dots(PairParams P, in
    __shared__ double sh[64];
    constexpr int PER = 256 / G;
    const int g = threadIdx.x % G;
-   double rz_d = 0, rz_p = 0, rr_d = 0, rr_p = 0;
+   float rz_d = 0.f, rz_p = 0.f, rr_d = 0.f, rr_p = 0.f;
    for (int i = blockIdx.x * PER + threadIdx.x / G; i < npad; i += gridDim.x * PER) {
       float f[6];
       precond_row<G>(P, i, g, f, nbr, nnbr, sp_start, sp_j, sp_sc, spos, r8);
@@ -451,17 +451,17 @@ __global__ void __launch_bounds__(256, 4) k_precond_sparse_dots(PairParams P, in
             if (D.init)
                D.conj[8 * i + c] = z;
             if (c < 3) {
-               rz_d += (double)r * z;
-               rr_d += (double)r * r;
+               rz_d += r * z;
+               rr_d += r * r;
             } else {
-               rz_p += (double)r * z;
-               rr_p += (double)r * r;
+               rz_p += r * z;
+               rr_p += r * r;
             }
          }
       }
    }
-   const double pv[4] = {rz_d, rz_p, rr_d, rr_p};
-   store_partials<4>(D.red, R_RZ_D, pv, sh);
+   const float pv[4] = {rz_d, rz_p, rr_d, rr_p};
+   store_partials_f<4>(D.red, R_RZ_D, pv, sh);
    if (!last_block(D.state + ST_TICKET0))
       return;
    double tot[4];

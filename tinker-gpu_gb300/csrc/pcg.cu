@@ -58,11 +58,11 @@ __global__ void k_init_guess(VecArgs A, const float* __restrict__ fld, float* __
    const int nualt = state[ST_NUALT];
    const int depth = predictor == 1 ? 16 : predictor == 2 ? 6 : 0;
    const bool predict = depth > 0 && nualt >= depth;
-   double coef[16];
+   float coef[16];
    if (predict)
       for (int k = 0; k < depth; ++k) {
          const int j = ((nualt - 1 - k) % depth + depth) % depth;
-         coef[k] = predictor == 1 ? c_aspc[j] : c_gear[j];
+         coef[k] = (float)(predictor == 1 ? c_aspc[j] : c_gear[j]);
       }
    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.ne; e += gridDim.x * blockDim.x) {
       const int s = e / 6, x = e + 2 * s;  // row s, component e - 6 s of [npad][8]
@@ -73,10 +73,11 @@ __global__ void k_init_guess(VecArgs A, const float* __restrict__ fld, float* __
       udir[x] = ud;
       float u = 0.f;
       if (predict) {
-         double v = 0;
+         // FP32: the extrapolation's rounding is far below its own error
+         float v = 0.f;
          for (int k = 0; k < depth; ++k)
-            v += coef[k] * (double)hist[(size_t)k * A.ne8 + x];
-         u = (float)v;
+            v = __fmaf_rn(coef[k], hist[(size_t)k * A.ne8 + x], v);
+         u = v;
       } else if (pcgguess) {
          u = ud;
       }
@@ -93,20 +94,21 @@ __global__ void k_predict(VecArgs A, int predictor, const float* __restrict__ hi
    const int nualt = state[ST_NUALT];
    const int depth = predictor == 1 ? 16 : predictor == 2 ? 6 : 0;
    const bool predict = depth > 0 && nualt >= depth;
-   double coef[16];
+   float coef[16];
    if (predict)
       for (int k = 0; k < depth; ++k) {
          const int j = ((nualt - 1 - k) % depth + depth) % depth;
-         coef[k] = predictor == 1 ? c_aspc[j] : c_gear[j];
+         coef[k] = (float)(predictor == 1 ? c_aspc[j] : c_gear[j]);
       }
    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.ne; e += gridDim.x * blockDim.x) {
       const int s = e / 6, x = e + 2 * s;  // row s, component e - 6 s of [npad][8]
       float u = 0.f;
       if (predict) {
-         double v = 0;
+         // FP32: the extrapolation's rounding is far below its own error
+         float v = 0.f;
          for (int k = 0; k < depth; ++k)
-            v += coef[k] * (double)hist[(size_t)k * A.ne8 + x];
-         u = (float)v;
+            v = __fmaf_rn(coef[k], hist[(size_t)k * A.ne8 + x], v);
+         u = v;
       }
       uind[x] = u;
    }
@@ -134,7 +136,7 @@ __global__ void k_precond_dot(VecArgs A, const float* __restrict__ rsd, float* _
    int n, double debye, double poleps, int politer, int miniter, cudaGraphConditionalHandle handle, int use_handle)
 {
    __shared__ double sh[64];
-   double rz_d = 0, rz_p = 0, rr_d = 0, rr_p = 0;
+   float rz_d = 0.f, rz_p = 0.f, rr_d = 0.f, rr_p = 0.f;
    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.ne; e += gridDim.x * blockDim.x) {
       const int s = e / 6, x = e + 2 * s;  // row s, component e - 6 s of [npad][8]
       const float r = rsd[x];
@@ -148,15 +150,15 @@ __global__ void k_precond_dot(VecArgs A, const float* __restrict__ rsd, float* _
       if (init)
          conj[x] = z;
       if (e - 6 * s < 3) {
-         rz_d += (double)r * z;
-         rr_d += (double)r * r;
+         rz_d += r * z;
+         rr_d += r * r;
       } else {
-         rz_p += (double)r * z;
-         rr_p += (double)r * r;
+         rz_p += r * z;
+         rr_p += r * r;
       }
    }
-   const double pv[4] = {rz_d, rz_p, rr_d, rr_p};
-   store_partials<4>(red, R_RZ_D, pv, sh);
+   const float pv[4] = {rz_d, rz_p, rr_d, rr_p};
+   store_partials_f<4>(red, R_RZ_D, pv, sh);
    if (!last_block(state + ST_TICKET0))
       return;
    double tot[4];
@@ -176,7 +178,7 @@ __global__ void k_pcg_p1(VecArgs A, const float* __restrict__ fld, float* __rest
    int* __restrict__ state)
 {
    __shared__ double sh[64];
-   double dd = 0, dp = 0;
+   float dd = 0.f, dp = 0.f;
    float bd = 0.f, bp = 0.f;
    if (DIR) {
       bd = (float)scal[S_B_D];
@@ -192,12 +194,12 @@ __global__ void k_pcg_p1(VecArgs A, const float* __restrict__ fld, float* __rest
       const float v = A.polinv[s] * p - fld[x];
       vec[x] = v;
       if (e - 6 * s < 3)
-         dd += (double)p * v;
+         dd += p * v;
       else
-         dp += (double)p * v;
+         dp += p * v;
    }
-   const double pv[2] = {dd, dp};
-   store_partials<2>(red, R_PAP_D, pv, sh);
+   const float pv[2] = {dd, dp};
+   store_partials_f<2>(red, R_PAP_D, pv, sh);
    if (!last_block(state + ST_TICKET1))
       return;
    double tot[2];

@@ -310,7 +310,7 @@ __global__ void k_conv(size_t ng, const float* __restrict__ infl, float2* __rest
 template <int MODE, bool ACC, bool AP, bool DIR>
 __device__ __forceinline__ void gather_atom(int s, int lane, const GridParams& G, const float4* __restrict__ spos,
    const float2* __restrict__ g, const float* __restrict__ rp, const float* __restrict__ u8, float* __restrict__ out,
-   const PcgAp& P, float bd, float bp, double* pap)
+   const PcgAp& P, float bd, float bp, float* pap)
 {
    int i1, i2, i3;
    float w1, w2, w3;
@@ -371,7 +371,7 @@ __device__ __forceinline__ void gather_atom(int s, int lane, const GridParams& G
          const float v = P.polinv[s] * p - fld;
          P.vec[x] = v;
          P.conj[x] = p;
-         pap[c < 3 ? 0 : 1] += (double)p * v;
+         pap[c < 3 ? 0 : 1] += p * v;
       }
       return;
    }
@@ -425,11 +425,11 @@ __global__ void __launch_bounds__(256, 6) k_gather_field(int n, GridParams G, co
    }
    __shared__ double sh[64];
    const float bd = (float)P.scal[S_B_D], bp = (float)P.scal[S_B_P];
-   double pap[2] = {0, 0};
+   float pap[2] = {0.f, 0.f};
    const int nw = (gridDim.x * blockDim.x) >> 5;
    for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < n; s += nw)
       gather_atom<MODE, ACC, true, false>(s, lane, G, spos, g, rp, u8, out, P, bd, bp, pap);
-   store_partials<2>(P.red, R_PAP_D, pap, sh);
+   store_partials_f<2>(P.red, R_PAP_D, pap, sh);
    if (!last_block(P.state + ST_TICKET1))
       return;
    double tot[2];
@@ -1084,19 +1084,22 @@ __global__ void __launch_bounds__(256) k_gather_force_perm(int n, int npad, Grid
       #pragma unroll
       for (int c = 0; c < 10; ++c)
          T[c] = f * phi[c];
-      double e = (double)m[0] * phi[0] + (double)m[1] * phi[1] + (double)m[2] * phi[2] + (double)m[3] * phi[3];
-      e += (double)m[4] * phi[4] + (double)m[5] * phi[5] + (double)m[6] * phi[6];
-      e += 2.0 * ((double)m[7] * phi[7] + (double)m[8] * phi[8] + (double)m[9] * phi[9]);
-      if (e_atom)
-         e_atom[s] = 0.5 * f * e;
+      // per-atom energies in FP32 (this GPU's FP64 pipe issues a warp
+      // instruction in tens of cycles even for one lane); the totals are
+      // FP64 sums of these
+      if (e_atom) {
+         float e = m[0] * phi[0] + m[1] * phi[1] + m[2] * phi[2] + m[3] * phi[3];
+         e += m[4] * phi[4] + m[5] * phi[5] + m[6] * phi[6];
+         e += 2.f * (m[7] * phi[7] + m[8] * phi[8] + m[9] * phi[9]);
+         e_atom[s] = (double)(0.5f * f * e);
+      }
       if (e_self) {
-         const double a2 = 2.0 * aewald * aewald;
-         const double fterm = -(double)f * aewald / 1.77245385090551602730;
-         const double cii = (double)m[0] * m[0];
-         const double dii = (double)m[1] * m[1] + (double)m[2] * m[2] + (double)m[3] * m[3];
-         const double qii = 2.0 * ((double)m[7] * m[7] + (double)m[8] * m[8] + (double)m[9] * m[9])
-            + (double)m[4] * m[4] + (double)m[5] * m[5] + (double)m[6] * m[6];
-         e_self[s] = fterm * (cii + a2 * (dii / 3.0 + 2.0 * a2 * qii * 0.2));
+         const float a2 = 2.f * aewald * aewald;
+         const float fterm = -f * aewald * 0.56418958354775628f;  // 1/sqrt(pi)
+         const float cii = m[0] * m[0];
+         const float dii = m[1] * m[1] + m[2] * m[2] + m[3] * m[3];
+         const float qii = 2.f * (m[7] * m[7] + m[8] * m[8] + m[9] * m[9]) + m[4] * m[4] + m[5] * m[5] + m[6] * m[6];
+         e_self[s] = (double)(fterm * (cii + a2 * (dii * (1.f / 3.f) + 0.4f * a2 * qii)));
       }
    }
    float us[3] = {0.f, 0.f, 0.f};

@@ -117,6 +117,38 @@ static __device__ __forceinline__ void store_partials(double* red, int first, co
    __syncthreads();
 }
 
+// store_partials for per-thread FP32 partials: the warp trees in FP32 (the
+// FP64 pipe of this GPU issues a warp instruction in tens of cycles, so the
+// per-thread and per-warp sums avoid it), the block's eight warp sums and
+// everything after them in FP64; the same fixed order, so deterministic
+template <int N>
+static __device__ __forceinline__ void store_partials_f(double* red, int first, const float* v, double* sh)
+{
+   float x[N];
+#pragma unroll
+   for (int c = 0; c < N; ++c)
+      x[c] = v[c];
+#pragma unroll
+   for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+      for (int c = 0; c < N; ++c)
+         x[c] += __shfl_down_sync(0xffffffffu, x[c], o);
+   const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+   if (l == 0)
+#pragma unroll
+      for (int c = 0; c < N; ++c)
+         sh[c * 8 + w] = (double)x[c];
+   __syncthreads();
+   if (threadIdx.x < N) {
+      // one thread per value: the warp sums in order
+      double r = 0.0;
+      for (int k = 0; k < nw; ++k)
+         r += sh[threadIdx.x * 8 + k];
+      red[(first + threadIdx.x) * RED_MAX + blockIdx.x] = r;
+   }
+   __syncthreads();
+}
+
 // true in the block that finishes last (threadfence + ticket); it resets the
 // ticket for the next launch
 static __device__ __forceinline__ bool last_block(int* ticket)
