@@ -627,9 +627,9 @@ __global__ void k_force_combine(int n, const int* __restrict__ iperm, const floa
 {
    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < n; a += gridDim.x * blockDim.x) {
       const int s = iperm[a];
-      double F[3];
+      float F[3];  // FP32, like the gradient it becomes
       for (int c = 0; c < 3; ++c)
-         F[c] = (double)f0[3 * s + c] + (f1 ? f1[3 * s + c] : 0.f) + (f2 ? f2[3 * s + c] : 0.f);
+         F[c] = f0[3 * s + c] + (f1 ? f1[3 * s + c] : 0.f) + (f2 ? f2[3 * s + c] : 0.f);
       for (int e = rev_start[s]; e < rev_start[s + 1]; ++e) {
          const int ent = rev_ent[e];
          const float* fb = fbuf + 12 * (ent >> 2) + 3 * (ent & 3);
@@ -637,7 +637,7 @@ __global__ void k_force_combine(int n, const int* __restrict__ iperm, const floa
             F[c] += fb[c];
       }
       for (int c = 0; c < 3; ++c)
-         grad[3 * a + c] = (float)(-F[c]);
+         grad[3 * a + c] = -F[c];
    }
 }
 

@@ -138,13 +138,15 @@ __global__ void __launch_bounds__(256) k_ehal(PairParams P, int npad, float cut,
       for (int q = pa + g; q < pb; q += G)
          hal_add<VIR>(P, a, vpos[sp_j[q]], sp_v[q], vtab, nvt, cut, off2, off, o);
    }
-   double acc[4] = {o.e, o.g[0], o.g[1], o.g[2]};
+   // FP32 lane sums of the FP32 lane partials (this GPU's FP64 pipe is far
+   // narrower); the per-site energy is stored as FP64 for the FP64 total
+   float acc[4] = {o.e, o.g[0], o.g[1], o.g[2]};
 #pragma unroll
    for (int c = 0; c < 4; ++c)
 #pragma unroll
       for (int s = G / 2; s > 0; s >>= 1)
          acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], s);
-   double wv[9];
+   float wv[9];
    if (VIR) {
 #pragma unroll
       for (int c = 0; c < 9; ++c) {
@@ -155,14 +157,14 @@ __global__ void __launch_bounds__(256) k_ehal(PairParams P, int npad, float cut,
       }
    }
    if (g == 0) {
-      e_atom[i] = acc[0];
-      fout[3 * i] = (float)acc[1];
-      fout[3 * i + 1] = (float)acc[2];
-      fout[3 * i + 2] = (float)acc[3];
+      e_atom[i] = (double)acc[0];
+      fout[3 * i] = acc[1];
+      fout[3 * i + 1] = acc[2];
+      fout[3 * i + 2] = acc[3];
       if (VIR)
 #pragma unroll
          for (int c = 0; c < 9; ++c)
-            wout[c * npad + i] = (float)wv[c];
+            wout[c * npad + i] = wv[c];
    }
 }
 
