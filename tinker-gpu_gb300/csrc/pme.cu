@@ -834,7 +834,7 @@ __global__ void k_conv_virial(int n1, int n2, int n3, float L1, float L2, float 
    double* __restrict__ red, double* __restrict__ out, int* __restrict__ state)
 {
    __shared__ double sh[64];
-   double v[6] = {0, 0, 0, 0, 0, 0};
+   float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // FP32 per thread and warp, FP64 above
    const size_t ng = (size_t)n1 * n2 * n3;
    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < ng; i += (size_t)gridDim.x * blockDim.x) {
       const int k1 = (int)(i % n1), k2 = (int)((i / n1) % n2), k3 = (int)(i / ((size_t)n1 * n2));
@@ -851,7 +851,7 @@ __global__ void k_conv_virial(int n1, int n2, int n3, float L1, float L2, float 
       const int r3 = (k3 < (n3 + 1) / 2) ? k3 : k3 - n3;
       const float h[3] = {r1 / L1, r2 / L2, r3 / L3};
       const float hsq = h[0] * h[0] + h[1] * h[1] + h[2] * h[2];
-      // per-point terms in FP32, sums in FP64
+      // per-point terms in FP32; the block and grid sums in FP64
       float w;
       if (MODE == 1) {
          w = wE * (F.x * F.x + F.y * F.y);
@@ -866,14 +866,14 @@ __global__ void k_conv_virial(int n1, int n2, int n3, float L1, float L2, float 
       }
       w *= infl[i];
       const float wf = w * (2.f * (1.f + pterm * hsq) / hsq);
-      v[0] += (double)(wf * h[0] * h[0] - w);
-      v[1] += (double)(wf * h[1] * h[1] - w);
-      v[2] += (double)(wf * h[2] * h[2] - w);
-      v[3] += (double)(wf * h[0] * h[1]);
-      v[4] += (double)(wf * h[0] * h[2]);
-      v[5] += (double)(wf * h[1] * h[2]);
+      v[0] += wf * h[0] * h[0] - w;
+      v[1] += wf * h[1] * h[1] - w;
+      v[2] += wf * h[2] * h[2] - w;
+      v[3] += wf * h[0] * h[1];
+      v[4] += wf * h[0] * h[2];
+      v[5] += wf * h[1] * h[2];
    }
-   store_partials<6>(red, 0, v, sh);
+   store_partials_f<6>(red, 0, v, sh);
    if (!last_block(state + ST_TICKET0))
       return;
    double t[4];
