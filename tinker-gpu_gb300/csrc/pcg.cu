@@ -205,9 +205,9 @@ __global__ void k_pcg_p1(VecArgs A, const float* __restrict__ fld, float* __rest
    double tot[2];
    sum_slots(red, R_PAP_D, 2, gridDim.x, sh, tot);
    const double pap_d = tot[0], pap_p = tot[1];
-   if (threadIdx.x == 0) {
-      scal[S_A_D] = pap_d == 0 ? 0.0 : scal[S_SUM_D] / pap_d;
-      scal[S_A_P] = pap_p == 0 ? 0.0 : scal[S_SUM_P] / pap_p;
+   if (threadIdx.x == 0) {  // the step lengths in FP32 (used as FP32)
+      scal[S_A_D] = pap_d == 0 ? 0.0 : (double)((float)scal[S_SUM_D] / (float)pap_d);
+      scal[S_A_P] = pap_p == 0 ? 0.0 : (double)((float)scal[S_SUM_P] / (float)pap_p);
    }
 }
 

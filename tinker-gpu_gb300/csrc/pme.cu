@@ -434,9 +434,9 @@ __global__ void __launch_bounds__(256, 6) k_gather_field(int n, GridParams G, co
       return;
    double tot[2];
    sum_slots(P.red, R_PAP_D, 2, gridDim.x, sh, tot);
-   if (threadIdx.x == 0) {
-      P.scal[S_A_D] = tot[0] == 0 ? 0.0 : P.scal[S_SUM_D] / tot[0];
-      P.scal[S_A_P] = tot[1] == 0 ? 0.0 : P.scal[S_SUM_P] / tot[1];
+   if (threadIdx.x == 0) {  // the step lengths in FP32 (used as FP32)
+      P.scal[S_A_D] = tot[0] == 0 ? 0.0 : (double)((float)P.scal[S_SUM_D] / (float)tot[0]);
+      P.scal[S_A_P] = tot[1] == 0 ? 0.0 : (double)((float)P.scal[S_SUM_P] / (float)tot[1]);
    }
 }
 

@@ -189,12 +189,15 @@ __device__ __forceinline__ void pcg_scalars(const double* tot, double* scal, int
       state[ST_STATUS] = T9GB_OK;
       return;
    }
+   // the ratios and the norm in FP32 from the FP64 sums: the kernels use
+   // b as FP32, and an FP64 division or square root takes this GPU's FP64
+   // pipe dozens of issue slots on the solve's critical path
    const double s_d = scal[S_SUM_D], s_p = scal[S_SUM_P];
-   scal[S_B_D] = s_d == 0 ? 0.0 : s1_d / s_d;
-   scal[S_B_P] = s_p == 0 ? 0.0 : s1_p / s_p;
+   scal[S_B_D] = s_d == 0 ? 0.0 : (double)((float)s1_d / (float)s_d);
+   scal[S_B_P] = s_p == 0 ? 0.0 : (double)((float)s1_p / (float)s_p);
    scal[S_SUM_D] = s1_d;
    scal[S_SUM_P] = s1_p;
-   const double eps = debye * sqrt(fmax(q_d, q_p) / n);
+   const double eps = (double)((float)debye * sqrtf((float)fmax(q_d, q_p) / (float)n));
    const int iter = state[ST_ITER] + 1;
    state[ST_ITER] = iter;
    bool done = eps < poleps;
