@@ -57,12 +57,14 @@ __global__ void k_md_kinetic(int n, const double* __restrict__ v, const double* 
    double* __restrict__ red, double* __restrict__ out, int* __restrict__ ticket)
 {
    __shared__ double sh[64];
-   double s = 0;
+   float s = 0.f;  // FP32 per thread and warp, FP64 above
    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
       const double* w = v + 3 * i;
-      s += (w[0] * w[0] + w[1] * w[1] + w[2] * w[2]) / minv[i];
+      const float x = (float)w[0], y = (float)w[1], z = (float)w[2];
+      s += (x * x + y * y + z * z) / (float)minv[i];
    }
-   store_partial(red, 0, s, sh);
+   const float pv[1] = {s};
+   store_partials_f<1>(red, 0, pv, sh);
    if (!last_block(ticket))
       return;
    double t[1];
