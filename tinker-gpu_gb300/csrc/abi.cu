@@ -70,6 +70,7 @@ static int alloc_all(Context* ctx)
    T9_CUDA(cudaMalloc(&ctx->scal, sizeof(double) * 64));
    T9_CUDA(cudaMemset(ctx->scal, 0, sizeof(double) * 64));
    T9_CUDA(cudaMalloc(&ctx->status, sizeof(int) * 16));
+   T9_CUDA(cudaMalloc(&ctx->sum_part, sizeof(double) * SUM_ROWS_MAX * SUM_PARTS));
    T9_CUDA(cudaMemset(ctx->status, 0, sizeof(int) * 16));
    T9_CUDA(cudaMallocHost(&ctx->h_status, sizeof(int) * 16));
    T9_CUDA(cudaMallocHost(&ctx->h_scal, sizeof(double) * 64));
@@ -100,7 +101,7 @@ static void free_all(Context* ctx)
       ctx->cell_count, ctx->cell_start, ctx->cell_atoms, ctx->atom_cell, ctx->rcp6, ctx->fld6, ctx->udir,
       ctx->efield, ctx->uind, ctx->rsd, ctx->zrsd, ctx->conj, ctx->vec, ctx->tmp6, ctx->e_atom, ctx->sframe, ctx->hout,
       ctx->red, ctx->scal, ctx->status, ctx->sref, ctx->lflag,
-      ctx->aspc_hist, ctx->thl, ctx->exfld};
+      ctx->aspc_hist, ctx->thl, ctx->exfld, ctx->sum_part};
    for (void* p : dev)
       if (p)
          cudaFree(p);

@@ -305,6 +305,7 @@ struct Context {
    float* fbuf = nullptr;
    float* wvir = nullptr;  // [27][npad] virial rows: real, frame, reciprocal
    double* vsum = nullptr; // their sums
+   double* sum_part = nullptr; // [SUM_ROWS_MAX][SUM_PARTS] partials of the fixed-order row sums
    int *rev_start = nullptr, *rev_ent = nullptr;
    std::vector<int> h_frames;  // [n][4] caller order
    // start policy (host): compare the plain and the learned start every
@@ -349,6 +350,9 @@ struct Context {
 // (1 - red) of a bond from its atom: 0.09 A for AMOEBA water hydrogens).
 constexpr double VDW_SITE_MARGIN = 0.25;
 
+// energy / virial row sums: at most SUM_ROWS_MAX rows per launch, each
+// split over SUM_PARTS blocks
+constexpr int SUM_ROWS_MAX = 32, SUM_PARTS = 8;
 constexpr int RED_MAX = 2048;
 constexpr int RED_SLOTS = 8;
 

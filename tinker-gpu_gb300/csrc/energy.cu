@@ -10,45 +10,68 @@
 //    reference's calc flags (include/tool/rcman.h:105-155), forces from
 //    force.cu.
 #include "common.cuh"
+#include "reduce.cuh"
 
 namespace t9gb {
 
-// block b sums arrays[b][0..n) in a fixed order into out[b]
-__global__ void k_sum_rows(int n, int stride, const double* __restrict__ a, double* __restrict__ out)
+// Fixed-order FP64 row sums spread over SUM_PARTS blocks per row (an FP64 add
+// on this GPU issues at a small fraction of the FP32 rate, so one SM per row
+// is slow): block (p, r) sums its segment of row r into part[r][p], and the
+// last block of the launch adds each row's parts in order into out[r].
+
+template <class T>
+__global__ void __launch_bounds__(256) k_sum_rows_t(int n, int stride, const T* __restrict__ a,
+   double* __restrict__ part, double* __restrict__ out, int* __restrict__ ticket)
 {
-   __shared__ double sh[1024];
-   const double* row = a + (size_t)blockIdx.x * stride;
+   __shared__ double sh[8];
+   const int r = blockIdx.y, p = blockIdx.x;
+   const T* row = a + (size_t)r * stride;
+   const int seg = (n + SUM_PARTS - 1) / SUM_PARTS, b = p * seg, e = min(n, b + seg);
    double v = 0;
-   for (int i = threadIdx.x; i < n; i += blockDim.x)
-      v += row[i];
-   sh[threadIdx.x] = v;
+   for (int i = b + threadIdx.x; i < e; i += blockDim.x)
+      v += (double)row[i];
+#pragma unroll
+   for (int o = 16; o > 0; o >>= 1)
+      v += __shfl_down_sync(0xffffffffu, v, o);
+   if ((threadIdx.x & 31) == 0)
+      sh[threadIdx.x >> 5] = v;
    __syncthreads();
-   for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-      if (threadIdx.x < o)
-         sh[threadIdx.x] += sh[threadIdx.x + o];
-      __syncthreads();
+   if (threadIdx.x == 0) {
+      double t = 0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
+         t += sh[w];
+      part[(size_t)r * SUM_PARTS + p] = t;
+   }
+   // the last block of the launch combines every row's parts
+   __shared__ bool last;
+   __threadfence();
+   __syncthreads();
+   if (threadIdx.x == 0)
+      last = atomicAdd(reinterpret_cast<unsigned*>(ticket), 1u) == gridDim.x * gridDim.y - 1;
+   __syncthreads();
+   if (!last)
+      return;
+   __threadfence();
+   for (int rr = threadIdx.x; rr < (int)gridDim.y; rr += blockDim.x) {
+      double t = 0;
+      for (int q = 0; q < SUM_PARTS; ++q)
+         t += part[(size_t)rr * SUM_PARTS + q];
+      out[rr] = t;
    }
    if (threadIdx.x == 0)
-      out[blockIdx.x] = sh[0];
+      *ticket = 0;
 }
 
-// block b sums the float row a[b][0..n) in a fixed order (double) into out[b]
-__global__ void k_sum_rows_f(int n, int stride, const float* __restrict__ a, double* __restrict__ out)
+// out[0..rows) = the fixed-order sums of rows of n entries (stride apart)
+template <class T>
+static int sum_rows_launch(Context* ctx, int rows, int n, int stride, const T* a, double* out)
 {
-   __shared__ double sh[1024];
-   const float* row = a + (size_t)blockIdx.x * stride;
-   double v = 0;
-   for (int i = threadIdx.x; i < n; i += blockDim.x)
-      v += row[i];
-   sh[threadIdx.x] = v;
-   __syncthreads();
-   for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-      if (threadIdx.x < o)
-         sh[threadIdx.x] += sh[threadIdx.x + o];
-      __syncthreads();
-   }
-   if (threadIdx.x == 0)
-      out[blockIdx.x] = sh[0];
+   if (rows < 1 || rows > SUM_ROWS_MAX)
+      return T9GB_BAD_ARG;
+   k_sum_rows_t<T><<<dim3(SUM_PARTS, rows), 256, 0, ctx->stream>>>(n, stride, a, ctx->sum_part, out,
+      ctx->status + ST_TICKET_SUM);
+   T9_CUDA(cudaGetLastError());
+   return T9GB_OK;
 }
 
 // e[s] = -1/2 f alpha_s^-1 (u_d . udir_p)
@@ -80,8 +103,7 @@ extern "C" int t9gb_empole_energy(t9gb_context* h, double* energy, double* parts
       T9_CHECK(launch_empole_real(ctx, ctx->e_atom));
       T9_CHECK(launch_empole_recip(ctx, ctx->e_atom + ctx->npad));
       T9_CHECK(launch_extfield_mpole(ctx, false, false));
-      k_sum_rows<<<3, 1024, 0, ctx->stream>>>(ctx->npad, ctx->npad, ctx->e_atom, ctx->scal + 32);
-      T9_CUDA(cudaGetLastError());
+      T9_CHECK(sum_rows_launch(ctx, 3, ctx->npad, ctx->npad, ctx->e_atom, ctx->scal + 32));
       T9_CUDA(cudaMemcpyAsync(ctx->h_scal + 32, ctx->scal + 32, sizeof(double) * 3, cudaMemcpyDeviceToHost, ctx->stream));
       T9_CUDA(cudaStreamSynchronize(ctx->stream));
       int redo = 0;
@@ -108,8 +130,7 @@ extern "C" int t9gb_epolar_energy(t9gb_context* h, double* energy)
       return T9GB_NOT_READY;
    k_epolar_dot<<<grid_for(ctx->npad, 256), 256, 0, ctx->stream>>>(ctx->npad, ctx->cfg.electric, ctx->uind, ctx->udir,
       ctx->spolinv, ctx->e_atom);
-   k_sum_rows<<<1, 1024, 0, ctx->stream>>>(ctx->npad, ctx->npad, ctx->e_atom, ctx->scal + 36);
-   T9_CUDA(cudaGetLastError());
+   T9_CHECK(sum_rows_launch(ctx, 1, ctx->npad, ctx->npad, ctx->e_atom, ctx->scal + 36));
    T9_CUDA(cudaMemcpyAsync(ctx->h_scal + 36, ctx->scal + 36, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
    T9_CUDA(cudaStreamSynchronize(ctx->stream));
    *energy = ctx->h_scal[36];
@@ -121,8 +142,7 @@ namespace t9gb {
 // fixed-order sum of nrows FP64 rows of npad per-slot terms
 int sum_rows_d(Context* ctx, const double* rows, int nrows, double* out)
 {
-   k_sum_rows<<<nrows, 1024, 0, ctx->stream>>>(ctx->npad, ctx->npad, rows, ctx->scal + 52);
-   T9_CUDA(cudaGetLastError());
+   T9_CHECK(sum_rows_launch(ctx, nrows, ctx->npad, ctx->npad, rows, ctx->scal + 52));
    double v[8];
    T9_CUDA(cudaMemcpyAsync(v, ctx->scal + 52, sizeof(double) * nrows, cudaMemcpyDeviceToHost, ctx->stream));
    T9_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -136,8 +156,7 @@ int sum_rows_d(Context* ctx, const double* rows, int nrows, double* out)
 // nblocks blocks of 9 FP32 virial rows [9][npad], summed and symmetrised
 int sum_rows_virial(Context* ctx, const float* rows, int nblocks, double* virial)
 {
-   k_sum_rows_f<<<9 * nblocks, 1024, 0, ctx->stream>>>(ctx->npad, ctx->npad, rows, ctx->vsum);
-   T9_CUDA(cudaGetLastError());
+   T9_CHECK(sum_rows_launch(ctx, 9 * nblocks, ctx->npad, ctx->npad, rows, ctx->vsum));
    double v[27];
    T9_CUDA(cudaMemcpyAsync(v, ctx->vsum, sizeof(double) * 9 * nblocks, cudaMemcpyDeviceToHost, ctx->stream));
    T9_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -153,8 +172,7 @@ int sum_rows_virial(Context* ctx, const float* rows, int nblocks, double* virial
 
 static int sum_empole(Context* ctx, double* energy)
 {
-   k_sum_rows<<<3, 1024, 0, ctx->stream>>>(ctx->npad, ctx->npad, ctx->e_atom, ctx->scal + 32);
-   T9_CUDA(cudaGetLastError());
+   T9_CHECK(sum_rows_launch(ctx, 3, ctx->npad, ctx->npad, ctx->e_atom, ctx->scal + 32));
    T9_CUDA(cudaMemcpyAsync(ctx->h_scal + 32, ctx->scal + 32, sizeof(double) * 3, cudaMemcpyDeviceToHost, ctx->stream));
    T9_CUDA(cudaStreamSynchronize(ctx->stream));
    *energy = ctx->h_scal[32] + ctx->h_scal[33] + ctx->h_scal[34];
@@ -181,8 +199,7 @@ static int check_vers(Context* ctx, int vers, double* energy, float* grad, doubl
 // the k-space sums, symmetrised; row-major 3 x 3
 static int sum_virial(Context* ctx, double* virial)
 {
-   k_sum_rows_f<<<27, 1024, 0, ctx->stream>>>(ctx->npad, ctx->npad, ctx->wvir, ctx->vsum);
-   T9_CUDA(cudaGetLastError());
+   T9_CHECK(sum_rows_launch(ctx, 27, ctx->npad, ctx->npad, ctx->wvir, ctx->vsum));
    double v[27], k[12];
    T9_CUDA(cudaMemcpyAsync(v, ctx->vsum, sizeof(double) * 27, cudaMemcpyDeviceToHost, ctx->stream));
    T9_CUDA(cudaMemcpyAsync(k, ctx->scal + 40, sizeof(double) * 12, cudaMemcpyDeviceToHost, ctx->stream));
@@ -255,8 +272,7 @@ static int elec_terms(Context* ctx, bool mpole, bool polar, int vers, double* en
       if (polar) {
          k_epolar_dot<<<grid_for(ctx->npad, 256), 256, 0, ctx->stream>>>(ctx->npad, ctx->cfg.electric, ctx->uind,
             ctx->udir, ctx->spolinv, ctx->e_atom);
-         k_sum_rows<<<1, 1024, 0, ctx->stream>>>(ctx->npad, ctx->npad, ctx->e_atom, ctx->scal + 36);
-         T9_CUDA(cudaGetLastError());
+         T9_CHECK(sum_rows_launch(ctx, 1, ctx->npad, ctx->npad, ctx->e_atom, ctx->scal + 36));
          T9_CUDA(cudaMemcpyAsync(ctx->h_scal + 36, ctx->scal + 36, sizeof(double), cudaMemcpyDeviceToHost,
             ctx->stream));
          T9_CUDA(cudaStreamSynchronize(ctx->stream));
