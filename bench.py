@@ -173,6 +173,23 @@ def algorithmic_bytes(kernel, n, entries, nfft):
     return n * 16
 
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of a
+# kernel group, from one `ncu --set full --clock-control none` capture on
+# GB300 of `bench.py --steps 3 --warmup 3 --no-learned --no-large
+# --no-cpu-baseline --no-flush --no-md` (water12288, fused 64^3 transform):
+# the dipole transform + convolution is k_fft_plane<64,1,0> 2,112,000 +
+# k_fft_zline<64,2> 3,158,528 + k_fft_plane<64,0,1> 2,109,952 bytes read
+# and no DRAM writes (the 2 MB grid's writes stay in L2 within a launch).
+# Keyed by (kernel, workload, transform); null elsewhere.
+MEASURED_TRAFFIC = {("fft_conv", "water12288", "own"): 7380480}
+
+
+def measured_traffic(kernel, workload, fft):
+    path = "own" if fft in ("auto", "own") else fft
+    v = MEASURED_TRAFFIC.get((kernel, workload, path))
+    return (v, "ncu capture of the same kernels on this workload") if v is not None else (None, None)
+
+
 def oracle_solves(s, tr, first, nhist, ntimed, budget_s=None):
     """FP64 oracle solves on frames first-nhist .. first+ntimed-1 of the
     trajectory: nhist untimed solves fill the 16-frame ASPC history (started
@@ -608,6 +625,7 @@ def main():
     kernels = {k: {"ms_total": v[0], "launches": v[1], "ms_per_launch": (v[0] / v[1] if v[1] else None)}
                for k, v in prof.items() if v[1]}
     dom = max(kernels, key=lambda k: kernels[k]["ms_total"])
+    traffic, traffic_src = measured_traffic(dom, args.config, args.fft)
     nfft = s.settings["nfft"][0]
     ls = eng.list_stats()
     alg = algorithmic_bytes(dom, s.n, ls["entries"], nfft)
@@ -707,8 +725,8 @@ def main():
             "e2e": {"value": e2e_value, "unit": "induce() calls/s", "ms_per_step": 1000 * e2e_sec / args.steps,
                     "h2d_bytes_per_step": 3 * s.n * 4, "d2h_bytes_per_step": 6 * s.n * 4},
             "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
-                         "algorithmic_bytes_per_launch": alg},
+                         "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_src,
+                         "peak_source": peak_kind, "algorithmic_bytes_per_launch": alg},
             "kernels": kernels,
             "kernel_rooflines": kernel_rooflines(kernels, s.n, ls["entries"], nfft, peak),
             "lists": ls,
