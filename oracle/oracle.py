@@ -52,6 +52,7 @@ class OrSystem(C.Structure):
         ("ptype", C.POINTER(C.c_int)),
         ("thl", C.POINTER(C.c_double)),
         ("exfld", C.c_double * 3),
+        ("real_only", C.c_int),
     ]
 
 
@@ -137,7 +138,7 @@ def frames(system, xyz=None):
 class OracleSystem:
     """Holds the numpy buffers an or_system points at."""
 
-    def __init__(self, system, xyz=None, rpole=None, use_ewald=None, cutoff=None, nfft=None):
+    def __init__(self, system, xyz=None, rpole=None, use_ewald=None, cutoff=None, nfft=None, real_only=False):
         st = system.settings
         xyz = np.ascontiguousarray(system.xyz if xyz is None else xyz, dtype=np.float64)
         self.x, self.y, self.z = [np.ascontiguousarray(xyz[:, d]) for d in range(3)]
@@ -178,6 +179,7 @@ class OracleSystem:
             self.thl = np.ascontiguousarray(system.thole_table, dtype=np.float64)
             s.nthl = int(self.thl.shape[0])
             s.ptype, s.thl = _ip(self.ptype), _dp(self.thl)
+        s.real_only = 1 if real_only else 0
         self.s = s
         self.n = system.n
         self.settings = st

@@ -30,8 +30,10 @@
  * defines it (include/math/libfunc.h:76-77).
  *
  * Parity pins: tests/golden holds the reference's own known answers for the
- * 22-atom local-frame case (test/localframe.cpp) and vectors produced by the
- * reference's pair headers compiled from source (oracle/build_ref.sh).
+ * 22-atom local-frame case (test/localframe.cpp) and four more reference
+ * tests; oracle/ref_harness.cpp runs the reference's own pair, frame and
+ * B-spline routines compiled from its source (oracle/build_ref.py), and
+ * tests/test_oracle_reference_build.py compares this file with them.
  */
 #include <complex.h>
 #include <math.h>
@@ -69,6 +71,7 @@ typedef struct {
    const int* ptype;        /* [n] polarization type, 0..nthl-1 */
    const double* thl;       /* [nthl][nthl] */
    double exfld[3];         /* uniform external field, e/A^2 (zero: none) */
+   int real_only;           /* 1: dfield / ufield leave out the reciprocal and self terms */
 } or_system;
 
 typedef struct {
@@ -1043,7 +1046,7 @@ void or_dfield(const or_system* s, double* field, double* fieldp)
    const int n = s->n;
    memset(field, 0, sizeof(double) * 3 * n);
    memset(fieldp, 0, sizeof(double) * 3 * n);
-   if (s->use_ewald) {
+   if (s->use_ewald && !s->real_only) {
       or_pme p;
       or_pme_init(s, &p);
       double* fmp = (double*)malloc(sizeof(double) * 10 * n);
@@ -1129,7 +1132,7 @@ static void or_ufield_c(const or_system* s, or_ucache* c, const double* uind, co
    const int n = s->n;
    memset(field, 0, sizeof(double) * 3 * n);
    memset(fieldp, 0, sizeof(double) * 3 * n);
-   if (s->use_ewald) {
+   if (s->use_ewald && !s->real_only) {
       or_pme* p = &c->pme;
       double* fuind = (double*)malloc(sizeof(double) * 3 * n);
       double* fuinp = (double*)malloc(sizeof(double) * 3 * n);
