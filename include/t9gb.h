@@ -185,6 +185,12 @@ int t9gb_md_stats(t9gb_context* ctx, long long* steps, long long* pcg_iterations
 int t9gb_set_xyz_host(t9gb_context* ctx, const double* xyz);
 int t9gb_set_xyz_device(t9gb_context* ctx, const float* xyz_device);
 
+/* Coordinates from three device arrays x[n], y[n], z[n] (float), the layout
+ * of the reference's `real *x, *y, *z` (include/ff/atom.h:43-45), as
+ * copyPosToXyz leaves them (src/atom.cpp:161-166).  Ordered on the
+ * context's stream. */
+int t9gb_set_xyz_soa_device(t9gb_context* ctx, const float* x, const float* y, const float* z);
+
 /* Build the spatial (Morton) order of the atoms from the current coordinates
  * and the scaled-partner table; the exact neighbour list is then rebuilt on
  * the device whenever coordinates change.  Replaces spatialBuild /
@@ -209,6 +215,12 @@ int t9gb_ufield(t9gb_context* ctx, const float* uind_device, const float* uinp_d
 /* z = M r with the sparse preconditioner.  Replaces sparsePrecondApply
  * (src/amoeba/induce.cpp:22-26, src/cu/amoeba/precond.cu:28-43). */
 int t9gb_sparse_precond_apply(t9gb_context* ctx, const float* rsd_device, const float* rsdp_device,
+   float* zrsd_device, float* zrsdp_device);
+
+/* z = alpha r with the diagonal preconditioner, caller order, device
+ * arrays [n][3]; rsdp and zrsdp may both be NULL (one dipole set).
+ * Replaces diagPrecond (src/cu/diagprecond.cu:5-35). */
+int t9gb_diag_precond_apply(t9gb_context* ctx, const float* rsd_device, const float* rsdp_device,
    float* zrsd_device, float* zrsdp_device);
 
 /* Mutual induced dipoles by PCG.  Replaces
@@ -276,6 +288,17 @@ int t9gb_epolar(t9gb_context* ctx, int vers, double* energy, float* grad_device,
  * src/cu/amoeba/emplar.cu:505-606). */
 int t9gb_emplar(t9gb_context* ctx, int vers, double* energy, float* grad_device, double* virial);
 
+/* A gradient [n][3] (device float, kcal/mol/A, as t9gb_empole / epolar /
+ * emplar / ehal / evalence write it) into the reference's fixed-point
+ * gradient arrays gx[n], gy[n], gz[n] (device, unsigned 64-bit at 2^32 per
+ * kcal/mol/A, grad_prec under TINKER_DETERMINISTIC_FORCE,
+ * include/ff/precision.h:102-106), converted as floatTo<fixed> does
+ * (include/syntax/cu/adddef.h:36-71).  accumulate = 0 writes, 1 adds like
+ * sumGradient (src/cu/egvop.cu:6-19); grad_device = NULL with accumulate = 0
+ * clears the three arrays.  One word per thread: deterministic. */
+int t9gb_gradient_fixed(t9gb_context* ctx, const float* grad_device, int accumulate, unsigned long long* gx_device,
+   unsigned long long* gy_device, unsigned long long* gz_device);
+
 /* Components of the last energy evaluation (t9gb_empole_energy, t9gb_empole,
  * t9gb_epolar, t9gb_emplar with T9GB_CALC_ENERGY): parts[4] = multipole
  * real-space, reciprocal and self energy, polarization energy (kcal/mol),
@@ -290,13 +313,16 @@ int t9gb_energy_components(t9gb_context* ctx, double* parts);
  * pattern, pcg.cu:144-145).  Both give bit-identical dipoles. */
 int t9gb_use_graph(t9gb_context* ctx, int enable);
 
-/* PME 3-D FFT: the library's fused transform (enable = 1; power-of-two grids
- * of 16..128 points per edge: five single-axis radix-2 passes in shared
- * memory, the fixed-point conversion in the first and the influence function
- * between the z passes) or cuFFT C2C (enable = 0, the default; always used
- * for other grid sizes).  Replaces fftfront/fftback + pmeConv
- * (src/cudart/fft.cpp:65-95, src/cu/pme.cu:908-1031).  Enabling on an
- * unsupported grid returns T9GB_BAD_ARG. */
+/* PME 3-D FFT: the library's fused transform (enable = 1; cubic grids of 32,
+ * 64 or 128 points per edge: a 2-D FFT of each z plane that also reads and
+ * clears the fixed-point grid, a z-line pass that applies the influence
+ * function between the forward and inverse transforms, and an inverse 2-D
+ * plane pass) or cuFFT C2C plus separate conversion and convolution kernels
+ * (enable = 0; always used for other grid sizes).  The default is the fused
+ * transform on 32^3 and 64^3 grids, where it measured faster on GB300, and
+ * cuFFT on every other grid, 128^3 included.  Replaces fftfront/fftback +
+ * pmeConv (src/cudart/fft.cpp:65-95, src/cu/pme.cu:908-1031).  Enabling on
+ * an unsupported grid returns T9GB_BAD_ARG. */
 int t9gb_pme_own_fft(t9gb_context* ctx, int enable);
 
 /* Lanes of a warp that share one atom's neighbour row in the real-space

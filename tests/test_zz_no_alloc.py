@@ -6,9 +6,10 @@ loops that forbid allocator calls) use this entry point; its only working
 memory is a static device array inside the library.  The test calls it
 through the C ABI twice in a row, with different dipoles, and checks each
 result against the existing entry point t9gb_ufield on a context configured
-for the same damped (non-Ewald) field, within the field tolerance used by the
-other GPU tests.  This file is collected last so a failure here leaves every
-other test already run.
+for the same damped (non-Ewald) field and against the FP64 oracle's
+non-Ewald ufield (every mutual scale of the water box is 1), within the
+field tolerance used by the other GPU tests.  This file is collected last so
+a failure here leaves every other test already run.
 """
 import ctypes as C
 
@@ -21,7 +22,7 @@ pytestmark = pytest.mark.gpu
 FIELD_RTOL = 5.0e-5
 
 
-def test_noalloc_ufield_matches_context_entry(gpu_lib, tg):
+def test_noalloc_ufield_matches_context_entry(gpu_lib, tg, oracle):
     import torch
 
     abi = gpu_lib
@@ -34,6 +35,8 @@ def test_noalloc_ufield_matches_context_entry(gpu_lib, tg):
     xyz = torch.tensor(s.xyz, dtype=torch.float32, device=dev).contiguous()
     pdamp = torch.tensor(s.pdamp, dtype=torch.float32, device=dev).contiguous()
     thole = torch.tensor(s.thole, dtype=torch.float32, device=dev).contiguous()
+    assert np.all(s.excl_scale[:, 3] == 1.0)
+    o = oracle.OracleSystem(s, use_ewald=0, cutoff=cutoff)
     rng = np.random.default_rng(3)
     stream = torch.cuda.current_stream().cuda_stream
     for call in range(2):
@@ -53,6 +56,10 @@ def test_noalloc_ufield_matches_context_entry(gpu_lib, tg):
         torch.cuda.synchronize()
         assert rel_err(cpu(f), cpu(ref)) < FIELD_RTOL, f"call {call}"
         assert rel_err(cpu(fp), cpu(refp)) < FIELD_RTOL, f"call {call}"
+        of, ofp = o.ufield(ud, up)
+        print(f"call {call}: vs oracle {rel_err(cpu(f), of):.2e} / {rel_err(cpu(fp), ofp):.2e}")
+        assert rel_err(cpu(f), of) < FIELD_RTOL, f"call {call}"
+        assert rel_err(cpu(fp), ofp) < FIELD_RTOL, f"call {call}"
 
 
 def test_noalloc_rejects_oversize(gpu_lib):

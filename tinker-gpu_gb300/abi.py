@@ -31,6 +31,7 @@ EXPORTS = [
     "t9gb_energy_components", "t9gb_pme_own_fft", "t9gb_pair_lanes", "t9gb_force_lanes", "t9gb_set_pcg_fusion",
     "t9gb_set_thole_pairs", "t9gb_set_external_field", "t9gb_set_vdw", "t9gb_ehal", "t9gb_set_valence",
     "t9gb_evalence", "t9gb_md_init", "t9gb_md_run", "t9gb_md_state", "t9gb_md_positions_device", "t9gb_md_stats",
+    "t9gb_set_xyz_soa_device", "t9gb_diag_precond_apply", "t9gb_gradient_fixed",
 ]
 CALC_ENERGY, CALC_GRAD, CALC_VIRIAL = 0x010, 0x020, 0x040
 
@@ -140,6 +141,9 @@ def load(path=None):
     lib.t9gb_md_state.argtypes = [vp, dp, dp, fp]
     lib.t9gb_md_positions_device.argtypes = [vp, fp]
     lib.t9gb_md_stats.argtypes = [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
+    lib.t9gb_set_xyz_soa_device.argtypes = [vp, fp, fp, fp]
+    lib.t9gb_diag_precond_apply.argtypes = [vp, fp, fp, fp, fp]
+    lib.t9gb_gradient_fixed.argtypes = [vp, fp, C.c_int, vp, vp, vp]
     for name in ("t9gb_empole", "t9gb_epolar", "t9gb_emplar"):
         getattr(lib, name).argtypes = [vp, C.c_int, dp, fp, dp]
     _lib = lib
@@ -337,6 +341,29 @@ class Engine:
             )
         )
         return f, fp
+
+    def diag_precond(self, rsd, rsdp):
+        t = self.torch
+        r = t.as_tensor(np.asarray(rsd, dtype=np.float32), device="cuda").contiguous()
+        rp = t.as_tensor(np.asarray(rsdp, dtype=np.float32), device="cuda").contiguous()
+        z, zp = self._empty3(), self._empty3()
+        self._check(
+            self.lib.t9gb_diag_precond_apply(
+                self.h, C.c_void_p(r.data_ptr()), C.c_void_p(rp.data_ptr()), C.c_void_p(z.data_ptr()),
+                C.c_void_p(zp.data_ptr()),
+            )
+        )
+        return z, zp
+
+    def gradient_fixed(self, grad, accumulate=None):
+        """Float gradient [n][3] (device) -> the reference's fixed-point
+        gx, gy, gz (int64 device tensors, two's-complement u64 words)."""
+        t = self.torch
+        out = accumulate if accumulate is not None else [t.zeros(self.n, dtype=t.int64, device="cuda")
+                                                          for _ in range(3)]
+        self._check(self.lib.t9gb_gradient_fixed(self.h, C.c_void_p(grad.data_ptr()), 1 if accumulate is not None else 0,
+                                                 *[C.c_void_p(o.data_ptr()) for o in out]))
+        return out
 
     def sparse_precond(self, rsd, rsdp):
         t = self.torch
