@@ -1,5 +1,5 @@
 """CUDA multipole and polarization energies against the FP64 oracle and the
-reference's known answers.  Tolerances: relative 2e-6 of the magnitude (FP32
+reference's known answers.  Tolerances: relative 1e-6 of the magnitude (FP32
 pair and spline arithmetic, FP64 accumulation) and the reference tests'
 absolute margins for the golden values."""
 import numpy as np
@@ -9,7 +9,7 @@ import lf_fixture as L
 from gpu_util import engine_for
 
 pytestmark = pytest.mark.gpu
-REL_E = 2.0e-6
+REL_E = 1.0e-6
 
 
 def test_localframe_empole_nonewald(gpu_lib):
