@@ -248,7 +248,7 @@ struct Context {
    int* nbr_over = nullptr;  // device max count seen (overflow check)
    int* h_over = nullptr;    // pinned mirror
    int pair_lanes = 8;            // lanes per atom in the field kernels
-   int pcg_fuse = 9;              // t9gb_set_pcg_fusion
+   int pcg_fuse = 25;             // t9gb_set_pcg_fusion (bit 4: programmatic dependent launch)
    int force_lanes = 4;           // lanes per atom in the real-space force kernel
    bool list_stale = true;        // positions changed since the last list check
    bool list_need_build = true;   // no valid list for the current order / capacity
@@ -373,6 +373,77 @@ constexpr int RED_SLOTS = 8;
    } while (0)
 
 inline int grid_for(long long n, int block) { return (int)((n + block - 1) / block); }
+
+// Programmatic dependent launch.  A kernel launched with launch_k(pdl =
+// true) may be scheduled while the kernel before it on the stream drains;
+// every such kernel calls pdl_wait() first, which returns once that kernel
+// has completed and its memory is visible (a no-op for a plain launch).
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+// lets the next kernel on the stream launch (its pdl_wait still waits for
+// this grid's completion); issued once a thread's main loop is done
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_k(bool pdl, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+   Args... args)
+{
+   if (!pdl) {
+      kernel<<<grid, block, smem, st>>>(static_cast<KArgs>(args)...);
+      return cudaGetLastError();
+   }
+   cudaLaunchConfig_t cfg = {};
+   cfg.gridDim = grid;
+   cfg.blockDim = block;
+   cfg.dynamicSmemBytes = smem;
+   cfg.stream = st;
+   cudaLaunchAttribute at[1];
+   at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+   at[0].val.programmaticStreamSerializationAllowed = 1;
+   cfg.attrs = at;
+   cfg.numAttrs = 1;
+   return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
+// programmatic dependent launch for the kernels of the PCG loop (fusion bit
+// 4), outside the per-kernel timing mode
+inline bool use_pdl(const Context* ctx) { return (ctx->pcg_fuse & 16) && !ctx->prof.on; }
+
+// Bounded wait on phase `phase` (parity) of an mbarrier in shared memory
+// (shared::cta address); false when the limit (about a second of polling)
+// ran out, so a copy that never completes cannot hang the kernel.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned phase)
+{
+   for (int it = 0; it < (1 << 20); ++it) {
+      unsigned ok;
+      asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+                   : "=r"(ok)
+                   : "r"(bar), "r"(phase)
+                   : "memory");
+      if (ok)
+         return true;
+   }
+   return false;
+}
+
+__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count)
+{
+   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes)
+{
+   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+// bulk asynchronous copy global -> this CTA's shared memory (16-byte aligned
+// addresses, size a multiple of 16), completing on the mbarrier
+__device__ __forceinline__ void bulk_g2s(unsigned dst, const void* src, unsigned bytes, unsigned bar)
+{
+   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                "l"(src), "r"(bytes), "r"(bar)
+                : "memory");
+}
 
 // timed launch bracket; a no-op unless profiling is on
 inline void prof_begin(Context* ctx, int cat)

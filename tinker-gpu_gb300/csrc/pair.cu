@@ -128,6 +128,7 @@ __global__ void __launch_bounds__(256) k_ufield_real(PairParams P, int npad, con
    const float* __restrict__ z8, const double* __restrict__ scal, const float* __restrict__ base8,
    float* __restrict__ out8)
 {
+   pdl_wait();
    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
    const int i = tid / G, g = tid % G;
    if (i >= npad)
@@ -184,6 +185,7 @@ __global__ void __launch_bounds__(256) k_ufield_real(PairParams P, int npad, con
          }
       }
    }
+   pdl_trigger();
    group_reduce<G, 6>(f);
    store6<G>(out8, i < P.n ? base8 : nullptr, i, g, f);
 }
@@ -433,6 +435,7 @@ __global__ void __launch_bounds__(256, 4) k_precond_sparse_dots(PairParams P, in
    const int* __restrict__ sp_j, const float4* __restrict__ sp_sc, const float4* __restrict__ spos,
    const float* __restrict__ r8, float* __restrict__ z8, PcgDots D)
 {
+   pdl_wait();
    __shared__ double sh[64];
    constexpr int PER = 256 / G;
    const int g = threadIdx.x % G;
@@ -461,6 +464,7 @@ __global__ void __launch_bounds__(256, 4) k_precond_sparse_dots(PairParams P, in
       }
    }
    const float pv[4] = {rz_d, rz_p, rr_d, rr_p};
+   pdl_trigger();
    store_partials_f<4>(D.red, R_RZ_D, pv, sh);
    if (!last_block(D.state + ST_TICKET0))
       return;
@@ -690,8 +694,12 @@ int launch_ufield_real(Context* ctx, const float* u6, const float* base6, float*
 {
    PairParams P = make_params(ctx, ctx->cfg.cutoff);
    prof_begin(ctx, P_UFIELD_REAL);
-   T9_LANES_DISPATCH2(k_ufield_real, false, P, ctx->npad, ctx->nbrc, ctx->nnbrc, ctx->sp_start, ctx->sp_j, ctx->sp_sc,
-      ctx->spos, u6, nullptr, nullptr, base6, out6);
+   const int g = ctx->pair_lanes;
+   const int nb = grid_for((long long)ctx->npad * g, PAIR_THREADS);
+   auto k = g == 4 ? k_ufield_real<4, false> : g == 8 ? k_ufield_real<8, false> : g == 32 ? k_ufield_real<32, false>
+                                                                                    : k_ufield_real<16, false>;
+   T9_CUDA(launch_k(use_pdl(ctx), k, nb, PAIR_THREADS, 0, ctx->stream, P, ctx->npad, ctx->nbrc, ctx->nnbrc,
+      ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos, u6, nullptr, nullptr, base6, out6));
    prof_end(ctx);
    T9_CUDA(cudaGetLastError());
    return T9GB_OK;
@@ -727,18 +735,10 @@ int launch_precond_sparse_dots(Context* ctx, const float* r6, float* z6, const P
    const int per = PAIR_THREADS / g;
    const int nb = std::min(RED_MAX, (ctx->npad + per - 1) / per);
    prof_begin(ctx, P_PRECOND);
-   if (g == 4)
-      k_precond_sparse_dots<4><<<nb, PAIR_THREADS, 0, ctx->stream>>>(P, ctx->npad, (float)ctx->cfg.udiag, ctx->nbrp,
-         ctx->nnbrp, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos, r6, z6, D);
-   else if (g == 8)
-      k_precond_sparse_dots<8><<<nb, PAIR_THREADS, 0, ctx->stream>>>(P, ctx->npad, (float)ctx->cfg.udiag, ctx->nbrp,
-         ctx->nnbrp, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos, r6, z6, D);
-   else if (g == 32)
-      k_precond_sparse_dots<32><<<nb, PAIR_THREADS, 0, ctx->stream>>>(P, ctx->npad, (float)ctx->cfg.udiag, ctx->nbrp,
-         ctx->nnbrp, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos, r6, z6, D);
-   else
-      k_precond_sparse_dots<16><<<nb, PAIR_THREADS, 0, ctx->stream>>>(P, ctx->npad, (float)ctx->cfg.udiag, ctx->nbrp,
-         ctx->nnbrp, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos, r6, z6, D);
+   auto k = g == 4 ? k_precond_sparse_dots<4> : g == 8 ? k_precond_sparse_dots<8> : g == 32
+         ? k_precond_sparse_dots<32> : k_precond_sparse_dots<16>;
+   T9_CUDA(launch_k(use_pdl(ctx), k, nb, PAIR_THREADS, 0, ctx->stream, P, ctx->npad, (float)ctx->cfg.udiag, ctx->nbrp,
+      ctx->nnbrp, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos, r6, z6, D));
    prof_end(ctx);
    T9_CUDA(cudaGetLastError());
    return T9GB_OK;

@@ -177,6 +177,7 @@ __global__ void k_pcg_p1(VecArgs A, const float* __restrict__ fld, float* __rest
    const float* __restrict__ zrsd, float* __restrict__ vec, double* __restrict__ red, double* __restrict__ scal,
    int* __restrict__ state)
 {
+   pdl_wait();
    __shared__ double sh[64];
    float dd = 0.f, dp = 0.f;
    float bd = 0.f, bp = 0.f;
@@ -199,6 +200,7 @@ __global__ void k_pcg_p1(VecArgs A, const float* __restrict__ fld, float* __rest
          dp += p * v;
    }
    const float pv[2] = {dd, dp};
+   pdl_trigger();
    store_partials_f<2>(red, R_PAP_D, pv, sh);
    if (!last_block(state + ST_TICKET1))
       return;
@@ -215,6 +217,7 @@ __global__ void k_pcg_p1(VecArgs A, const float* __restrict__ fld, float* __rest
 __global__ void k_pcg_p2(VecArgs A, const double* __restrict__ scal, float* __restrict__ uind,
    const float* __restrict__ conj, float* __restrict__ rsd, const float* __restrict__ vec)
 {
+   pdl_wait();
    const float a = (float)scal[S_A_D], ap = (float)scal[S_A_P];
    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.ne; e += gridDim.x * blockDim.x) {
       const int s = e / 6, x = e + 2 * s;  // row s, component e - 6 s of [npad][8]
@@ -231,6 +234,7 @@ __global__ void k_pcg_p2(VecArgs A, const double* __restrict__ scal, float* __re
 __global__ void k_pcg_dir(VecArgs A, const double* __restrict__ scal, float* __restrict__ conj,
    const float* __restrict__ zrsd)
 {
+   pdl_wait();
    const float b = (float)scal[S_B_D], bp = (float)scal[S_B_P];
    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.ne; e += gridDim.x * blockDim.x) {
       const int s = e / 6, x = e + 2 * s;  // row s, component e - 6 s of [npad][8]
@@ -525,17 +529,19 @@ static int pcg_body(Context* ctx, const VecArgs& A, cudaGraphConditionalHandle h
             ctx->scal, ctx->status);
       }
    } else {
+      const bool pdl = use_pdl(ctx);
       prof_begin(ctx, P_VECTOR);
-      k_pcg_dir<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->scal, ctx->conj, ctx->zrsd);
+      T9_CUDA(launch_k(pdl, k_pcg_dir, A.nb, VB, 0, ctx->stream, A, ctx->scal, ctx->conj, ctx->zrsd));
       prof_end(ctx);
       T9_CHECK(ufield6(ctx, ctx->conj, ctx->fld6));
       prof_begin(ctx, P_VECTOR);
-      k_pcg_p1<false><<<A.nb, VB, 0, ctx->stream>>>(A, ctx->fld6, ctx->conj, nullptr, ctx->vec, ctx->red, ctx->scal,
-         ctx->status);
+      T9_CUDA(launch_k(pdl, k_pcg_p1<false>, A.nb, VB, 0, ctx->stream, A, ctx->fld6, ctx->conj, nullptr, ctx->vec,
+         ctx->red, ctx->scal, ctx->status));
       prof_end(ctx);
    }
    prof_begin(ctx, P_VECTOR);
-   k_pcg_p2<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->scal, ctx->uind, ctx->conj, ctx->rsd, ctx->vec);
+   T9_CUDA(launch_k(use_pdl(ctx), k_pcg_p2, A.nb, VB, 0, ctx->stream, A, ctx->scal, ctx->uind, ctx->conj, ctx->rsd,
+      ctx->vec));
    prof_end(ctx);
    T9_CUDA(cudaGetLastError());
    return precond_dots(ctx, A, 0, handle, use_handle);

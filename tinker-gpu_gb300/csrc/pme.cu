@@ -220,6 +220,7 @@ __global__ void __launch_bounds__(256) k_spread(int n, GridParams G, const float
    const float* __restrict__ src, const float* __restrict__ z8, const double* __restrict__ scal,
    unsigned long long* __restrict__ q)
 {
+   pdl_wait();
    const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
    const int lane = threadIdx.x & 31;
    if (s >= n || lane >= 25)
@@ -411,6 +412,7 @@ __global__ void __launch_bounds__(256, 6) k_gather_field(int n, GridParams G, co
    const float2* __restrict__ g, const float* __restrict__ rp, const float* __restrict__ u8, float* __restrict__ out,
    PcgAp P)
 {
+   pdl_wait();
    const int lane = threadIdx.x & 31;
    if (!AP) {
       const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -673,6 +675,7 @@ template <int N, bool FROM_FX, bool INV>
 __global__ void __launch_bounds__(N * fft_threads_per_line<N>()) k_fft_plane(long long* __restrict__ qfx,
    float2* __restrict__ g, int packed, float inv)
 {
+   pdl_wait();
    // element (y, x) at fsm[fsig(y) LD + fsig(x)]; the padding keeps the two
    // lines of a 16-thread shared-memory phase on different banks
    constexpr int T = fft_threads_per_line<N>(), LD = fft_plane_ld<N>(), NT = N * T, R = N / T;
@@ -728,6 +731,7 @@ template <int N, int MODE>
 __global__ void __launch_bounds__(16 * fft_threads_per_line<N>()) k_fft_zline(const float* __restrict__ infl,
    float2* __restrict__ g)
 {
+   pdl_wait();
    // element z of line l at sm[fsig(z) LD + l]
    constexpr int T = fft_threads_per_line<N>(), XL = 16, LD = fft_zline_ld<N>(), NT = XL * T, R = N / T;
    __shared__ float2 sm[N * LD];
@@ -798,24 +802,24 @@ static int fft_setup_kernels(Context* ctx)
 
 // forward planes; vir: the z pass stops after the forward transform
 template <int N>
-static void fft_own_forward(const PmeGrid& P, cudaStream_t st, bool split)
+static void fft_own_forward(const PmeGrid& P, cudaStream_t st, bool split, bool pdl)
 {
    constexpr int T = fft_threads_per_line<N>();
-   k_fft_plane<N, true, false><<<N, N * T, fft_plane_smem<N>(), st>>>(P.qfx, P.qgrid, P.packed ? 1 : 0,
+   launch_k(pdl, k_fft_plane<N, true, false>, N, N * T, fft_plane_smem<N>(), st, P.qfx, P.qgrid, P.packed ? 1 : 0,
       1.0f / (float)(1 << P.pack_shift));
    if (split)
-      k_fft_zline<N, 0><<<N * N / 16, 16 * T, 0, st>>>(P.infl, P.qgrid);
+      launch_k(pdl, k_fft_zline<N, 0>, N * N / 16, 16 * T, 0, st, P.infl, P.qgrid);
    else
-      k_fft_zline<N, 2><<<N * N / 16, 16 * T, 0, st>>>(P.infl, P.qgrid);
+      launch_k(pdl, k_fft_zline<N, 2>, N * N / 16, 16 * T, 0, st, P.infl, P.qgrid);
 }
 
 template <int N>
-static void fft_own_inverse(const PmeGrid& P, cudaStream_t st, bool split)
+static void fft_own_inverse(const PmeGrid& P, cudaStream_t st, bool split, bool pdl)
 {
    constexpr int T = fft_threads_per_line<N>();
    if (split)
-      k_fft_zline<N, 1><<<N * N / 16, 16 * T, 0, st>>>(P.infl, P.qgrid);
-   k_fft_plane<N, false, true><<<N, N * T, fft_plane_smem<N>(), st>>>(P.qfx, P.qgrid, 0, 0.f);
+      launch_k(pdl, k_fft_zline<N, 1>, N * N / 16, 16 * T, 0, st, P.infl, P.qgrid);
+   launch_k(pdl, k_fft_plane<N, false, true>, N, N * T, fft_plane_smem<N>(), st, P.qfx, P.qgrid, 0, 0.f);
 }
 
 // ---------------------------------------------------------------------------
@@ -1370,22 +1374,23 @@ static int fft_conv(Context* ctx, int vir = 0, float wE = 0.f, float wP = 0.f, b
    if (P.own_fft) {
       cudaStream_t st = ctx->stream;
       const bool split = vir != 0;
+      const bool pdl = use_pdl(ctx);
       if (P.n1 == 32)
-         fft_own_forward<32>(P, st, split);
+         fft_own_forward<32>(P, st, split, pdl);
       else if (P.n1 == 64)
-         fft_own_forward<64>(P, st, split);
+         fft_own_forward<64>(P, st, split, pdl);
       else
-         fft_own_forward<128>(P, st, split);
+         fft_own_forward<128>(P, st, split, pdl);
       if (split) {
          T9_CHECK(conv_virial(ctx, vir, wE, wP, stash, out));
          k_conv<<<cb, 256, 0, st>>>(ng, P.infl, P.qgrid);
       }
       if (P.n1 == 32)
-         fft_own_inverse<32>(P, st, split);
+         fft_own_inverse<32>(P, st, split, pdl && !split);
       else if (P.n1 == 64)
-         fft_own_inverse<64>(P, st, split);
+         fft_own_inverse<64>(P, st, split, pdl && !split);
       else
-         fft_own_inverse<128>(P, st, split);
+         fft_own_inverse<128>(P, st, split, pdl && !split);
       T9_CUDA(cudaGetLastError());
       prof_end(ctx);
       return T9GB_OK;
@@ -1458,8 +1463,8 @@ int launch_ufield_recip_grid(Context* ctx, const float* u6)
    GridParams G = grid_params(ctx);
    prof_begin(ctx, P_SPREAD_UIND);
    ctx->pme.packed = true;
-   k_spread<1><<<grid_for((long long)ctx->n * 32, 256), 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, u6,
-      nullptr, nullptr, reinterpret_cast<unsigned long long*>(ctx->pme.qfx));
+   T9_CUDA(launch_k(use_pdl(ctx), k_spread<1, false>, grid_for((long long)ctx->n * 32, 256), 256, 0, ctx->stream,
+      ctx->n, G, ctx->spos, u6, nullptr, nullptr, reinterpret_cast<unsigned long long*>(ctx->pme.qfx)));
    prof_end(ctx);
    T9_CUDA(cudaGetLastError());
    return fft_conv(ctx);
@@ -1472,12 +1477,8 @@ int launch_ufield_recip_gather(Context* ctx, const float* u6, float* out6, bool 
    GridParams G = grid_params(ctx);
    const int nb = grid_for((long long)ctx->n * 32, 256);
    prof_begin(ctx, P_GATHER_UIND);
-   if (acc)
-      k_gather_field<1, true><<<nb, 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->pme.qgrid, nullptr, u6, out6,
-         PcgAp{});
-   else
-      k_gather_field<1, false><<<nb, 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, ctx->pme.qgrid, nullptr, u6, out6,
-         PcgAp{});
+   T9_CUDA(launch_k(use_pdl(ctx), acc ? k_gather_field<1, true> : k_gather_field<1, false>, nb, 256, 0, ctx->stream,
+      ctx->n, G, ctx->spos, ctx->pme.qgrid, nullptr, u6, out6, PcgAp{}));
    prof_end(ctx);
    T9_CUDA(cudaGetLastError());
    return T9GB_OK;
