@@ -8,7 +8,9 @@ synthetic: molecules librate and rattle about seeded lattice sites, so the
 induce legs time the same coordinates on every run.  The MD leg (ns/day)
 integrates the same box with the whole water force field.
 
-value: induce() calls per second over all ranks, inputs resident in HBM.
+value: induce() calls per second over all ranks, inputs resident in HBM
+       (the librating trajectory; induce_md_frames repeats the solve on
+       frames of the MD leg's trajectory of the relaxed box).
 e2e:   the same through t9gb_induce_host: host coordinates in, host dipoles
        out, both copies inside the timed region.
 The working set (~10 MB) is smaller than L2, so L2 is flushed (a 512 MB
@@ -161,8 +163,10 @@ def algorithmic_bytes(kernel, n, entries, nfft):
     if kernel == "spread_mpole":
         return n * (16 + 40) + 8 * ng
     if kernel == "fft_conv":
-        # fixed grid read + clear 16 B/pt, float grid write 8, conv r/w 16 + table 4, two FFTs r/w 32
-        return ng * (16 + 8 + 16 + 4 + 32)
+        # compulsory traffic of one transform + convolution: the packed fixed-point grid read (8 B/pt) and
+        # cleared (8), the influence table read (4), the complex grid written for the gather (8); the
+        # intermediate passes of the transform are not compulsory (FFT_PASS_BYTES)
+        return ng * (8 + 8 + 4 + 8)
     if kernel in ("gather_uind", "gather_mpole"):
         return 8 * ng + n * (16 + 24 + 24)
     if kernel == "pcg_vector":
@@ -171,6 +175,12 @@ def algorithmic_bytes(kernel, n, entries, nfft):
     if kernel == "nblist":
         return n * 16 + 4 * entries
     return n * 16
+
+
+# Bytes a three-pass transform also moves between its passes (complex grid
+# written and read by the plane, z-line and plane passes): reported beside the
+# compulsory figure, not counted in it.
+FFT_PASS_BYTES = 8 + 8 + 8 + 8
 
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of a
@@ -375,6 +385,27 @@ def md_leg(args, abi, tg, stream, nrec, local, config):
         "config": f"{config}: {s.n} atoms, PME {s.settings['nfft'][0]}^3; multipole + polarization (ASPC, PCG "
                   "1e-6 D), HAL 9 A, water valence; Bussi 298 K (tau 0.1 ps), 1 fs velocity Verlet",
     }, frames, s
+
+
+def md_frames_leg(args, abi, s, stream, frames, flush):
+    """induce() ms/step and PCG iterations on frames of the relaxed box's MD
+    trajectory (recorded by the MD leg): the configured workload's
+    coordinates, rougher than the synthetic librating trajectory of `value`.
+    ASPC after --history frames, --warmup untimed, --steps timed."""
+    import torch
+
+    H, W, K = args.history, args.warmup, args.steps
+    if frames is None or frames.shape[0] < H + W + K:
+        return None
+    eng = abi.Engine(s, predictor=1 if args.predictor == "aspc" else 0, stream=stream)
+    eng.prepare(frames[0].double().cpu().numpy())
+    ud = torch.zeros((s.n, 3), device="cuda")
+    up = torch.zeros((s.n, 3), device="cuda")
+    time_steps(eng, frames, range(H + W), stream, flush, ud, up)
+    ms, its, _ = time_steps(eng, frames, range(H + W, H + W + K), stream, flush, ud, up)
+    eng.close()
+    return {"induce_ms_per_step": float(np.mean(ms)), "pcg_iterations_per_step": float(np.mean(its)),
+            "steps": K, "frames": "MD trajectory of the relaxed box (2 ps NVT, then the timed MD steps)"}
 
 
 def large_leg(args, abi, tg, stream, flush, peak):
@@ -633,7 +664,7 @@ def main():
     per_launch_s = kernels[dom]["ms_per_launch"] / 1000.0
     achieved = alg / per_launch_s / 1e9
     mean_it = float(np.mean(iters))
-    # own kernels per step (fused FFT, default CG fusion): positions 1, rotpole 2, list 5, permanent
+    # own kernels per step (fused FFT, default CG fusion; programmatic launches count as launches): positions 1, rotpole 2, list 5, permanent
     # field 6 (real, spread, 3 transform, gather), guess 1, field of the guess 6, r0 1, M r0 with the
     # dots 1, peek + predictor save 1, predictor index 1, output 1; per PCG iteration: direction 1,
     # field 6, Ap 1, update 1, M r with the dots 1
@@ -662,9 +693,14 @@ def main():
     # ---- MD (ns/day), recording the frames of the learned-guess legs ----
     want_learned = not args.no_learned and args.learn_train > 0
     nrec = args.learn_train + 3 * (args.warmup + args.steps) if want_learned else 0
+    nrec = max(nrec, args.history + args.warmup + args.steps)
     md, md_frames, md_sys = None, None, None
     if not args.no_md:
         md, md_frames, md_sys = md_leg(args, abi, tg, stream, nrec, local, args.config)
+
+    md_frames_res = None
+    if md_frames is not None:
+        md_frames_res = md_frames_leg(args, abi, md_sys, stream, md_frames, flush)
 
     learned = None
     if want_learned:
@@ -717,6 +753,10 @@ def main():
             },
             "induce_ms_per_step": 1000 * dev_sec / args.steps,
             "pcg_iterations_per_step": mean_it,
+            "induce_md_frames": md_frames_res,
+            "induce_note": "value and induce_ms_per_step: the seeded librating trajectory (smoother than MD: "
+                           "fewer PCG iterations); induce_md_frames: the same solve on frames of the relaxed "
+                           "box's MD trajectory",
             "ns_per_day": None if md is None else md["ns_per_day"],
             "ns_per_day_note": "MD leg (see md)" if md is not None else "MD leg skipped (--no-md)",
             "md": md,
@@ -726,7 +766,10 @@ def main():
                     "h2d_bytes_per_step": 3 * s.n * 4, "d2h_bytes_per_step": 6 * s.n * 4},
             "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_src,
-                         "peak_source": peak_kind, "algorithmic_bytes_per_launch": alg},
+                         "peak_source": peak_kind, "algorithmic_bytes_per_launch": alg,
+                         "algorithmic_basis": "compulsory bytes per launch (see algorithmic_bytes in bench.py)",
+                         "transform_pass_bytes_per_launch": (FFT_PASS_BYTES * nfft ** 3 if dom == "fft_conv"
+                                                             else None)},
             "kernels": kernels,
             "kernel_rooflines": kernel_rooflines(kernels, s.n, ls["entries"], nfft, peak),
             "lists": ls,

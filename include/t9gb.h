@@ -325,6 +325,35 @@ int t9gb_use_graph(t9gb_context* ctx, int enable);
  * an unsupported grid returns T9GB_BAD_ARG. */
 int t9gb_pme_own_fft(t9gb_context* ctx, int enable);
 
+/* Partition of the fused transform's two plane passes: ctas = 0 (the
+ * default) runs one CTA per z plane; 2, 4 or 8 (8 on grids of 64 points
+ * per edge or more) spread each plane over a thread-block cluster of that
+ * many CTAs, which stage their row slabs with bulk asynchronous copies and
+ * exchange rows for columns through distributed shared memory.
+ * Bit-identical results either way.  A tuning knob: on GB300 at 64^3 the
+ * clustered passes measured 22.8 / 24.2 / 25.0 us per transform +
+ * convolution against 21.0 us for one CTA per plane. */
+int t9gb_pme_fft_cluster(t9gb_context* ctx, int ctas);
+
+/* Staged real-space mutual-field and preconditioner kernels (enable = 1):
+ * each 32-atom block copies the rows of the neighbouring 32-atom blocks it
+ * needs into shared memory with bulk asynchronous copies and reads every
+ * neighbour from there; enable = 0 (the default) reads each neighbour row
+ * from global memory through L1.  Bit-identical fields either way (the same
+ * pairs in the same order); used with 4 or 8 lanes per atom.  A tuning knob:
+ * measured on GB300 the staged kernels are slower (mutual field 22.6 vs
+ * 20.7 us at 12,288 atoms, 161 vs 101 us at 98,304), because a block stages
+ * about 39 neighbouring blocks of 1.5 KB, three times the rows it reads,
+ * while the global kernels hit L1 on 85% of their row sectors. */
+int t9gb_pair_staging(t9gb_context* ctx, int enable);
+
+/* Device flags of the library's asynchronous copies, read after a
+ * synchronisation: bit 0 a staging copy of the pair kernels, bit 1 a slab
+ * copy of the transform's clustered plane passes did not complete within
+ * the kernel's bounded wait (the kernel then went on and its results are
+ * not valid).  Zero in normal operation. */
+int t9gb_copy_error(t9gb_context* ctx, int* flag);
+
 /* Lanes of a warp that share one atom's neighbour row in the real-space
  * field and preconditioner kernels: 4, 8, 16 or 32 (default 8 up to 32,768
  * atoms, 4 above).  A tuning knob; results are identical up to the order of
@@ -434,6 +463,13 @@ int t9gb_learn_eval(t9gb_context* ctx, int rows, const float* x, const float* t,
 /* One AdamW step (beta 0.9/0.999, eps 1e-8) with the gradient of the last
  * t9gb_learn_eval. */
 int t9gb_learn_adamw(t9gb_context* ctx);
+/* Tensor-core path of the network's forward pass: 0 (default) the
+ * warp-level mma.sync GEMMs with separate bias / SiLU kernels; 1 one fused
+ * kernel per 128 rows on the fifth-generation tensor cores (tcgen05.mma with
+ * the accumulators in tensor memory, read back with tcgen05.ld for the bias
+ * and SiLU epilogue of each layer).  Same outputs up to the order of the
+ * FP32 accumulation.  The backward pass uses the mma.sync GEMMs either way. */
+int t9gb_learn_tensor_path(t9gb_context* ctx, int path);
 /* Raw features of the last solve, device [2n][32]: rows 0..n-1 for the d
  * dipoles, n..2n-1 for the p dipoles, caller atom order. */
 int t9gb_learn_features(t9gb_context* ctx, float* features_device);

@@ -57,3 +57,35 @@ def test_forces_and_virial_32cubed_vs_oracle(gpu_lib, oracle, tg):
     ud, up, *_ = oracle.OracleSystem(s).induce()
     wo2 = oracle.epolar_virial_fd(s, ud, up, diag_only=True, cutoff=9.0)
     assert np.abs(np.diag(w2) - np.diag(wo2)).max() < 2e-3 + 2e-5 * np.abs(np.diag(wo2)).max()
+
+
+@pytest.mark.parametrize("name,nfft", [("water648", 32), ("water12288", 64)])
+@pytest.mark.parametrize("ctas", [2, 4, 8])
+def test_cluster_plane_passes_bit_identical(gpu_lib, tg, name, nfft, ctas):
+    """Plane passes spread over a thread-block cluster per z plane (bulk
+    copies of the row slabs, rows exchanged for columns through distributed
+    shared memory) give the same bits as one CTA per plane: fields of both
+    grids, a whole graph-captured solve, and the k-space virial split."""
+    if ctas == 8 and nfft < 64:
+        pytest.skip("8-CTA clusters need 64 points per edge")
+    s = tg.systems.make_config(name, nfft=nfft)
+    a = engine_for(s)
+    a.pme_own_fft(True)
+    a.fft_cluster(0)
+    b = engine_for(s)
+    b.pme_own_fft(True)
+    b.fft_cluster(ctas)
+    for x, y in zip(a.dfield(), b.dfield()):
+        assert np.array_equal(cpu(x), cpu(y))
+    rng = np.random.default_rng(8)
+    u, up = rng.normal(size=(s.n, 3)) * 0.05, rng.normal(size=(s.n, 3)) * 0.05
+    for x, y in zip(a.ufield(u, up), b.ufield(u, up)):
+        assert np.array_equal(cpu(x), cpu(y))
+    ua, pa, _ = a.induce()
+    ub, pb, _ = b.induce()
+    assert a.stats()[0] == b.stats()[0]
+    assert np.array_equal(cpu(ua), cpu(ub)) and np.array_equal(cpu(pa), cpu(pb))
+    ea, ga, wa = a.emplar(0x070)
+    eb, gb, wb = b.emplar(0x070)
+    assert ea == eb and np.array_equal(cpu(ga), cpu(gb)) and np.array_equal(wa, wb)
+    assert b.copy_error() == 0

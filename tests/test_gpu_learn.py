@@ -187,3 +187,44 @@ def test_learned_graph_matches_stepwise(gpu_lib, tg):
     assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
     assert np.array_equal(out[0][2], out[1][2])
     assert out[0][3] == out[1][3]
+
+
+def test_tensor_core_forward_matches_oracle(gpu_lib, tg, LO):
+    """The fused tcgen05 forward pass (tensor-memory accumulators, one CTA
+    per 128 rows, a partial last tile here) gives the network outputs, loss
+    and gradient within the same bar as the mma.sync path, and close to it."""
+    s = tg.systems.make_config("water648")
+    e = engine_for(s)
+    e.learn_reset(seed=7)
+    w = e.learn_weights().astype(np.float64)
+    rng = np.random.default_rng(8)
+    rows = 1000
+    x = rng.normal(size=(rows, 32)).astype(np.float32)
+    t = rng.normal(size=(rows, 3)).astype(np.float32)
+    y0, g0, l0 = e.learn_eval(x, t)
+    e.learn_tensor_path(1)
+    y, g, loss = e.learn_eval(x, t)
+    assert e.copy_error() == 0
+    yo, lo, go = LO.loss_grad(w, x.astype(np.float64), t.astype(np.float64), bf=True)
+    print("tcgen05 vs mma.sync: y", float(np.linalg.norm(y - y0) / np.linalg.norm(y0)),
+          "vs oracle", float(np.linalg.norm(y - yo) / np.linalg.norm(yo)))
+    assert np.linalg.norm(y - yo) < NET_TOL * np.linalg.norm(yo)
+    assert abs(loss - lo) < NET_TOL * lo
+    assert np.linalg.norm(g - go) < NET_TOL * np.linalg.norm(go)
+    assert np.linalg.norm(y - y0) < NET_TOL * np.linalg.norm(y0)
+
+
+def test_tensor_core_learned_solve(gpu_lib, oracle, tg):
+    """Training and the learned start with the tcgen05 forward pass: the
+    solve still converges to the oracle's dipoles."""
+    s = tg.systems.make_config("water648")
+    e = engine_for(s)
+    e.learn_tensor_path(1)
+    e.learn_reset(seed=1)
+    e.learn_config(3)
+    for _ in range(3):
+        ud, up, rc = e.induce_host(s.xyz)
+    assert rc == 0 and e.copy_error() == 0
+    ou, op, *_ = oracle.OracleSystem(s).induce()
+    D = tg.units.DEBYE
+    assert rms_err(ud * D, ou * D) < DIPOLE_RMS_DEBYE and rms_err(up * D, op * D) < DIPOLE_RMS_DEBYE

@@ -31,7 +31,8 @@ EXPORTS = [
     "t9gb_energy_components", "t9gb_pme_own_fft", "t9gb_pair_lanes", "t9gb_force_lanes", "t9gb_set_pcg_fusion",
     "t9gb_set_thole_pairs", "t9gb_set_external_field", "t9gb_set_vdw", "t9gb_ehal", "t9gb_set_valence",
     "t9gb_evalence", "t9gb_md_init", "t9gb_md_run", "t9gb_md_state", "t9gb_md_positions_device", "t9gb_md_stats",
-    "t9gb_set_xyz_soa_device", "t9gb_diag_precond_apply", "t9gb_gradient_fixed",
+    "t9gb_set_xyz_soa_device", "t9gb_diag_precond_apply", "t9gb_gradient_fixed", "t9gb_pme_fft_cluster",
+    "t9gb_copy_error", "t9gb_pair_staging", "t9gb_learn_tensor_path",
 ]
 CALC_ENERGY, CALC_GRAD, CALC_VIRIAL = 0x010, 0x020, 0x040
 
@@ -125,6 +126,10 @@ def load(path=None):
     lib.t9gb_learn_features.argtypes = [vp, fp]
     lib.t9gb_energy_components.argtypes = [vp, dp]
     lib.t9gb_pme_own_fft.argtypes = [vp, C.c_int]
+    lib.t9gb_pme_fft_cluster.argtypes = [vp, C.c_int]
+    lib.t9gb_copy_error.argtypes = [vp, ip]
+    lib.t9gb_pair_staging.argtypes = [vp, C.c_int]
+    lib.t9gb_learn_tensor_path.argtypes = [vp, C.c_int]
     lib.t9gb_pair_lanes.argtypes = [vp, C.c_int]
     lib.t9gb_set_pcg_fusion.argtypes = [vp, C.c_int]
     lib.t9gb_force_lanes.argtypes = [vp, C.c_int]
@@ -414,6 +419,22 @@ class Engine:
         """Fused power-of-two FFT (default where supported) or cuFFT."""
         self._check(self.lib.t9gb_pme_own_fft(self.h, 1 if enable else 0))
 
+    def fft_cluster(self, ctas=4):
+        """CTAs per z plane in the fused transform's plane passes (0: one)."""
+        self._check(self.lib.t9gb_pme_fft_cluster(self.h, int(ctas)))
+
+    def pair_staging(self, enable=True):
+        """Staged (shared-memory) or global-memory rows in the field and
+        preconditioner pair kernels."""
+        self._check(self.lib.t9gb_pair_staging(self.h, 1 if enable else 0))
+
+    def copy_error(self):
+        """Bit 0: a pair-kernel staging copy, bit 1: a transform slab copy
+        timed out (0 in normal operation)."""
+        f = C.c_int()
+        self._check(self.lib.t9gb_copy_error(self.h, C.byref(f)))
+        return f.value
+
     def pair_lanes(self, lanes=16):
         self._check(self.lib.t9gb_pair_lanes(self.h, int(lanes)))
 
@@ -496,6 +517,10 @@ class Engine:
         loss = C.c_double()
         self._check(self.lib.t9gb_learn_eval(self.h, rows, _fp(x), _fp(t), _fp(y), _fp(g), C.byref(loss)))
         return y, g, loss.value
+
+    def learn_tensor_path(self, path=1):
+        """0: mma.sync GEMMs; 1: the fused tcgen05 forward pass."""
+        self._check(self.lib.t9gb_learn_tensor_path(self.h, int(path)))
 
     def learn_adamw(self):
         self._check(self.lib.t9gb_learn_adamw(self.h))

@@ -48,6 +48,8 @@ static int alloc_all(Context* ctx)
    T9_CUDA(cudaMemset(ctx->nnbrp, 0, sizeof(int) * npad));
    T9_CUDA(cudaMalloc(&ctx->nbr_over, sizeof(int)));
    T9_CUDA(cudaMemset(ctx->nbr_over, 0, sizeof(int)));
+   T9_CUDA(cudaMalloc(&ctx->copy_err, sizeof(int)));
+   T9_CUDA(cudaMemset(ctx->copy_err, 0, sizeof(int)));
    T9_CUDA(cudaMallocHost(&ctx->h_over, sizeof(int)));
    *ctx->h_over = 0;
    T9_CUDA(cudaMalloc(&ctx->cell_atoms, sizeof(int) * npad));
@@ -98,6 +100,7 @@ static void free_all(Context* ctx)
 {
    void* dev[] = {ctx->frames, ctx->pole, ctx->xyz, ctx->perm, ctx->iperm, ctx->spos, ctx->spolar, ctx->spolinv,
       ctx->sdamp, ctx->srpole, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->nbr, ctx->nnbr, ctx->nbr_over, ctx->nbrc, ctx->nnbrc, ctx->nbrp, ctx->nnbrp,
+      ctx->jbl, ctx->jbn, ctx->nbrc_l, ctx->nbrp_l, ctx->copy_err,
       ctx->cell_count, ctx->cell_start, ctx->cell_atoms, ctx->atom_cell, ctx->rcp6, ctx->fld6, ctx->udir,
       ctx->efield, ctx->uind, ctx->rsd, ctx->zrsd, ctx->conj, ctx->vec, ctx->tmp6, ctx->e_atom, ctx->sframe, ctx->hout,
       ctx->red, ctx->scal, ctx->status, ctx->sref, ctx->lflag,
@@ -209,6 +212,10 @@ int t9gb_create(const t9gb_config* cfg, t9gb_context** out)
       rc = alloc_all(ctx);
    if (rc == T9GB_OK)
       rc = pme_setup(ctx);
+   if (rc == T9GB_OK)
+      rc = pair_staging_setup();
+   if (rc == T9GB_OK)
+      rc = mlp_tc_setup();
    if (rc != T9GB_OK) {
       free_all(ctx);
       delete h;
@@ -606,6 +613,63 @@ int t9gb_set_pcg_fusion(t9gb_context* h, int mask)
    if (mask != h->c.pcg_fuse)
       drop_graphs(&h->c);
    h->c.pcg_fuse = mask;
+   return T9GB_OK;
+}
+
+int t9gb_pme_fft_cluster(t9gb_context* h, int ctas)
+{
+   if (!h)
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   const int n = ctx->pme.n1;
+   if (!(ctas == 0 || ((ctas == 2 || ctas == 4 || (ctas == 8 && n >= 64)) && ctx->pme.own_fft_ok)))
+      return T9GB_BAD_ARG;
+   if (ctas != ctx->pme.fft_cl)
+      drop_graphs(ctx);
+   ctx->pme.fft_cl = ctas;
+   return T9GB_OK;
+}
+
+int t9gb_copy_error(t9gb_context* h, int* flag)
+{
+   if (!h || !flag)
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   int a = 0, b = 0;
+   T9_CUDA(cudaMemcpyAsync(&a, ctx->copy_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+   if (ctx->pme.fft_err)
+      T9_CUDA(cudaMemcpyAsync(&b, ctx->pme.fft_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+   T9_CUDA(cudaStreamSynchronize(ctx->stream));
+   *flag = (a ? 1 : 0) | (b ? 2 : 0);
+   return T9GB_OK;
+}
+
+int t9gb_learn_tensor_path(t9gb_context* h, int path)
+{
+   if (!h || (path != 0 && path != 1))
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   if ((path == 1) != ctx->mlp_tc)
+      drop_graphs(ctx);
+   ctx->mlp_tc = path == 1;
+   return T9GB_OK;
+}
+
+int t9gb_pair_staging(t9gb_context* h, int enable)
+{
+   if (!h)
+      return T9GB_BAD_ARG;
+   Context* ctx = &h->c;
+   if ((enable != 0) != ctx->pair_staged) {
+      drop_graphs(ctx);
+      // the staged kernels read the local indices and j-block lists of the
+      // latest staging filter pass: refilter before the next field, and
+      // until then no block is staged
+      if (ctx->jbn)
+         T9_CUDA(cudaMemsetAsync(ctx->jbn, 0x7f, sizeof(int) * (size_t)(ctx->npad / 32), ctx->stream));
+      ctx->list_stale = true;
+   }
+   ctx->pair_staged = enable != 0;
    return T9GB_OK;
 }
 

@@ -73,6 +73,8 @@ struct PmeGrid {
    bool packed = false;       // the fixed-point grid holds packed d / p dipole values
    int pack_shift = 24;       // their 32-bit fixed-point scale 2^pack_shift (16 after a range fallback)
    bool probe = false;        // spreads of the learned guess's residual: their own range flag
+   int fft_cl = 0;            // fused transform: CTAs per z plane (a thread-block cluster), 0: one CTA
+   int* fft_err = nullptr;    // device flag: a staged slab copy of a plane pass did not complete in time
 };
 
 // Per-kernel event timing (tracing): categories of timed launches.
@@ -245,6 +247,18 @@ struct Context {
    int* nnbrc = nullptr;
    int* nbrp = nullptr;
    int* nnbrp = nullptr;
+   // staged field / preconditioner kernels (t9gb_pair_staging): per 32-slot
+   // block the j-blocks its sub-list entries fall in (ascending, at most
+   // STAGE_JB_CAP; jbn > cap means the block reads rows from global memory),
+   // and every sub-list entry as a local index (j-block position x 32 +
+   // slot within the block)
+   int* jbl = nullptr;               // [npad / 32][STAGE_JB_CAP]
+   int* jbn = nullptr;               // [npad / 32]
+   unsigned short* nbrc_l = nullptr; // [npad][nbr_cap]
+   unsigned short* nbrp_l = nullptr; // [npad][nbr_cap]
+   bool pair_staged = false;         // t9gb_pair_staging
+   bool mlp_tc = false;              // learned guess: forward pass on tcgen05 (t9gb_learn_tensor_path)
+   int* copy_err = nullptr;          // device flag: a staging copy did not complete in time
    int* nbr_over = nullptr;  // device max count seen (overflow check)
    int* h_over = nullptr;    // pinned mirror
    int pair_lanes = 8;            // lanes per atom in the field kernels
@@ -349,6 +363,10 @@ struct Context {
 // and their atoms' separation that the stored list allows for (each site lies
 // (1 - red) of a bond from its atom: 0.09 A for AMOEBA water hydrogens).
 constexpr double VDW_SITE_MARGIN = 0.25;
+// j-blocks a 32-slot block stages into shared memory (48 of 1.5 KB: 72 KB,
+// three blocks per SM); water blocks need 39 on average, 45 at most at a
+// 7 A cutoff
+constexpr int STAGE_JB_CAP = 48;
 
 // energy / virial row sums: at most SUM_ROWS_MAX rows per launch, each
 // split over SUM_PARTS blocks
@@ -482,6 +500,8 @@ int list_update(Context* ctx);  // device: exact neighbour list
 int ensure_list(Context* ctx);  // list_update when the coordinates changed
 int check_list_overflow(Context* ctx, int* redo);
 int alloc_lists(Context* ctx, int cap);          // nbr, nbrc, nbrp with row capacity cap
+int pair_staging_setup();                         // pair.cu: shared-memory limits of the staged kernels
+int mlp_tc_setup();                               // mlp.cu: shared-memory limit of the tcgen05 forward
 int launch_list_filter(Context* ctx);             // pair.cu  // after a sync; redo = 1: grown, repeat
 // The fused kernels of a CG iteration: the sparse preconditioner with the
 // r.z / r.r sums and the CG scalars (pair.cu), and the mutual-field gather

@@ -429,11 +429,214 @@ int mlp_get_weights(Context* ctx, float* w_host)
    return T9GB_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Forward pass on the fifth-generation tensor cores (tcgen05): one CTA of
+// four warps per 128 rows.  The row tile and the transposed weights are
+// staged in shared memory in the canonical K-major layout without swizzle
+// (8-row x 16-byte core matrices; LBO = 128 B between core matrices along K,
+// SBO = K / 8 x 128 B between 8-row groups), one thread issues the
+// tcgen05.mma instructions (M = 128, K = 16 per instruction, BF16 in, FP32
+// accumulated in tensor memory), tcgen05.commit signals an mbarrier, and each
+// warp reads its 32 rows back with tcgen05.ld for the bias + SiLU epilogue,
+// which writes the next layer's operand tile.  The outputs are those of the
+// mma.sync path (z1, h1, z2, h2, y), equal to them up to the order of the
+// FP32 accumulation inside the MMA.
+
+constexpr int TC_ROWS = 128;
+constexpr int TC_TMEM_COLS = 128;  // D1 in columns 0-63, D2 in 64-127, D3 in 0-15
+
+// byte offset of element (r, k) in a K-major no-swizzle tile with K columns
+__device__ __forceinline__ int kmaj_off(int r, int k, int K)
+{
+   return ((r >> 3) * (K >> 3) + (k >> 3)) * 128 + (r & 7) * 16 + (k & 7) * 2;
+}
+
+// shared-memory matrix descriptor: start address, LBO, SBO (all >> 4), the
+// fixed 0b001 at bits 46-48, no swizzle
+__device__ __forceinline__ unsigned long long smem_desc(unsigned addr, int K)
+{
+   const unsigned long long lbo = 128 >> 4, sbo = (unsigned long long)((K >> 3) * 128) >> 4;
+   return (unsigned long long)((addr & 0x3ffff) >> 4) | (lbo << 16) | (sbo << 32) | (1ull << 46);
+}
+
+// kind::f16 instruction descriptor: D f32, A and B bf16, both K-major, N, M = 128
+__host__ __device__ constexpr unsigned tc_idesc(int n)
+{
+   return (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(n >> 3) << 17) | ((unsigned)(TC_ROWS >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_mma(unsigned dtmem, unsigned long long adesc, unsigned long long bdesc,
+   unsigned idesc, int accum)
+{
+   asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
+                "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accum)
+                : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(unsigned bar)
+{
+   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                : "memory");
+}
+
+// 16 consecutive FP32 columns of this warp's 32 TMEM lanes
+__device__ __forceinline__ void tc_ld16(unsigned taddr, float* v)
+{
+   unsigned r[16];
+   asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
+                "%13, %14, %15}, [%16];\n"
+                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                : "r"(taddr));
+   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+   for (int i = 0; i < 16; ++i)
+      v[i] = __uint_as_float(r[i]);
+}
+
+// operand tiles (bytes): X [128][32], H1 / H2 [128][64], W1^T [64][32],
+// W2^T [64][64], W3^T [16][64] (columns 8-15 zero)
+constexpr int TC_SX = 0, TC_SH1 = TC_SX + 128 * 32 * 2, TC_SH2 = TC_SH1 + 128 * 64 * 2;
+constexpr int TC_SW1 = TC_SH2 + 128 * 64 * 2, TC_SW2 = TC_SW1 + 64 * 32 * 2, TC_SW3 = TC_SW2 + 64 * 64 * 2;
+constexpr int TC_SMEM = TC_SW3 + 16 * 64 * 2;  // 55,296 bytes: at most four CTAs per SM, 4 x 128 TMEM columns
+
+__global__ void __launch_bounds__(128) k_mlp_forward_tc(int rows, const __nv_bfloat16* __restrict__ x,
+   const __nv_bfloat16* __restrict__ wb, const float* __restrict__ w, float* __restrict__ z1,
+   __nv_bfloat16* __restrict__ h1, float* __restrict__ z2, __nv_bfloat16* __restrict__ h2, float* __restrict__ y,
+   int* __restrict__ err)
+{
+   extern __shared__ __align__(128) unsigned char tsm[];
+   __shared__ __align__(8) unsigned long long bar;
+   __shared__ unsigned tmem_slot;
+   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+   const int r0 = blockIdx.x * TC_ROWS;
+   const unsigned base = (unsigned)__cvta_generic_to_shared(tsm);
+   const unsigned bar_s = (unsigned)__cvta_generic_to_shared(&bar);
+
+   // tensor memory for the accumulators (warp 0 allocates, and frees at the end)
+   if (warp == 0) {
+      asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                      (unsigned)__cvta_generic_to_shared(&tmem_slot)),
+                   "r"((unsigned)TC_TMEM_COLS)
+                   : "memory");
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+   }
+   if (tid == 0)
+      mbar_init(bar_s, 1);
+   // operand tiles: the input rows and the transposed weights
+   for (int e = tid; e < TC_ROWS * MLP_IN; e += 128) {
+      const int r = e / MLP_IN, k = e % MLP_IN;
+      const __nv_bfloat16 v = r0 + r < rows ? x[(size_t)(r0 + r) * MLP_IN + k] : __float2bfloat16(0.f);
+      *reinterpret_cast<__nv_bfloat16*>(tsm + TC_SX + kmaj_off(r, k, MLP_IN)) = v;
+   }
+   for (int e = tid; e < MLP_HID * MLP_IN; e += 128) {  // W1^T: (n, k) = W1[k][n]
+      const int n = e / MLP_IN, k = e % MLP_IN;
+      *reinterpret_cast<__nv_bfloat16*>(tsm + TC_SW1 + kmaj_off(n, k, MLP_IN)) = wb[BF_W1 + k * MLP_HID + n];
+   }
+   for (int e = tid; e < MLP_HID * MLP_HID; e += 128) {
+      const int n = e / MLP_HID, k = e % MLP_HID;
+      *reinterpret_cast<__nv_bfloat16*>(tsm + TC_SW2 + kmaj_off(n, k, MLP_HID)) = wb[BF_W2 + k * MLP_HID + n];
+   }
+   for (int e = tid; e < 16 * MLP_HID; e += 128) {
+      const int n = e / MLP_HID, k = e % MLP_HID;
+      *reinterpret_cast<__nv_bfloat16*>(tsm + TC_SW3 + kmaj_off(n, k, MLP_HID)) =
+         n < MLP_OUT_PAD ? wb[BF_W3 + k * MLP_OUT_PAD + n] : __float2bfloat16(0.f);
+   }
+   // the tiles (generic proxy) before the tensor core reads them (async proxy)
+   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+   __syncthreads();
+   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+   const unsigned tmem = tmem_slot;
+   const unsigned lane_base = tmem + ((unsigned)(32 * warp) << 16);
+   const int r = r0 + 32 * warp + lane;  // this thread's row
+   unsigned phase = 0;
+
+   // one layer: D[columns dcol..] = A B over K (K / 16 MMAs), then wait
+   auto layer = [&](unsigned a_off, unsigned b_off, int K, int n, unsigned dcol) {
+      if (tid == 0) {
+         for (int kk = 0; kk < K / 16; ++kk)
+            tc_mma(tmem + dcol, smem_desc(base + a_off + kk * 256, K), smem_desc(base + b_off + kk * 256, K),
+               tc_idesc(n), kk > 0);
+         tc_commit(bar_s);
+      }
+      if (!mbar_wait_bounded(bar_s, phase)) {
+         // record it, and give the MMAs in flight a second bounded wait
+         // before their operands and accumulators are reused or freed
+         if (tid == 0)
+            atomicExch(err, 1);
+         mbar_wait_bounded(bar_s, phase);
+      }
+      phase ^= 1u;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+   };
+
+   // hidden layer epilogue: z = D + b, h = silu(z), also into the next operand tile
+   auto hidden = [&](unsigned dcol, const float* b, float* zg, __nv_bfloat16* hg, unsigned h_off) {
+#pragma unroll
+      for (int c0 = 0; c0 < MLP_HID; c0 += 16) {
+         float v[16];
+         tc_ld16(lane_base + dcol + c0, v);
+#pragma unroll
+         for (int i = 0; i < 16; ++i) {
+            const int c = c0 + i;
+            const float z = v[i] + b[c];
+            const __nv_bfloat16 hv = __float2bfloat16(silu(z));
+            if (r < rows) {
+               zg[(size_t)r * MLP_HID + c] = z;
+               hg[(size_t)r * MLP_HID + c] = hv;
+            }
+            *reinterpret_cast<__nv_bfloat16*>(tsm + h_off + kmaj_off(32 * warp + lane, c, MLP_HID)) =
+               r < rows ? hv : __float2bfloat16(0.f);
+         }
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncthreads();
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+   };
+
+   layer(TC_SX, TC_SW1, MLP_IN, MLP_HID, 0);
+   hidden(0, w + OFF_B1, z1, h1, TC_SH1);
+   layer(TC_SH1, TC_SW2, MLP_HID, MLP_HID, 64);
+   hidden(64, w + OFF_B2, z2, h2, TC_SH2);
+   layer(TC_SH2, TC_SW3, MLP_HID, 16, 0);
+   {
+      float v[16];
+      tc_ld16(lane_base, v);
+      if (r < rows)
+#pragma unroll
+         for (int c = 0; c < MLP_OUT_PAD; ++c)
+            y[(size_t)r * MLP_OUT_PAD + c] = v[c] + w[OFF_B3 + c];
+   }
+   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+   __syncthreads();
+   if (warp == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((unsigned)TC_TMEM_COLS)
+                   : "memory");
+   }
+}
+
+int mlp_tc_setup()
+{
+   return cudaFuncSetAttribute(k_mlp_forward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM) == cudaSuccess
+      ? T9GB_OK
+      : T9GB_CUDA_ERR;
+}
+
 // forward over rows of S.x; outputs in S.y [rows][8]
 int mlp_forward(Context* ctx, int rows)
 {
    MlpState& S = ctx->mlp;
    const __nv_bfloat16* wb = reinterpret_cast<const __nv_bfloat16*>(S.wb);
+   if (ctx->mlp_tc) {
+      k_mlp_forward_tc<<<grid_for(rows, TC_ROWS), 128, TC_SMEM, ctx->stream>>>(rows, S.x, wb, S.w, S.z1, S.h1, S.z2,
+         S.h2, S.y, ctx->copy_err);
+      T9_CUDA(cudaGetLastError());
+      return T9GB_OK;
+   }
    T9_CHECK(gemm(ctx, false, false, rows, MLP_HID, MLP_IN, S.x, MLP_IN, wb + BF_W1, MLP_HID, S.c, 1));
    k_bias_act<<<grid_for((long long)rows * MLP_HID, 256), 256, 0, ctx->stream>>>(rows, MLP_HID, MLP_HID, S.c,
       S.w + OFF_B1, S.z1, S.h1, 1);

@@ -62,6 +62,18 @@ int alloc_lists(Context* ctx, int cap)
       *p = nullptr;
       T9_CUDA(cudaMalloc(p, sizeof(int) * (size_t)ctx->npad * cap));
    }
+   for (unsigned short** p : {&ctx->nbrc_l, &ctx->nbrp_l}) {
+      cudaFree(*p);
+      *p = nullptr;
+      T9_CUDA(cudaMalloc(p, sizeof(unsigned short) * (size_t)ctx->npad * cap));
+   }
+   if (!ctx->jbl) {
+      const int nblk = ctx->npad / 32;
+      T9_CUDA(cudaMalloc(&ctx->jbl, sizeof(int) * (size_t)nblk * STAGE_JB_CAP));
+      T9_CUDA(cudaMalloc(&ctx->jbn, sizeof(int) * (size_t)nblk));
+      // no staging until a staging filter pass has written the lists
+      T9_CUDA(cudaMemset(ctx->jbn, 0x7f, sizeof(int) * (size_t)nblk));
+   }
    ctx->nbr_cap = cap;
    return T9GB_OK;
 }

@@ -476,6 +476,283 @@ __global__ void __launch_bounds__(256, 4) k_precond_sparse_dots(PairParams P, in
 }
 
 // ---------------------------------------------------------------------------
+// Staged field and preconditioner kernels (t9gb_pair_staging): one CTA per
+// 32-slot block (32 atoms x G lanes).  The block's j-blocks (the 32-slot
+// blocks its sub-list entries fall in, listed by the filter) are copied into
+// shared memory by the bulk-copy engine (cp.async.bulk: one 512-byte
+// position copy and one 1-KB row copy per j-block, completing on an
+// mbarrier), and every neighbour row is then read from shared memory through
+// the entry's local index: one coalesced 2-byte index load per neighbour
+// instead of a dependent scattered 48-byte global gather.  The neighbour
+// order and the arithmetic are those of the global-memory kernels, so the
+// fields are bit-identical to theirs; a block with more j-blocks than
+// STAGE_JB_CAP reads its rows from global memory the same way.
+
+constexpr unsigned STAGE_POS_BYTES = 32 * 16;   // one j-block of positions
+constexpr unsigned STAGE_ROW_BYTES = 32 * 32;   // one j-block of 8-float rows
+constexpr size_t STAGE_SMEM = (size_t)STAGE_JB_CAP * (STAGE_POS_BYTES + STAGE_ROW_BYTES);
+
+// Stages the j-blocks jl[0..cnt) of positions and rows and waits for them
+// (phase `phase` of the CTA's mbarrier); a wait that runs out is recorded in
+// *err.  The caller has synchronised the CTA since its last read of the
+// staging buffers.
+__device__ __forceinline__ void stage_rows(unsigned char* stg, unsigned bar, unsigned phase, const int* __restrict__ jl,
+   int cnt, const float4* __restrict__ spos, const float* __restrict__ r8, int* __restrict__ err)
+{
+   const unsigned pos_s = (unsigned)__cvta_generic_to_shared(stg);
+   const unsigned row_s = pos_s + STAGE_JB_CAP * STAGE_POS_BYTES;
+   if (threadIdx.x == 0)
+      mbar_expect_tx(bar, (unsigned)cnt * (STAGE_POS_BYTES + STAGE_ROW_BYTES));
+   // the previous pass's reads of the buffers (generic proxy) before the
+   // copies' writes (async proxy)
+   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+   for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
+      const int jb = jl[q];
+      bulk_g2s(pos_s + q * STAGE_POS_BYTES, spos + (size_t)jb * 32, STAGE_POS_BYTES, bar);
+      bulk_g2s(row_s + q * STAGE_ROW_BYTES, r8 + (size_t)jb * 32 * 8, STAGE_ROW_BYTES, bar);
+   }
+   if (mbar_wait_bounded(bar, phase))
+      return;
+   if (threadIdx.x == 0)
+      atomicExch(err, 1);
+   mbar_wait_bounded(bar, phase);  // the copies in flight, before the buffers are reused
+}
+
+// neighbour row L from the staged buffers
+__device__ __forceinline__ void staged_row(const unsigned char* stg, int L, float4& p, float* v)
+{
+   p = reinterpret_cast<const float4*>(stg)[L];
+   const float4* r = reinterpret_cast<const float4*>(stg + STAGE_JB_CAP * STAGE_POS_BYTES) + 2 * L;
+   const float4 x = r[0], y = r[1];
+   v[0] = x.x;
+   v[1] = x.y;
+   v[2] = x.z;
+   v[3] = x.w;
+   v[4] = y.x;
+   v[5] = y.y;
+   v[6] = y.z;
+   v[7] = y.w;
+}
+
+template <int G>
+__global__ void __launch_bounds__(32 * G) k_ufield_stg(PairParams P, const int* __restrict__ nbr,
+   const unsigned short* __restrict__ nbr_l, const int* __restrict__ nnbr, const int* __restrict__ jbl,
+   const int* __restrict__ jbn, const int* __restrict__ sp_start, const int* __restrict__ sp_j,
+   const float4* __restrict__ sp_sc, const float4* __restrict__ spos, const float* __restrict__ u8,
+   const float* __restrict__ base8, float* __restrict__ out8, int* __restrict__ err)
+{
+   pdl_wait();
+   extern __shared__ __align__(128) unsigned char stg[];
+   __shared__ __align__(8) unsigned long long bar;
+   const int blk = blockIdx.x;
+   const int i = blk * 32 + threadIdx.x / G, g = threadIdx.x % G;
+   const int nj = jbn[blk];
+   const bool staged = nj <= STAGE_JB_CAP;
+   if (staged) {
+      const unsigned bar_s = (unsigned)__cvta_generic_to_shared(&bar);
+      if (threadIdx.x == 0)
+         mbar_init(bar_s, 1);
+      __syncthreads();
+      stage_rows(stg, bar_s, 0, jbl + (size_t)blk * STAGE_JB_CAP, nj, spos, u8, err);
+   }
+   float f[6] = {0, 0, 0, 0, 0, 0};
+   if (i < P.n) {
+      const float4 pi = spos[i];
+      const float pti = u8[8 * i + 6];
+      const int cnt = nnbr[i];
+      int k = g;
+      if (staged) {
+         const unsigned short* row = nbr_l + (size_t)i * P.cap;
+         for (; k + G < cnt; k += 2 * G) {
+            float4 p0, p1;
+            float u0[8], u1[8];
+            staged_row(stg, row[k], p0, u0);
+            staged_row(stg, row[k + G], p1, u1);
+            const float3 s0 = sep(P, pi, p0), s1 = sep(P, pi, p1);
+            const float r0 = s0.x * s0.x + s0.y * s0.y + s0.z * s0.z;
+            const float r1 = s1.x * s1.x + s1.y * s1.y + s1.z * s1.z;
+            if (r0 <= P.cut2)
+               ufield_i(P, r0, s0, 1.f, pi.w, pti, p0.w, u0[6], u0, f);
+            if (r1 <= P.cut2)
+               ufield_i(P, r1, s1, 1.f, pi.w, pti, p1.w, u1[6], u1, f);
+         }
+         if (k < cnt) {
+            float4 pk;
+            float uk[8];
+            staged_row(stg, row[k], pk, uk);
+            const float3 d = sep(P, pi, pk);
+            const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
+            if (r2 <= P.cut2)
+               ufield_i(P, r2, d, 1.f, pi.w, pti, pk.w, uk[6], uk, f);
+         }
+      } else {
+         const int* row = nbr + (size_t)i * P.cap;
+         for (; k + G < cnt; k += 2 * G) {
+            const int j0 = row[k], j1 = row[k + G];
+            const float4 p0 = spos[j0], p1 = spos[j1];
+            float u0[8], u1[8];
+            load8(u8, j0, u0);
+            load8(u8, j1, u1);
+            const float3 s0 = sep(P, pi, p0), s1 = sep(P, pi, p1);
+            const float r0 = s0.x * s0.x + s0.y * s0.y + s0.z * s0.z;
+            const float r1 = s1.x * s1.x + s1.y * s1.y + s1.z * s1.z;
+            if (r0 <= P.cut2)
+               ufield_i(P, r0, s0, 1.f, pi.w, pti, p0.w, u0[6], u0, f);
+            if (r1 <= P.cut2)
+               ufield_i(P, r1, s1, 1.f, pi.w, pti, p1.w, u1[6], u1, f);
+         }
+         if (k < cnt) {
+            const int j = row[k];
+            const float4 pk = spos[j];
+            const float3 d = sep(P, pi, pk);
+            const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
+            if (r2 <= P.cut2) {
+               float uk[8];
+               load8(u8, j, uk);
+               ufield_i(P, r2, d, 1.f, pi.w, pti, pk.w, uk[6], uk, f);
+            }
+         }
+      }
+      const int pa = sp_start[i], pb = sp_start[i + 1];
+      for (int q = pa + g; q < pb; q += G) {
+         const int j = sp_j[q];
+         const float4 pk = spos[j];
+         const float3 d = sep(P, pi, pk);
+         const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
+         if (r2 <= P.cut2) {
+            float uk[8];
+            load8(u8, j, uk);
+            ufield_i(P, r2, d, sp_sc[q].w, pi.w, pti, pk.w, uk[6], uk, f);
+         }
+      }
+   }
+   pdl_trigger();
+   group_reduce<G, 6>(f);
+   store6<G>(out8, i < P.n ? base8 : nullptr, i, g, f);
+}
+
+// the preconditioner row of slot i, rows from the staged buffers
+template <int G>
+__device__ __forceinline__ void precond_row_stg(const PairParams& P, int i, int g, const unsigned char* stg, float* f,
+   const unsigned short* __restrict__ nbr_l, const int* __restrict__ nnbr, const int* __restrict__ sp_start,
+   const int* __restrict__ sp_j, const float4* __restrict__ sp_sc, const float4* __restrict__ spos,
+   const float* __restrict__ r8)
+{
+#pragma unroll
+   for (int c = 0; c < 6; ++c)
+      f[c] = 0.f;
+   const float poli = r8[8 * i + 7];
+   if (i < P.n) {
+      const float4 pi = spos[i];
+      const float pti = r8[8 * i + 6];
+      const unsigned short* row = nbr_l + (size_t)i * P.cap;
+      const int cnt = nnbr[i];
+      int k = g;
+      for (; k + G < cnt; k += 2 * G) {
+         float4 p0, p1;
+         float r0v[8], r1v[8];
+         staged_row(stg, row[k], p0, r0v);
+         staged_row(stg, row[k + G], p1, r1v);
+         const float3 s0 = sep(P, pi, p0), s1 = sep(P, pi, p1);
+         const float q0 = s0.x * s0.x + s0.y * s0.y + s0.z * s0.z;
+         const float q1 = s1.x * s1.x + s1.y * s1.y + s1.z * s1.z;
+         if (q0 <= P.cut2)
+            precond_i(P, q0, s0, 1.f, poli, pi.w, pti, p0.w, r0v, f);
+         if (q1 <= P.cut2)
+            precond_i(P, q1, s1, 1.f, poli, pi.w, pti, p1.w, r1v, f);
+      }
+      if (k < cnt) {
+         float4 pk;
+         float rk[8];
+         staged_row(stg, row[k], pk, rk);
+         const float3 d = sep(P, pi, pk);
+         const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
+         if (r2 <= P.cut2)
+            precond_i(P, r2, d, 1.f, poli, pi.w, pti, pk.w, rk, f);
+      }
+      const int pa = sp_start[i], pb = sp_start[i + 1];
+      for (int q = pa + g; q < pb; q += G) {
+         const int j = sp_j[q];
+         const float4 pk = spos[j];
+         const float3 d = sep(P, pi, pk);
+         const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
+         if (r2 <= P.cut2) {
+            float rk[8];
+            load8(r8, j, rk);
+            precond_i(P, r2, d, sp_sc[q].w, poli, pi.w, pti, pk.w, rk, f);
+         }
+      }
+   }
+   group_reduce<G, 6>(f);
+}
+
+// z = M r with the r.z / r.r partial sums and, in the last block, the CG
+// scalars (k_precond_sparse_dots), one 32-slot block per CTA pass; a CTA
+// takes blocks blockIdx.x, + gridDim.x, ... (at most RED_MAX CTAs), the
+// staging mbarrier's phase flipping with each staged pass.
+template <int G>
+__global__ void __launch_bounds__(32 * G) k_precond_dots_stg(PairParams P, int nblk, float udiag,
+   const int* __restrict__ nbr, const unsigned short* __restrict__ nbr_l, const int* __restrict__ nnbr,
+   const int* __restrict__ jbl, const int* __restrict__ jbn, const int* __restrict__ sp_start,
+   const int* __restrict__ sp_j, const float4* __restrict__ sp_sc, const float4* __restrict__ spos,
+   const float* __restrict__ r8, float* __restrict__ z8, PcgDots D, int* __restrict__ err)
+{
+   pdl_wait();
+   extern __shared__ __align__(128) unsigned char stg[];
+   __shared__ __align__(8) unsigned long long bar;
+   __shared__ double sh[64];
+   const unsigned bar_s = (unsigned)__cvta_generic_to_shared(&bar);
+   if (threadIdx.x == 0)
+      mbar_init(bar_s, 1);
+   __syncthreads();
+   const int g = threadIdx.x % G;
+   float rz_d = 0.f, rz_p = 0.f, rr_d = 0.f, rr_p = 0.f;
+   unsigned phase = 0;
+   for (int blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
+      const int i = blk * 32 + threadIdx.x / G;
+      const int nj = jbn[blk];
+      float f[6];
+      if (nj <= STAGE_JB_CAP) {
+         __syncthreads();  // the previous pass has read the buffers
+         stage_rows(stg, bar_s, phase, jbl + (size_t)blk * STAGE_JB_CAP, nj, spos, r8, err);
+         phase ^= 1u;
+         precond_row_stg<G>(P, i, g, stg, f, nbr_l, nnbr, sp_start, sp_j, sp_sc, spos, r8);
+      } else {
+         precond_row<G>(P, i, g, f, nbr, nnbr, sp_start, sp_j, sp_sc, spos, r8);
+      }
+      const float poli = r8[8 * i + 7];
+#pragma unroll
+      for (int c0 = 0; c0 < 6; c0 += G) {
+         const int c = c0 + g;
+         if (c < 6) {
+            const float r = r8[8 * i + c];
+            const float z = udiag * poli * r + pick6(f, c);
+            z8[8 * i + c] = z;
+            if (D.init)
+               D.conj[8 * i + c] = z;
+            if (c < 3) {
+               rz_d += r * z;
+               rr_d += r * r;
+            } else {
+               rz_p += r * z;
+               rr_p += r * r;
+            }
+         }
+      }
+   }
+   const float pv[4] = {rz_d, rz_p, rr_d, rr_p};
+   pdl_trigger();
+   store_partials_f<4>(D.red, R_RZ_D, pv, sh);
+   if (!last_block(D.state + ST_TICKET0))
+      return;
+   double tot[4];
+   sum_slots_bd(D.red, R_RZ_D, 4, gridDim.x, sh, tot);
+   if (threadIdx.x == 0)
+      pcg_scalars(tot, D.scal, D.state, D.init, D.n, D.debye, D.poleps, D.politer, D.miniter, D.handle,
+         D.use_handle);
+}
+
+// ---------------------------------------------------------------------------
 // permanent-multipole energy, real space (pair_mpole energy terms,
 // include/seq/pair_mpole.h:62-152); exclusion correction (m - 1) x bare pair
 // as the reference's exclusion loop does (src/cu/amoeba/empole_cu1.cc:110)
@@ -602,19 +879,35 @@ __global__ void __launch_bounds__(256) k_empole_real(PairParams P, int npad, flo
 static constexpr int PAIR_THREADS = 256;
 
 // ---------------------------------------------------------------------------
-// Per-step sub-lists: warp per atom, each row of the (reused, buffered) list
-// is filtered into the pairs within the cutoff and those within the
-// preconditioner cutoff, in the row's order (ballot compaction), so the field
-// and preconditioner kernels visit only pairs they use.  The kernels repeat
-// the same r^2 test with the same arithmetic.
-__global__ void __launch_bounds__(256) k_list_filter(PairParams P, float cutp2, int npad, const int* __restrict__ nbr,
+// Per-step sub-lists: one CTA per 32-slot block, warp w filtering the row of
+// slot 32 b + w.  Each row of the (reused, buffered) list is filtered into
+// the pairs within the cutoff and those within the preconditioner cutoff, in
+// the row's order (ballot compaction), so the field and preconditioner
+// kernels visit only pairs they use; the kernels repeat the same r^2 test
+// with the same arithmetic.  STAGE: the block also records which 32-slot
+// j-blocks its entries fall in (a bitmap over all blocks in shared memory),
+// lists them in ascending order, and rewrites every entry as a local index
+// into that list (position x 32 + slot within the j-block), which is where
+// the staged kernels find the row in shared memory.
+template <bool STAGE>
+__global__ void __launch_bounds__(1024) k_list_filter(PairParams P, float cutp2, int npad, const int* __restrict__ nbr,
    const int* __restrict__ nnbr, const float4* __restrict__ spos, int* __restrict__ nbrc, int* __restrict__ nnbrc,
-   int* __restrict__ nbrp, int* __restrict__ nnbrp)
+   int* __restrict__ nbrp, int* __restrict__ nnbrp, int* __restrict__ jbl, int* __restrict__ jbn,
+   unsigned short* __restrict__ nbrc_l, unsigned short* __restrict__ nbrp_l)
 {
-   const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-   const int lane = threadIdx.x & 31;
-   if (i >= npad)
-      return;
+   extern __shared__ unsigned bits_sm[];
+   __shared__ int total_sm;
+   const int words = (npad / 32 + 31) / 32;
+   unsigned* bm = bits_sm;
+   int* pre = reinterpret_cast<int*>(bits_sm + words);
+   if (STAGE) {
+      for (int w = threadIdx.x; w < words; w += blockDim.x)
+         bm[w] = 0u;
+      __syncthreads();
+   }
+   const int blk = blockIdx.x;
+   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+   const int i = blk * 32 + warp;
    int oc = 0, op = 0;
    if (i < P.n) {
       const float4 pi = spos[i];
@@ -639,6 +932,8 @@ __global__ void __launch_bounds__(256) k_list_filter(PairParams P, float cutp2, 
             rc[oc + __popc(mc & lt)] = j;
          if (inp)
             rp[op + __popc(mp & lt)] = j;
+         if (STAGE && (inc || inp))
+            atomicOr(&bm[j >> 10], 1u << ((j >> 5) & 31));
          oc += __popc(mc);
          op += __popc(mp);
       }
@@ -647,6 +942,61 @@ __global__ void __launch_bounds__(256) k_list_filter(PairParams P, float cutp2, 
       nnbrc[i] = oc;
       nnbrp[i] = op;
    }
+   if (!STAGE)
+      return;
+   __syncthreads();
+   // set bits before each word, and the block's j-block list
+   if (warp == 0) {
+      int run = 0;
+      for (int w0 = 0; w0 < words; w0 += 32) {
+         const int w = w0 + lane;
+         const int c = w < words ? __popc(bm[w]) : 0;
+         int incl = c;
+#pragma unroll
+         for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o)
+               incl += t;
+         }
+         if (w < words)
+            pre[w] = run + incl - c;
+         run += __shfl_sync(0xffffffffu, incl, 31);
+      }
+      if (lane == 0) {
+         total_sm = run;
+         jbn[blk] = run;
+      }
+   }
+   __syncthreads();
+   const int total = total_sm;
+   if (total > STAGE_JB_CAP)
+      return;  // this block reads its rows from global memory
+   for (int w = threadIdx.x; w < words; w += blockDim.x) {
+      unsigned m = bm[w];
+      int q = pre[w];
+      while (m) {
+         const int b = __ffs(m) - 1;
+         jbl[(size_t)blk * STAGE_JB_CAP + q] = w * 32 + b;
+         ++q;
+         m &= m - 1u;
+      }
+   }
+   if (i < P.n) {
+      const int* rc = nbrc + (size_t)i * P.cap;
+      const int* rp = nbrp + (size_t)i * P.cap;
+      unsigned short* lc = nbrc_l + (size_t)i * P.cap;
+      unsigned short* lp = nbrp_l + (size_t)i * P.cap;
+      for (int k = lane; k < oc; k += 32) {
+         const int j = rc[k], jb = j >> 5;
+         const int q = pre[jb >> 5] + __popc(bm[jb >> 5] & ((1u << (jb & 31)) - 1u));
+         lc[k] = (unsigned short)(q * 32 + (j & 31));
+      }
+      for (int k = lane; k < op; k += 32) {
+         const int j = rp[k], jb = j >> 5;
+         const int q = pre[jb >> 5] + __popc(bm[jb >> 5] & ((1u << (jb & 31)) - 1u));
+         lp[k] = (unsigned short)(q * 32 + (j & 31));
+      }
+   }
 }
 
 int launch_list_filter(Context* ctx)
@@ -654,8 +1004,15 @@ int launch_list_filter(Context* ctx)
    PairParams P = make_params(ctx, ctx->cfg.cutoff);
    const double cp = ctx->cfg.usolve_cutoff + ctx->cfg.pbuffer;
    const float cutp2 = cp * cp > 3.0e38 ? 3.0e38f : (float)(cp * cp);
-   k_list_filter<<<grid_for((long long)ctx->npad * 32, 256), 256, 0, ctx->stream>>>(P, cutp2, ctx->npad, ctx->nbr,
-      ctx->nnbr, ctx->spos, ctx->nbrc, ctx->nnbrc, ctx->nbrp, ctx->nnbrp);
+   const int nblk = ctx->npad / 32;
+   const int words = (nblk + 31) / 32;
+   const size_t smem = sizeof(unsigned) * 2 * (size_t)words;
+   if (ctx->pair_staged)
+      k_list_filter<true><<<nblk, 1024, smem, ctx->stream>>>(P, cutp2, ctx->npad, ctx->nbr, ctx->nnbr, ctx->spos,
+         ctx->nbrc, ctx->nnbrc, ctx->nbrp, ctx->nnbrp, ctx->jbl, ctx->jbn, ctx->nbrc_l, ctx->nbrp_l);
+   else
+      k_list_filter<false><<<nblk, 1024, 0, ctx->stream>>>(P, cutp2, ctx->npad, ctx->nbr, ctx->nnbr, ctx->spos,
+         ctx->nbrc, ctx->nnbrc, ctx->nbrp, ctx->nnbrp, ctx->jbl, ctx->jbn, ctx->nbrc_l, ctx->nbrp_l);
    T9_CUDA(cudaGetLastError());
    return T9GB_OK;
 }
@@ -690,10 +1047,36 @@ int launch_list_filter(Context* ctx)
          KERNEL<16, ARG><<<nb_, PAIR_THREADS, 0, ctx->stream>>>(__VA_ARGS__);                                          \
    } while (0)
 
+// the staged kernels: 4 or 8 lanes per atom
+static bool staged_lanes(const Context* ctx)
+{
+   return ctx->pair_staged && (ctx->pair_lanes == 4 || ctx->pair_lanes == 8);
+}
+
+int pair_staging_setup()
+{
+   const int bytes = (int)STAGE_SMEM;
+   if (cudaFuncSetAttribute(k_ufield_stg<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess ||
+      cudaFuncSetAttribute(k_ufield_stg<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess ||
+      cudaFuncSetAttribute(k_precond_dots_stg<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) !=
+         cudaSuccess ||
+      cudaFuncSetAttribute(k_precond_dots_stg<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess)
+      return T9GB_CUDA_ERR;
+   return T9GB_OK;
+}
+
 int launch_ufield_real(Context* ctx, const float* u6, const float* base6, float* out6)
 {
    PairParams P = make_params(ctx, ctx->cfg.cutoff);
    prof_begin(ctx, P_UFIELD_REAL);
+   if (staged_lanes(ctx)) {
+      auto k = ctx->pair_lanes == 8 ? k_ufield_stg<8> : k_ufield_stg<4>;
+      T9_CUDA(launch_k(use_pdl(ctx), k, ctx->npad / 32, 32 * ctx->pair_lanes, STAGE_SMEM, ctx->stream, P, ctx->nbrc,
+         ctx->nbrc_l, ctx->nnbrc, ctx->jbl, ctx->jbn, ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos, u6, base6, out6,
+         ctx->copy_err));
+      prof_end(ctx);
+      return T9GB_OK;
+   }
    const int g = ctx->pair_lanes;
    const int nb = grid_for((long long)ctx->npad * g, PAIR_THREADS);
    auto k = g == 4 ? k_ufield_real<4, false> : g == 8 ? k_ufield_real<8, false> : g == 32 ? k_ufield_real<32, false>
@@ -735,6 +1118,15 @@ int launch_precond_sparse_dots(Context* ctx, const float* r6, float* z6, const P
    const int per = PAIR_THREADS / g;
    const int nb = std::min(RED_MAX, (ctx->npad + per - 1) / per);
    prof_begin(ctx, P_PRECOND);
+   if (staged_lanes(ctx)) {
+      const int nblk = ctx->npad / 32;
+      auto ks = g == 8 ? k_precond_dots_stg<8> : k_precond_dots_stg<4>;
+      T9_CUDA(launch_k(use_pdl(ctx), ks, std::min(RED_MAX, nblk), 32 * g, STAGE_SMEM, ctx->stream, P, nblk,
+         (float)ctx->cfg.udiag, ctx->nbrp, ctx->nbrp_l, ctx->nnbrp, ctx->jbl, ctx->jbn, ctx->sp_start, ctx->sp_j,
+         ctx->sp_sc, ctx->spos, r6, z6, D, ctx->copy_err));
+      prof_end(ctx);
+      return T9GB_OK;
+   }
    auto k = g == 4 ? k_precond_sparse_dots<4> : g == 8 ? k_precond_sparse_dots<8> : g == 32
          ? k_precond_sparse_dots<32> : k_precond_sparse_dots<16>;
    T9_CUDA(launch_k(use_pdl(ctx), k, nb, PAIR_THREADS, 0, ctx->stream, P, ctx->npad, (float)ctx->cfg.udiag, ctx->nbrp,

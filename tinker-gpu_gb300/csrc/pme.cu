@@ -783,15 +783,182 @@ __global__ void __launch_bounds__(16 * fft_threads_per_line<N>()) k_fft_zline(co
       g[base + (size_t)(ez + r * ZS) * zs + ex] = sm[fsig<T>(ez + r * ZS) * LD + ex];
 }
 
+// ---------------------------------------------------------------------------
+// The same 2-D plane transform spread over a thread-block cluster of CL CTAs
+// per z plane (N CL CTAs in all).  CTA r of the cluster stages rows
+// [r R, r R + R) of the plane (R = N / CL), one contiguous R N-word slab,
+// with one bulk asynchronous copy (cp.async.bulk, completion on an mbarrier
+// with a bounded wait), transforms them along x, and after a cluster barrier
+// gathers columns [r R, r R + R) of the whole plane from the R-row tiles of
+// the CL CTAs through distributed shared memory; it transforms those along y
+// and stores them.  The per-line arithmetic is fft_line's, in the same order
+// as k_fft_plane, so the results are bit-identical to it.
+template <int N, int CL>
+struct PlaneCl {
+   static constexpr int T = fft_threads_per_line<N>();
+   static constexpr int R = N / CL;           // rows (and columns) per CTA
+   static constexpr int NT = R * T;           // threads
+   static constexpr int LDR = N + 2;          // row tile pitch (float2)
+   static constexpr int LDC = R + 1;          // column tile pitch
+   static constexpr int PER = R * N / NT;     // elements per thread in a tile copy
+   static constexpr size_t STAGE = (size_t)R * N * 8;  // bytes of the staged slab
+   static constexpr size_t SMEM = STAGE + sizeof(float2) * ((size_t)R * LDR + (size_t)N * LDC + 128) + 16;
+};
+
+template <int N, int CL, bool FROM_FX, bool INV>
+__global__ void __launch_bounds__(PlaneCl<N, CL>::NT) k_fft_plane_cl(long long* __restrict__ qfx,
+   float2* __restrict__ g, int packed, float inv, int* __restrict__ err)
+{
+   using C = PlaneCl<N, CL>;
+   constexpr int T = C::T, R = C::R, NT = C::NT, LDR = C::LDR, LDC = C::LDC, PER = C::PER;
+   extern __shared__ __align__(128) unsigned char smem_raw[];
+   unsigned long long* stage = reinterpret_cast<unsigned long long*>(smem_raw);
+   float2* rowt = reinterpret_cast<float2*>(smem_raw + C::STAGE);
+   float2* colt = rowt + R * LDR;
+   float2* tw = colt + N * LDC;
+   unsigned long long* bar = reinterpret_cast<unsigned long long*>(tw + 128);
+   unsigned rank;
+   asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(rank));
+   const int z = blockIdx.x / CL;
+   const size_t base = (size_t)z * N * N + (size_t)rank * R * N;  // first word of this CTA's rows
+   const unsigned bar_s = (unsigned)__cvta_generic_to_shared(bar);
+   const unsigned stage_s = (unsigned)__cvta_generic_to_shared(stage);
+   if (threadIdx.x == 0)
+      mbar_init(bar_s, 1);
+   __syncthreads();
+   if (threadIdx.x == 0) {
+      const void* src = FROM_FX ? static_cast<const void*>(qfx + base) : static_cast<const void*>(g + base);
+      mbar_expect_tx(bar_s, (unsigned)C::STAGE);
+      bulk_g2s(stage_s, src, (unsigned)C::STAGE, bar_s);
+   }
+   for (int k = threadIdx.x; k < 128; k += NT)
+      tw[k] = c_tw[k];
+   if (!mbar_wait_bounded(bar_s, 0)) {
+      // the copy never completed: record it, wait once more for it, go on
+      if (threadIdx.x == 0)
+         atomicExch(err, 1);
+      mbar_wait_bounded(bar_s, 0);
+   }
+   // staged slab -> row tile (element e: row e / N, column e % N)
+#pragma unroll
+   for (int k = 0; k < PER; ++k) {
+      const int e = threadIdx.x + k * NT;
+      float2 v;
+      if (FROM_FX)
+         v = grid_word((long long)stage[e], packed, inv);
+      else
+         v = reinterpret_cast<const float2*>(stage)[e];
+      rowt[(e / N) * LDR + fsig<T>(e % N)] = v;
+   }
+   if (FROM_FX) {
+      // the fixed-point slab is cleared for the next spread
+      long long* q = qfx + base;
+#pragma unroll
+      for (int k = 0; k < PER; ++k)
+         q[threadIdx.x + k * NT] = 0;
+   }
+   __syncthreads();
+   const int line = threadIdx.x / T, t = threadIdx.x % T;
+   float2 wt[N / T];
+   fft_twiddles<N, T>(t, tw, wt);
+   fft_line<N, T, INV>(rowt + line * LDR, 1, t, tw, wt);  // row rank R + line, along x
+   // every CTA's rows transformed before any column gather
+   asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+   // columns [rank R, rank R + R) of all N rows, from the owners' row tiles;
+   // all PER remote loads are issued before any store
+   const unsigned rowt_s = (unsigned)__cvta_generic_to_shared(rowt);
+   float2 v[PER];
+#pragma unroll
+   for (int k = 0; k < PER; ++k) {
+      const int e = threadIdx.x + k * NT;
+      const int y = e / R, xl = e % R;
+      const unsigned owner = (unsigned)(y / R);
+      const unsigned local = rowt_s + (unsigned)(((y % R) * LDR + fsig<T>((int)rank * R + xl)) * sizeof(float2));
+      unsigned remote;
+      asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(remote) : "r"(local), "r"(owner));
+      // volatile keeps the loads after the cluster barrier; no memory clobber, so they pipeline
+      asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v[k].x), "=f"(v[k].y) : "r"(remote));
+   }
+#pragma unroll
+   for (int k = 0; k < PER; ++k) {
+      const int e = threadIdx.x + k * NT;
+      colt[fsig<T>(e / R) * LDC + e % R] = v[k];
+   }
+   __syncthreads();
+   fft_line<N, T, INV>(colt + line, LDC, t, tw, wt);  // column rank R + line, along y
+   __syncthreads();
+   float2* out = g + (size_t)z * N * N + (size_t)rank * R;
+#pragma unroll
+   for (int k = 0; k < PER; ++k) {
+      const int e = threadIdx.x + k * NT;
+      const int y = e / R, xl = e % R;
+      out[(size_t)y * N + xl] = colt[fsig<T>(y) * LDC + xl];
+   }
+   // no CTA leaves while a peer may still read its row tile
+   asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+template <int N, int CL, bool FROM_FX, bool INV>
+static cudaError_t launch_plane_cl(long long* qfx, float2* g, int packed, float inv, int* err, cudaStream_t st)
+{
+   using C = PlaneCl<N, CL>;
+   cudaLaunchConfig_t cfg = {};
+   cfg.gridDim = dim3(N * CL);
+   cfg.blockDim = dim3(C::NT);
+   cfg.dynamicSmemBytes = C::SMEM;
+   cfg.stream = st;
+   cudaLaunchAttribute at[1];
+   at[0].id = cudaLaunchAttributeClusterDimension;
+   at[0].val.clusterDim.x = CL;
+   at[0].val.clusterDim.y = 1;
+   at[0].val.clusterDim.z = 1;
+   cfg.attrs = at;
+   cfg.numAttrs = 1;
+   return cudaLaunchKernelEx(&cfg, k_fft_plane_cl<N, CL, FROM_FX, INV>, qfx, g, packed, inv, err);
+}
+
+template <int N, int CL>
+static int plane_cl_setup(Context* ctx)
+{
+   const int bytes = (int)PlaneCl<N, CL>::SMEM;
+   T9_CUDA(cudaFuncSetAttribute(k_fft_plane_cl<N, CL, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+      bytes));
+   T9_CUDA(cudaFuncSetAttribute(k_fft_plane_cl<N, CL, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+      bytes));
+   return T9GB_OK;
+}
+
 template <int N>
 static size_t fft_plane_smem()
 {
    return sizeof(float2) * ((size_t)N * fft_plane_ld<N>() + 128);
 }
 
+// plane pass with clusters of P.fft_cl CTAs (0: one CTA per plane)
+template <int N, bool FROM_FX, bool INV>
+static void plane_pass(const PmeGrid& P, cudaStream_t st, int packed, float inv, bool pdl)
+{
+   constexpr int T = fft_threads_per_line<N>();
+   if (P.fft_cl == 2)
+      launch_plane_cl<N, 2, FROM_FX, INV>(P.qfx, P.qgrid, packed, inv, P.fft_err, st);
+   else if (P.fft_cl == 4)
+      launch_plane_cl<N, 4, FROM_FX, INV>(P.qfx, P.qgrid, packed, inv, P.fft_err, st);
+   else if (P.fft_cl == 8)
+      launch_plane_cl<N, 8, FROM_FX, INV>(P.qfx, P.qgrid, packed, inv, P.fft_err, st);
+   else
+      launch_k(pdl, k_fft_plane<N, FROM_FX, INV>, N, N * T, fft_plane_smem<N>(), st, P.qfx, P.qgrid, packed, inv);
+}
+
+
 template <int N>
 static int fft_setup_kernels(Context* ctx)
 {
+   int rc = plane_cl_setup<N, 2>(ctx);
+   if (rc == T9GB_OK)
+      rc = plane_cl_setup<N, 4>(ctx);
+   if (rc == T9GB_OK && N >= 64)
+      rc = plane_cl_setup<N, 8>(ctx);
+   T9_CHECK(rc);
    const int bytes = (int)fft_plane_smem<N>();
    void (*fwd)(long long*, float2*, int, float) = k_fft_plane<N, true, false>;
    void (*inv)(long long*, float2*, int, float) = k_fft_plane<N, false, true>;
@@ -805,8 +972,7 @@ template <int N>
 static void fft_own_forward(const PmeGrid& P, cudaStream_t st, bool split, bool pdl)
 {
    constexpr int T = fft_threads_per_line<N>();
-   launch_k(pdl, k_fft_plane<N, true, false>, N, N * T, fft_plane_smem<N>(), st, P.qfx, P.qgrid, P.packed ? 1 : 0,
-      1.0f / (float)(1 << P.pack_shift));
+   plane_pass<N, true, false>(P, st, P.packed ? 1 : 0, 1.0f / (float)(1 << P.pack_shift), pdl);
    if (split)
       launch_k(pdl, k_fft_zline<N, 0>, N * N / 16, 16 * T, 0, st, P.infl, P.qgrid);
    else
@@ -819,7 +985,7 @@ static void fft_own_inverse(const PmeGrid& P, cudaStream_t st, bool split, bool 
    constexpr int T = fft_threads_per_line<N>();
    if (split)
       launch_k(pdl, k_fft_zline<N, 1>, N * N / 16, 16 * T, 0, st, P.infl, P.qgrid);
-   launch_k(pdl, k_fft_plane<N, false, true>, N, N * T, fft_plane_smem<N>(), st, P.qfx, P.qgrid, 0, 0.f);
+   plane_pass<N, false, true>(P, st, 0, 0.f, pdl);
 }
 
 // ---------------------------------------------------------------------------
@@ -1281,6 +1447,8 @@ int pme_setup(Context* ctx)
    T9_CUDA(cudaMalloc(&d_infl, sizeof(float) * ng));
    T9_CUDA(cudaMemcpy(d_infl, infl.data(), sizeof(float) * ng, cudaMemcpyHostToDevice));
    P.infl = d_infl;
+   T9_CUDA(cudaMalloc(&P.fft_err, sizeof(int)));
+   T9_CUDA(cudaMemset(P.fft_err, 0, sizeof(int)));
    if (cufftPlan3d(&P.plan, P.n3, P.n2, P.n1, CUFFT_C2C) != CUFFT_SUCCESS ||
       cufftPlan3d(&P.plan2, P.n3, P.n2, P.n1, CUFFT_C2C) != CUFFT_SUCCESS) {
       ctx->last_error = "cufftPlan3d failed";
@@ -1320,6 +1488,7 @@ void pme_free(Context* ctx)
    cudaFree(P.qfx);
    cudaFree(P.infl);
    cudaFree(P.qstash);
+   cudaFree(P.fft_err);
    P = PmeGrid();
 }
 

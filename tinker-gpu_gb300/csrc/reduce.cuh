@@ -75,6 +75,44 @@ static __device__ __forceinline__ void sum_slots(const double* red, int first, i
    __syncthreads();
 }
 
+// sum_slots for blocks of 128 or 256 threads: blockDim / 4 threads per slot
+// (ns <= 4), the same fixed order for a given block size
+static __device__ __forceinline__ void sum_slots_bd(const double* red, int first, int ns, int nb, double* sh,
+   double* out)
+{
+   const int per = blockDim.x >> 2, wps = per >> 5;
+   const int slot = threadIdx.x / per, sub = threadIdx.x % per;
+   double v = 0;
+   if (slot < ns) {
+      const double* p = red + (first + slot) * RED_MAX;
+      int i = sub;
+      for (; i + 7 * per < nb; i += 8 * per) {
+         double t[8];
+#pragma unroll
+         for (int k = 0; k < 8; ++k)
+            t[k] = p[i + k * per];
+#pragma unroll
+         for (int k = 0; k < 8; ++k)
+            v += t[k];
+      }
+      for (; i < nb; i += per)
+         v += p[i];
+   }
+#pragma unroll
+   for (int o = 16; o > 0; o >>= 1)
+      v += __shfl_down_sync(0xffffffffu, v, o);
+   if ((threadIdx.x & 31) == 0)
+      sh[threadIdx.x >> 5] = v;
+   __syncthreads();
+   for (int k = 0; k < ns; ++k) {
+      double t = 0;
+      for (int w = 0; w < wps; ++w)
+         t += sh[k * wps + w];
+      out[k] = t;
+   }
+   __syncthreads();
+}
+
 // store this block's partial sum of v
 static __device__ __forceinline__ void store_partial(double* red, int slot, double v, double* sh)
 {
