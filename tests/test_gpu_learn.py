@@ -194,17 +194,25 @@ def test_tensor_core_forward_matches_oracle(gpu_lib, tg, LO):
     per 128 rows, a partial last tile here) gives the network outputs, loss
     and gradient within the same bar as the mma.sync path, and close to it."""
     s = tg.systems.make_config("water648")
-    e = engine_for(s)
-    e.learn_reset(seed=7)
-    w = e.learn_weights().astype(np.float64)
     rng = np.random.default_rng(8)
     rows = 1000
     x = rng.normal(size=(rows, 32)).astype(np.float32)
     t = rng.normal(size=(rows, 3)).astype(np.float32)
-    y0, g0, l0 = e.learn_eval(x, t)
+    # two contexts with the same weights, so neither reads the other's outputs
+    ref = engine_for(s)
+    ref.learn_reset(seed=7)
+    y0, g0, l0 = ref.learn_eval(x, t)
+    e = engine_for(s)
+    e.learn_reset(seed=7)
     e.learn_tensor_path(1)
+    w = e.learn_weights().astype(np.float64)
     y, g, loss = e.learn_eval(x, t)
     assert e.copy_error() == 0
+    # a second batch through the same context: new outputs, not the last call's
+    y2, _, _ = e.learn_eval(-x, t)
+    assert not np.array_equal(y2, y)
+    yo2, _, _ = LO.loss_grad(w, -x.astype(np.float64), t.astype(np.float64), bf=True)
+    assert np.linalg.norm(y2 - yo2) < NET_TOL * np.linalg.norm(yo2)
     yo, lo, go = LO.loss_grad(w, x.astype(np.float64), t.astype(np.float64), bf=True)
     print("tcgen05 vs mma.sync: y", float(np.linalg.norm(y - y0) / np.linalg.norm(y0)),
           "vs oracle", float(np.linalg.norm(y - yo) / np.linalg.norm(yo)))
