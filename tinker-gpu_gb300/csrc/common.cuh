@@ -574,7 +574,7 @@ int mlp_alloc(Context* ctx, int max_rows, unsigned seed);
 void mlp_free(Context* ctx);
 int mlp_set_weights(Context* ctx, const float* w_host);
 int mlp_get_weights(Context* ctx, float* w_host);
-int mlp_forward(Context* ctx, int rows);
+int mlp_forward(Context* ctx, int rows, bool act);
 int mlp_backward(Context* ctx, int rows, const float* rowpol, int npad);
 int mlp_adamw(Context* ctx, float lr, float wd);
 // learned guess (learn.cu)

@@ -265,7 +265,7 @@ int learn_forward(Context* ctx)
    k_normalize<<<grid_for(2LL * npad * 32, LB), LB, 0, ctx->stream>>>(npad, ctx->xf, ctx->spolar, ctx->fstat,
       ctx->mlp.x);
    T9_CUDA(cudaGetLastError());
-   return mlp_forward(ctx, 2 * npad);
+   return mlp_forward(ctx, 2 * npad, (ctx->learn_mode & 1) != 0);
 }
 
 int learn_guess(Context* ctx, float* ug8, int set_choice)

@@ -501,6 +501,9 @@ constexpr int TC_SX = 0, TC_SH1 = TC_SX + 128 * 32 * 2, TC_SH2 = TC_SH1 + 128 * 
 constexpr int TC_SW1 = TC_SH2 + 128 * 64 * 2, TC_SW2 = TC_SW1 + 64 * 32 * 2, TC_SW3 = TC_SW2 + 64 * 64 * 2;
 constexpr int TC_SMEM = TC_SW3 + 16 * 64 * 2;  // 55,296 bytes: at most four CTAs per SM, 4 x 128 TMEM columns
 
+// ACT: also store z1, h1, z2, h2 (the backward pass reads them); the
+// inference forward stores only y
+template <bool ACT>
 __global__ void __launch_bounds__(128) k_mlp_forward_tc(int rows, const __nv_bfloat16* __restrict__ x,
    const __nv_bfloat16* __restrict__ wb, const float* __restrict__ w, float* __restrict__ z1,
    __nv_bfloat16* __restrict__ h1, float* __restrict__ z2, __nv_bfloat16* __restrict__ h2, float* __restrict__ y,
@@ -530,16 +533,18 @@ __global__ void __launch_bounds__(128) k_mlp_forward_tc(int rows, const __nv_bfl
       const __nv_bfloat16 v = r0 + r < rows ? x[(size_t)(r0 + r) * MLP_IN + k] : __float2bfloat16(0.f);
       *reinterpret_cast<__nv_bfloat16*>(tsm + TC_SX + kmaj_off(r, k, MLP_IN)) = v;
    }
-   for (int e = tid; e < MLP_HID * MLP_IN; e += 128) {  // W1^T: (n, k) = W1[k][n]
-      const int n = e / MLP_IN, k = e % MLP_IN;
-      *reinterpret_cast<__nv_bfloat16*>(tsm + TC_SW1 + kmaj_off(n, k, MLP_IN)) = wb[BF_W1 + k * MLP_HID + n];
+   // the weights are read in memory order (W[k][n], n fastest: coalesced)
+   // and stored transposed, (n, k) = W[k][n]
+   for (int e = tid; e < MLP_IN * MLP_HID; e += 128) {
+      const int k = e / MLP_HID, n = e % MLP_HID;
+      *reinterpret_cast<__nv_bfloat16*>(tsm + TC_SW1 + kmaj_off(n, k, MLP_IN)) = wb[BF_W1 + e];
    }
    for (int e = tid; e < MLP_HID * MLP_HID; e += 128) {
-      const int n = e / MLP_HID, k = e % MLP_HID;
-      *reinterpret_cast<__nv_bfloat16*>(tsm + TC_SW2 + kmaj_off(n, k, MLP_HID)) = wb[BF_W2 + k * MLP_HID + n];
+      const int k = e / MLP_HID, n = e % MLP_HID;
+      *reinterpret_cast<__nv_bfloat16*>(tsm + TC_SW2 + kmaj_off(n, k, MLP_HID)) = wb[BF_W2 + e];
    }
-   for (int e = tid; e < 16 * MLP_HID; e += 128) {
-      const int n = e / MLP_HID, k = e % MLP_HID;
+   for (int e = tid; e < MLP_HID * 16; e += 128) {
+      const int k = e / 16, n = e % 16;
       *reinterpret_cast<__nv_bfloat16*>(tsm + TC_SW3 + kmaj_off(n, k, MLP_HID)) =
          n < MLP_OUT_PAD ? wb[BF_W3 + k * MLP_OUT_PAD + n] : __float2bfloat16(0.f);
    }
@@ -583,7 +588,7 @@ __global__ void __launch_bounds__(128) k_mlp_forward_tc(int rows, const __nv_bfl
             const int c = c0 + i;
             const float z = v[i] + b[c];
             const __nv_bfloat16 hv = __float2bfloat16(silu(z));
-            if (r < rows) {
+            if (ACT && r < rows) {
                zg[(size_t)r * MLP_HID + c] = z;
                hg[(size_t)r * MLP_HID + c] = hv;
             }
@@ -621,19 +626,25 @@ __global__ void __launch_bounds__(128) k_mlp_forward_tc(int rows, const __nv_bfl
 
 int mlp_tc_setup()
 {
-   return cudaFuncSetAttribute(k_mlp_forward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM) == cudaSuccess
+   return cudaFuncSetAttribute(k_mlp_forward_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM) ==
+            cudaSuccess &&
+         cudaFuncSetAttribute(k_mlp_forward_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM) ==
+            cudaSuccess
       ? T9GB_OK
       : T9GB_CUDA_ERR;
 }
 
-// forward over rows of S.x; outputs in S.y [rows][8]
-int mlp_forward(Context* ctx, int rows)
+// forward over rows of S.x; outputs in S.y [rows][8]; act: also the
+// activations the backward pass reads (the tcgen05 path leaves them out
+// otherwise; the mma.sync path always keeps them)
+int mlp_forward(Context* ctx, int rows, bool act)
 {
    MlpState& S = ctx->mlp;
    const __nv_bfloat16* wb = reinterpret_cast<const __nv_bfloat16*>(S.wb);
    if (ctx->mlp_tc) {
-      k_mlp_forward_tc<<<grid_for(rows, TC_ROWS), 128, TC_SMEM, ctx->stream>>>(rows, S.x, wb, S.w, S.z1, S.h1, S.z2,
-         S.h2, S.y, ctx->copy_err);
+      auto k = act ? k_mlp_forward_tc<true> : k_mlp_forward_tc<false>;
+      k<<<grid_for(rows, TC_ROWS), 128, TC_SMEM, ctx->stream>>>(rows, S.x, wb, S.w, S.z1, S.h1, S.z2, S.h2, S.y,
+         ctx->copy_err);
       T9_CUDA(cudaGetLastError());
       return T9GB_OK;
    }
