@@ -190,9 +190,10 @@ def test_learned_graph_matches_stepwise(gpu_lib, tg):
 
 
 def test_tensor_core_forward_matches_oracle(gpu_lib, tg, LO):
-    """The fused tcgen05 forward pass (tensor-memory accumulators, one CTA
-    per 128 rows, a partial last tile here) gives the network outputs, loss
-    and gradient within the same bar as the mma.sync path, and close to it."""
+    """The fused tcgen05 forward pass (the default; tensor-memory
+    accumulators, one CTA per 128 rows, a partial last tile here) gives the
+    network outputs, loss and gradient within the same bar as the mma.sync
+    path, and close to it."""
     s = tg.systems.make_config("water648")
     rng = np.random.default_rng(8)
     rows = 1000
@@ -200,6 +201,7 @@ def test_tensor_core_forward_matches_oracle(gpu_lib, tg, LO):
     t = rng.normal(size=(rows, 3)).astype(np.float32)
     # two contexts with the same weights, so neither reads the other's outputs
     ref = engine_for(s)
+    ref.learn_tensor_path(0)
     ref.learn_reset(seed=7)
     y0, g0, l0 = ref.learn_eval(x, t)
     e = engine_for(s)

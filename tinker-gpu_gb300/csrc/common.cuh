@@ -257,7 +257,7 @@ struct Context {
    unsigned short* nbrc_l = nullptr; // [npad][nbr_cap]
    unsigned short* nbrp_l = nullptr; // [npad][nbr_cap]
    bool pair_staged = false;         // t9gb_pair_staging
-   bool mlp_tc = false;              // learned guess: forward pass on tcgen05 (t9gb_learn_tensor_path)
+   bool mlp_tc = true;               // learned guess: forward pass on tcgen05 (t9gb_learn_tensor_path)
    int* copy_err = nullptr;          // device flag: a staging copy did not complete in time
    int* nbr_over = nullptr;  // device max count seen (overflow check)
    int* h_over = nullptr;    // pinned mirror

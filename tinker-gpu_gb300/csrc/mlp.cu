@@ -500,6 +500,10 @@ __device__ __forceinline__ void tc_ld16(unsigned taddr, float* v)
 constexpr int TC_SX = 0, TC_SH1 = TC_SX + 128 * 32 * 2, TC_SH2 = TC_SH1 + 128 * 64 * 2;
 constexpr int TC_SW1 = TC_SH2 + 128 * 64 * 2, TC_SW2 = TC_SW1 + 64 * 32 * 2, TC_SW3 = TC_SW2 + 64 * 64 * 2;
 constexpr int TC_SMEM = TC_SW3 + 16 * 64 * 2;  // 55,296 bytes: at most four CTAs per SM, 4 x 128 TMEM columns
+// with the activations kept: a [128][65] FP32 staging tile for coalesced
+// stores of z (88,576 bytes: at most two CTAs per SM)
+constexpr int TC_ZLD = MLP_HID + 1;
+constexpr int TC_SMEM_ACT = TC_SMEM + TC_ROWS * TC_ZLD * 4;
 
 // ACT: also store z1, h1, z2, h2 (the backward pass reads them); the
 // inference forward stores only y
@@ -577,7 +581,10 @@ __global__ void __launch_bounds__(128) k_mlp_forward_tc(int rows, const __nv_bfl
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
    };
 
-   // hidden layer epilogue: z = D + b, h = silu(z), also into the next operand tile
+   // hidden layer epilogue: z = D + b, h = silu(z) into the next operand
+   // tile; ACT: z through the staging tile, then z and h stored row-major
+   // with consecutive threads on consecutive columns
+   float* zst = reinterpret_cast<float*>(tsm + TC_SMEM);
    auto hidden = [&](unsigned dcol, const float* b, float* zg, __nv_bfloat16* hg, unsigned h_off) {
 #pragma unroll
       for (int c0 = 0; c0 < MLP_HID; c0 += 16) {
@@ -588,10 +595,8 @@ __global__ void __launch_bounds__(128) k_mlp_forward_tc(int rows, const __nv_bfl
             const int c = c0 + i;
             const float z = v[i] + b[c];
             const __nv_bfloat16 hv = __float2bfloat16(silu(z));
-            if (ACT && r < rows) {
-               zg[(size_t)r * MLP_HID + c] = z;
-               hg[(size_t)r * MLP_HID + c] = hv;
-            }
+            if (ACT)
+               zst[(32 * warp + lane) * TC_ZLD + c] = z;
             *reinterpret_cast<__nv_bfloat16*>(tsm + h_off + kmaj_off(32 * warp + lane, c, MLP_HID)) =
                r < rows ? hv : __float2bfloat16(0.f);
          }
@@ -600,6 +605,17 @@ __global__ void __launch_bounds__(128) k_mlp_forward_tc(int rows, const __nv_bfl
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       __syncthreads();
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      if (ACT) {
+         for (int e = tid; e < TC_ROWS * MLP_HID; e += 128) {
+            const int rl = e / MLP_HID, c = e % MLP_HID;
+            if (r0 + rl < rows) {
+               zg[(size_t)(r0 + rl) * MLP_HID + c] = zst[rl * TC_ZLD + c];
+               hg[(size_t)(r0 + rl) * MLP_HID + c] =
+                  *reinterpret_cast<const __nv_bfloat16*>(tsm + h_off + kmaj_off(rl, c, MLP_HID));
+            }
+         }
+         __syncthreads();  // the staging tile is reused by the next layer
+      }
    };
 
    layer(TC_SX, TC_SW1, MLP_IN, MLP_HID, 0);
@@ -626,7 +642,7 @@ __global__ void __launch_bounds__(128) k_mlp_forward_tc(int rows, const __nv_bfl
 
 int mlp_tc_setup()
 {
-   return cudaFuncSetAttribute(k_mlp_forward_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM) ==
+   return cudaFuncSetAttribute(k_mlp_forward_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_ACT) ==
             cudaSuccess &&
          cudaFuncSetAttribute(k_mlp_forward_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM) ==
             cudaSuccess
@@ -643,8 +659,8 @@ int mlp_forward(Context* ctx, int rows, bool act)
    const __nv_bfloat16* wb = reinterpret_cast<const __nv_bfloat16*>(S.wb);
    if (ctx->mlp_tc) {
       auto k = act ? k_mlp_forward_tc<true> : k_mlp_forward_tc<false>;
-      k<<<grid_for(rows, TC_ROWS), 128, TC_SMEM, ctx->stream>>>(rows, S.x, wb, S.w, S.z1, S.h1, S.z2, S.h2, S.y,
-         ctx->copy_err);
+      k<<<grid_for(rows, TC_ROWS), 128, act ? TC_SMEM_ACT : TC_SMEM, ctx->stream>>>(rows, S.x, wb, S.w, S.z1, S.h1,
+         S.z2, S.h2, S.y, ctx->copy_err);
       T9_CUDA(cudaGetLastError());
       return T9GB_OK;
    }
