@@ -35,7 +35,7 @@ extern "C" {
 #define T9GB_CUDA_ERR 4
 #define T9GB_NO_DEVICE 5
 #define T9GB_NOT_READY 6 /* topology / positions / list missing */
-#define T9GB_TOO_LARGE 7 /* more atoms than a fixed-capacity entry point holds */
+#define T9GB_TOO_LARGE 7 /* input above a fixed capacity: atoms of the no-alloc entry point, rows of t9gb_learn_eval */
 
 typedef struct t9gb_context t9gb_context;
 
@@ -349,9 +349,10 @@ int t9gb_pair_staging(t9gb_context* ctx, int enable);
 
 /* Device flags of the library's asynchronous copies, read after a
  * synchronisation: bit 0 a staging copy of the pair kernels, bit 1 a slab
- * copy of the transform's clustered plane passes did not complete within
- * the kernel's bounded wait (the kernel then went on and its results are
- * not valid).  Zero in normal operation. */
+ * copy of the transform's clustered plane passes, bit 2 a tensor-core
+ * product of the learned-guess network did not complete within the
+ * kernel's bounded wait (the kernel then went on and its results are not
+ * valid).  Zero in normal operation. */
 int t9gb_copy_error(t9gb_context* ctx, int* flag);
 
 /* Lanes of a warp that share one atom's neighbour row in the real-space
@@ -457,7 +458,8 @@ int t9gb_learn_get_weights(t9gb_context* ctx, float* w, int nparam);
 int t9gb_learn_set_weights(t9gb_context* ctx, const float* w, int nparam);
 /* Network forward and backward on caller rows, host arrays: x[rows][32]
  * (rounded to BF16), targets t[rows][3] -> y[rows][3], grad[T9GB_LEARN_NPARAM]
- * of the loss mean((y - t)^2), and the loss.  For gradient checks. */
+ * of the loss mean((y - t)^2), and the loss.  For gradient checks; rows at
+ * most 2 x the atom count rounded up to 32 (else T9GB_TOO_LARGE). */
 int t9gb_learn_eval(t9gb_context* ctx, int rows, const float* x, const float* t, float* y, float* grad,
    double* loss);
 /* One AdamW step (beta 0.9/0.999, eps 1e-8) with the gradient of the last

@@ -190,10 +190,10 @@ def test_learned_graph_matches_stepwise(gpu_lib, tg):
 
 
 def test_tensor_core_forward_matches_oracle(gpu_lib, tg, LO):
-    """The fused tcgen05 forward pass (the default; tensor-memory
-    accumulators, one CTA per 128 rows, a partial last tile here) gives the
-    network outputs, loss and gradient within the same bar as the mma.sync
-    path, and close to it."""
+    """The fused tcgen05 forward and backward passes (the default;
+    tensor-memory accumulators, one CTA per 128 rows, a partial last tile
+    here) give the network outputs, loss and gradient within the same bar as
+    the mma.sync path, and close to it."""
     s = tg.systems.make_config("water648")
     rng = np.random.default_rng(8)
     rows = 1000
@@ -222,6 +222,33 @@ def test_tensor_core_forward_matches_oracle(gpu_lib, tg, LO):
     assert abs(loss - lo) < NET_TOL * lo
     assert np.linalg.norm(g - go) < NET_TOL * np.linalg.norm(go)
     assert np.linalg.norm(y - y0) < NET_TOL * np.linalg.norm(y0)
+    # backward: every parameter block against the oracle and the mma.sync path
+    print("tcgen05 vs mma.sync: g", float(np.linalg.norm(g - g0) / np.linalg.norm(g0)))
+    assert abs(loss - l0) < NET_TOL * l0
+    for name, a, b, c in zip(["W1", "b1", "W2", "b2", "W3", "b3"], LO.unpack(g).values(), LO.unpack(go).values(),
+                             LO.unpack(g0).values()):
+        assert np.linalg.norm(a - b) <= NET_TOL * np.linalg.norm(b) + 1e-9, name
+        assert np.linalg.norm(a - c) <= NET_TOL * np.linalg.norm(c) + 1e-9, name
+    assert np.all(LO.unpack(g)["W3"][:, 3:] == 0) and np.all(LO.unpack(g)["b3"][3:] == 0)
+
+
+@pytest.mark.parametrize("rows", [1, 77, 128, 1300])
+def test_tensor_core_backward_tiles(gpu_lib, tg, LO, rows):
+    """Partial, single and many 128-row tiles of the fused backward pass
+    against the oracle (BF16 rounding emulated)."""
+    s = tg.systems.make_config("water648")
+    rng = np.random.default_rng(rows)
+    x = rng.normal(size=(rows, 32)).astype(np.float32)
+    t = rng.normal(size=(rows, 3)).astype(np.float32)
+    e = engine_for(s)
+    e.learn_reset(seed=3)
+    e.learn_tensor_path(1)
+    w = e.learn_weights().astype(np.float64)
+    y, g, loss = e.learn_eval(x, t)
+    assert e.copy_error() == 0
+    yo, lo, go = LO.loss_grad(w, x.astype(np.float64), t.astype(np.float64), bf=True)
+    assert abs(loss - lo) < NET_TOL * lo
+    assert np.linalg.norm(g - go) < NET_TOL * np.linalg.norm(go)
 
 
 def test_tensor_core_learned_solve(gpu_lib, oracle, tg):

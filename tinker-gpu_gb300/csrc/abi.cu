@@ -165,7 +165,7 @@ const char* t9gb_status_string(int status)
    case T9GB_NOT_READY:
       return "topology, coordinates or neighbour list missing";
    case T9GB_TOO_LARGE:
-      return "more atoms than the fixed-capacity entry point holds";
+      return "input larger than a fixed capacity";
    default:
       return "unknown status";
    }
@@ -640,7 +640,7 @@ int t9gb_copy_error(t9gb_context* h, int* flag)
    if (ctx->pme.fft_err)
       T9_CUDA(cudaMemcpyAsync(&b, ctx->pme.fft_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
    T9_CUDA(cudaStreamSynchronize(ctx->stream));
-   *flag = (a ? 1 : 0) | (b ? 2 : 0);
+   *flag = (a & 5) | (b ? 2 : 0);
    return T9GB_OK;
 }
 
@@ -749,8 +749,10 @@ int t9gb_learn_eval(t9gb_context* h, int rows, const float* x, const float* t, f
    Context* ctx = &h->c;
    T9_CHECK(learn_setup(ctx));
    MlpState& S = ctx->mlp;
-   if (rows > S.max_rows)
+   if (rows > S.max_rows) {
+      ctx->last_error = "more rows than the network's buffers hold (2 x the atom count rounded up to 32)";
       return T9GB_TOO_LARGE;
+   }
    std::vector<__nv_bfloat16> xb((size_t)rows * MLP_IN);
    for (size_t i = 0; i < xb.size(); ++i)
       xb[i] = __float2bfloat16(x[i]);

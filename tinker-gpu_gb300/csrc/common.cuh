@@ -131,6 +131,7 @@ struct MlpState {
    double* err = nullptr;        // [rows] squared error
    double* loss = nullptr;
    float* split = nullptr;       // split-K / column-sum partials
+   float* gpart = nullptr;       // [rows / 128][MLP_NPARAM] per-tile gradients (tcgen05 backward)
 };
 
 struct Context {

@@ -353,6 +353,7 @@ int mlp_alloc(Context* ctx, int max_rows, unsigned seed)
    T9_CUDA(cudaMalloc(&S.loss, sizeof(double)));
    S.nsplit = 128;
    T9_CUDA(cudaMalloc(&S.split, sizeof(float) * (size_t)std::max<size_t>(S.nsplit * MLP_HID * MLP_HID, 1024 * MLP_HID)));
+   T9_CUDA(cudaMalloc(&S.gpart, sizeof(float) * ((R + 127) / 128) * MLP_NPARAM));  // 128-row tiles
    return mlp_init(ctx, seed);
 }
 
@@ -392,7 +393,7 @@ void mlp_free(Context* ctx)
 {
    MlpState& S = ctx->mlp;
    void* p[] = {S.step, S.w, S.g, S.m, S.v, S.mask, S.wb_index, S.wb, S.x, S.z1, S.z2, S.h1, S.h2, S.c, S.y, S.t, S.dy,
-      S.dyf, S.dz, S.dzf, S.err, S.loss, S.split};
+      S.dyf, S.dz, S.dzf, S.err, S.loss, S.split, S.gpart};
    for (void* q : p)
       if (q)
          cudaFree(q);
@@ -442,7 +443,7 @@ int mlp_get_weights(Context* ctx, float* w_host)
 // mma.sync path (z1, h1, z2, h2, y), equal to them up to the order of the
 // FP32 accumulation inside the MMA.
 
-constexpr int TC_ROWS = 128;
+constexpr int TC_ROWS = 128;  // also the tile of S.gpart
 constexpr int TC_TMEM_COLS = 128;  // D1 in columns 0-63, D2 in 64-127, D3 in 0-15
 
 // byte offset of element (r, k) in a K-major no-swizzle tile with K columns
@@ -574,7 +575,7 @@ __global__ void __launch_bounds__(128) k_mlp_forward_tc(int rows, const __nv_bfl
          // record it, and give the MMAs in flight a second bounded wait
          // before their operands and accumulators are reused or freed
          if (tid == 0)
-            atomicExch(err, 1);
+            atomicOr(err, 4);
          mbar_wait_bounded(bar_s, phase);
       }
       phase ^= 1u;
@@ -640,14 +641,291 @@ __global__ void __launch_bounds__(128) k_mlp_forward_tc(int rows, const __nv_bfl
    }
 }
 
+// ---------------------------------------------------------------------------
+// Backward pass on tcgen05: one CTA of four warps per 128 rows computes the
+// loss gradient dY, the hidden deltas dZ2 = (dY W3^T) silu'(z2) and
+// dZ1 = (dZ2 W2^T) silu'(z1), and this tile's weight gradients
+// dW3 = H2^T dY, dW2 = H1^T dZ2, dW1 = X^T dZ1 (the transposed activations
+// padded to 128 rows, so every MMA has M = 128), plus the bias-gradient
+// column sums and the squared error; it writes them as one partial vector
+// per CTA, which k_grad_reduce adds in a fixed order.  The BF16 rounding
+// points are those of the mma.sync path (dY and the deltas rounded for the
+// products, kept in FP32 for the bias sums).
+constexpr int TB_SXT = 0;                              // X^T pad   [128][128]
+constexpr int TB_SH1T = TB_SXT + 128 * 128 * 2;        // H1^T pad  [128][128]
+constexpr int TB_SH2T = TB_SH1T + 128 * 128 * 2;       // H2^T pad  [128][128]
+constexpr int TB_SW3 = TB_SH2T + 128 * 128 * 2;        // W3 as B   [64][16]
+constexpr int TB_SW2 = TB_SW3 + 64 * 16 * 2;           // W2 as B   [64][64]
+constexpr int TB_SDY = TB_SW2 + 64 * 64 * 2;           // dY        [128][16]
+constexpr int TB_SDYT = TB_SDY + 128 * 16 * 2;         // dY^T      [16][128]
+constexpr int TB_SDZ = TB_SDYT + 16 * 128 * 2;         // dZ2       [128][64]
+constexpr int TB_SDZT = TB_SDZ + 128 * 64 * 2;         // dZ^T      [64][128]
+constexpr int TB_SZ = TB_SDZT + 64 * 128 * 2;          // z staging [128][65] f32
+constexpr int TB_SB = TB_SZ + 128 * TC_ZLD * 4;        // bias partials [4 warps][8 + 64 + 64] f32
+constexpr int TB_SMEM = TB_SB + 4 * (8 + 64 + 64) * 4; // 184,960 bytes: one CTA per SM
+static_assert(TB_SMEM == 184960, "backward tile layout");
+constexpr int TB_TMEM_COLS = 512;  // dH2 0-63, dW3 64-79, dH1 128-191, dW2 192-255, dW1 256-319
+
+// column sums of one value per lane and column over a warp (butterfly: every
+// lane ends with the sum; lane 0 stores it)
+template <int N>
+__device__ __forceinline__ void warp_colsum(const float* v, float* out, int lane)
+{
+#pragma unroll
+   for (int c = 0; c < N; ++c) {
+      float a = v[c];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1)
+         a += __shfl_xor_sync(0xffffffffu, a, o);
+      if (lane == 0)
+         out[c] = a;
+   }
+}
+
+__global__ void __launch_bounds__(128) k_mlp_backward_tc(int rows, int npad, const float* __restrict__ rowpol,
+   const __nv_bfloat16* __restrict__ x, const float* __restrict__ z1, const __nv_bfloat16* __restrict__ h1,
+   const float* __restrict__ z2, const __nv_bfloat16* __restrict__ h2, const float* __restrict__ y,
+   const float* __restrict__ t, const __nv_bfloat16* __restrict__ wb, float* __restrict__ gpart,
+   double* __restrict__ lpart, int* __restrict__ err)
+{
+   extern __shared__ __align__(128) unsigned char bsm[];
+   __shared__ __align__(8) unsigned long long bar;
+   __shared__ unsigned tmem_slot;
+   __shared__ double lsum[4];
+   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+   const int r0 = blockIdx.x * TC_ROWS;
+   const int rl = 32 * warp + lane, r = r0 + rl;  // this thread's row
+   const unsigned base = (unsigned)__cvta_generic_to_shared(bsm);
+   const unsigned bar_s = (unsigned)__cvta_generic_to_shared(&bar);
+   float* zst = reinterpret_cast<float*>(bsm + TB_SZ);
+   float* bpart = reinterpret_cast<float*>(bsm + TB_SB);
+   auto bf = [&](int off, int rr, int k, int K) -> __nv_bfloat16& {
+      return *reinterpret_cast<__nv_bfloat16*>(bsm + off + kmaj_off(rr, k, K));
+   };
+
+   if (warp == 0) {
+      asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                      (unsigned)__cvta_generic_to_shared(&tmem_slot)),
+                   "r"((unsigned)TB_TMEM_COLS)
+                   : "memory");
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+   }
+   if (tid == 0)
+      mbar_init(bar_s, 1);
+   const __nv_bfloat16 zero = __float2bfloat16(0.f);
+   // transposed activation tiles, rows past the data zero
+   for (int e = tid; e < 128 * 128; e += 128) {
+      const int m = e / 128, k = e % 128;
+      if (m >= MLP_IN)
+         bf(TB_SXT, m, k, 128) = zero;
+      if (m >= MLP_HID) {
+         bf(TB_SH1T, m, k, 128) = zero;
+         bf(TB_SH2T, m, k, 128) = zero;
+      }
+   }
+   for (int e = tid; e < TC_ROWS * MLP_IN; e += 128) {  // (m = i, k = row) = x[row][i]
+      const int rr = e / MLP_IN, i = e % MLP_IN;
+      bf(TB_SXT, i, rr, 128) = r0 + rr < rows ? x[(size_t)(r0 + rr) * MLP_IN + i] : zero;
+   }
+   for (int e = tid; e < TC_ROWS * MLP_HID; e += 128) {
+      const int rr = e / MLP_HID, h = e % MLP_HID;
+      const bool in = r0 + rr < rows;
+      bf(TB_SH1T, h, rr, 128) = in ? h1[(size_t)(r0 + rr) * MLP_HID + h] : zero;
+      bf(TB_SH2T, h, rr, 128) = in ? h2[(size_t)(r0 + rr) * MLP_HID + h] : zero;
+      zst[rr * TC_ZLD + h] = in ? z2[(size_t)(r0 + rr) * MLP_HID + h] : 0.f;
+   }
+   for (int e = tid; e < MLP_HID * 16; e += 128) {  // (n = h, k = o) = W3[h][o]
+      const int h = e / 16, o = e % 16;
+      bf(TB_SW3, h, o, 16) = o < MLP_OUT_PAD ? wb[BF_W3 + h * MLP_OUT_PAD + o] : zero;
+   }
+   for (int e = tid; e < MLP_HID * MLP_HID; e += 128) {  // (n = h1, k = h2) = W2[h1][h2]
+      const int a = e / MLP_HID, b = e % MLP_HID;
+      bf(TB_SW2, a, b, MLP_HID) = wb[BF_W2 + e];
+   }
+   // loss gradient of this row (k_loss_grad): dY = 2 (y - t) / (3 rows)
+   const bool live = r < rows && (!rowpol || rowpol[r % npad] != 0.f);
+   double se = 0;
+   float dyf[MLP_OUT_PAD];
+#pragma unroll
+   for (int c = 0; c < MLP_OUT_PAD; ++c) {
+      float g = 0.f;
+      if (c < MLP_OUT && live) {
+         const float d = y[(size_t)r * MLP_OUT_PAD + c] - t[(size_t)r * MLP_OUT + c];
+         se += (double)d * d;
+         g = 2.f * d / (float)(rows * MLP_OUT);
+      }
+      dyf[c] = g;
+   }
+#pragma unroll
+   for (int c = 0; c < 16; ++c) {
+      const __nv_bfloat16 v = c < MLP_OUT_PAD ? __float2bfloat16(dyf[c]) : zero;
+      bf(TB_SDY, rl, c, 16) = v;
+      bf(TB_SDYT, c, rl, 128) = v;
+   }
+   // bias column sums over the tile: per warp here, across the four warps at the end
+   warp_colsum<MLP_OUT_PAD>(dyf, bpart + warp * 136, lane);
+   {
+      double a = se;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1)
+         a += __shfl_xor_sync(0xffffffffu, a, o);
+      if (lane == 0)
+         lsum[warp] = a;
+   }
+   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+   __syncthreads();
+   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+   const unsigned tmem = tmem_slot;
+   const unsigned lane_base = tmem + ((unsigned)(32 * warp) << 16);
+   unsigned phase = 0;
+   auto mmas = [&](unsigned dcol, unsigned a_off, int KA, unsigned b_off, int K, int n) {
+      for (int kk = 0; kk < K / 16; ++kk)
+         tc_mma(tmem + dcol, smem_desc(base + a_off + kk * 256, KA), smem_desc(base + b_off + kk * 256, KA),
+            tc_idesc(n), kk > 0);
+   };
+   auto wait = [&]() {
+      if (!mbar_wait_bounded(bar_s, phase)) {
+         if (tid == 0)
+            atomicOr(err, 4);
+         mbar_wait_bounded(bar_s, phase);
+      }
+      phase ^= 1u;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+   };
+   auto sync_tiles = [&]() {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncthreads();
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+   };
+   // dH2 = dY W3^T (K = 16), dW3 = H2^T dY (K = 128 rows)
+   if (tid == 0) {
+      mmas(0, TB_SDY, 16, TB_SW3, 16, MLP_HID);
+      mmas(64, TB_SH2T, 128, TB_SDYT, 128, 16);
+      tc_commit(bar_s);
+   }
+   wait();
+   // hidden delta 2 (k_silu_back): dZ2 = dH2 silu'(z2); z2 from the staging tile
+   float dz[16];
+   auto delta = [&](unsigned dcol, int bias_off) {
+      float cs[MLP_HID];
+#pragma unroll
+      for (int c0 = 0; c0 < MLP_HID; c0 += 16) {
+         tc_ld16(lane_base + dcol + c0, dz);
+#pragma unroll
+         for (int i = 0; i < 16; ++i) {
+            const int c = c0 + i;
+            const float v = r < rows ? dz[i] * silu_grad(zst[rl * TC_ZLD + c]) : 0.f;
+            cs[c] = v;
+            const __nv_bfloat16 vb = __float2bfloat16(v);
+            bf(TB_SDZ, rl, c, MLP_HID) = vb;
+            bf(TB_SDZT, c, rl, 128) = vb;
+         }
+      }
+      warp_colsum<MLP_HID>(cs, bpart + warp * 136 + bias_off, lane);
+   };
+   delta(0, 8);
+   __syncthreads();  // every thread done with z2 before z1 replaces it
+   for (int e = tid; e < TC_ROWS * MLP_HID; e += 128) {
+      const int rr = e / MLP_HID, h = e % MLP_HID;
+      zst[rr * TC_ZLD + h] = r0 + rr < rows ? z1[(size_t)(r0 + rr) * MLP_HID + h] : 0.f;
+   }
+   sync_tiles();
+   // dH1 = dZ2 W2^T (K = 64), dW2 = H1^T dZ2 (K = 128 rows)
+   if (tid == 0) {
+      mmas(128, TB_SDZ, MLP_HID, TB_SW2, MLP_HID, MLP_HID);
+      mmas(192, TB_SH1T, 128, TB_SDZT, 128, MLP_HID);
+      tc_commit(bar_s);
+   }
+   wait();
+   // hidden delta 1: dZ1 = dH1 silu'(z1) into the dZ^T tile (dW2 has read it)
+   delta(128, 72);
+   sync_tiles();
+   // dW1 = X^T dZ1 (K = 128 rows)
+   if (tid == 0) {
+      mmas(256, TB_SXT, 128, TB_SDZT, 128, MLP_HID);
+      tc_commit(bar_s);
+   }
+   wait();
+   // this tile's gradient vector, in the parameter layout of S.g
+   float* gp = gpart + (size_t)blockIdx.x * MLP_NPARAM;
+   if (warp < 2) {  // TMEM lanes 0-63: dW3 rows h, dW2 rows h1
+      float v[16];
+      tc_ld16(lane_base + 64, v);
+#pragma unroll
+      for (int o = 0; o < MLP_OUT_PAD; ++o)
+         gp[OFF_W3 + rl * MLP_OUT_PAD + o] = v[o];
+#pragma unroll
+      for (int c0 = 0; c0 < MLP_HID; c0 += 16) {
+         tc_ld16(lane_base + 192 + c0, v);
+#pragma unroll
+         for (int i = 0; i < 16; ++i)
+            gp[OFF_W2 + rl * MLP_HID + c0 + i] = v[i];
+      }
+   }
+   if (warp == 0) {  // TMEM lanes 0-31: dW1 rows i
+      float v[16];
+#pragma unroll
+      for (int c0 = 0; c0 < MLP_HID; c0 += 16) {
+         tc_ld16(lane_base + 256 + c0, v);
+#pragma unroll
+         for (int i = 0; i < 16; ++i)
+            gp[OFF_W1 + rl * MLP_HID + c0 + i] = v[i];
+      }
+   }
+   __syncthreads();
+   for (int c = tid; c < 136; c += 128) {
+      const float a = (bpart[c] + bpart[136 + c]) + (bpart[272 + c] + bpart[408 + c]);
+      if (c < 8)
+         gp[OFF_B3 + c] = a;
+      else if (c < 72)
+         gp[OFF_B2 + c - 8] = a;
+      else
+         gp[OFF_B1 + c - 72] = a;
+   }
+   if (tid == 0)
+      lpart[blockIdx.x] = (lsum[0] + lsum[1]) + (lsum[2] + lsum[3]);
+   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+   __syncthreads();
+   if (warp == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((unsigned)TB_TMEM_COLS)
+                   : "memory");
+   }
+}
+
 int mlp_tc_setup()
 {
-   return cudaFuncSetAttribute(k_mlp_forward_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_ACT) ==
+   return cudaFuncSetAttribute(k_mlp_backward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TB_SMEM) ==
+            cudaSuccess &&
+         cudaFuncSetAttribute(k_mlp_forward_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_ACT) ==
             cudaSuccess &&
          cudaFuncSetAttribute(k_mlp_forward_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM) ==
             cudaSuccess
       ? T9GB_OK
       : T9GB_CUDA_ERR;
+}
+
+// fixed-order sum of the per-CTA partial gradients (and, in one thread, of
+// the squared errors); the padding parameters stay zero
+__global__ void __launch_bounds__(256) k_grad_reduce(int ncta, const float* __restrict__ gpart,
+   const double* __restrict__ lpart, const unsigned char* __restrict__ mask, float* __restrict__ g,
+   double* __restrict__ loss)
+{
+   const int p = blockIdx.x * blockDim.x + threadIdx.x;
+   if (p < MLP_NPARAM) {
+      float a = 0.f;
+      for (int c = 0; c < ncta; ++c)
+         a += gpart[(size_t)c * MLP_NPARAM + p];
+      g[p] = mask[p] ? a : 0.f;
+   }
+   if (p == 0) {
+      double l = 0;
+      for (int c = 0; c < ncta; ++c)
+         l += lpart[c];
+      *loss = l;
+   }
 }
 
 // forward over rows of S.x; outputs in S.y [rows][8]; act: also the
@@ -684,6 +962,16 @@ int mlp_backward(Context* ctx, int rows, const float* rowpol, int npad)
 {
    MlpState& S = ctx->mlp;
    const __nv_bfloat16* wb = reinterpret_cast<const __nv_bfloat16*>(S.wb);
+   if (ctx->mlp_tc) {
+      // one fused pass per 128 rows, then the fixed-order tile sum; the
+      // per-tile squared errors go to the front of S.err
+      const int ncta = (rows + TC_ROWS - 1) / TC_ROWS;
+      k_mlp_backward_tc<<<ncta, 128, TB_SMEM, ctx->stream>>>(rows, npad, rowpol, S.x, S.z1, S.h1, S.z2, S.h2, S.y,
+         S.t, wb, S.gpart, S.err, ctx->copy_err);
+      k_grad_reduce<<<(MLP_NPARAM + 255) / 256, 256, 0, ctx->stream>>>(ncta, S.gpart, S.err, S.mask, S.g, S.loss);
+      T9_CUDA(cudaGetLastError());
+      return T9GB_OK;
+   }
    const int ns = S.nsplit;
    k_loss_grad<<<grid_for(rows, 256), 256, 0, ctx->stream>>>(rows, S.y, S.t, rowpol, npad, S.dy, S.dyf,
       S.err);
