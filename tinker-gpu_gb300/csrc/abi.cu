@@ -759,7 +759,7 @@ int t9gb_learn_eval(t9gb_context* h, int rows, const float* x, const float* t, f
    cudaStream_t st = ctx->stream;
    T9_CUDA(cudaMemcpyAsync(S.x, xb.data(), sizeof(__nv_bfloat16) * xb.size(), cudaMemcpyHostToDevice, st));
    T9_CUDA(cudaMemcpyAsync(S.t, t, sizeof(float) * rows * MLP_OUT, cudaMemcpyHostToDevice, st));
-   T9_CHECK(mlp_forward(ctx, rows, true));
+   T9_CHECK(mlp_forward(ctx, rows));
    T9_CHECK(mlp_backward(ctx, rows, nullptr, 0));
    std::vector<float> yy((size_t)rows * MLP_OUT_PAD);
    double l = 0;

@@ -131,7 +131,9 @@ struct MlpState {
    double* err = nullptr;        // [rows] squared error
    double* loss = nullptr;
    float* split = nullptr;       // split-K / column-sum partials
-   float* gpart = nullptr;       // [rows / 128][MLP_NPARAM] per-tile gradients (tcgen05 backward)
+   float* gpart = nullptr;       // [rows / 128][MLP_NPARAM] per-CTA gradients (tcgen05 training pass)
+   int* ticket = nullptr;        // blocks done in the gradient sum (reset by the last)
+   int sms = 1;                  // multiprocessors: CTAs of the training pass
 };
 
 struct Context {
@@ -575,8 +577,12 @@ int mlp_alloc(Context* ctx, int max_rows, unsigned seed);
 void mlp_free(Context* ctx);
 int mlp_set_weights(Context* ctx, const float* w_host);
 int mlp_get_weights(Context* ctx, float* w_host);
-int mlp_forward(Context* ctx, int rows, bool act);
+int mlp_forward(Context* ctx, int rows);
 int mlp_backward(Context* ctx, int rows, const float* rowpol, int npad);
+// tcgen05 path: recomputed forward, loss, gradient and AdamW step in two
+// launches; scal (may be null) takes the summed squared error x loss_norm
+int mlp_train_step_tc(Context* ctx, int rows, const float* rowpol, int npad, float lr, float wd, double* scal,
+   double loss_norm);
 int mlp_adamw(Context* ctx, float lr, float wd);
 // learned guess (learn.cu)
 int launch_learn_features(Context* ctx, const float* e8, const float* u8, float* xf);  // pair.cu
@@ -595,7 +601,7 @@ int induce_sorted(Context* ctx);
 int learn_setup(Context* ctx);
 void learn_free(Context* ctx);
 int learn_reset(Context* ctx, unsigned seed);
-int learn_forward(Context* ctx);
+int learn_forward(Context* ctx, bool need_y);
 int learn_guess(Context* ctx, float* ug8, int set_choice);
 void drop_graphs(Context* ctx);  // pcg.cu
 // energy.cu: fixed-order sums of per-slot rows (nrows <= 8 FP64 rows; nblocks

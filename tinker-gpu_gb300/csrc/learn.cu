@@ -257,7 +257,9 @@ int learn_reset(Context* ctx, unsigned seed)
 }
 
 // features of the current solve (efield, udir), statistics, forward pass
-int learn_forward(Context* ctx)
+// (need_y: the guess reads the outputs; the mma.sync training path reads
+// the activations; the tcgen05 training pass recomputes both)
+int learn_forward(Context* ctx, bool need_y)
 {
    const int npad = ctx->npad;
    T9_CHECK(launch_learn_features(ctx, ctx->efield, ctx->udir, ctx->xf));
@@ -265,7 +267,9 @@ int learn_forward(Context* ctx)
    k_normalize<<<grid_for(2LL * npad * 32, LB), LB, 0, ctx->stream>>>(npad, ctx->xf, ctx->spolar, ctx->fstat,
       ctx->mlp.x);
    T9_CUDA(cudaGetLastError());
-   return mlp_forward(ctx, 2 * npad, (ctx->learn_mode & 1) != 0);
+   if (need_y || (!ctx->mlp_tc && (ctx->learn_mode & 1)))
+      return mlp_forward(ctx, 2 * npad);
+   return T9GB_OK;
 }
 
 int learn_guess(Context* ctx, float* ug8, int set_choice)
@@ -297,8 +301,12 @@ int learn_train(Context* ctx)
    k_targets<<<grid_for(2 * npad, LB), LB, 0, ctx->stream>>>(npad, ctx->uind, ctx->udir, ctx->sframe, ctx->spolar,
       ctx->fstat, ctx->mlp.t);
    T9_CUDA(cudaGetLastError());
+   const double norm = 1.0 / (6.0 * std::max(1, ctx->n));
+   if (ctx->mlp_tc)
+      return mlp_train_step_tc(ctx, 2 * npad, ctx->spolar, npad, ctx->learn_lr, ctx->learn_wd, ctx->scal + S_L_LOSS,
+         norm);
    T9_CHECK(mlp_backward(ctx, 2 * npad, ctx->spolar, npad));
-   k_store_loss<<<1, 1, 0, ctx->stream>>>(ctx->mlp.loss, 1.0 / (6.0 * std::max(1, ctx->n)), ctx->scal);
+   k_store_loss<<<1, 1, 0, ctx->stream>>>(ctx->mlp.loss, norm, ctx->scal);
    T9_CHECK(mlp_adamw(ctx, ctx->learn_lr, ctx->learn_wd));
    return T9GB_OK;
 }

@@ -354,6 +354,9 @@ int mlp_alloc(Context* ctx, int max_rows, unsigned seed)
    S.nsplit = 128;
    T9_CUDA(cudaMalloc(&S.split, sizeof(float) * (size_t)std::max<size_t>(S.nsplit * MLP_HID * MLP_HID, 1024 * MLP_HID)));
    T9_CUDA(cudaMalloc(&S.gpart, sizeof(float) * ((R + 127) / 128) * MLP_NPARAM));  // 128-row tiles
+   T9_CUDA(cudaMalloc(&S.ticket, sizeof(int)));
+   T9_CUDA(cudaMemset(S.ticket, 0, sizeof(int)));
+   T9_CUDA(cudaDeviceGetAttribute(&S.sms, cudaDevAttrMultiProcessorCount, ctx->dev));
    return mlp_init(ctx, seed);
 }
 
@@ -393,7 +396,7 @@ void mlp_free(Context* ctx)
 {
    MlpState& S = ctx->mlp;
    void* p[] = {S.step, S.w, S.g, S.m, S.v, S.mask, S.wb_index, S.wb, S.x, S.z1, S.z2, S.h1, S.h2, S.c, S.y, S.t, S.dy,
-      S.dyf, S.dz, S.dzf, S.err, S.loss, S.split, S.gpart};
+      S.dyf, S.dz, S.dzf, S.err, S.loss, S.split, S.gpart, S.ticket};
    for (void* q : p)
       if (q)
          cudaFree(q);
@@ -460,6 +463,16 @@ __device__ __forceinline__ unsigned long long smem_desc(unsigned addr, int K)
    return (unsigned long long)((addr & 0x3ffff) >> 4) | (lbo << 16) | (sbo << 32) | (1ull << 46);
 }
 
+// the same tile read MN-major (its rows are the K dimension): without
+// swizzle the descriptor's SBO is the stride between core matrices along
+// M / N (128 B, adjacent 8-column groups) and LBO the stride between 8-row
+// groups along K
+__device__ __forceinline__ unsigned long long smem_desc_mn(unsigned addr, int width)
+{
+   const unsigned long long lbo = (unsigned long long)((width >> 3) * 128) >> 4, sbo = 128 >> 4;
+   return (unsigned long long)((addr & 0x3ffff) >> 4) | (lbo << 16) | (sbo << 32) | (1ull << 46);
+}
+
 // kind::f16 instruction descriptor: D f32, A and B bf16, both K-major, N, M = 128
 __host__ __device__ constexpr unsigned tc_idesc(int n)
 {
@@ -496,23 +509,28 @@ __device__ __forceinline__ void tc_ld16(unsigned taddr, float* v)
       v[i] = __uint_as_float(r[i]);
 }
 
+// 16-byte store of 8 bf16 (round to nearest, as __float2bfloat16)
+__device__ __forceinline__ void st_bf8(unsigned char* p, const float* v)
+{
+   uint4 u;
+   unsigned* w = reinterpret_cast<unsigned*>(&u);
+#pragma unroll
+   for (int i = 0; i < 4; ++i) {
+      const __nv_bfloat162 b = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
+      w[i] = *reinterpret_cast<const unsigned*>(&b);
+   }
+   *reinterpret_cast<uint4*>(p) = u;
+}
+
 // operand tiles (bytes): X [128][32], H1 / H2 [128][64], W1^T [64][32],
 // W2^T [64][64], W3^T [16][64] (columns 8-15 zero)
 constexpr int TC_SX = 0, TC_SH1 = TC_SX + 128 * 32 * 2, TC_SH2 = TC_SH1 + 128 * 64 * 2;
 constexpr int TC_SW1 = TC_SH2 + 128 * 64 * 2, TC_SW2 = TC_SW1 + 64 * 32 * 2, TC_SW3 = TC_SW2 + 64 * 64 * 2;
 constexpr int TC_SMEM = TC_SW3 + 16 * 64 * 2;  // 55,296 bytes: at most four CTAs per SM, 4 x 128 TMEM columns
-// with the activations kept: a [128][65] FP32 staging tile for coalesced
-// stores of z (88,576 bytes: at most two CTAs per SM)
-constexpr int TC_ZLD = MLP_HID + 1;
-constexpr int TC_SMEM_ACT = TC_SMEM + TC_ROWS * TC_ZLD * 4;
 
-// ACT: also store z1, h1, z2, h2 (the backward pass reads them); the
-// inference forward stores only y
-template <bool ACT>
+// inference: stores only y (the training pass recomputes the activations)
 __global__ void __launch_bounds__(128) k_mlp_forward_tc(int rows, const __nv_bfloat16* __restrict__ x,
-   const __nv_bfloat16* __restrict__ wb, const float* __restrict__ w, float* __restrict__ z1,
-   __nv_bfloat16* __restrict__ h1, float* __restrict__ z2, __nv_bfloat16* __restrict__ h2, float* __restrict__ y,
-   int* __restrict__ err)
+   const __nv_bfloat16* __restrict__ wb, const float* __restrict__ w, float* __restrict__ y, int* __restrict__ err)
 {
    extern __shared__ __align__(128) unsigned char tsm[];
    __shared__ __align__(8) unsigned long long bar;
@@ -582,47 +600,29 @@ __global__ void __launch_bounds__(128) k_mlp_forward_tc(int rows, const __nv_bfl
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
    };
 
-   // hidden layer epilogue: z = D + b, h = silu(z) into the next operand
-   // tile; ACT: z through the staging tile, then z and h stored row-major
-   // with consecutive threads on consecutive columns
-   float* zst = reinterpret_cast<float*>(tsm + TC_SMEM);
-   auto hidden = [&](unsigned dcol, const float* b, float* zg, __nv_bfloat16* hg, unsigned h_off) {
+   // hidden layer epilogue: h = silu(D + b) into the next operand tile
+   // (zero past the rows)
+   auto hidden = [&](unsigned dcol, const float* b, unsigned h_off) {
 #pragma unroll
       for (int c0 = 0; c0 < MLP_HID; c0 += 16) {
          float v[16];
          tc_ld16(lane_base + dcol + c0, v);
 #pragma unroll
-         for (int i = 0; i < 16; ++i) {
-            const int c = c0 + i;
-            const float z = v[i] + b[c];
-            const __nv_bfloat16 hv = __float2bfloat16(silu(z));
-            if (ACT)
-               zst[(32 * warp + lane) * TC_ZLD + c] = z;
-            *reinterpret_cast<__nv_bfloat16*>(tsm + h_off + kmaj_off(32 * warp + lane, c, MLP_HID)) =
-               r < rows ? hv : __float2bfloat16(0.f);
-         }
+         for (int i = 0; i < 16; ++i)
+            v[i] = r < rows ? silu(v[i] + b[c0 + i]) : 0.f;
+         st_bf8(tsm + h_off + kmaj_off(32 * warp + lane, c0, MLP_HID), v);
+         st_bf8(tsm + h_off + kmaj_off(32 * warp + lane, c0 + 8, MLP_HID), v + 8);
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       __syncthreads();
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      if (ACT) {
-         for (int e = tid; e < TC_ROWS * MLP_HID; e += 128) {
-            const int rl = e / MLP_HID, c = e % MLP_HID;
-            if (r0 + rl < rows) {
-               zg[(size_t)(r0 + rl) * MLP_HID + c] = zst[rl * TC_ZLD + c];
-               hg[(size_t)(r0 + rl) * MLP_HID + c] =
-                  *reinterpret_cast<const __nv_bfloat16*>(tsm + h_off + kmaj_off(rl, c, MLP_HID));
-            }
-         }
-         __syncthreads();  // the staging tile is reused by the next layer
-      }
    };
 
    layer(TC_SX, TC_SW1, MLP_IN, MLP_HID, 0);
-   hidden(0, w + OFF_B1, z1, h1, TC_SH1);
+   hidden(0, w + OFF_B1, TC_SH1);
    layer(TC_SH1, TC_SW2, MLP_HID, MLP_HID, 64);
-   hidden(64, w + OFF_B2, z2, h2, TC_SH2);
+   hidden(64, w + OFF_B2, TC_SH2);
    layer(TC_SH2, TC_SW3, MLP_HID, 16, 0);
    {
       float v[16];
@@ -642,128 +642,322 @@ __global__ void __launch_bounds__(128) k_mlp_forward_tc(int rows, const __nv_bfl
 }
 
 // ---------------------------------------------------------------------------
-// Backward pass on tcgen05: one CTA of four warps per 128 rows computes the
-// loss gradient dY, the hidden deltas dZ2 = (dY W3^T) silu'(z2) and
-// dZ1 = (dZ2 W2^T) silu'(z1), and this tile's weight gradients
-// dW3 = H2^T dY, dW2 = H1^T dZ2, dW1 = X^T dZ1 (the transposed activations
-// padded to 128 rows, so every MMA has M = 128), plus the bias-gradient
-// column sums and the squared error; it writes them as one partial vector
-// per CTA, which k_grad_reduce adds in a fixed order.  The BF16 rounding
-// points are those of the mma.sync path (dY and the deltas rounded for the
-// products, kept in FP32 for the bias sums).
-constexpr int TB_SXT = 0;                              // X^T pad   [128][128]
-constexpr int TB_SH1T = TB_SXT + 128 * 128 * 2;        // H1^T pad  [128][128]
-constexpr int TB_SH2T = TB_SH1T + 128 * 128 * 2;       // H2^T pad  [128][128]
-constexpr int TB_SW3 = TB_SH2T + 128 * 128 * 2;        // W3 as B   [64][16]
-constexpr int TB_SW2 = TB_SW3 + 64 * 16 * 2;           // W2 as B   [64][64]
-constexpr int TB_SDY = TB_SW2 + 64 * 64 * 2;           // dY        [128][16]
-constexpr int TB_SDYT = TB_SDY + 128 * 16 * 2;         // dY^T      [16][128]
-constexpr int TB_SDZ = TB_SDYT + 16 * 128 * 2;         // dZ2       [128][64]
-constexpr int TB_SDZT = TB_SDZ + 128 * 64 * 2;         // dZ^T      [64][128]
-constexpr int TB_SZ = TB_SDZT + 64 * 128 * 2;          // z staging [128][65] f32
-constexpr int TB_SB = TB_SZ + 128 * TC_ZLD * 4;        // bias partials [4 warps][8 + 64 + 64] f32
-constexpr int TB_SMEM = TB_SB + 4 * (8 + 64 + 64) * 4; // 184,960 bytes: one CTA per SM
-static_assert(TB_SMEM == 184960, "backward tile layout");
-constexpr int TB_TMEM_COLS = 512;  // dH2 0-63, dW3 64-79, dH1 128-191, dW2 192-255, dW1 256-319
+// Training pass on tcgen05.  A persistent CTA of four warps takes 128-row
+// tiles (tile = blockIdx.x + k gridDim.x, a fixed assignment) and for each
+// one recomputes the forward pass from x alone (no stored activations), then
+// the loss gradient dY, the deltas dZ2 = (dY W3^T) silu'(z2) and
+// dZ1 = (dZ2 W2^T) silu'(z1), and adds the tile's weight gradients into
+// tensor-memory accumulators that live across its tiles:
+//     [dW2 . ; . dW3] += [h1 h2]^T [dZ2 dY]   (one 128 x 80 product)
+//     [. ; dW1 ; .]   += [dZ1 x 0]^T dZ1       (rows 64-95 are dW1)
+// The transposed operands are the row-major tiles themselves, read
+// MN-major by the tensor core, so no transposed copies are stored.  The bias
+// gradients are column sums of the FP32 deltas (warp halving butterflies,
+// then the four warps); the squared error is summed in FP64.  Each CTA
+// writes one partial gradient vector; k_grad_sum adds them in a fixed order.
+// The BF16 rounding points are those of the mma.sync path: operands and
+// deltas rounded for the products, the bias sums and dY kept in FP32.
 
-// column sums of one value per lane and column over a warp (butterfly: every
-// lane ends with the sum; lane 0 stores it)
-template <int N>
-__device__ __forceinline__ void warp_colsum(const float* v, float* out, int lane)
+// shared-memory tiles (bf16, the K-major no-swizzle layout of kmaj_off)
+constexpr int TT_Q = 0;                          // [128][128]: dZ1 0-63 | x 64-95 | 0
+constexpr int TT_H = TT_Q + 128 * 128 * 2;       // [128][128]: h1 0-63 | h2 64-127
+constexpr int TT_G = TT_H + 128 * 128 * 2;       // [128][80]:  dZ2 0-63 | dY 64-71 | 0
+constexpr int TT_W1T = TT_G + 128 * 80 * 2;      // [64][32]  (n, k) = W1[k][n]
+constexpr int TT_W2T = TT_W1T + 64 * 32 * 2;     // [64][64]  (n, k) = W2[k][n]
+constexpr int TT_W3T = TT_W2T + 64 * 64 * 2;     // [16][64]  (n, k) = W3[k][n], rows 8-15 zero
+constexpr int TT_W2 = TT_W3T + 16 * 64 * 2;      // [64][64]  (n, k) = W2[n][k]
+constexpr int TT_W3 = TT_W2 + 64 * 64 * 2;       // [64][16]  (n, k) = W3[n][k], columns 8-15 zero
+constexpr int TT_BIAS = TT_W3 + 64 * 16 * 2;     // b1 | b2 | b3, f32 [136]
+constexpr int TT_BP = TT_BIAS + 136 * 4;         // bias-gradient partials, f32 [4 warps][136]
+constexpr int TT_END = TT_BP + 4 * 136 * 4;      // 113,312 bytes
+static_assert(TT_END == 113312, "training tile layout");
+// requested: 116 KB, so that two CTAs never share an SM (each holds 512
+// tensor-memory columns, all of an SM's)
+constexpr int TT_SMEM = 116 * 1024;
+// tensor-memory columns: forward accumulators, the delta product (dH2, then
+// dH1 in the same columns once dY W3^T has been read), the gradients
+constexpr int TT_C_D1 = 0, TT_C_D2 = 64, TT_C_D3 = 128, TT_C_DH = 128, TT_C_DWS = 192, TT_C_DW1 = 288;
+constexpr int TT_TMEM_COLS = 512;
+
+// column sums over the warp's 32 rows of 64 values per lane: five halving
+// stages (lane bit 4, 3, .. 0 keeps the upper or lower half and adds its
+// partner's other half); lane L ends with the sums of columns 2L, 2L + 1
+__device__ __forceinline__ void warp_colsum64(float* v, int lane, float& c0, float& c1)
 {
 #pragma unroll
-   for (int c = 0; c < N; ++c) {
-      float a = v[c];
+   for (int st = 0; st < 5; ++st) {
+      const int d = 16 >> st, h = 32 >> st;
+      const bool up = (lane & d) != 0;
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1)
-         a += __shfl_xor_sync(0xffffffffu, a, o);
-      if (lane == 0)
-         out[c] = a;
+      for (int i = 0; i < h; ++i) {
+         const float send = up ? v[i] : v[i + h];
+         const float keep = up ? v[i + h] : v[i];
+         v[i] = keep + __shfl_xor_sync(0xffffffffu, send, d);
+      }
    }
+   c0 = v[0];
+   c1 = v[1];
 }
 
-__global__ void __launch_bounds__(128) k_mlp_backward_tc(int rows, int npad, const float* __restrict__ rowpol,
-   const __nv_bfloat16* __restrict__ x, const float* __restrict__ z1, const __nv_bfloat16* __restrict__ h1,
-   const float* __restrict__ z2, const __nv_bfloat16* __restrict__ h2, const float* __restrict__ y,
-   const float* __restrict__ t, const __nv_bfloat16* __restrict__ wb, float* __restrict__ gpart,
+// column sums of 8 values per lane: three halving stages, then two plain
+// butterfly stages; lane L holds the sum of column L >> 2
+__device__ __forceinline__ float warp_colsum8(float* v, int lane)
+{
+#pragma unroll
+   for (int st = 0; st < 3; ++st) {
+      const int d = 16 >> st, h = 4 >> st;
+      const bool up = (lane & d) != 0;
+#pragma unroll
+      for (int i = 0; i < h; ++i) {
+         const float send = up ? v[i] : v[i + h];
+         const float keep = up ? v[i + h] : v[i];
+         v[i] = keep + __shfl_xor_sync(0xffffffffu, send, d);
+      }
+   }
+   float a = v[0];
+   a += __shfl_xor_sync(0xffffffffu, a, 2);
+   a += __shfl_xor_sync(0xffffffffu, a, 1);
+   return a;
+}
+
+__global__ void __launch_bounds__(128, 1) k_mlp_train_tc(int rows, int tiles_per_cta, int npad,
+   const float* __restrict__ rowpol, const __nv_bfloat16* __restrict__ x, const float* __restrict__ t,
+   const __nv_bfloat16* __restrict__ wb, const float* __restrict__ w, float* __restrict__ gpart,
    double* __restrict__ lpart, int* __restrict__ err)
 {
-   extern __shared__ __align__(128) unsigned char bsm[];
+   extern __shared__ __align__(128) unsigned char tsm[];
    __shared__ __align__(8) unsigned long long bar;
    __shared__ unsigned tmem_slot;
    __shared__ double lsum[4];
    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-   const int r0 = blockIdx.x * TC_ROWS;
-   const int rl = 32 * warp + lane, r = r0 + rl;  // this thread's row
-   const unsigned base = (unsigned)__cvta_generic_to_shared(bsm);
+   const int rl = 32 * warp + lane;  // this thread's row of a tile (its TMEM lane)
+   const unsigned base = (unsigned)__cvta_generic_to_shared(tsm);
    const unsigned bar_s = (unsigned)__cvta_generic_to_shared(&bar);
-   float* zst = reinterpret_cast<float*>(bsm + TB_SZ);
-   float* bpart = reinterpret_cast<float*>(bsm + TB_SB);
-   auto bf = [&](int off, int rr, int k, int K) -> __nv_bfloat16& {
-      return *reinterpret_cast<__nv_bfloat16*>(bsm + off + kmaj_off(rr, k, K));
+   float* bias = reinterpret_cast<float*>(tsm + TT_BIAS);
+   float* bpart = reinterpret_cast<float*>(tsm + TT_BP);
+   auto bf = [&](int off, int r, int k, int K) -> __nv_bfloat16& {
+      return *reinterpret_cast<__nv_bfloat16*>(tsm + off + kmaj_off(r, k, K));
    };
 
    if (warp == 0) {
       asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                       (unsigned)__cvta_generic_to_shared(&tmem_slot)),
-                   "r"((unsigned)TB_TMEM_COLS)
+                   "r"((unsigned)TT_TMEM_COLS)
                    : "memory");
       asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
    }
    if (tid == 0)
       mbar_init(bar_s, 1);
+   // weights (read in memory order, coalesced), biases, cleared partials and
+   // the zero columns of Q, once per CTA
    const __nv_bfloat16 zero = __float2bfloat16(0.f);
-   // transposed activation tiles, rows past the data zero
-   for (int e = tid; e < 128 * 128; e += 128) {
-      const int m = e / 128, k = e % 128;
-      if (m >= MLP_IN)
-         bf(TB_SXT, m, k, 128) = zero;
-      if (m >= MLP_HID) {
-         bf(TB_SH1T, m, k, 128) = zero;
-         bf(TB_SH2T, m, k, 128) = zero;
-      }
-   }
-   for (int e = tid; e < TC_ROWS * MLP_IN; e += 128) {  // (m = i, k = row) = x[row][i]
-      const int rr = e / MLP_IN, i = e % MLP_IN;
-      bf(TB_SXT, i, rr, 128) = r0 + rr < rows ? x[(size_t)(r0 + rr) * MLP_IN + i] : zero;
-   }
-   for (int e = tid; e < TC_ROWS * MLP_HID; e += 128) {
-      const int rr = e / MLP_HID, h = e % MLP_HID;
-      const bool in = r0 + rr < rows;
-      bf(TB_SH1T, h, rr, 128) = in ? h1[(size_t)(r0 + rr) * MLP_HID + h] : zero;
-      bf(TB_SH2T, h, rr, 128) = in ? h2[(size_t)(r0 + rr) * MLP_HID + h] : zero;
-      zst[rr * TC_ZLD + h] = in ? z2[(size_t)(r0 + rr) * MLP_HID + h] : 0.f;
-   }
-   for (int e = tid; e < MLP_HID * 16; e += 128) {  // (n = h, k = o) = W3[h][o]
-      const int h = e / 16, o = e % 16;
-      bf(TB_SW3, h, o, 16) = o < MLP_OUT_PAD ? wb[BF_W3 + h * MLP_OUT_PAD + o] : zero;
-   }
-   for (int e = tid; e < MLP_HID * MLP_HID; e += 128) {  // (n = h1, k = h2) = W2[h1][h2]
+   for (int e = tid; e < MLP_IN * MLP_HID; e += 128)
+      bf(TT_W1T, e % MLP_HID, e / MLP_HID, MLP_IN) = wb[BF_W1 + e];
+   for (int e = tid; e < MLP_HID * MLP_HID; e += 128) {
       const int a = e / MLP_HID, b = e % MLP_HID;
-      bf(TB_SW2, a, b, MLP_HID) = wb[BF_W2 + e];
+      bf(TT_W2T, b, a, MLP_HID) = wb[BF_W2 + e];
+      bf(TT_W2, a, b, MLP_HID) = wb[BF_W2 + e];
    }
-   // loss gradient of this row (k_loss_grad): dY = 2 (y - t) / (3 rows)
-   const bool live = r < rows && (!rowpol || rowpol[r % npad] != 0.f);
-   double se = 0;
-   float dyf[MLP_OUT_PAD];
-#pragma unroll
-   for (int c = 0; c < MLP_OUT_PAD; ++c) {
-      float g = 0.f;
-      if (c < MLP_OUT && live) {
-         const float d = y[(size_t)r * MLP_OUT_PAD + c] - t[(size_t)r * MLP_OUT + c];
-         se += (double)d * d;
-         g = 2.f * d / (float)(rows * MLP_OUT);
+   for (int e = tid; e < MLP_HID * 16; e += 128) {
+      const int h = e / 16, o = e % 16;
+      const __nv_bfloat16 v = o < MLP_OUT_PAD ? wb[BF_W3 + h * MLP_OUT_PAD + o] : zero;
+      bf(TT_W3T, o, h, MLP_HID) = v;
+      bf(TT_W3, h, o, 16) = v;
+   }
+   for (int c = tid; c < 136; c += 128)
+      bias[c] = c < 64 ? w[OFF_B1 + c] : c < 128 ? w[OFF_B2 + c - 64] : w[OFF_B3 + c - 128];
+   for (int c = tid; c < 4 * 136; c += 128)
+      bpart[c] = 0.f;
+   for (int e = tid; e < 128 * 4; e += 128)
+      *reinterpret_cast<uint4*>(tsm + TT_Q + kmaj_off(e >> 2, 96 + 8 * (e & 3), 128)) = make_uint4(0, 0, 0, 0);
+
+   unsigned phase = 0;
+   auto sync_tiles = [&]() {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncthreads();
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+   };
+   auto wait = [&]() {
+      if (!mbar_wait_bounded(bar_s, phase)) {
+         // record it, and give the products in flight a second bounded wait
+         // before their operands and accumulators are reused or freed
+         if (tid == 0)
+            atomicOr(err, 4);
+         mbar_wait_bounded(bar_s, phase);
       }
-      dyf[c] = g;
-   }
+      phase ^= 1u;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+   };
+   sync_tiles();
+   const unsigned tmem = tmem_slot;
+   const unsigned lane_base = tmem + ((unsigned)(32 * warp) << 16);
+   // D[dcol..] (+)= A B over K: A at a_off in a tile of width wa, B at b_off
+   // in a tile of width wb_; K-major operands step 16 columns (256 bytes),
+   // MN-major ones 16 rows (two 8-row groups)
+   auto mmas = [&](int dcol, int a_off, int wa, int b_off, int wbw, int K, int n, bool mn, bool acc) {
+      const unsigned idesc = tc_idesc(n) | (mn ? (1u << 15) | (1u << 16) : 0u);
+      const int sa = mn ? 2 * (wa / 8) * 128 : 256, sb = mn ? 2 * (wbw / 8) * 128 : 256;
+      for (int kk = 0; kk < K / 16; ++kk) {
+         const unsigned a = base + a_off + kk * sa, b = base + b_off + kk * sb;
+         tc_mma(tmem + dcol, mn ? smem_desc_mn(a, wa) : smem_desc(a, wa), mn ? smem_desc_mn(b, wbw) : smem_desc(b, wbw),
+            idesc, acc || kk > 0);
+      }
+   };
+   // hidden layer: z = D + b, h = silu(z) into H columns hcol.. (zero past the rows)
+   auto hidden = [&](int dcol, const float* b, int hcol, bool in) {
 #pragma unroll
-   for (int c = 0; c < 16; ++c) {
-      const __nv_bfloat16 v = c < MLP_OUT_PAD ? __float2bfloat16(dyf[c]) : zero;
-      bf(TB_SDY, rl, c, 16) = v;
-      bf(TB_SDYT, c, rl, 128) = v;
+      for (int c0 = 0; c0 < MLP_HID; c0 += 16) {
+         float v[16];
+         tc_ld16(lane_base + dcol + c0, v);
+#pragma unroll
+         for (int i = 0; i < 16; ++i)
+            v[i] = in ? silu(v[i] + b[c0 + i]) : 0.f;
+         st_bf8(tsm + TT_H + kmaj_off(rl, hcol + c0, 128), v);
+         st_bf8(tsm + TT_H + kmaj_off(rl, hcol + c0 + 8, 128), v + 8);
+      }
+   };
+   // delta: dZ = dH silu'(z), z = D + b re-read from the forward
+   // accumulator; BF16 into (off, width) columns 0-63, FP32 column sums
+   // into bpart[warp][boff..]
+   auto delta = [&](int zcol, const float* b, int off, int width, int boff, bool in) {
+      float cs[MLP_HID];
+#pragma unroll
+      for (int c0 = 0; c0 < MLP_HID; c0 += 16) {
+         float dh[16], z[16];
+         tc_ld16(lane_base + TT_C_DH + c0, dh);
+         tc_ld16(lane_base + zcol + c0, z);
+#pragma unroll
+         for (int i = 0; i < 16; ++i)
+            cs[c0 + i] = in ? dh[i] * silu_grad(z[i] + b[c0 + i]) : 0.f;
+         st_bf8(tsm + off + kmaj_off(rl, c0, width), cs + c0);
+         st_bf8(tsm + off + kmaj_off(rl, c0 + 8, width), cs + c0 + 8);
+      }
+      float a0, a1;
+      warp_colsum64(cs, lane, a0, a1);
+      bpart[warp * 136 + boff + 2 * lane] += a0;
+      bpart[warp * 136 + boff + 2 * lane + 1] += a1;
+   };
+
+   double se = 0;
+   const float dscale = 2.f / (float)(rows * MLP_OUT);
+   for (int it = 0; it < tiles_per_cta; ++it) {
+      const int r0 = (blockIdx.x + it * gridDim.x) * TC_ROWS;
+      if (r0 >= rows)
+         break;  // uniform over the CTA
+      // x rows into Q columns 64-95 (16-byte chunks, coalesced)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+         const int e = tid + 128 * j, rr = e >> 2, ch = e & 3;
+         uint4 v = make_uint4(0, 0, 0, 0);
+         if (r0 + rr < rows)
+            v = __ldg(reinterpret_cast<const uint4*>(x + (size_t)(r0 + rr) * MLP_IN) + ch);
+         *reinterpret_cast<uint4*>(tsm + TT_Q + kmaj_off(rr, 64 + 8 * ch, 128)) = v;
+      }
+      const int r = r0 + rl;
+      const bool in = r < rows;
+      const bool live = in && (!rowpol || rowpol[r % npad] != 0.f);
+      float tv[MLP_OUT] = {0.f, 0.f, 0.f};
+      if (live)
+#pragma unroll
+         for (int c = 0; c < MLP_OUT; ++c)
+            tv[c] = t[(size_t)r * MLP_OUT + c];
+      sync_tiles();
+      // forward: z1 = x W1 + b1, z2 = h1 W2 + b2, y = h2 W3 + b3
+      if (tid == 0) {
+         mmas(TT_C_D1, TT_Q + 1024, 128, TT_W1T, MLP_IN, MLP_IN, MLP_HID, false, false);
+         tc_commit(bar_s);
+      }
+      wait();
+      hidden(TT_C_D1, bias, 0, in);
+      sync_tiles();
+      if (tid == 0) {
+         mmas(TT_C_D2, TT_H, 128, TT_W2T, MLP_HID, MLP_HID, MLP_HID, false, false);
+         tc_commit(bar_s);
+      }
+      wait();
+      hidden(TT_C_D2, bias + 64, 64, in);
+      sync_tiles();
+      if (tid == 0) {
+         mmas(TT_C_D3, TT_H + 1024, 128, TT_W3T, MLP_HID, MLP_HID, 16, false, false);
+         tc_commit(bar_s);
+      }
+      wait();
+      // loss gradient (k_loss_grad): dY = 2 (y - t) / (3 rows) on live rows
+      {
+         float v[16], dy[MLP_OUT_PAD];
+         tc_ld16(lane_base + TT_C_D3, v);
+#pragma unroll
+         for (int c = 0; c < MLP_OUT_PAD; ++c) {
+            float g = 0.f;
+            if (c < MLP_OUT && live) {
+               const float d = v[c] + bias[128 + c] - tv[c];
+               se += (double)d * d;
+               g = dscale * d;
+            }
+            dy[c] = g;
+         }
+         st_bf8(tsm + TT_G + kmaj_off(rl, 64, 80), dy);
+         *reinterpret_cast<uint4*>(tsm + TT_G + kmaj_off(rl, 72, 80)) = make_uint4(0, 0, 0, 0);
+         const float a = warp_colsum8(dy, lane);
+         if ((lane & 3) == 0)
+            bpart[warp * 136 + 128 + (lane >> 2)] += a;
+      }
+      sync_tiles();
+      // dH2 = dY W3^T
+      if (tid == 0) {
+         mmas(TT_C_DH, TT_G + 1024, 80, TT_W3, 16, 16, MLP_HID, false, false);
+         tc_commit(bar_s);
+      }
+      wait();
+      delta(TT_C_D2, bias + 64, TT_G, 80, 64, in);
+      sync_tiles();
+      // dH1 = dZ2 W2^T; [dW2 . ; . dW3] += [h1 h2]^T [dZ2 dY]
+      if (tid == 0) {
+         mmas(TT_C_DH, TT_G, 80, TT_W2, MLP_HID, MLP_HID, MLP_HID, false, false);
+         mmas(TT_C_DWS, TT_H, 128, TT_G, 80, TC_ROWS, 80, true, it > 0);
+         tc_commit(bar_s);
+      }
+      wait();
+      delta(TT_C_D1, bias, TT_Q, 128, 0, in);
+      sync_tiles();
+      // rows 64-95 of [dZ1 x 0]^T dZ1 are dW1 = x^T dZ1
+      if (tid == 0) {
+         mmas(TT_C_DW1, TT_Q, 128, TT_Q, 128, TC_ROWS, MLP_HID, true, it > 0);
+         tc_commit(bar_s);
+      }
+      wait();  // Q is rewritten by the next tile
    }
-   // bias column sums over the tile: per warp here, across the four warps at the end
-   warp_colsum<MLP_OUT_PAD>(dyf, bpart + warp * 136, lane);
+
+   // this CTA's gradient vector, in the parameter layout of the master weights
+   float* gp = gpart + (size_t)blockIdx.x * MLP_NPARAM;
+   if (warp < 2) {  // lanes 0-63: dW2 rows
+      float v[16];
+#pragma unroll
+      for (int c0 = 0; c0 < MLP_HID; c0 += 16) {
+         tc_ld16(lane_base + TT_C_DWS + c0, v);
+#pragma unroll
+         for (int i = 0; i < 16; i += 4)
+            *reinterpret_cast<float4*>(gp + OFF_W2 + rl * MLP_HID + c0 + i) = make_float4(v[i], v[i + 1], v[i + 2],
+               v[i + 3]);
+      }
+   } else {  // lanes 64-127: dW3 rows; lanes 64-95: dW1 rows
+      const int h = rl - 64;
+      float v[16];
+      tc_ld16(lane_base + TT_C_DWS + 64, v);
+      *reinterpret_cast<float4*>(gp + OFF_W3 + h * MLP_OUT_PAD) = make_float4(v[0], v[1], v[2], v[3]);
+      *reinterpret_cast<float4*>(gp + OFF_W3 + h * MLP_OUT_PAD + 4) = make_float4(v[4], v[5], v[6], v[7]);
+      if (warp == 2) {
+#pragma unroll
+         for (int c0 = 0; c0 < MLP_HID; c0 += 16) {
+            tc_ld16(lane_base + TT_C_DW1 + c0, v);
+#pragma unroll
+            for (int i = 0; i < 16; i += 4)
+               *reinterpret_cast<float4*>(gp + OFF_W1 + h * MLP_HID + c0 + i) = make_float4(v[i], v[i + 1],
+                  v[i + 2], v[i + 3]);
+         }
+      }
+   }
    {
       double a = se;
 #pragma unroll
@@ -772,173 +966,103 @@ __global__ void __launch_bounds__(128) k_mlp_backward_tc(int rows, int npad, con
       if (lane == 0)
          lsum[warp] = a;
    }
-   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-   __syncthreads();
-   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-   const unsigned tmem = tmem_slot;
-   const unsigned lane_base = tmem + ((unsigned)(32 * warp) << 16);
-   unsigned phase = 0;
-   auto mmas = [&](unsigned dcol, unsigned a_off, int KA, unsigned b_off, int K, int n) {
-      for (int kk = 0; kk < K / 16; ++kk)
-         tc_mma(tmem + dcol, smem_desc(base + a_off + kk * 256, KA), smem_desc(base + b_off + kk * 256, KA),
-            tc_idesc(n), kk > 0);
-   };
-   auto wait = [&]() {
-      if (!mbar_wait_bounded(bar_s, phase)) {
-         if (tid == 0)
-            atomicOr(err, 4);
-         mbar_wait_bounded(bar_s, phase);
-      }
-      phase ^= 1u;
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-   };
-   auto sync_tiles = [&]() {
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      __syncthreads();
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-   };
-   // dH2 = dY W3^T (K = 16), dW3 = H2^T dY (K = 128 rows)
-   if (tid == 0) {
-      mmas(0, TB_SDY, 16, TB_SW3, 16, MLP_HID);
-      mmas(64, TB_SH2T, 128, TB_SDYT, 128, 16);
-      tc_commit(bar_s);
-   }
-   wait();
-   // hidden delta 2 (k_silu_back): dZ2 = dH2 silu'(z2); z2 from the staging tile
-   float dz[16];
-   auto delta = [&](unsigned dcol, int bias_off) {
-      float cs[MLP_HID];
-#pragma unroll
-      for (int c0 = 0; c0 < MLP_HID; c0 += 16) {
-         tc_ld16(lane_base + dcol + c0, dz);
-#pragma unroll
-         for (int i = 0; i < 16; ++i) {
-            const int c = c0 + i;
-            const float v = r < rows ? dz[i] * silu_grad(zst[rl * TC_ZLD + c]) : 0.f;
-            cs[c] = v;
-            const __nv_bfloat16 vb = __float2bfloat16(v);
-            bf(TB_SDZ, rl, c, MLP_HID) = vb;
-            bf(TB_SDZT, c, rl, 128) = vb;
-         }
-      }
-      warp_colsum<MLP_HID>(cs, bpart + warp * 136 + bias_off, lane);
-   };
-   delta(0, 8);
-   __syncthreads();  // every thread done with z2 before z1 replaces it
-   for (int e = tid; e < TC_ROWS * MLP_HID; e += 128) {
-      const int rr = e / MLP_HID, h = e % MLP_HID;
-      zst[rr * TC_ZLD + h] = r0 + rr < rows ? z1[(size_t)(r0 + rr) * MLP_HID + h] : 0.f;
-   }
-   sync_tiles();
-   // dH1 = dZ2 W2^T (K = 64), dW2 = H1^T dZ2 (K = 128 rows)
-   if (tid == 0) {
-      mmas(128, TB_SDZ, MLP_HID, TB_SW2, MLP_HID, MLP_HID);
-      mmas(192, TB_SH1T, 128, TB_SDZT, 128, MLP_HID);
-      tc_commit(bar_s);
-   }
-   wait();
-   // hidden delta 1: dZ1 = dH1 silu'(z1) into the dZ^T tile (dW2 has read it)
-   delta(128, 72);
-   sync_tiles();
-   // dW1 = X^T dZ1 (K = 128 rows)
-   if (tid == 0) {
-      mmas(256, TB_SXT, 128, TB_SDZT, 128, MLP_HID);
-      tc_commit(bar_s);
-   }
-   wait();
-   // this tile's gradient vector, in the parameter layout of S.g
-   float* gp = gpart + (size_t)blockIdx.x * MLP_NPARAM;
-   if (warp < 2) {  // TMEM lanes 0-63: dW3 rows h, dW2 rows h1
-      float v[16];
-      tc_ld16(lane_base + 64, v);
-#pragma unroll
-      for (int o = 0; o < MLP_OUT_PAD; ++o)
-         gp[OFF_W3 + rl * MLP_OUT_PAD + o] = v[o];
-#pragma unroll
-      for (int c0 = 0; c0 < MLP_HID; c0 += 16) {
-         tc_ld16(lane_base + 192 + c0, v);
-#pragma unroll
-         for (int i = 0; i < 16; ++i)
-            gp[OFF_W2 + rl * MLP_HID + c0 + i] = v[i];
-      }
-   }
-   if (warp == 0) {  // TMEM lanes 0-31: dW1 rows i
-      float v[16];
-#pragma unroll
-      for (int c0 = 0; c0 < MLP_HID; c0 += 16) {
-         tc_ld16(lane_base + 256 + c0, v);
-#pragma unroll
-         for (int i = 0; i < 16; ++i)
-            gp[OFF_W1 + rl * MLP_HID + c0 + i] = v[i];
-      }
-   }
    __syncthreads();
    for (int c = tid; c < 136; c += 128) {
       const float a = (bpart[c] + bpart[136 + c]) + (bpart[272 + c] + bpart[408 + c]);
-      if (c < 8)
-         gp[OFF_B3 + c] = a;
-      else if (c < 72)
-         gp[OFF_B2 + c - 8] = a;
-      else
-         gp[OFF_B1 + c - 72] = a;
+      gp[c < 64 ? OFF_B1 + c : c < 128 ? OFF_B2 + c - 64 : OFF_B3 + c - 128] = a;
    }
    if (tid == 0)
       lpart[blockIdx.x] = (lsum[0] + lsum[1]) + (lsum[2] + lsum[3]);
-   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-   __syncthreads();
    if (warp == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((unsigned)TB_TMEM_COLS)
+      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((unsigned)TT_TMEM_COLS)
                    : "memory");
    }
 }
 
 int mlp_tc_setup()
 {
-   return cudaFuncSetAttribute(k_mlp_backward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TB_SMEM) ==
+   return cudaFuncSetAttribute(k_mlp_train_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TT_SMEM) ==
             cudaSuccess &&
-         cudaFuncSetAttribute(k_mlp_forward_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_ACT) ==
-            cudaSuccess &&
-         cudaFuncSetAttribute(k_mlp_forward_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM) ==
-            cudaSuccess
+         cudaFuncSetAttribute(k_mlp_forward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM) == cudaSuccess
       ? T9GB_OK
       : T9GB_CUDA_ERR;
 }
 
-// fixed-order sum of the per-CTA partial gradients (and, in one thread, of
-// the squared errors); the padding parameters stay zero
-__global__ void __launch_bounds__(256) k_grad_reduce(int ncta, const float* __restrict__ gpart,
+// Fixed-order sum of the per-CTA partial gradients: a block takes 32
+// parameters, its eight warps stride over the partials, and the eight warp
+// sums combine in a fixed tree.  ADAM: the AdamW step (as k_adamw) follows
+// in the same thread; the step count is read by every block and advanced by
+// the last one.  Block 0 sums the squared errors; scal (may be null) takes
+// them times loss_norm.
+template <bool ADAM>
+__global__ void __launch_bounds__(256) k_grad_sum(int ncta, const float* __restrict__ gpart,
    const double* __restrict__ lpart, const unsigned char* __restrict__ mask, float* __restrict__ g,
-   double* __restrict__ loss)
+   double* __restrict__ loss, double* __restrict__ scal, double loss_norm, float lr, float wd,
+   int* __restrict__ step, int* __restrict__ ticket, float* __restrict__ w, float* __restrict__ m,
+   float* __restrict__ v, __nv_bfloat16* __restrict__ wb, const int* __restrict__ wb_index)
 {
-   const int p = blockIdx.x * blockDim.x + threadIdx.x;
-   if (p < MLP_NPARAM) {
-      float a = 0.f;
-      for (int c = 0; c < ncta; ++c)
+   __shared__ float sh[8][33];
+   const int pl = threadIdx.x & 31, sl = threadIdx.x >> 5;
+   const int p = blockIdx.x * 32 + pl;
+   const int t = ADAM ? *step + 1 : 0;
+   float a = 0.f;
+   if (p < MLP_NPARAM)
+      for (int c = sl; c < ncta; c += 8)
          a += gpart[(size_t)c * MLP_NPARAM + p];
-      g[p] = mask[p] ? a : 0.f;
+   sh[sl][pl] = a;
+   __syncthreads();
+   if (sl == 0 && p < MLP_NPARAM) {
+      const float gi =
+         mask[p] ? ((sh[0][pl] + sh[1][pl]) + (sh[2][pl] + sh[3][pl])) + ((sh[4][pl] + sh[5][pl]) + (sh[6][pl] + sh[7][pl]))
+                 : 0.f;
+      g[p] = gi;
+      if (ADAM && mask[p]) {
+         const float beta1 = 0.9f, beta2 = 0.999f, eps = 1e-8f;
+         const float c1 = 1.f - powf(beta1, (float)t), c2 = 1.f - powf(beta2, (float)t);
+         const float mi = beta1 * m[p] + (1.f - beta1) * gi;
+         const float vi = beta2 * v[p] + (1.f - beta2) * gi * gi;
+         m[p] = mi;
+         v[p] = vi;
+         float wi = w[p];
+         wi -= lr * ((mi / c1) / (sqrtf(vi / c2) + eps) + wd * wi);
+         w[p] = wi;
+         if (wb_index[p] >= 0)
+            wb[wb_index[p]] = __float2bfloat16(wi);
+      }
    }
-   if (p == 0) {
+   if (blockIdx.x == 0 && threadIdx.x == 32) {
       double l = 0;
       for (int c = 0; c < ncta; ++c)
          l += lpart[c];
       *loss = l;
+      if (scal)
+         *scal = l * loss_norm;
+   }
+   if (ADAM) {
+      __shared__ bool last;
+      __threadfence();
+      __syncthreads();
+      if (threadIdx.x == 0)
+         last = atomicAdd(ticket, 1) == (int)gridDim.x - 1;
+      __syncthreads();
+      if (last && threadIdx.x == 0) {
+         *step = t;
+         *ticket = 0;
+      }
    }
 }
 
-// forward over rows of S.x; outputs in S.y [rows][8]; act: also the
-// activations the backward pass reads (the tcgen05 path leaves them out
-// otherwise; the mma.sync path always keeps them)
-int mlp_forward(Context* ctx, int rows, bool act)
+// forward over rows of S.x; outputs in S.y [rows][8] (the mma.sync path
+// also keeps the activations its backward pass reads)
+int mlp_forward(Context* ctx, int rows)
 {
    MlpState& S = ctx->mlp;
    const __nv_bfloat16* wb = reinterpret_cast<const __nv_bfloat16*>(S.wb);
    if (ctx->mlp_tc) {
-      auto k = act ? k_mlp_forward_tc<true> : k_mlp_forward_tc<false>;
-      k<<<grid_for(rows, TC_ROWS), 128, act ? TC_SMEM_ACT : TC_SMEM, ctx->stream>>>(rows, S.x, wb, S.w, S.z1, S.h1,
-         S.z2, S.h2, S.y, ctx->copy_err);
+      k_mlp_forward_tc<<<grid_for(rows, TC_ROWS), 128, TC_SMEM, ctx->stream>>>(rows, S.x, wb, S.w, S.y,
+         ctx->copy_err);
       T9_CUDA(cudaGetLastError());
       return T9GB_OK;
    }
@@ -955,23 +1079,34 @@ int mlp_forward(Context* ctx, int rows, bool act)
    return T9GB_OK;
 }
 
-// loss and full gradient for rows of S.x with targets S.t (after forward);
-// gradient in S.g, summed squared error in S.loss.  rowpol (may be null):
-// rows r with rowpol[r % npad] == 0 are left out.
+// the tcgen05 training pass over rows of S.x with targets S.t, then the
+// gradient sum (ADAM: and the AdamW step; scal: the loss times loss_norm)
+static int train_tc(Context* ctx, int rows, const float* rowpol, int npad, bool adam, float lr, float wd,
+   double* scal, double loss_norm)
+{
+   MlpState& S = ctx->mlp;
+   const int tiles = (rows + TC_ROWS - 1) / TC_ROWS;
+   const int per = (tiles + S.sms - 1) / S.sms;
+   const int grid = (tiles + per - 1) / per;
+   k_mlp_train_tc<<<grid, 128, TT_SMEM, ctx->stream>>>(rows, per, npad, rowpol, S.x, S.t,
+      reinterpret_cast<const __nv_bfloat16*>(S.wb), S.w, S.gpart, S.err, ctx->copy_err);
+   auto k = adam ? k_grad_sum<true> : k_grad_sum<false>;
+   k<<<(MLP_NPARAM + 31) / 32, 256, 0, ctx->stream>>>(grid, S.gpart, S.err, S.mask, S.g, S.loss, scal, loss_norm, lr,
+      wd, S.step, S.ticket, S.w, S.m, S.v, reinterpret_cast<__nv_bfloat16*>(S.wb), S.wb_index);
+   T9_CUDA(cudaGetLastError());
+   return T9GB_OK;
+}
+
+// loss and full gradient for rows of S.x with targets S.t: gradient in S.g,
+// summed squared error in S.loss.  rowpol (may be null): rows r with
+// rowpol[r % npad] == 0 are left out.  The mma.sync path reads the
+// activations of the last mlp_forward; the tcgen05 path recomputes them.
 int mlp_backward(Context* ctx, int rows, const float* rowpol, int npad)
 {
    MlpState& S = ctx->mlp;
    const __nv_bfloat16* wb = reinterpret_cast<const __nv_bfloat16*>(S.wb);
-   if (ctx->mlp_tc) {
-      // one fused pass per 128 rows, then the fixed-order tile sum; the
-      // per-tile squared errors go to the front of S.err
-      const int ncta = (rows + TC_ROWS - 1) / TC_ROWS;
-      k_mlp_backward_tc<<<ncta, 128, TB_SMEM, ctx->stream>>>(rows, npad, rowpol, S.x, S.z1, S.h1, S.z2, S.h2, S.y,
-         S.t, wb, S.gpart, S.err, ctx->copy_err);
-      k_grad_reduce<<<(MLP_NPARAM + 255) / 256, 256, 0, ctx->stream>>>(ncta, S.gpart, S.err, S.mask, S.g, S.loss);
-      T9_CUDA(cudaGetLastError());
-      return T9GB_OK;
-   }
+   if (ctx->mlp_tc)
+      return train_tc(ctx, rows, rowpol, npad, false, 0.f, 0.f, nullptr, 0.0);
    const int ns = S.nsplit;
    k_loss_grad<<<grid_for(rows, 256), 256, 0, ctx->stream>>>(rows, S.y, S.t, rowpol, npad, S.dy, S.dyf,
       S.err);
@@ -1000,6 +1135,12 @@ int mlp_backward(Context* ctx, int rows, const float* rowpol, int npad)
    colsum(MLP_HID, S.dzf, S.g + OFF_B1);
    T9_CUDA(cudaGetLastError());
    return T9GB_OK;
+}
+
+int mlp_train_step_tc(Context* ctx, int rows, const float* rowpol, int npad, float lr, float wd, double* scal,
+   double loss_norm)
+{
+   return train_tc(ctx, rows, rowpol, npad, true, lr, wd, scal, loss_norm);
 }
 
 int mlp_adamw(Context* ctx, float lr, float wd)

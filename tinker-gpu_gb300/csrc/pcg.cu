@@ -598,7 +598,7 @@ static int pcg_start_predict(Context* ctx, const VecArgs& A, bool graph)
    k_init_guess<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->fld6, ctx->efield, ctx->udir, ctx->uind, c.pcgguess,
       c.predictor, ctx->aspc_hist, ctx->status, 0);
    if (ctx->learn_mode & 1)
-      T9_CHECK(learn_forward(ctx));
+      T9_CHECK(learn_forward(ctx, false));
    k_init_rsd<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->tmp6, ctx->efield, ctx->udir, ctx->uind, ctx->rsd, 0);
    T9_CUDA(cudaGetLastError());
    return precond_dots(ctx, A, 1, 0, 0);
@@ -630,7 +630,7 @@ static int pcg_start(Context* ctx, const VecArgs& A, bool graph, int variant)
       c.predictor, ctx->aspc_hist, ctx->status, 1);
    // the network runs when its guess is used or when this solve trains it
    if ((ctx->learn_mode & 1) || variant != V_PLAIN)
-      T9_CHECK(learn_forward(ctx));
+      T9_CHECK(learn_forward(ctx, variant != V_PLAIN));
    if (variant == V_LEARNED)
       T9_CHECK(learn_guess(ctx, ctx->uind, 1));
    else if (variant == V_COMPARE)
