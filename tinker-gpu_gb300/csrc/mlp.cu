@@ -522,6 +522,61 @@ __device__ __forceinline__ void st_bf8(unsigned char* p, const float* v)
    *reinterpret_cast<uint4*>(p) = u;
 }
 
+// The BF16 weights (W1 | W2 | W3: 832 16-byte chunks) read in one batch of
+// independent loads, then scattered into the operand tiles: transposed,
+// (n, k) = W[k][n], at w1t / w2t / w3t (W3^T rows 8-15 zero) for the forward
+// products; with w2 / w3 >= 0 also as stored, (n, k) = W[n][k] (W3 columns
+// 8-15 zero), for the backward products.
+template <int NT>
+__device__ __forceinline__ void stage_weights(unsigned char* sm, const __nv_bfloat16* __restrict__ wb, int w1t,
+   int w2t, int w3t, int w2, int w3)
+{
+   constexpr int NCH = BF_END / 8, PER = (NCH + NT - 1) / NT;
+   static_assert(BF_END % 8 == 0 && BF_W2 % 8 == 0 && BF_W3 % 8 == 0, "16-byte weight chunks");
+   const int tid = threadIdx.x;
+   uint4 c[PER];
+#pragma unroll
+   for (int j = 0; j < PER; ++j) {
+      const int q = tid + NT * j;
+      c[j] = q < NCH ? __ldg(reinterpret_cast<const uint4*>(wb) + q) : make_uint4(0, 0, 0, 0);
+   }
+   auto st = [&](int off, int n, int k, int K, __nv_bfloat16 v) {
+      *reinterpret_cast<__nv_bfloat16*>(sm + off + kmaj_off(n, k, K)) = v;
+   };
+#pragma unroll
+   for (int j = 0; j < PER; ++j) {
+      const int q = tid + NT * j;
+      if (q >= NCH)
+         break;
+      const __nv_bfloat16* v = reinterpret_cast<const __nv_bfloat16*>(&c[j]);
+      const int e = 8 * q;
+      if (e < BF_W2) {  // W1[i][h0 .. h0 + 7]
+         const int i = e / MLP_HID, h0 = e % MLP_HID;
+#pragma unroll
+         for (int u = 0; u < 8; ++u)
+            st(w1t, h0 + u, i, MLP_IN, v[u]);
+      } else if (e < BF_W3) {  // W2[a][b0 .. b0 + 7]
+         const int a = (e - BF_W2) / MLP_HID, b0 = (e - BF_W2) % MLP_HID;
+#pragma unroll
+         for (int u = 0; u < 8; ++u)
+            st(w2t, b0 + u, a, MLP_HID, v[u]);
+         if (w2 >= 0)
+            *reinterpret_cast<uint4*>(sm + w2 + kmaj_off(a, b0, MLP_HID)) = c[j];
+      } else {  // W3[h][0 .. 7]
+         const int h = (e - BF_W3) / MLP_OUT_PAD;
+#pragma unroll
+         for (int u = 0; u < 8; ++u)
+            st(w3t, u, h, MLP_HID, v[u]);
+         if (w3 >= 0) {
+            *reinterpret_cast<uint4*>(sm + w3 + kmaj_off(h, 0, 16)) = c[j];
+            *reinterpret_cast<uint4*>(sm + w3 + kmaj_off(h, 8, 16)) = make_uint4(0, 0, 0, 0);
+         }
+      }
+   }
+   for (int e = tid; e < 8 * MLP_HID; e += NT)
+      st(w3t, 8 + e / MLP_HID, e % MLP_HID, MLP_HID, __float2bfloat16(0.f));
+}
+
 // operand tiles (bytes): X [128][32], H1 / H2 [128][64], W1^T [64][32],
 // W2^T [64][64], W3^T [16][64] (columns 8-15 zero)
 constexpr int TC_SX = 0, TC_SH1 = TC_SX + 128 * 32 * 2, TC_SH2 = TC_SH1 + 128 * 64 * 2;
@@ -550,27 +605,14 @@ __global__ void __launch_bounds__(128) k_mlp_forward_tc(int rows, const __nv_bfl
    }
    if (tid == 0)
       mbar_init(bar_s, 1);
-   // operand tiles: the input rows and the transposed weights
-   for (int e = tid; e < TC_ROWS * MLP_IN; e += 128) {
-      const int r = e / MLP_IN, k = e % MLP_IN;
-      const __nv_bfloat16 v = r0 + r < rows ? x[(size_t)(r0 + r) * MLP_IN + k] : __float2bfloat16(0.f);
-      *reinterpret_cast<__nv_bfloat16*>(tsm + TC_SX + kmaj_off(r, k, MLP_IN)) = v;
+   // operand tiles: the input rows (16-byte chunks) and the transposed weights
+   for (int e = tid; e < TC_ROWS * MLP_IN / 8; e += 128) {
+      const int r = e >> 2, ch = e & 3;
+      const uint4 v = r0 + r < rows ? __ldg(reinterpret_cast<const uint4*>(x + (size_t)(r0 + r) * MLP_IN) + ch)
+                                    : make_uint4(0, 0, 0, 0);
+      *reinterpret_cast<uint4*>(tsm + TC_SX + kmaj_off(r, 8 * ch, MLP_IN)) = v;
    }
-   // the weights are read in memory order (W[k][n], n fastest: coalesced)
-   // and stored transposed, (n, k) = W[k][n]
-   for (int e = tid; e < MLP_IN * MLP_HID; e += 128) {
-      const int k = e / MLP_HID, n = e % MLP_HID;
-      *reinterpret_cast<__nv_bfloat16*>(tsm + TC_SW1 + kmaj_off(n, k, MLP_IN)) = wb[BF_W1 + e];
-   }
-   for (int e = tid; e < MLP_HID * MLP_HID; e += 128) {
-      const int k = e / MLP_HID, n = e % MLP_HID;
-      *reinterpret_cast<__nv_bfloat16*>(tsm + TC_SW2 + kmaj_off(n, k, MLP_HID)) = wb[BF_W2 + e];
-   }
-   for (int e = tid; e < MLP_HID * 16; e += 128) {
-      const int k = e / 16, n = e % 16;
-      *reinterpret_cast<__nv_bfloat16*>(tsm + TC_SW3 + kmaj_off(n, k, MLP_HID)) =
-         n < MLP_OUT_PAD ? wb[BF_W3 + k * MLP_OUT_PAD + n] : __float2bfloat16(0.f);
-   }
+   stage_weights<128>(tsm, wb, TC_SW1, TC_SW2, TC_SW3, -1, -1);
    // the tiles (generic proxy) before the tensor core reads them (async proxy)
    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -642,7 +684,7 @@ __global__ void __launch_bounds__(128) k_mlp_forward_tc(int rows, const __nv_bfl
 }
 
 // ---------------------------------------------------------------------------
-// Training pass on tcgen05.  A persistent CTA of four warps takes 128-row
+// Training pass on tcgen05.  A persistent CTA of 16 warps takes 128-row
 // tiles (tile = blockIdx.x + k gridDim.x, a fixed assignment) and for each
 // one recomputes the forward pass from x alone (no stored activations), then
 // the loss gradient dY, the deltas dZ2 = (dY W3^T) silu'(z2) and
@@ -653,7 +695,7 @@ __global__ void __launch_bounds__(128) k_mlp_forward_tc(int rows, const __nv_bfl
 // The transposed operands are the row-major tiles themselves, read
 // MN-major by the tensor core, so no transposed copies are stored.  The bias
 // gradients are column sums of the FP32 deltas (warp halving butterflies,
-// then the four warps); the squared error is summed in FP64.  Each CTA
+// then the four row quadrants); the squared error is summed in FP64.  Each CTA
 // writes one partial gradient vector; k_grad_sum adds them in a fixed order.
 // The BF16 rounding points are those of the mma.sync path: operands and
 // deltas rounded for the products, the bias sums and dY kept in FP32.
@@ -679,14 +721,15 @@ constexpr int TT_SMEM = 116 * 1024;
 constexpr int TT_C_D1 = 0, TT_C_D2 = 64, TT_C_D3 = 128, TT_C_DH = 128, TT_C_DWS = 192, TT_C_DW1 = 288;
 constexpr int TT_TMEM_COLS = 512;
 
-// column sums over the warp's 32 rows of 64 values per lane: five halving
-// stages (lane bit 4, 3, .. 0 keeps the upper or lower half and adds its
-// partner's other half); lane L ends with the sums of columns 2L, 2L + 1
-__device__ __forceinline__ void warp_colsum64(float* v, int lane, float& c0, float& c1)
+// column sums over the warp's 32 rows of 16 values per lane: four halving
+// stages (lane bit 4, 3, 2, 1 keeps the upper or lower half of its values
+// and adds its partner's other half), then one butterfly stage; lane L holds
+// the sum of column L >> 1
+__device__ __forceinline__ float warp_colsum16(float* v, int lane)
 {
 #pragma unroll
-   for (int st = 0; st < 5; ++st) {
-      const int d = 16 >> st, h = 32 >> st;
+   for (int st = 0; st < 4; ++st) {
+      const int d = 16 >> st, h = 8 >> st;
       const bool up = (lane & d) != 0;
 #pragma unroll
       for (int i = 0; i < h; ++i) {
@@ -695,12 +738,11 @@ __device__ __forceinline__ void warp_colsum64(float* v, int lane, float& c0, flo
          v[i] = keep + __shfl_xor_sync(0xffffffffu, send, d);
       }
    }
-   c0 = v[0];
-   c1 = v[1];
+   return v[0] + __shfl_xor_sync(0xffffffffu, v[0], 1);
 }
 
-// column sums of 8 values per lane: three halving stages, then two plain
-// butterfly stages; lane L holds the sum of column L >> 2
+// the same for 8 values: three halving stages, two butterfly stages; lane L
+// holds the sum of column L >> 2
 __device__ __forceinline__ float warp_colsum8(float* v, int lane)
 {
 #pragma unroll
@@ -720,7 +762,11 @@ __device__ __forceinline__ float warp_colsum8(float* v, int lane)
    return a;
 }
 
-__global__ void __launch_bounds__(128, 1) k_mlp_train_tc(int rows, int tiles_per_cta, int npad,
+// 16 warps: warp w reads TMEM lanes 32 (w % 4) .. + 31 (its rows) and
+// columns 16 (w / 4) .. + 15 of each 64-column accumulator
+constexpr int TT_THREADS = 512;
+
+__global__ void __launch_bounds__(TT_THREADS, 1) k_mlp_train_tc(int rows, int tiles_per_cta, int npad,
    const float* __restrict__ rowpol, const __nv_bfloat16* __restrict__ x, const float* __restrict__ t,
    const __nv_bfloat16* __restrict__ wb, const float* __restrict__ w, float* __restrict__ gpart,
    double* __restrict__ lpart, int* __restrict__ err)
@@ -728,16 +774,15 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train_tc(int rows, int tiles_per
    extern __shared__ __align__(128) unsigned char tsm[];
    __shared__ __align__(8) unsigned long long bar;
    __shared__ unsigned tmem_slot;
-   __shared__ double lsum[4];
+   __shared__ double lsum[TT_THREADS / 32];
    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-   const int rl = 32 * warp + lane;  // this thread's row of a tile (its TMEM lane)
+   const int quad = warp & 3, cg = warp >> 2;  // TMEM lane quadrant, 16-column group
+   const int rl = 32 * quad + lane;            // this thread's row of a tile (its TMEM lane)
+   const int col = 16 * cg;
    const unsigned base = (unsigned)__cvta_generic_to_shared(tsm);
    const unsigned bar_s = (unsigned)__cvta_generic_to_shared(&bar);
    float* bias = reinterpret_cast<float*>(tsm + TT_BIAS);
-   float* bpart = reinterpret_cast<float*>(tsm + TT_BP);
-   auto bf = [&](int off, int r, int k, int K) -> __nv_bfloat16& {
-      return *reinterpret_cast<__nv_bfloat16*>(tsm + off + kmaj_off(r, k, K));
-   };
+   float* bpart = reinterpret_cast<float*>(tsm + TT_BP);  // [quadrant][136]
 
    if (warp == 0) {
       asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
@@ -748,28 +793,13 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train_tc(int rows, int tiles_per
    }
    if (tid == 0)
       mbar_init(bar_s, 1);
-   // weights (read in memory order, coalesced), biases, cleared partials and
-   // the zero columns of Q, once per CTA
-   const __nv_bfloat16 zero = __float2bfloat16(0.f);
-   for (int e = tid; e < MLP_IN * MLP_HID; e += 128)
-      bf(TT_W1T, e % MLP_HID, e / MLP_HID, MLP_IN) = wb[BF_W1 + e];
-   for (int e = tid; e < MLP_HID * MLP_HID; e += 128) {
-      const int a = e / MLP_HID, b = e % MLP_HID;
-      bf(TT_W2T, b, a, MLP_HID) = wb[BF_W2 + e];
-      bf(TT_W2, a, b, MLP_HID) = wb[BF_W2 + e];
-   }
-   for (int e = tid; e < MLP_HID * 16; e += 128) {
-      const int h = e / 16, o = e % 16;
-      const __nv_bfloat16 v = o < MLP_OUT_PAD ? wb[BF_W3 + h * MLP_OUT_PAD + o] : zero;
-      bf(TT_W3T, o, h, MLP_HID) = v;
-      bf(TT_W3, h, o, 16) = v;
-   }
-   for (int c = tid; c < 136; c += 128)
+   // weights, biases, cleared partials and the zero columns of Q, once per CTA
+   stage_weights<TT_THREADS>(tsm, wb, TT_W1T, TT_W2T, TT_W3T, TT_W2, TT_W3);
+   for (int c = tid; c < 136; c += TT_THREADS)
       bias[c] = c < 64 ? w[OFF_B1 + c] : c < 128 ? w[OFF_B2 + c - 64] : w[OFF_B3 + c - 128];
-   for (int c = tid; c < 4 * 136; c += 128)
+   for (int c = tid; c < 4 * 136; c += TT_THREADS)
       bpart[c] = 0.f;
-   for (int e = tid; e < 128 * 4; e += 128)
-      *reinterpret_cast<uint4*>(tsm + TT_Q + kmaj_off(e >> 2, 96 + 8 * (e & 3), 128)) = make_uint4(0, 0, 0, 0);
+   *reinterpret_cast<uint4*>(tsm + TT_Q + kmaj_off(tid >> 2, 96 + 8 * (tid & 3), 128)) = make_uint4(0, 0, 0, 0);
 
    unsigned phase = 0;
    auto sync_tiles = [&]() {
@@ -791,9 +821,9 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train_tc(int rows, int tiles_per
    };
    sync_tiles();
    const unsigned tmem = tmem_slot;
-   const unsigned lane_base = tmem + ((unsigned)(32 * warp) << 16);
+   const unsigned lane_base = tmem + ((unsigned)(32 * quad) << 16);
    // D[dcol..] (+)= A B over K: A at a_off in a tile of width wa, B at b_off
-   // in a tile of width wb_; K-major operands step 16 columns (256 bytes),
+   // in a tile of width wbw; K-major operands step 16 columns (256 bytes),
    // MN-major ones 16 rows (two 8-row groups)
    auto mmas = [&](int dcol, int a_off, int wa, int b_off, int wbw, int K, int n, bool mn, bool acc) {
       const unsigned idesc = tc_idesc(n) | (mn ? (1u << 15) | (1u << 16) : 0u);
@@ -804,39 +834,31 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train_tc(int rows, int tiles_per
             idesc, acc || kk > 0);
       }
    };
-   // hidden layer: z = D + b, h = silu(z) into H columns hcol.. (zero past the rows)
+   // hidden layer: h = silu(D + b) into H columns hcol.. (zero past the rows)
    auto hidden = [&](int dcol, const float* b, int hcol, bool in) {
+      float v[16];
+      tc_ld16(lane_base + dcol + col, v);
 #pragma unroll
-      for (int c0 = 0; c0 < MLP_HID; c0 += 16) {
-         float v[16];
-         tc_ld16(lane_base + dcol + c0, v);
-#pragma unroll
-         for (int i = 0; i < 16; ++i)
-            v[i] = in ? silu(v[i] + b[c0 + i]) : 0.f;
-         st_bf8(tsm + TT_H + kmaj_off(rl, hcol + c0, 128), v);
-         st_bf8(tsm + TT_H + kmaj_off(rl, hcol + c0 + 8, 128), v + 8);
-      }
+      for (int i = 0; i < 16; ++i)
+         v[i] = in ? silu(v[i] + b[col + i]) : 0.f;
+      st_bf8(tsm + TT_H + kmaj_off(rl, hcol + col, 128), v);
+      st_bf8(tsm + TT_H + kmaj_off(rl, hcol + col + 8, 128), v + 8);
    };
    // delta: dZ = dH silu'(z), z = D + b re-read from the forward
    // accumulator; BF16 into (off, width) columns 0-63, FP32 column sums
-   // into bpart[warp][boff..]
+   // into bpart[quad][boff..]
    auto delta = [&](int zcol, const float* b, int off, int width, int boff, bool in) {
-      float cs[MLP_HID];
+      float dh[16], z[16];
+      tc_ld16(lane_base + TT_C_DH + col, dh);
+      tc_ld16(lane_base + zcol + col, z);
 #pragma unroll
-      for (int c0 = 0; c0 < MLP_HID; c0 += 16) {
-         float dh[16], z[16];
-         tc_ld16(lane_base + TT_C_DH + c0, dh);
-         tc_ld16(lane_base + zcol + c0, z);
-#pragma unroll
-         for (int i = 0; i < 16; ++i)
-            cs[c0 + i] = in ? dh[i] * silu_grad(z[i] + b[c0 + i]) : 0.f;
-         st_bf8(tsm + off + kmaj_off(rl, c0, width), cs + c0);
-         st_bf8(tsm + off + kmaj_off(rl, c0 + 8, width), cs + c0 + 8);
-      }
-      float a0, a1;
-      warp_colsum64(cs, lane, a0, a1);
-      bpart[warp * 136 + boff + 2 * lane] += a0;
-      bpart[warp * 136 + boff + 2 * lane + 1] += a1;
+      for (int i = 0; i < 16; ++i)
+         dh[i] = in ? dh[i] * silu_grad(z[i] + b[col + i]) : 0.f;
+      st_bf8(tsm + off + kmaj_off(rl, col, width), dh);
+      st_bf8(tsm + off + kmaj_off(rl, col + 8, width), dh + 8);
+      const float a = warp_colsum16(dh, lane);
+      if ((lane & 1) == 0)
+         bpart[quad * 136 + boff + col + (lane >> 1)] += a;
    };
 
    double se = 0;
@@ -845,10 +867,8 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train_tc(int rows, int tiles_per
       const int r0 = (blockIdx.x + it * gridDim.x) * TC_ROWS;
       if (r0 >= rows)
          break;  // uniform over the CTA
-      // x rows into Q columns 64-95 (16-byte chunks, coalesced)
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-         const int e = tid + 128 * j, rr = e >> 2, ch = e & 3;
+      {  // x rows into Q columns 64-95: one 16-byte chunk per thread, coalesced
+         const int rr = tid >> 2, ch = tid & 3;
          uint4 v = make_uint4(0, 0, 0, 0);
          if (r0 + rr < rows)
             v = __ldg(reinterpret_cast<const uint4*>(x + (size_t)(r0 + rr) * MLP_IN) + ch);
@@ -856,7 +876,8 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train_tc(int rows, int tiles_per
       }
       const int r = r0 + rl;
       const bool in = r < rows;
-      const bool live = in && (!rowpol || rowpol[r % npad] != 0.f);
+      // the loss rows: warps of column group 0
+      const bool live = cg == 0 && in && (!rowpol || rowpol[r % npad] != 0.f);
       float tv[MLP_OUT] = {0.f, 0.f, 0.f};
       if (live)
 #pragma unroll
@@ -884,7 +905,7 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train_tc(int rows, int tiles_per
       }
       wait();
       // loss gradient (k_loss_grad): dY = 2 (y - t) / (3 rows) on live rows
-      {
+      if (cg == 0) {
          float v[16], dy[MLP_OUT_PAD];
          tc_ld16(lane_base + TT_C_D3, v);
 #pragma unroll
@@ -901,7 +922,7 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train_tc(int rows, int tiles_per
          *reinterpret_cast<uint4*>(tsm + TT_G + kmaj_off(rl, 72, 80)) = make_uint4(0, 0, 0, 0);
          const float a = warp_colsum8(dy, lane);
          if ((lane & 3) == 0)
-            bpart[warp * 136 + 128 + (lane >> 2)] += a;
+            bpart[quad * 136 + 128 + (lane >> 2)] += a;
       }
       sync_tiles();
       // dH2 = dY W3^T
@@ -931,30 +952,26 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train_tc(int rows, int tiles_per
 
    // this CTA's gradient vector, in the parameter layout of the master weights
    float* gp = gpart + (size_t)blockIdx.x * MLP_NPARAM;
-   if (warp < 2) {  // lanes 0-63: dW2 rows
+   {
       float v[16];
-#pragma unroll
-      for (int c0 = 0; c0 < MLP_HID; c0 += 16) {
-         tc_ld16(lane_base + TT_C_DWS + c0, v);
+      auto put16 = [&](float* dst) {
 #pragma unroll
          for (int i = 0; i < 16; i += 4)
-            *reinterpret_cast<float4*>(gp + OFF_W2 + rl * MLP_HID + c0 + i) = make_float4(v[i], v[i + 1], v[i + 2],
-               v[i + 3]);
-      }
-   } else {  // lanes 64-127: dW3 rows; lanes 64-95: dW1 rows
-      const int h = rl - 64;
-      float v[16];
-      tc_ld16(lane_base + TT_C_DWS + 64, v);
-      *reinterpret_cast<float4*>(gp + OFF_W3 + h * MLP_OUT_PAD) = make_float4(v[0], v[1], v[2], v[3]);
-      *reinterpret_cast<float4*>(gp + OFF_W3 + h * MLP_OUT_PAD + 4) = make_float4(v[4], v[5], v[6], v[7]);
-      if (warp == 2) {
-#pragma unroll
-         for (int c0 = 0; c0 < MLP_HID; c0 += 16) {
-            tc_ld16(lane_base + TT_C_DW1 + c0, v);
-#pragma unroll
-            for (int i = 0; i < 16; i += 4)
-               *reinterpret_cast<float4*>(gp + OFF_W1 + h * MLP_HID + c0 + i) = make_float4(v[i], v[i + 1],
-                  v[i + 2], v[i + 3]);
+            *reinterpret_cast<float4*>(dst + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+      };
+      if (quad < 2) {  // lanes 0-63: dW2 rows
+         tc_ld16(lane_base + TT_C_DWS + col, v);
+         put16(gp + OFF_W2 + rl * MLP_HID + col);
+      } else {
+         const int h = rl - 64;
+         if (cg == 0) {  // lanes 64-127: dW3 rows
+            tc_ld16(lane_base + TT_C_DWS + 64, v);
+            *reinterpret_cast<float4*>(gp + OFF_W3 + h * MLP_OUT_PAD) = make_float4(v[0], v[1], v[2], v[3]);
+            *reinterpret_cast<float4*>(gp + OFF_W3 + h * MLP_OUT_PAD + 4) = make_float4(v[4], v[5], v[6], v[7]);
+         }
+         if (quad == 2) {  // lanes 64-95: dW1 rows
+            tc_ld16(lane_base + TT_C_DW1 + col, v);
+            put16(gp + OFF_W1 + h * MLP_HID + col);
          }
       }
    }
@@ -968,11 +985,11 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train_tc(int rows, int tiles_per
    }
    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
    __syncthreads();
-   for (int c = tid; c < 136; c += 128) {
+   for (int c = tid; c < 136; c += TT_THREADS) {
       const float a = (bpart[c] + bpart[136 + c]) + (bpart[272 + c] + bpart[408 + c]);
       gp[c < 64 ? OFF_B1 + c : c < 128 ? OFF_B2 + c - 64 : OFF_B3 + c - 128] = a;
    }
-   if (tid == 0)
+   if (tid == 0)  // the loss rows are in warps 0-3
       lpart[blockIdx.x] = (lsum[0] + lsum[1]) + (lsum[2] + lsum[3]);
    if (warp == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -1088,7 +1105,7 @@ static int train_tc(Context* ctx, int rows, const float* rowpol, int npad, bool 
    const int tiles = (rows + TC_ROWS - 1) / TC_ROWS;
    const int per = (tiles + S.sms - 1) / S.sms;
    const int grid = (tiles + per - 1) / per;
-   k_mlp_train_tc<<<grid, 128, TT_SMEM, ctx->stream>>>(rows, per, npad, rowpol, S.x, S.t,
+   k_mlp_train_tc<<<grid, TT_THREADS, TT_SMEM, ctx->stream>>>(rows, per, npad, rowpol, S.x, S.t,
       reinterpret_cast<const __nv_bfloat16*>(S.wb), S.w, S.gpart, S.err, ctx->copy_err);
    auto k = adam ? k_grad_sum<true> : k_grad_sum<false>;
    k<<<(MLP_NPARAM + 31) / 32, 256, 0, ctx->stream>>>(grid, S.gpart, S.err, S.mask, S.g, S.loss, scal, loss_norm, lr,
