@@ -1024,10 +1024,21 @@ __global__ void __launch_bounds__(256) k_grad_sum(int ncta, const float* __restr
    const int pl = threadIdx.x & 31, sl = threadIdx.x >> 5;
    const int p = blockIdx.x * 32 + pl;
    const int t = ADAM ? *step + 1 : 0;
+   // eight independent loads in flight per step (a dependent chain of
+   // global loads would pay the latency per partial)
    float a = 0.f;
    if (p < MLP_NPARAM)
-      for (int c = sl; c < ncta; c += 8)
-         a += gpart[(size_t)c * MLP_NPARAM + p];
+      for (int c0 = sl; c0 < ncta; c0 += 64) {
+         float u[8];
+#pragma unroll
+         for (int k = 0; k < 8; ++k) {
+            const int c = c0 + 8 * k;
+            u[k] = c < ncta ? gpart[(size_t)c * MLP_NPARAM + p] : 0.f;
+         }
+#pragma unroll
+         for (int k = 0; k < 8; ++k)
+            a += u[k];
+      }
    sh[sl][pl] = a;
    __syncthreads();
    if (sl == 0 && p < MLP_NPARAM) {

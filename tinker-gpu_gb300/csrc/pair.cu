@@ -1221,15 +1221,24 @@ __device__ __forceinline__ void desc_pair(const PairParams& P, float r2, float3 
    const float ir3 = invr * invr * invr;
    const float rr3 = us * s3 * ir3;
    const float rr5 = 3.f * us * s5 * ir3 * invr * invr;
-   const int o = r < 3.5f ? 0 : 3;
-   float c = rr5 * (d.x * uk[0] + d.y * uk[1] + d.z * uk[2]);
-   acc[22 + o] += c * d.x - rr3 * uk[0];
-   acc[23 + o] += c * d.y - rr3 * uk[1];
-   acc[24 + o] += c * d.z - rr3 * uk[2];
-   c = rr5 * (d.x * uk[3] + d.y * uk[4] + d.z * uk[5]);
-   acc[28 + o] += c * d.x - rr3 * uk[3];
-   acc[29 + o] += c * d.y - rr3 * uk[4];
-   acc[30 + o] += c * d.z - rr3 * uk[5];
+   const float cd = rr5 * (d.x * uk[0] + d.y * uk[1] + d.z * uk[2]);
+   const float cp = rr5 * (d.x * uk[3] + d.y * uk[4] + d.z * uk[5]);
+   // constant indices in both branches keep acc in registers
+   if (r < 3.5f) {
+      acc[22] += cd * d.x - rr3 * uk[0];
+      acc[23] += cd * d.y - rr3 * uk[1];
+      acc[24] += cd * d.z - rr3 * uk[2];
+      acc[28] += cp * d.x - rr3 * uk[3];
+      acc[29] += cp * d.y - rr3 * uk[4];
+      acc[30] += cp * d.z - rr3 * uk[5];
+   } else {
+      acc[25] += cd * d.x - rr3 * uk[0];
+      acc[26] += cd * d.y - rr3 * uk[1];
+      acc[27] += cd * d.z - rr3 * uk[2];
+      acc[31] += cp * d.x - rr3 * uk[3];
+      acc[32] += cp * d.y - rr3 * uk[4];
+      acc[33] += cp * d.z - rr3 * uk[5];
+   }
 }
 
 __device__ __forceinline__ void to_local(const float* F, const float* v, float* out)
@@ -1318,12 +1327,15 @@ __global__ void __launch_bounds__(256) k_learn_features(PairParams P, int npad, 
    x[20] = l[2];
    for (int c = 0; c < 5; ++c)
       x[21 + c] = acc[17 + c];
-   const int fo = g == 0 ? 22 : 28;
-   to_local(F, acc + fo, l);
+   float f[6];
+#pragma unroll
+   for (int c = 0; c < 6; ++c)
+      f[c] = g == 0 ? acc[22 + c] : acc[28 + c];
+   to_local(F, f, l);
    x[26] = l[0];
    x[27] = l[1];
    x[28] = l[2];
-   to_local(F, acc + fo + 3, l);
+   to_local(F, f + 3, l);
    x[29] = l[0];
    x[30] = l[1];
    x[31] = l[2];
