@@ -585,7 +585,8 @@ int mlp_train_step_tc(Context* ctx, int rows, const float* rowpol, int npad, flo
    double loss_norm);
 int mlp_adamw(Context* ctx, float lr, float wd);
 // learned guess (learn.cu)
-int launch_learn_features(Context* ctx, const float* e8, const float* u8, float* xf);  // pair.cu
+int launch_learn_features(Context* ctx, const float* e8, const float* u8, float* xf, const float* fstat,
+   __nv_bfloat16* xn);  // pair.cu
 // forces (force.cu, pme.cu)
 int force_setup(Context* ctx);
 void force_free(Context* ctx);

@@ -36,8 +36,12 @@ __global__ void k_feature_stats(int npad, const float* __restrict__ xf, const fl
    float* __restrict__ fstat, int* __restrict__ state)
 {
    __shared__ double sh[40];
-   if (state[ST_LREADY] & 1)
+   if (state[ST_LREADY] & 1) {
+      // fixed before this solve: the feature kernel has normalised
+      if (blockIdx.x == 0 && threadIdx.x == 0)
+         state[ST_LREADY] &= ~8;
       return;
+   }
    const int c = blockIdx.x;
    double s1 = 0, s2 = 0, cnt = 0;
    for (int r = threadIdx.x; r < 2 * npad; r += blockDim.x) {
@@ -59,13 +63,17 @@ __global__ void k_feature_stats(int npad, const float* __restrict__ xf, const fl
       fstat[F_ISTD + c] = sd > 1e-6 * (fabs(mean) + 1e-3) ? (float)(1.0 / sd) : 0.f;
    }
    if (last_block(state + ST_TICKET1) && threadIdx.x == 0)
-      state[ST_LREADY] |= 1;
+      state[ST_LREADY] |= 1 | 8;  // bit 3: k_normalize runs in this solve
 }
 
-// BF16 network input: (x - mean) / std, zero rows for padding slots
+// BF16 network input: (x - mean) / std, zero rows for padding slots.  Only
+// in the solve that fixed the statistics (bit 3); afterwards the feature
+// kernel writes it.
 __global__ void k_normalize(int npad, const float* __restrict__ xf, const float* __restrict__ polar,
-   const float* __restrict__ fstat, __nv_bfloat16* __restrict__ x)
+   const float* __restrict__ fstat, const int* __restrict__ state, __nv_bfloat16* __restrict__ x)
 {
+   if (!(state[ST_LREADY] & 8))
+      return;
    const int total = 2 * npad * 32;
    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
       const int r = e / 32, c = e % 32;
@@ -262,10 +270,10 @@ int learn_reset(Context* ctx, unsigned seed)
 int learn_forward(Context* ctx, bool need_y)
 {
    const int npad = ctx->npad;
-   T9_CHECK(launch_learn_features(ctx, ctx->efield, ctx->udir, ctx->xf));
+   T9_CHECK(launch_learn_features(ctx, ctx->efield, ctx->udir, ctx->xf, ctx->fstat, ctx->mlp.x));
    k_feature_stats<<<32, LB, 0, ctx->stream>>>(npad, ctx->xf, ctx->spolar, ctx->fstat, ctx->status);
    k_normalize<<<grid_for(2LL * npad * 32, LB), LB, 0, ctx->stream>>>(npad, ctx->xf, ctx->spolar, ctx->fstat,
-      ctx->mlp.x);
+      ctx->status, ctx->mlp.x);
    T9_CUDA(cudaGetLastError());
    if (need_y || (!ctx->mlp_tc && (ctx->learn_mode & 1)))
       return mlp_forward(ctx, 2 * npad);

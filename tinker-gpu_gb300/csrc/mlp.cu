@@ -1060,13 +1060,18 @@ __global__ void __launch_bounds__(256) k_grad_sum(int ncta, const float* __restr
             wb[wb_index[p]] = __float2bfloat16(wi);
       }
    }
-   if (blockIdx.x == 0 && threadIdx.x == 32) {
+   if (blockIdx.x == 0 && sl == 1) {  // the squared errors: lane strides, then a fixed butterfly
       double l = 0;
-      for (int c = 0; c < ncta; ++c)
+      for (int c = pl; c < ncta; c += 32)
          l += lpart[c];
-      *loss = l;
-      if (scal)
-         *scal = l * loss_norm;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1)
+         l += __shfl_xor_sync(0xffffffffu, l, o);
+      if (pl == 0) {
+         *loss = l;
+         if (scal)
+            *scal = l * loss_norm;
+      }
    }
    if (ADAM) {
       __shared__ bool last;

@@ -1190,6 +1190,25 @@ __device__ __forceinline__ float gauss(float r, float mu, float inv2s2)
    return __expf(-t * t * inv2s2);
 }
 
+// acc[j] += w g(r; mu0 + j dmu, s), j < N, c = 1 / (2 s^2), by the product
+// recurrence g_{j+1} = g_j R_j, R_j = exp(c (2 dmu (r - mu0) - dmu^2))
+// exp(-2 c dmu^2)^j: two exponentials per series instead of N (relative
+// error a few units of 1e-7 over the series)
+template <int N>
+__device__ __forceinline__ void gauss_series(float r, float mu0, float dmu, float c, float w, float* acc)
+{
+   const float t = r - mu0;
+   float g = __expf(-t * t * c);
+   float R = __expf(c * (2.f * dmu * t - dmu * dmu));
+   const float B = __expf(-2.f * c * dmu * dmu);  // constant: folded by the compiler
+#pragma unroll
+   for (int j = 0; j < N; ++j) {
+      acc[j] += w * g;
+      g *= R;
+      R *= B;
+   }
+}
+
 // acc layout: gr[0..7) gq[7..11) dq[11..17) ga[17..22) fd[22..28) fp[28..34)
 constexpr int DACC = 34;
 
@@ -1199,12 +1218,8 @@ __device__ __forceinline__ void desc_pair(const PairParams& P, float r2, float3 
    const float invr = rsqrtf(r2);
    const float r = r2 * invr;
    const float fc = 0.5f * (__cosf(3.14159265f / DESC_CUT * r) + 1.f);
-#pragma unroll
-   for (int j = 0; j < 7; ++j)
-      acc[j] += fc * gauss(r, 1.f + (5.f / 6.f) * j, 2.f);
-#pragma unroll
-   for (int j = 0; j < 4; ++j)
-      acc[7 + j] += qk * fc * gauss(r, 1.5f * (j + 1), 1.f / (2.f * 0.75f * 0.75f));
+   gauss_series<7>(r, 1.f, 5.f / 6.f, 2.f, fc, acc);
+   gauss_series<4>(r, 1.5f, 1.5f, 1.f / (2.f * 0.75f * 0.75f), qk * fc, acc + 7);
    const float h0 = qk * fc * gauss(r, 2.f, 0.5f) * invr, h1 = qk * fc * gauss(r, 4.5f, 0.5f) * invr;
    acc[11] += h0 * d.x;
    acc[12] += h0 * d.y;
@@ -1212,10 +1227,7 @@ __device__ __forceinline__ void desc_pair(const PairParams& P, float r2, float3 
    acc[14] += h1 * d.x;
    acc[15] += h1 * d.y;
    acc[16] += h1 * d.z;
-   const float polk = uk[7];
-#pragma unroll
-   for (int j = 0; j < 5; ++j)
-      acc[17 + j] += polk * fc * gauss(r, 1.f + 1.25f * j, 1.f / (2.f * 0.6f * 0.6f));
+   gauss_series<5>(r, 1.f, 1.25f, 1.f / (2.f * 0.6f * 0.6f), uk[7] * fc, acc + 17);
    float s3, s5, s7;
    thole_damp(r, pdi, pair_gamma(P, pti, uk[6]), pdk, s3, s5, s7);
    const float ir3 = invr * invr * invr;
@@ -1253,12 +1265,15 @@ __global__ void __launch_bounds__(256) k_learn_features(PairParams P, int npad, 
    const int* __restrict__ nnbr, const int* __restrict__ sp_start, const int* __restrict__ sp_j,
    const float4* __restrict__ sp_sc, const float4* __restrict__ spos, const float* __restrict__ srpole,
    const float* __restrict__ sframe, const float* __restrict__ e8, const float* __restrict__ u8,
-   float* __restrict__ xf)
+   float* __restrict__ xf, const float* __restrict__ polar, const float* __restrict__ fstat,
+   const int* __restrict__ state, __nv_bfloat16* __restrict__ xn)
 {
    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
    const int i = tid / G, g = tid % G;
    if (i >= npad)
       return;
+   // with the column statistics fixed (bit 0), also the BF16 network input
+   const bool norm = (state[ST_LREADY] & 1) != 0;
    float acc[DACC];
 #pragma unroll
    for (int c = 0; c < DACC; ++c)
@@ -1296,58 +1311,71 @@ __global__ void __launch_bounds__(256) k_learn_features(PairParams P, int npad, 
    if (g >= 2)
       return;
    // lane 0 writes the d row, lane 1 the p row
-   float* x = xf + (size_t)(g == 0 ? i : npad + i) * NFEAT;
-   if (i >= P.n) {
-      for (int c = 0; c < NFEAT; ++c)
-         x[c] = 0.f;
-      return;
-   }
-   float F[9];
-   for (int c = 0; c < 9; ++c)
-      F[c] = sframe[9 * i + c];
-   float v[3], l[3];
-   for (int c = 0; c < 3; ++c)
-      v[c] = e8[8 * i + 3 * g + c];
-   to_local(F, v, l);
-   x[0] = l[0];
-   x[1] = l[1];
-   x[2] = l[2];
-   x[3] = u8[8 * i + 7];
-   for (int c = 0; c < 7; ++c)
-      x[4 + c] = acc[c];
-   for (int c = 0; c < 4; ++c)
-      x[11 + c] = acc[7 + c];
-   to_local(F, acc + 11, l);
-   x[15] = l[0];
-   x[16] = l[1];
-   x[17] = l[2];
-   to_local(F, acc + 14, l);
-   x[18] = l[0];
-   x[19] = l[1];
-   x[20] = l[2];
-   for (int c = 0; c < 5; ++c)
-      x[21 + c] = acc[17 + c];
-   float f[6];
+   const size_t row = (size_t)(g == 0 ? i : npad + i);
+   float x[NFEAT];
 #pragma unroll
-   for (int c = 0; c < 6; ++c)
-      f[c] = g == 0 ? acc[22 + c] : acc[28 + c];
-   to_local(F, f, l);
-   x[26] = l[0];
-   x[27] = l[1];
-   x[28] = l[2];
-   to_local(F, f + 3, l);
-   x[29] = l[0];
-   x[30] = l[1];
-   x[31] = l[2];
+   for (int c = 0; c < NFEAT; ++c)
+      x[c] = 0.f;
+   if (i < P.n) {
+      float F[9];
+#pragma unroll
+      for (int c = 0; c < 9; ++c)
+         F[c] = sframe[9 * i + c];
+      float v[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+         v[c] = e8[8 * i + 3 * g + c];
+      to_local(F, v, x);
+      x[3] = u8[8 * i + 7];
+#pragma unroll
+      for (int c = 0; c < 7; ++c)
+         x[4 + c] = acc[c];
+#pragma unroll
+      for (int c = 0; c < 4; ++c)
+         x[11 + c] = acc[7 + c];
+      to_local(F, acc + 11, x + 15);
+      to_local(F, acc + 14, x + 18);
+#pragma unroll
+      for (int c = 0; c < 5; ++c)
+         x[21 + c] = acc[17 + c];
+      float f[6];
+#pragma unroll
+      for (int c = 0; c < 6; ++c)
+         f[c] = g == 0 ? acc[22 + c] : acc[28 + c];
+      to_local(F, f, x + 26);
+      to_local(F, f + 3, x + 29);
+   }
+   float4* xo = reinterpret_cast<float4*>(xf + row * NFEAT);
+#pragma unroll
+   for (int c = 0; c < NFEAT; c += 4)
+      xo[c / 4] = make_float4(x[c], x[c + 1], x[c + 2], x[c + 3]);
+   if (norm) {  // as k_normalize: (x - mean) / std, zero rows where alpha = 0
+      const bool live = polar[i] != 0.f;
+      uint4* q = reinterpret_cast<uint4*>(xn + row * NFEAT);
+#pragma unroll
+      for (int c = 0; c < NFEAT; c += 8) {
+         unsigned wv[4];
+#pragma unroll
+         for (int k = 0; k < 4; ++k) {
+            const int a = c + 2 * k;
+            const float v0 = live ? (x[a] - fstat[a]) * fstat[32 + a] : 0.f;
+            const float v1 = live ? (x[a + 1] - fstat[a + 1]) * fstat[32 + a + 1] : 0.f;
+            const __nv_bfloat162 b = __floats2bfloat162_rn(v0, v1);
+            wv[k] = *reinterpret_cast<const unsigned*>(&b);
+         }
+         q[c / 8] = make_uint4(wv[0], wv[1], wv[2], wv[3]);
+      }
+   }
 }
 
-int launch_learn_features(Context* ctx, const float* e8, const float* u8, float* xf)
+int launch_learn_features(Context* ctx, const float* e8, const float* u8, float* xf, const float* fstat,
+   __nv_bfloat16* xn)
 {
    PairParams P = make_params(ctx, DESC_CUT);
    k_learn_features<GROUP><<<grid_for((long long)ctx->npad * GROUP, PAIR_THREADS), PAIR_THREADS, 0, ctx->stream>>>(P,
       ctx->npad, ctx->cfg.cutoff >= DESC_CUT ? ctx->nbrc : ctx->nbr, ctx->cfg.cutoff >= DESC_CUT ? ctx->nnbrc : ctx->nnbr,
-      ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos, ctx->srpole, ctx->sframe, e8,
-      u8, xf);
+      ctx->sp_start, ctx->sp_j, ctx->sp_sc, ctx->spos, ctx->srpole, ctx->sframe, e8, u8, xf, ctx->spolar, fstat,
+      ctx->status, xn);
    T9_CUDA(cudaGetLastError());
    return T9GB_OK;
 }

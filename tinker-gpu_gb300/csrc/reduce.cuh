@@ -11,7 +11,8 @@ namespace t9gb {
 enum { S_SUM_D = 0, S_SUM_P, S_A_D, S_A_P, S_B_D, S_B_P, S_EPS, S_L_PLAIN_D = 8, S_L_PLAIN_P, S_L_LEARN_D,
    S_L_LEARN_P, S_L_LOSS, S_NSCAL = 16 };
 // ST_LCHOICE: bit 0 / 1 set when the d / p solve started from the learned
-// guess; ST_LREADY: bit 0 feature statistics, bit 1 target scale fixed
+// guess; ST_LREADY: bit 0 feature statistics, bit 1 target scale fixed,
+// bit 3 statistics fixed in this solve (k_normalize writes the network input)
 // ST_RANGE: a dipole-grid contribution reached the packed fixed-point guard;
 // ST_RANGE_L: the same while evaluating the learned guess's residual;
 // ST_TICKET_SUM: the last-block ticket of the energy / virial row sums
