@@ -465,15 +465,15 @@ int t9gb_learn_eval(t9gb_context* ctx, int rows, const float* x, const float* t,
 /* One AdamW step (beta 0.9/0.999, eps 1e-8) with the gradient of the last
  * t9gb_learn_eval. */
 int t9gb_learn_adamw(t9gb_context* ctx);
-/* Tensor-core path of the network's forward pass: 1 (default) one fused
- * kernel per 128 rows on the fifth-generation tensor cores (tcgen05.mma with
- * the accumulators in tensor memory, read back with tcgen05.ld for the bias
- * and SiLU epilogue of each layer); 0 the warp-level mma.sync GEMMs with
- * separate bias / SiLU kernels.  Same outputs (bit-identical in the tests:
- * both sum the same 16-term products into FP32).  The backward pass uses the
- * mma.sync GEMMs either way.  GB300, 12,288 atoms: a solve comparing the
- * learned and plain starts 0.884 -> 0.857 ms, a training solve 1.054 ->
- * 1.045 ms. */
+/* Tensor-core path of the network: 1 (default) the fifth-generation tensor
+ * cores (tcgen05.mma, accumulators in tensor memory): one fused kernel per
+ * 128 rows for the forward pass, and for training one persistent kernel
+ * that recomputes the forward pass and accumulates the weight gradients in
+ * tensor memory, then one kernel for the fixed-order gradient sum and the
+ * AdamW step; 0 the warp-level mma.sync GEMMs with separate bias, SiLU,
+ * loss, column-sum and AdamW kernels.  Same rounding points (gradients
+ * within 1.2e-7 relative in the tests).  GB300, 12,288 atoms: a training
+ * solve 1.045 (path 0) -> 0.860 ms (plain 0.789 ms). */
 int t9gb_learn_tensor_path(t9gb_context* ctx, int path);
 /* Raw features of the last solve, device [2n][32]: rows 0..n-1 for the d
  * dipoles, n..2n-1 for the p dipoles, caller atom order. */
