@@ -165,7 +165,7 @@ const char* t9gb_status_string(int status)
    case T9GB_NOT_READY:
       return "topology, coordinates or neighbour list missing";
    case T9GB_TOO_LARGE:
-      return "input larger than a fixed capacity";
+      return "input larger than a fixed-capacity entry point or buffer holds";
    default:
       return "unknown status";
    }

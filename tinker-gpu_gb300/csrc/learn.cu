@@ -272,8 +272,9 @@ int learn_forward(Context* ctx, bool need_y)
    const int npad = ctx->npad;
    T9_CHECK(launch_learn_features(ctx, ctx->efield, ctx->udir, ctx->xf, ctx->fstat, ctx->mlp.x));
    k_feature_stats<<<32, LB, 0, ctx->stream>>>(npad, ctx->xf, ctx->spolar, ctx->fstat, ctx->status);
-   k_normalize<<<grid_for(2LL * npad * 32, LB), LB, 0, ctx->stream>>>(npad, ctx->xf, ctx->spolar, ctx->fstat,
-      ctx->status, ctx->mlp.x);
+   // grid-stride: usually every block returns at once
+   k_normalize<<<std::min(512, grid_for(2LL * npad * 32, LB)), LB, 0, ctx->stream>>>(npad, ctx->xf, ctx->spolar,
+      ctx->fstat, ctx->status, ctx->mlp.x);
    T9_CUDA(cudaGetLastError());
    if (need_y || (!ctx->mlp_tc && (ctx->learn_mode & 1)))
       return mlp_forward(ctx, 2 * npad);

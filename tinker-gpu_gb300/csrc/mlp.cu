@@ -435,16 +435,16 @@ int mlp_get_weights(Context* ctx, float* w_host)
 
 // ---------------------------------------------------------------------------
 // Forward pass on the fifth-generation tensor cores (tcgen05): one CTA of
-// four warps per 128 rows.  The row tile and the transposed weights are
+// 16 warps per 128 rows.  The row tile and the transposed weights are
 // staged in shared memory in the canonical K-major layout without swizzle
 // (8-row x 16-byte core matrices; LBO = 128 B between core matrices along K,
 // SBO = K / 8 x 128 B between 8-row groups), one thread issues the
 // tcgen05.mma instructions (M = 128, K = 16 per instruction, BF16 in, FP32
 // accumulated in tensor memory), tcgen05.commit signals an mbarrier, and each
-// warp reads its 32 rows back with tcgen05.ld for the bias + SiLU epilogue,
-// which writes the next layer's operand tile.  The outputs are those of the
-// mma.sync path (z1, h1, z2, h2, y), equal to them up to the order of the
-// FP32 accumulation inside the MMA.
+// warp reads 16 columns of its 32 rows back with tcgen05.ld for the bias +
+// SiLU epilogue, which writes the next layer's operand tile.  The outputs
+// are those of the mma.sync path, equal to them up to the order of the FP32
+// accumulation inside the MMA.
 
 constexpr int TC_ROWS = 128;  // also the tile of S.gpart
 constexpr int TC_TMEM_COLS = 128;  // D1 in columns 0-63, D2 in 64-127, D3 in 0-15
@@ -583,15 +583,21 @@ constexpr int TC_SX = 0, TC_SH1 = TC_SX + 128 * 32 * 2, TC_SH2 = TC_SH1 + 128 * 
 constexpr int TC_SW1 = TC_SH2 + 128 * 64 * 2, TC_SW2 = TC_SW1 + 64 * 32 * 2, TC_SW3 = TC_SW2 + 64 * 64 * 2;
 constexpr int TC_SMEM = TC_SW3 + 16 * 64 * 2;  // 55,296 bytes: at most four CTAs per SM, 4 x 128 TMEM columns
 
-// inference: stores only y (the training pass recomputes the activations)
-__global__ void __launch_bounds__(128) k_mlp_forward_tc(int rows, const __nv_bfloat16* __restrict__ x,
+// inference: stores only y (the training pass recomputes the activations).
+// 16 warps: warp w reads TMEM lanes 32 (w % 4) .. + 31 (its rows) and
+// columns 16 (w / 4) .. + 15 of each 64-column accumulator.
+constexpr int TC_THREADS = 512;
+
+__global__ void __launch_bounds__(TC_THREADS, 2) k_mlp_forward_tc(int rows, const __nv_bfloat16* __restrict__ x,
    const __nv_bfloat16* __restrict__ wb, const float* __restrict__ w, float* __restrict__ y, int* __restrict__ err)
 {
    extern __shared__ __align__(128) unsigned char tsm[];
    __shared__ __align__(8) unsigned long long bar;
    __shared__ unsigned tmem_slot;
    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+   const int quad = warp & 3, col = 16 * (warp >> 2);
    const int r0 = blockIdx.x * TC_ROWS;
+   const int rl = 32 * quad + lane, r = r0 + rl;  // this thread's row
    const unsigned base = (unsigned)__cvta_generic_to_shared(tsm);
    const unsigned bar_s = (unsigned)__cvta_generic_to_shared(&bar);
 
@@ -605,22 +611,22 @@ __global__ void __launch_bounds__(128) k_mlp_forward_tc(int rows, const __nv_bfl
    }
    if (tid == 0)
       mbar_init(bar_s, 1);
-   // operand tiles: the input rows (16-byte chunks) and the transposed weights
-   for (int e = tid; e < TC_ROWS * MLP_IN / 8; e += 128) {
-      const int r = e >> 2, ch = e & 3;
-      const uint4 v = r0 + r < rows ? __ldg(reinterpret_cast<const uint4*>(x + (size_t)(r0 + r) * MLP_IN) + ch)
-                                    : make_uint4(0, 0, 0, 0);
-      *reinterpret_cast<uint4*>(tsm + TC_SX + kmaj_off(r, 8 * ch, MLP_IN)) = v;
+   // operand tiles: the input rows (one 16-byte chunk per thread) and the
+   // transposed weights
+   {
+      const int rr = tid >> 2, ch = tid & 3;
+      const uint4 v = r0 + rr < rows ? __ldg(reinterpret_cast<const uint4*>(x + (size_t)(r0 + rr) * MLP_IN) + ch)
+                                     : make_uint4(0, 0, 0, 0);
+      *reinterpret_cast<uint4*>(tsm + TC_SX + kmaj_off(rr, 8 * ch, MLP_IN)) = v;
    }
-   stage_weights<128>(tsm, wb, TC_SW1, TC_SW2, TC_SW3, -1, -1);
+   stage_weights<TC_THREADS>(tsm, wb, TC_SW1, TC_SW2, TC_SW3, -1, -1);
    // the tiles (generic proxy) before the tensor core reads them (async proxy)
    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
    __syncthreads();
    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
    const unsigned tmem = tmem_slot;
-   const unsigned lane_base = tmem + ((unsigned)(32 * warp) << 16);
-   const int r = r0 + 32 * warp + lane;  // this thread's row
+   const unsigned lane_base = tmem + ((unsigned)(32 * quad) << 16);
    unsigned phase = 0;
 
    // one layer: D[columns dcol..] = A B over K (K / 16 MMAs), then wait
@@ -645,16 +651,13 @@ __global__ void __launch_bounds__(128) k_mlp_forward_tc(int rows, const __nv_bfl
    // hidden layer epilogue: h = silu(D + b) into the next operand tile
    // (zero past the rows)
    auto hidden = [&](unsigned dcol, const float* b, unsigned h_off) {
+      float v[16];
+      tc_ld16(lane_base + dcol + col, v);
 #pragma unroll
-      for (int c0 = 0; c0 < MLP_HID; c0 += 16) {
-         float v[16];
-         tc_ld16(lane_base + dcol + c0, v);
-#pragma unroll
-         for (int i = 0; i < 16; ++i)
-            v[i] = r < rows ? silu(v[i] + b[c0 + i]) : 0.f;
-         st_bf8(tsm + h_off + kmaj_off(32 * warp + lane, c0, MLP_HID), v);
-         st_bf8(tsm + h_off + kmaj_off(32 * warp + lane, c0 + 8, MLP_HID), v + 8);
-      }
+      for (int i = 0; i < 16; ++i)
+         v[i] = r < rows ? silu(v[i] + b[col + i]) : 0.f;
+      st_bf8(tsm + h_off + kmaj_off(rl, col, MLP_HID), v);
+      st_bf8(tsm + h_off + kmaj_off(rl, col + 8, MLP_HID), v + 8);
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       __syncthreads();
@@ -666,13 +669,14 @@ __global__ void __launch_bounds__(128) k_mlp_forward_tc(int rows, const __nv_bfl
    layer(TC_SH1, TC_SW2, MLP_HID, MLP_HID, 64);
    hidden(64, w + OFF_B2, TC_SH2);
    layer(TC_SH2, TC_SW3, MLP_HID, 16, 0);
-   {
+   if (col == 0) {
       float v[16];
       tc_ld16(lane_base, v);
-      if (r < rows)
-#pragma unroll
-         for (int c = 0; c < MLP_OUT_PAD; ++c)
-            y[(size_t)r * MLP_OUT_PAD + c] = v[c] + w[OFF_B3 + c];
+      if (r < rows) {
+         float4* yo = reinterpret_cast<float4*>(y + (size_t)r * MLP_OUT_PAD);
+         yo[0] = make_float4(v[0] + w[OFF_B3], v[1] + w[OFF_B3 + 1], v[2] + w[OFF_B3 + 2], v[3] + w[OFF_B3 + 3]);
+         yo[1] = make_float4(v[4] + w[OFF_B3 + 4], v[5] + w[OFF_B3 + 5], v[6] + w[OFF_B3 + 6], v[7] + w[OFF_B3 + 7]);
+      }
    }
    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
    __syncthreads();
@@ -1094,7 +1098,7 @@ int mlp_forward(Context* ctx, int rows)
    MlpState& S = ctx->mlp;
    const __nv_bfloat16* wb = reinterpret_cast<const __nv_bfloat16*>(S.wb);
    if (ctx->mlp_tc) {
-      k_mlp_forward_tc<<<grid_for(rows, TC_ROWS), 128, TC_SMEM, ctx->stream>>>(rows, S.x, wb, S.w, S.y,
+      k_mlp_forward_tc<<<grid_for(rows, TC_ROWS), TC_THREADS, TC_SMEM, ctx->stream>>>(rows, S.x, wb, S.w, S.y,
          ctx->copy_err);
       T9_CUDA(cudaGetLastError());
       return T9GB_OK;
