@@ -64,6 +64,8 @@ def parse():
                     help="lanes per atom in the real-space field kernels (0: the library's choice by box size)")
     ap.add_argument("--no-flush", action="store_true",
                     help="skip the 512 MB L2 flush buffer (for ncu captures only; numbers are not bench values)")
+    ap.add_argument("--stepwise", action="store_true",
+                    help="learned legs without CUDA graphs, so that ncu sees each launch (numbers are not bench values)")
     return ap.parse_args()
 
 
@@ -496,6 +498,8 @@ def learned_legs(args, s, abi, stream, dev, flush, check_oracle):
     for pred, name in ((0, "direct"), (1, "aspc")):
         eng = abi.Engine(s, predictor=pred, stream=stream)
         eng.prepare(dev[0].double().cpu().numpy())
+        if args.stepwise:
+            eng.use_graph(False)
         eng.learn_reset(seed=1)
         eng.learn_config(1)
         t0 = time.perf_counter()
