@@ -172,10 +172,13 @@ __global__ void k_precond_dot(VecArgs A, const float* __restrict__ rsd, float* _
 // Ap = p/alpha - ufield(p); partials p.Ap; last block: a = s / p.Ap.
 // DIR: p = z + b p_old is formed here (as the field kernels formed it) and
 // stored.
+// fld2 (may be null): the reciprocal + self part, stored apart from the
+// real-space part in fld; the field is fld + fld2, the sum the gather forms
+// when it adds itself to the real-space field.
 template <bool DIR>
-__global__ void k_pcg_p1(VecArgs A, const float* __restrict__ fld, float* __restrict__ conj,
-   const float* __restrict__ zrsd, float* __restrict__ vec, double* __restrict__ red, double* __restrict__ scal,
-   int* __restrict__ state)
+__global__ void k_pcg_p1(VecArgs A, const float* __restrict__ fld, const float* __restrict__ fld2,
+   float* __restrict__ conj, const float* __restrict__ zrsd, float* __restrict__ vec, double* __restrict__ red,
+   double* __restrict__ scal, int* __restrict__ state)
 {
    pdl_wait();
    __shared__ double sh[64];
@@ -192,7 +195,8 @@ __global__ void k_pcg_p1(VecArgs A, const float* __restrict__ fld, float* __rest
          p = __fmaf_rn(e - 6 * s < 3 ? bd : bp, p, zrsd[x]);
          conj[x] = p;
       }
-      const float v = A.polinv[s] * p - fld[x];
+      const float f = fld2 ? fld[x] + fld2[x] : fld[x];
+      const float v = A.polinv[s] * p - f;
       vec[x] = v;
       if (e - 6 * s < 3)
          dd += p * v;
@@ -525,18 +529,37 @@ static int pcg_body(Context* ctx, const VecArgs& A, cudaGraphConditionalHandle h
          T9_CHECK(launch_ufield_recip_gather_ap(ctx, ctx->fld6, P));
       } else {
          T9_CHECK(launch_ufield_recip_gather_dir(ctx, ctx->fld6, P));
-         k_pcg_p1<true><<<A.nb, VB, 0, ctx->stream>>>(A, ctx->fld6, ctx->conj, ctx->zrsd, ctx->vec, ctx->red,
-            ctx->scal, ctx->status);
+         k_pcg_p1<true><<<A.nb, VB, 0, ctx->stream>>>(A, ctx->fld6, nullptr, ctx->conj, ctx->zrsd, ctx->vec,
+            ctx->red, ctx->scal, ctx->status);
       }
    } else {
       const bool pdl = use_pdl(ctx);
       prof_begin(ctx, P_VECTOR);
       T9_CUDA(launch_k(pdl, k_pcg_dir, A.nb, VB, 0, ctx->stream, A, ctx->scal, ctx->conj, ctx->zrsd));
       prof_end(ctx);
-      T9_CHECK(ufield6(ctx, ctx->conj, ctx->fld6));
+      const float* rcp = nullptr;
+      if (ctx->cfg.use_ewald && (ctx->pcg_fuse & 32) && !ctx->prof.on) {
+         // the gather follows the transform on the side stream (a programmatic
+         // dependent of its last pass, so its position-only prologue overlaps
+         // it) into rcp6; the Ap kernel adds it to the real-space field
+         const int k = side_index(ctx);
+         T9_CHECK(recip_fork(ctx, k));
+         cudaStream_t main = ctx->stream;
+         ctx->stream = ctx->side_stream[k];
+         int rc = launch_ufield_recip_grid(ctx, ctx->conj);
+         if (rc == T9GB_OK)
+            rc = launch_ufield_recip_gather(ctx, ctx->conj, ctx->rcp6, false);
+         ctx->stream = main;
+         T9_CHECK(rc);
+         T9_CHECK(launch_ufield_real(ctx, ctx->conj, nullptr, ctx->fld6));
+         T9_CHECK(recip_join(ctx, k));
+         rcp = ctx->rcp6;
+      } else {
+         T9_CHECK(ufield6(ctx, ctx->conj, ctx->fld6));
+      }
       prof_begin(ctx, P_VECTOR);
-      T9_CUDA(launch_k(pdl, k_pcg_p1<false>, A.nb, VB, 0, ctx->stream, A, ctx->fld6, ctx->conj, nullptr, ctx->vec,
-         ctx->red, ctx->scal, ctx->status));
+      T9_CUDA(launch_k(pdl, k_pcg_p1<false>, A.nb, VB, 0, ctx->stream, A, ctx->fld6, rcp, ctx->conj, nullptr,
+         ctx->vec, ctx->red, ctx->scal, ctx->status));
       prof_end(ctx);
    }
    prof_begin(ctx, P_VECTOR);

@@ -308,7 +308,10 @@ __global__ void k_conv(size_t ng, const float* __restrict__ infl, float2* __rest
 // p and Ap = p/alpha - field, and the block partials of p.Ap give, in the
 // last block, the step length a = s / p.Ap.  Atoms are visited warp-strided
 // over at most RED_MAX blocks.
-template <int MODE, bool ACC, bool AP, bool DIR>
+// LATE: the kernel has not waited for its programmatic predecessor yet; the
+// site and the B-splines (positions only) are formed first, then the wait,
+// then the grid and dipole reads, so the prologue overlaps the predecessor.
+template <int MODE, bool ACC, bool AP, bool DIR, bool LATE = false>
 __device__ __forceinline__ void gather_atom(int s, int lane, const GridParams& G, const float4* __restrict__ spos,
    const float2* __restrict__ g, const float* __restrict__ rp, const float* __restrict__ u8, float* __restrict__ out,
    const PcgAp& P, float bd, float bp, float* pap)
@@ -317,11 +320,13 @@ __device__ __forceinline__ void gather_atom(int s, int lane, const GridParams& G
    float w1, w2, w3;
    site(G, spos[s], i1, i2, i3, w1, w2, w3);
    float acc[6] = {0, 0, 0, 0, 0, 0};
+   float t1[5][2], t2[5][2], t3[5][2];
+   bspline5<2>(w1, t1);
+   bspline5<2>(w2, t2);
+   bspline5<2>(w3, t3);
+   if (LATE)
+      pdl_wait();
    if (lane < 25) {
-      float t1[5][2], t2[5][2], t3[5][2];
-      bspline5<2>(w1, t1);
-      bspline5<2>(w2, t2);
-      bspline5<2>(w3, t3);
       const int jy = lane % 5, kz = lane / 5;
       int zb = i3 + kz;
       zb -= (zb >= G.n3 ? G.n3 : 0);
@@ -412,7 +417,10 @@ __global__ void __launch_bounds__(256, 6) k_gather_field(int n, GridParams G, co
    const float2* __restrict__ g, const float* __restrict__ rp, const float* __restrict__ u8, float* __restrict__ out,
    PcgAp P)
 {
-   pdl_wait();
+   // the plain gather waits inside gather_atom, after its position-only prologue
+   constexpr bool LATE = !AP && !DIR;
+   if (!LATE)
+      pdl_wait();
    const int lane = threadIdx.x & 31;
    if (!AP) {
       const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -422,7 +430,9 @@ __global__ void __launch_bounds__(256, 6) k_gather_field(int n, GridParams G, co
          bp = (float)P.scal[S_B_P];
       }
       if (s < n)
-         gather_atom<MODE, ACC, false, DIR>(s, lane, G, spos, g, rp, u8, out, P, bd, bp, nullptr);
+         gather_atom<MODE, ACC, false, DIR, LATE>(s, lane, G, spos, g, rp, u8, out, P, bd, bp, nullptr);
+      else if (LATE)
+         pdl_wait();
       return;
    }
    __shared__ double sh[64];
@@ -676,6 +686,7 @@ __global__ void __launch_bounds__(N * fft_threads_per_line<N>()) k_fft_plane(lon
    float2* __restrict__ g, int packed, float inv)
 {
    pdl_wait();
+   pdl_trigger();  // the next kernel may stage its blocks and run its prologue
    // element (y, x) at fsm[fsig(y) LD + fsig(x)]; the padding keeps the two
    // lines of a 16-thread shared-memory phase on different banks
    constexpr int T = fft_threads_per_line<N>(), LD = fft_plane_ld<N>(), NT = N * T, R = N / T;
@@ -732,6 +743,7 @@ __global__ void __launch_bounds__(16 * fft_threads_per_line<N>()) k_fft_zline(co
    float2* __restrict__ g)
 {
    pdl_wait();
+   pdl_trigger();  // the next kernel may stage its blocks and run its prologue
    // element z of line l at sm[fsig(z) LD + l]
    constexpr int T = fft_threads_per_line<N>(), XL = 16, LD = fft_zline_ld<N>(), NT = XL * T, R = N / T;
    __shared__ float2 sm[N * LD];
