@@ -369,7 +369,7 @@ int t9gb_pair_lanes(t9gb_context* ctx, int lanes);
  * 4.071, 8 0.768 / 4.148, 16 0.797 / 4.355 (1 and 2 are not built). */
 int t9gb_force_lanes(t9gb_context* ctx, int lanes);
 
-/* Kernel fusion and overlap of the CG solve (bit mask; default 25 = 16 | 8 | 1).  Bit 0: the
+/* Kernel fusion and overlap of the CG solve (bit mask; default 121 = 64 | 32 | 16 | 8 | 1).  Bit 0: the
  * sparse preconditioner also forms r.z, r.r and the CG scalars (else a
  * separate dot kernel, sparsePrecondApply + the dot products of
  * src/cu/amoeba/pcg.cu:120-150).  Bit 1 (PME only): the search direction
@@ -385,8 +385,17 @@ int t9gb_force_lanes(t9gb_context* ctx, int lanes);
  * programmatic dependents of the kernel before them on their stream: each
  * is scheduled while its predecessor drains and waits for it at its start
  * (griddepcontrol), which gives the same results as plain launches; GB300:
- * 0.527 -> 0.514 ms at 12,288 atoms, 2.313 -> 2.293 ms at 98,304.  A tuning
- * knob: the same iteration, results equal
+ * 0.527 -> 0.514 ms at 12,288 atoms, 2.313 -> 2.293 ms at 98,304.  Bit 5
+ * (PME, without bit 1): the search direction's gather runs right after the
+ * transform on the reciprocal stream, as a programmatic dependent of its
+ * last pass (the spread and the gather form their B-splines, which need
+ * the positions only, before they wait), and stores recip + self apart; the
+ * Ap kernel adds it to the real-space field, the sum the gather would form.
+ * Bit 6 (with bit 5): that chain stays on the main stream behind the
+ * direction kernel and the real-space field runs on the side stream.  Bits
+ * 5-6 give the same bits as without them; GB300 (induce ms, 12,288 /
+ * 98,304 atoms): mask 25 0.4925 / 2.344, 57 0.4829 / 2.297, 121 (the
+ * default) 0.473 / 2.285.  A tuning knob: the same iteration, results equal
  * up to the order of the partial sums.  Measured on GB300 (induce ms per
  * step, 12,288 / 98,304 atoms): mask 0 0.612 / 2.889, 1 0.609 / 2.853,
  * 3 0.606 / 2.959, 7 0.632 / 2.962.  Bit 1 makes the real-space kernel read

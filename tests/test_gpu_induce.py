@@ -249,29 +249,30 @@ def test_predicted_start_overlap_is_bit_identical(gpu_lib, tg):
 
 @pytest.mark.parametrize("name", ["water648", "water12288"])
 def test_side_gather_bit_identical(gpu_lib, tg, name):
-    """Fusion bit 5 moves the CG direction's gather onto the side stream
-    behind the transform (recip + self stored apart, added to the real-space
-    field by the Ap kernel): the same operands in the same order, so the
-    same bits as the gather that adds itself, in the graph and in the
-    host-driven loop, over a predictor trajectory."""
+    """Fusion bit 5 moves the CG direction's gather behind the transform on
+    the reciprocal stream (recip + self stored apart, added to the
+    real-space field by the Ap kernel), bit 6 keeps that chain on the main
+    stream and the real-space field on the side stream: the same operands in
+    the same order, so the same bits as the gather that adds itself, in the
+    graph and in the host-driven loop, over a predictor trajectory."""
     s = tg.systems.make_config(name)
     tr = tg.systems.Trajectory(s)
     a = engine_for(s, predictor=1)
     a.pcg_fusion(25)
-    b = engine_for(s, predictor=1)
-    b.pcg_fusion(25 | 32)
-    c = engine_for(s, predictor=1)
-    c.pcg_fusion(25 | 32)
-    c.use_graph(False)
+    others = []
+    for mask, graph in ((25 | 32, True), (25 | 32, False), (25 | 32 | 64, True), (25 | 32 | 64, False)):
+        e = engine_for(s, predictor=1)
+        e.pcg_fusion(mask)
+        e.use_graph(graph)
+        others.append(e)
     for step in range(20):
         x = tr.frame(step)
         ua, pa, _ = a.induce_host(x)
-        ub, pb, rc = b.induce_host(x)
-        uc, pc, _ = c.induce_host(x)
-        assert rc == 0
-        assert a.stats()[0] == b.stats()[0] == c.stats()[0], step
-        assert np.array_equal(ua, ub) and np.array_equal(pa, pb), step
-        assert np.array_equal(ua, uc) and np.array_equal(pa, pc), step
+        for e in others:
+            ub, pb, rc = e.induce_host(x)
+            assert rc == 0
+            assert a.stats()[0] == e.stats()[0], step
+            assert np.array_equal(ua, ub) and np.array_equal(pa, pb), step
 
 
 @pytest.mark.parametrize("name", ["water648", "water12288"])

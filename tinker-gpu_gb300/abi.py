@@ -441,7 +441,7 @@ class Engine:
     def force_lanes(self, lanes=4):
         self._check(self.lib.t9gb_force_lanes(self.h, int(lanes)))
 
-    def pcg_fusion(self, mask=57):
+    def pcg_fusion(self, mask=121):
         """Fusion and overlap of the CG solve (bit 0 preconditioner + dots,
         bit 1 direction formed by its readers, bit 2 Ap fused into the gather,
         bit 3 the predicted guess's field beside the permanent field, bit 4

@@ -608,7 +608,7 @@ int t9gb_force_lanes(t9gb_context* h, int lanes)
 
 int t9gb_set_pcg_fusion(t9gb_context* h, int mask)
 {
-   if (!h || mask < 0 || mask > 63)
+   if (!h || mask < 0 || mask > 127)
       return T9GB_BAD_ARG;
    if (mask != h->c.pcg_fuse)
       drop_graphs(&h->c);

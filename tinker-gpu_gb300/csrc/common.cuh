@@ -265,7 +265,7 @@ struct Context {
    int* nbr_over = nullptr;  // device max count seen (overflow check)
    int* h_over = nullptr;    // pinned mirror
    int pair_lanes = 8;            // lanes per atom in the field kernels
-   int pcg_fuse = 57;             // t9gb_set_pcg_fusion (bit 4: programmatic dependent launch, bit 5: side gather)
+   int pcg_fuse = 121;            // t9gb_set_pcg_fusion (bit 4: programmatic dependent launch, bits 5-6: gather and stream layout)
    int force_lanes = 4;           // lanes per atom in the real-space force kernel
    bool list_stale = true;        // positions changed since the last list check
    bool list_need_build = true;   // no valid list for the current order / capacity

@@ -239,6 +239,7 @@ __global__ void k_pcg_dir(VecArgs A, const double* __restrict__ scal, float* __r
    const float* __restrict__ zrsd)
 {
    pdl_wait();
+   pdl_trigger();  // the spread may stage its blocks and form its B-splines
    const float b = (float)scal[S_B_D], bp = (float)scal[S_B_P];
    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.ne; e += gridDim.x * blockDim.x) {
       const int s = e / 6, x = e + 2 * s;  // row s, component e - 6 s of [npad][8]
@@ -538,7 +539,22 @@ static int pcg_body(Context* ctx, const VecArgs& A, cudaGraphConditionalHandle h
       T9_CUDA(launch_k(pdl, k_pcg_dir, A.nb, VB, 0, ctx->stream, A, ctx->scal, ctx->conj, ctx->zrsd));
       prof_end(ctx);
       const float* rcp = nullptr;
-      if (ctx->cfg.use_ewald && (ctx->pcg_fuse & 32) && !ctx->prof.on) {
+      if (ctx->cfg.use_ewald && (ctx->pcg_fuse & 96) == 96 && !ctx->prof.on) {
+         // the reciprocal chain (spread, transform passes, gather into rcp6)
+         // stays on this stream as programmatic dependents of the direction
+         // kernel; the real-space field runs on the side stream
+         const int k = side_index(ctx);
+         T9_CHECK(recip_fork(ctx, k));
+         cudaStream_t main = ctx->stream;
+         ctx->stream = ctx->side_stream[k];
+         int rc = launch_ufield_real(ctx, ctx->conj, nullptr, ctx->fld6);
+         ctx->stream = main;
+         T9_CHECK(rc);
+         T9_CHECK(launch_ufield_recip_grid(ctx, ctx->conj));
+         T9_CHECK(launch_ufield_recip_gather(ctx, ctx->conj, ctx->rcp6, false));
+         T9_CHECK(recip_join(ctx, k));
+         rcp = ctx->rcp6;
+      } else if (ctx->cfg.use_ewald && (ctx->pcg_fuse & 32) && !ctx->prof.on) {
          // the gather follows the transform on the side stream (a programmatic
          // dependent of its last pass, so its position-only prologue overlaps
          // it) into rcp6; the Ap kernel adds it to the real-space field

@@ -220,7 +220,8 @@ __global__ void __launch_bounds__(256) k_spread(int n, GridParams G, const float
    const float* __restrict__ src, const float* __restrict__ z8, const double* __restrict__ scal,
    unsigned long long* __restrict__ q)
 {
-   pdl_wait();
+   // the site and the B-splines need the positions only: they are formed
+   // before the wait for the programmatic predecessor (no-op otherwise)
    const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
    const int lane = threadIdx.x & 31;
    if (s >= n || lane >= 25)
@@ -233,6 +234,8 @@ __global__ void __launch_bounds__(256) k_spread(int n, GridParams G, const float
    bspline5<L>(w1, t1);
    bspline5<L>(w2, t2);
    bspline5<L>(w3, t3);
+   pdl_wait();
+   pdl_trigger();
    const int jy = lane % 5, kz = lane / 5;
    int zb = i3 + kz;
    zb -= (zb >= G.n3 ? G.n3 : 0);
