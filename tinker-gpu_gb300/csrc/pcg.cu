@@ -222,6 +222,7 @@ __global__ void k_pcg_p2(VecArgs A, const double* __restrict__ scal, float* __re
    const float* __restrict__ conj, float* __restrict__ rsd, const float* __restrict__ vec)
 {
    pdl_wait();
+   pdl_trigger();  // the preconditioner may stage its blocks
    const float a = (float)scal[S_A_D], ap = (float)scal[S_A_P];
    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.ne; e += gridDim.x * blockDim.x) {
       const int s = e / 6, x = e + 2 * s;  // row s, component e - 6 s of [npad][8]

@@ -1705,8 +1705,8 @@ int launch_ufield_recip_grid_dir(Context* ctx, const float* p6, const float* z6,
    GridParams G = grid_params(ctx);
    prof_begin(ctx, P_SPREAD_UIND);
    ctx->pme.packed = true;
-   k_spread<1, true><<<grid_for((long long)ctx->n * 32, 256), 256, 0, ctx->stream>>>(ctx->n, G, ctx->spos, p6, z6,
-      scal, reinterpret_cast<unsigned long long*>(ctx->pme.qfx));
+   T9_CUDA(launch_k(use_pdl(ctx), k_spread<1, true>, grid_for((long long)ctx->n * 32, 256), 256, 0, ctx->stream,
+      ctx->n, G, ctx->spos, p6, z6, scal, reinterpret_cast<unsigned long long*>(ctx->pme.qfx)));
    prof_end(ctx);
    T9_CUDA(cudaGetLastError());
    return fft_conv(ctx);
