@@ -471,14 +471,11 @@ int t9gb_induce(t9gb_context* h, float* uind, float* uinp)
    Context* ctx = &h->c;
    if (!ctx->have_order)
       return T9GB_NOT_READY;
-   int st = induce_sorted(ctx);
-   if (st != T9GB_OK && st != T9GB_NOT_CONVERGED && st != T9GB_NAN_DETECTED)
-      return st;
-   if (uind || uinp) {
-      int rc = scatter_from_sorted3(ctx, ctx->uind, uind, uinp);
-      if (rc != T9GB_OK)
-         return rc;
-   }
+   // the caller-order copy rides in the solve's synchronisation
+   ctx->out_d = uind;
+   ctx->out_p = uinp;
+   const int st = induce_sorted(ctx);
+   ctx->out_d = ctx->out_p = nullptr;
    return st;
 }
 

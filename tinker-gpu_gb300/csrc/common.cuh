@@ -340,6 +340,8 @@ struct Context {
    // t9gb_induce_host: enqueue the caller-order dipole copy before the
    // solve's one synchronisation
    bool stage_out = false;
+   float* out_d = nullptr;  // t9gb_induce's device outputs, written before the solve's synchronisation
+   float* out_p = nullptr;
    // second streams for the reciprocal grid half of a field evaluation, run
    // beside the real-space pair kernel (fork / join by events).  A stream
    // that joined a graph capture stays in it until that capture ends, so the

@@ -727,6 +727,8 @@ static int induce_stepwise(Context* ctx, int variant)
    T9_CHECK(pcg_finish(ctx, A));
    if (ctx->stage_out)
       T9_CHECK(stage_dipoles(ctx));
+   else if (ctx->out_d || ctx->out_p)
+      T9_CHECK(scatter_from_sorted3(ctx, ctx->uind, ctx->out_d, ctx->out_p));
    T9_CUDA(cudaStreamSynchronize(ctx->stream));
    return T9GB_OK;
 }
@@ -808,6 +810,8 @@ static int induce_graph(Context* ctx, int variant)
    T9_CUDA(cudaGraphLaunch(ctx->graph_exec[variant], ctx->stream));
    if (ctx->stage_out)
       T9_CHECK(stage_dipoles(ctx));
+   else if (ctx->out_d || ctx->out_p)
+      T9_CHECK(scatter_from_sorted3(ctx, ctx->uind, ctx->out_d, ctx->out_p));
    T9_CUDA(cudaStreamSynchronize(ctx->stream));
    ctx->list_stale = false;
    return T9GB_OK;

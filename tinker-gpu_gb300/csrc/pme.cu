@@ -209,6 +209,20 @@ __device__ __forceinline__ float2 grid_word(long long w, int packed, float inv)
    return make_float2((float)a * inv, (float)b * inv);
 }
 
+// the guard on the sums of a packed word: each contribution stays below
+// 2^26, so a half at or above 2^30 in magnitude (16 or more near-limit
+// contributions of one sign, far beyond real grids) is taken as a sum that
+// may have left the 32-bit range, and the solve is repeated at the wider
+// scale, as for a large contribution
+__device__ __forceinline__ bool grid_word_big(long long w, int packed)
+{
+   if (!packed)
+      return false;
+   const int b = (int)(unsigned)(unsigned long long)w;
+   const int a = (int)((w - (long long)b) >> 32);
+   return a >= (1 << 30) || a <= -(1 << 30) || b >= (1 << 30) || b <= -(1 << 30);
+}
+
 // Spreading, one warp per atom: lane (jy, kz) < 25 owns one row of five x
 // points.  MODE 0 spreads fractional multipoles into the real part; MODE 1
 // spreads fractional d dipoles into the real and p dipoles into the
@@ -283,12 +297,18 @@ __global__ void __launch_bounds__(256) k_spread(int n, GridParams G, const float
 }
 
 // fixed -> complex float, clearing the fixed grid for the next spread
-__global__ void k_fx_to_grid(size_t ng, long long* __restrict__ q, float2* __restrict__ g, int packed, float inv)
+__global__ void k_fx_to_grid(size_t ng, long long* __restrict__ q, float2* __restrict__ g, int packed, float inv,
+   int* __restrict__ range)
 {
+   bool big = false;
    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < ng; i += (size_t)gridDim.x * blockDim.x) {
-      g[i] = grid_word(q[i], packed, inv);
+      const long long w = q[i];
+      big |= grid_word_big(w, packed);
+      g[i] = grid_word(w, packed, inv);
       q[i] = 0;
    }
+   if (big)
+      atomicOr(range, 1);
 }
 
 // reciprocal convolution with the tabulated influence function
@@ -686,7 +706,7 @@ __host__ __device__ constexpr int fft_zline_ld()
 // memory N (N + 1) + 128 float2
 template <int N, bool FROM_FX, bool INV>
 __global__ void __launch_bounds__(N * fft_threads_per_line<N>()) k_fft_plane(long long* __restrict__ qfx,
-   float2* __restrict__ g, int packed, float inv)
+   float2* __restrict__ g, int packed, float inv, int* __restrict__ range)
 {
    pdl_wait();
    pdl_trigger();  // the next kernel may stage its blocks and run its prologue
@@ -699,6 +719,7 @@ __global__ void __launch_bounds__(N * fft_threads_per_line<N>()) k_fft_plane(lon
       tw[k] = c_tw[k];
    const size_t base = (size_t)blockIdx.x * N * N;
    // element e = threadIdx.x + r NT, r < R: all loads of a chunk in flight together
+   bool big = false;
 #pragma unroll
    for (int c = 0; c < R; c += 8) {
       float2 v[8];
@@ -711,6 +732,7 @@ __global__ void __launch_bounds__(N * fft_threads_per_line<N>()) k_fft_plane(lon
 #pragma unroll
          for (int r = 0; r < 8; ++r) {
             q[(c + r) * NT] = 0;
+            big |= grid_word_big(f[r], packed);
             v[r] = grid_word(f[r], packed, inv);
          }
       } else {
@@ -724,6 +746,8 @@ __global__ void __launch_bounds__(N * fft_threads_per_line<N>()) k_fft_plane(lon
          fsm[fsig<T>(e / N) * LD + fsig<T>(e % N)] = v[r];
       }
    }
+   if (FROM_FX && big)
+      atomicOr(range, 1);
    __syncthreads();
    const int line = threadIdx.x / T, t = threadIdx.x % T;
    float2 wt[N / T];
@@ -951,7 +975,7 @@ static size_t fft_plane_smem()
 
 // plane pass with clusters of P.fft_cl CTAs (0: one CTA per plane)
 template <int N, bool FROM_FX, bool INV>
-static void plane_pass(const PmeGrid& P, cudaStream_t st, int packed, float inv, bool pdl)
+static void plane_pass(const PmeGrid& P, cudaStream_t st, int packed, float inv, bool pdl, int* range)
 {
    constexpr int T = fft_threads_per_line<N>();
    if (P.fft_cl == 2)
@@ -961,7 +985,8 @@ static void plane_pass(const PmeGrid& P, cudaStream_t st, int packed, float inv,
    else if (P.fft_cl == 8)
       launch_plane_cl<N, 8, FROM_FX, INV>(P.qfx, P.qgrid, packed, inv, P.fft_err, st);
    else
-      launch_k(pdl, k_fft_plane<N, FROM_FX, INV>, N, N * T, fft_plane_smem<N>(), st, P.qfx, P.qgrid, packed, inv);
+      launch_k(pdl, k_fft_plane<N, FROM_FX, INV>, N, N * T, fft_plane_smem<N>(), st, P.qfx, P.qgrid, packed, inv,
+         range);
 }
 
 
@@ -975,8 +1000,8 @@ static int fft_setup_kernels(Context* ctx)
       rc = plane_cl_setup<N, 8>(ctx);
    T9_CHECK(rc);
    const int bytes = (int)fft_plane_smem<N>();
-   void (*fwd)(long long*, float2*, int, float) = k_fft_plane<N, true, false>;
-   void (*inv)(long long*, float2*, int, float) = k_fft_plane<N, false, true>;
+   void (*fwd)(long long*, float2*, int, float, int*) = k_fft_plane<N, true, false>;
+   void (*inv)(long long*, float2*, int, float, int*) = k_fft_plane<N, false, true>;
    T9_CUDA(cudaFuncSetAttribute(fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
    T9_CUDA(cudaFuncSetAttribute(inv, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
    return T9GB_OK;
@@ -984,10 +1009,10 @@ static int fft_setup_kernels(Context* ctx)
 
 // forward planes; vir: the z pass stops after the forward transform
 template <int N>
-static void fft_own_forward(const PmeGrid& P, cudaStream_t st, bool split, bool pdl)
+static void fft_own_forward(const PmeGrid& P, cudaStream_t st, bool split, bool pdl, int* range)
 {
    constexpr int T = fft_threads_per_line<N>();
-   plane_pass<N, true, false>(P, st, P.packed ? 1 : 0, 1.0f / (float)(1 << P.pack_shift), pdl);
+   plane_pass<N, true, false>(P, st, P.packed ? 1 : 0, 1.0f / (float)(1 << P.pack_shift), pdl, range);
    if (split)
       launch_k(pdl, k_fft_zline<N, 0>, N * N / 16, 16 * T, 0, st, P.infl, P.qgrid);
    else
@@ -1000,7 +1025,7 @@ static void fft_own_inverse(const PmeGrid& P, cudaStream_t st, bool split, bool 
    constexpr int T = fft_threads_per_line<N>();
    if (split)
       launch_k(pdl, k_fft_zline<N, 1>, N * N / 16, 16 * T, 0, st, P.infl, P.qgrid);
-   plane_pass<N, false, true>(P, st, 0, 0.f, pdl);
+   plane_pass<N, false, true>(P, st, 0, 0.f, pdl, nullptr);
 }
 
 // ---------------------------------------------------------------------------
@@ -1555,16 +1580,17 @@ static int fft_conv(Context* ctx, int vir = 0, float wE = 0.f, float wP = 0.f, b
    const size_t ng = (size_t)P.n1 * P.n2 * P.n3;
    const int cb = (int)std::min<size_t>((ng + 255) / 256, 152 * 16);
    prof_begin(ctx, P_FFT_CONV);
+   int* range = ctx->status + (P.probe ? ST_RANGE_L : ST_RANGE);
    if (P.own_fft) {
       cudaStream_t st = ctx->stream;
       const bool split = vir != 0;
       const bool pdl = use_pdl(ctx);
       if (P.n1 == 32)
-         fft_own_forward<32>(P, st, split, pdl);
+         fft_own_forward<32>(P, st, split, pdl, range);
       else if (P.n1 == 64)
-         fft_own_forward<64>(P, st, split, pdl);
+         fft_own_forward<64>(P, st, split, pdl, range);
       else
-         fft_own_forward<128>(P, st, split, pdl);
+         fft_own_forward<128>(P, st, split, pdl, range);
       if (split) {
          T9_CHECK(conv_virial(ctx, vir, wE, wP, stash, out));
          k_conv<<<cb, 256, 0, st>>>(ng, P.infl, P.qgrid);
@@ -1580,7 +1606,7 @@ static int fft_conv(Context* ctx, int vir = 0, float wE = 0.f, float wP = 0.f, b
       return T9GB_OK;
    }
    k_fx_to_grid<<<cb, 256, 0, ctx->stream>>>(ng, P.qfx, P.qgrid, P.packed ? 1 : 0,
-      1.0f / (float)(1 << P.pack_shift));
+      1.0f / (float)(1 << P.pack_shift), range);
    T9_CUDA(cudaGetLastError());
    cufftSetStream(P.plan, ctx->stream);
    if (cufftExecC2C(P.plan, (cufftComplex*)P.qgrid, (cufftComplex*)P.qgrid, CUFFT_FORWARD) != CUFFT_SUCCESS) {
