@@ -49,6 +49,9 @@ def parse():
     ap.add_argument("--history", type=int, default=20, help="trajectory frames run before warm-up (predictor ring)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--learn-train", type=int, default=500, help="online training steps before the learned legs")
+    ap.add_argument("--learn-steps", type=int, default=1500,
+                    help="timed steps per learned leg on the 12,288-atom MD frames (the network in use on steps "
+                    "500-2000 of the learned-guess configuration)")
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--no-forces", action="store_true")
     ap.add_argument("--no-md", action="store_true", help="skip the MD leg (ns/day)")
@@ -476,7 +479,7 @@ def time_steps(eng, dev_frames, idxs, stream, flush, ud, up):
     return ms, its, ls
 
 
-def learned_legs(args, s, abi, stream, dev, flush, check_oracle):
+def learned_legs(args, s, abi, stream, dev, flush, check_oracle, timed=None):
     """The learned initial guess against the plain guesses.
 
     Two engines follow the trajectory: one with the direct guess alpha E (no
@@ -486,10 +489,11 @@ def learned_legs(args, s, abi, stream, dev, flush, check_oracle):
     legs of --steps frames, each after --warmup untimed frames: the plain
     start (network off), the learned start compared with the plain one on
     every solve (probe 1), and the comparison on every 16th solve (probe 16).
-    Training is off in the timed legs.  dev: device frames [>= T + 3 (W + K)][n][3]."""
+    Training is off in the timed legs.  dev: device frames [>= T + 3 (W + K)][n][3];
+    K = timed (default --steps)."""
     import torch
 
-    T, K, W = args.learn_train, args.steps, args.warmup
+    T, K, W = args.learn_train, timed or args.steps, args.warmup
     assert dev.shape[0] >= T + 3 * (W + K)
     ud = torch.zeros((s.n, 3), device="cuda")
     up = torch.zeros((s.n, 3), device="cuda")
@@ -696,7 +700,7 @@ def main():
 
     # ---- MD (ns/day), recording the frames of the learned-guess legs ----
     want_learned = not args.no_learned and args.learn_train > 0
-    nrec = args.learn_train + 3 * (args.warmup + args.steps) if want_learned else 0
+    nrec = args.learn_train + 3 * (args.warmup + args.learn_steps) if want_learned else 0
     nrec = max(nrec, args.history + args.warmup + args.steps)
     md, md_frames, md_sys = None, None, None
     if not args.no_md:
@@ -710,11 +714,12 @@ def main():
     if want_learned:
         check = rank == 0 and not args.no_cpu_baseline
         if md_frames is not None:
-            learned = learned_legs(args, md_sys, abi, stream, md_frames, flush, check_oracle=check)
+            learned = learned_legs(args, md_sys, abi, stream, md_frames, flush, check_oracle=check,
+                                   timed=args.learn_steps)
             learned["frames"] = "MD trajectory of the relaxed box (the MD leg's, continued)"
         else:
             lf = torch.from_numpy(np.stack([tr.frame(100000 + t) for t in range(nrec)]).astype(np.float32)).to("cuda")
-            learned = learned_legs(args, s, abi, stream, lf, flush, check_oracle=check)
+            learned = learned_legs(args, s, abi, stream, lf, flush, check_oracle=check, timed=args.learn_steps)
             learned["frames"] = "synthetic librating trajectory"
         del md_frames
 
