@@ -10,7 +10,7 @@ field of (150, -300, 450) MV/cm (test/extfield.cpp:15-173):
   test/ref/extfield.2.txt  polarization term only
   test/ref/extfield.3.txt  both
 Reads the files as text; run in a checkout that has the reference at
-REFERENCE_ROOT (default /root/reference).  The GPU machine never runs this.
+REFERENCE_ROOT (default /root/reference).  Machines without the checkout never run this.
 """
 import json
 import os

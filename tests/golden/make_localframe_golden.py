@@ -6,7 +6,7 @@ Reads, as text, the 22-atom local-frame test case of the reference:
                                                and the scale-factor keywords
   test/localframe.cpp                          known answers (Fortran Tinker)
 and writes one JSON fixture.  Run in a checkout that has the reference at
-REFERENCE_ROOT (default /root/reference); the GPU machine never runs this.
+REFERENCE_ROOT (default /root/reference); machines without the checkout never run this.
 """
 import json
 import os

@@ -8,7 +8,7 @@ Two-ion known answers of the multipole energy, gradient and virial:
           (z-only frames with dipoles and quadrupoles) come before the
           parameter file's and the two ions are bonded (1-2 scale 0)
 Reads the files as text; run in a checkout that has the reference at
-REFERENCE_ROOT (default /root/reference).  The GPU machine never runs this.
+REFERENCE_ROOT (default /root/reference).  Machines without the checkout never run this.
 """
 import json
 import os

@@ -7,7 +7,7 @@ Known answers of the Na+/Cl- pair with a POLPAIR Thole coefficient
   test/ref/polpair.1.txt (Ewald), .2.txt     total energy (multipole +
                                              polarization), virial, gradient
 Reads the files as text; run in a checkout that has the reference at
-REFERENCE_ROOT (default /root/reference).  The GPU machine never runs this.
+REFERENCE_ROOT (default /root/reference).  Machines without the checkout never run this.
 """
 import json
 import os

@@ -11,7 +11,7 @@ The reference test (test/tinkernist.cpp:195-365, TinkerNIST-SAVE1) compares
 the first and last two atoms of each frame at 0.001; the fixture keeps every
 atom.  Coordinates and dipoles are stored as the files' six-decimal integers.
 Run in a checkout that has the reference at REFERENCE_ROOT (default
-/root/reference); the GPU machine never runs this.
+/root/reference); machines without the checkout never run this.
 """
 import importlib
 import json

@@ -9,7 +9,7 @@ Known answers of the valence terms the AMOEBA water MD step uses:
 Bond and Urey-Bradley parameters are resolved here from the atom classes
 (the parameter files' atom records).  Reads the files as text; run in a
 checkout that has the reference at REFERENCE_ROOT (default /root/reference).
-The GPU machine never runs this.
+Machines without the checkout never run this.
 """
 import json
 import os

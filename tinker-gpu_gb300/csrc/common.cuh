@@ -326,7 +326,7 @@ struct Context {
    int *rev_start = nullptr, *rev_ent = nullptr;
    std::vector<int> h_frames;  // [n][4] caller order
    // start policy (host): compare the plain and the learned start every
-   // learn_probe solves; in between reuse the last comparison's verdict
+   // learn_probe solves; in between reuse the last comparison's result
    int learn_probe = 1;
    int learn_since_probe = 1 << 30;
    int learn_last_choice = 0;
