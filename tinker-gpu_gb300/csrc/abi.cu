@@ -85,6 +85,7 @@ static int alloc_all(Context* ctx)
    T9_CUDA(cudaMallocHost(&ctx->h_stage, ctx->h_stage_bytes));
    T9_CUDA(cudaMallocHost(&ctx->h_in, sizeof(float) * 3 * (size_t)npad));
    T9_CUDA(cudaEventCreateWithFlags(&ctx->ev_in, cudaEventDisableTiming));
+   T9_CUDA(cudaEventCreateWithFlags(&ctx->ev_solved, cudaEventDisableTiming));
    for (int k = 0; k < 4; ++k) {
       T9_CUDA(cudaStreamCreateWithFlags(&ctx->side_stream[k], cudaStreamNonBlocking));
       T9_CUDA(cudaEventCreateWithFlags(&ctx->ev_fork[k], cudaEventDisableTiming));
@@ -139,6 +140,8 @@ static void free_all(Context* ctx)
       if (ctx->ev_join[k])
          cudaEventDestroy(ctx->ev_join[k]);
    }
+   if (ctx->ev_solved)
+      cudaEventDestroy(ctx->ev_solved);
    for (auto& e : ctx->prof.ev)
       cudaEventDestroy(e);
    if (ctx->own_stream && ctx->stream)

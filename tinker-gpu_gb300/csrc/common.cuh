@@ -217,6 +217,7 @@ struct Context {
    std::vector<double> h_xyz;  // host copy for the ordering, refreshed by t9gb_nblist_build
    float* h_in = nullptr;      // pinned staging of host coordinates
    cudaEvent_t ev_in = nullptr; // its last copy to the device
+   cudaEvent_t ev_solved = nullptr;  // the induce graph and its status copies (work queued after it runs on)
    bool ev_in_pending = false;
    bool have_xyz = false;
    bool have_topology = false;
@@ -342,6 +343,12 @@ struct Context {
    bool stage_out = false;
    float* out_d = nullptr;  // t9gb_induce's device outputs, written before the solve's synchronisation
    float* out_p = nullptr;
+   // work queued behind the induce graph before the solve's synchronisation
+   // (the MD step's forces); after_done: it ran; induce_redone: the solve was
+   // repeated after it ran (a list or range retry), so it used a discarded solve
+   const std::function<int()>* after_launch = nullptr;
+   bool after_done = false;
+   bool induce_redone = false;
    // second streams for the reciprocal grid half of a field evaluation, run
    // beside the real-space pair kernel (fork / join by events).  A stream
    // that joined a graph capture stays in it until that capture ends, so the
@@ -542,7 +549,8 @@ int launch_ufield_recip_gather_alt(Context* ctx, const float* u6, float* out6);
 int scatter_positions(Context* ctx);
 // t9gb_emplar(grad) with `beside` called once the dipoles are solved and the
 // list is current, before the electrostatic forces are launched
-int emplar_grad_beside(Context* ctx, float* grad, const std::function<int()>& beside);
+int emplar_grad_beside(Context* ctx, float* grad, const std::function<int()>& beside,
+   const std::function<int()>& reset);
 // side stream of the current capture level, and the fork / join of work on
 // it with the main stream (events, no host synchronisation)
 int side_index(const Context* ctx);

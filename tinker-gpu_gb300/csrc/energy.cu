@@ -285,9 +285,37 @@ static int elec_terms(Context* ctx, bool mpole, bool polar, int vers, double* en
    return T9GB_OK;
 }
 
-int emplar_grad_beside(Context* ctx, float* grad, const std::function<int()>& beside)
+// The MD step's gradient: the forces (and the beside work) are queued right
+// behind the induce graph, before the solve's status synchronisation, so the
+// device does not wait for the host between the solve and the forces; the
+// same kernels in the same stream order as elec_terms.  When the solve had to
+// be repeated (a list or range retry) the queued work used the discarded
+// solve: reset() clears what the beside work accumulates and the forces are
+// queued again on the final solve and list.
+int emplar_grad_beside(Context* ctx, float* grad, const std::function<int()>& beside,
+   const std::function<int()>& reset)
 {
-   return elec_terms(ctx, true, true, T9GB_CALC_GRAD, nullptr, grad, nullptr, &beside);
+   if (!ctx->use_graph || ctx->prof.on)
+      return elec_terms(ctx, true, true, T9GB_CALC_GRAD, nullptr, grad, nullptr, &beside);
+   const std::function<int()> forces = [&]() -> int {
+      T9_CHECK(beside());
+      T9_CUDA(cudaMemsetAsync(ctx->e_atom, 0, sizeof(double) * 3 * ctx->npad, ctx->stream));
+      return elec_forces(ctx, true, true, grad, false);
+   };
+   ctx->after_launch = &forces;
+   ctx->after_done = false;
+   const int rc = induce_sorted(ctx);
+   const bool queued = ctx->after_done, redone = ctx->induce_redone;
+   ctx->after_launch = nullptr;
+   ctx->after_done = false;
+   if (rc != T9GB_OK)
+      return rc;
+   if (queued && !redone)
+      return T9GB_OK;
+   if (queued)
+      T9_CHECK(reset());
+   T9_CHECK(ensure_list(ctx));
+   return forces();
 }
 
 }  // namespace t9gb

@@ -139,7 +139,16 @@ static int md_forces(Context* ctx, t9gb_context* h)
       ctx->stream = main;
       return rc;
    };
-   const int st = emplar_grad_beside(ctx, ctx->md_g, beside);
+   const std::function<int()> reset = [&]() -> int {
+      if (forked) {  // the first pass's beside work ends before it is redone
+         T9_CUDA(cudaEventRecord(ctx->ev_join[3], ctx->side_stream[3]));
+         T9_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->ev_join[3], 0));
+      }
+      if (extra)
+         T9_CUDA(cudaMemsetAsync(ctx->md_g2, 0, sizeof(float) * 3 * ctx->n, ctx->stream));
+      return T9GB_OK;
+   };
+   const int st = emplar_grad_beside(ctx, ctx->md_g, beside, reset);
    if (forked) {
       T9_CUDA(cudaEventRecord(ctx->ev_join[3], ctx->side_stream[3]));
       T9_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->ev_join[3], 0));

@@ -812,7 +812,16 @@ static int induce_graph(Context* ctx, int variant)
       T9_CHECK(stage_dipoles(ctx));
    else if (ctx->out_d || ctx->out_p)
       T9_CHECK(scatter_from_sorted3(ctx, ctx->uind, ctx->out_d, ctx->out_p));
-   T9_CUDA(cudaStreamSynchronize(ctx->stream));
+   if (ctx->after_launch && !ctx->after_done) {
+      // the host waits for the solve only: the queued work runs on while it
+      // reads the status and queues what follows
+      T9_CUDA(cudaEventRecord(ctx->ev_solved, ctx->stream));
+      T9_CHECK((*ctx->after_launch)());
+      ctx->after_done = true;
+      T9_CUDA(cudaEventSynchronize(ctx->ev_solved));
+   } else {
+      T9_CUDA(cudaStreamSynchronize(ctx->stream));
+   }
    ctx->list_stale = false;
    return T9GB_OK;
 }
@@ -858,7 +867,10 @@ int induce_sorted(Context* ctx)
    const bool graph = ctx->use_graph && !ctx->prof.on;
    const int variant = pick_variant(ctx);
    bool range_failed = false;
+   ctx->induce_redone = false;
    for (int attempt = 0; attempt < 3; ++attempt) {
+      if (attempt > 0)
+         ctx->induce_redone = true;
       T9_CHECK(graph ? induce_graph(ctx, variant) : induce_stepwise(ctx, variant));
       int redo = 0;
       T9_CHECK(check_list_overflow(ctx, &redo));
