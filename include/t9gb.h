@@ -484,6 +484,16 @@ int t9gb_learn_adamw(t9gb_context* ctx);
  * within 1.2e-7 relative in the tests).  GB300, 12,288 atoms: a training
  * solve 1.045 (path 0) -> 0.860 ms (plain 0.789 ms). */
 int t9gb_learn_tensor_path(t9gb_context* ctx, int path);
+
+/* Learned extrapolation of the predictor ring (ASPC contexts only): after
+ * every solve, a least-squares fit of the converged dipoles on the `order`
+ * most recent ring frames (2 .. 8; their backward differences as the basis,
+ * FP64 normal equations over every element of both dipole sets, forgetting
+ * factor 0.99, solved on the device) gives the ring coefficients of the next
+ * solve's start, in place of ASPC's (from the second fit on).  The PCG
+ * convergence test is unchanged.  0 (the default) keeps ASPC.  A new order
+ * starts a new fit.  T9GB_BAD_ARG for other orders or without ASPC. */
+int t9gb_learn_extrapolation(t9gb_context* ctx, int order);
 /* Raw features of the last solve, device [2n][32]: rows 0..n-1 for the d
  * dipoles, n..2n-1 for the p dipoles, caller atom order. */
 int t9gb_learn_features(t9gb_context* ctx, float* features_device);

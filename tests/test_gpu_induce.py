@@ -299,3 +299,42 @@ def test_programmatic_dependent_launch_bit_identical(gpu_lib, tg, name):
         assert a.stats()[0] == b.stats()[0] == c.stats()[0], step
         assert np.array_equal(ua, ub) and np.array_equal(pa, pb), step
         assert np.array_equal(ua, uc) and np.array_equal(pa, pc), step
+
+
+def test_learned_extrapolation(gpu_lib, oracle, tg):
+    """The learned extrapolation of the ASPC ring (online least squares over
+    the last 7 frames): the dipoles still meet the oracle's, the start needs
+    no more iterations than ASPC's on a trajectory, graph and host-driven
+    loop agree bit for bit, and orders outside 2..8 or a context without
+    ASPC are rejected."""
+    s = tg.systems.make_config("water648")
+    tr = tg.systems.Trajectory(s)
+    a = engine_for(s, predictor=1)
+    b = engine_for(s, predictor=1)
+    b.learn_extrapolation(7)
+    c = engine_for(s, predictor=1)
+    c.learn_extrapolation(7)
+    c.use_graph(False)
+    ia, ib = [], []
+    for step in range(40):
+        x = tr.frame(step)
+        ua, pa, _ = a.induce_host(x)
+        ub, pb, rc = b.induce_host(x)
+        uc, pc, _ = c.induce_host(x)
+        assert rc == 0
+        assert np.array_equal(ub, uc) and np.array_equal(pb, pc), step
+        if step >= 24:
+            ia.append(a.stats()[0])
+            ib.append(b.stats()[0])
+    print("iterations ASPC", np.mean(ia), "learned extrapolation", np.mean(ib))
+    assert np.mean(ib) <= np.mean(ia)
+    ou, op, *_ = oracle.OracleSystem(s, xyz=tr.frame(39)).induce()
+    D = tg.units.DEBYE
+    assert rms_err(ub * D, ou * D) < DIPOLE_RMS_DEBYE and rms_err(pb * D, op * D) < DIPOLE_RMS_DEBYE
+    abi = gpu_lib
+    for bad in (1, 9, -1):
+        with pytest.raises(abi.T9Error):
+            b.learn_extrapolation(bad)
+    d = engine_for(s, predictor=0)
+    with pytest.raises(abi.T9Error):
+        d.learn_extrapolation(7)

@@ -32,7 +32,7 @@ EXPORTS = [
     "t9gb_set_thole_pairs", "t9gb_set_external_field", "t9gb_set_vdw", "t9gb_ehal", "t9gb_set_valence",
     "t9gb_evalence", "t9gb_md_init", "t9gb_md_run", "t9gb_md_state", "t9gb_md_positions_device", "t9gb_md_stats",
     "t9gb_set_xyz_soa_device", "t9gb_diag_precond_apply", "t9gb_gradient_fixed", "t9gb_pme_fft_cluster",
-    "t9gb_copy_error", "t9gb_pair_staging", "t9gb_learn_tensor_path",
+    "t9gb_copy_error", "t9gb_pair_staging", "t9gb_learn_tensor_path", "t9gb_learn_extrapolation",
 ]
 CALC_ENERGY, CALC_GRAD, CALC_VIRIAL = 0x010, 0x020, 0x040
 
@@ -130,6 +130,7 @@ def load(path=None):
     lib.t9gb_copy_error.argtypes = [vp, ip]
     lib.t9gb_pair_staging.argtypes = [vp, C.c_int]
     lib.t9gb_learn_tensor_path.argtypes = [vp, C.c_int]
+    lib.t9gb_learn_extrapolation.argtypes = [vp, C.c_int]
     lib.t9gb_pair_lanes.argtypes = [vp, C.c_int]
     lib.t9gb_set_pcg_fusion.argtypes = [vp, C.c_int]
     lib.t9gb_force_lanes.argtypes = [vp, C.c_int]
@@ -521,6 +522,10 @@ class Engine:
     def learn_tensor_path(self, path=1):
         """0: mma.sync GEMMs; 1: the fused tcgen05 forward pass."""
         self._check(self.lib.t9gb_learn_tensor_path(self.h, int(path)))
+
+    def learn_extrapolation(self, order=7):
+        """Learned extrapolation of the ASPC ring over `order` frames (2-8); 0 restores ASPC."""
+        self._check(self.lib.t9gb_learn_extrapolation(self.h, int(order)))
 
     def learn_adamw(self):
         self._check(self.lib.t9gb_learn_adamw(self.h))

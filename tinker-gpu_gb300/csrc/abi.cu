@@ -105,7 +105,7 @@ static void free_all(Context* ctx)
       ctx->cell_count, ctx->cell_start, ctx->cell_atoms, ctx->atom_cell, ctx->rcp6, ctx->fld6, ctx->udir,
       ctx->efield, ctx->uind, ctx->rsd, ctx->zrsd, ctx->conj, ctx->vec, ctx->tmp6, ctx->e_atom, ctx->sframe, ctx->hout,
       ctx->red, ctx->scal, ctx->status, ctx->sref, ctx->lflag,
-      ctx->aspc_hist, ctx->thl, ctx->exfld, ctx->sum_part};
+      ctx->aspc_hist, ctx->thl, ctx->exfld, ctx->sum_part, ctx->lx_ab, ctx->lx_part, ctx->lx_coef_buf, ctx->lx_ticket};
    for (void* p : dev)
       if (p)
          cudaFree(p);
@@ -142,6 +142,12 @@ static void free_all(Context* ctx)
    }
    if (ctx->ev_solved)
       cudaEventDestroy(ctx->ev_solved);
+   if (ctx->lx_stream)
+      cudaStreamDestroy(ctx->lx_stream);
+   if (ctx->ev_lx_fork)
+      cudaEventDestroy(ctx->ev_lx_fork);
+   if (ctx->ev_lx_done)
+      cudaEventDestroy(ctx->ev_lx_done);
    for (auto& e : ctx->prof.ev)
       cudaEventDestroy(e);
    if (ctx->own_stream && ctx->stream)
@@ -233,6 +239,8 @@ void t9gb_destroy(t9gb_context* h)
    if (!h)
       return;
    cudaStreamSynchronize(h->c.stream);
+   if (h->c.lx_stream)
+      cudaStreamSynchronize(h->c.lx_stream);
    free_all(&h->c);
    delete h;
 }
@@ -642,6 +650,13 @@ int t9gb_copy_error(t9gb_context* h, int* flag)
    T9_CUDA(cudaStreamSynchronize(ctx->stream));
    *flag = (a & 5) | (b ? 2 : 0);
    return T9GB_OK;
+}
+
+int t9gb_learn_extrapolation(t9gb_context* h, int order)
+{
+   if (!h)
+      return T9GB_BAD_ARG;
+   return lx_config(&h->c, order);
 }
 
 int t9gb_learn_tensor_path(t9gb_context* h, int path)

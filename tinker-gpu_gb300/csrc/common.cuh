@@ -306,6 +306,16 @@ struct Context {
    // predictor ring (ASPC 16 / Gear 6 frames), sorted [depth][npad][8]; the
    // ring count is device state
    float* aspc_hist = nullptr;
+   // learned extrapolation of the ASPC ring (t9gb_learn_extrapolation)
+   int lx_k = 0;                  // ring frames of the fit, 0: off
+   double* lx_ab = nullptr;       // normal equations [8][8] + [8]
+   double* lx_part = nullptr;     // per-block partial sums
+   float* lx_coef_buf = nullptr;  // ring coefficients by frame age [16]
+   float* lx_coef = nullptr;      // lx_coef_buf while on, else null
+   int* lx_ticket = nullptr;      // last-block ticket of the fit
+   cudaStream_t lx_stream = nullptr;  // the fit runs here, after the solve's graph
+   cudaEvent_t ev_lx_fork = nullptr, ev_lx_done = nullptr;
+   bool lx_pending = false;       // a fit is queued that the next solve waits for
 
    // learned initial guess (learn.cu)
    int learn_mode = 0;          // bit 0: train after each solve, bit 1: start from the learned guess
@@ -511,6 +521,8 @@ int order_build(Context* ctx);  // host: spatial order, scaled partners
 int list_update(Context* ctx);  // device: exact neighbour list
 int ensure_list(Context* ctx);  // list_update when the coordinates changed
 int check_list_overflow(Context* ctx, int* redo);
+int lx_config(Context* ctx, int order);   // pcg.cu
+int lx_wait(Context* ctx);                // pcg.cu
 int alloc_lists(Context* ctx, int cap);          // nbr, nbrc, nbrp with row capacity cap
 int pair_staging_setup();                         // pair.cu: shared-memory limits of the staged kernels
 int mlp_tc_setup();                               // mlp.cu: shared-memory limit of the tcgen05 forward

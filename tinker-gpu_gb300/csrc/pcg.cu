@@ -51,9 +51,19 @@ struct VecArgs {
 // E = field, udir = alpha E, guess: the predictor's extrapolation once its
 // ring (depth 16 for ASPC, 6 for Gear) is full, else the direct guess
 // alpha E (pcgguess) or zero
+// coefficient of ring slot k (its frame's age j): ASPC / Gear, or the
+// learned extrapolation's once it has two fits (lcoef: null when off)
+__device__ __forceinline__ float ring_coef(int predictor, int j, const float* __restrict__ lcoef,
+   const int* __restrict__ state)
+{
+   if (lcoef && state[ST_LX] >= 2)
+      return lcoef[j];
+   return (float)(predictor == 1 ? c_aspc[j] : c_gear[j]);
+}
+
 __global__ void k_init_guess(VecArgs A, const float* __restrict__ fld, float* __restrict__ efield,
    float* __restrict__ udir, float* __restrict__ uind, int pcgguess, int predictor, const float* __restrict__ hist,
-   const int* __restrict__ state, int set_uind)
+   const int* __restrict__ state, int set_uind, const float* __restrict__ lcoef)
 {
    const int nualt = state[ST_NUALT];
    const int depth = predictor == 1 ? 16 : predictor == 2 ? 6 : 0;
@@ -62,7 +72,7 @@ __global__ void k_init_guess(VecArgs A, const float* __restrict__ fld, float* __
    if (predict)
       for (int k = 0; k < depth; ++k) {
          const int j = ((nualt - 1 - k) % depth + depth) % depth;
-         coef[k] = (float)(predictor == 1 ? c_aspc[j] : c_gear[j]);
+         coef[k] = ring_coef(predictor, j, lcoef, state);
       }
    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.ne; e += gridDim.x * blockDim.x) {
       const int s = e / 6, x = e + 2 * s;  // row s, component e - 6 s of [npad][8]
@@ -89,7 +99,7 @@ __global__ void k_init_guess(VecArgs A, const float* __restrict__ fld, float* __
 // the predictor's guess alone (zero while its ring is not full), before the
 // permanent field is known: the same extrapolation as k_init_guess
 __global__ void k_predict(VecArgs A, int predictor, const float* __restrict__ hist, const int* __restrict__ state,
-   float* __restrict__ uind)
+   float* __restrict__ uind, const float* __restrict__ lcoef)
 {
    const int nualt = state[ST_NUALT];
    const int depth = predictor == 1 ? 16 : predictor == 2 ? 6 : 0;
@@ -98,7 +108,7 @@ __global__ void k_predict(VecArgs A, int predictor, const float* __restrict__ hi
    if (predict)
       for (int k = 0; k < depth; ++k) {
          const int j = ((nualt - 1 - k) % depth + depth) % depth;
-         coef[k] = (float)(predictor == 1 ? c_aspc[j] : c_gear[j]);
+         coef[k] = ring_coef(predictor, j, lcoef, state);
       }
    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.ne; e += gridDim.x * blockDim.x) {
       const int s = e / 6, x = e + 2 * s;  // row s, component e - 6 s of [npad][8]
@@ -273,6 +283,199 @@ __global__ void k_bump_nualt(int* state, int depth)
 }
 
 // ---------------------------------------------------------------------------
+
+// Learned extrapolation of the predictor ring (t9gb_learn_extrapolation).
+// After each solve the converged dipoles u_t (just saved in the ring) and
+// the K frames before them give one least-squares sample per element of
+// both dipole sets: u_t ~ sum_k a_k D^k u_{t-1}, D^k the k-th backward
+// difference over the ring (a well-conditioned basis: Jacobi-scaled
+// condition numbers of 10^2 - 10^3 at K = 6 - 8).  The normal equations are
+// summed in FP64 in a fixed order, kept with forgetting factor LX_LAMBDA,
+// and solved by Cholesky in the launch's last block; the raw coefficients
+// c_j = sum_k a_k (-1)^j C(k, j) of the ring frames replace the
+// predictor's (ring_coef).  The PCG convergence test is unchanged.
+constexpr int LX_MAXK = 8;
+constexpr double LX_LAMBDA = 0.99;
+constexpr int LX_NB = 152;                                // blocks of k_lx_train
+constexpr int LX_NV = LX_MAXK * (LX_MAXK + 1) / 2 + LX_MAXK;  // partial sums per block
+
+// signed binomials (-1)^j C(k, j), k, j < 8 (Pascal's triangle)
+__constant__ float c_sbinom[LX_MAXK][LX_MAXK] = {
+   {1, 0, 0, 0, 0, 0, 0, 0},
+   {1, -1, 0, 0, 0, 0, 0, 0},
+   {1, -2, 1, 0, 0, 0, 0, 0},
+   {1, -3, 3, -1, 0, 0, 0, 0},
+   {1, -4, 6, -4, 1, 0, 0, 0},
+   {1, -5, 10, -10, 5, -1, 0, 0},
+   {1, -6, 15, -20, 15, -6, 1, 0},
+   {1, -7, 21, -35, 35, -21, 7, -1}};
+
+// The differences are formed in FP64 from the FP32 ring (exact: small
+// integer weights), rounded to FP32 (their own relative precision), and the
+// products summed in FP32 per thread and block (a few hundred terms), then
+// in FP64 across blocks: FP64 arithmetic is slow on this GPU.
+template <int K>
+__global__ void __launch_bounds__(256) k_lx_train(VecArgs A, const float* __restrict__ hist, double* __restrict__ part,
+   double* __restrict__ lx, float* __restrict__ lcoef, int* __restrict__ state, int* __restrict__ ticket)
+{
+   constexpr int NV = K * (K + 1) / 2 + K;
+   __shared__ float sh[8][NV];
+   const int nualt = state[ST_NUALT] - 1;  // after the solve's bump: the new frame is slot nualt % 16
+   if (nualt < K)
+      return;  // every block alike
+   float acc[NV];
+#pragma unroll
+   for (int v = 0; v < NV; ++v)
+      acc[v] = 0.f;
+   const float* fy = hist + (size_t)(nualt % 16) * A.ne8;
+   const float* fr[K];
+#pragma unroll
+   for (int j = 0; j < K; ++j)
+      fr[j] = hist + (size_t)(((nualt - 1 - j) % 16 + 16) % 16) * A.ne8;
+   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.ne; e += gridDim.x * blockDim.x) {
+      const int s = e / 6, x = e + 2 * s;
+      double t[K];
+#pragma unroll
+      for (int j = 0; j < K; ++j)
+         t[j] = fr[j][x];
+      float d[K];
+#pragma unroll
+      for (int k = 0; k < K; ++k) {  // the difference table: d_k = sum_j (-1)^j C(k, j) u_j
+         d[k] = (float)t[0];
+#pragma unroll
+         for (int j = 0; j + 1 < K - k; ++j)
+            t[j] -= t[j + 1];
+      }
+      const float y = fy[x];
+      int v = 0;
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+#pragma unroll
+         for (int l = 0; l <= k; ++l)
+            acc[v++] += d[k] * d[l];
+      }
+#pragma unroll
+      for (int k = 0; k < K; ++k)
+         acc[v++] += d[k] * y;
+   }
+   // block sums (warp trees, then the eight warps in order), one row per block
+   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+#pragma unroll
+   for (int v = 0; v < NV; ++v) {
+      float a = acc[v];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1)
+         a += __shfl_xor_sync(0xffffffffu, a, o);
+      if (l == 0)
+         sh[w][v] = a;
+   }
+   __syncthreads();
+   for (int v = threadIdx.x; v < NV; v += blockDim.x)
+      part[(size_t)v * LX_NB + blockIdx.x] =
+         (double)(((sh[0][v] + sh[1][v]) + (sh[2][v] + sh[3][v])) + ((sh[4][v] + sh[5][v]) + (sh[6][v] + sh[7][v])));
+   if (!last_block(ticket))
+      return;
+   // the block partials: eight threads per value, each over every eighth
+   // block in order, then the eight in a fixed tree
+   __shared__ double tot[NV];
+   __shared__ double sum8[256];
+   for (int v0 = 0; v0 < NV; v0 += 32) {
+      const int v = v0 + (threadIdx.x >> 3), q = threadIdx.x & 7;
+      double a = 0.0;
+      if (v < NV)
+         for (int b = q; b < LX_NB; b += 8)
+            a += part[(size_t)v * LX_NB + b];
+      sum8[threadIdx.x] = a;
+      __syncthreads();
+      if (q == 0 && v < NV) {
+         const double* t = sum8 + threadIdx.x;
+         tot[v] = ((t[0] + t[1]) + (t[2] + t[3])) + ((t[4] + t[5]) + (t[6] + t[7]));
+      }
+      __syncthreads();
+   }
+   // normal equations with forgetting, one entry per thread: lx = [A, b];
+   // the scaled system into shared memory for the solve
+   __shared__ double Ms[K][K + 1];
+   for (int v = threadIdx.x; v < NV; v += blockDim.x) {
+      int k, q;
+      if (v < K * (K + 1) / 2) {
+         k = 0;
+         while ((k + 1) * (k + 2) / 2 <= v)
+            ++k;
+         q = v - k * (k + 1) / 2;
+      } else {
+         k = v - K * (K + 1) / 2;
+         q = K;
+      }
+      const int at = q < K ? k * LX_MAXK + q : LX_MAXK * LX_MAXK + k;
+      const double a = LX_LAMBDA * lx[at] + tot[v];
+      lx[at] = a;
+      if (q < K) {
+         lx[q * LX_MAXK + k] = a;
+         Ms[k][q] = a;
+         Ms[q][k] = a;
+      } else {
+         Ms[k][K] = a;
+      }
+   }
+   __syncthreads();
+   if (threadIdx.x != 0)
+      return;
+   // the Jacobi-scaled system (condition numbers 10 - 10^3) in FP32: the
+   // sums above are FP64, the solve needs no more than FP32
+   float M[K][K], r[K], sc[K];
+   for (int k = 0; k < K; ++k) {
+      const float a = (float)Ms[k][k];
+      if (!(a > 0.f))
+         return;  // no information yet: the predictor's coefficients stay
+      sc[k] = rsqrtf(a);
+   }
+   for (int k = 0; k < K; ++k) {
+      for (int q = 0; q < K; ++q)
+         M[k][q] = (float)Ms[k][q] * sc[k] * sc[q] + (k == q ? 1e-6f : 0.f);
+      r[k] = (float)Ms[k][K] * sc[k];
+   }
+   // Cholesky M = L L^T in place (lower), then L z = r, L^T a = z
+   for (int k = 0; k < K; ++k) {
+      float dkk = M[k][k];
+      for (int q = 0; q < k; ++q)
+         dkk -= M[k][q] * M[k][q];
+      if (!(dkk > 0.f))
+         return;
+      dkk = sqrtf(dkk);
+      M[k][k] = dkk;
+      const float inv = 1.f / dkk;
+      for (int i = k + 1; i < K; ++i) {
+         float t = M[i][k];
+         for (int q = 0; q < k; ++q)
+            t -= M[i][q] * M[k][q];
+         M[i][k] = t * inv;
+      }
+   }
+   for (int k = 0; k < K; ++k) {
+      float t = r[k];
+      for (int q = 0; q < k; ++q)
+         t -= M[k][q] * r[q];
+      r[k] = t / M[k][k];
+   }
+   for (int k = K - 1; k >= 0; --k) {
+      float t = r[k];
+      for (int q = k + 1; q < K; ++q)
+         t -= M[q][k] * r[q];
+      r[k] = t / M[k][k];
+   }
+   float cf[16];
+   for (int j = 0; j < 16; ++j) {
+      float c = 0.f;
+      if (j < K)
+         for (int k = j; k < K; ++k)
+            c += r[k] * sc[k] * c_sbinom[k][j];
+      cf[j] = c;
+   }
+   for (int j = 0; j < 16; ++j)
+      lcoef[j] = cf[j];
+   state[ST_LX] = min(state[ST_LX] + 1, 1 << 20);
+}
 
 static VecArgs vec_args(const Context* ctx)
 {
@@ -602,7 +805,7 @@ enum { V_PLAIN = 0, V_LEARNED = 1, V_COMPARE = 2, V_PREDICT = 3 };
 static int pcg_start_predict(Context* ctx, const VecArgs& A, bool graph)
 {
    const t9gb_config& c = ctx->cfg;
-   k_predict<<<A.nb, VB, 0, ctx->stream>>>(A, c.predictor, ctx->aspc_hist, ctx->status, ctx->uind);
+   k_predict<<<A.nb, VB, 0, ctx->stream>>>(A, c.predictor, ctx->aspc_hist, ctx->status, ctx->uind, ctx->lx_coef);
    T9_CUDA(cudaGetLastError());
    // the two reciprocal grids need no neighbour list: they start first and
    // run beside the list refresh (side 0: the permanent grid; side 3: the
@@ -636,7 +839,7 @@ static int pcg_start_predict(Context* ctx, const VecArgs& A, bool graph)
    T9_CHECK(launch_dfield_recip_gather(ctx, ctx->fld6, true));
    T9_CHECK(recip_join(ctx, 2));
    k_init_guess<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->fld6, ctx->efield, ctx->udir, ctx->uind, c.pcgguess,
-      c.predictor, ctx->aspc_hist, ctx->status, 0);
+      c.predictor, ctx->aspc_hist, ctx->status, 0, ctx->lx_coef);
    if (ctx->learn_mode & 1)
       T9_CHECK(learn_forward(ctx, false));
    k_init_rsd<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->tmp6, ctx->efield, ctx->udir, ctx->uind, ctx->rsd, 0);
@@ -667,7 +870,7 @@ static int pcg_start(Context* ctx, const VecArgs& A, bool graph, int variant)
       T9_CHECK(dfield6(ctx, ctx->fld6));
    }
    k_init_guess<<<A.nb, VB, 0, ctx->stream>>>(A, ctx->fld6, ctx->efield, ctx->udir, ctx->uind, c.pcgguess,
-      c.predictor, ctx->aspc_hist, ctx->status, 1);
+      c.predictor, ctx->aspc_hist, ctx->status, 1, ctx->lx_coef);
    // the network runs when its guess is used or when this solve trains it
    if ((ctx->learn_mode & 1) || variant != V_PLAIN)
       T9_CHECK(learn_forward(ctx, variant != V_PLAIN));
@@ -808,6 +1011,8 @@ static int induce_graph(Context* ctx, int variant)
       T9_CHECK(induce_capture(ctx, variant));
    T9_CHECK(list_request(ctx));
    T9_CUDA(cudaGraphLaunch(ctx->graph_exec[variant], ctx->stream));
+   if (ctx->lx_k > 0)
+      T9_CUDA(cudaEventRecord(ctx->ev_lx_fork, ctx->stream));
    if (ctx->stage_out)
       T9_CHECK(stage_dipoles(ctx));
    else if (ctx->out_d || ctx->out_p)
@@ -862,12 +1067,15 @@ static int pick_variant(Context* ctx)
    return v;
 }
 
+static int lx_train_launch(Context* ctx, bool side);
+
 int induce_sorted(Context* ctx)
 {
    const bool graph = ctx->use_graph && !ctx->prof.on;
    const int variant = pick_variant(ctx);
    bool range_failed = false;
    ctx->induce_redone = false;
+   T9_CHECK(lx_wait(ctx));
    for (int attempt = 0; attempt < 3; ++attempt) {
       if (attempt > 0)
          ctx->induce_redone = true;
@@ -896,6 +1104,8 @@ int induce_sorted(Context* ctx)
          T9_CUDA(cudaMemcpy(ctx->status + ST_NUALT, &v, sizeof(int), cudaMemcpyHostToDevice));
       }
    }
+   if (!range_failed && ctx->h_status[ST_STATUS] == T9GB_OK)
+      T9_CHECK(lx_train_launch(ctx, graph));
    prof_collect(ctx);
    ctx->last_iter = ctx->h_status[ST_ITER];
    ctx->last_eps = ctx->h_scal[S_EPS];
@@ -919,8 +1129,76 @@ int induce_sorted(Context* ctx)
    return ctx->last_status;
 }
 
+// The fit of the solve just finished runs on its own stream, after the
+// solve's graph (the converged frame is in the ring), beside what the host
+// queues next; the next solve waits for it before it starts.  In the
+// host-driven loop it runs in order.  Not after a failed solve.
+static int lx_train_launch(Context* ctx, bool side)
+{
+   if (ctx->lx_k <= 0 || pred_depth(ctx->cfg) != 16)
+      return T9GB_OK;
+   const VecArgs A = vec_args(ctx);
+   auto k = ctx->lx_k == 2 ? k_lx_train<2> : ctx->lx_k == 3 ? k_lx_train<3> : ctx->lx_k == 4 ? k_lx_train<4>
+      : ctx->lx_k == 5 ? k_lx_train<5> : ctx->lx_k == 6 ? k_lx_train<6> : ctx->lx_k == 7 ? k_lx_train<7>
+      : k_lx_train<8>;
+   cudaStream_t st = ctx->stream;
+   if (side) {
+      T9_CUDA(cudaStreamWaitEvent(ctx->lx_stream, ctx->ev_lx_fork, 0));
+      st = ctx->lx_stream;
+   }
+   k<<<LX_NB, 256, 0, st>>>(A, ctx->aspc_hist, ctx->lx_part, ctx->lx_ab, ctx->lx_coef_buf, ctx->status,
+      ctx->lx_ticket);
+   T9_CUDA(cudaGetLastError());
+   if (side) {
+      T9_CUDA(cudaEventRecord(ctx->ev_lx_done, ctx->lx_stream));
+      ctx->lx_pending = true;
+   }
+   return T9GB_OK;
+}
+
+// work on the ring and the coefficients waits for a fit still running
+int lx_wait(Context* ctx)
+{
+   if (ctx->lx_pending) {
+      T9_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->ev_lx_done, 0));
+      ctx->lx_pending = false;
+   }
+   return T9GB_OK;
+}
+
+// t9gb_learn_extrapolation: order 0 (the predictor's own coefficients) or
+// 2 .. 8 ring frames; a new order starts a new fit
+int lx_config(Context* ctx, int order)
+{
+   if (order != 0 && (order < 2 || order > LX_MAXK || ctx->cfg.predictor != 1))
+      return T9GB_BAD_ARG;
+   T9_CHECK(lx_wait(ctx));
+   if (order > 0 && !ctx->lx_ab) {
+      T9_CUDA(cudaMalloc(&ctx->lx_ab, sizeof(double) * (LX_MAXK * LX_MAXK + LX_MAXK)));
+      T9_CUDA(cudaMalloc(&ctx->lx_part, sizeof(double) * LX_NV * LX_NB));
+      T9_CUDA(cudaMalloc(&ctx->lx_coef_buf, sizeof(float) * 16));
+      T9_CUDA(cudaMalloc(&ctx->lx_ticket, sizeof(int)));
+      T9_CUDA(cudaMemset(ctx->lx_ticket, 0, sizeof(int)));
+      T9_CUDA(cudaStreamCreateWithFlags(&ctx->lx_stream, cudaStreamNonBlocking));
+      T9_CUDA(cudaEventCreateWithFlags(&ctx->ev_lx_fork, cudaEventDisableTiming));
+      T9_CUDA(cudaEventCreateWithFlags(&ctx->ev_lx_done, cudaEventDisableTiming));
+   }
+   if (ctx->lx_ab) {
+      T9_CUDA(cudaMemsetAsync(ctx->lx_ab, 0, sizeof(double) * (LX_MAXK * LX_MAXK + LX_MAXK), ctx->stream));
+      T9_CUDA(cudaMemsetAsync(ctx->lx_coef_buf, 0, sizeof(float) * 16, ctx->stream));
+   }
+   T9_CUDA(cudaMemsetAsync(ctx->status + ST_LX, 0, sizeof(int), ctx->stream));
+   T9_CUDA(cudaStreamSynchronize(ctx->stream));
+   if (order != ctx->lx_k)
+      drop_graphs(ctx);
+   ctx->lx_k = order;
+   ctx->lx_coef = order > 0 ? ctx->lx_coef_buf : nullptr;
+   return T9GB_OK;
+}
+
 int reset_predictor(Context* ctx)
 {
+   T9_CHECK(lx_wait(ctx));
    ctx->learn_ring_full = false;
    T9_CUDA(cudaMemsetAsync(ctx->status + ST_NUALT, 0, sizeof(int), ctx->stream));
    return T9GB_OK;
