@@ -312,7 +312,18 @@ def kernel_rooflines(kernels, n, entries, nfft, peak):
     return out
 
 
-def md_leg(args, abi, tg, stream, nrec, local, config):
+# ring frames of the learned extrapolation (t9gb_learn_extrapolation) in its legs
+LX_ORDER = 8
+
+
+def lx_state(eng):
+    """Fits, rejected fits and the fitted ring coefficients (newest frame
+    first) of an engine's learned extrapolation."""
+    fits, rej, cf = eng.learn_extrapolation_state()
+    return {"fits": fits, "rejected_fits": rej, "ring_coefficients": [round(float(c), 5) for c in cf[:LX_ORDER]]}
+
+
+def md_leg(args, abi, tg, stream, nrec, local, config, lx=0):
     """ns/day: velocity-Verlet MD of the configuration with the whole water
     force field -- multipole + polarization (induce with the ASPC predictor,
     PCG to 1e-6 D), buffered 14-7 van der Waals (9 A, taper from 8.1 A) and
@@ -335,6 +346,8 @@ def md_leg(args, abi, tg, stream, nrec, local, config):
     eng.prepare(s.xyz)
     if args.fft != "auto":
         eng.pme_own_fft(args.fft == "own")
+    if lx:
+        eng.learn_extrapolation(lx)
     dt = 1e-3
     K = args.md_steps
     eng.md_init(s.xyz, mass, v0)
@@ -374,6 +387,7 @@ def md_leg(args, abi, tg, stream, nrec, local, config):
                 eng.md_positions_device(frames[k])
             torch.cuda.synchronize()
     ms = a.elapsed_time(b) / K
+    lxs = lx_state(eng) if lx else None
     eng.close()
     return {
         "ms_per_step": ms,
@@ -386,13 +400,14 @@ def md_leg(args, abi, tg, stream, nrec, local, config):
                        "schedule": "0.2 ps Bussi tau 0.01 ps, 1.8 ps Bussi tau 0.1 ps, 298 K"},
         "clocks": ck,
         "recorded_frames": nrec,
+        **({"extrapolation": lxs} if lxs else {}),
         "status": "ok" if not bad else f"solver status {bad[0]} in {len(bad)} run(s): trajectory stopped early",
         "config": f"{config}: {s.n} atoms, PME {s.settings['nfft'][0]}^3; multipole + polarization (ASPC, PCG "
                   "1e-6 D), HAL 9 A, water valence; Bussi 298 K (tau 0.1 ps), 1 fs velocity Verlet",
     }, frames, s
 
 
-def md_frames_leg(args, abi, s, stream, frames, flush):
+def md_frames_leg(args, abi, s, stream, frames, flush, lx=0):
     """induce() ms/step and PCG iterations on frames of the relaxed box's MD
     trajectory (recorded by the MD leg): the configured workload's
     coordinates, rougher than the synthetic librating trajectory of `value`.
@@ -404,13 +419,20 @@ def md_frames_leg(args, abi, s, stream, frames, flush):
         return None
     eng = abi.Engine(s, predictor=1 if args.predictor == "aspc" else 0, stream=stream)
     eng.prepare(frames[0].double().cpu().numpy())
+    if lx:
+        eng.learn_extrapolation(lx)
     ud = torch.zeros((s.n, 3), device="cuda")
     up = torch.zeros((s.n, 3), device="cuda")
     time_steps(eng, frames, range(H + W), stream, flush, ud, up)
     ms, its, _ = time_steps(eng, frames, range(H + W, H + W + K), stream, flush, ud, up)
+    lxs = lx_state(eng) if lx else None
     eng.close()
-    return {"induce_ms_per_step": float(np.mean(ms)), "pcg_iterations_per_step": float(np.mean(its)),
-            "steps": K, "frames": "MD trajectory of the relaxed box (2 ps NVT, then the timed MD steps)"}
+    out = {"induce_ms_per_step": float(np.mean(ms)), "pcg_iterations_per_step": float(np.mean(its)),
+           "steps": K, "frames": "MD trajectory of the relaxed box (2 ps NVT, then the timed MD steps)"}
+    if lx:
+        out["start"] = f"learned extrapolation of the ASPC ring ({lx} frames, fitted online)"
+        out["extrapolation"] = lxs
+    return out
 
 
 def large_leg(args, abi, tg, stream, flush, peak):
@@ -442,13 +464,26 @@ def large_leg(args, abi, tg, stream, flush, peak):
     kernels = {k: {"ms_total": v[0], "launches": v[1], "ms_per_launch": (v[0] / v[1] if v[1] else None)}
                for k, v in prof.items() if v[1]}
     ls = eng.list_stats()
+    e2 = abi.Engine(s, predictor=1, stream=stream)
+    e2.prepare(tr.frame(0))
+    if args.fft != "auto":
+        e2.pme_own_fft(args.fft == "own")
+    e2.learn_extrapolation(LX_ORDER)
+    time_steps(e2, dev, range(H + W), stream, flush, ud, up)
+    lms, lits, _ = time_steps(e2, dev, range(H + W, H + W + K), stream, flush, ud, up)
+    lxs = lx_state(e2)
+    e2.close()
     out = {"workload": args.large_config, "atoms": s.n, "pme_grid": list(s.settings["nfft"]),
            "induce_ms_per_step": float(np.mean(ms)), "pcg_iterations_per_step": float(np.mean(its)),
+           "induce_learned_extrapolation": {"induce_ms_per_step": float(np.mean(lms)),
+                                            "pcg_iterations_per_step": float(np.mean(lits)),
+                                            "speedup_vs_aspc": float(np.mean(ms)) / float(np.mean(lms)),
+                                            "extrapolation": lxs},
            "kernels": kernels,
            "rooflines": kernel_rooflines(kernels, s.n, ls["entries"], s.settings["nfft"][0], peak)}
     eng.close()
     if not args.no_learned and args.learn_train > 0:
-        nfr = args.learn_train + 3 * (args.warmup + args.steps)
+        nfr = args.learn_train + 4 * (args.warmup + args.steps)
         x0 = 100000  # frames after the measurement's
         lf = torch.from_numpy(np.stack([tr.frame(x0 + t) for t in range(nfr)]).astype(np.float32)).to("cuda")
         out["learned_guess"] = learned_legs(args, s, abi, stream, lf, flush, check_oracle=False)
@@ -489,12 +524,14 @@ def learned_legs(args, s, abi, stream, dev, flush, check_oracle, timed=None):
     legs of --steps frames, each after --warmup untimed frames: the plain
     start (network off), the learned start compared with the plain one on
     every solve (probe 1), and the comparison on every 16th solve (probe 16).
-    Training is off in the timed legs.  dev: device frames [>= T + 3 (W + K)][n][3];
+    Training is off in the timed legs.  The ASPC engine adds a fourth leg: the
+    learned extrapolation of its ring (LX_ORDER frames, fitted online after
+    every solve).  dev: device frames [>= T + 4 (W + K)][n][3];
     K = timed (default --steps)."""
     import torch
 
     T, K, W = args.learn_train, timed or args.steps, args.warmup
-    assert dev.shape[0] >= T + 3 * (W + K)
+    assert dev.shape[0] >= T + 4 * (W + K)
     ud = torch.zeros((s.n, 3), device="cuda")
     up = torch.zeros((s.n, 3), device="cuda")
     out = {"train_steps": T, "timed_steps": K, "rows_per_batch": 2 * s.n,
@@ -511,14 +548,22 @@ def learned_legs(args, s, abi, stream, dev, flush, check_oracle, timed=None):
         res = {"train_ms_per_step": float(np.mean(tr_ms[-50:])), "train_iters_last50": float(np.mean(tr_it[-50:])),
                "train_loss_last": tr_ls[-1][3], "train_wall_s": time.perf_counter() - t0}
         f = T
-        for mode, probe, leg in ((0, 1, "plain"), (2, 1, "learned_probe1"), (2, 16, "learned_probe16")):
+        legs = [(0, 1, "plain"), (2, 1, "learned_probe1"), (2, 16, "learned_probe16")]
+        if pred == 1:
+            legs.append((0, 1, "learned_extrapolation"))
+        for mode, probe, leg in legs:
             eng.learn_config(mode)
             eng.learn_policy(probe)
+            if leg == "learned_extrapolation":
+                eng.learn_extrapolation(LX_ORDER)
             time_steps(eng, dev, range(f, f + W), stream, flush, ud, up)
             idx = list(range(f + W, f + W + K))
             f += W + K
             ms, its, ls = time_steps(eng, dev, idx, stream, flush, ud, up)
             r = {"induce_ms_per_step": float(np.mean(ms)), "pcg_iterations_per_step": float(np.mean(its))}
+            if leg == "learned_extrapolation":
+                r["extrapolation"] = lx_state(eng)
+                r["iterations_histogram"] = np.bincount(its).tolist()
             if mode == 2:
                 r["learned_start_fraction"] = float(np.mean([((c & 1) + ((c >> 1) & 1)) / 2 for c, *_ in ls]))
                 r["compared_fraction"] = float(np.mean([l[4] for l in ls]))
@@ -536,8 +581,9 @@ def learned_legs(args, s, abi, stream, dev, flush, check_oracle, timed=None):
                     r["oracle_rms_dipole_error_debye"] = float(max(
                         np.sqrt(((g_ud - ou) ** 2).sum(1).mean()) * D, np.sqrt(((g_up - op) ** 2).sum(1).mean()) * D))
             res[leg] = r
-        for leg in ("learned_probe1", "learned_probe16"):
-            res[leg]["speedup_vs_plain"] = res["plain"]["induce_ms_per_step"] / res[leg]["induce_ms_per_step"]
+        for leg in ("learned_probe1", "learned_probe16", "learned_extrapolation"):
+            if leg in res:
+                res[leg]["speedup_vs_plain"] = res["plain"]["induce_ms_per_step"] / res[leg]["induce_ms_per_step"]
         out[name] = res
         eng.close()
     return out
@@ -633,6 +679,26 @@ def main():
         dev_sec = float(t.item())
     value = world * args.steps / dev_sec
 
+    # ---- the same frames from the learned extrapolation of the ASPC ring ----
+    lx_res = None
+    if pred == 1:
+        e2 = abi.Engine(s, predictor=1, stream=stream)
+        e2.prepare(tr.frame(0))
+        if args.fft != "auto":
+            e2.pme_own_fft(args.fft == "own")
+        if args.lanes:
+            e2.pair_lanes(args.lanes)
+        e2.learn_extrapolation(LX_ORDER)
+        time_steps(e2, dev_frames, range(args.history + args.warmup), stream, flush, ud, up)
+        lms, lits, _ = time_steps(e2, dev_frames, range(args.history + args.warmup,
+                                                         args.history + args.warmup + args.steps), stream, flush, ud, up)
+        lxs = lx_state(e2)
+        e2.close()
+        lx_res = {"induce_ms_per_step": float(np.mean(lms)), "pcg_iterations_per_step": float(np.mean(lits)),
+                  "speedup_vs_aspc": (1000 * dev_sec / args.steps) / float(np.mean(lms)),
+                  "start": f"learned extrapolation of the ASPC ring ({LX_ORDER} frames, fitted online after every "
+                           "solve)", "frames": "the timed frames of value", "extrapolation": lxs}
+
     # ---- e2e: host coordinates in, host dipoles out ----
     hu = np.zeros((s.n, 3))
     hp = np.zeros((s.n, 3))
@@ -700,15 +766,18 @@ def main():
 
     # ---- MD (ns/day), recording the frames of the learned-guess legs ----
     want_learned = not args.no_learned and args.learn_train > 0
-    nrec = args.learn_train + 3 * (args.warmup + args.learn_steps) if want_learned else 0
+    nrec = args.learn_train + 4 * (args.warmup + args.learn_steps) if want_learned else 0
     nrec = max(nrec, args.history + args.warmup + args.steps)
     md, md_frames, md_sys = None, None, None
     if not args.no_md:
         md, md_frames, md_sys = md_leg(args, abi, tg, stream, nrec, local, args.config)
 
-    md_frames_res = None
+    md_frames_res = md_frames_lx = None
     if md_frames is not None:
         md_frames_res = md_frames_leg(args, abi, md_sys, stream, md_frames, flush)
+        if pred == 1:
+            md_frames_lx = md_frames_leg(args, abi, md_sys, stream, md_frames, flush, lx=LX_ORDER)
+            md_frames_lx["speedup_vs_aspc"] = md_frames_res["induce_ms_per_step"] / md_frames_lx["induce_ms_per_step"]
 
     learned = None
     if want_learned:
@@ -727,11 +796,15 @@ def main():
     if not args.no_large:
         large = large_leg(args, abi, tg, stream, flush, peak)
 
-    # ---- MD of the other configurations (ns/day only) ----
+    # ---- MD of the other configurations (ns/day only), and of this one from
+    # the learned extrapolation of the ASPC ring ----
     md_other = {}
+    md_lx = None
     if not args.no_md:
         for name in [c for c in args.md_extra.split(",") if c and c != args.config]:
             md_other[name] = md_leg(args, abi, tg, stream, 0, local, name)[0]
+        md_lx = md_leg(args, abi, tg, stream, 0, local, args.config, lx=LX_ORDER)[0]
+        md_lx["start"] = f"learned extrapolation of the ASPC ring ({LX_ORDER} frames, fitted online after every solve)"
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -763,12 +836,16 @@ def main():
             "induce_ms_per_step": 1000 * dev_sec / args.steps,
             "pcg_iterations_per_step": mean_it,
             "induce_md_frames": md_frames_res,
+            "induce_learned_extrapolation": lx_res,
+            "induce_md_frames_learned_extrapolation": md_frames_lx,
             "induce_note": "value and induce_ms_per_step: the seeded librating trajectory (smoother than MD: "
-                           "fewer PCG iterations); induce_md_frames: the same solve on frames of the relaxed "
-                           "box's MD trajectory",
+                           "fewer PCG iterations), ASPC start as the reference; induce_md_frames: the same solve "
+                           "on frames of the relaxed box's MD trajectory; *_learned_extrapolation: the same frames "
+                           "from the learned extrapolation of the ASPC ring",
             "ns_per_day": None if md is None else md["ns_per_day"],
             "ns_per_day_note": "MD leg (see md)" if md is not None else "MD leg skipped (--no-md)",
             "md": md,
+            "md_learned_extrapolation": md_lx,
             "md_other_configs": md_other,
             "wall_s_timed": wall,
             "e2e": {"value": e2e_value, "unit": "induce() calls/s", "ms_per_step": 1000 * e2e_sec / args.steps,

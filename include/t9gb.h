@@ -494,6 +494,11 @@ int t9gb_learn_tensor_path(t9gb_context* ctx, int path);
  * convergence test is unchanged.  0 (the default) keeps ASPC.  A new order
  * starts a new fit.  T9GB_BAD_ARG for other orders or without ASPC. */
 int t9gb_learn_extrapolation(t9gb_context* ctx, int order);
+/* State of the learned extrapolation after the last solve: the fits so far
+ * (*fits), those whose solve failed and left the previous coefficients in
+ * place (*rejected), and the 16 ring coefficients by frame age (coef[0] the
+ * newest frame; 0 beyond the order).  Zeros while the extrapolation is off. */
+int t9gb_learn_extrapolation_state(t9gb_context* ctx, int* fits, int* rejected, float* coef16);
 /* Raw features of the last solve, device [2n][32]: rows 0..n-1 for the d
  * dipoles, n..2n-1 for the p dipoles, caller atom order. */
 int t9gb_learn_features(t9gb_context* ctx, float* features_device);

@@ -328,6 +328,14 @@ def test_learned_extrapolation(gpu_lib, oracle, tg):
             ib.append(b.stats()[0])
     print("iterations ASPC", np.mean(ia), "learned extrapolation", np.mean(ib))
     assert np.mean(ib) <= np.mean(ia)
+    # a fit after every solve from the eighth on (7 ring frames and the new
+    # one), none rejected; the coefficients reproduce a constant frame
+    fb, rb, cb = b.learn_extrapolation_state()
+    fc, rc_, cc = c.learn_extrapolation_state()
+    assert (fb, rb) == (fc, rc_) == (33, 0)
+    assert np.array_equal(cb, cc) and not cb[7:].any()
+    assert abs(float(cb.sum()) - 1.0) < 0.05, cb
+    assert a.learn_extrapolation_state()[:2] == (0, 0) and not a.learn_extrapolation_state()[2].any()
     ou, op, *_ = oracle.OracleSystem(s, xyz=tr.frame(39)).induce()
     D = tg.units.DEBYE
     assert rms_err(ub * D, ou * D) < DIPOLE_RMS_DEBYE and rms_err(pb * D, op * D) < DIPOLE_RMS_DEBYE

@@ -33,6 +33,7 @@ EXPORTS = [
     "t9gb_evalence", "t9gb_md_init", "t9gb_md_run", "t9gb_md_state", "t9gb_md_positions_device", "t9gb_md_stats",
     "t9gb_set_xyz_soa_device", "t9gb_diag_precond_apply", "t9gb_gradient_fixed", "t9gb_pme_fft_cluster",
     "t9gb_copy_error", "t9gb_pair_staging", "t9gb_learn_tensor_path", "t9gb_learn_extrapolation",
+    "t9gb_learn_extrapolation_state",
 ]
 CALC_ENERGY, CALC_GRAD, CALC_VIRIAL = 0x010, 0x020, 0x040
 
@@ -131,6 +132,8 @@ def load(path=None):
     lib.t9gb_pair_staging.argtypes = [vp, C.c_int]
     lib.t9gb_learn_tensor_path.argtypes = [vp, C.c_int]
     lib.t9gb_learn_extrapolation.argtypes = [vp, C.c_int]
+    lib.t9gb_learn_extrapolation_state.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                                   C.POINTER(C.c_float)]
     lib.t9gb_pair_lanes.argtypes = [vp, C.c_int]
     lib.t9gb_set_pcg_fusion.argtypes = [vp, C.c_int]
     lib.t9gb_force_lanes.argtypes = [vp, C.c_int]
@@ -523,9 +526,15 @@ class Engine:
         """0: mma.sync GEMMs; 1: the fused tcgen05 forward pass."""
         self._check(self.lib.t9gb_learn_tensor_path(self.h, int(path)))
 
-    def learn_extrapolation(self, order=7):
+    def learn_extrapolation(self, order=8):
         """Learned extrapolation of the ASPC ring over `order` frames (2-8); 0 restores ASPC."""
         self._check(self.lib.t9gb_learn_extrapolation(self.h, int(order)))
+
+    def learn_extrapolation_state(self):
+        """(fits, rejected fits, the 16 ring coefficients by frame age) after the last solve."""
+        fits, rej, cf = C.c_int(), C.c_int(), (C.c_float * 16)()
+        self._check(self.lib.t9gb_learn_extrapolation_state(self.h, C.byref(fits), C.byref(rej), cf))
+        return fits.value, rej.value, np.array(cf[:], dtype=np.float32)
 
     def learn_adamw(self):
         self._check(self.lib.t9gb_learn_adamw(self.h))

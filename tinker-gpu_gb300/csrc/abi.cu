@@ -659,6 +659,13 @@ int t9gb_learn_extrapolation(t9gb_context* h, int order)
    return lx_config(&h->c, order);
 }
 
+int t9gb_learn_extrapolation_state(t9gb_context* h, int* fits, int* rejected, float* coef16)
+{
+   if (!h)
+      return T9GB_BAD_ARG;
+   return lx_state(&h->c, fits, rejected, coef16);
+}
+
 int t9gb_learn_tensor_path(t9gb_context* h, int path)
 {
    if (!h || (path != 0 && path != 1))

@@ -522,6 +522,7 @@ int list_update(Context* ctx);  // device: exact neighbour list
 int ensure_list(Context* ctx);  // list_update when the coordinates changed
 int check_list_overflow(Context* ctx, int* redo);
 int lx_config(Context* ctx, int order);   // pcg.cu
+int lx_state(Context* ctx, int* fits, int* rejected, float* coef16);  // pcg.cu
 int lx_wait(Context* ctx);                // pcg.cu
 int alloc_lists(Context* ctx, int cap);          // nbr, nbrc, nbrp with row capacity cap
 int pair_staging_setup();                         // pair.cu: shared-memory limits of the staged kernels

@@ -310,6 +310,63 @@ __constant__ float c_sbinom[LX_MAXK][LX_MAXK] = {
    {1, -6, 15, -20, 15, -6, 1, 0},
    {1, -7, 21, -35, 35, -21, 7, -1}};
 
+// Cholesky solve of the Jacobi-scaled normal equations (M + ridge I) z = r
+// in FP32 (M = S A S, r = S b, S = diag(sc)); false when a pivot is not
+// positive.  r returns the unscaled solution S z.
+template <int K>
+__device__ bool lx_solve(const double (*Ms)[K + 1], const float* sc, float ridge, float* r)
+{
+   float M[K][K];
+#pragma unroll
+   for (int k = 0; k < K; ++k) {
+#pragma unroll
+      for (int q = 0; q < K; ++q)
+         M[k][q] = (float)Ms[k][q] * sc[k] * sc[q] + (k == q ? ridge : 0.f);
+      r[k] = (float)Ms[k][K] * sc[k];
+   }
+   // M = L L^T in place (lower), then L z = r, L^T a = z
+#pragma unroll
+   for (int k = 0; k < K; ++k) {
+      float dkk = M[k][k];
+#pragma unroll
+      for (int q = 0; q < k; ++q)
+         dkk -= M[k][q] * M[k][q];
+      if (!(dkk > 0.f))
+         return false;
+      dkk = sqrtf(dkk);
+      M[k][k] = dkk;
+      const float inv = 1.f / dkk;
+#pragma unroll
+      for (int i = k + 1; i < K; ++i) {
+         float t = M[i][k];
+#pragma unroll
+         for (int q = 0; q < k; ++q)
+            t -= M[i][q] * M[k][q];
+         M[i][k] = t * inv;
+      }
+   }
+#pragma unroll
+   for (int k = 0; k < K; ++k) {
+      float t = r[k];
+#pragma unroll
+      for (int q = 0; q < k; ++q)
+         t -= M[k][q] * r[q];
+      r[k] = t / M[k][k];
+   }
+#pragma unroll
+   for (int k = K - 1; k >= 0; --k) {
+      float t = r[k];
+#pragma unroll
+      for (int q = k + 1; q < K; ++q)
+         t -= M[q][k] * r[q];
+      r[k] = t / M[k][k];
+   }
+#pragma unroll
+   for (int k = 0; k < K; ++k)
+      r[k] *= sc[k];
+   return true;
+}
+
 // The differences are formed in FP64 from the FP32 ring (exact: small
 // integer weights), rounded to FP32 (their own relative precision), and the
 // products summed in FP32 per thread and block (a few hundred terms), then
@@ -422,54 +479,31 @@ __global__ void __launch_bounds__(256) k_lx_train(VecArgs A, const float* __rest
    if (threadIdx.x != 0)
       return;
    // the Jacobi-scaled system (condition numbers 10 - 10^3) in FP32: the
-   // sums above are FP64, the solve needs no more than FP32
-   float M[K][K], r[K], sc[K];
+   // sums above are FP64, the solve needs no more than FP32.  A failed
+   // factorisation retries with a 100x larger ridge (twice), then leaves the
+   // previous coefficients in place and counts the rejection.
+   float sc[K], r[K];
+   bool ok = true;
    for (int k = 0; k < K; ++k) {
       const float a = (float)Ms[k][k];
-      if (!(a > 0.f))
-         return;  // no information yet: the predictor's coefficients stay
-      sc[k] = rsqrtf(a);
+      ok = ok && a > 0.f;  // no information yet: the predictor's coefficients stay
+      sc[k] = ok ? rsqrtf(a) : 0.f;
    }
-   for (int k = 0; k < K; ++k) {
-      for (int q = 0; q < K; ++q)
-         M[k][q] = (float)Ms[k][q] * sc[k] * sc[q] + (k == q ? 1e-6f : 0.f);
-      r[k] = (float)Ms[k][K] * sc[k];
+   if (ok) {
+      ok = false;
+      for (float ridge = 1e-6f; !ok && ridge < 1e-1f; ridge *= 100.f)
+         ok = lx_solve<K>(Ms, sc, ridge, r);
    }
-   // Cholesky M = L L^T in place (lower), then L z = r, L^T a = z
-   for (int k = 0; k < K; ++k) {
-      float dkk = M[k][k];
-      for (int q = 0; q < k; ++q)
-         dkk -= M[k][q] * M[k][q];
-      if (!(dkk > 0.f))
-         return;
-      dkk = sqrtf(dkk);
-      M[k][k] = dkk;
-      const float inv = 1.f / dkk;
-      for (int i = k + 1; i < K; ++i) {
-         float t = M[i][k];
-         for (int q = 0; q < k; ++q)
-            t -= M[i][q] * M[k][q];
-         M[i][k] = t * inv;
-      }
-   }
-   for (int k = 0; k < K; ++k) {
-      float t = r[k];
-      for (int q = 0; q < k; ++q)
-         t -= M[k][q] * r[q];
-      r[k] = t / M[k][k];
-   }
-   for (int k = K - 1; k >= 0; --k) {
-      float t = r[k];
-      for (int q = k + 1; q < K; ++q)
-         t -= M[q][k] * r[q];
-      r[k] = t / M[k][k];
+   if (!ok) {
+      state[ST_LX_REJ] = min(state[ST_LX_REJ] + 1, 1 << 20);
+      return;
    }
    float cf[16];
    for (int j = 0; j < 16; ++j) {
       float c = 0.f;
       if (j < K)
          for (int k = j; k < K; ++k)
-            c += r[k] * sc[k] * c_sbinom[k][j];
+            c += r[k] * c_sbinom[k][j];
       cf[j] = c;
    }
    for (int j = 0; j < 16; ++j)
@@ -1187,12 +1221,33 @@ int lx_config(Context* ctx, int order)
       T9_CUDA(cudaMemsetAsync(ctx->lx_ab, 0, sizeof(double) * (LX_MAXK * LX_MAXK + LX_MAXK), ctx->stream));
       T9_CUDA(cudaMemsetAsync(ctx->lx_coef_buf, 0, sizeof(float) * 16, ctx->stream));
    }
-   T9_CUDA(cudaMemsetAsync(ctx->status + ST_LX, 0, sizeof(int), ctx->stream));
+   T9_CUDA(cudaMemsetAsync(ctx->status + ST_LX, 0, 2 * sizeof(int), ctx->stream));  // ST_LX, ST_LX_REJ
    T9_CUDA(cudaStreamSynchronize(ctx->stream));
    if (order != ctx->lx_k)
       drop_graphs(ctx);
    ctx->lx_k = order;
    ctx->lx_coef = order > 0 ? ctx->lx_coef_buf : nullptr;
+   return T9GB_OK;
+}
+
+// t9gb_learn_extrapolation_state: after the fit of the last solve
+int lx_state(Context* ctx, int* fits, int* rejected, float* coef16)
+{
+   int st[2] = {0, 0};
+   float cf[16] = {};
+   if (ctx->lx_k > 0) {
+      T9_CHECK(lx_wait(ctx));
+      T9_CUDA(cudaMemcpyAsync(st, ctx->status + ST_LX, sizeof(st), cudaMemcpyDeviceToHost, ctx->stream));
+      T9_CUDA(cudaMemcpyAsync(cf, ctx->lx_coef_buf, sizeof(cf), cudaMemcpyDeviceToHost, ctx->stream));
+      T9_CUDA(cudaStreamSynchronize(ctx->stream));
+   }
+   if (fits)
+      *fits = st[0];
+   if (rejected)
+      *rejected = st[1];
+   if (coef16)
+      for (int j = 0; j < 16; ++j)
+         coef16[j] = cf[j];
    return T9GB_OK;
 }
 

@@ -17,9 +17,9 @@ enum { S_SUM_D = 0, S_SUM_P, S_A_D, S_A_P, S_B_D, S_B_P, S_EPS, S_L_PLAIN_D = 8,
 // ST_RANGE_L: the same while evaluating the learned guess's residual;
 // ST_TICKET_SUM: the last-block ticket of the energy / virial row sums;
 // ST_LX: fits of the learned extrapolation so far (its coefficients replace
-// the predictor's from the second on)
+// the predictor's from the second on); ST_LX_REJ: fits whose solve failed
 enum { ST_ITER = 0, ST_DONE, ST_STATUS, ST_NUALT, ST_TICKET0, ST_TICKET1, ST_LCHOICE, ST_LREADY, ST_RANGE,
-   ST_RANGE_L, ST_TICKET_SUM, ST_LX, ST_NSTAT };
+   ST_RANGE_L, ST_TICKET_SUM, ST_LX, ST_LX_REJ, ST_NSTAT };
 static_assert(ST_NSTAT <= 16, "the context allocates 16 status words");
 enum { R_PAP_D = 0, R_PAP_P, R_RZ_D, R_RZ_P, R_RR_D, R_RR_P };
 
