@@ -228,3 +228,38 @@ def guess(system, y, field_d, field_p, frames, tscale):
     g = np.einsum("nab,na->nb", frames, y[:n]) * tscale
     gp = np.einsum("nab,na->nb", frames, y[n:]) * tscale
     return alpha * (field_d + g), alpha * (field_p + gp)
+
+
+def lx_ring_coefficients(frames, order, lam=0.99, ridge=1e-6):
+    """The learned extrapolation of the predictor ring, restated in FP64.
+
+    frames: the converged dipoles of consecutive solves (any shape; the d and
+    p sets of one solve together), oldest first.  After every solve t >= order
+    the newest frame y = u_t and the `order` frames before it give the samples
+    y ~ sum_k a_k D^k u_{t-1} over every element, D^k u_{t-1} =
+    sum_j (-1)^j C(k, j) u_{t-1-j} the k-th backward difference.  The normal
+    equations accumulate with forgetting factor lam (N <- lam N + D^T D,
+    r <- lam r + D^T y); each fit solves the Jacobi-scaled system plus ridge on
+    its diagonal.  Returns the 16 ring coefficients by frame age (0 the newest;
+    zero beyond the order) after the last fit, c_j = sum_k a_k (-1)^j C(k, j),
+    and the number of fits."""
+    from math import comb
+
+    K = order
+    U = [np.asarray(f, dtype=np.float64).ravel() for f in frames]
+    N = np.zeros((K, K))
+    r = np.zeros(K)
+    coef = np.zeros(16)
+    fits = 0
+    S = np.array([[(-1) ** j * comb(k, j) for j in range(K)] for k in range(K)], dtype=np.float64)
+    for t in range(K, len(U)):
+        prev = np.stack([U[t - 1 - j] for j in range(K)], 1)   # [m][K], ages 0..K-1
+        D = prev @ S.T                                          # [m][K], differences 0..K-1
+        N = lam * N + D.T @ D
+        r = lam * r + D.T @ U[t]
+        sc = 1.0 / np.sqrt(np.diag(N))
+        z = np.linalg.solve(N * np.outer(sc, sc) + ridge * np.eye(K), r * sc)
+        a = z * sc
+        coef[:K] = S.T @ a
+        fits += 1
+    return coef, fits

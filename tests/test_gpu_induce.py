@@ -315,7 +315,7 @@ def test_learned_extrapolation(gpu_lib, oracle, tg):
     c = engine_for(s, predictor=1)
     c.learn_extrapolation(7)
     c.use_graph(False)
-    ia, ib = [], []
+    ia, ib, hist = [], [], []
     for step in range(40):
         x = tr.frame(step)
         ua, pa, _ = a.induce_host(x)
@@ -323,6 +323,7 @@ def test_learned_extrapolation(gpu_lib, oracle, tg):
         uc, pc, _ = c.induce_host(x)
         assert rc == 0
         assert np.array_equal(ub, uc) and np.array_equal(pb, pc), step
+        hist.append(np.concatenate([ub, pb]))
         if step >= 24:
             ia.append(a.stats()[0])
             ib.append(b.stats()[0])
@@ -335,6 +336,15 @@ def test_learned_extrapolation(gpu_lib, oracle, tg):
     assert (fb, rb) == (fc, rc_) == (33, 0)
     assert np.array_equal(cb, cc) and not cb[7:].any()
     assert abs(float(cb.sum()) - 1.0) < 0.05, cb
+    # the same online fit restated in FP64 over the returned dipoles (the
+    # ring holds exactly those values; the device sums products in FP32 and
+    # solves in FP32: 7e-5 of the largest coefficient measured)
+    from oracle import learn_oracle as LO
+
+    ref, nfit = LO.lx_ring_coefficients(hist, 7)
+    err = float(np.abs(cb - ref).max())
+    print("ring coefficients", cb[:7], "FP64 restatement", ref[:7], "max error", err)
+    assert nfit == 33 and err < 2e-4 * max(1.0, float(np.abs(ref).max()))  # measured 7e-5
     assert a.learn_extrapolation_state()[:2] == (0, 0) and not a.learn_extrapolation_state()[2].any()
     ou, op, *_ = oracle.OracleSystem(s, xyz=tr.frame(39)).induce()
     D = tg.units.DEBYE

@@ -144,3 +144,22 @@ def test_features_two_atoms_by_hand(tg):
     q1 = s.pole[1, 0]
     assert X[0, 17] == pytest.approx(q1 * fc * np.exp(-((r - 2.0) ** 2) / 2.0))
     assert X[1, 17] == pytest.approx(-s.pole[0, 0] * fc * np.exp(-((r - 2.0) ** 2) / 2.0))
+
+
+def test_lx_ring_coefficients_polynomial():
+    """The restated online fit of the ring extrapolation: frames that follow
+    polynomials of degree K - 1 in time are extrapolated exactly by
+    c_j = (-1)^j C(K, j + 1) (the K-th difference vanishes), one fit after
+    each frame from the (K + 1)-th on; the coefficients sum to 1."""
+    from math import comb
+
+    rng = np.random.default_rng(3)
+    for K in (2, 4, 6):
+        P = rng.normal(size=(K, 300))
+        frames = [sum(P[d] * (0.1 * t) ** d for d in range(K)) for t in range(K + 20)]
+        c, nfit = LO.lx_ring_coefficients(frames, K, ridge=0.0)
+        want = np.zeros(16)
+        want[:K] = [(-1) ** j * comb(K, j + 1) for j in range(K)]
+        assert nfit == 20
+        assert np.abs(c - want).max() < 1e-6 * comb(K, K // 2), (K, c[:K])
+        assert c.sum() == pytest.approx(1.0, abs=1e-8)
