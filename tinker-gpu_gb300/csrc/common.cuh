@@ -309,7 +309,7 @@ struct Context {
    // learned extrapolation of the ASPC ring (t9gb_learn_extrapolation)
    int lx_k = 0;                  // ring frames of the fit, 0: off
    double* lx_ab = nullptr;       // normal equations [8][8] + [8]
-   double* lx_part = nullptr;     // per-block partial sums
+   float* lx_part = nullptr;      // per-block partial sums
    float* lx_coef_buf = nullptr;  // ring coefficients by frame age [16]
    float* lx_coef = nullptr;      // lx_coef_buf while on, else null
    int* lx_ticket = nullptr;      // last-block ticket of the fit

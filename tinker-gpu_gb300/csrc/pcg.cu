@@ -290,8 +290,9 @@ __global__ void k_bump_nualt(int* state, int depth)
 // both dipole sets: u_t ~ sum_k a_k D^k u_{t-1}, D^k the k-th backward
 // difference over the ring (a well-conditioned basis: Jacobi-scaled
 // condition numbers of 10^2 - 10^3 at K = 6 - 8).  The normal equations are
-// summed in FP64 in a fixed order, kept with forgetting factor LX_LAMBDA,
-// and solved by Cholesky in the launch's last block; the raw coefficients
+// summed in a fixed order (FP32 per block, compensated FP32 across blocks),
+// kept in FP64 with forgetting factor LX_LAMBDA, and solved by an FP32
+// Cholesky in the launch's last block; the raw coefficients
 // c_j = sum_k a_k (-1)^j C(k, j) of the ring frames replace the
 // predictor's (ring_coef).  The PCG convergence test is unchanged.
 constexpr int LX_MAXK = 8;
@@ -310,19 +311,30 @@ __constant__ float c_sbinom[LX_MAXK][LX_MAXK] = {
    {1, -6, 15, -20, 15, -6, 1, 0},
    {1, -7, 21, -35, 35, -21, 7, -1}};
 
+// a + b = s + e exactly (Knuth's two-sum, no FMA contraction of sums);
+// returns e, s into *out (which may alias a)
+__device__ __forceinline__ float two_sum(float a, float b, float& out)
+{
+   const float s = __fadd_rn(a, b);
+   const float bb = __fsub_rn(s, a);
+   const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+   out = s;
+   return e;
+}
+
 // Cholesky solve of the Jacobi-scaled normal equations (M + ridge I) z = r
 // in FP32 (M = S A S, r = S b, S = diag(sc)); false when a pivot is not
 // positive.  r returns the unscaled solution S z.
 template <int K>
-__device__ bool lx_solve(const double (*Ms)[K + 1], const float* sc, float ridge, float* r)
+__device__ bool lx_solve(const float (*Ms)[K + 1], const float* sc, float ridge, float* r)
 {
    float M[K][K];
 #pragma unroll
    for (int k = 0; k < K; ++k) {
 #pragma unroll
       for (int q = 0; q < K; ++q)
-         M[k][q] = (float)Ms[k][q] * sc[k] * sc[q] + (k == q ? ridge : 0.f);
-      r[k] = (float)Ms[k][K] * sc[k];
+         M[k][q] = Ms[k][q] * sc[k] * sc[q] + (k == q ? ridge : 0.f);
+      r[k] = Ms[k][K] * sc[k];
    }
    // M = L L^T in place (lower), then L z = r, L^T a = z
 #pragma unroll
@@ -368,11 +380,12 @@ __device__ bool lx_solve(const double (*Ms)[K + 1], const float* sc, float ridge
 }
 
 // The differences are formed in FP32 (each subtraction rounds to its own
-// result; FP64, which keeps them exact, took the kernel from 15.3 to 20.8 us
-// at 12,288 atoms), and the products summed in FP32 per thread and block (a
-// few hundred terms), then in FP64 across blocks.
+// result) and the products summed in FP32 per thread and block (a few
+// hundred terms).  FP64 runs at 1/64 of the FP32 rate on this GPU: FP64
+// differences and FP64 cross-block sums made the kernel 20.8 us at 12,288
+// atoms, against 10.7 us now.
 template <int K>
-__global__ void __launch_bounds__(256) k_lx_train(VecArgs A, const float* __restrict__ hist, double* __restrict__ part,
+__global__ void __launch_bounds__(256) k_lx_train(VecArgs A, const float* __restrict__ hist, float* __restrict__ part,
    double* __restrict__ lx, float* __restrict__ lcoef, int* __restrict__ state, int* __restrict__ ticket)
 {
    constexpr int NV = K * (K + 1) / 2 + K;
@@ -429,38 +442,44 @@ __global__ void __launch_bounds__(256) k_lx_train(VecArgs A, const float* __rest
    __syncthreads();
    for (int v = threadIdx.x; v < NV; v += blockDim.x)
       part[(size_t)v * LX_NB + blockIdx.x] =
-         (double)(((sh[0][v] + sh[1][v]) + (sh[2][v] + sh[3][v])) + ((sh[4][v] + sh[5][v]) + (sh[6][v] + sh[7][v])));
+         ((sh[0][v] + sh[1][v]) + (sh[2][v] + sh[3][v])) + ((sh[4][v] + sh[5][v]) + (sh[6][v] + sh[7][v]));
    if (!last_block(ticket))
       return;
    // the block partials: warp w sums values w, w + 8, ..., every lane over
-   // the blocks lane + 32 i in order, then a fixed butterfly; all of a
-   // lane's loads are issued before the first sum
+   // the blocks lane + 32 i in order, then a fixed butterfly, in compensated
+   // FP32 (the sum and its exact rounding errors, two_sum): as accurate as
+   // FP64 here, which runs at 1/64 of the FP32 rate on this GPU
    constexpr int NVW = (NV + 7) / 8, NBL = (LX_NB + 31) / 32;
-   __shared__ double tot[NV];
-   double pv[NVW][NBL];
+   __shared__ float tot_s[NV], tot_c[NV];
+   float pv[NVW][NBL];
 #pragma unroll
    for (int i = 0; i < NVW; ++i)
 #pragma unroll
       for (int q = 0; q < NBL; ++q) {
          const int v = w + 8 * i, b = l + 32 * q;
-         pv[i][q] = v < NV && b < LX_NB ? __ldcg(part + (size_t)v * LX_NB + b) : 0.0;
+         pv[i][q] = v < NV && b < LX_NB ? __ldcg(part + (size_t)v * LX_NB + b) : 0.f;
       }
 #pragma unroll
    for (int i = 0; i < NVW; ++i) {
-      double a = pv[i][0];
+      float a = pv[i][0], c = 0.f;
 #pragma unroll
       for (int q = 1; q < NBL; ++q)
-         a += pv[i][q];
+         c += two_sum(a, pv[i][q], a);
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1)
-         a += __shfl_xor_sync(0xffffffffu, a, o);
-      if (l == 0 && w + 8 * i < NV)
-         tot[w + 8 * i] = a;
+      for (int o = 16; o > 0; o >>= 1) {
+         const float a2 = __shfl_xor_sync(0xffffffffu, a, o), c2 = __shfl_xor_sync(0xffffffffu, c, o);
+         const float e = two_sum(a, a2, a);
+         c = (c + c2) + e;
+      }
+      if (l == 0 && w + 8 * i < NV) {
+         tot_s[w + 8 * i] = a;
+         tot_c[w + 8 * i] = c;
+      }
    }
    __syncthreads();
-   // normal equations with forgetting, one entry per thread: lx = [A, b];
-   // the scaled system into shared memory for the solve
-   __shared__ double Ms[K][K + 1];
+   // normal equations with forgetting (FP64), one entry per thread:
+   // lx = [A, b]; the system in FP32 into shared memory for the solve
+   __shared__ float Ms[K][K + 1];
    for (int v = threadIdx.x; v < NV; v += blockDim.x) {
       int k, q;
       if (v < K * (K + 1) / 2) {
@@ -473,27 +492,28 @@ __global__ void __launch_bounds__(256) k_lx_train(VecArgs A, const float* __rest
          q = K;
       }
       const int at = q < K ? k * LX_MAXK + q : LX_MAXK * LX_MAXK + k;
-      const double a = LX_LAMBDA * lx[at] + tot[v];
+      const double a = LX_LAMBDA * lx[at] + ((double)tot_s[v] + (double)tot_c[v]);
       lx[at] = a;
+      const float af = (float)a;
       if (q < K) {
          lx[q * LX_MAXK + k] = a;
-         Ms[k][q] = a;
-         Ms[q][k] = a;
+         Ms[k][q] = af;
+         Ms[q][k] = af;
       } else {
-         Ms[k][K] = a;
+         Ms[k][K] = af;
       }
    }
    __syncthreads();
    if (threadIdx.x != 0)
       return;
    // the Jacobi-scaled system (condition numbers 10 - 10^3) in FP32: the
-   // sums above are FP64, the solve needs no more than FP32.  A failed
+   // sums above carry FP64 accuracy, the solve needs no more.  A failed
    // factorisation retries with a 100x larger ridge (twice), then leaves the
    // previous coefficients in place and counts the rejection.
    float sc[K], r[K];
    bool ok = true;
    for (int k = 0; k < K; ++k) {
-      const float a = (float)Ms[k][k];
+      const float a = Ms[k][k];
       ok = ok && a > 0.f;  // no information yet: the predictor's coefficients stay
       sc[k] = ok ? rsqrtf(a) : 0.f;
    }
@@ -1217,7 +1237,7 @@ int lx_config(Context* ctx, int order)
    T9_CHECK(lx_wait(ctx));
    if (order > 0 && !ctx->lx_ab) {
       T9_CUDA(cudaMalloc(&ctx->lx_ab, sizeof(double) * (LX_MAXK * LX_MAXK + LX_MAXK)));
-      T9_CUDA(cudaMalloc(&ctx->lx_part, sizeof(double) * LX_NV * LX_NB));
+      T9_CUDA(cudaMalloc(&ctx->lx_part, sizeof(float) * LX_NV * LX_NB));
       T9_CUDA(cudaMalloc(&ctx->lx_coef_buf, sizeof(float) * 16));
       T9_CUDA(cudaMalloc(&ctx->lx_ticket, sizeof(int)));
       T9_CUDA(cudaMemset(ctx->lx_ticket, 0, sizeof(int)));
