@@ -96,6 +96,7 @@ def _tinkernist_files(d):
         f.write("parameters  nist\n# comment line\nverbose\n")
         f.write(f"a-axis {m['box'][0]}\nneighbor-list\nvdw-cutoff {m['vdw_cutoff']}\newald\n")
         f.write(f"ewald-cutoff {m['ewald_cutoff']}\npme-grid {T.NFFT} {T.NFFT} {T.NFFT}\npolar-eps {m['polar_eps']}\n")
+        f.write("polar-predict\n")  # as test/file/water30/water30.key
     lines = []
     for k, v in m["scales"].items():
         lines.append(f"{k:<24s}{v}")
@@ -138,6 +139,7 @@ def test_system_from_tinker_files(tmp_path):
     for k in ("use_ewald", "nfft", "ewald_cutoff", "bsorder"):
         assert s.settings[k] == ref.settings[k], k
     assert s.settings["poleps"] == 1e-5  # the key's polar-eps
+    assert s.settings["predictor"] == 1  # polar-predict without a modifier: ASPC
     assert s.settings["aewald"] == pytest.approx(ref.settings["aewald"], rel=1e-12)
     for k in ("vtype", "radmin", "epsilon", "red", "parent", "scaled_ik", "scaled_v"):
         assert np.allclose(np.asarray(getattr(s.vdw, k)), np.asarray(getattr(ref.vdw, k))), k
@@ -149,3 +151,14 @@ def test_system_from_tinker_files(tmp_path):
     assert s.valence.bond_cubic == ref.valence.bond_cubic and s.valence.angle_terms == ref.valence.angle_terms
     P = tio.read_prm(os.path.join(tmp_path, "nist.prm"))
     assert np.allclose(tio.masses(s.types, P), mass)
+
+
+def test_predictor_keyword():
+    """POLAR-PREDICT as the reference maps its modifier (src/amoeba/epolar.cpp:426-444):
+    ASPC 1, GEAR 2, absent 0; no modifier ASPC; LSQR has no GPU path."""
+    assert tio.predictor_from_keys({}) == 0
+    assert tio.predictor_from_keys({"polar-predict": []}) == 1
+    assert tio.predictor_from_keys({"polar-predict": ["aspc"]}) == 1
+    assert tio.predictor_from_keys({"polar-predict": ["GEAR"]}) == 2
+    with pytest.raises(ValueError):
+        tio.predictor_from_keys({"polar-predict": ["LSQR"]})

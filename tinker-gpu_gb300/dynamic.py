@@ -33,11 +33,14 @@ def maxwell_velocities(mass, kelvin, seed=1):
 
 
 def run(xyz, key=None, prm=None, nsteps=1000, dt_fs=1.0, save_every=0, kelvin=None, tau_ps=0.1, seed=1,
-        dyn_in=None, arc=None, dyn_out=None, uind_out=None, predictor=1, stream=None):
+        dyn_in=None, arc=None, dyn_out=None, uind_out=None, predictor=None, extrapolation=0, stream=None):
     """Integrate nsteps velocity-Verlet steps of dt_fs: Bussi thermostat at
-    kelvin with coupling tau_ps when kelvin is given, else NVE.  Returns the
-    steps done, the final kinetic energy (kcal/mol), temperature (K),
-    positions (A) and velocities (A/ps)."""
+    kelvin with coupling tau_ps when kelvin is given, else NVE.  predictor:
+    0 none, 1 ASPC, 2 Gear; None takes the keyword file's POLAR-PREDICT
+    (tinkerio.predictor_from_keys).  extrapolation: frames of the learned
+    extrapolation of the ASPC ring (t9gb_learn_extrapolation, 2-8), 0 off.
+    Returns the steps done, the final kinetic energy (kcal/mol), temperature
+    (K), positions (A) and velocities (A/ps)."""
     abi = importlib.import_module(__package__ + ".abi")
     key, prm = tio.resolve_files(xyz, key, prm)
     s = tio.system_from_tinker(xyz, key, prm)
@@ -48,8 +51,12 @@ def run(xyz, key=None, prm=None, nsteps=1000, dt_fs=1.0, save_every=0, kelvin=No
         x0, v0, _, _, _ = tio.read_dyn(dyn_in)
     elif kelvin is not None:
         v0 = maxwell_velocities(mass, kelvin, seed)
+    if predictor is None:
+        predictor = s.settings.get("predictor", 0)
     eng = abi.Engine(s, predictor=predictor, stream=stream)
     eng.prepare(x0)
+    if extrapolation:
+        eng.learn_extrapolation(extrapolation)
     eng.md_init(x0, mass, v0)
     dt = dt_fs * 1e-3
     thermo = 1 if kelvin is not None else 0

@@ -325,6 +325,25 @@ def resolve_files(xyz_path, key_path=None, prm_path=None):
     return key_path, prm_path
 
 
+def predictor_from_keys(keys):
+    """The induced-dipole predictor a keyword file selects, as the reference
+    maps it (src/amoeba/epolar.cpp:426-444): POLAR-PREDICT ASPC -> 1, GEAR ->
+    2; no POLAR-PREDICT -> 0 (none).  POLAR-PREDICT without a modifier (as in
+    the reference's test/file/water30/water30.key) -> 1: the Fortran keyword
+    reader that fills the reference's default modifier is not part of the
+    reference, and ASPC is the predictor its CUDA path and its tests use.
+    LSQR, which the reference's CUDA path lacks, raises ValueError."""
+    if "polar-predict" not in keys:
+        return 0
+    v = keys["polar-predict"]
+    mod = v[0].upper() if v else "ASPC"
+    if mod == "ASPC":
+        return 1
+    if mod == "GEAR":
+        return 2
+    raise ValueError(f"polar-predict {mod}: only ASPC and GEAR have a GPU path")
+
+
 def system_from_tinker(xyz_path, key_path=None, prm_path=None, frame=0, vdw=True, valence=True):
     """A System from a Tinker coordinate file, its keyword file (default: the
     .key beside the .xyz) and the parameter file the key names (or prm_path).
@@ -332,7 +351,8 @@ def system_from_tinker(xyz_path, key_path=None, prm_path=None, frame=0, vdw=True
     pme-grid, pme-order, polar-eps, polar-iter, usolve-cutoff, usolve-diag,
     pcg-peek, pcg-guess, pcg-precond, neighbor-list buffer (list-buffer),
     a-axis / b-axis / c-axis (else the file's box line), vdw-cutoff,
-    vdw-taper; Tinker's defaults otherwise."""
+    vdw-taper, polar-predict (settings["predictor"], predictor_from_keys);
+    Tinker's defaults otherwise."""
     fr = read_xyz(xyz_path)[frame]
     key_path, prm_path = resolve_files(xyz_path, key_path, prm_path)
     keys = read_key(key_path) if key_path else {}
@@ -378,6 +398,7 @@ def system_from_tinker(xyz_path, key_path=None, prm_path=None, frame=0, vdw=True
     if "pcg-noprecond" in keys:
         st["pcgprec"] = 0
     st["list_buffer"] = _fkey(keys, "list-buffer", st["list_buffer"])
+    st["predictor"] = predictor_from_keys(keys)
     s.settings = st
     if vdw and P.vdw:
         vrec = {}
