@@ -40,3 +40,23 @@ def test_dynamic_from_tinker_files(gpu_lib, tmp_path):
         assert np.abs(du).max() < m["reference_eps"]
     x, v, _, _, b = tio.read_dyn(os.path.join(d, "out.dyn"))
     assert np.allclose(x, out["xyz"], rtol=1e-15) and np.allclose(v, out["vel"], rtol=1e-15)
+
+
+def test_dynamic_learned_extrapolation(gpu_lib, tmp_path):
+    """The same run continued for 40 steps with the learned extrapolation of
+    the ASPC ring (dynamic.run(extrapolation=8)): the trajectory stays on the
+    plain ASPC one (the solves meet the same 1e-6 D tolerance)."""
+    dyn = importlib.import_module("tinker-gpu_gb300.dynamic")
+    tio = importlib.import_module("tinker-gpu_gb300.tinkerio")
+    d = str(tmp_path)
+    _tinkernist_files(d)
+    fx = T.load()
+    m = fx["meta"]
+    tio.write_dyn(os.path.join(d, "nist.dyn"), "AMOEBA Water Box", fx["dyn_x"], fx["dyn_v"], box=tuple(m["box"]))
+    kw = dict(nsteps=40, dt_fs=1000 * m["dt_ps"], dyn_in=os.path.join(d, "nist.dyn"))
+    a = dyn.run(os.path.join(d, "nist.xyz"), **kw)
+    b = dyn.run(os.path.join(d, "nist.xyz"), extrapolation=8, **kw)
+    assert a["steps"] == b["steps"] == 40
+    dx = np.abs(a["xyz"] - b["xyz"]).max()
+    print(f"40 steps: positions differ by {dx:.2e} A")
+    assert dx < 3e-5  # measured 3e-6 A: dipoles within the tolerance from different starts
