@@ -13,6 +13,11 @@ value: induce() calls per second over all ranks, inputs resident in HBM
        frames of the MD leg's trajectory of the relaxed box).
 e2e:   the same through t9gb_induce_host: host coordinates in, host dipoles
        out, both copies inside the timed region.
+*_learned_extrapolation: the librating, MD-frame, 98,304-atom and MD legs
+       again with the ASPC ring's coefficients fitted online after every solve
+       (t9gb_learn_extrapolation, LX_ORDER frames) instead of ASPC's own.
+learned_guess: the per-atom network's starts on MD frames against the plain
+       ones (alpha E and ASPC).
 The working set (~10 MB) is smaller than L2, so L2 is flushed (a 512 MB
 write) between timed steps, outside the per-step CUDA-event brackets.
 
