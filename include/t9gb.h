@@ -485,14 +485,16 @@ int t9gb_learn_adamw(t9gb_context* ctx);
  * solve 1.045 (path 0) -> 0.860 ms (plain 0.789 ms). */
 int t9gb_learn_tensor_path(t9gb_context* ctx, int path);
 
-/* Learned extrapolation of the predictor ring (ASPC contexts only): after
+/* Learned extrapolation of the predictor ring (ASPC or Gear contexts): after
  * every solve, a least-squares fit of the converged dipoles on the `order`
- * most recent ring frames (2 .. 8; their backward differences as the basis,
- * FP64 normal equations over every element of both dipole sets, forgetting
- * factor 0.99, solved on the device) gives the ring coefficients of the next
- * solve's start, in place of ASPC's (from the second fit on).  The PCG
- * convergence test is unchanged.  0 (the default) keeps ASPC.  A new order
- * starts a new fit.  T9GB_BAD_ARG for other orders or without ASPC. */
+ * most recent ring frames (2 .. 8 with ASPC's ring of 16, 2 .. 5 with Gear's
+ * ring of 6; their backward differences as the basis, normal equations over
+ * every element of both dipole sets kept in FP64 with forgetting factor 0.99,
+ * solved on the device) gives the ring coefficients of the next solve's
+ * start, in place of the predictor's (from the second fit on).  The PCG
+ * convergence test is unchanged.  0 (the default) keeps the predictor's own
+ * coefficients.  A new order starts a new fit.  T9GB_BAD_ARG for other
+ * orders or without a predictor. */
 int t9gb_learn_extrapolation(t9gb_context* ctx, int order);
 /* State of the learned extrapolation after the last solve: the fits so far
  * (*fits), those whose solve failed and left the previous coefficients in

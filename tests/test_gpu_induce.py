@@ -356,3 +356,39 @@ def test_learned_extrapolation(gpu_lib, oracle, tg):
     d = engine_for(s, predictor=0)
     with pytest.raises(abi.T9Error):
         d.learn_extrapolation(7)
+
+
+def test_learned_extrapolation_gear(gpu_lib, oracle, tg):
+    """The learned extrapolation over Gear's ring of 6 frames (order 5): no
+    more iterations than Gear's own start, the oracle's dipoles, coefficients
+    as the FP64 restatement fits them; order 6 does not fit in the ring."""
+    from oracle import learn_oracle as LO
+
+    s = tg.systems.make_config("water648")
+    tr = tg.systems.Trajectory(s)
+    a = engine_for(s, predictor=2)
+    b = engine_for(s, predictor=2)
+    b.learn_extrapolation(5)
+    ia, ib, hist = [], [], []
+    for step in range(40):
+        x = tr.frame(step)
+        a.induce_host(x)
+        ub, pb, rc = b.induce_host(x)
+        assert rc == 0
+        hist.append(np.concatenate([ub, pb]))
+        if step >= 16:
+            ia.append(a.stats()[0])
+            ib.append(b.stats()[0])
+    print("iterations Gear", np.mean(ia), "learned extrapolation", np.mean(ib))
+    assert np.mean(ib) <= np.mean(ia)
+    ou, op, *_ = oracle.OracleSystem(s, xyz=tr.frame(39)).induce()
+    D = tg.units.DEBYE
+    assert rms_err(ub * D, ou * D) < DIPOLE_RMS_DEBYE and rms_err(pb * D, op * D) < DIPOLE_RMS_DEBYE
+    fits, rej, cb = b.learn_extrapolation_state()
+    ref, nfit = LO.lx_ring_coefficients(hist, 5)
+    err = float(np.abs(cb - ref).max())
+    print("ring coefficients", cb[:5], "FP64 restatement", ref[:5], "max error", err)
+    assert (fits, rej) == (nfit, 0) == (35, 0)
+    assert err < 1e-3 * max(1.0, float(np.abs(ref).max()))
+    with pytest.raises(gpu_lib.T9Error):
+        b.learn_extrapolation(6)

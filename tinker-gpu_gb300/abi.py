@@ -527,7 +527,8 @@ class Engine:
         self._check(self.lib.t9gb_learn_tensor_path(self.h, int(path)))
 
     def learn_extrapolation(self, order=8):
-        """Learned extrapolation of the ASPC ring over `order` frames (2-8); 0 restores ASPC."""
+        """Learned extrapolation of the predictor ring over `order` frames (2-8 with ASPC,
+        2-5 with Gear); 0 restores the predictor's own coefficients."""
         self._check(self.lib.t9gb_learn_extrapolation(self.h, int(order)))
 
     def learn_extrapolation_state(self):

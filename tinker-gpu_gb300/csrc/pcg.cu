@@ -386,22 +386,22 @@ __device__ bool lx_solve(const float (*Ms)[K + 1], const float* sc, float ridge,
 // atoms, against 10.7 us now.
 template <int K>
 __global__ void __launch_bounds__(256) k_lx_train(VecArgs A, const float* __restrict__ hist, float* __restrict__ part,
-   double* __restrict__ lx, float* __restrict__ lcoef, int* __restrict__ state, int* __restrict__ ticket)
+   double* __restrict__ lx, float* __restrict__ lcoef, int* __restrict__ state, int* __restrict__ ticket, int depth)
 {
    constexpr int NV = K * (K + 1) / 2 + K;
    __shared__ float sh[8][NV];
-   const int nualt = state[ST_NUALT] - 1;  // after the solve's bump: the new frame is slot nualt % 16
+   const int nualt = state[ST_NUALT] - 1;  // after the solve's bump: the new frame is slot nualt % depth
    if (nualt < K)
       return;  // every block alike
    float acc[NV];
 #pragma unroll
    for (int v = 0; v < NV; ++v)
       acc[v] = 0.f;
-   const float* fy = hist + (size_t)(nualt % 16) * A.ne8;
+   const float* fy = hist + (size_t)(nualt % depth) * A.ne8;
    const float* fr[K];
 #pragma unroll
    for (int j = 0; j < K; ++j)
-      fr[j] = hist + (size_t)(((nualt - 1 - j) % 16 + 16) % 16) * A.ne8;
+      fr[j] = hist + (size_t)(((nualt - 1 - j) % depth + depth) % depth) * A.ne8;
    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.ne; e += gridDim.x * blockDim.x) {
       const int s = e / 6, x = e + 2 * s;
       float t[K];
@@ -1197,7 +1197,8 @@ int induce_sorted(Context* ctx)
 // host-driven loop it runs in order.  Not after a failed solve.
 static int lx_train_launch(Context* ctx, bool side)
 {
-   if (ctx->lx_k <= 0 || pred_depth(ctx->cfg) != 16)
+   const int depth = pred_depth(ctx->cfg);
+   if (ctx->lx_k <= 0 || ctx->lx_k >= depth)
       return T9GB_OK;
    const VecArgs A = vec_args(ctx);
    auto k = ctx->lx_k == 2 ? k_lx_train<2> : ctx->lx_k == 3 ? k_lx_train<3> : ctx->lx_k == 4 ? k_lx_train<4>
@@ -1209,7 +1210,7 @@ static int lx_train_launch(Context* ctx, bool side)
       st = ctx->lx_stream;
    }
    k<<<LX_NB, 256, 0, st>>>(A, ctx->aspc_hist, ctx->lx_part, ctx->lx_ab, ctx->lx_coef_buf, ctx->status,
-      ctx->lx_ticket);
+      ctx->lx_ticket, depth);
    T9_CUDA(cudaGetLastError());
    if (side) {
       T9_CUDA(cudaEventRecord(ctx->ev_lx_done, ctx->lx_stream));
@@ -1229,10 +1230,11 @@ int lx_wait(Context* ctx)
 }
 
 // t9gb_learn_extrapolation: order 0 (the predictor's own coefficients) or
-// 2 .. 8 ring frames; a new order starts a new fit
+// 2 .. 8 ring frames (ASPC's ring of 16) / 2 .. 5 (Gear's ring of 6); a new
+// order starts a new fit
 int lx_config(Context* ctx, int order)
 {
-   if (order != 0 && (order < 2 || order > LX_MAXK || ctx->cfg.predictor != 1))
+   if (order != 0 && (order < 2 || order > LX_MAXK || order >= pred_depth(ctx->cfg)))
       return T9GB_BAD_ARG;
    T9_CHECK(lx_wait(ctx));
    if (order > 0 && !ctx->lx_ab) {
