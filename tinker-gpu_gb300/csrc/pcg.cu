@@ -311,8 +311,9 @@ __constant__ float c_sbinom[LX_MAXK][LX_MAXK] = {
    {1, -6, 15, -20, 15, -6, 1, 0},
    {1, -7, 21, -35, 35, -21, 7, -1}};
 
-// a + b = s + e exactly (Knuth's two-sum, no FMA contraction of sums);
-// returns e, s into *out (which may alias a)
+// a + b = s + e exactly (Knuth's two-sum; the intrinsics keep the compiler
+// from fusing or reordering the sums): returns e and writes s to out, which
+// may alias a
 __device__ __forceinline__ float two_sum(float a, float b, float& out)
 {
    const float s = __fadd_rn(a, b);
