@@ -38,7 +38,8 @@ def run(xyz, key=None, prm=None, nsteps=1000, dt_fs=1.0, save_every=0, kelvin=No
     kelvin with coupling tau_ps when kelvin is given, else NVE.  predictor:
     0 none, 1 ASPC, 2 Gear; None takes the keyword file's POLAR-PREDICT
     (tinkerio.predictor_from_keys).  extrapolation: frames of the learned
-    extrapolation of the ASPC ring (t9gb_learn_extrapolation, 2-8), 0 off.
+    extrapolation of the predictor ring (t9gb_learn_extrapolation, 2-8 with
+    ASPC, 2-5 with Gear), 0 off.
     Returns the steps done, the final kinetic energy (kcal/mol), temperature
     (K), positions (A) and velocities (A/ps)."""
     abi = importlib.import_module(__package__ + ".abi")
