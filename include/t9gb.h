@@ -493,7 +493,7 @@ int t9gb_learn_tensor_path(t9gb_context* ctx, int path);
  * solved on the device) gives the ring coefficients of the next solve's
  * start, in place of the predictor's (from the second fit on).  The PCG
  * convergence test is unchanged.  0 (the default) keeps the predictor's own
- * coefficients.  A new order starts a new fit.  T9GB_BAD_ARG for other
+ * coefficients.  Every call starts a new fit.  T9GB_BAD_ARG for other
  * orders or without a predictor. */
 int t9gb_learn_extrapolation(t9gb_context* ctx, int order);
 /* State of the learned extrapolation after the last solve: the fits so far

@@ -265,3 +265,32 @@ def test_tensor_core_learned_solve(gpu_lib, oracle, tg):
     ou, op, *_ = oracle.OracleSystem(s).induce()
     D = tg.units.DEBYE
     assert rms_err(ud * D, ou * D) < DIPOLE_RMS_DEBYE and rms_err(up * D, op * D) < DIPOLE_RMS_DEBYE
+
+
+def test_network_beside_learned_extrapolation(gpu_lib, oracle, tg):
+    """Both learned starts on one ASPC context: the network trains and is
+    compared with the plain start, which is now the learned extrapolation of
+    the ring; the graph and the host-driven loop agree bit for bit, every
+    solve converges, the dipoles meet the oracle and no fit is rejected."""
+    s = tg.systems.make_config("water648")
+    traj = tg.systems.Trajectory(s)
+    out = []
+    for graph in (True, False):
+        e = engine_for(s, predictor=1)
+        e.use_graph(graph)
+        e.learn_extrapolation(8)
+        e.learn_reset(seed=3)
+        rec = []
+        _run(e, traj, range(20), 1, rec)
+        _run(e, traj, range(20, 30), 3, rec)
+        assert all(r[2] == 0 and r[1] < 1e-6 for r in rec)
+        ud, up, _ = e.induce_host(traj.frame(30))
+        fits, rej, coef = e.learn_extrapolation_state()
+        assert fits == 23 and rej == 0
+        out.append((ud, up, coef, e.learn_weights()))
+    for a, b in zip(out[0], out[1]):
+        assert np.array_equal(a, b)
+    ou, op, *_ = oracle.OracleSystem(s, traj.frame(30)).induce()
+    D = tg.units.DEBYE
+    assert rms_err(out[0][0] * D, ou * D) < DIPOLE_RMS_DEBYE
+    assert rms_err(out[0][1] * D, op * D) < DIPOLE_RMS_DEBYE

@@ -1231,8 +1231,8 @@ int lx_wait(Context* ctx)
 }
 
 // t9gb_learn_extrapolation: order 0 (the predictor's own coefficients) or
-// 2 .. 8 ring frames (ASPC's ring of 16) / 2 .. 5 (Gear's ring of 6); a new
-// order starts a new fit
+// 2 .. 8 ring frames (ASPC's ring of 16) / 2 .. 5 (Gear's ring of 6); every
+// call starts a new fit
 int lx_config(Context* ctx, int order)
 {
    if (order != 0 && (order < 2 || order > LX_MAXK || order >= pred_depth(ctx->cfg)))
